@@ -1,0 +1,282 @@
+"""Generate the golden fixtures under tests/golden/ from the reference.
+
+Run in the build container only (it reads the read-only reference tree and
+runs the reference's own code; the GPU machine has neither):
+
+    python tests/golden/make_golden.py
+
+Sources of each fixture:
+
+* ``tabulate_se_a_op.npz`` — the inline arrays of the reference op test
+  source/tests/pt/test_tabulate_fusion_se_a.py (read as data with ``ast``).
+* ``deeppot_sea_case.npz`` / ``deeppot_sea_model.npz`` — the three blocks of
+  source/tests/infer/deeppot-testcase.yaml and the weights of the TorchScript
+  model source/tests/infer/deeppot_sea.pth (state dict, loaded on CPU).
+* ``env_mat_a.npz``, ``fmt_nlist.npz``, ``prod_force_a.npz``,
+  ``prod_virial_a.npz`` — the inline golden arrays of source/lib/tests/*.cc
+  together with the inputs those tests derive (ghost copy and candidate list),
+  reproduced by calling the reference's own CPU library (oracle/_ref).
+* ``water192.npz`` — the reference PyTorch model (deepmd.pt, eager FP64 on
+  CPU) on the 64-molecule water box with the seeded water-model weights:
+  energy, forces, virial, atomic energy/virial, the typed neighbour list, the
+  environment matrix and the descriptor of the first atoms.
+* ``water192_compressed.npz`` — the same model after the reference's
+  ``enable_compression`` (coarse strides so the fixture stays small): the
+  tables, table_info and the compressed energy/forces/virial.
+"""
+from __future__ import annotations
+
+import ast
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("DPGB_REFERENCE", "/root/reference")
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, os.path.join(REPO, "deepmd-kit_gb300"))
+
+
+def _read(rel):
+    with open(os.path.join(REF, rel)) as f:
+        return f.read()
+
+
+def cpp_vector(text, name):
+    m = re.search(r"std::vector<\w+>\s+" + name + r"\s*=\s*\{([^}]*)\}", text)
+    if m is None:
+        raise KeyError(name)
+    body = re.sub(r"//[^\n]*", "", m.group(1))
+    return np.array([float(x) for x in body.replace("\n", " ").split(",") if x.strip()])
+
+
+def py_test_arrays(rel):
+    tree = ast.parse(_read(rel))
+    out = {}
+    for node in ast.walk(tree):
+        if not (isinstance(node, ast.Assign) and isinstance(node.targets[0], ast.Attribute)):
+            continue
+        name, v = node.targets[0].attr, node.value
+        shape = None
+        if isinstance(v, ast.Call) and isinstance(v.func, ast.Attribute) and v.func.attr == "reshape":
+            shape = tuple(ast.literal_eval(a) for a in v.args)
+            v = v.func.value
+        if isinstance(v, ast.Call) and isinstance(v.func, ast.Attribute) and v.func.attr == "tensor":
+            arr = np.array(ast.literal_eval(v.args[0]), dtype=np.float64)
+            out[name] = arr.reshape(shape) if shape else arr
+        elif isinstance(v, ast.Constant) and name not in out:
+            out[name] = v.value
+    return out
+
+
+def make_tabulate():
+    a = py_test_arrays("source/tests/pt/test_tabulate_fusion_se_a.py")
+    np.savez_compressed(os.path.join(HERE, "tabulate_se_a_op.npz"),
+                        table=a["table_tensor"], table_info=a["table_info_tensor"],
+                        em_x=a["em_x_tensor"], em=a["em_tensor"],
+                        last_layer_size=a["last_layer_size"],
+                        descriptor=a["expected_descriptor_tensor"],
+                        dy_dem_x=a["expected_dy_dem_x"], dy_dem=a["expected_dy_dem"])
+
+
+def _yaml_blocks(text):
+    """The three result blocks of deeppot-testcase.yaml (a fixed layout)."""
+    blocks = []
+    for chunk in text.split("\n  - coord:")[1:]:
+        chunk = "coord:" + chunk
+        rec = {}
+        for key in ("coord", "atype", "box", "atomic_energy", "force", "atomic_virial"):
+            m = re.search(r"(?m)^\s*" + key + r":\s*(null|\[[^\]]*\])", chunk)
+            if m is None:
+                raise KeyError(key)
+            rec[key] = None if m.group(1) == "null" else np.array(
+                [float(x) for x in m.group(1).strip("[]").replace("\n", " ").split(",") if x.strip()])
+        blocks.append(rec)
+    return blocks
+
+
+def make_deeppot_case():
+    import torch
+
+    blocks = _yaml_blocks(_read("source/tests/infer/deeppot-testcase.yaml"))
+    out = {}
+    for i, b in enumerate(blocks):
+        for k, v in b.items():
+            out[f"b{i}_{k}"] = np.zeros(0) if v is None else v
+    np.savez_compressed(os.path.join(HERE, "deeppot_sea_case.npz"), nblock=len(blocks), **out)
+    m = torch.jit.load(os.path.join(REF, "source/tests/infer/deeppot_sea.pth"), map_location="cpu")
+    sd = {k: v.numpy() for k, v in m.state_dict().items() if "._networks." not in k}
+    np.savez_compressed(os.path.join(HERE, "deeppot_sea_model.npz"), **sd)
+
+
+def _lib_test_setup(posi, atype, box, rc, rc_smth, sel):
+    import oracle as O
+
+    ext, ext_t, mapping, rows, counts = O.ref_copy_coord_build_nlist(posi, atype, box, rc, legacy=True)
+    nloc = len(atype)
+    nnei = int(sum(sel))
+    avg = np.zeros((len(sel), nnei, 4))
+    std = np.ones((len(sel), nnei, 4))
+    em, der, rij, nl = O.prod_env_mat_a_ref(ext, ext_t, rows, counts, avg, std, nloc, rc, rc_smth, sel)
+    return dict(coord_ext=ext, atype_ext=ext_t, mapping=mapping, rows=rows, counts=counts,
+                em=em, em_deriv=der, rij=rij, nlist=nl)
+
+
+def make_lib_tests():
+    posi = None
+    t_env = _read("source/lib/tests/test_env_mat_a.cc")
+    posi = cpp_vector(t_env, "posi")
+    atype = cpp_vector(t_env, "atype").astype(np.int32)
+    box = np.array([13., 0, 0, 0, 13., 0, 0, 0, 13.])
+    s = _lib_test_setup(posi, atype, box, 6.0, 0.8, [10, 10])
+    np.savez_compressed(os.path.join(HERE, "env_mat_a.npz"), posi=posi, atype=atype, box=box,
+                        rc=6.0, rc_smth=0.8, sel=np.array([10, 10]),
+                        expected_env=cpp_vector(t_env, "expected_env"), **s)
+
+    t_fmt = _read("source/lib/tests/test_fmt_nlist.cc")
+    s = _lib_test_setup(posi, atype, box, 6.0, 0.8, [10, 10])
+    np.savez_compressed(os.path.join(HERE, "fmt_nlist.npz"), posi=posi, atype=atype, box=box,
+                        rc=6.0, sel=np.array([10, 10]),
+                        expect_nlist_cpy=cpp_vector(t_fmt, "expect_nlist_cpy").astype(np.int32), **s)
+
+    for name, fname in (("prod_force_a", "test_prod_force_a.cc"), ("prod_virial_a", "test_prod_virial_a.cc")):
+        txt = _read("source/lib/tests/" + fname)
+        s = _lib_test_setup(posi, atype, box, 6.0, 0.8, [5, 5])
+        nloc, nnei = s["nlist"].shape
+        net_deriv = 10 - np.arange(nloc * nnei * 4) * 0.01
+        extra = {}
+        if name == "prod_force_a":
+            extra["expected_force"] = cpp_vector(txt, "expected_force")
+        else:
+            extra["expected_virial"] = cpp_vector(txt, "expected_virial")
+            extra["expected_atom_virial"] = cpp_vector(txt, "expected_atom_virial")
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), posi=posi, atype=atype, box=box,
+                            rc=6.0, rc_smth=0.8, sel=np.array([5, 5]), net_deriv=net_deriv,
+                            **extra, **s)
+
+
+def _reference_model(params, compress=None):
+    import torch
+    import refshim
+
+    refshim.install()
+    from deepmd.pt.model.model import get_model
+
+    c = params.config
+    cfg = {"type_map": [str(i) for i in range(c.ntypes)],
+           "descriptor": {"type": "se_e2_a", "sel": list(c.sel), "rcut_smth": c.rcut_smth,
+                          "rcut": c.rcut, "neuron": list(c.neuron), "axis_neuron": c.axis_neuron,
+                          "type_one_side": c.type_one_side, "resnet_dt": c.resnet_dt,
+                          "precision": "float64", "seed": 1},
+           "fitting_net": {"neuron": list(c.fit_neuron), "resnet_dt": c.fit_resnet_dt,
+                           "precision": "float64", "seed": 1}}
+    model = get_model(cfg)
+    sd = model.state_dict()
+    for k, v in params.to_state_dict().items():
+        assert k in sd, k
+        sd[k] = torch.as_tensor(v, dtype=sd[k].dtype).reshape(sd[k].shape)
+    for k in list(sd):
+        if "._networks." in k:
+            sd[k] = sd[k.replace("._networks.", ".networks.")]
+    model.load_state_dict(sd)
+    if compress is not None:
+        model.atomic_model.enable_compression(*compress)
+    return model
+
+
+def _run_reference(model, coord, atype, box):
+    import torch
+    from deepmd.pt.utils.nlist import extend_input_and_build_neighbor_list
+
+    c = torch.as_tensor(coord.reshape(1, -1), dtype=torch.float64)
+    t = torch.as_tensor(atype.reshape(1, -1), dtype=torch.int64)
+    b = torch.as_tensor(box.reshape(1, 9), dtype=torch.float64)
+    ret = model.forward(c, t, b, do_atomic_virial=True)
+    ext, ext_t, mapping, nlist = extend_input_and_build_neighbor_list(
+        c, t, model.get_rcut(), model.get_sel(), mixed_types=True, box=b)
+    nlist = model.format_nlist(ext, ext_t, nlist)
+    return ret, ext, ext_t, mapping, nlist
+
+
+def _shift_order(box, rcut):
+    """The image order the reference's (unstable) CPU argsort produced."""
+    import torch
+    from deepmd.pt.utils.region import to_face_distance
+
+    cell = torch.as_tensor(box.reshape(1, 3, 3))
+    nbuff = torch.ceil(rcut / to_face_distance(cell)).to(torch.int64).amax(0)
+    xi = [torch.arange(-n, n + 1, dtype=torch.int64) for n in nbuff.tolist()]
+    eye = torch.eye(3, dtype=torch.float64)
+    xyz = (xi[0].view(-1, 1, 1, 1) * eye[0] + xi[1].view(1, -1, 1, 1) * eye[1]
+           + xi[2].view(1, 1, -1, 1) * eye[2]).view(-1, 3)
+    return torch.argsort(torch.linalg.norm(xyz, dim=-1)).numpy()
+
+
+def make_water():
+    import torch
+    from dpgb import params as P, synth
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    cfg = P.water_config()
+    params = P.init_params(cfg, seed=1)
+    coord, atype, box = synth.water_box(4, seed=0)
+    model = _reference_model(params)
+    ret, ext, ext_t, mapping, nlist = _run_reference(model, coord, atype, box)
+    from deepmd.pt.model.descriptor.env_mat import prod_env_mat
+
+    desc = model.atomic_model.descriptor
+    em, diff, sw = prod_env_mat(ext, nlist, ext_t[:, :192], desc.sea.mean, desc.sea.stddev,
+                                cfg.rcut, cfg.rcut_smth)
+    d, rot, _, _, _ = desc(ext, ext_t, nlist)
+    nkeep = 8
+    np.savez_compressed(
+        os.path.join(HERE, "water192.npz"), coord=coord, atype=atype, box=box,
+        params_seed=1, coord_seed=0,
+        energy=ret["energy"].detach().numpy().reshape(-1),
+        force=ret["force"].detach().numpy().reshape(-1, 3),
+        virial=ret["virial"].detach().numpy().reshape(-1),
+        atom_energy=ret["atom_energy"].detach().numpy().reshape(-1),
+        atom_virial=ret["atom_virial"].detach().numpy().reshape(-1, 9),
+        nlist=nlist.numpy().reshape(192, -1).astype(np.int32),
+        mapping=mapping.numpy().reshape(-1).astype(np.int32),
+        coord_ext=ext.detach().numpy().reshape(-1, 3),
+        shift_order=_shift_order(box, cfg.rcut),
+        env_mat=em.detach().numpy().reshape(192, -1, 4)[:nkeep],
+        sw=sw.detach().numpy().reshape(192, -1)[:nkeep],
+        descriptor=d.detach().numpy().reshape(192, -1)[:nkeep],
+        rot_mat=rot.detach().numpy().reshape(192, cfg.ng, 3)[:nkeep])
+    return params, coord, atype, box
+
+
+def make_water_compressed(params, coord, atype, box):
+    # coarse strides keep the four tables small (the production strides are
+    # 0.01 / 0.1; the algorithm is the same)
+    min_nbor_dist, extrap, s1, s2 = 0.8, 5, 0.1, 1.0
+    model = _reference_model(params, compress=(min_nbor_dist, extrap, s1, s2, -1))
+    ret, *_ = _run_reference(model, coord, atype, box)
+    sea = model.atomic_model.descriptor.sea
+    tabs = {f"table_{e}": t.detach().numpy() for e, t in enumerate(sea.compress_data)}
+    infos = {f"info_{e}": t.detach().numpy() for e, t in enumerate(sea.compress_info)}
+    np.savez_compressed(
+        os.path.join(HERE, "water192_compressed.npz"), min_nbor_dist=min_nbor_dist,
+        extrapolate=extrap, stride0=s1, stride1=s2,
+        energy=ret["energy"].detach().numpy().reshape(-1),
+        force=ret["force"].detach().numpy().reshape(-1, 3),
+        virial=ret["virial"].detach().numpy().reshape(-1), **tabs, **infos)
+
+
+if __name__ == "__main__":
+    import oracle as O
+
+    O.build_ref()
+    make_tabulate()
+    make_deeppot_case()
+    make_lib_tests()
+    p, c, t, b = make_water()
+    make_water_compressed(p, c, t, b)
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
