@@ -1,0 +1,346 @@
+"""Benchmark: atom-steps/s of se_e2_a energy + force + virial on one GB300.
+
+Workload: 4096 water molecules (12,288 atoms, periodic cubic box 49.6 A),
+seeded synthetic coordinates (O lattice 3.1 A jittered U(+-0.3 A), H at
+0.9572 A / 104.52 deg, random rotations) and the seeded random-init water
+model (rcut 6, rcut_smth 0.5, sel [46, 92], embedding [25, 50, 100],
+axis 16, fitting [240, 240, 240]).  One step = one full evaluation from
+coordinates: wrap, cell-list neighbour list, descriptor, fitting, forces,
+virial.  `value` is the mixed-precision form with coordinates resident in
+HBM; `e2e` is the same step through the DP_DeepPotCompute-style C API with
+host buffers (host->device coordinates, device->host energy/forces/virial
+inside the timed region).  The plain FP64 form is measured on the same
+workload and reported in `config` together with the mixed-vs-FP64 errors.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl dpgb|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "deepmd-kit_gb300"))
+
+METRIC = "atom-steps/s se_e2_a E+F+virial, mixed vs FP64 on 1 GB300 at F-RMSE<=1e-3 eV/A"
+UNIT = "atom-steps/s"
+NMOL_SIDE = 16  # 16^3 molecules = 12,288 atoms
+
+
+def _peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p, "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _allreduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def algorithmic_flops(n_atoms: int, n_pairs: int, cfg) -> dict:
+    """FLOPs of one E+F+V step per stage (the survey's per-atom-step counts):
+    embedding 2*(25+25*50+50*100) per pair, G^T R~ 2*4*100 per pair, D
+    2*100*4*16 per atom, fitting 2*(1600*240+2*240*240+240) per atom; the
+    force pass repeats the input-gradient of each GEMM, the descriptor
+    backward also recomputes the embedding."""
+    w = [1] + list(cfg.neuron)
+    emb = 2 * sum(w[i] * w[i + 1] for i in range(len(w) - 1))
+    gr = 2 * 4 * cfg.ng
+    dmat = 2 * cfg.ng * 4 * cfg.axis_neuron
+    fw = [cfg.dim_descrpt] + list(cfg.fit_neuron) + [1]
+    fit = 2 * sum(fw[i] * fw[i + 1] for i in range(len(fw) - 1))
+    return {
+        "desc_fwd": n_pairs * (emb + gr) + n_atoms * dmat,
+        "fitting": 2 * n_atoms * fit,
+        "desc_bwd": n_pairs * (2 * emb + 2 * gr) + n_atoms * 2 * dmat,
+        "total_useful": n_pairs * 2 * (emb + gr) + n_atoms * (2 * dmat + 2 * fit),
+    }
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU path as restated by the oracle (the reference's own
+    compiled library is x86-only here and its Python model is not on the GPU
+    box), timed on the host cores on a bounded sample of the workload: the
+    full neighbourhoods of the first `sample` centre atoms of the 12,288-atom
+    box per step."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    from dpgb import params as P, synth
+
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    params = P.init_params(P.water_config(), seed=1)
+    coord, atype, box = synth.water_box(NMOL_SIDE, seed=0)
+    om = O.OracleModel(params)
+    cn = O.normalize_coord(coord, box)
+    ext, ext_t, _ = O.extend_coord_with_ghosts(cn, atype, box, params.config.rcut)
+    nloc = coord.shape[0]
+    nl = O.build_nlist_pt(ext, ext_t, nloc, params.config.rcut, params.config.sel)
+    sample = args.ref_sample
+    for _ in range(args.warmup):
+        om.energy_force_ext(ext, ext_t, nl[:sample], sample)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        om.energy_force_ext(ext, ext_t, nl[:sample], sample)
+    dt = time.perf_counter() - t0
+    value = sample * args.steps / dt
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": "water 4096 H2O (12,288 atoms), se_e2_a plain FP64, CPU", "natoms": nloc,
+                   "sample_atoms_per_step": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.lib().orc_num_threads(), "kind": "port",
+                         "sample": f"{sample} centre atoms (full neighbourhoods) of the 12,288-atom box per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def cpu_baseline_port(sample: int, steps: int = 2):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    from dpgb import params as P, synth
+
+    params = P.init_params(P.water_config(), seed=1)
+    coord, atype, box = synth.water_box(NMOL_SIDE, seed=0)
+    om = O.OracleModel(params)
+    cn = O.normalize_coord(coord, box)
+    ext, ext_t, _ = O.extend_coord_with_ghosts(cn, atype, box, params.config.rcut)
+    nl = O.build_nlist_pt(ext, ext_t, coord.shape[0], params.config.rcut, params.config.sel)
+    om.energy_force_ext(ext, ext_t, nl[:sample], sample)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        om.energy_force_ext(ext, ext_t, nl[:sample], sample)
+    dt = time.perf_counter() - t0
+    return {"value": sample * steps / dt, "unit": UNIT, "cores": O.lib().orc_num_threads(), "kind": "port",
+            "sample": f"{steps} x {sample} centre atoms (full neighbourhoods) of the 12,288-atom box, FP64 oracle"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="dpgb", choices=["dpgb", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--ref-sample", type=int, default=768)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = _dist()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from dpgb import nlist as N, params as P, synth
+    from dpgb.deeppot import DeepPot
+
+    params = P.init_params(P.water_config(), seed=1)
+    cfg = params.config
+    coord, atype, box = synth.water_box(NMOL_SIDE, seed=rank)
+    nloc = coord.shape[0]
+    dev = torch.device("cuda", local)
+    coord_dev = torch.tensor(coord.reshape(1, -1), dtype=torch.float64, device=dev)
+    boxh = box.reshape(1, 9)
+
+    # neighbour statistics of the workload (outside the timed region)
+    nl = N.build_neighbor_list_local(N.normalize_coord(coord_dev.reshape(-1, 3), box),
+                                     torch.tensor(atype, device=dev, dtype=torch.int32), box, cfg.rcut, cfg.sel)
+    n_pairs = int((nl >= 0).sum().item())
+    flops = algorithmic_flops(nloc, n_pairs, cfg)
+
+    mixed = DeepPot(params, "mixed", device=local)
+    out = mixed.eval_device(coord_dev, boxh, atype)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        mixed.eval_device(coord_dev, boxh, atype, out=out)
+    torch.cuda.synchronize()
+    mixed.set_profiling(True)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    _barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.fill_(float(k))  # evict L2 between timed steps (untimed)
+            starts[k].record(stream)
+            mixed.eval_device(coord_dev, boxh, atype, out=out)
+            ends[k].record(stream)
+            mixed.collect_stages()
+        torch.cuda.synchronize()
+    _barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_ms = _allreduce_max(sum(step_ms), world)
+    launches = mixed.last_launches()
+    stages, ncalls = mixed.stage_times()
+    value = world * nloc * args.steps / (t_ms * 1e-3)
+
+    # end to end through the C API with host buffers
+    mixed.set_profiling(False)
+    for _ in range(2):
+        mixed.eval(coord.reshape(1, -1), boxh, atype)
+    _barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e_h, f_h, v_h = mixed.eval(coord.reshape(1, -1), boxh, atype)
+    e2e_s = _allreduce_max(time.perf_counter() - t0, world)
+    e2e = {"value": world * nloc * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(coord.nbytes), "d2h_bytes_per_step": int(8 + f_h.nbytes + v_h.nbytes)}
+
+    # the plain FP64 form on the same workload, and the mixed-vs-FP64 error
+    fp64 = DeepPot(params, "fp64", device=local)
+    o64 = fp64.eval_device(coord_dev, boxh, atype)
+    torch.cuda.synchronize()
+    s64, e64 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s64.record(stream)
+    for _ in range(args.fp64_steps):
+        fp64.eval_device(coord_dev, boxh, atype, out=o64)
+    e64.record(stream)
+    torch.cuda.synchronize()
+    fp64_ms = s64.elapsed_time(e64) / args.fp64_steps
+    fp64_value = nloc / (fp64_ms * 1e-3)
+    f_m, f_d = out["force"].double().cpu().numpy(), o64["force"].cpu().numpy()
+    f_rmse = float(np.sqrt(np.mean((f_m - f_d) ** 2)))
+    f_rms = float(np.sqrt(np.mean(f_d ** 2)))
+    e_err = float(abs(out["energy"].item() - o64["energy"].item()) / nloc)
+    v_err = float(np.abs(out["virial"].cpu().numpy() - o64["virial"].cpu().numpy()).max())
+
+    if rank != 0:
+        return
+    peaks, peak_kind = _peaks()
+    dom = max((k for k in stages if k in flops), key=lambda k: stages[k])
+    dom_ms = stages[dom] / max(ncalls, 1)
+    achieved = flops[dom] / (dom_ms * 1e-3) / 1e12
+    peak = peaks.get("bf16_tflops", 1900.0)
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline_port(sample=args.ref_sample // 2)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {
+            "workload": "water 4096 H2O (12,288 atoms), box 49.6 A, se_e2_a rc 6 sel [46,92] emb [25,50,100] "
+                        "axis 16 fit [240,240,240]; mixed form; full step incl. neighbour list",
+            "natoms": nloc, "real_pairs": n_pairs, "l2": "flushed between timed steps (256 MB write, untimed)",
+            "fp64_atom_steps_per_s": fp64_value, "fp64_ms_per_step": fp64_ms,
+            "mixed_over_fp64": value / world / fp64_value,
+            "force_rmse_vs_fp64_eV_per_A": f_rmse, "force_rms_fp64": f_rms,
+            "energy_err_per_atom_vs_fp64": e_err, "virial_max_abs_err_vs_fp64": v_err,
+            "stage_ms_per_step": {k: v / max(ncalls, 1) for k, v in stages.items()},
+            "parallelism": f"replicas x{world}",
+        },
+        "roofline": {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": f"{peak_kind} bf16_tflops", "algorithmic_flops_per_launch": flops[dom]},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

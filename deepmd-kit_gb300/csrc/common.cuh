@@ -1,0 +1,93 @@
+// Shared helpers of the dpgb CUDA library: error plumbing, launch checks and
+// small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+
+#include "dpgb.h"
+
+namespace dpgb {
+
+// Thread-local last-error text behind dpgb_last_error().
+void set_error(const std::string& msg);
+void clear_error();
+
+inline int fail(int code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+
+inline int check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    return fail(DPGB_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+  return DPGB_OK;
+}
+
+// After a launch: configuration errors surface here (asynchronous faults are
+// reported by the next synchronising call).
+inline int check_launch(const char* what) {
+  return check_cuda(cudaGetLastError(), what);
+}
+
+#define DPGB_TRY(x)                 \
+  do {                              \
+    int _rc = (x);                  \
+    if (_rc != DPGB_OK) return _rc; \
+  } while (0)
+
+#define DPGB_CUDA(x) DPGB_TRY(::dpgb::check_cuda((x), #x))
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Device-side status word layout (one int per code, atomicMax'ed).
+enum StatusSlot { kStatusOverflow = 0, kStatusOverflowAtom = 1, kStatusTimeout = 2, kStatusSlots = 4 };
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Scoped device allocation used by op-level entry points (workspace).
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DeviceBuffer() = default;
+  DeviceBuffer(const DeviceBuffer&) = delete;
+  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+  ~DeviceBuffer() {
+    if (ptr) cudaFree(ptr);
+  }
+  int alloc(size_t n) {
+    if (n <= bytes) return DPGB_OK;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    if (n == 0) return DPGB_OK;
+    cudaError_t e = cudaMalloc(&ptr, n);
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      return fail(DPGB_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    bytes = n;
+    return DPGB_OK;
+  }
+  template <typename T>
+  T* as() const {
+    return reinterpret_cast<T*>(ptr);
+  }
+};
+
+}  // namespace dpgb

@@ -1,0 +1,714 @@
+// DeepPot: the se_e2_a energy / force / virial evaluation behind the C API
+// (source/api_c/include/c_api.h:150,244-322, source/api_cc/src/DeepPotPT.cc:
+// 170-378 semantics: wrap, ghost images, typed neighbour list, descriptor,
+// fitting, dE/dr, ghost-to-local force reduction, virial).
+//
+// Pipeline per call (all on one stream, no host synchronisation in the
+// device form):
+//   normalise -> cell-list neighbour list (per frame) -> sorted transpose of
+//   the list -> desc_fwd -> fitting fwd+bwd per type -> desc_bwd ->
+//   force / atomic-virial gather -> per-frame FP64 energy and virial sums.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "se_a.cuh"
+
+namespace dpgb {
+namespace {
+
+template <typename T>
+struct DevModel {
+  EmbParams<T> emb{};
+  FitParams<T> fit{};
+  T* davg = nullptr;
+  T* dstd = nullptr;
+  TabMeta<T>* meta = nullptr;
+  std::vector<DeviceBuffer*> owned;
+  ~DevModel() {
+    for (auto* b : owned) delete b;
+  }
+  template <typename S>
+  T* upload(const std::vector<S>& h) {
+    std::vector<T> c(h.begin(), h.end());
+    auto* b = new DeviceBuffer();
+    owned.push_back(b);
+    if (b->alloc(sizeof(T) * std::max<size_t>(c.size(), 1)) != DPGB_OK) return nullptr;
+    if (!c.empty() && cudaMemcpy(b->ptr, c.data(), sizeof(T) * c.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+      return nullptr;
+    return b->as<T>();
+  }
+};
+
+// ---- pipeline kernels --------------------------------------------------------
+__global__ void model_keys_kernel(int* __restrict__ keys, const int* __restrict__ nlist, long long npair,
+                                  int nnei, int nloc) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npair) return;
+  const int nb = nlist[p];
+  const long long row = p / nnei;
+  const int f = (int)(row / nloc);
+  keys[p] = nb < 0 ? -1 : f * nloc + nb % nloc;
+}
+
+// F[row] = sum_slots g[row] - sum_{pairs -> row} g;  optional atomic virial on
+// the neighbour: -sum_{pairs -> row} g (x) d
+template <typename T>
+__global__ void force_gather_model_kernel(double* __restrict__ force, double* __restrict__ atom_vir,
+                                          const T* __restrict__ g, Transpose tr, const int* __restrict__ nlist,
+                                          const double* __restrict__ coord, const double* __restrict__ svec,
+                                          int nshift, int nloc, int nnei, int nrows) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= nrows) return;
+  double f[3] = {0, 0, 0};
+  const T* gr = g + (size_t)row * nnei * 3;
+  for (int s = 0; s < nnei; ++s) {
+    f[0] += (double)gr[3 * s];
+    f[1] += (double)gr[3 * s + 1];
+    f[2] += (double)gr[3 * s + 2];
+  }
+  double av[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) av[k] = 0.0;
+  for (int t = tr.offsets[row]; t < tr.offsets[row + 1]; ++t) {
+    const int p = tr.pairs[t];
+    const double g0 = (double)g[3 * (size_t)p], g1 = (double)g[3 * (size_t)p + 1], g2 = (double)g[3 * (size_t)p + 2];
+    f[0] -= g0;
+    f[1] -= g1;
+    f[2] -= g2;
+    if (atom_vir) {
+      const int prow = p / nnei;
+      const int fr = prow / nloc, i = prow - fr * nloc;
+      const int nb = nlist[p];
+      const int s = nb / nloc, jj = nb - s * nloc;
+      const double* cf = coord + (size_t)fr * nloc * 3;
+      const double* sv = svec + ((size_t)fr * nshift + s) * 3;
+      const double d[3] = {(cf[3 * jj] + sv[0]) - cf[3 * i], (cf[3 * jj + 1] + sv[1]) - cf[3 * i + 1],
+                           (cf[3 * jj + 2] + sv[2]) - cf[3 * i + 2]};
+      const double gg[3] = {g0, g1, g2};
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int l = 0; l < 3; ++l) av[3 * k + l] -= gg[k] * d[l];
+    }
+  }
+  force[3 * (size_t)row] = f[0];
+  force[3 * (size_t)row + 1] = f[1];
+  force[3 * (size_t)row + 2] = f[2];
+  if (atom_vir)
+#pragma unroll
+    for (int k = 0; k < 9; ++k) atom_vir[9 * (size_t)row + k] = av[k];
+}
+
+// atom energy in the original order (+ per-type bias), 0 for virtual atoms
+__global__ void atom_energy_kernel(double* __restrict__ e_row, const double* __restrict__ e_sorted,
+                                   const int* __restrict__ row_pos, const int* __restrict__ atype,
+                                   const double* __restrict__ bias, int nloc, int nrows) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= nrows) return;
+  const int t = atype[row % nloc];
+  e_row[row] = t < 0 ? 0.0 : e_sorted[row_pos[row]] + bias[t];
+}
+
+// per-frame sums: blockIdx.x = frame, blockIdx.y = 0 energy, 1..9 virial
+__global__ void frame_sum_kernel(double* __restrict__ energy, double* __restrict__ virial,
+                                 const double* __restrict__ e_row, const double* __restrict__ vir_row,
+                                 int nloc) {
+  __shared__ double s[256];
+  const int f = blockIdx.x, q = blockIdx.y;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nloc; i += blockDim.x) {
+    const size_t row = (size_t)f * nloc + i;
+    acc += q == 0 ? e_row[row] : vir_row[row * 9 + (q - 1)];
+  }
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (q == 0)
+      energy[f] = s[0];
+    else
+      virial[(size_t)f * 9 + q - 1] = s[0];
+  }
+}
+
+}  // namespace
+
+struct DeepPotImpl {
+  dpgb_se_a_desc desc;
+  int precision = DPGB_PREC_FP64;
+  SelInfo sel{};
+  int ng = 0, dim = 0, nnets = 0, pad_zero = 1;
+  std::unique_ptr<DevModel<double>> m64;
+  std::unique_ptr<DevModel<float>> m32;
+  DeviceBuffer bias_dev, pair_mask_dev;
+  // host-side caches
+  std::vector<int> atype_cache;
+  std::vector<int> row_pos_h, type_count, type_off;
+  int cached_nframes = -1;
+  DeviceBuffer row_pos_dev, atype_dev;
+  // workspace
+  DeviceBuffer ws_nlist, ws_cell, ws_tr, ws_keys, ws_status, ws_coord, ws_svec, ws_spos;
+  DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf;
+  DeviceBuffer io_coord, io_force, io_av, io_e, io_v, io_ae;
+  std::string err;
+  int launches = 0;
+  cudaStream_t stream = nullptr;
+  // stage timing (events recorded on the compute stream when enabled)
+  int profiling = 0;
+  cudaEvent_t ev[2 * DPGB_NUM_STAGES] = {};
+  int ev_recorded = 0;
+  double stage_ms[DPGB_NUM_STAGES] = {};
+  int stage_calls = 0;
+  void mark(int stage, int end, cudaStream_t st) {
+    if (!profiling) return;
+    cudaEventRecord(ev[2 * stage + end], st);
+    ev_recorded = 1;
+  }
+};
+
+namespace {
+
+int validate_desc(const dpgb_se_a_desc* d) {
+  if (!d) return fail(DPGB_EINVAL, "NULL model description");
+  if (d->ntypes <= 0 || d->ntypes > DPGB_MAX_TYPES) return fail(DPGB_EINVAL, "ntypes out of range");
+  if (d->n_emb <= 0 || d->n_emb > kMaxEmbLayers) return fail(DPGB_EINVAL, "1..4 embedding layers are supported");
+  for (int l = 0; l < d->n_emb; ++l)
+    if (d->emb_neuron[l] <= 0 || d->emb_neuron[l] > 128)
+      return fail(DPGB_EINVAL, "embedding widths must be in 1..128");
+  if (d->n_fit <= 0 || d->n_fit > kMaxFitLayers) return fail(DPGB_EINVAL, "1..5 hidden fitting layers are supported");
+  const int ng = d->emb_neuron[d->n_emb - 1];
+  if (d->axis_neuron <= 0 || d->axis_neuron > ng) return fail(DPGB_EINVAL, "bad axis_neuron");
+  if (d->dim_descrpt != ng * d->axis_neuron) return fail(DPGB_EINVAL, "dim_descrpt != ng * axis_neuron");
+  if (!(d->rcut_smth < d->rcut)) return fail(DPGB_EINVAL, "rmin should be less than rmax.");
+  if (!d->davg || !d->dstd || !d->atom_ener_bias) return fail(DPGB_EINVAL, "missing davg/dstd/bias");
+  int nnei = 0;
+  for (int t = 0; t < d->ntypes; ++t) nnei += d->sel[t];
+  if (nnei <= 0 || nnei > 1024) return fail(DPGB_EINVAL, "sum(sel) must be in 1..1024");
+  return DPGB_OK;
+}
+
+template <typename T>
+int build_dev_model(DeepPotImpl& dp, DevModel<T>& m) {
+  const dpgb_se_a_desc& d = dp.desc;
+  const int nt = d.ntypes, nnei = dp.sel.nnei;
+  const int nnets = dp.nnets;
+  // embedding: W[l] [nnets, nin, nout]
+  int nin = 1;
+  m.emb.n_layer = d.n_emb;
+  for (int l = 0; l < d.n_emb; ++l) {
+    const int nout = d.emb_neuron[l];
+    m.emb.width[l] = nout;
+    std::vector<double> W((size_t)nnets * nin * nout), b((size_t)nnets * nout), idt;
+    bool has_idt = false;
+    for (int e = 0; e < nnets; ++e) has_idt |= d.emb_idt[e][l] != nullptr;
+    if (has_idt) idt.assign((size_t)nnets * nout, 1.0);
+    for (int e = 0; e < nnets; ++e) {
+      if (!d.compressed && (!d.emb_w[e][l] || !d.emb_b[e][l])) return fail(DPGB_EINVAL, "missing embedding weights");
+      if (d.emb_w[e][l]) std::copy(d.emb_w[e][l], d.emb_w[e][l] + (size_t)nin * nout, W.begin() + (size_t)e * nin * nout);
+      if (d.emb_b[e][l]) std::copy(d.emb_b[e][l], d.emb_b[e][l] + nout, b.begin() + (size_t)e * nout);
+      if (d.emb_idt[e][l]) std::copy(d.emb_idt[e][l], d.emb_idt[e][l] + nout, idt.begin() + (size_t)e * nout);
+    }
+    m.emb.W[l] = m.upload(W);
+    m.emb.b[l] = m.upload(b);
+    m.emb.idt[l] = has_idt ? m.upload(idt) : nullptr;
+    if (!m.emb.W[l] || !m.emb.b[l]) return fail(DPGB_ENOMEM, "weight upload failed");
+    nin = nout;
+  }
+  // compressed tables
+  m.emb.compressed = d.compressed;
+  if (d.compressed) {
+    std::vector<double> tab;
+    std::vector<TabMeta<T>> meta(nnets);
+    for (int e = 0; e < nnets; ++e) {
+      const double* info = d.table_info[e];
+      if (!d.table[e] || !(info[3] > 0) || !(info[4] > 0)) return fail(DPGB_EINVAL, "missing compression table");
+      TabMeta<T> tm;
+      tm.lower = (T)info[0];
+      tm.upper = (T)info[1];
+      tm.mx = (T)info[2];
+      tm.s0 = (T)info[3];
+      tm.s1 = (T)info[4];
+      tm.first = (int)((tm.upper - tm.lower) / tm.s0);
+      const T bxx = std::nextafter(tm.mx, tm.lower);
+      tm.hi_idx = tm.first + (int)((bxx - tm.upper) / tm.s1);
+      tm.hi_xx = tm.mx - ((tm.hi_idx - tm.first) * tm.s1 + tm.upper);
+      tm.offset = (long long)tab.size();
+      const long long nspline = (long long)tm.hi_idx + 1;
+      tab.insert(tab.end(), d.table[e], d.table[e] + nspline * 6 * dp.ng);
+      meta[e] = tm;
+    }
+    m.emb.table = m.upload(tab);
+    auto* b = new DeviceBuffer();
+    m.owned.push_back(b);
+    DPGB_TRY(b->alloc(sizeof(TabMeta<T>) * nnets));
+    DPGB_CUDA(cudaMemcpy(b->ptr, meta.data(), sizeof(TabMeta<T>) * nnets, cudaMemcpyHostToDevice));
+    m.emb.meta = b->as<TabMeta<T>>();
+  }
+  // fitting: W[l] [nt, nin, nout]
+  m.fit.n_hidden = d.n_fit;
+  m.fit.width[0] = d.dim_descrpt;
+  for (int l = 0; l < d.n_fit; ++l) m.fit.width[l + 1] = d.fit_neuron[l];
+  for (int l = 0; l < d.n_fit; ++l) {
+    const int a = m.fit.width[l], o = m.fit.width[l + 1];
+    std::vector<double> W((size_t)nt * a * o), b((size_t)nt * o), idt;
+    bool has_idt = false;
+    for (int t = 0; t < nt; ++t) has_idt |= d.fit_idt[t][l] != nullptr;
+    if (has_idt) idt.assign((size_t)nt * o, 1.0);
+    for (int t = 0; t < nt; ++t) {
+      if (!d.fit_w[t][l] || !d.fit_b[t][l]) return fail(DPGB_EINVAL, "missing fitting weights");
+      std::copy(d.fit_w[t][l], d.fit_w[t][l] + (size_t)a * o, W.begin() + (size_t)t * a * o);
+      std::copy(d.fit_b[t][l], d.fit_b[t][l] + o, b.begin() + (size_t)t * o);
+      if (d.fit_idt[t][l]) std::copy(d.fit_idt[t][l], d.fit_idt[t][l] + o, idt.begin() + (size_t)t * o);
+    }
+    m.fit.W[l] = m.upload(W);
+    m.fit.b[l] = m.upload(b);
+    m.fit.idt[l] = has_idt ? m.upload(idt) : nullptr;
+  }
+  {
+    const int wl = m.fit.width[d.n_fit];
+    std::vector<double> w((size_t)nt * wl), b(nt, 0.0);
+    for (int t = 0; t < nt; ++t) {
+      if (!d.fit_w[t][d.n_fit]) return fail(DPGB_EINVAL, "missing output layer");
+      std::copy(d.fit_w[t][d.n_fit], d.fit_w[t][d.n_fit] + wl, w.begin() + (size_t)t * wl);
+      if (d.fit_b[t][d.n_fit]) b[t] = d.fit_b[t][d.n_fit][0];
+    }
+    m.fit.w_out = m.upload(w);
+    m.fit.b_out = m.upload(b);
+  }
+  std::vector<double> avg(d.davg, d.davg + (size_t)nt * nnei * 4), sd(d.dstd, d.dstd + (size_t)nt * nnei * 4);
+  m.davg = m.upload(avg);
+  m.dstd = m.upload(sd);
+  return DPGB_OK;
+}
+
+// stable sort of the integer image shifts by norm (ties keep enumeration order)
+std::vector<int> default_shifts(const int nbuff[3]) {
+  std::vector<int> xyz;
+  for (int x = -nbuff[0]; x <= nbuff[0]; ++x)
+    for (int y = -nbuff[1]; y <= nbuff[1]; ++y)
+      for (int z = -nbuff[2]; z <= nbuff[2]; ++z) {
+        xyz.push_back(x);
+        xyz.push_back(y);
+        xyz.push_back(z);
+      }
+  const int n = (int)xyz.size() / 3;
+  std::vector<int> idx(n);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+    const double na = std::sqrt((double)(xyz[3 * a] * xyz[3 * a] + xyz[3 * a + 1] * xyz[3 * a + 1] + xyz[3 * a + 2] * xyz[3 * a + 2]));
+    const double nb = std::sqrt((double)(xyz[3 * b] * xyz[3 * b] + xyz[3 * b + 1] * xyz[3 * b + 1] + xyz[3 * b + 2] * xyz[3 * b + 2]));
+    return na < nb;
+  });
+  std::vector<int> out;
+  for (int i : idx) {
+    out.push_back(xyz[3 * i]);
+    out.push_back(xyz[3 * i + 1]);
+    out.push_back(xyz[3 * i + 2]);
+  }
+  return out;
+}
+
+int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host, cudaStream_t st) {
+  const bool same = dp.cached_nframes == nframes && (int)dp.atype_cache.size() == natom &&
+                    std::equal(dp.atype_cache.begin(), dp.atype_cache.end(), atype_host);
+  if (same) return DPGB_OK;
+  const int nt = dp.desc.ntypes;
+  for (int i = 0; i < natom; ++i)
+    if (atype_host[i] >= nt) return fail(DPGB_EINVAL, "atom type out of range");
+  dp.atype_cache.assign(atype_host, atype_host + natom);
+  dp.type_count.assign(nt, 0);
+  for (int i = 0; i < natom; ++i)
+    if (atype_host[i] >= 0) dp.type_count[atype_host[i]] += nframes;
+  dp.type_off.assign(nt + 1, 0);
+  for (int t = 0; t < nt; ++t) dp.type_off[t + 1] = dp.type_off[t] + dp.type_count[t];
+  // sorted position of every (frame, atom): by type, then frame, then atom
+  dp.row_pos_h.assign((size_t)nframes * natom, 0);
+  std::vector<int> cur(dp.type_off.begin(), dp.type_off.end() - 1);
+  for (int t = 0; t < nt; ++t)
+    for (int f = 0; f < nframes; ++f)
+      for (int i = 0; i < natom; ++i)
+        if (atype_host[i] == t) dp.row_pos_h[(size_t)f * natom + i] = cur[t]++;
+  const int nvirt = natom * nframes - dp.type_off[nt];
+  (void)nvirt;
+  DPGB_TRY(dp.row_pos_dev.alloc(sizeof(int) * dp.row_pos_h.size()));
+  DPGB_TRY(dp.atype_dev.alloc(sizeof(int) * natom));
+  DPGB_CUDA(cudaMemcpyAsync(dp.row_pos_dev.ptr, dp.row_pos_h.data(), sizeof(int) * dp.row_pos_h.size(),
+                            cudaMemcpyHostToDevice, st));
+  DPGB_CUDA(cudaMemcpyAsync(dp.atype_dev.ptr, atype_host, sizeof(int) * natom, cudaMemcpyHostToDevice, st));
+  DPGB_CUDA(cudaStreamSynchronize(st));  // host vectors may change on the next call
+  dp.cached_nframes = nframes;
+  return DPGB_OK;
+}
+
+template <typename T>
+int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* coord_dev, const double* box_host,
+        double* energy, double* force, double* virial, double* atom_energy, double* atom_virial, cudaStream_t st) {
+  const dpgb_se_a_desc& d = dp.desc;
+  const int nnei = dp.sel.nnei;
+  const long long nrows = (long long)nframes * natom;
+  if (nrows >= (1LL << 31) / std::max(nnei, 1)) return fail(DPGB_EINVAL, "too many atoms for 32-bit pair ids");
+  int launches = 0;
+  // --- geometry (host) ---
+  std::vector<CellGeom> geo(nframes);
+  std::vector<std::vector<int>> spos(nframes);
+  int nshift_max = 1;
+  std::vector<std::vector<double>> svecs(nframes);
+  std::vector<double> host_coord;
+  for (int f = 0; f < nframes; ++f) {
+    if (box_host) {
+      CellGeom g0;
+      DPGB_TRY(box_geom(box_host + 9 * f, g0));
+      // reference image range from the face distances
+      CellGeom tmp;
+      std::vector<int> dummy;
+      double face_rc = d.rcut;
+      // nbuff = ceil(rcut / face distance)
+      const double* c = box_host + 9 * f;
+      auto crn = [&](int p, int q) {
+        const double x = c[p * 3 + 1] * c[q * 3 + 2] - c[p * 3 + 2] * c[q * 3 + 1];
+        const double y = c[p * 3 + 2] * c[q * 3 + 0] - c[p * 3 + 0] * c[q * 3 + 2];
+        const double z = c[p * 3 + 0] * c[q * 3 + 1] - c[p * 3 + 1] * c[q * 3 + 0];
+        return std::sqrt(x * x + y * y + z * z);
+      };
+      const double vol = std::fabs(c[0] * (c[4] * c[8] - c[5] * c[7]) - c[1] * (c[3] * c[8] - c[5] * c[6]) +
+                                   c[2] * (c[3] * c[7] - c[4] * c[6]));
+      const int nb[3] = {(int)std::ceil(face_rc / (vol / crn(1, 2))), (int)std::ceil(face_rc / (vol / crn(2, 0))),
+                         (int)std::ceil(face_rc / (vol / crn(0, 1)))};
+      const std::vector<int> shifts = default_shifts(nb);
+      const int ns = (int)shifts.size() / 3;
+      DPGB_TRY(periodic_geom(box_host + 9 * f, d.rcut, ns, shifts.data(), geo[f], spos[f]));
+      shift_vectors(geo[f], shifts.data(), ns, svecs[f]);
+      nshift_max = std::max(nshift_max, ns);
+      (void)tmp;
+      (void)dummy;
+    } else {
+      if (host_coord.empty()) {
+        host_coord.resize((size_t)nframes * natom * 3);
+        DPGB_CUDA(cudaMemcpyAsync(host_coord.data(), coord_dev, sizeof(double) * host_coord.size(),
+                                  cudaMemcpyDeviceToHost, st));
+        DPGB_CUDA(cudaStreamSynchronize(st));
+      }
+      DPGB_TRY(open_geom(host_coord.data() + (size_t)f * natom * 3, natom, d.rcut, geo[f]));
+      spos[f].assign(1, 0);
+      svecs[f].assign(3, 0.0);
+    }
+  }
+  // --- device workspace ---
+  size_t cell_bytes = 0;
+  for (int f = 0; f < nframes; ++f) cell_bytes = std::max(cell_bytes, nlist_pt_workspace(natom, geo[f]));
+  const long long npair = nrows * nnei;
+  const int ng = dp.ng, dim = dp.dim;
+  int maxw = 0;
+  for (int l = 1; l <= m.fit.n_hidden; ++l) maxw = std::max(maxw, m.fit.width[l]);
+  DPGB_TRY(dp.ws_cell.alloc(cell_bytes));
+  DPGB_TRY(dp.ws_nlist.alloc(sizeof(int) * npair));
+  DPGB_TRY(dp.ws_keys.alloc(sizeof(int) * npair));
+  DPGB_TRY(dp.ws_tr.alloc(transpose_workspace(npair, (int)nrows)));
+  DPGB_TRY(dp.ws_status.alloc(sizeof(int) * kStatusSlots));
+  DPGB_TRY(dp.ws_coord.alloc(sizeof(double) * nrows * 3));
+  DPGB_TRY(dp.ws_svec.alloc(sizeof(double) * 3 * (size_t)nshift_max * nframes));
+  size_t spos_n = 0;
+  for (auto& v : spos) spos_n = std::max(spos_n, v.size());
+  DPGB_TRY(dp.ws_spos.alloc(sizeof(int) * spos_n * nframes));
+  DPGB_TRY(dp.ws_D.alloc(sizeof(T) * nrows * dim));
+  DPGB_TRY(dp.ws_dD.alloc(sizeof(T) * nrows * dim));
+  DPGB_TRY(dp.ws_xyz.alloc(sizeof(T) * nrows * 4 * ng));
+  DPGB_TRY(dp.ws_g.alloc(sizeof(T) * npair * 3));
+  DPGB_TRY(dp.ws_vir.alloc(sizeof(double) * nrows * 9));
+  DPGB_TRY(dp.ws_erow.alloc(sizeof(double) * nrows));
+  DPGB_TRY(dp.ws_esorted.alloc(sizeof(double) * nrows));
+  DPGB_TRY(dp.ws_act.alloc(sizeof(T) * 2 * m.fit.n_hidden * nrows * maxw));
+  DPGB_TRY(dp.ws_gbuf.alloc(sizeof(T) * 4 * nrows * maxw));
+
+  int* status = dp.ws_status.as<int>();
+  DPGB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * kStatusSlots, st));
+  // shift tables
+  {
+    std::vector<double> sv((size_t)3 * nshift_max * nframes, 0.0);
+    std::vector<int> sp(spos_n * nframes, -1);
+    for (int f = 0; f < nframes; ++f) {
+      std::copy(svecs[f].begin(), svecs[f].end(), sv.begin() + (size_t)3 * nshift_max * f);
+      std::copy(spos[f].begin(), spos[f].end(), sp.begin() + spos_n * f);
+    }
+    DPGB_CUDA(cudaMemcpyAsync(dp.ws_svec.ptr, sv.data(), sizeof(double) * sv.size(), cudaMemcpyHostToDevice, st));
+    DPGB_CUDA(cudaMemcpyAsync(dp.ws_spos.ptr, sp.data(), sizeof(int) * sp.size(), cudaMemcpyHostToDevice, st));
+  }
+  double* coord_n = dp.ws_coord.as<double>();
+  int* nlist = dp.ws_nlist.as<int>();
+  dp.mark(DPGB_STAGE_NLIST, 0, st);
+  for (int f = 0; f < nframes; ++f) {
+    const double* cin = coord_dev + (size_t)f * natom * 3;
+    double* cout = coord_n + (size_t)f * natom * 3;
+    if (box_host) {
+      DPGB_TRY(launch_normalize(cout, cin, natom, geo[f], st));
+    } else {
+      DPGB_CUDA(cudaMemcpyAsync(cout, cin, sizeof(double) * natom * 3, cudaMemcpyDeviceToDevice, st));
+    }
+    ++launches;
+    DPGB_TRY(launch_nlist_pt(nlist + (size_t)f * natom * nnei, cout, dp.atype_dev.as<int>(), natom, geo[f],
+                             dp.ws_spos.as<int>() + spos_n * f, dp.ws_svec.as<double>() + (size_t)3 * nshift_max * f,
+                             d.rcut, dp.sel, dp.ws_cell.ptr, status, st));
+    launches += 4;
+  }
+  dp.mark(DPGB_STAGE_NLIST, 1, st);
+  // sorted transpose of the list over local rows
+  dp.mark(DPGB_STAGE_TRANSPOSE, 0, st);
+  Transpose tr;
+  if (npair > 0) {
+    model_keys_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(dp.ws_keys.as<int>(), nlist, npair, nnei, natom);
+    DPGB_TRY(check_launch("model_keys"));
+    ++launches;
+  }
+  DPGB_TRY(launch_transpose(tr, dp.ws_keys.as<int>(), npair, (int)nrows, 0, dp.ws_tr.ptr, status, st));
+  launches += 4;
+  dp.mark(DPGB_STAGE_TRANSPOSE, 1, st);
+  // descriptor forward
+  DescParams<T> p{};
+  p.nloc = natom;
+  p.nrows = (int)nrows;
+  p.nnei = nnei;
+  p.ntypes = d.ntypes;
+  for (int t = 0; t <= d.ntypes; ++t) p.sec[t] = dp.sel.sec[t];
+  p.type_one_side = d.type_one_side;
+  p.ng = ng;
+  p.axis = d.axis_neuron;
+  p.pad_zero = dp.pad_zero;
+  p.rcut = d.rcut;
+  p.rcut_smth = d.rcut_smth;
+  p.davg = m.davg;
+  p.dstd = m.dstd;
+  p.pair_mask = d.pair_mask ? dp.pair_mask_dev.as<int>() : nullptr;
+  p.coord = coord_n;
+  p.atype = dp.atype_dev.as<int>();
+  p.nlist = nlist;
+  p.svec = dp.ws_svec.as<double>();
+  p.nshift = nshift_max;
+  p.row_pos = dp.row_pos_dev.as<int>();
+  // virtual rows have no sorted position: point them at row 0 only for
+  // reading (the kernels never write a virtual row)
+  dp.mark(DPGB_STAGE_DESC_FWD, 0, st);
+  DPGB_TRY(launch_desc_fwd<T>(p, m.emb, dp.ws_D.as<T>(), dp.ws_xyz.as<T>(), desc_fwd_smem<T>(p, m.emb), st));
+  ++launches;
+  dp.mark(DPGB_STAGE_DESC_FWD, 1, st);
+  dp.mark(DPGB_STAGE_FITTING, 0, st);
+  for (int t = 0; t < d.ntypes; ++t) {
+    if (dp.type_count[t] == 0) continue;
+    DPGB_TRY(launch_fitting<T>(m.fit, t, dp.type_off[t], dp.type_count[t], (int)nrows, dp.ws_D.as<T>(),
+                               dp.ws_dD.as<T>(), dp.ws_act.as<T>(), dp.ws_gbuf.as<T>(), dp.ws_esorted.as<double>(),
+                               0.0, st));
+    launches += 2 * m.fit.n_hidden + 2;
+  }
+  dp.mark(DPGB_STAGE_FITTING, 1, st);
+  dp.mark(DPGB_STAGE_DESC_BWD, 0, st);
+  DPGB_TRY(launch_desc_bwd<T>(p, m.emb, dp.ws_dD.as<T>(), dp.ws_xyz.as<T>(), dp.ws_g.as<T>(), dp.ws_vir.as<double>(),
+                              desc_bwd_smem<T>(p, m.emb), st));
+  ++launches;
+  dp.mark(DPGB_STAGE_DESC_BWD, 1, st);
+  dp.mark(DPGB_STAGE_REDUCE, 0, st);
+  force_gather_model_kernel<T><<<ceil_div(nrows, 128), 128, 0, st>>>(
+      force, atom_virial, dp.ws_g.as<T>(), tr, nlist, coord_n, dp.ws_svec.as<double>(), nshift_max, natom, nnei,
+      (int)nrows);
+  DPGB_TRY(check_launch("force_gather"));
+  ++launches;
+  double* e_row = atom_energy ? atom_energy : dp.ws_erow.as<double>();
+  atom_energy_kernel<<<ceil_div(nrows, 256), 256, 0, st>>>(e_row, dp.ws_esorted.as<double>(), dp.row_pos_dev.as<int>(),
+                                                           dp.atype_dev.as<int>(), dp.bias_dev.as<double>(), natom,
+                                                           (int)nrows);
+  DPGB_TRY(check_launch("atom_energy"));
+  frame_sum_kernel<<<dim3(nframes, 10), 256, 0, st>>>(energy, virial, e_row, dp.ws_vir.as<double>(), natom);
+  DPGB_TRY(check_launch("frame_sum"));
+  launches += 2;
+  dp.mark(DPGB_STAGE_REDUCE, 1, st);
+  dp.launches = launches;
+  return DPGB_OK;
+}
+
+int check_status(DeepPotImpl& dp, cudaStream_t st) {
+  int h[kStatusSlots];
+  DPGB_TRY(read_status(dp.ws_status.as<int>(), st, h));
+  if (h[kStatusOverflow] > 0)
+    return fail(DPGB_EOVERFLOW, "neighbour capacity exceeded (" + std::to_string(h[kStatusOverflow]) +
+                                    " entries) at atom/row " + std::to_string(h[kStatusOverflowAtom] - 1));
+  return DPGB_OK;
+}
+
+int compute_device_impl(DeepPotImpl& dp, int nframes, int natom, const double* coord, const int* atype_host,
+                        const double* box_host, double* energy, double* force, double* virial, double* atom_energy,
+                        double* atom_virial, cudaStream_t st) {
+  if (nframes <= 0 || natom <= 0) return fail(DPGB_EINVAL, "nframes and natom must be positive");
+  if (!coord || !atype_host || !energy || !force || !virial) return fail(DPGB_EINVAL, "NULL argument");
+  DPGB_TRY(prepare_types(dp, nframes, natom, atype_host, st));
+  if (dp.precision == DPGB_PREC_FP64)
+    return run<double>(dp, *dp.m64, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial, st);
+  return run<float>(dp, *dp.m32, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial, st);
+}
+
+}  // namespace
+}  // namespace dpgb
+
+using namespace dpgb;
+
+struct dpgb_deeppot {
+  DeepPotImpl impl;
+};
+
+extern "C" {
+
+dpgb_deeppot* dpgb_deeppot_new(const dpgb_se_a_desc* desc, int precision) {
+  clear_error();
+  if (validate_desc(desc) != DPGB_OK) return nullptr;
+  if (precision != DPGB_PREC_FP64 && precision != DPGB_PREC_MIXED) {
+    fail(DPGB_EINVAL, "unknown precision");
+    return nullptr;
+  }
+  std::unique_ptr<dpgb_deeppot> dp(new dpgb_deeppot());
+  DeepPotImpl& im = dp->impl;
+  im.desc = *desc;
+  im.precision = precision;
+  if (sel_from_host(desc->sel, desc->ntypes, im.sel) != DPGB_OK) return nullptr;
+  im.ng = desc->emb_neuron[desc->n_emb - 1];
+  im.dim = desc->dim_descrpt;
+  im.nnets = desc->type_one_side ? desc->ntypes : desc->ntypes * desc->ntypes;
+  im.pad_zero = 1;
+  for (size_t q = 0; q < (size_t)desc->ntypes * im.sel.nnei * 4; ++q)
+    if (desc->davg[q] != 0.0) im.pad_zero = 0;
+  std::vector<double> bias(desc->atom_ener_bias, desc->atom_ener_bias + desc->ntypes);
+  if (im.bias_dev.alloc(sizeof(double) * bias.size()) != DPGB_OK) return nullptr;
+  if (cudaMemcpy(im.bias_dev.ptr, bias.data(), sizeof(double) * bias.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+    fail(DPGB_ECUDA, "bias upload failed");
+    return nullptr;
+  }
+  if (desc->pair_mask) {
+    if (im.pair_mask_dev.alloc(sizeof(int) * desc->ntypes * desc->ntypes) != DPGB_OK) return nullptr;
+    cudaMemcpy(im.pair_mask_dev.ptr, desc->pair_mask, sizeof(int) * desc->ntypes * desc->ntypes, cudaMemcpyHostToDevice);
+  }
+  if (precision == DPGB_PREC_FP64) {
+    im.m64.reset(new DevModel<double>());
+    if (build_dev_model<double>(im, *im.m64) != DPGB_OK) return nullptr;
+  } else {
+    im.m32.reset(new DevModel<float>());
+    if (build_dev_model<float>(im, *im.m32) != DPGB_OK) return nullptr;
+  }
+  // the host pointers of the description are not kept
+  for (int e = 0; e < DPGB_MAX_TYPES * DPGB_MAX_TYPES; ++e) {
+    for (int l = 0; l < DPGB_MAX_LAYERS; ++l) im.desc.emb_w[e][l] = im.desc.emb_b[e][l] = im.desc.emb_idt[e][l] = nullptr;
+    im.desc.table[e] = nullptr;
+  }
+  for (int t = 0; t < DPGB_MAX_TYPES; ++t)
+    for (int l = 0; l <= DPGB_MAX_LAYERS; ++l) im.desc.fit_w[t][l] = im.desc.fit_b[t][l] = im.desc.fit_idt[t][l] = nullptr;
+  im.desc.davg = im.desc.dstd = im.desc.atom_ener_bias = nullptr;
+  if (cudaStreamCreateWithFlags(&im.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    fail(DPGB_ECUDA, "stream creation failed");
+    return nullptr;
+  }
+  return dp.release();
+}
+
+void dpgb_deeppot_delete(dpgb_deeppot* dp) {
+  if (!dp) return;
+  if (dp->impl.stream) {
+    cudaStreamSynchronize(dp->impl.stream);
+    cudaStreamDestroy(dp->impl.stream);
+  }
+  for (auto& e : dp->impl.ev)
+    if (e) cudaEventDestroy(e);
+  delete dp;
+}
+
+const char* dpgb_deeppot_check_ok(dpgb_deeppot* dp) { return dp ? dp->impl.err.c_str() : "NULL handle"; }
+
+int dpgb_deeppot_last_launches(dpgb_deeppot* dp) { return dp ? dp->impl.launches : 0; }
+
+int dpgb_deeppot_set_profiling(dpgb_deeppot* dp, int on) {
+  clear_error();
+  if (!dp) return fail(DPGB_EINVAL, "NULL handle");
+  DeepPotImpl& im = dp->impl;
+  if (on && !im.ev[0])
+    for (auto& e : im.ev) DPGB_CUDA(cudaEventCreate(&e));
+  im.profiling = on;
+  for (auto& x : im.stage_ms) x = 0.0;
+  im.stage_calls = 0;
+  im.ev_recorded = 0;
+  return DPGB_OK;
+}
+
+int dpgb_deeppot_collect_stages(dpgb_deeppot* dp) {
+  clear_error();
+  if (!dp) return fail(DPGB_EINVAL, "NULL handle");
+  DeepPotImpl& im = dp->impl;
+  if (!im.profiling || !im.ev_recorded) return DPGB_OK;
+  DPGB_CUDA(cudaEventSynchronize(im.ev[2 * DPGB_NUM_STAGES - 1]));
+  for (int s = 0; s < DPGB_NUM_STAGES; ++s) {
+    float ms = 0.f;
+    DPGB_CUDA(cudaEventElapsedTime(&ms, im.ev[2 * s], im.ev[2 * s + 1]));
+    im.stage_ms[s] += ms;
+  }
+  im.stage_calls += 1;
+  im.ev_recorded = 0;
+  return DPGB_OK;
+}
+
+int dpgb_deeppot_stage_times(dpgb_deeppot* dp, double* ms, int* ncalls) {
+  clear_error();
+  if (!dp || !ms) return fail(DPGB_EINVAL, "NULL argument");
+  for (int s = 0; s < DPGB_NUM_STAGES; ++s) ms[s] = dp->impl.stage_ms[s];
+  if (ncalls) *ncalls = dp->impl.stage_calls;
+  return DPGB_OK;
+}
+
+int dpgb_deeppot_compute_device(dpgb_deeppot* dp, int nframes, int natom, const double* coord, const int* atype_host,
+                                const double* box_host, double* energy, double* force, double* virial,
+                                double* atom_energy, double* atom_virial, void* stream) {
+  clear_error();
+  if (!dp) return fail(DPGB_EINVAL, "NULL handle");
+  int rc = compute_device_impl(dp->impl, nframes, natom, coord, atype_host, box_host, energy, force, virial,
+                               atom_energy, atom_virial, as_stream(stream));
+  dp->impl.err = rc == DPGB_OK ? "" : dpgb_last_error();
+  return rc;
+}
+
+int dpgb_deeppot_compute(dpgb_deeppot* dp, int nframes, int natom, const double* coord, const int* atype,
+                         const double* box, double* energy, double* force, double* virial, double* atom_energy,
+                         double* atom_virial) {
+  clear_error();
+  if (!dp) return fail(DPGB_EINVAL, "NULL handle");
+  DeepPotImpl& im = dp->impl;
+  cudaStream_t st = im.stream;
+  auto body = [&]() -> int {
+    if (nframes <= 0 || natom <= 0 || !coord || !atype || !energy || !force || !virial)
+      return fail(DPGB_EINVAL, "bad arguments");
+    const size_t nrow = (size_t)nframes * natom;
+    DPGB_TRY(im.io_coord.alloc(sizeof(double) * nrow * 3));
+    DPGB_TRY(im.io_force.alloc(sizeof(double) * nrow * 3));
+    DPGB_TRY(im.io_e.alloc(sizeof(double) * nframes));
+    DPGB_TRY(im.io_v.alloc(sizeof(double) * nframes * 9));
+    if (atom_energy) DPGB_TRY(im.io_ae.alloc(sizeof(double) * nrow));
+    if (atom_virial) DPGB_TRY(im.io_av.alloc(sizeof(double) * nrow * 9));
+    DPGB_CUDA(cudaMemcpyAsync(im.io_coord.ptr, coord, sizeof(double) * nrow * 3, cudaMemcpyHostToDevice, st));
+    DPGB_TRY(compute_device_impl(im, nframes, natom, im.io_coord.as<double>(), atype, box, im.io_e.as<double>(),
+                                 im.io_force.as<double>(), im.io_v.as<double>(),
+                                 atom_energy ? im.io_ae.as<double>() : nullptr,
+                                 atom_virial ? im.io_av.as<double>() : nullptr, st));
+    DPGB_CUDA(cudaMemcpyAsync(energy, im.io_e.ptr, sizeof(double) * nframes, cudaMemcpyDeviceToHost, st));
+    DPGB_CUDA(cudaMemcpyAsync(force, im.io_force.ptr, sizeof(double) * nrow * 3, cudaMemcpyDeviceToHost, st));
+    DPGB_CUDA(cudaMemcpyAsync(virial, im.io_v.ptr, sizeof(double) * nframes * 9, cudaMemcpyDeviceToHost, st));
+    if (atom_energy)
+      DPGB_CUDA(cudaMemcpyAsync(atom_energy, im.io_ae.ptr, sizeof(double) * nrow, cudaMemcpyDeviceToHost, st));
+    if (atom_virial)
+      DPGB_CUDA(cudaMemcpyAsync(atom_virial, im.io_av.ptr, sizeof(double) * nrow * 9, cudaMemcpyDeviceToHost, st));
+    return check_status(im, st);  // synchronises
+  };
+  int rc = body();
+  im.err = rc == DPGB_OK ? "" : dpgb_last_error();
+  return rc;
+}
+
+}  // extern "C"

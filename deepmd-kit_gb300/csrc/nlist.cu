@@ -1,0 +1,687 @@
+// Neighbour lists: periodic wrap, ghost layout, the O(N) cell-list build in
+// the reference PyTorch order, and the formatting of a candidate list in the
+// reference C++ order.  Also the sorted transpose of a list used to gather
+// neighbour contributions without atomics.
+#include <cmath>
+#include <vector>
+
+#include "nlist.cuh"
+
+namespace dpgb {
+
+// ---------------------------------------------------------------------------
+// host geometry helpers
+int box_geom(const double* box, CellGeom& g) {
+  if (!box) return fail(DPGB_EINVAL, "box is required");
+  double c[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) c[a][b] = box[a * 3 + b];
+  const double det = c[0][0] * (c[1][1] * c[2][2] - c[1][2] * c[2][1]) -
+                     c[0][1] * (c[1][0] * c[2][2] - c[1][2] * c[2][0]) +
+                     c[0][2] * (c[1][0] * c[2][1] - c[1][1] * c[2][0]);
+  if (!(std::fabs(det) > 0)) return fail(DPGB_EINVAL, "singular box");
+  double r[3][3];
+  r[0][0] = (c[1][1] * c[2][2] - c[1][2] * c[2][1]) / det;
+  r[0][1] = (c[0][2] * c[2][1] - c[0][1] * c[2][2]) / det;
+  r[0][2] = (c[0][1] * c[1][2] - c[0][2] * c[1][1]) / det;
+  r[1][0] = (c[1][2] * c[2][0] - c[1][0] * c[2][2]) / det;
+  r[1][1] = (c[0][0] * c[2][2] - c[0][2] * c[2][0]) / det;
+  r[1][2] = (c[0][2] * c[1][0] - c[0][0] * c[1][2]) / det;
+  r[2][0] = (c[1][0] * c[2][1] - c[1][1] * c[2][0]) / det;
+  r[2][1] = (c[0][1] * c[2][0] - c[0][0] * c[2][1]) / det;
+  r[2][2] = (c[0][0] * c[1][1] - c[0][1] * c[1][0]) / det;
+  // a diagonal cell inverts exactly to 1/L (as LU-based inversion does), so
+  // the wrap of an orthorhombic box is bitwise that of the reference
+  const bool diag = c[0][1] == 0 && c[0][2] == 0 && c[1][0] == 0 && c[1][2] == 0 &&
+                    c[2][0] == 0 && c[2][1] == 0;
+  if (diag)
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) r[a][b] = a == b ? 1.0 / c[a][a] : 0.0;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      g.cell[a * 3 + b] = c[a][b];
+      g.rec[a * 3 + b] = r[a][b];
+    }
+  g.periodic = 1;
+  return DPGB_OK;
+}
+
+static void face_distances(const CellGeom& g, double face[3]) {
+  const double* c = g.cell;
+  auto cr = [&](int p, int q) {
+    const double x = c[p * 3 + 1] * c[q * 3 + 2] - c[p * 3 + 2] * c[q * 3 + 1];
+    const double y = c[p * 3 + 2] * c[q * 3 + 0] - c[p * 3 + 0] * c[q * 3 + 2];
+    const double z = c[p * 3 + 0] * c[q * 3 + 1] - c[p * 3 + 1] * c[q * 3 + 0];
+    return std::sqrt(x * x + y * y + z * z);
+  };
+  const double vol = std::fabs(c[0] * (c[4] * c[8] - c[5] * c[7]) - c[1] * (c[3] * c[8] - c[5] * c[6]) +
+                               c[2] * (c[3] * c[7] - c[4] * c[6]));
+  face[0] = vol / cr(1, 2);
+  face[1] = vol / cr(2, 0);
+  face[2] = vol / cr(0, 1);
+}
+
+int periodic_geom(const double* box, double rcut, int nshift, const int* shift_idx, CellGeom& g,
+                  std::vector<int>& shift_pos) {
+  DPGB_TRY(box_geom(box, g));
+  if (!shift_idx || nshift <= 0) return fail(DPGB_EINVAL, "shift_idx is required with a box");
+  double face[3];
+  face_distances(g, face);
+  const double rc_margin = rcut * (1.0 + 1e-9) + 1e-12;
+  for (int d = 0; d < 3; ++d) {
+    int n = (int)std::floor(face[d] / rc_margin);
+    n = n < 1 ? 1 : (n > 64 ? 64 : n);
+    g.ncell[d] = n;
+    g.reach[d] = (int)std::ceil(rc_margin * n / face[d]);
+    g.nbuff[d] = (int)std::ceil(rcut / face[d]);
+  }
+  const int sx = 2 * g.nbuff[0] + 1, sy = 2 * g.nbuff[1] + 1, sz = 2 * g.nbuff[2] + 1;
+  if (nshift != sx * sy * sz)
+    return fail(DPGB_EINVAL, "shift_idx must enumerate the (2*nbuff+1)^3 periodic images, nbuff = ceil(rcut/face distance)");
+  shift_pos.assign((size_t)sx * sy * sz, -1);
+  g.zero_shift = -1;
+  for (int s = 0; s < nshift; ++s) {
+    const int tx = shift_idx[3 * s], ty = shift_idx[3 * s + 1], tz = shift_idx[3 * s + 2];
+    if (std::abs(tx) > g.nbuff[0] || std::abs(ty) > g.nbuff[1] || std::abs(tz) > g.nbuff[2])
+      return fail(DPGB_EINVAL, "shift_idx entry outside the image range");
+    const int key = ((tx + g.nbuff[0]) * sy + (ty + g.nbuff[1])) * sz + (tz + g.nbuff[2]);
+    if (shift_pos[key] != -1) return fail(DPGB_EINVAL, "duplicate shift in shift_idx");
+    shift_pos[key] = s;
+    if (tx == 0 && ty == 0 && tz == 0) g.zero_shift = s;
+  }
+  g.nshift = nshift;
+  return DPGB_OK;
+}
+
+int open_geom(const double* coord, int n, double rcut, CellGeom& g) {
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      const double x = coord[3 * i + d];
+      if (i == 0 || x < lo[d]) lo[d] = x;
+      if (i == 0 || x > hi[d]) hi[d] = x;
+    }
+  for (int k = 0; k < 9; ++k) {
+    g.cell[k] = 0;
+    g.rec[k] = 0;
+  }
+  const double rc_margin = rcut * (1.0 + 1e-9) + 1e-12;
+  for (int d = 0; d < 3; ++d) {
+    const double ext = hi[d] - lo[d];
+    int nc = (int)std::floor(ext / rc_margin);
+    nc = nc < 1 ? 1 : (nc > 64 ? 64 : nc);
+    g.ncell[d] = nc;
+    g.csize[d] = std::max(ext / nc, rc_margin);
+    g.origin[d] = lo[d];
+    g.reach[d] = 1;
+    g.nbuff[d] = 0;
+  }
+  g.nshift = 1;
+  g.zero_shift = 0;
+  g.periodic = 0;
+  return DPGB_OK;
+}
+
+// shift vectors t . cell (the reference's einsum over d, in order d = 0,1,2)
+void shift_vectors(const CellGeom& g, const int* shift_idx, int nshift, std::vector<double>& out) {
+  out.assign((size_t)nshift * 3, 0.0);
+  if (!g.periodic) return;
+  for (int s = 0; s < nshift; ++s)
+    for (int k = 0; k < 3; ++k) {
+      double v = 0.0;
+      for (int d = 0; d < 3; ++d) v += (double)shift_idx[3 * s + d] * g.cell[d * 3 + k];
+      out[(size_t)s * 3 + k] = v;
+    }
+}
+
+int sel_from_host(const int* sel_host, int ntypes, SelInfo& s) {
+  if (!sel_host || ntypes <= 0 || ntypes > DPGB_MAX_TYPES) return fail(DPGB_EINVAL, "bad sel/ntypes");
+  s.ntypes = ntypes;
+  s.sec[0] = 0;
+  for (int t = 0; t < ntypes; ++t) {
+    if (sel_host[t] < 0) return fail(DPGB_EINVAL, "negative sel");
+    s.sel[t] = sel_host[t];
+    s.sec[t + 1] = s.sec[t] + sel_host[t];
+  }
+  s.nnei = s.sec[ntypes];
+  return DPGB_OK;
+}
+
+namespace {
+
+__device__ __forceinline__ double dist_fma(double dx, double dy, double dz) {
+  // the FMA chain of torch.linalg.norm (sqrt(fma(z,z,fma(y,y,x*x)))), so
+  // that near-equal distances order exactly as in the reference
+  return sqrt(fma(dz, dz, fma(dy, dy, dx * dx)));
+}
+
+__global__ void normalize_kernel(double* __restrict__ out, const double* __restrict__ in, int n,
+                                 CellGeom g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double x = in[3 * i], y = in[3 * i + 1], z = in[3 * i + 2];
+  double f[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double v = fma(z, g.rec[6 + k], fma(y, g.rec[3 + k], x * g.rec[k]));
+    v = v - floor(v);
+    f[k] = v;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    out[3 * i + k] = fma(f[2], g.cell[6 + k], fma(f[1], g.cell[3 + k], f[0] * g.cell[k]));
+}
+
+__global__ void extend_kernel(double* __restrict__ cext, int* __restrict__ text,
+                              int* __restrict__ mapping, const double* __restrict__ coord,
+                              const int* __restrict__ atype, int nloc, int nshift,
+                              const double* __restrict__ svec) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (long long)nloc * nshift) return;
+  const int s = (int)(q / nloc), j = (int)(q % nloc);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) cext[3 * q + k] = coord[3 * j + k] + svec[3 * s + k];
+  if (text) text[q] = atype[j];
+  if (mapping) mapping[q] = j;
+}
+
+__global__ void cell_count_kernel(int* __restrict__ cell_of, int* __restrict__ counts,
+                                  const double* __restrict__ coord, int n, CellGeom g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double f;
+    if (g.periodic)
+      f = (coord[3 * i] * g.rec[k] + coord[3 * i + 1] * g.rec[3 + k] +
+           coord[3 * i + 2] * g.rec[6 + k]) * g.ncell[k];
+    else
+      f = (coord[3 * i + k] - g.origin[k]) / g.csize[k];
+    int ci = (int)floor(f);
+    ci = ci < 0 ? 0 : (ci >= g.ncell[k] ? g.ncell[k] - 1 : ci);
+    c[k] = ci;
+  }
+  const int id = (c[0] * g.ncell[1] + c[1]) * g.ncell[2] + c[2];
+  cell_of[i] = id;
+  atomicAdd(&counts[id], 1);
+}
+
+__global__ void cell_fill_kernel(int* __restrict__ cell_atoms, int* __restrict__ cursor,
+                                 const int* __restrict__ offsets, const int* __restrict__ cell_of,
+                                 int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = cell_of[i];
+  cell_atoms[offsets[c] + atomicAdd(&cursor[c], 1)] = i;
+}
+
+constexpr int kSearchWarps = 2;
+
+// stencil cell -> (wrapped cell, periodic image); false when outside an open box
+__device__ __forceinline__ bool wrap_cell(int x, int n, int periodic, int& xw, int& t) {
+  if (!periodic) {
+    xw = x;
+    t = 0;
+    return x >= 0 && x < n;
+  }
+  t = x >= 0 ? x / n : -((-x + n - 1) / n);
+  xw = x - t * n;
+  return true;
+}
+constexpr int kCap = 1024;
+
+struct Cand {
+  double r;
+  int idx;
+  int type;
+};
+
+__device__ __forceinline__ bool cand_less(double ra, int ia, double rb, int ib) {
+  return ra < rb || (ra == rb && ia < ib);
+}
+
+// One warp per centre atom: gather the atoms of the stencil cells within
+// rcut, rank them by (distance, extended index), keep the nearest nsel and
+// place each in its type section while its per-type rank < sel[t].
+__global__ void __launch_bounds__(kSearchWarps * 32)
+nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
+                const int* __restrict__ atype, const int* __restrict__ cell_of,
+                const int* __restrict__ offsets, const int* __restrict__ cell_atoms,
+                const int* __restrict__ shift_pos, const double* __restrict__ svec, int nloc,
+                CellGeom g, double rcut, SelInfo sel, int* __restrict__ status) {
+  __shared__ double s_r[kSearchWarps][kCap];
+  __shared__ int s_idx[kSearchWarps][kCap];
+  __shared__ int s_type[kSearchWarps][kCap];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kSearchWarps + warp;
+  if (i >= nloc) return;
+  int* row = nlist + (size_t)i * sel.nnei;
+  for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
+  if (atype[i] < 0) return;
+  const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
+  const int ci = cell_of[i];
+  const int cz = ci % g.ncell[2], cy = (ci / g.ncell[2]) % g.ncell[1],
+            cx = ci / (g.ncell[1] * g.ncell[2]);
+  const int sy = 2 * g.nbuff[1] + 1, sz = 2 * g.nbuff[2] + 1;
+  int n = 0;
+  bool overflow = false;
+  for (int ox = -g.reach[0]; ox <= g.reach[0]; ++ox) {
+    int xw, tx;
+    if (!wrap_cell(cx + ox, g.ncell[0], g.periodic, xw, tx)) continue;
+    for (int oy = -g.reach[1]; oy <= g.reach[1]; ++oy) {
+      int yw, ty;
+      if (!wrap_cell(cy + oy, g.ncell[1], g.periodic, yw, ty)) continue;
+      for (int oz = -g.reach[2]; oz <= g.reach[2]; ++oz) {
+        int zw, tz;
+        if (!wrap_cell(cz + oz, g.ncell[2], g.periodic, zw, tz)) continue;
+        if (abs(tx) > g.nbuff[0] || abs(ty) > g.nbuff[1] || abs(tz) > g.nbuff[2]) continue;
+        const int s = shift_pos[((tx + g.nbuff[0]) * sy + (ty + g.nbuff[1])) * sz + (tz + g.nbuff[2])];
+        const double sx0 = svec[3 * s], sx1 = svec[3 * s + 1], sx2 = svec[3 * s + 2];
+        const int c = (xw * g.ncell[1] + yw) * g.ncell[2] + zw;
+        const int beg = offsets[c], end = offsets[c + 1];
+        for (int p0 = beg; p0 < end; p0 += 32) {
+          const int p = p0 + lane;
+          bool keep = false;
+          double r = 0.0;
+          int j = -1, tj = -1;
+          if (p < end) {
+            j = cell_atoms[p];
+            tj = atype[j];
+            if (tj >= 0 && !(j == i && s == g.zero_shift)) {
+              const double dx = (coord[3 * j] + sx0) - xi;
+              const double dy = (coord[3 * j + 1] + sx1) - yi;
+              const double dz = (coord[3 * j + 2] + sx2) - zi;
+              r = dist_fma(dx, dy, dz);
+              keep = r <= rcut;
+            }
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, keep);
+          const int pos = n + __popc(m & ((1u << lane) - 1u));
+          if (keep) {
+            if (pos < kCap) {
+              s_r[warp][pos] = r;
+              s_idx[warp][pos] = s * nloc + j;
+              s_type[warp][pos] = tj;
+            } else {
+              overflow = true;
+            }
+          }
+          n += __popc(m);
+        }
+      }
+    }
+  }
+  overflow = __any_sync(0xffffffffu, overflow);
+  if (overflow) {
+    if (lane == 0) {
+      atomicMax(&status[kStatusOverflow], n);
+      atomicMax(&status[kStatusOverflowAtom], i + 1);
+    }
+    return;
+  }
+  __syncwarp();
+  for (int k = lane; k < n; k += 32) {
+    const double rk = s_r[warp][k];
+    const int ik = s_idx[warp][k], tk = s_type[warp][k];
+    int rank = 0, trank = 0;
+    for (int m2 = 0; m2 < n; ++m2) {
+      const bool lt = cand_less(s_r[warp][m2], s_idx[warp][m2], rk, ik);
+      rank += lt;
+      trank += lt && s_type[warp][m2] == tk;
+    }
+    // topk(sum(sel)): candidates of global rank >= nnei are dropped
+    if (rank < sel.nnei && tk < sel.ntypes && trank < sel.sel[tk]) row[sel.sec[tk] + trank] = ik;
+  }
+}
+
+// C++ order (source/lib/src/fmt_nlist.cc:98-150): fp32 r^2 computed without
+// contraction, (type, r^2, index) order, per-type truncation.
+__global__ void __launch_bounds__(kSearchWarps * 32)
+format_nlist_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
+                    const int* __restrict__ atype, const int* __restrict__ rows,
+                    const int* __restrict__ counts, int max_nbor, int nloc, float rcut2,
+                    SelInfo sel, int* __restrict__ status) {
+  __shared__ float s_r[kSearchWarps][kCap];
+  __shared__ int s_idx[kSearchWarps][kCap];
+  __shared__ int s_type[kSearchWarps][kCap];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kSearchWarps + warp;
+  if (i >= nloc) return;
+  int* row = nlist + (size_t)i * sel.nnei;
+  for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
+  const float xi = (float)coord[3 * i], yi = (float)coord[3 * i + 1], zi = (float)coord[3 * i + 2];
+  int n = 0;
+  bool overflow = false;
+  const int cnt = counts[i];
+  for (int p0 = 0; p0 < cnt; p0 += 32) {
+    const int p = p0 + lane;
+    bool keep = false;
+    float r2 = 0.f;
+    int j = -1, tj = -1;
+    if (p < cnt) {
+      j = rows[(size_t)i * max_nbor + p];
+      tj = atype[j];
+      if (tj >= 0) {
+        const float dx = __fsub_rn((float)coord[3 * j], xi);
+        const float dy = __fsub_rn((float)coord[3 * j + 1], yi);
+        const float dz = __fsub_rn((float)coord[3 * j + 2], zi);
+        r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+        keep = r2 <= rcut2;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const int pos = n + __popc(m & ((1u << lane) - 1u));
+    if (keep) {
+      if (pos < kCap) {
+        s_r[warp][pos] = r2;
+        s_idx[warp][pos] = j;
+        s_type[warp][pos] = tj;
+      } else {
+        overflow = true;
+      }
+    }
+    n += __popc(m);
+  }
+  if (__any_sync(0xffffffffu, overflow)) {
+    if (lane == 0) {
+      atomicMax(&status[kStatusOverflow], n);
+      atomicMax(&status[kStatusOverflowAtom], i + 1);
+    }
+    return;
+  }
+  __syncwarp();
+  bool dropped = false;
+  for (int k = lane; k < n; k += 32) {
+    const float rk = s_r[warp][k];
+    const int ik = s_idx[warp][k], tk = s_type[warp][k];
+    int trank = 0;
+    for (int m2 = 0; m2 < n; ++m2) {
+      const int tm = s_type[warp][m2];
+      const float rm = s_r[warp][m2];
+      const int im = s_idx[warp][m2];
+      trank += (tm == tk) && (rm < rk || (rm == rk && im < ik));
+    }
+    if (tk < sel.ntypes && trank < sel.sel[tk])
+      row[sel.sec[tk] + trank] = ik;
+    else
+      dropped = true;
+  }
+  if (__any_sync(0xffffffffu, dropped) && lane == 0) atomicAdd(&status[kStatusDropped], 1);
+}
+
+// single-block exclusive scan of n ints (n+1 outputs)
+__global__ void scan_kernel(int* __restrict__ out, const int* __restrict__ in, int n) {
+  __shared__ int s_part[1024];
+  const int t = threadIdx.x;
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int b = t * per, e = min(n, b + per);
+  int s = 0;
+  for (int k = b; k < e; ++k) s += in[k];
+  s_part[t] = s;
+  __syncthreads();
+  for (int o = 1; o < blockDim.x; o <<= 1) {
+    int v = t >= o ? s_part[t - o] : 0;
+    __syncthreads();
+    s_part[t] += v;
+    __syncthreads();
+  }
+  int run = t == 0 ? 0 : s_part[t - 1];
+  for (int k = b; k < e; ++k) {
+    out[k] = run;
+    run += in[k];
+  }
+  if (t == blockDim.x - 1) out[n] = s_part[t];
+}
+
+// transpose: count, fill, then sort every bucket by pair id
+__global__ void tr_count_kernel(int* __restrict__ counts, const int* __restrict__ keys, long long npair,
+                                int mod) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npair) return;
+  int k = keys[p];
+  if (k < 0) return;
+  if (mod > 0) k %= mod;
+  atomicAdd(&counts[k], 1);
+}
+__global__ void tr_fill_kernel(int* __restrict__ pairs, int* __restrict__ cursor,
+                               const int* __restrict__ offsets, const int* __restrict__ keys,
+                               long long npair, int mod) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npair) return;
+  int k = keys[p];
+  if (k < 0) return;
+  if (mod > 0) k %= mod;
+  pairs[offsets[k] + atomicAdd(&cursor[k], 1)] = (int)p;
+}
+constexpr int kTrCap = 2048;
+__global__ void tr_sort_kernel(int* __restrict__ pairs, const int* __restrict__ offsets, int nkeys,
+                               int* __restrict__ status) {
+  __shared__ int s_v[kTrCap];
+  const int k = blockIdx.x;
+  if (k >= nkeys) return;
+  const int beg = offsets[k], n = offsets[k + 1] - beg;
+  if (n <= 1) return;
+  if (n > kTrCap) {
+    if (threadIdx.x == 0) {
+      atomicMax(&status[kStatusOverflow], n);
+      atomicMax(&status[kStatusOverflowAtom], k + 1);
+    }
+    return;
+  }
+  for (int q = threadIdx.x; q < n; q += blockDim.x) s_v[q] = pairs[beg + q];
+  __syncthreads();
+  int mine[kTrCap / 128];
+  int cnt = 0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int v = s_v[q];
+    int rank = 0;
+    for (int m = 0; m < n; ++m) rank += s_v[m] < v;
+    mine[cnt++] = rank;
+  }
+  __syncthreads();
+  cnt = 0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int v = s_v[q];
+    pairs[beg + mine[cnt++]] = v;
+  }
+}
+
+}  // namespace
+
+int launch_normalize(double* out, const double* in, int n, const CellGeom& g, cudaStream_t st) {
+  if (n <= 0) return DPGB_OK;
+  normalize_kernel<<<ceil_div(n, 256), 256, 0, st>>>(out, in, n, g);
+  return check_launch("normalize_coord");
+}
+
+int launch_extend(double* cext, int* text, int* mapping, const double* coord, const int* atype,
+                  int nloc, int nshift, const double* svec_dev, cudaStream_t st) {
+  const long long tot = (long long)nloc * nshift;
+  if (tot <= 0) return DPGB_OK;
+  extend_kernel<<<ceil_div(tot, 256), 256, 0, st>>>(cext, text, mapping, coord, atype, nloc, nshift,
+                                                     svec_dev);
+  return check_launch("extend_coord");
+}
+
+size_t nlist_pt_workspace(int nloc, const CellGeom& g) {
+  const size_t ncell = (size_t)g.ncell[0] * g.ncell[1] * g.ncell[2];
+  return sizeof(int) * (2 * (size_t)nloc + 3 * (ncell + 1)) + 256 * 4;
+}
+
+int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc, const CellGeom& g,
+                    const int* shift_pos_dev, const double* svec_dev, double rcut,
+                    const SelInfo& sel, void* workspace, int* status, cudaStream_t st) {
+  if (nloc <= 0) return DPGB_OK;
+  const int ncell = g.ncell[0] * g.ncell[1] * g.ncell[2];
+  int* cell_of = reinterpret_cast<int*>(workspace);
+  int* cell_atoms = cell_of + nloc;
+  int* counts = cell_atoms + nloc;
+  int* offsets = counts + (ncell + 1);
+  int* cursor = offsets + (ncell + 1);
+  DPGB_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (ncell + 1), st));
+  DPGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * (ncell + 1), st));
+  cell_count_kernel<<<ceil_div(nloc, 256), 256, 0, st>>>(cell_of, counts, coord, nloc, g);
+  DPGB_TRY(check_launch("cell_count"));
+  scan_kernel<<<1, 1024, 0, st>>>(offsets, counts, ncell);
+  DPGB_TRY(check_launch("cell_scan"));
+  cell_fill_kernel<<<ceil_div(nloc, 256), 256, 0, st>>>(cell_atoms, cursor, offsets, cell_of, nloc);
+  DPGB_TRY(check_launch("cell_fill"));
+  nlist_pt_kernel<<<ceil_div(nloc, kSearchWarps), kSearchWarps * 32, 0, st>>>(
+      nlist, coord, atype, cell_of, offsets, cell_atoms, shift_pos_dev, svec_dev, nloc, g, rcut, sel,
+      status);
+  return check_launch("nlist_pt");
+}
+
+int launch_format_nlist(int* nlist, const double* coord, const int* atype, const int* rows,
+                        const int* counts, int max_nbor, int nloc, double rcut, const SelInfo& sel,
+                        int* status, cudaStream_t st) {
+  if (nloc <= 0) return DPGB_OK;
+  const float rc = (float)rcut;
+  format_nlist_kernel<<<ceil_div(nloc, kSearchWarps), kSearchWarps * 32, 0, st>>>(
+      nlist, coord, atype, rows, counts, max_nbor, nloc, rc * rc, sel, status);
+  return check_launch("format_nlist");
+}
+
+size_t transpose_workspace(long long npair, int nkeys) {
+  return sizeof(int) * (3 * ((size_t)nkeys + 1) + (size_t)npair) + 256;
+}
+
+int launch_transpose(Transpose& tr, const int* keys, long long npair, int nkeys, int mod,
+                     void* workspace, int* status, cudaStream_t st) {
+  int* counts = reinterpret_cast<int*>(workspace);
+  tr.offsets = counts + (nkeys + 1);
+  int* cursor = tr.offsets + (nkeys + 1);
+  tr.pairs = cursor + (nkeys + 1);
+  tr.nkeys = nkeys;
+  DPGB_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), st));
+  DPGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * (nkeys + 1), st));
+  if (npair > 0) {
+    tr_count_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(counts, keys, npair, mod);
+    DPGB_TRY(check_launch("transpose_count"));
+  }
+  scan_kernel<<<1, 1024, 0, st>>>(tr.offsets, counts, nkeys);
+  DPGB_TRY(check_launch("transpose_scan"));
+  if (npair > 0) {
+    tr_fill_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(tr.pairs, cursor, tr.offsets, keys, npair,
+                                                          mod);
+    DPGB_TRY(check_launch("transpose_fill"));
+    tr_sort_kernel<<<nkeys, 128, 0, st>>>(tr.pairs, tr.offsets, nkeys, status);
+    DPGB_TRY(check_launch("transpose_sort"));
+  }
+  return DPGB_OK;
+}
+
+int read_status(int* status_dev, cudaStream_t st, int out[kStatusSlots]) {
+  DPGB_CUDA(cudaMemcpyAsync(out, status_dev, sizeof(int) * kStatusSlots, cudaMemcpyDeviceToHost, st));
+  DPGB_CUDA(cudaStreamSynchronize(st));
+  return DPGB_OK;
+}
+
+}  // namespace dpgb
+
+using namespace dpgb;
+
+
+extern "C" {
+
+int dpgb_normalize_coord(double* out, const double* coord, int natom, const double* box,
+                         void* stream) {
+  clear_error();
+  if (natom < 0 || (natom > 0 && (!out || !coord)) || !box)
+    return fail(DPGB_EINVAL, "normalize_coord: bad args (box is required)");
+  CellGeom g;
+  DPGB_TRY(box_geom(box, g));
+  return launch_normalize(out, coord, natom, g, as_stream(stream));
+}
+
+int dpgb_extend_coord(double* cext, int* text, int* mapping, const double* coord, const int* atype,
+                      int nloc, const double* box, const int* shift_idx, int nshift, void* stream) {
+  clear_error();
+  if (nloc < 0 || !box || !shift_idx || nshift <= 0) return fail(DPGB_EINVAL, "extend_coord: bad args");
+  CellGeom g;
+  DPGB_TRY(box_geom(box, g));
+  std::vector<double> svec;
+  shift_vectors(g, shift_idx, nshift, svec);
+  DeviceBuffer d;
+  DPGB_TRY(d.alloc(sizeof(double) * svec.size()));
+  cudaStream_t st = as_stream(stream);
+  DPGB_CUDA(cudaMemcpyAsync(d.ptr, svec.data(), sizeof(double) * svec.size(), cudaMemcpyHostToDevice, st));
+  DPGB_TRY(launch_extend(cext, text, mapping, coord, atype, nloc, nshift, d.as<double>(), st));
+  DPGB_CUDA(cudaStreamSynchronize(st));  // before the temporary is freed
+  return DPGB_OK;
+}
+
+int dpgb_build_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc,
+                        const double* box, const int* shift_idx, int nshift, double rcut,
+                        const int* sel_host, int ntypes, void* stream) {
+  clear_error();
+  SelInfo sel;
+  DPGB_TRY(sel_from_host(sel_host, ntypes, sel));
+  if (nloc < 0 || (nloc > 0 && (!nlist || !coord || !atype)) || !(rcut > 0))
+    return fail(DPGB_EINVAL, "build_nlist_pt: bad args");
+  if (nloc == 0) return DPGB_OK;
+  cudaStream_t st = as_stream(stream);
+  CellGeom g;
+  std::vector<int> shift_pos(1, 0);
+  std::vector<double> svec;
+  if (box) {
+    DPGB_TRY(periodic_geom(box, rcut, nshift, shift_idx, g, shift_pos));
+    shift_vectors(g, shift_idx, nshift, svec);
+  } else {
+    // open boundary: the cell list spans the atoms' bounding box (needs the
+    // coordinates on the host for the box; one copy of 24*nloc bytes)
+    std::vector<double> hc((size_t)nloc * 3);
+    DPGB_CUDA(cudaMemcpyAsync(hc.data(), coord, sizeof(double) * hc.size(), cudaMemcpyDeviceToHost, st));
+    DPGB_CUDA(cudaStreamSynchronize(st));
+    DPGB_TRY(open_geom(hc.data(), nloc, rcut, g));
+    svec.assign(3, 0.0);
+  }
+  DeviceBuffer ws;
+  const size_t wbytes = nlist_pt_workspace(nloc, g);
+  const size_t extra = sizeof(int) * shift_pos.size() + sizeof(double) * svec.size() +
+                       sizeof(int) * kStatusSlots + 64;
+  DPGB_TRY(ws.alloc(wbytes + extra));
+  char* base = ws.as<char>();
+  int* status = reinterpret_cast<int*>(base);
+  int* spos = status + kStatusSlots;
+  double* sv = reinterpret_cast<double*>(reinterpret_cast<char*>(spos) +
+                                         ((sizeof(int) * shift_pos.size() + 15) / 16) * 16);
+  void* work = reinterpret_cast<char*>(sv) + ((sizeof(double) * svec.size() + 15) / 16) * 16;
+  DPGB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * kStatusSlots, st));
+  DPGB_CUDA(cudaMemcpyAsync(spos, shift_pos.data(), sizeof(int) * shift_pos.size(), cudaMemcpyHostToDevice, st));
+  DPGB_CUDA(cudaMemcpyAsync(sv, svec.data(), sizeof(double) * svec.size(), cudaMemcpyHostToDevice, st));
+  DPGB_TRY(launch_nlist_pt(nlist, coord, atype, nloc, g, spos, sv, rcut, sel, work, status, st));
+  int h[kStatusSlots];
+  DPGB_TRY(read_status(status, st, h));
+  if (h[kStatusOverflow] > 0)
+    return fail(DPGB_EOVERFLOW, "build_nlist_pt: atom " + std::to_string(h[kStatusOverflowAtom] - 1) +
+                                    " has more than 1024 atoms within rcut");
+  return DPGB_OK;
+}
+
+int dpgb_format_nlist_a(int* nlist, const double* coord, const int* atype, const int* rows,
+                        const int* counts, int max_nbor, int nloc, int nall, double rcut,
+                        const int* sel_host, int ntypes, int* overflow_host, void* stream) {
+  clear_error();
+  SelInfo sel;
+  DPGB_TRY(sel_from_host(sel_host, ntypes, sel));
+  if (nloc < 0 || nall < nloc || max_nbor < 0 || (nloc > 0 && (!nlist || !coord || !atype || !counts)))
+    return fail(DPGB_EINVAL, "format_nlist_a: bad args");
+  if (nloc == 0) return DPGB_OK;
+  cudaStream_t st = as_stream(stream);
+  DeviceBuffer ws;
+  DPGB_TRY(ws.alloc(sizeof(int) * kStatusSlots));
+  int* status = ws.as<int>();
+  DPGB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * kStatusSlots, st));
+  DPGB_TRY(launch_format_nlist(nlist, coord, atype, rows, counts, max_nbor, nloc, rcut, sel, status, st));
+  int h[kStatusSlots];
+  DPGB_TRY(read_status(status, st, h));
+  if (overflow_host) *overflow_host = h[kStatusDropped];
+  if (h[kStatusOverflow] > 0)
+    return fail(DPGB_EOVERFLOW, "format_nlist_a: row " + std::to_string(h[kStatusOverflowAtom] - 1) +
+                                    " has more than 1024 candidates within rcut");
+  return DPGB_OK;
+}
+
+}  // extern "C"

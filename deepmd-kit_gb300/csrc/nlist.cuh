@@ -1,0 +1,67 @@
+// Neighbour-list building blocks shared by the op-level entry points and the
+// DeepPot pipeline.
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace dpgb {
+
+enum StatusExtra { kStatusDropped = 3 };
+
+// Cell-list geometry of one frame (host-computed, passed by value).
+struct CellGeom {
+  double cell[9];     // rows are the cell vectors
+  double rec[9];      // inverse of cell
+  double origin[3];   // open boundary: lower corner of the atoms' bounding box
+  double csize[3];    // open boundary: cell edge
+  int ncell[3];       // cells per direction
+  int reach[3];       // stencil half-width in cells
+  int nbuff[3];       // periodic image range (reference nbuff)
+  int nshift;
+  int zero_shift;     // position of the (0,0,0) image
+  int periodic;
+};
+
+struct SelInfo {
+  int ntypes;
+  int nnei;
+  int sel[DPGB_MAX_TYPES];
+  int sec[DPGB_MAX_TYPES + 1];
+};
+
+// Sorted transpose of a list: for key k, pairs[offsets[k] .. offsets[k+1])
+// are the pair ids p (ascending) with keys[p] (mod `mod`) == k.
+struct Transpose {
+  int* offsets = nullptr;
+  int* pairs = nullptr;
+  int nkeys = 0;
+};
+
+// cell, inverse cell and face distances of a periodic box
+int box_geom(const double* box, CellGeom& g);
+// periodic cell list + image table for the reference's image order
+int periodic_geom(const double* box, double rcut, int nshift, const int* shift_idx, CellGeom& g,
+                  std::vector<int>& shift_pos);
+// open boundary: bounding box of host coordinates
+int open_geom(const double* coord_host, int n, double rcut, CellGeom& g);
+void shift_vectors(const CellGeom& g, const int* shift_idx, int nshift, std::vector<double>& out);
+
+int launch_normalize(double* out, const double* in, int n, const CellGeom& g, cudaStream_t st);
+int launch_extend(double* cext, int* text, int* mapping, const double* coord, const int* atype,
+                  int nloc, int nshift, const double* svec_dev, cudaStream_t st);
+size_t nlist_pt_workspace(int nloc, const CellGeom& g);
+int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc, const CellGeom& g,
+                    const int* shift_pos_dev, const double* svec_dev, double rcut,
+                    const SelInfo& sel, void* workspace, int* status, cudaStream_t st);
+int launch_format_nlist(int* nlist, const double* coord, const int* atype, const int* rows,
+                        const int* counts, int max_nbor, int nloc, double rcut, const SelInfo& sel,
+                        int* status, cudaStream_t st);
+size_t transpose_workspace(long long npair, int nkeys);
+int launch_transpose(Transpose& tr, const int* keys, long long npair, int nkeys, int mod,
+                     void* workspace, int* status, cudaStream_t st);
+int read_status(int* status_dev, cudaStream_t st, int out[kStatusSlots]);
+int sel_from_host(const int* sel_host, int ntypes, SelInfo& s);
+
+}  // namespace dpgb

@@ -1,0 +1,99 @@
+// Device-side description of a se_e2_a model and the launchers of the fused
+// descriptor / fitting kernels used by the DeepPot pipeline.
+#pragma once
+
+#include "nlist.cuh"
+
+namespace dpgb {
+
+constexpr int kMaxEmbLayers = 4;
+constexpr int kMaxFitLayers = 5;
+constexpr int kMaxNets = DPGB_MAX_TYPES * DPGB_MAX_TYPES;
+
+// Table interval data of one compressed net (locate_xx constants).
+template <typename T>
+struct TabMeta {
+  T lower, upper, mx, s0, s1, hi_xx;
+  int first, hi_idx;
+  long long offset;  // element offset of the net's table in the table buffer
+};
+
+// Embedding nets: all nets share widths; W[l] is [nnets, nin_l, nout_l],
+// b[l] / idt[l] are [nnets, nout_l] (idt NULL when the layer has none).
+template <typename T>
+struct EmbParams {
+  int n_layer;
+  int width[kMaxEmbLayers];  // output widths; input of layer 0 is 1
+  const T* W[kMaxEmbLayers];
+  const T* b[kMaxEmbLayers];
+  const T* idt[kMaxEmbLayers];
+  int compressed;
+  const T* table;            // compressed: all nets' tables
+  const TabMeta<T>* meta;    // compressed: [nnets]
+};
+
+template <typename T>
+struct DescParams {
+  int nloc;       // atoms per frame
+  int nrows;      // nframes * nloc
+  int nnei;
+  int ntypes;
+  int sec[DPGB_MAX_TYPES + 1];
+  int type_one_side;
+  int ng, axis;
+  int pad_zero;   // padding slots contribute exactly zero (mean == 0)
+  double rcut, rcut_smth;
+  const T* davg;  // [ntypes, nnei, 4]
+  const T* dstd;
+  const int* pair_mask;     // [ntypes*ntypes] or NULL
+  const double* coord;      // [nframes, nloc, 3] normalised
+  const int* atype;         // [nloc]
+  const int* nlist;         // [nrows, nnei] extended indices (image-major)
+  const double* svec;       // [nframes, nshift, 3] image shift vectors
+  int nshift;
+  const int* row_pos;       // [nrows] sorted (by type) row of each atom
+};
+
+// Fitting nets of all types: W[l] [ntypes, nin_l, nout_l] ...
+template <typename T>
+struct FitParams {
+  int n_hidden;
+  int width[kMaxFitLayers + 1];  // width[0] = dim_descrpt, width[l+1] = hidden l
+  const T* W[kMaxFitLayers];
+  const T* b[kMaxFitLayers];
+  const T* idt[kMaxFitLayers];
+  const T* w_out;  // [ntypes, width[n_hidden]]
+  const T* b_out;  // [ntypes]
+};
+
+// Buffers of one evaluation (rows in type-sorted order unless stated).
+template <typename T>
+struct Work {
+  T* D;      // [nrows, dim]
+  T* dD;     // [nrows, dim]
+  T* xyz;    // [nrows, 4, ng] original row order
+  T* gpair;  // [nrows, nnei, 3] original row order
+  double* vir_row;   // [nrows, 9]
+  double* e_row;     // [nrows] atom energy, original order
+  T* act;    // fitting activations: per hidden layer Y and tanh T: 2*n_hidden*[nrows, maxw]
+  T* gbuf;   // fitting gradients: 2 * [nrows, maxw]
+};
+
+template <typename T>
+int launch_desc_fwd(const DescParams<T>& p, const EmbParams<T>& e, T* D, T* xyz, size_t smem,
+                    cudaStream_t st);
+template <typename T>
+size_t desc_fwd_smem(const DescParams<T>& p, const EmbParams<T>& e);
+template <typename T>
+int launch_desc_bwd(const DescParams<T>& p, const EmbParams<T>& e, const T* dD, const T* xyz,
+                    T* gpair, double* vir_row, size_t smem, cudaStream_t st);
+template <typename T>
+size_t desc_bwd_smem(const DescParams<T>& p, const EmbParams<T>& e);
+
+// fitting of the rows [row0, row0+nrow) of one type
+template <typename T>
+int launch_fitting(const FitParams<T>& f, int type, int row0, int nrow, int nrows_total,
+                   const T* D, T* dD, T* act, T* gbuf, double* e_sorted, double ener_bias,
+                   cudaStream_t st);
+
+}  // namespace dpgb

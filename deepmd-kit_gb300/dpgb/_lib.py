@@ -1,0 +1,136 @@
+"""ctypes binding of the C-ABI library ``libdpgb.so`` (include/dpgb.h).
+
+There is no CPU fallback: if the library is missing, :func:`lib` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+_P = C.c_void_p
+_I = C.c_int
+_D = C.c_double
+_IP = C.POINTER(C.c_int)
+_DP = C.POINTER(C.c_double)
+_FP = C.POINTER(C.c_float)
+
+MAX_TYPES = 8
+MAX_LAYERS = 6
+
+
+class DpgbError(RuntimeError):
+    """Raised when a dpgb entry point returns a non-zero status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"dpgb error {code}: {msg}")
+        self.code = code
+
+
+class SeADesc(C.Structure):
+    """dpgb_se_a_desc of include/dpgb.h."""
+
+    _fields_ = [
+        ("ntypes", C.c_int),
+        ("sel", C.c_int * MAX_TYPES),
+        ("rcut", C.c_double),
+        ("rcut_smth", C.c_double),
+        ("type_one_side", C.c_int),
+        ("n_emb", C.c_int),
+        ("emb_neuron", C.c_int * MAX_LAYERS),
+        ("axis_neuron", C.c_int),
+        ("n_fit", C.c_int),
+        ("fit_neuron", C.c_int * MAX_LAYERS),
+        ("dim_descrpt", C.c_int),
+        ("davg", _DP),
+        ("dstd", _DP),
+        ("emb_w", (_DP * MAX_LAYERS) * (MAX_TYPES * MAX_TYPES)),
+        ("emb_b", (_DP * MAX_LAYERS) * (MAX_TYPES * MAX_TYPES)),
+        ("emb_idt", (_DP * MAX_LAYERS) * (MAX_TYPES * MAX_TYPES)),
+        ("fit_w", (_DP * (MAX_LAYERS + 1)) * MAX_TYPES),
+        ("fit_b", (_DP * (MAX_LAYERS + 1)) * MAX_TYPES),
+        ("fit_idt", (_DP * (MAX_LAYERS + 1)) * MAX_TYPES),
+        ("atom_ener_bias", _DP),
+        ("pair_mask", _IP),
+        ("table", _DP * (MAX_TYPES * MAX_TYPES)),
+        ("table_info", (C.c_double * 6) * (MAX_TYPES * MAX_TYPES)),
+        ("compressed", C.c_int),
+    ]
+
+
+# name -> argtypes (all return int unless listed in _RESTYPE)
+_SIGS = {
+    "dpgb_last_error": [],
+    "dpgb_version": [],
+    "dpgb_tabulate_fusion_se_a_f64": [_P, _P, _DP, _P, _P, _I, _I, _I, _I, _P],
+    "dpgb_tabulate_fusion_se_a_f32": [_P, _P, _FP, _P, _P, _I, _I, _I, _I, _P],
+    "dpgb_tabulate_fusion_se_a_grad_f64": [_P, _P, _P, _DP, _P, _P, _P, _I, _I, _I, _I, _P],
+    "dpgb_tabulate_fusion_se_a_grad_f32": [_P, _P, _P, _FP, _P, _P, _P, _I, _I, _I, _I, _P],
+    "dpgb_tabulate_fusion_se_a_grad_grad_f64": [_P, _P, _DP, _P, _P, _P, _P, _I, _I, _I, _I, _P],
+    "dpgb_tabulate_fusion_se_a_grad_grad_f32": [_P, _P, _FP, _P, _P, _P, _P, _I, _I, _I, _I, _P],
+    "dpgb_format_nlist_a": [_P, _P, _P, _P, _P, _I, _I, _I, _D, _IP, _I, _IP, _P],
+    "dpgb_build_nlist_pt": [_P, _P, _P, _I, _DP, _IP, _I, _D, _IP, _I, _P],
+    "dpgb_normalize_coord": [_P, _P, _I, _DP, _P],
+    "dpgb_extend_coord": [_P, _P, _P, _P, _P, _I, _DP, _IP, _I, _P],
+    "dpgb_prod_env_mat_a_f64": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _P, _P, _I, _I, _D, _D, _IP, _I, _P],
+    "dpgb_env_mat_pt_f64": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _P],
+    "dpgb_prod_force_a_f64": [_P, _P, _P, _P, _I, _I, _I, _I, _P],
+    "dpgb_prod_virial_a_f64": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _P],
+    "dpgb_prod_force_grad_a_f64": [_P, _P, _P, _P, _I, _I, _I, _P],
+    "dpgb_prod_virial_grad_a_f64": [_P, _P, _P, _P, _P, _I, _I, _P],
+    "dpgb_deeppot_new": [C.POINTER(SeADesc), _I],
+    "dpgb_deeppot_delete": [_P],
+    "dpgb_deeppot_check_ok": [_P],
+    "dpgb_deeppot_compute": [_P, _I, _I, _DP, _IP, _DP, _DP, _DP, _DP, _DP, _DP],
+    "dpgb_deeppot_compute_device": [_P, _I, _I, _P, _IP, _DP, _P, _P, _P, _P, _P, _P],
+    "dpgb_deeppot_last_launches": [_P],
+    "dpgb_deeppot_set_profiling": [_P, _I],
+    "dpgb_deeppot_collect_stages": [_P],
+    "dpgb_deeppot_stage_times": [_P, _DP, _IP],
+}
+STAGES = ["nlist", "transpose", "desc_fwd", "fitting", "desc_bwd", "reduce"]
+_RESTYPE = {
+    "dpgb_last_error": C.c_char_p,
+    "dpgb_version": C.c_char_p,
+    "dpgb_deeppot_new": _P,
+    "dpgb_deeppot_delete": None,
+    "dpgb_deeppot_check_ok": C.c_char_p,
+}
+EXPORTED = sorted(_SIGS)
+
+_lock = threading.Lock()
+_handle = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = True):
+    """The loaded library.  Builds it in-tree when missing (nvcc required)."""
+    global _handle
+    with _lock:
+        if _handle is None:
+            path = lib_path()
+            if build_if_missing and (not os.path.exists(path) or _build.needs_build()):
+                _build.build()
+            if not os.path.exists(path):
+                raise ImportError(f"dpgb CUDA library not found at {path}")
+            h = C.CDLL(path)
+            for name, args in _SIGS.items():
+                fn = getattr(h, name)
+                fn.argtypes = args
+                fn.restype = _RESTYPE.get(name, C.c_int)
+            _handle = h
+    return _handle
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        raise DpgbError(rc, lib().dpgb_last_error().decode())
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib(), name)(*args))

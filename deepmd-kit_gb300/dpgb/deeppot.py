@@ -1,0 +1,182 @@
+"""DeepPot: energy / force / virial of se_e2_a models through libdpgb.
+
+Mirrors the reference inference API (deepmd/infer/deep_pot.py ``DeepPot.eval``
+and the C API ``DP_DeepPotCompute``, source/api_c/include/c_api.h:244-254):
+
+    dp = DeepPot(params, precision="fp64")          # or "mixed"
+    e, f, v = dp.eval(coord, box, atype)            # host numpy in/out
+    e, f, v, ae, av = dp.eval(coord, box, atype, atomic=True)
+
+``coord`` is [nframes, natom*3] (or [natom, 3] for one frame), ``box``
+[nframes, 9] or None (open boundary), ``atype`` [natom].  Energies, virials
+and forces come back in FP64.  :meth:`eval_device` keeps coordinates and
+outputs on the GPU (torch tensors) for MD loops.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from .params import SeAParams
+
+PRECISIONS = {"fp64": 0, "float64": 0, "mixed": 1}
+
+
+def pack_desc(params: SeAParams):
+    """Fill a dpgb_se_a_desc from SeAParams; returns (struct, keepalive)."""
+    c = params.config
+    c.validate()
+    keep = []
+
+    def ptr(a, ctype=C.c_double):
+        if a is None:
+            return C.cast(None, C.POINTER(ctype))
+        a = np.ascontiguousarray(a, dtype=np.float64 if ctype is C.c_double else np.int32)
+        keep.append(a)
+        return a.ctypes.data_as(C.POINTER(ctype))
+
+    d = _lib.SeADesc()
+    d.ntypes = c.ntypes
+    for i, s in enumerate(c.sel):
+        d.sel[i] = s
+    d.rcut, d.rcut_smth = c.rcut, c.rcut_smth
+    d.type_one_side = int(c.type_one_side)
+    d.n_emb = len(c.neuron)
+    for i, w in enumerate(c.neuron):
+        d.emb_neuron[i] = w
+    d.axis_neuron = c.axis_neuron
+    d.n_fit = len(c.fit_neuron)
+    for i, w in enumerate(c.fit_neuron):
+        d.fit_neuron[i] = w
+    d.dim_descrpt = c.dim_descrpt
+    d.davg = ptr(params.mean)
+    d.dstd = ptr(params.stddev)
+    for e, layers in enumerate(params.emb):
+        for l, (w, b, idt) in enumerate(layers):
+            d.emb_w[e][l] = ptr(w)
+            d.emb_b[e][l] = ptr(b)
+            d.emb_idt[e][l] = ptr(idt)
+    for t, layers in enumerate(params.fit):
+        for l, (w, b, idt) in enumerate(layers):
+            d.fit_w[t][l] = ptr(w)
+            d.fit_b[t][l] = ptr(b)
+            d.fit_idt[t][l] = ptr(idt)
+    d.atom_ener_bias = ptr(params.atom_ener_bias())
+    pm = c.pair_mask()
+    d.pair_mask = ptr(pm, C.c_int) if pm is not None else C.cast(None, C.POINTER(C.c_int))
+    if params.compressed:
+        d.compressed = 1
+        for e, (tab, info) in enumerate(zip(params.tables, params.table_info)):
+            d.table[e] = ptr(tab)
+            for k in range(6):
+                d.table_info[e][k] = float(info[k])
+    return d, keep
+
+
+class DeepPot:
+    def __init__(self, params: SeAParams, precision: str = "fp64", device: int = 0):
+        import torch
+
+        if not torch.cuda.is_available():
+            raise RuntimeError("dpgb DeepPot needs a CUDA device")
+        torch.cuda.set_device(device)
+        self.params = params
+        self.precision = precision
+        self.device = device
+        lib = _lib.lib()
+        desc, keep = pack_desc(params)
+        self._h = lib.dpgb_deeppot_new(C.byref(desc), PRECISIONS[precision])
+        del keep
+        if not self._h:
+            raise _lib.DpgbError(-1, lib.dpgb_last_error().decode())
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.lib().dpgb_deeppot_delete(h)
+            self._h = None
+
+    @property
+    def rcut(self) -> float:
+        return self.params.config.rcut
+
+    @property
+    def ntypes(self) -> int:
+        return self.params.config.ntypes
+
+    def last_launches(self) -> int:
+        return int(_lib.lib().dpgb_deeppot_last_launches(self._h))
+
+    def set_profiling(self, on: bool) -> None:
+        _lib.check(_lib.lib().dpgb_deeppot_set_profiling(self._h, int(on)))
+
+    def collect_stages(self) -> None:
+        _lib.check(_lib.lib().dpgb_deeppot_collect_stages(self._h))
+
+    def stage_times(self):
+        """{stage: total ms}, number of collected calls."""
+        ms = (C.c_double * len(_lib.STAGES))()
+        n = C.c_int(0)
+        _lib.check(_lib.lib().dpgb_deeppot_stage_times(self._h, ms, C.byref(n)))
+        return dict(zip(_lib.STAGES, list(ms))), int(n.value)
+
+    def eval(self, coord, box, atype, atomic: bool = False):
+        """Host arrays in and out (DP_DeepPotCompute)."""
+        atype = np.ascontiguousarray(atype, dtype=np.int32).reshape(-1)
+        natom = atype.shape[0]
+        coord = np.ascontiguousarray(coord, dtype=np.float64).reshape(-1, natom * 3)
+        nf = coord.shape[0]
+        boxa = None if box is None else np.ascontiguousarray(box, dtype=np.float64).reshape(nf, 9)
+        e = np.zeros(nf)
+        f = np.zeros((nf, natom, 3))
+        v = np.zeros((nf, 9))
+        ae = np.zeros((nf, natom)) if atomic else None
+        av = np.zeros((nf, natom, 9)) if atomic else None
+        dp = C.POINTER(C.c_double)
+
+        def P(a):
+            return C.cast(None, dp) if a is None else a.ctypes.data_as(dp)
+
+        rc = _lib.lib().dpgb_deeppot_compute(self._h, nf, natom, P(coord), atype.ctypes.data_as(C.POINTER(C.c_int)),
+                                             P(boxa), P(e), P(f), P(v), P(ae), P(av))
+        _lib.check(rc)
+        if atomic:
+            return e, f, v, ae, av
+        return e, f, v
+
+    def eval_device(self, coord, box, atype, atomic: bool = False, out=None):
+        """Device form: ``coord`` a CUDA float64 tensor [nframes, natom*3]
+        (or [natom, 3]); ``box`` host array or None; ``atype`` host array.
+        Returns CUDA tensors; nothing is synchronised."""
+        import torch
+
+        atype = np.ascontiguousarray(atype, dtype=np.int32).reshape(-1)
+        natom = atype.shape[0]
+        coord = coord.reshape(-1, natom * 3)
+        if coord.dtype != torch.float64 or not coord.is_cuda:
+            raise TypeError("coord must be a CUDA float64 tensor")
+        coord = coord.contiguous()
+        nf = coord.shape[0]
+        boxa = None if box is None else np.ascontiguousarray(box, dtype=np.float64).reshape(nf, 9)
+        if out is None:
+            dev = coord.device
+            out = dict(energy=torch.empty(nf, dtype=torch.float64, device=dev),
+                       force=torch.empty(nf, natom, 3, dtype=torch.float64, device=dev),
+                       virial=torch.empty(nf, 9, dtype=torch.float64, device=dev))
+            if atomic:
+                out["atom_energy"] = torch.empty(nf, natom, dtype=torch.float64, device=dev)
+                out["atom_virial"] = torch.empty(nf, natom, 9, dtype=torch.float64, device=dev)
+        vp = C.c_void_p
+        ae = out.get("atom_energy") if atomic else None
+        av = out.get("atom_virial") if atomic else None
+        rc = _lib.lib().dpgb_deeppot_compute_device(
+            self._h, nf, natom, vp(coord.data_ptr()), atype.ctypes.data_as(C.POINTER(C.c_int)),
+            C.cast(None, C.POINTER(C.c_double)) if boxa is None else boxa.ctypes.data_as(C.POINTER(C.c_double)),
+            vp(out["energy"].data_ptr()), vp(out["force"].data_ptr()), vp(out["virial"].data_ptr()),
+            vp(ae.data_ptr()) if ae is not None else None, vp(av.data_ptr()) if av is not None else None,
+            vp(torch.cuda.current_stream().cuda_stream))
+        _lib.check(rc)
+        return out

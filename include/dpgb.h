@@ -1,0 +1,289 @@
+/* dpgb — GB300-native (sm_103a) se_e2_a energy / force / virial library.
+ *
+ * Plain C ABI: device or host pointers and sizes, no C++ or torch types.
+ * Every function returns 0 on success or a negative DPGB_E* code; the text of
+ * the last error of the calling thread is returned by dpgb_last_error().
+ * Kernels are enqueued on the caller's stream (`stream` is a cudaStream_t,
+ * NULL = the legacy default stream); functions that return device results do
+ * not synchronise unless they say so.  No function uses atomics for floating
+ * point accumulation: results are bitwise reproducible run to run.
+ *
+ * Each declaration names the reference interface it replaces (paths in the
+ * deepmodeling/deepmd-kit tree).
+ */
+#ifndef DPGB_H
+#define DPGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DPGB_OK 0
+#define DPGB_EINVAL -1    /* bad argument (sizes, NULL pointers, dims) */
+#define DPGB_ECUDA -2     /* a CUDA runtime call failed */
+#define DPGB_EOVERFLOW -3 /* a neighbour buffer or bucket capacity was exceeded */
+#define DPGB_ENOMEM -4    /* device allocation failed */
+#define DPGB_ETIMEOUT -5  /* a bounded device-side wait gave up */
+
+#define DPGB_MAX_TYPES 8
+#define DPGB_MAX_LAYERS 6
+
+/* Text of the last error raised on the calling thread ("" when none). */
+const char* dpgb_last_error(void);
+/* Library version string. */
+const char* dpgb_version(void);
+
+/* ------------------------------------------------------------------------
+ * tabulate_fusion_se_a — the compressed embedding fused with G^T R~.
+ * Replaces deepmd::tabulate_fusion_se_a_gpu / _grad_gpu / _grad_grad_gpu
+ * (source/lib/include/tabulate.h:11-71, source/lib/src/gpu/tabulate.cu:
+ * 1218-1367) behind torch.ops.deepmd.tabulate_fusion_se_a
+ * (source/op/pt/tabulate_multi_device.cc:1630).  Device pointers:
+ *   table [nspline, 6*last_layer_size], em_x [nloc*nnei], em [nloc,nnei,4],
+ *   out / dz_dy [nloc, 4, last_layer_size], dy [nloc, 4, last_layer_size],
+ *   dy_dem_x [nloc*nnei], dy_dem [nloc, nnei, 4].
+ * table_info is a HOST array of 6: {lower, upper, upper*extrapolate,
+ * stride0, stride1, check_frequency} (tabulate_multi_device.cc:33-49).
+ * is_sorted folds trailing padding exactly like the reference. */
+int dpgb_tabulate_fusion_se_a_f64(double* out, const double* table,
+                                  const double* table_info_host,
+                                  const double* em_x, const double* em,
+                                  int nloc, int nnei, int last_layer_size,
+                                  int is_sorted, void* stream);
+int dpgb_tabulate_fusion_se_a_f32(float* out, const float* table,
+                                  const float* table_info_host,
+                                  const float* em_x, const float* em, int nloc,
+                                  int nnei, int last_layer_size, int is_sorted,
+                                  void* stream);
+int dpgb_tabulate_fusion_se_a_grad_f64(double* dy_dem_x, double* dy_dem,
+                                       const double* table,
+                                       const double* table_info_host,
+                                       const double* em_x, const double* em,
+                                       const double* dy, int nloc, int nnei,
+                                       int last_layer_size, int is_sorted,
+                                       void* stream);
+int dpgb_tabulate_fusion_se_a_grad_f32(float* dy_dem_x, float* dy_dem,
+                                       const float* table,
+                                       const float* table_info_host,
+                                       const float* em_x, const float* em,
+                                       const float* dy, int nloc, int nnei,
+                                       int last_layer_size, int is_sorted,
+                                       void* stream);
+int dpgb_tabulate_fusion_se_a_grad_grad_f64(
+    double* dz_dy, const double* table, const double* table_info_host,
+    const double* em_x, const double* em, const double* dz_dy_dem_x,
+    const double* dz_dy_dem, int nloc, int nnei, int last_layer_size,
+    int is_sorted, void* stream);
+int dpgb_tabulate_fusion_se_a_grad_grad_f32(
+    float* dz_dy, const float* table, const float* table_info_host,
+    const float* em_x, const float* em, const float* dz_dy_dem_x,
+    const float* dz_dy_dem, int nloc, int nnei, int last_layer_size,
+    int is_sorted, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Neighbour lists.
+ *
+ * dpgb_format_nlist_a: format a candidate list into typed sections.
+ * Replaces deepmd::format_nbor_list_gpu (source/lib/src/gpu/
+ * prod_env_mat.cu:618-679) / format_nlist_cpu (source/lib/src/fmt_nlist.cc:
+ * 98-150).  Candidates come as a dense device array in_rows [nloc, max_nbor]
+ * with in_counts [nloc] (the reference's InputNlist ilist/numneigh/
+ * firstneigh, ilist = identity).  Order: (type, fp32 r^2, index), each type
+ * truncated to sel[t]; nlist [nloc, sum(sel)] (-1 padded).  *overflow_host
+ * (optional) receives the number of rows that dropped neighbours; passing it
+ * synchronises the stream.  Returns DPGB_EOVERFLOW when a row holds more than
+ * 1024 candidates within rcut. */
+int dpgb_format_nlist_a(int* nlist, const double* coord_ext, const int* atype_ext,
+                        const int* in_rows, const int* in_counts, int max_nbor,
+                        int nloc, int nall, double rcut, const int* sel_host,
+                        int ntypes, int* overflow_host, void* stream);
+
+/* dpgb_build_nlist_pt: typed neighbour list of one periodic (or open) frame
+ * in the order of the reference PyTorch path: extended atoms (all periodic
+ * images, image-major, images in the order `shift_idx` gives) within rcut
+ * ordered by (fp64 distance, extended index), the nearest sum(sel) kept, then
+ * split per type keeping the first sel[t] (deepmd/pt/utils/nlist.py:14-199,
+ * 304-337, 424-513).  Built with a cell list in O(N).
+ *   coord [nloc,3] (already normalised), atype [nloc] (device),
+ *   box_host [9] (NULL = open boundary), shift_idx_host [nshift, 3] integer
+ *   image shifts in reference order (ignored when box_host is NULL),
+ *   nlist [nloc, sum(sel)] extended indices, -1 padded (device).
+ * Returns DPGB_EOVERFLOW when an atom has more than 1024 atoms within rcut. */
+int dpgb_build_nlist_pt(int* nlist, const double* coord, const int* atype,
+                        int nloc, const double* box_host,
+                        const int* shift_idx_host, int nshift, double rcut,
+                        const int* sel_host, int ntypes, void* stream);
+
+/* Periodic wrap of coordinates into the cell: deepmd/pt/utils/region.py:86
+ * normalize_coord / source/lib/src/gpu/coord.cu:45 normalize_one. */
+int dpgb_normalize_coord(double* coord_out, const double* coord, int natom,
+                         const double* box_host, void* stream);
+
+/* Extended (ghost) coordinates, types and mapping in the reference PyTorch
+ * layout: ext[s*nloc + j] = coord[j] + shift_idx[s] . box
+ * (deepmd/pt/utils/nlist.py:424-513).  Device outputs sized nshift*nloc. */
+int dpgb_extend_coord(double* coord_ext, int* atype_ext, int* mapping,
+                      const double* coord, const int* atype, int nloc,
+                      const double* box_host, const int* shift_idx_host,
+                      int nshift, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Environment matrix.  Replaces deepmd::prod_env_mat_a_gpu
+ * (source/lib/include/prod_env_mat.h, source/lib/src/gpu/prod_env_mat.cu:
+ * 681-726): formats the candidate list (dpgb_format_nlist_a) and evaluates
+ * em [nloc, nnei, 4] = (R~ - avg[t_i]) / std[t_i],
+ * em_deriv [nloc, nnei, 4, 3] = dR~/d r_centre / std, rij [nloc, nnei, 3],
+ * nlist [nloc, nnei].  avg/std [ntypes, nnei, 4] device. */
+int dpgb_prod_env_mat_a_f64(double* em, double* em_deriv, double* rij,
+                            int* nlist, const double* coord_ext,
+                            const int* atype_ext, const int* in_rows,
+                            const int* in_counts, int max_nbor,
+                            const double* avg, const double* std, int nloc,
+                            int nall, double rcut, double rcut_smth,
+                            const int* sel_host, int ntypes, void* stream);
+
+/* Environment matrix of an already typed list, PyTorch API semantics
+ * (deepmd/pt/model/descriptor/env_mat.py:18-119 prod_env_mat): every
+ * non-negative slot evaluated, padding = (0 - avg)/std.  Outputs em
+ * [nf*nloc, nnei, 4], diff [.., 3], sw [.., 1]; nlist holds extended indices
+ * into coord_ext [nf, nall, 3]. */
+int dpgb_env_mat_pt_f64(double* em, double* diff, double* sw,
+                        const double* coord_ext, const int* atype_ext,
+                        const int* nlist, const double* avg, const double* std,
+                        int nf, int nloc, int nall, int nnei, double rcut,
+                        double rcut_smth, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Force and virial from net_deriv = dE/d em.  Replace deepmd::prod_force_a_gpu
+ * (source/lib/src/gpu/prod_force.cu:4-130) and prod_virial_a_gpu
+ * (prod_virial.cu:4-134) without atomics: neighbour contributions are
+ * gathered through a sorted transpose of the list.
+ *   net_deriv [nf*nloc, 4*nnei], env_deriv [nf*nloc, 4*nnei, 3],
+ *   rij [nloc, nnei, 3], nlist [nf*nloc, nnei] (indices < nall),
+ *   force [nf, nall, 3], virial [9], atom_virial [nall, 9]. */
+int dpgb_prod_force_a_f64(double* force, const double* net_deriv,
+                          const double* env_deriv, const int* nlist, int nloc,
+                          int nall, int nnei, int nframes, void* stream);
+int dpgb_prod_virial_a_f64(double* virial, double* atom_virial,
+                           const double* net_deriv, const double* env_deriv,
+                           const double* rij, const int* nlist, int nloc,
+                           int nall, int nnei, void* stream);
+/* Second-order terms for force-loss training: replace
+ * deepmd::prod_force_grad_a_gpu (source/lib/src/gpu/prod_force_grad.cu:
+ * 10-57) and prod_virial_grad_a_gpu (prod_virial_grad.cu:14-52).
+ *   grad [nf, nloc, 3] (force cotangent) / [9] (virial cotangent),
+ *   grad_net [nf*nloc, 4*nnei]. */
+int dpgb_prod_force_grad_a_f64(double* grad_net, const double* grad,
+                               const double* env_deriv, const int* nlist,
+                               int nloc, int nnei, int nframes, void* stream);
+int dpgb_prod_virial_grad_a_f64(double* grad_net, const double* grad,
+                                const double* env_deriv, const double* rij,
+                                const int* nlist, int nloc, int nnei,
+                                void* stream);
+
+/* ------------------------------------------------------------------------
+ * DeepPot: the whole se_e2_a energy / force / virial evaluation.
+ * Mirrors the C API DP_NewDeepPot / DP_DeepPotCompute / DP_DeepPotComputeNList
+ * (source/api_c/include/c_api.h:150,244-322) and the backend method
+ * DeepPotBackend::computew (source/api_cc/include/DeepPot.h:14-200).
+ *
+ * The model is described by host pointers in the reference's own
+ * parameterisation (descriptor mean/stddev [ntypes, nnei, 4]; per-net layer
+ * matrices [num_in, num_out] row-major, biases, timesteps; fitting nets;
+ * per-type energy bias) and copied to the device at creation. */
+typedef struct dpgb_se_a_desc {
+  int ntypes;
+  int sel[DPGB_MAX_TYPES];
+  double rcut, rcut_smth;
+  int type_one_side;
+  int n_emb;
+  int emb_neuron[DPGB_MAX_LAYERS];
+  int axis_neuron;
+  int n_fit;
+  int fit_neuron[DPGB_MAX_LAYERS];
+  int dim_descrpt;
+  const double* davg;
+  const double* dstd;
+  const double* emb_w[DPGB_MAX_TYPES * DPGB_MAX_TYPES][DPGB_MAX_LAYERS];
+  const double* emb_b[DPGB_MAX_TYPES * DPGB_MAX_TYPES][DPGB_MAX_LAYERS];
+  const double* emb_idt[DPGB_MAX_TYPES * DPGB_MAX_TYPES][DPGB_MAX_LAYERS];
+  const double* fit_w[DPGB_MAX_TYPES][DPGB_MAX_LAYERS + 1];
+  const double* fit_b[DPGB_MAX_TYPES][DPGB_MAX_LAYERS + 1];
+  const double* fit_idt[DPGB_MAX_TYPES][DPGB_MAX_LAYERS + 1];
+  const double* atom_ener_bias; /* [ntypes]: bias_atom_e + out_bias */
+  const int* pair_mask;         /* [ntypes*ntypes] 1 keep, 0 excluded; or NULL */
+  const double* table[DPGB_MAX_TYPES * DPGB_MAX_TYPES]; /* compressed nets */
+  double table_info[DPGB_MAX_TYPES * DPGB_MAX_TYPES][6];
+  int compressed;
+} dpgb_se_a_desc;
+
+/* Precision of a DeepPot evaluation. */
+#define DPGB_PREC_FP64 0  /* plain FP64 throughout (the drop-in form) */
+#define DPGB_PREC_MIXED 1 /* FP64 displacement, FP32 env matrix, BF16 tensor-core
+                             embedding (split hi+lo on G) and fitting GEMMs
+                             with FP32 accumulation, FP64 energy/virial sums */
+
+typedef struct dpgb_deeppot dpgb_deeppot;
+
+/* Creates a model on the current CUDA device.  Returns NULL on failure
+ * (message in dpgb_last_error()). */
+dpgb_deeppot* dpgb_deeppot_new(const dpgb_se_a_desc* desc, int precision);
+void dpgb_deeppot_delete(dpgb_deeppot* dp);
+/* Text of the last error stored on the handle, "" when the last call
+ * succeeded (c_api.cc:2730 DP_DeepPotCheckOK). */
+const char* dpgb_deeppot_check_ok(dpgb_deeppot* dp);
+
+/* One or more frames of the same atom count with HOST buffers, as
+ * DP_DeepPotCompute: coord [nframes, natom, 3], atype [natom] (shared by the
+ * frames), box [nframes, 9] or NULL (open boundary).  Outputs (host, caller
+ * allocated): energy [nframes], force [nframes, natom, 3], virial
+ * [nframes, 9], atom_energy [nframes, natom] or NULL, atom_virial
+ * [nframes, natom, 9] or NULL.  Copies in, evaluates, copies out and
+ * synchronises its stream.  Neighbour lists are rebuilt every call. */
+int dpgb_deeppot_compute(dpgb_deeppot* dp, int nframes, int natom,
+                         const double* coord, const int* atype,
+                         const double* box, double* energy, double* force,
+                         double* virial, double* atom_energy,
+                         double* atom_virial);
+
+/* The same with DEVICE coordinates and outputs on `stream`, without a final
+ * synchronisation: the device-resident form used inside an MD loop.  The
+ * atom types stay a HOST array (static metadata of the system; the type
+ * grouping is cached across calls with identical types).  energy [nframes],
+ * force [nframes, natom, 3], virial [nframes, 9], atom_energy, atom_virial
+ * (optional) are FP64 device arrays. */
+int dpgb_deeppot_compute_device(dpgb_deeppot* dp, int nframes, int natom,
+                                const double* coord, const int* atype_host,
+                                const double* box_host, double* energy,
+                                double* force, double* virial,
+                                double* atom_energy, double* atom_virial,
+                                void* stream);
+
+/* Number of kernel launches the last compute issued (for the benchmark). */
+int dpgb_deeppot_last_launches(dpgb_deeppot* dp);
+
+/* Stage timing with CUDA events on the compute stream (no counterpart in
+ * the reference, whose DP_PROFILER hooks the libtorch profiler instead,
+ * source/api_cc/src/DeepPotPT.cc:73-101).  set_profiling(1) creates the
+ * events and clears the totals; after each compute, collect_stages()
+ * waits for that call's events and adds its stage times; stage_times()
+ * returns the totals in ms (DPGB_NUM_STAGES entries) and the number of
+ * collected calls. */
+#define DPGB_STAGE_NLIST 0     /* wrap + cell-list neighbour list */
+#define DPGB_STAGE_TRANSPOSE 1 /* sorted transpose of the list */
+#define DPGB_STAGE_DESC_FWD 2  /* env matrix + embedding + D */
+#define DPGB_STAGE_FITTING 3   /* fitting forward + backward */
+#define DPGB_STAGE_DESC_BWD 4  /* embedding recompute + backward + pair grads */
+#define DPGB_STAGE_REDUCE 5    /* force gather, energy / virial sums */
+#define DPGB_NUM_STAGES 6
+int dpgb_deeppot_set_profiling(dpgb_deeppot* dp, int on);
+int dpgb_deeppot_collect_stages(dpgb_deeppot* dp);
+int dpgb_deeppot_stage_times(dpgb_deeppot* dp, double* ms, int* ncalls);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -196,11 +196,32 @@ static void spline5(double xx, double rmin, double rmax, double* vv,
   }
 }
 
+/* The C++ library's switch takes the radii as float references, so the
+ * interval width rmax - rmin is a float subtraction
+ * (source/lib/include/switcher.h spline5_switch, env_mat.cc:132-133). */
+static void spline5_fr(double xx, float rmin, float rmax, double* vv, double* dd) {
+  if (xx < rmin) {
+    *dd = 0.;
+    *vv = 1.;
+  } else if (xx < rmax) {
+    const float w = rmax - rmin;
+    const double uu = (xx - rmin) / w;
+    const double du = 1. / w;
+    *vv = uu * uu * uu * (-6. * uu * uu + 15. * uu - 10.) + 1.;
+    *dd = (3. * uu * uu * (-6. * uu * uu + 15. * uu - 10.) +
+           uu * uu * uu * (-12. * uu + 15.)) *
+          du;
+  } else {
+    *dd = 0.;
+    *vv = 0.;
+  }
+}
+
 /* The 4-vector R~ = s(r)[1/r, x/r^2, y/r^2, z/r^2] of a displacement d =
  * r_j - r_i and its derivative with respect to the CENTRE atom (the sign
  * convention of source/lib/src/env_mat.cc:156-216), deriv[c*3+k]. */
-static void env_row(const double d[3], double rmin, double rmax, double em[4],
-                    double deriv[12]) {
+static void env_row_sw(const double d[3], double rmin, double rmax, int float_radii,
+                       double em[4], double deriv[12]) {
   const double nr2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
   const double inr = 1. / sqrt(nr2);
   const double nr = nr2 * inr;
@@ -208,7 +229,10 @@ static void env_row(const double d[3], double rmin, double rmax, double em[4],
   const double inr4 = inr2 * inr2;
   const double inr3 = inr4 * nr;
   double sw, dsw;
-  spline5(nr, rmin, rmax, &sw, &dsw);
+  if (float_radii)
+    spline5_fr(nr, (float)rmin, (float)rmax, &sw, &dsw);
+  else
+    spline5(nr, rmin, rmax, &sw, &dsw);
   const double v0 = 1. / nr;
   const double v[3] = {d[0] / nr2, d[1] / nr2, d[2] / nr2};
   for (int k = 0; k < 3; ++k)
@@ -220,6 +244,11 @@ static void env_row(const double d[3], double rmin, double rmax, double em[4],
           v[c] * dsw * d[k] * inr;
   em[0] = v0 * sw;
   for (int c = 0; c < 3; ++c) em[1 + c] = v[c] * sw;
+}
+
+static void env_row(const double d[3], double rmin, double rmax, double em[4],
+                    double deriv[12]) {
+  env_row_sw(d, rmin, rmax, 0, em, deriv);
 }
 
 /* source/lib/src/env_mat.cc:123-223 with the normalisation of
@@ -241,7 +270,7 @@ void orc_env_mat_a(double* em, double* em_deriv, double* rij,
       if (jx >= 0) {
         for (int k = 0; k < 3; ++k)
           d[k] = coord_ext[(size_t)jx * 3 + k] - coord_ext[(size_t)ii * 3 + k];
-        env_row(d, rcut_smth, rcut, e4, dv);
+        env_row_sw(d, rcut_smth, rcut, 1, e4, dv);
       }
       for (int k = 0; k < 3; ++k) rij[s * 3 + k] = d[k];
       for (int c = 0; c < 4; ++c) {

@@ -93,7 +93,8 @@ int orc_build_nlist_pt(int* nlist, const double* coord_ext, const int* atype_ext
 
 /* ---- env matrix (source/lib/src/env_mat.cc:123-223 + prod_env_mat.cc:14-132)
  * em [nloc, nnei, 4] normalised, em_deriv [nloc, nnei, 4, 3] (derivative with
- * respect to the centre atom, divided by std), rij [nloc, nnei, 3]. */
+ * respect to the centre atom, divided by std), rij [nloc, nnei, 3].  As in the
+ * reference, the switching radii are used as floats. */
 void orc_env_mat_a(double* em, double* em_deriv, double* rij,
                    const double* coord_ext, const int* atype_ext,
                    const int* nlist, const double* davg, const double* dstd,

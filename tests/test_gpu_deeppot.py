@@ -1,0 +1,116 @@
+"""GPU: the whole energy / force / virial path (DeepPot) against the
+reference's own outputs:
+
+* the reference PyTorch model on the 64-molecule water box (FP64 plain form,
+  1e-10 relative) and its compressed form (FP64 table);
+* the reference C/C++ API golden case (source/tests/infer/
+  deeppot-testcase.yaml with deeppot_sea.pth: periodic, open boundary and an
+  elongated box);
+* the mixed-precision form against FP64 (force RMSE <= 1e-3 eV/A, the bound
+  the benchmark metric is quoted at);
+* bitwise reproducibility and multi-frame batching.
+"""
+import numpy as np
+import pytest
+
+from conftest import deeppot_sea_params, golden, water_params
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def water_fp64(cuda):
+    from dpgb.deeppot import DeepPot
+
+    return DeepPot(water_params(), "fp64")
+
+
+def test_water192_fp64_matches_reference(water_fp64):
+    g = golden("water192")
+    e, f, v, ae, av = water_fp64.eval(g["coord"].reshape(1, -1), g["box"].reshape(1, 9), g["atype"], atomic=True)
+    assert rel(e, g["energy"]) < 1e-10
+    assert rel(f[0], g["force"]) < 1e-10
+    assert rel(v[0], g["virial"]) < 1e-10
+    assert rel(ae[0], g["atom_energy"]) < 1e-10
+    assert rel(av[0], g["atom_virial"]) < 1e-10
+
+
+def test_deeppot_testcase(cuda):
+    from dpgb.deeppot import DeepPot
+
+    c = golden("deeppot_sea_case")
+    dp = DeepPot(deeppot_sea_params(), "fp64")
+    for b in range(int(c["nblock"])):
+        box = c[f"b{b}_box"]
+        e, f, v, ae, av = dp.eval(c[f"b{b}_coord"], None if box.size == 0 else box, c[f"b{b}_atype"], atomic=True)
+        np.testing.assert_allclose(ae[0], c[f"b{b}_atomic_energy"], rtol=1e-10, atol=1e-10)
+        np.testing.assert_allclose(f[0].reshape(-1), c[f"b{b}_force"], rtol=1e-10, atol=1e-12)
+        np.testing.assert_allclose(av[0].reshape(-1), c[f"b{b}_atomic_virial"], rtol=1e-10, atol=1e-12)
+        np.testing.assert_allclose(e[0], c[f"b{b}_atomic_energy"].sum(), rtol=1e-12)
+
+
+def test_water192_compressed_matches_reference(cuda):
+    from dpgb.deeppot import DeepPot
+
+    g = golden("water192_compressed")
+    w = golden("water192")
+    dp = DeepPot(water_params(compressed=True), "fp64")
+    e, f, v = dp.eval(w["coord"].reshape(1, -1), w["box"].reshape(1, 9), w["atype"])
+    assert rel(e, g["energy"]) < 1e-10
+    assert rel(f[0], g["force"]) < 1e-10
+    assert rel(v[0], g["virial"]) < 1e-10
+
+
+def test_mixed_vs_fp64(cuda, water_fp64):
+    from dpgb import synth
+    from dpgb.deeppot import DeepPot
+
+    coord, atype, box = synth.water_box(8, seed=4)
+    e64, f64, v64 = water_fp64.eval(coord.reshape(1, -1), box, atype)
+    mixed = DeepPot(water_params(), "mixed")
+    e32, f32, v32 = mixed.eval(coord.reshape(1, -1), box, atype)
+    n = atype.shape[0]
+    rmse = float(np.sqrt(np.mean((f32 - f64) ** 2)))
+    assert rmse <= 1e-3
+    assert rmse <= 1e-3 * float(np.sqrt(np.mean(f64 ** 2))) + 1e-9  # also tight relative to |F|
+    assert abs(e32[0] - e64[0]) / n < 1e-5
+    assert rel(v32[0], v64[0]) < 1e-3
+
+
+def test_bitwise_reproducible(water_fp64):
+    g = golden("water192")
+    a = water_fp64.eval(g["coord"].reshape(1, -1), g["box"].reshape(1, 9), g["atype"])
+    b = water_fp64.eval(g["coord"].reshape(1, -1), g["box"].reshape(1, 9), g["atype"])
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_multi_frame_batch(water_fp64):
+    from dpgb import synth
+
+    c1, atype, box = synth.water_box(4, seed=1)
+    c2, _, _ = synth.water_box(4, seed=2)
+    e, f, v = water_fp64.eval(np.stack([c1.reshape(-1), c2.reshape(-1)]), np.stack([box, box]), atype)
+    e1, f1, v1 = water_fp64.eval(c1.reshape(1, -1), box, atype)
+    e2, f2, v2 = water_fp64.eval(c2.reshape(1, -1), box, atype)
+    np.testing.assert_allclose(e, [e1[0], e2[0]], rtol=1e-13)
+    np.testing.assert_allclose(f, np.concatenate([f1, f2]), rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(v, np.concatenate([v1, v2]), rtol=1e-12, atol=1e-15)
+
+
+def test_device_api_matches_host_api(water_fp64):
+    import torch
+
+    g = golden("water192")
+    e, f, v = water_fp64.eval(g["coord"].reshape(1, -1), g["box"].reshape(1, 9), g["atype"])
+    out = water_fp64.eval_device(torch.tensor(g["coord"].reshape(1, -1), device="cuda"), g["box"].reshape(1, 9),
+                                 g["atype"])
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out["energy"].cpu().numpy(), e)
+    np.testing.assert_array_equal(out["force"].cpu().numpy(), f)
+    np.testing.assert_array_equal(out["virial"].cpu().numpy(), v)
