@@ -42,7 +42,7 @@ __global__ void env_mat_a_kernel(double* __restrict__ em, double* __restrict__ e
   if (q >= (long long)nloc * nnei) return;
   const int i = (int)(q / nnei), jj = (int)(q % nnei);
   const int ti = atype[i];
-  const int j = nlist[q];
+  const int j = nlist[q];  // written by the formatter: -1 or a checked index < nall
   double e4[4] = {0, 0, 0, 0}, dv[12], d[3] = {0, 0, 0};
 #pragma unroll
   for (int k = 0; k < 12; ++k) dv[k] = 0.0;
@@ -93,7 +93,8 @@ __global__ void env_mat_pt_kernel(double* __restrict__ em, double* __restrict__ 
   const int f = (int)(row / nloc), i = (int)(row % nloc);
   const double* cf = coord + (size_t)f * nall * 3;
   const int ti = atype[(size_t)f * nall + i];
-  const int j = nlist[q];
+  int j = nlist[q];
+  if (j >= nall) j = -1;  // out-of-range entries are treated as padding, never dereferenced
   double d[3] = {0, 0, 0}, e4[4] = {0, 0, 0, 0}, w = 0.0;
   if (j >= 0) {
 #pragma unroll
@@ -162,7 +163,7 @@ __global__ void frame_keys_kernel(int* __restrict__ keys, const int* __restrict_
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npair) return;
   const int j = nlist[p];
-  keys[p] = j < 0 ? -1 : (int)(j + (p / per_frame) * nall);
+  keys[p] = (j < 0 || j >= nall) ? -1 : (int)(j + (p / per_frame) * nall);
 }
 
 // per-pair virial pv[9] = sum_a nd[a] * rij[d1] * ed[a][d0]

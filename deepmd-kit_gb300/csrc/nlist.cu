@@ -340,7 +340,7 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
 __global__ void __launch_bounds__(kSearchWarps * 32)
 format_nlist_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
                     const int* __restrict__ atype, const int* __restrict__ rows,
-                    const int* __restrict__ counts, int max_nbor, int nloc, float rcut2,
+                    const int* __restrict__ counts, int max_nbor, int nloc, int nall, float rcut2,
                     SelInfo sel, int* __restrict__ status) {
   __shared__ float s_r[kSearchWarps][kCap];
   __shared__ int s_idx[kSearchWarps][kCap];
@@ -353,7 +353,7 @@ format_nlist_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
   const float xi = (float)coord[3 * i], yi = (float)coord[3 * i + 1], zi = (float)coord[3 * i + 2];
   int n = 0;
   bool overflow = false;
-  const int cnt = counts[i];
+  const int cnt = min(counts[i], max_nbor);
   for (int p0 = 0; p0 < cnt; p0 += 32) {
     const int p = p0 + lane;
     bool keep = false;
@@ -361,7 +361,8 @@ format_nlist_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
     int j = -1, tj = -1;
     if (p < cnt) {
       j = rows[(size_t)i * max_nbor + p];
-      tj = atype[j];
+      // an index outside [0, nall) is skipped rather than dereferenced
+      tj = (j >= 0 && j < nall) ? atype[j] : -1;
       if (tj >= 0) {
         const float dx = __fsub_rn((float)coord[3 * j], xi);
         const float dy = __fsub_rn((float)coord[3 * j + 1], yi);
@@ -435,23 +436,22 @@ __global__ void scan_kernel(int* __restrict__ out, const int* __restrict__ in, i
 }
 
 // transpose: count, fill, then sort every bucket by pair id
+// keys outside [0, nkeys) (padding -1 or a bad index) take no part
 __global__ void tr_count_kernel(int* __restrict__ counts, const int* __restrict__ keys, long long npair,
-                                int mod) {
+                                int nkeys) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npair) return;
-  int k = keys[p];
-  if (k < 0) return;
-  if (mod > 0) k %= mod;
+  const int k = keys[p];
+  if (k < 0 || k >= nkeys) return;
   atomicAdd(&counts[k], 1);
 }
 __global__ void tr_fill_kernel(int* __restrict__ pairs, int* __restrict__ cursor,
                                const int* __restrict__ offsets, const int* __restrict__ keys,
-                               long long npair, int mod) {
+                               long long npair, int nkeys) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npair) return;
-  int k = keys[p];
-  if (k < 0) return;
-  if (mod > 0) k %= mod;
+  const int k = keys[p];
+  if (k < 0 || k >= nkeys) return;
   pairs[offsets[k] + atomicAdd(&cursor[k], 1)] = (int)p;
 }
 constexpr int kTrCap = 2048;
@@ -533,13 +533,13 @@ int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc,
   return check_launch("nlist_pt");
 }
 
-int launch_format_nlist(int* nlist, const double* coord, const int* atype, const int* rows,
+int launch_format_nlist(int* nlist, const double* coord, const int* atype, const int* rows, int nall,
                         const int* counts, int max_nbor, int nloc, double rcut, const SelInfo& sel,
                         int* status, cudaStream_t st) {
   if (nloc <= 0) return DPGB_OK;
   const float rc = (float)rcut;
   format_nlist_kernel<<<ceil_div(nloc, kSearchWarps), kSearchWarps * 32, 0, st>>>(
-      nlist, coord, atype, rows, counts, max_nbor, nloc, rc * rc, sel, status);
+      nlist, coord, atype, rows, counts, max_nbor, nloc, nall, rc * rc, sel, status);
   return check_launch("format_nlist");
 }
 
@@ -556,15 +556,16 @@ int launch_transpose(Transpose& tr, const int* keys, long long npair, int nkeys,
   tr.nkeys = nkeys;
   DPGB_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (nkeys + 1), st));
   DPGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * (nkeys + 1), st));
+  (void)mod;
   if (npair > 0) {
-    tr_count_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(counts, keys, npair, mod);
+    tr_count_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(counts, keys, npair, nkeys);
     DPGB_TRY(check_launch("transpose_count"));
   }
   scan_kernel<<<1, 1024, 0, st>>>(tr.offsets, counts, nkeys);
   DPGB_TRY(check_launch("transpose_scan"));
   if (npair > 0) {
     tr_fill_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(tr.pairs, cursor, tr.offsets, keys, npair,
-                                                          mod);
+                                                          nkeys);
     DPGB_TRY(check_launch("transpose_fill"));
     tr_sort_kernel<<<nkeys, 128, 0, st>>>(tr.pairs, tr.offsets, nkeys, status);
     DPGB_TRY(check_launch("transpose_sort"));
@@ -674,7 +675,7 @@ int dpgb_format_nlist_a(int* nlist, const double* coord, const int* atype, const
   DPGB_TRY(ws.alloc(sizeof(int) * kStatusSlots));
   int* status = ws.as<int>();
   DPGB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * kStatusSlots, st));
-  DPGB_TRY(launch_format_nlist(nlist, coord, atype, rows, counts, max_nbor, nloc, rcut, sel, status, st));
+  DPGB_TRY(launch_format_nlist(nlist, coord, atype, rows, nall, counts, max_nbor, nloc, rcut, sel, status, st));
   int h[kStatusSlots];
   DPGB_TRY(read_status(status, st, h));
   if (overflow_host) *overflow_host = h[kStatusDropped];

@@ -55,7 +55,7 @@ size_t nlist_pt_workspace(int nloc, const CellGeom& g);
 int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc, const CellGeom& g,
                     const int* shift_pos_dev, const double* svec_dev, double rcut,
                     const SelInfo& sel, void* workspace, int* status, cudaStream_t st);
-int launch_format_nlist(int* nlist, const double* coord, const int* atype, const int* rows,
+int launch_format_nlist(int* nlist, const double* coord, const int* atype, const int* rows, int nall,
                         const int* counts, int max_nbor, int nloc, double rcut, const SelInfo& sel,
                         int* status, cudaStream_t st);
 size_t transpose_workspace(long long npair, int nkeys);

@@ -142,7 +142,11 @@ def format_nlist_a(coord_ext: torch.Tensor, atype_ext: torch.Tensor, rows: torch
     sel_a = np.ascontiguousarray(sel, np.int32)
     out = torch.empty(nloc, int(sel_a.sum()), dtype=torch.int32, device=coord_ext.device)
     ov = np.zeros(1, np.int32)
-    _lib.call("dpgb_format_nlist_a", _vp(out), _vp(coord_ext.contiguous()), _vp(atype_ext.to(torch.int32).contiguous()),
-              _vp(rows.to(torch.int32).contiguous()), _vp(counts.to(torch.int32).contiguous()), rows.shape[1], nloc,
-              coord_ext.reshape(-1, 3).shape[0], C.c_double(rcut), _ip(sel_a), len(sel_a), _ip(ov), _stream())
+    # converted copies must stay referenced until the call returns
+    c = coord_ext.contiguous()
+    t = atype_ext.to(torch.int32).contiguous()
+    r = rows.to(torch.int32).contiguous()
+    n = counts.to(torch.int32).contiguous()
+    _lib.call("dpgb_format_nlist_a", _vp(out), _vp(c), _vp(t), _vp(r), _vp(n), r.shape[1], nloc,
+              c.reshape(-1, 3).shape[0], C.c_double(rcut), _ip(sel_a), len(sel_a), _ip(ov), _stream())
     return out, int(ov[0])

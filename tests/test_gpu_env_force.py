@@ -46,9 +46,13 @@ def test_prod_env_mat_a_golden(cuda):
     nl = torch.empty(nloc, nnei, dtype=torch.int32, device=cuda)
     avg = torch.zeros(2, nnei, 4, dtype=torch.float64, device=cuda)
     std = torch.ones(2, nnei, 4, dtype=torch.float64, device=cuda)
+    # every device buffer is bound to a name for the duration of the call
     rows = _t(g["rows"], cuda, torch.int32)
-    _lib.call("dpgb_prod_env_mat_a_f64", _vp(em), _vp(der), _vp(rij), _vp(nl), _vp(_t(g["coord_ext"], cuda)),
-              _vp(_t(g["atype_ext"], cuda, torch.int32)), _vp(rows), _vp(_t(g["counts"], cuda, torch.int32)),
+    cext = _t(g["coord_ext"], cuda)
+    text = _t(g["atype_ext"], cuda, torch.int32)
+    counts = _t(g["counts"], cuda, torch.int32)
+    _lib.call("dpgb_prod_env_mat_a_f64", _vp(em), _vp(der), _vp(rij), _vp(nl), _vp(cext),
+              _vp(text), _vp(rows), _vp(counts),
               rows.shape[1], _vp(avg), _vp(std), nloc, nall, ctypes.c_double(float(g["rc"])),
               ctypes.c_double(float(g["rc_smth"])), sel.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), 2, _stream())
     torch.cuda.synchronize()
@@ -89,8 +93,10 @@ def test_prod_force_virial_golden(cuda):
     g = golden("prod_virial_a")
     v = torch.empty(9, dtype=torch.float64, device=cuda)
     av = torch.empty(nall, 9, dtype=torch.float64, device=cuda)
-    _lib.call("dpgb_prod_virial_a_f64", _vp(v), _vp(av), _vp(_t(g["net_deriv"], cuda)), _vp(_t(g["em_deriv"], cuda)),
-              _vp(_t(g["rij"], cuda)), _vp(_t(g["nlist"], cuda, torch.int32)), nloc, nall, nnei, _stream())
+    vnd, ved, vrij = _t(g["net_deriv"], cuda), _t(g["em_deriv"], cuda), _t(g["rij"], cuda)
+    vnl = _t(g["nlist"], cuda, torch.int32)
+    _lib.call("dpgb_prod_virial_a_f64", _vp(v), _vp(av), _vp(vnd), _vp(ved), _vp(vrij), _vp(vnl), nloc, nall, nnei,
+              _stream())
     np.testing.assert_allclose(v.cpu().numpy(), g["expected_virial"], atol=1e-5)
     np.testing.assert_allclose(av.cpu().numpy().reshape(-1), g["expected_atom_virial"], atol=1e-5)
 
@@ -109,11 +115,13 @@ def test_prod_force_deterministic_and_grads(cuda):
     rng = np.random.default_rng(2)
     grad = rng.normal(size=(nloc, 3))
     out = torch.empty(nloc, 4 * nnei, dtype=torch.float64, device=cuda)
-    _lib.call("dpgb_prod_force_grad_a_f64", _vp(out), _vp(_t(grad, cuda)), _vp(ed), _vp(nl), nloc, nnei, 1, _stream())
+    grad_d = _t(grad, cuda)
+    _lib.call("dpgb_prod_force_grad_a_f64", _vp(out), _vp(grad_d), _vp(ed), _vp(nl), nloc, nnei, 1, _stream())
     np.testing.assert_allclose(out.cpu().numpy(), O.prod_force_grad_a(grad, g["em_deriv"], g["nlist"]), atol=1e-12)
     gv = rng.normal(size=9)
     out2 = torch.empty(nloc, 4 * nnei, dtype=torch.float64, device=cuda)
-    _lib.call("dpgb_prod_virial_grad_a_f64", _vp(out2), _vp(_t(gv, cuda)), _vp(ed), _vp(_t(g["rij"], cuda)), _vp(nl),
+    gv_d, rij_d = _t(gv, cuda), _t(g["rij"], cuda)
+    _lib.call("dpgb_prod_virial_grad_a_f64", _vp(out2), _vp(gv_d), _vp(ed), _vp(rij_d), _vp(nl),
               nloc, nnei, _stream())
     np.testing.assert_allclose(out2.cpu().numpy(), O.prod_virial_grad_a(gv, g["em_deriv"], g["rij"], g["nlist"]),
                                atol=1e-12)
@@ -136,8 +144,8 @@ def test_env_mat_pt_matches_reference_model(cuda):
     at = np.tile(g["atype"], nall // 192).astype(np.int32)
     import ctypes
 
-    _lib.call("dpgb_env_mat_pt_f64", _vp(em), _vp(diff), _vp(sw), _vp(_t(g["coord_ext"], cuda)),
-              _vp(_t(at, cuda, torch.int32)), _vp(_t(g["nlist"], cuda, torch.int32)), _vp(avg), _vp(std), 1, 192,
+    cext, at_d, nl_d = _t(g["coord_ext"], cuda), _t(at, cuda, torch.int32), _t(g["nlist"], cuda, torch.int32)
+    _lib.call("dpgb_env_mat_pt_f64", _vp(em), _vp(diff), _vp(sw), _vp(cext), _vp(at_d), _vp(nl_d), _vp(avg), _vp(std), 1, 192,
               nall, nnei, ctypes.c_double(6.0), ctypes.c_double(0.5), _stream())
     np.testing.assert_allclose(em.cpu().numpy()[:8], g["env_mat"], rtol=1e-12, atol=1e-14)
     np.testing.assert_allclose(sw.cpu().numpy()[:8], g["sw"], rtol=1e-12, atol=1e-14)
