@@ -80,6 +80,7 @@ _SIGS = {
     "dpgb_prod_virial_a_f64": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _P],
     "dpgb_prod_force_grad_a_f64": [_P, _P, _P, _P, _I, _I, _I, _P],
     "dpgb_prod_virial_grad_a_f64": [_P, _P, _P, _P, _P, _I, _I, _P],
+    "dpgb_tc_gemm_bf16": [_P, _P, _P, _I, _I, _I, _P],
     "dpgb_deeppot_new": [C.POINTER(SeADesc), _I],
     "dpgb_deeppot_delete": [_P],
     "dpgb_deeppot_check_ok": [_P],

@@ -185,6 +185,15 @@ int dpgb_prod_virial_grad_a_f64(double* grad_net, const double* grad,
                                 void* stream);
 
 /* ------------------------------------------------------------------------
+ * Plain tensor-core GEMM (no counterpart in the reference, whose kernels use
+ * no tensor cores): D[M,N] (FP32, row-major) = A[M,K] . B[K,N] with A BF16
+ * row-major and B given as Bt [N,K] BF16 row-major.  tcgen05.mma with TMEM
+ * accumulators; N in 16..256 (multiple of 16), K a multiple of 16; device
+ * pointers; synchronises the stream. */
+int dpgb_tc_gemm_bf16(float* D, const void* A, const void* Bt, int M, int N,
+                      int K, void* stream);
+
+/* ------------------------------------------------------------------------
  * DeepPot: the whole se_e2_a energy / force / virial evaluation.
  * Mirrors the C API DP_NewDeepPot / DP_DeepPotCompute / DP_DeepPotComputeNList
  * (source/api_c/include/c_api.h:150,244-322) and the backend method
