@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "emb_tc.cuh"
 #include "se_a.cuh"
 
 namespace dpgb {
@@ -66,7 +67,9 @@ __global__ void force_gather_model_kernel(double* __restrict__ force, double* __
   if (row >= nrows) return;
   double f[3] = {0, 0, 0};
   const T* gr = g + (size_t)row * nnei * 3;
+  const int* nr = nlist + (size_t)row * nnei;
   for (int s = 0; s < nnei; ++s) {
+    if (nr[s] < 0) continue;  // padding slots carry no force (and may be unwritten)
     f[0] += (double)gr[3 * s];
     f[1] += (double)gr[3 * s + 1];
     f[2] += (double)gr[3 * s + 2];
@@ -153,7 +156,12 @@ struct DeepPotImpl {
   std::vector<int> atype_cache;
   std::vector<int> row_pos_h, type_count, type_off;
   int cached_nframes = -1;
-  DeviceBuffer row_pos_dev, atype_dev;
+  DeviceBuffer row_pos_dev, atype_dev, sorted_rows_dev, chunks_dev;
+  int nchunks = 0;
+  // tensor-core embedding (mixed precision)
+  int use_tc = 0;
+  EmbTC tc{};
+  DeviceBuffer tc_images, tc_vec, ws_runlen, ws_dxyz;
   // workspace
   DeviceBuffer ws_nlist, ws_cell, ws_tr, ws_keys, ws_status, ws_coord, ws_svec, ws_spos;
   DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf;
@@ -336,13 +344,37 @@ int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host
     for (int f = 0; f < nframes; ++f)
       for (int i = 0; i < natom; ++i)
         if (atype_host[i] == t) dp.row_pos_h[(size_t)f * natom + i] = cur[t]++;
-  const int nvirt = natom * nframes - dp.type_off[nt];
-  (void)nvirt;
+  // inverse map (sorted position -> row) of the typed rows
+  const int nsorted = dp.type_off[nt];
+  std::vector<int> sorted_rows((size_t)std::max(nsorted, 1), 0);
+  for (int f = 0; f < nframes; ++f)
+    for (int i = 0; i < natom; ++i)
+      if (atype_host[i] >= 0) sorted_rows[dp.row_pos_h[(size_t)f * natom + i]] = f * natom + i;
+  // work chunks of the tensor-core embedding: contiguous sorted rows of one
+  // centre type, about two chunks per SM
+  std::vector<WorkChunk> chunks;
+  {
+    int dev = 0, nsm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int target = std::max(1, nsorted / std::max(1, 2 * nsm));
+    for (int t = 0; t < nt; ++t)
+      for (int r = dp.type_off[t]; r < dp.type_off[t + 1]; r += target)
+        chunks.push_back(WorkChunk{r, std::min(r + target, dp.type_off[t + 1]), t, 0});
+  }
+  dp.nchunks = (int)chunks.size();
   DPGB_TRY(dp.row_pos_dev.alloc(sizeof(int) * dp.row_pos_h.size()));
   DPGB_TRY(dp.atype_dev.alloc(sizeof(int) * natom));
+  DPGB_TRY(dp.sorted_rows_dev.alloc(sizeof(int) * sorted_rows.size()));
+  DPGB_TRY(dp.chunks_dev.alloc(sizeof(WorkChunk) * std::max<size_t>(chunks.size(), 1)));
   DPGB_CUDA(cudaMemcpyAsync(dp.row_pos_dev.ptr, dp.row_pos_h.data(), sizeof(int) * dp.row_pos_h.size(),
                             cudaMemcpyHostToDevice, st));
   DPGB_CUDA(cudaMemcpyAsync(dp.atype_dev.ptr, atype_host, sizeof(int) * natom, cudaMemcpyHostToDevice, st));
+  DPGB_CUDA(cudaMemcpyAsync(dp.sorted_rows_dev.ptr, sorted_rows.data(), sizeof(int) * sorted_rows.size(),
+                            cudaMemcpyHostToDevice, st));
+  if (!chunks.empty())
+    DPGB_CUDA(cudaMemcpyAsync(dp.chunks_dev.ptr, chunks.data(), sizeof(WorkChunk) * chunks.size(),
+                              cudaMemcpyHostToDevice, st));
   DPGB_CUDA(cudaStreamSynchronize(st));  // host vectors may change on the next call
   dp.cached_nframes = nframes;
   return DPGB_OK;
@@ -494,9 +526,25 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   p.row_pos = dp.row_pos_dev.as<int>();
   // virtual rows have no sorted position: point them at row 0 only for
   // reading (the kernels never write a virtual row)
+  bool tc_path = false;
+  if constexpr (std::is_same<T, float>::value) tc_path = dp.use_tc != 0;
   dp.mark(DPGB_STAGE_DESC_FWD, 0, st);
-  DPGB_TRY(launch_desc_fwd<T>(p, m.emb, dp.ws_D.as<T>(), dp.ws_xyz.as<T>(), desc_fwd_smem<T>(p, m.emb), st));
-  ++launches;
+  if constexpr (std::is_same<T, float>::value) {
+    if (tc_path) {
+      const int nsorted = dp.type_off[d.ntypes];
+      DPGB_TRY(dp.ws_runlen.alloc(sizeof(int) * (size_t)std::max(nsorted, 1) * d.ntypes));
+      DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ng));
+      DPGB_TRY(launch_run_lengths(dp.ws_runlen.as<int>(), nlist, dp.sorted_rows_dev.as<int>(), nsorted, nnei, dp.sel,
+                                  dp.pad_zero, st));
+      DPGB_TRY(launch_emb_tc_fwd(p, dp.tc, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.ws_runlen.as<int>(),
+                                 dp.sorted_rows_dev.as<int>(), dp.ws_xyz.as<float>(), dp.ws_D.as<float>(), status, st));
+      launches += 2;
+    }
+  }
+  if (!tc_path) {
+    DPGB_TRY(launch_desc_fwd<T>(p, m.emb, dp.ws_D.as<T>(), dp.ws_xyz.as<T>(), desc_fwd_smem<T>(p, m.emb), st));
+    ++launches;
+  }
   dp.mark(DPGB_STAGE_DESC_FWD, 1, st);
   dp.mark(DPGB_STAGE_FITTING, 0, st);
   for (int t = 0; t < d.ntypes; ++t) {
@@ -508,9 +556,22 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   }
   dp.mark(DPGB_STAGE_FITTING, 1, st);
   dp.mark(DPGB_STAGE_DESC_BWD, 0, st);
-  DPGB_TRY(launch_desc_bwd<T>(p, m.emb, dp.ws_dD.as<T>(), dp.ws_xyz.as<T>(), dp.ws_g.as<T>(), dp.ws_vir.as<double>(),
-                              desc_bwd_smem<T>(p, m.emb), st));
-  ++launches;
+  if constexpr (std::is_same<T, float>::value) {
+    if (tc_path) {
+      // rows of virtual atoms are never visited by the tile kernels
+      DPGB_CUDA(cudaMemsetAsync(dp.ws_vir.ptr, 0, sizeof(double) * nrows * 9, st));
+      DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
+      DPGB_TRY(launch_emb_tc_bwd(p, dp.tc, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.ws_runlen.as<int>(),
+                                 dp.sorted_rows_dev.as<int>(), dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(),
+                                 dp.ws_vir.as<double>(), status, st));
+      launches += 2;
+    }
+  }
+  if (!tc_path) {
+    DPGB_TRY(launch_desc_bwd<T>(p, m.emb, dp.ws_dD.as<T>(), dp.ws_xyz.as<T>(), dp.ws_g.as<T>(), dp.ws_vir.as<double>(),
+                                desc_bwd_smem<T>(p, m.emb), st));
+    ++launches;
+  }
   dp.mark(DPGB_STAGE_DESC_BWD, 1, st);
   dp.mark(DPGB_STAGE_REDUCE, 0, st);
   force_gather_model_kernel<T><<<ceil_div(nrows, 128), 128, 0, st>>>(
@@ -596,6 +657,21 @@ dpgb_deeppot* dpgb_deeppot_new(const dpgb_se_a_desc* desc, int precision) {
   } else {
     im.m32.reset(new DevModel<float>());
     if (build_dev_model<float>(im, *im.m32) != DPGB_OK) return nullptr;
+    const char* no_tc = getenv("DPGB_NO_TENSOR_CORES");
+    if (emb_tc_eligible(*desc) && !(no_tc && no_tc[0] == '1')) {
+      std::vector<unsigned char> img;
+      std::vector<float> vec;
+      if (build_emb_tc(*desc, img, im.tc, vec) != DPGB_OK) return nullptr;
+      if (im.tc_images.alloc(img.size()) != DPGB_OK || im.tc_vec.alloc(sizeof(float) * vec.size()) != DPGB_OK)
+        return nullptr;
+      if (cudaMemcpy(im.tc_images.ptr, img.data(), img.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+          cudaMemcpy(im.tc_vec.ptr, vec.data(), sizeof(float) * vec.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        fail(DPGB_ECUDA, "tensor-core weight upload failed");
+        return nullptr;
+      }
+      emb_tc_bind(im.tc, im.tc_images.as<unsigned char>(), 0, im.tc_vec.as<float>());
+      im.use_tc = 1;
+    }
   }
   // the host pointers of the description are not kept
   for (int e = 0; e < DPGB_MAX_TYPES * DPGB_MAX_TYPES; ++e) {

@@ -1,0 +1,857 @@
+// Tensor-core se_e2_a embedding (mixed precision): the two dense layers of
+// the 1 -> w1 -> w2 -> w3 embedding net (and their input-gradient products in
+// the backward pass) run as tcgen05.mma with BF16 operands in shared memory
+// and FP32 accumulators in TMEM; the tanh epilogues, the per-atom contraction
+// xyz = sum_j R~_j^T G_j and the force products run on the CUDA cores in
+// FP32.  G itself is never rounded to BF16: it is formed in FP32 from the
+// FP32 accumulator and contracted in FP32.
+//
+// Work decomposition: a persistent CTA owns contiguous ranges of type-sorted
+// atoms of one centre type.  For each neighbour-type section it packs whole
+// per-atom runs of active slots into tiles of up to 128 pairs (= the 128 TMEM
+// lanes / MMA rows) and at most 16 atoms, so every atom's xyz and virial are
+// accumulated by one CTA in a fixed order: no atomics, bitwise reproducible.
+// Semantics follow deepmd/pt/model/descriptor/se_a.py:742-858 and
+// env_mat.py:18-119 (padding slots hold (0 - avg)/std and go through the net
+// unless avg == 0; excluded pairs contribute zero).
+#include <cstring>
+#include <vector>
+
+#include "emb_tc.cuh"
+#include "tc.cuh"
+
+namespace dpgb {
+
+static inline int pad16(int x) { return (x + 15) / 16 * 16; }
+
+int emb_tc_eligible(const dpgb_se_a_desc& d) {
+  if (d.compressed || d.n_emb != 3) return 0;
+  const int w1 = d.emb_neuron[0], w2 = d.emb_neuron[1], w3 = d.emb_neuron[2];
+  const bool shape_a = (w1 == 25 && w2 == 50 && w3 == 100);
+  const bool shape_b = (w1 == 3 && w2 == 6 && w3 == 12);
+  if (!shape_a && !shape_b) return 0;
+  for (int t = 0; t < d.ntypes; ++t)
+    if (d.sel[t] > kTcRows) return 0;
+  return 1;
+}
+
+size_t emb_tc_image_bytes(const EmbTC& m, int kind) {
+  switch (kind) {
+    case 0: return (size_t)m.n2 * m.k1 * 2;
+    case 1: return (size_t)m.n3 * m.n2 * 2;
+    case 2: return (size_t)m.n2 * m.n3 * 2;
+    default: return (size_t)m.k1 * m.n2 * 2;
+  }
+}
+
+static void put_bf16(std::vector<unsigned char>& img, size_t base, int r, int k, int K, float v) {
+  const __nv_bfloat16 b = __float2bfloat16_rn(v);
+  std::memcpy(img.data() + base + tc::cm_offset(r, k, K), &b, 2);
+}
+
+int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, EmbTC& m, std::vector<float>& vec) {
+  const int nnets = d.type_one_side ? d.ntypes : d.ntypes * d.ntypes;
+  m.w1 = d.emb_neuron[0];
+  m.w2 = d.emb_neuron[1];
+  m.w3 = d.emb_neuron[2];
+  m.k1 = pad16(m.w1);
+  m.n2 = pad16(m.w2);
+  m.n3 = pad16(m.w3);
+  m.nnets = nnets;
+  m.vec_stride = 3 * m.k1 + 2 * m.n2 + 2 * m.n3;
+  size_t per[4];
+  for (int k = 0; k < 4; ++k) per[k] = emb_tc_image_bytes(m, k);
+  images.assign((per[0] + per[1] + per[2] + per[3]) * nnets, 0);
+  vec.assign((size_t)m.vec_stride * nnets, 0.f);
+  m.has_idt1 = m.has_idt2 = m.has_idt3 = 0;
+  for (int e = 0; e < nnets; ++e) {
+    const double* W1 = d.emb_w[e][0];  // [1, w1]
+    const double* W2 = d.emb_w[e][1];  // [w1, w2]
+    const double* W3 = d.emb_w[e][2];  // [w2, w3]
+    if (!W1 || !W2 || !W3 || !d.emb_b[e][0] || !d.emb_b[e][1] || !d.emb_b[e][2]) return fail(DPGB_EINVAL, "missing embedding weights");
+    const size_t b0 = per[0] * e, b1 = per[0] * nnets + per[1] * e, b2 = (per[0] + per[1]) * nnets + per[2] * e,
+                 b3 = (per[0] + per[1] + per[2]) * nnets + per[3] * e;
+    for (int o = 0; o < m.w2; ++o)
+      for (int k = 0; k < m.w1; ++k) {
+        put_bf16(images, b0, o, k, m.k1, (float)W2[(size_t)k * m.w2 + o]);  // W2^T [n2 x k1]
+        put_bf16(images, b3, k, o, m.n2, (float)W2[(size_t)k * m.w2 + o]);  // W2 [k1 x n2]
+      }
+    for (int o = 0; o < m.w3; ++o)
+      for (int k = 0; k < m.w2; ++k) {
+        put_bf16(images, b1, o, k, m.n2, (float)W3[(size_t)k * m.w3 + o]);  // W3^T [n3 x n2]
+        put_bf16(images, b2, k, o, m.n3, (float)W3[(size_t)k * m.w3 + o]);  // W3 [n2 x n3]
+      }
+    float* v = vec.data() + (size_t)m.vec_stride * e;
+    for (int k = 0; k < m.w1; ++k) {
+      v[k] = (float)W1[k];
+      v[m.k1 + k] = (float)d.emb_b[e][0][k];
+      v[2 * m.k1 + k] = d.emb_idt[e][0] ? (float)d.emb_idt[e][0][k] : 1.f;
+    }
+    float* v2 = v + 3 * m.k1;
+    for (int o = 0; o < m.w2; ++o) {
+      v2[o] = (float)d.emb_b[e][1][o];
+      v2[m.n2 + o] = d.emb_idt[e][1] ? (float)d.emb_idt[e][1][o] : 1.f;
+    }
+    float* v3 = v2 + 2 * m.n2;
+    for (int o = 0; o < m.w3; ++o) {
+      v3[o] = (float)d.emb_b[e][2][o];
+      v3[m.n3 + o] = d.emb_idt[e][2] ? (float)d.emb_idt[e][2][o] : 1.f;
+    }
+    m.has_idt1 |= d.emb_idt[e][0] != nullptr;
+    m.has_idt2 |= d.emb_idt[e][1] != nullptr;
+    m.has_idt3 |= d.emb_idt[e][2] != nullptr;
+  }
+  return DPGB_OK;
+}
+
+void emb_tc_bind(EmbTC& m, const unsigned char* dev, size_t, const float* dev_vec) {
+  const size_t p0 = emb_tc_image_bytes(m, 0) * m.nnets, p1 = emb_tc_image_bytes(m, 1) * m.nnets,
+               p2 = emb_tc_image_bytes(m, 2) * m.nnets;
+  m.fw2 = dev;
+  m.fw3 = dev + p0;
+  m.bw3 = dev + p0 + p1;
+  m.bw2 = dev + p0 + p1 + p2;
+  m.vec = dev_vec;
+}
+
+namespace {
+
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// copy a net's weight image (bytes multiple of 16) into shared memory
+__device__ __forceinline__ void copy16(unsigned char* dst, const unsigned char* src, int bytes) {
+  for (int q = threadIdx.x; q < bytes / 16; q += blockDim.x)
+    reinterpret_cast<uint4*>(dst)[q] = reinterpret_cast<const uint4*>(src)[q];
+}
+
+// store 8 consecutive bf16 values of row r, columns k0..k0+7, in the
+// core-matrix layout of a tile with K columns
+__device__ __forceinline__ void store8(unsigned char* base, int r, int k0, int K, const float* v) {
+  __nv_bfloat162 h[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+  *reinterpret_cast<uint4*>(base + tc::cm_offset(r, k0, K)) = *reinterpret_cast<uint4*>(h);
+}
+
+template <int K1, int N>
+__device__ __forceinline__ void issue_mma(uint32_t d_tmem, uint32_t a_s, uint32_t b_s, int kdim) {
+  const uint32_t idesc = tc::idesc_bf16_f32(128, N);
+  const uint32_t sbo = (uint32_t)(kdim / 8) * 128;
+  for (int ks = 0; ks < kdim / 16; ++ks)
+    tc::mma_bf16(d_tmem, tc::smem_desc(a_s + ks * 256, 128, sbo), tc::smem_desc(b_s + ks * 256, 128, sbo), idesc,
+                 ks > 0 ? 1u : 0u);
+}
+
+// Environment of the tile's pair p: fills Rn (normalised), d (displacement,
+// FP32 after the FP64 subtraction), the slot index and flags.
+struct PairInfo {
+  int row, slot, nb, keep, valid, k;
+};
+
+__device__ __forceinline__ void pair_env(const DescParams<float>& p, int t, int ti, const int* s_row,
+                                         const int* s_off, int ntile, int pp, PairInfo& pi, float rn[4],
+                                         float dvec[3]) {
+  pi.valid = pp < s_off[ntile];
+  rn[0] = rn[1] = rn[2] = rn[3] = 0.f;
+  dvec[0] = dvec[1] = dvec[2] = 0.f;
+  pi.nb = -1;
+  pi.keep = 0;
+  pi.k = 0;
+  pi.row = 0;
+  pi.slot = 0;
+  if (!pi.valid) return;
+  int k = 0;
+  while (k + 1 < ntile && s_off[k + 1] <= pp) ++k;
+  pi.k = k;
+  pi.row = s_row[k];
+  pi.slot = p.sec[t] + (pp - s_off[k]);
+  const int f = pi.row / p.nloc, i = pi.row - f * p.nloc;
+  pi.nb = p.nlist[(size_t)pi.row * p.nnei + pi.slot];
+  const float* av = p.davg + ((size_t)ti * p.nnei + pi.slot) * 4;
+  const float* sd = p.dstd + ((size_t)ti * p.nnei + pi.slot) * 4;
+  float e4[4] = {0.f, 0.f, 0.f, 0.f};
+  if (pi.nb >= 0) {
+    const double* cf = p.coord + (size_t)f * p.nloc * 3;
+    const int s = pi.nb / p.nloc, jj = pi.nb - s * p.nloc;
+    const double* sv = p.svec + ((size_t)f * p.nshift + s) * 3;
+    const double dx = (cf[3 * jj] + sv[0]) - cf[3 * i];
+    const double dy = (cf[3 * jj + 1] + sv[1]) - cf[3 * i + 1];
+    const double dz = (cf[3 * jj + 2] + sv[2]) - cf[3 * i + 2];
+    dvec[0] = (float)dx;
+    dvec[1] = (float)dy;
+    dvec[2] = (float)dz;
+    pi.keep = p.pair_mask ? p.pair_mask[ti * p.ntypes + p.atype[jj]] : 1;
+    if (pi.keep) {
+      const float nr2 = dvec[0] * dvec[0] + dvec[1] * dvec[1] + dvec[2] * dvec[2];
+      const float nr = sqrtf(nr2);
+      const float inr = 1.f / nr;
+      const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
+      float sw;
+      if (nr < rmin) {
+        sw = 1.f;
+      } else if (nr < rmax) {
+        const float uu = (nr - rmin) / (rmax - rmin);
+        sw = uu * uu * uu * (-6.f * uu * uu + 15.f * uu - 10.f) + 1.f;
+      } else {
+        sw = 0.f;
+      }
+      const float inr2 = inr * inr;
+      e4[0] = inr * sw;
+      e4[1] = dvec[0] * inr2 * sw;
+      e4[2] = dvec[1] * inr2 * sw;
+      e4[3] = dvec[2] * inr2 * sw;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) rn[c] = (pi.nb >= 0 && !pi.keep) ? 0.f : (e4[c] - av[c]) / sd[c];
+}
+
+// d R~ / d r_centre of a kept pair (env_mat.cc:156-216), FP32
+__device__ __forceinline__ void env_deriv(const float d[3], float rmin, float rmax, float der[12]) {
+  const float nr2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  const float nr = sqrtf(nr2);
+  const float inr = 1.f / nr;
+  float sw, dsw;
+  if (nr < rmin) {
+    sw = 1.f;
+    dsw = 0.f;
+  } else if (nr < rmax) {
+    const float du = 1.f / (rmax - rmin);
+    const float uu = (nr - rmin) * du;
+    const float poly = -6.f * uu * uu + 15.f * uu - 10.f;
+    sw = uu * uu * uu * poly + 1.f;
+    dsw = (3.f * uu * uu * poly + uu * uu * uu * (-12.f * uu + 15.f)) * du;
+  } else {
+    sw = 0.f;
+    dsw = 0.f;
+  }
+  const float inr2 = inr * inr, inr3 = inr2 * inr, inr4 = inr2 * inr2;
+  const float v0 = inr;
+  const float v[3] = {d[0] * inr2, d[1] * inr2, d[2] * inr2};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) der[k] = d[k] * inr3 * sw - v0 * dsw * d[k] * inr;
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      der[3 + 3 * c + k] = (2.f * d[c] * d[k] * inr4 - (c == k ? inr2 : 0.f)) * sw - v[c] * dsw * d[k] * inr;
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory plan (bytes), identical for forward and backward where shared
+template <int W1, int W2, int W3>
+struct Plan {
+  static constexpr int K1 = (W1 + 15) / 16 * 16, N2 = (W2 + 15) / 16 * 16, N3 = (W3 + 15) / 16 * 16;
+  static constexpr int LDG = W3 + 1;  // fp32 G row stride (odd: no bank conflicts)
+  static constexpr int VEC = 3 * K1 + 2 * N2 + 2 * N3;
+  static constexpr int fw2 = 0;
+  static constexpr int fw3 = fw2 + N2 * K1 * 2;
+  static constexpr int bw3 = fw3 + N3 * N2 * 2;
+  static constexpr int bw2 = bw3 + N2 * N3 * 2;
+  static constexpr int a1 = bw2 + K1 * N2 * 2;
+  static constexpr int a2 = a1 + 128 * K1 * 2;
+  static constexpr int a3 = a2 + 128 * N2 * 2;           // backward dP3 operand
+  static constexpr int gbuf = a3 + 128 * N3 * 2;         // forward G (fp32) / backward dxyz of tile atoms
+  static constexpr int gbytes_f = 128 * LDG * 4;
+  static constexpr int gbytes_b = kTcMaxAtoms * 4 * W3 * 4;
+  static constexpr int rn = gbuf + (gbytes_f > gbytes_b ? gbytes_f : gbytes_b);
+  static constexpr int vec = rn + 128 * 4 * 4;
+  static constexpr int vir = vec + VEC * 4;                // backward per-pair virial (double)
+  static constexpr int total = vir + 128 * 9 * 8;
+  static constexpr int tmem_cols = (N2 + N3 <= 256) ? 256 : 512;
+};
+
+template <int W1, int W2, int W3>
+__global__ void __launch_bounds__(128, 1)
+emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ chunks, int nchunks,
+                  const int* __restrict__ run_len, const int* __restrict__ sorted_rows, float* __restrict__ xyz,
+                  float* __restrict__ Dout, int* __restrict__ status) {
+  using P = Plan<W1, W2, W3>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_row[kTcMaxAtoms], s_off[kTcMaxAtoms + 1], s_ntile, s_cursor;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int ng = p.ng;
+  if (warp == 0) tc::tmem_alloc(&s_tmem, P::tmem_cols);
+  if (tid == 0) tc::mbar_init(&bar, 1);
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tbase = s_tmem;
+  uint32_t phase = 0;
+  bool alive = true;
+  float* sG = reinterpret_cast<float*>(smem + P::gbuf);
+  float* sRn = reinterpret_cast<float*>(smem + P::rn);
+  float* sV = reinterpret_cast<float*>(smem + P::vec);
+  const uint32_t sA1 = tc::smem_u32(smem + P::a1), sA2 = tc::smem_u32(smem + P::a2);
+  const uint32_t sW2 = tc::smem_u32(smem + P::fw2), sW3 = tc::smem_u32(smem + P::fw3);
+  for (int c = blockIdx.x; c < nchunks && alive; c += gridDim.x) {
+    const WorkChunk ch = chunks[c];
+    const int ti = ch.ti;
+    for (int q = tid; q < (ch.row1 - ch.row0) * 4 * ng; q += blockDim.x)
+      xyz[(size_t)sorted_rows[ch.row0 + q / (4 * ng)] * 4 * ng + q % (4 * ng)] = 0.f;
+    __syncthreads();
+    for (int t = 0; t < p.ntypes && alive; ++t) {
+      const int net = p.type_one_side ? t : t * p.ntypes + ti;
+      copy16(smem + P::fw2, e.fw2 + (size_t)net * P::N2 * P::K1 * 2, P::N2 * P::K1 * 2);
+      copy16(smem + P::fw3, e.fw3 + (size_t)net * P::N3 * P::N2 * 2, P::N3 * P::N2 * 2);
+      for (int q = tid; q < P::VEC; q += blockDim.x) sV[q] = e.vec[(size_t)net * P::VEC + q];
+      if (tid == 0) s_cursor = ch.row0;
+      __syncthreads();
+      const float* w1 = sV;
+      const float* b1 = sV + P::K1;
+      const float* i1 = sV + 2 * P::K1;
+      const float* b2 = sV + 3 * P::K1;
+      const float* i2 = b2 + P::N2;
+      const float* b3 = i2 + P::N2;
+      const float* i3 = b3 + P::N3;
+      while (alive) {
+        // pack whole runs of this section into a tile
+        if (tid == 0) {
+          int cur = s_cursor, n = 0, pairs = 0;
+          while (cur < ch.row1 && n < kTcMaxAtoms) {
+            const int len = run_len[(size_t)cur * p.ntypes + t];
+            if (len == 0) {
+              ++cur;
+              continue;
+            }
+            if (pairs + len > kTcRows) break;
+            s_row[n] = sorted_rows[cur];
+            s_off[n] = pairs;
+            pairs += len;
+            ++n;
+            ++cur;
+          }
+          s_off[n] = pairs;
+          s_ntile = n;
+          s_cursor = cur;
+        }
+        __syncthreads();
+        const int ntile = s_ntile;
+        if (ntile == 0) break;
+        // pair environment and layer 1 (1 -> W1) on the CUDA cores
+        PairInfo pi;
+        float rn[4], dv[3];
+        pair_env(p, t, ti, s_row, s_off, ntile, tid, pi, rn, dv);
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) sRn[tid * 4 + cc] = rn[cc];
+        const float x = rn[0];
+        float h1[W1];
+#pragma unroll
+        for (int k = 0; k < W1; ++k) {
+          const float tv = tanh_fast(fmaf(x, w1[k], b1[k]));
+          float h = tv * i1[k];
+          if (W1 == 1) h += x;
+          if (W1 == 2) h += x;
+          h1[k] = pi.valid ? h : 0.f;
+        }
+#pragma unroll
+        for (int k0 = 0; k0 < P::K1; k0 += 8) {
+          float v[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[i] = (k0 + i < W1) ? h1[k0 + i] : 0.f;
+          store8(smem + P::a1, tid, k0, P::K1, v);
+        }
+        tc::fence_async_smem();
+        __syncthreads();
+        tc::fence_after();
+        if (tid == 0) {
+          issue_mma<P::K1, P::N2>(tbase, sA1, sW2, P::K1);
+          tc::mma_commit(&bar);
+        }
+        bool ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout);
+        phase ^= 1;
+        tc::fence_after();
+        // epilogue 2: H2 = tanh(acc + b2) * idt2 + skip(H1)
+        float h2[W2];
+#pragma unroll
+        for (int c0 = 0; c0 < P::N2; c0 += 16) {
+          float v[16];
+          tc::tmem_ld16(tc::taddr(tbase, warp * 32, c0), v);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int o = c0 + i;
+            if (o < W2) {
+              float h = tanh_fast(v[i] + b2[o]) * i2[o];
+              if (W2 == W1) h += h1[o];
+              if (W2 == 2 * W1) h += h1[o < W1 ? o : o - W1];
+              h2[o] = pi.valid ? h : 0.f;
+            }
+          }
+        }
+#pragma unroll
+        for (int k0 = 0; k0 < P::N2; k0 += 8) {
+          float v[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[i] = (k0 + i < W2) ? h2[k0 + i] : 0.f;
+          store8(smem + P::a2, tid, k0, P::N2, v);
+        }
+        tc::fence_before();
+        tc::fence_async_smem();
+        __syncthreads();
+        tc::fence_after();
+        if (tid == 0) {
+          issue_mma<P::N2, P::N3>(tbase + P::N2, sA2, sW3, P::N2);
+          tc::mma_commit(&bar);
+        }
+        ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;
+        phase ^= 1;
+        tc::fence_after();
+        // epilogue 3: G = tanh(acc + b3) * idt3 + skip(H2), kept in FP32
+#pragma unroll
+        for (int c0 = 0; c0 < P::N3; c0 += 16) {
+          float v[16];
+          tc::tmem_ld16(tc::taddr(tbase, warp * 32, P::N2 + c0), v);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int o = c0 + i;
+            if (o < W3) {
+              float g = tanh_fast(v[i] + b3[o]) * i3[o];
+              if (W3 == W2) g += h2[o];
+              if (W3 == 2 * W2) g += h2[o < W2 ? o : o - W2];
+              sG[tid * P::LDG + o] = pi.valid ? g : 0.f;
+            }
+          }
+        }
+        tc::fence_before();
+        alive = __syncthreads_and(ok) != 0;
+        if (!alive) break;
+        // xyz[atom][c][n] += sum_{pairs of the atom} Rn[c] G[n]  (FP32, fixed order)
+        for (int q = tid; q < ntile * 4 * W3; q += blockDim.x) {
+          const int k = q / (4 * W3), rem = q - k * 4 * W3, cc = rem / W3, n = rem - cc * W3;
+          float s = 0.f;
+          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) s = fmaf(sRn[pp * 4 + cc], sG[pp * P::LDG + n], s);
+          float* dst = xyz + (size_t)s_row[k] * 4 * ng + cc * ng + n;
+          *dst += s;
+        }
+        __syncthreads();
+      }
+    }
+    // finalize the chunk: D = (xyz/nnei)^T (xyz/nnei)[:, :axis], then scale xyz
+    const float inv = 1.f / (float)p.nnei;
+    const int dim = ng * p.axis;
+    __syncthreads();
+    for (int q = tid; q < (ch.row1 - ch.row0) * dim; q += blockDim.x) {
+      const int r = ch.row0 + q / dim, rem = q % dim, n = rem / p.axis, m = rem - n * p.axis;
+      const float* xr = xyz + (size_t)sorted_rows[r] * 4 * ng;
+      float s = 0.f;
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) s = fmaf(xr[cc * ng + n], xr[cc * ng + m], s);
+      Dout[(size_t)r * dim + rem] = s * inv * inv;
+    }
+    __syncthreads();
+    for (int q = tid; q < (ch.row1 - ch.row0) * 4 * ng; q += blockDim.x)
+      xyz[(size_t)sorted_rows[ch.row0 + q / (4 * ng)] * 4 * ng + q % (4 * ng)] *= inv;
+    __syncthreads();
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tbase, P::tmem_cols);
+}
+
+// ---------------------------------------------------------------------------
+template <int W1, int W2, int W3>
+__global__ void __launch_bounds__(128, 1)
+emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ chunks, int nchunks,
+                  const int* __restrict__ run_len, const int* __restrict__ sorted_rows,
+                  const float* __restrict__ dxyz, float* __restrict__ gpair, double* __restrict__ vir_row,
+                  int* __restrict__ status) {
+  using P = Plan<W1, W2, W3>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_row[kTcMaxAtoms], s_off[kTcMaxAtoms + 1], s_ntile, s_cursor;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int ng = p.ng;
+  if (warp == 0) tc::tmem_alloc(&s_tmem, P::tmem_cols);
+  if (tid == 0) tc::mbar_init(&bar, 1);
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tbase = s_tmem;
+  uint32_t phase = 0;
+  bool alive = true;
+  float* sDX = reinterpret_cast<float*>(smem + P::gbuf);  // [kTcMaxAtoms][4][W3]
+  float* sV = reinterpret_cast<float*>(smem + P::vec);
+  double* sVir = reinterpret_cast<double*>(smem + P::vir);
+  const uint32_t sA1 = tc::smem_u32(smem + P::a1), sA2 = tc::smem_u32(smem + P::a2), sA3 = tc::smem_u32(smem + P::a3);
+  const uint32_t sW2 = tc::smem_u32(smem + P::fw2), sW3 = tc::smem_u32(smem + P::fw3);
+  const uint32_t sB3 = tc::smem_u32(smem + P::bw3), sB2 = tc::smem_u32(smem + P::bw2);
+  const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
+  for (int c = blockIdx.x; c < nchunks && alive; c += gridDim.x) {
+    const WorkChunk ch = chunks[c];
+    const int ti = ch.ti;
+    for (int q = tid; q < (ch.row1 - ch.row0) * 9; q += blockDim.x)
+      vir_row[(size_t)sorted_rows[ch.row0 + q / 9] * 9 + q % 9] = 0.0;
+    __syncthreads();
+    for (int t = 0; t < p.ntypes && alive; ++t) {
+      const int net = p.type_one_side ? t : t * p.ntypes + ti;
+      copy16(smem + P::fw2, e.fw2 + (size_t)net * P::N2 * P::K1 * 2, P::N2 * P::K1 * 2);
+      copy16(smem + P::fw3, e.fw3 + (size_t)net * P::N3 * P::N2 * 2, P::N3 * P::N2 * 2);
+      copy16(smem + P::bw3, e.bw3 + (size_t)net * P::N2 * P::N3 * 2, P::N2 * P::N3 * 2);
+      copy16(smem + P::bw2, e.bw2 + (size_t)net * P::K1 * P::N2 * 2, P::K1 * P::N2 * 2);
+      for (int q = tid; q < P::VEC; q += blockDim.x) sV[q] = e.vec[(size_t)net * P::VEC + q];
+      if (tid == 0) s_cursor = ch.row0;
+      __syncthreads();
+      const float* w1 = sV;
+      const float* b1 = sV + P::K1;
+      const float* i1 = sV + 2 * P::K1;
+      const float* b2 = sV + 3 * P::K1;
+      const float* i2 = b2 + P::N2;
+      const float* b3 = i2 + P::N2;
+      const float* i3 = b3 + P::N3;
+      while (alive) {
+        if (tid == 0) {
+          int cur = s_cursor, n = 0, pairs = 0;
+          while (cur < ch.row1 && n < kTcMaxAtoms) {
+            const int len = run_len[(size_t)cur * p.ntypes + t];
+            if (len == 0) {
+              ++cur;
+              continue;
+            }
+            if (pairs + len > kTcRows) break;
+            s_row[n] = sorted_rows[cur];
+            s_off[n] = pairs;
+            pairs += len;
+            ++n;
+            ++cur;
+          }
+          s_off[n] = pairs;
+          s_ntile = n;
+          s_cursor = cur;
+        }
+        __syncthreads();
+        const int ntile = s_ntile;
+        if (ntile == 0) break;
+        for (int q = tid; q < ntile * 4 * W3; q += blockDim.x) {
+          const int k = q / (4 * W3), rem = q - k * 4 * W3, cc = rem / W3, n = rem - cc * W3;
+          sDX[q] = dxyz[(size_t)s_row[k] * 4 * ng + cc * ng + n];
+        }
+        PairInfo pi;
+        float rn[4], dv[3];
+        pair_env(p, t, ti, s_row, s_off, ntile, tid, pi, rn, dv);
+        const float x = rn[0];
+        float t1[W1], h1[W1];
+#pragma unroll
+        for (int k = 0; k < W1; ++k) {
+          const float tv = tanh_fast(fmaf(x, w1[k], b1[k]));
+          t1[k] = tv;
+          float h = tv * i1[k];
+          if (W1 == 1) h += x;
+          if (W1 == 2) h += x;
+          h1[k] = pi.valid ? h : 0.f;
+        }
+#pragma unroll
+        for (int k0 = 0; k0 < P::K1; k0 += 8) {
+          float v[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[i] = (k0 + i < W1) ? h1[k0 + i] : 0.f;
+          store8(smem + P::a1, tid, k0, P::K1, v);
+        }
+        tc::fence_async_smem();
+        __syncthreads();
+        tc::fence_after();
+        if (tid == 0) {
+          issue_mma<P::K1, P::N2>(tbase, sA1, sW2, P::K1);
+          tc::mma_commit(&bar);
+        }
+        bool ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout);
+        phase ^= 1;
+        tc::fence_after();
+        float t2[W2], h2[W2];
+#pragma unroll
+        for (int c0 = 0; c0 < P::N2; c0 += 16) {
+          float v[16];
+          tc::tmem_ld16(tc::taddr(tbase, warp * 32, c0), v);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int o = c0 + i;
+            if (o < W2) {
+              const float tv = tanh_fast(v[i] + b2[o]);
+              t2[o] = tv;
+              float h = tv * i2[o];
+              if (W2 == W1) h += h1[o];
+              if (W2 == 2 * W1) h += h1[o < W1 ? o : o - W1];
+              h2[o] = pi.valid ? h : 0.f;
+            }
+          }
+        }
+#pragma unroll
+        for (int k0 = 0; k0 < P::N2; k0 += 8) {
+          float v[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[i] = (k0 + i < W2) ? h2[k0 + i] : 0.f;
+          store8(smem + P::a2, tid, k0, P::N2, v);
+        }
+        tc::fence_before();
+        tc::fence_async_smem();
+        __syncthreads();
+        tc::fence_after();
+        if (tid == 0) {
+          issue_mma<P::N2, P::N3>(tbase + P::N2, sA2, sW3, P::N2);
+          tc::mma_commit(&bar);
+        }
+        ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;
+        phase ^= 1;
+        tc::fence_after();
+        // epilogue 3 of the backward: G, dG = Rn . dxyz, dRn (direct part),
+        // dP3 = dG * idt3 * (1 - t3^2) into the BF16 operand, skip folds
+        const float* dx = sDX + pi.k * 4 * W3;
+        float drn[4] = {0.f, 0.f, 0.f, 0.f};
+        float dh2[W2];
+#pragma unroll
+        for (int o = 0; o < W2; ++o) dh2[o] = 0.f;
+#pragma unroll
+        for (int c0 = 0; c0 < P::N3; c0 += 16) {
+          float v[16], dp[16];
+          tc::tmem_ld16(tc::taddr(tbase, warp * 32, P::N2 + c0), v);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int o = c0 + i;
+            dp[i] = 0.f;
+            if (o < W3) {
+              const float tv = tanh_fast(v[i] + b3[o]);
+              float g = tv * i3[o];
+              if (W3 == W2) g += h2[o];
+              if (W3 == 2 * W2) g += h2[o < W2 ? o : o - W2];
+              const float d0 = dx[o], d1 = dx[W3 + o], d2 = dx[2 * W3 + o], d3 = dx[3 * W3 + o];
+              drn[0] = fmaf(g, d0, drn[0]);
+              drn[1] = fmaf(g, d1, drn[1]);
+              drn[2] = fmaf(g, d2, drn[2]);
+              drn[3] = fmaf(g, d3, drn[3]);
+              const float dg = rn[0] * d0 + rn[1] * d1 + rn[2] * d2 + rn[3] * d3;
+              dp[i] = pi.valid ? dg * i3[o] * (1.f - tv * tv) : 0.f;
+              if (W3 == W2) dh2[o] += dg;
+              if (W3 == 2 * W2) dh2[o < W2 ? o : o - W2] += dg;
+            }
+          }
+          store8(smem + P::a3, tid, c0, P::N3, dp);
+          store8(smem + P::a3, tid, c0 + 8, P::N3, dp + 8);
+        }
+        tc::fence_before();
+        tc::fence_async_smem();
+        __syncthreads();
+        tc::fence_after();
+        if (tid == 0) {
+          issue_mma<P::N3, P::N2>(tbase, sA3, sB3, P::N3);  // dH2 = dP3 . W3^T
+          tc::mma_commit(&bar);
+        }
+        ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;
+        phase ^= 1;
+        tc::fence_after();
+        float dh1[W1];
+#pragma unroll
+        for (int k = 0; k < W1; ++k) dh1[k] = 0.f;
+#pragma unroll
+        for (int c0 = 0; c0 < P::N2; c0 += 16) {
+          float v[16], dp[16];
+          tc::tmem_ld16(tc::taddr(tbase, warp * 32, c0), v);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int o = c0 + i;
+            dp[i] = 0.f;
+            if (o < W2) {
+              const float dh = v[i] + dh2[o];
+              dp[i] = pi.valid ? dh * i2[o] * (1.f - t2[o] * t2[o]) : 0.f;
+              if (W2 == W1) dh1[o] += dh;
+              if (W2 == 2 * W1) dh1[o < W1 ? o : o - W1] += dh;
+            }
+          }
+          store8(smem + P::a2, tid, c0, P::N2, dp);
+          store8(smem + P::a2, tid, c0 + 8, P::N2, dp + 8);
+        }
+        tc::fence_before();
+        tc::fence_async_smem();
+        __syncthreads();
+        tc::fence_after();
+        if (tid == 0) {
+          issue_mma<P::N2, P::K1>(tbase + P::N2, sA2, sB2, P::N2);  // dH1 = dP2 . W2^T
+          tc::mma_commit(&bar);
+        }
+        ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;
+        phase ^= 1;
+        tc::fence_after();
+        float dss = 0.f;
+#pragma unroll
+        for (int c0 = 0; c0 < P::K1; c0 += 16) {
+          float v[16];
+          tc::tmem_ld16(tc::taddr(tbase, warp * 32, P::N2 + c0), v);
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int k = c0 + i;
+            if (k < W1) {
+              const float dh = v[i] + dh1[k];
+              dss = fmaf(dh * i1[k] * (1.f - t1[k] * t1[k]), w1[k], dss);
+              if (W1 == 1 || W1 == 2) dss += dh;
+            }
+          }
+        }
+        drn[0] += dss;
+        // pair gradient g = dE/d(r_j - r_i) and the pair virial -g (x) d
+        float g[3] = {0.f, 0.f, 0.f};
+        if (pi.valid && pi.nb >= 0 && pi.keep) {
+          float der[12];
+          env_deriv(dv, rmin, rmax, der);
+          const float* sd = p.dstd + ((size_t)ti * p.nnei + pi.slot) * 4;
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) {
+            const float w = drn[cc] / sd[cc];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) g[k] -= w * der[3 * cc + k];
+          }
+        }
+        if (pi.valid) {
+          float* gp = gpair + ((size_t)pi.row * p.nnei + pi.slot) * 3;
+          gp[0] = g[0];
+          gp[1] = g[1];
+          gp[2] = g[2];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int l = 0; l < 3; ++l) sVir[tid * 9 + 3 * k + l] = -(double)g[k] * (double)dv[l];
+        tc::fence_before();
+        alive = __syncthreads_and(ok) != 0;
+        if (!alive) break;
+        for (int q = tid; q < ntile * 9; q += blockDim.x) {
+          const int k = q / 9, comp = q - 9 * k;
+          double s = 0.0;
+          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) s += sVir[pp * 9 + comp];
+          vir_row[(size_t)s_row[k] * 9 + comp] += s;
+        }
+        __syncthreads();
+      }
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tbase, P::tmem_cols);
+}
+
+// run lengths of active slots per (sorted row, section)
+__global__ void run_len_kernel(int* __restrict__ run_len, const int* __restrict__ nlist,
+                               const int* __restrict__ sorted_rows, int nrows, int nnei, SelInfo sel, int pad_zero) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nrows * sel.ntypes) return;
+  const int r = q / sel.ntypes, t = q - r * sel.ntypes;
+  const int row = sorted_rows[r];
+  int n = 0;
+  if (pad_zero) {
+    const int* nl = nlist + (size_t)row * nnei + sel.sec[t];
+    for (int j = 0; j < sel.sel[t]; ++j) n += nl[j] >= 0;
+  } else {
+    n = sel.sel[t];
+  }
+  run_len[q] = n;
+}
+
+// dE/dxyz (before the forward's 1/nnei): dxyz[c][n] = (sum_m dD[n][m] xyz[c][m]
+// + [n < M] sum_n' dD[n'][n] xyz[c][n']) / nnei ; one CTA per row
+__global__ void dxyz_kernel(float* __restrict__ dxyz, const float* __restrict__ dD, const float* __restrict__ xyz,
+                            const int* __restrict__ row_pos, const int* __restrict__ atype, int nloc, int ng, int M,
+                            int nnei) {
+  extern __shared__ float s_x[];
+  const int row = blockIdx.x;
+  const float* xr = xyz + (size_t)row * 4 * ng;
+  for (int q = threadIdx.x; q < 4 * ng; q += blockDim.x) s_x[q] = xr[q];
+  __syncthreads();
+  if (atype[row % nloc] < 0) {
+    for (int q = threadIdx.x; q < 4 * ng; q += blockDim.x) dxyz[(size_t)row * 4 * ng + q] = 0.f;
+    return;
+  }
+  const float* d = dD + (size_t)row_pos[row] * ng * M;
+  const float inv = 1.f / (float)nnei;
+  for (int q = threadIdx.x; q < 4 * ng; q += blockDim.x) {
+    const int c = q / ng, n = q - c * ng;
+    float s = 0.f;
+    for (int m = 0; m < M; ++m) s = fmaf(__ldg(d + n * M + m), s_x[c * ng + m], s);
+    if (n < M)
+      for (int n2 = 0; n2 < ng; ++n2) s = fmaf(__ldg(d + n2 * M + n), s_x[c * ng + n2], s);
+    dxyz[(size_t)row * 4 * ng + q] = s * inv;
+  }
+}
+
+template <int W1, int W2, int W3>
+int launch_fwd_t(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks, const int* run_len,
+                 const int* sorted_rows, float* xyz, float* D, int* status, cudaStream_t st, int nsm) {
+  using P = Plan<W1, W2, W3>;
+  auto k = emb_tc_fwd_kernel<W1, W2, W3>;
+  DPGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, P::total));
+  const int grid = nchunks < nsm ? nchunks : nsm;
+  k<<<grid, 128, P::total, st>>>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, D, status);
+  return check_launch("emb_tc_fwd");
+}
+template <int W1, int W2, int W3>
+int launch_bwd_t(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks, const int* run_len,
+                 const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, int* status, cudaStream_t st,
+                 int nsm) {
+  using P = Plan<W1, W2, W3>;
+  auto k = emb_tc_bwd_kernel<W1, W2, W3>;
+  DPGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, P::total));
+  const int grid = nchunks < nsm ? nchunks : nsm;
+  k<<<grid, 128, P::total, st>>>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status);
+  return check_launch("emb_tc_bwd");
+}
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+}  // namespace
+
+int launch_run_lengths(int* run_len, const int* nlist, const int* sorted_rows, int nrows, int nnei, const SelInfo& sel,
+                       int pad_zero, cudaStream_t st) {
+  if (nrows <= 0) return DPGB_OK;
+  run_len_kernel<<<ceil_div((long long)nrows * sel.ntypes, 256), 256, 0, st>>>(run_len, nlist, sorted_rows, nrows,
+                                                                                nnei, sel, pad_zero);
+  return check_launch("run_len");
+}
+
+int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks,
+                      const int* run_len, const int* sorted_rows, float* xyz, float* D, int* status, cudaStream_t st) {
+  if (nchunks <= 0) return DPGB_OK;
+  const int nsm = 2 * sm_count();
+  if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100)
+    return launch_fwd_t<25, 50, 100>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, D, status, st, nsm);
+  if (e.w1 == 3 && e.w2 == 6 && e.w3 == 12)
+    return launch_fwd_t<3, 6, 12>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, D, status, st, nsm);
+  return fail(DPGB_EINVAL, "embedding widths without a tensor-core kernel");
+}
+
+int launch_dxyz(const DescParams<float>& p, const float* dD, const float* xyz, float* dxyz, cudaStream_t st) {
+  if (p.nrows <= 0) return DPGB_OK;
+  dxyz_kernel<<<p.nrows, 128, sizeof(float) * 4 * p.ng, st>>>(dxyz, dD, xyz, p.row_pos, p.atype, p.nloc, p.ng, p.axis,
+                                                              p.nnei);
+  return check_launch("dxyz");
+}
+
+int launch_emb_tc_bwd(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks,
+                      const int* run_len, const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row,
+                      int* status, cudaStream_t st) {
+  if (nchunks <= 0) return DPGB_OK;
+  const int nsm = 2 * sm_count();
+  if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100)
+    return launch_bwd_t<25, 50, 100>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status, st,
+                                     nsm);
+  if (e.w1 == 3 && e.w2 == 6 && e.w3 == 12)
+    return launch_bwd_t<3, 6, 12>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status, st, nsm);
+  return fail(DPGB_EINVAL, "embedding widths without a tensor-core kernel");
+}
+
+}  // namespace dpgb
