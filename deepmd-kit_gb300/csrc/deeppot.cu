@@ -16,7 +16,10 @@
 #include <string>
 #include <vector>
 
+#include <type_traits>
+
 #include "emb_tc.cuh"
+#include "fit_tc.cuh"
 #include "se_a.cuh"
 
 namespace dpgb {
@@ -162,6 +165,16 @@ struct DeepPotImpl {
   int use_tc = 0;
   EmbTC tc{};
   DeviceBuffer tc_images, tc_vec, ws_runlen, ws_dxyz;
+  // tensor-core fitting (mixed precision)
+  int use_fit_tc = 0;
+  int fit_nh = 0, fit_width[kMaxFitLayers + 1] = {};
+  const __nv_bfloat16* fit_Wt[kMaxFitLayers] = {};  // forward B: [nt][out][in]
+  const __nv_bfloat16* fit_Wb[kMaxFitLayers] = {};  // backward B: [nt][in][out]
+  const float* fit_b[kMaxFitLayers] = {};
+  const float* fit_idt[kMaxFitLayers] = {};
+  const float* fit_wout = nullptr;
+  std::vector<float> fit_bout;
+  DeviceBuffer fit_w16, fit_f32, ws_fitb;
   // workspace
   DeviceBuffer ws_nlist, ws_cell, ws_tr, ws_keys, ws_status, ws_coord, ws_svec, ws_spos;
   DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf;
@@ -183,6 +196,146 @@ struct DeepPotImpl {
 };
 
 namespace {
+
+// BF16 weight images of the tensor-core fitting: forward B = W^T [out][in],
+// backward B = W [in][out] per type; FP32 bias / timestep / output layer.
+int build_fit_tc(DeepPotImpl& im, const dpgb_se_a_desc& d) {
+  const int nt = d.ntypes;
+  im.fit_nh = d.n_fit;
+  im.fit_width[0] = d.dim_descrpt;
+  for (int l = 0; l < d.n_fit; ++l) im.fit_width[l + 1] = d.fit_neuron[l];
+  std::vector<__nv_bfloat16> w16;
+  std::vector<float> f32;
+  size_t offWt[kMaxFitLayers], offWb[kMaxFitLayers], offb[kMaxFitLayers], offi[kMaxFitLayers];
+  for (int l = 0; l < d.n_fit; ++l) {
+    const int a = im.fit_width[l], o = im.fit_width[l + 1];
+    offWt[l] = w16.size();
+    for (int t = 0; t < nt; ++t)
+      for (int n = 0; n < o; ++n)
+        for (int k = 0; k < a; ++k) w16.push_back(__float2bfloat16_rn((float)d.fit_w[t][l][(size_t)k * o + n]));
+    offWb[l] = w16.size();
+    for (int t = 0; t < nt; ++t)
+      for (int k = 0; k < a; ++k)
+        for (int n = 0; n < o; ++n) w16.push_back(__float2bfloat16_rn((float)d.fit_w[t][l][(size_t)k * o + n]));
+    offb[l] = f32.size();
+    for (int t = 0; t < nt; ++t)
+      for (int n = 0; n < o; ++n) f32.push_back((float)d.fit_b[t][l][n]);
+    offi[l] = (size_t)-1;
+    bool has = false;
+    for (int t = 0; t < nt; ++t) has |= d.fit_idt[t][l] != nullptr;
+    if (has) {
+      offi[l] = f32.size();
+      for (int t = 0; t < nt; ++t)
+        for (int n = 0; n < o; ++n) f32.push_back(d.fit_idt[t][l] ? (float)d.fit_idt[t][l][n] : 1.f);
+    }
+  }
+  const int wl = im.fit_width[d.n_fit];
+  const size_t offw = f32.size();
+  im.fit_bout.assign(nt, 0.f);
+  for (int t = 0; t < nt; ++t) {
+    for (int n = 0; n < wl; ++n) f32.push_back((float)d.fit_w[t][d.n_fit][n]);
+    if (d.fit_b[t][d.n_fit]) im.fit_bout[t] = (float)d.fit_b[t][d.n_fit][0];
+  }
+  DPGB_TRY(im.fit_w16.alloc(sizeof(__nv_bfloat16) * w16.size()));
+  DPGB_TRY(im.fit_f32.alloc(sizeof(float) * f32.size()));
+  DPGB_CUDA(cudaMemcpy(im.fit_w16.ptr, w16.data(), sizeof(__nv_bfloat16) * w16.size(), cudaMemcpyHostToDevice));
+  DPGB_CUDA(cudaMemcpy(im.fit_f32.ptr, f32.data(), sizeof(float) * f32.size(), cudaMemcpyHostToDevice));
+  const __nv_bfloat16* w = im.fit_w16.as<__nv_bfloat16>();
+  const float* f = im.fit_f32.as<float>();
+  for (int l = 0; l < d.n_fit; ++l) {
+    im.fit_Wt[l] = w + offWt[l];
+    im.fit_Wb[l] = w + offWb[l];
+    im.fit_b[l] = f + offb[l];
+    im.fit_idt[l] = offi[l] == (size_t)-1 ? nullptr : f + offi[l];
+  }
+  im.fit_wout = f + offw;
+  im.use_fit_tc = 1;
+  return DPGB_OK;
+}
+
+// forward + input-gradient backward of the fitting of one type's sorted rows
+// [r0, r0+n) on the tensor cores.  Db: BF16 descriptors; dD: FP32 output.
+int run_fit_tc(DeepPotImpl& dp, int t, int r0, int n, int nrows, const __nv_bfloat16* Db, float* dD, float* act,
+               float* gbuf, __nv_bfloat16* fitb, double* e_sorted, int* err, cudaStream_t st) {
+  const int nh = dp.fit_nh, dim = dp.fit_width[0];
+  int maxw = 0;
+  for (int l = 1; l <= nh; ++l) maxw = std::max(maxw, dp.fit_width[l]);
+  const size_t plane = (size_t)nrows * maxw;
+  auto Yf = [&](int l) { return act + (size_t)l * plane + (size_t)r0 * maxw; };
+  auto Tt = [&](int l) { return act + (size_t)(nh + l) * plane + (size_t)r0 * maxw; };
+  auto Yb = [&](int l) { return fitb + (size_t)l * plane + (size_t)r0 * maxw; };
+  auto dPb = [&](int k) { return fitb + (size_t)(nh + k) * plane + (size_t)r0 * maxw; };
+  auto dX = [&](int k) { return gbuf + (size_t)k * plane + (size_t)r0 * maxw; };
+  const int wl = dp.fit_width[nh];
+  for (int l = 0; l < nh; ++l) {
+    const int a = dp.fit_width[l], o = dp.fit_width[l + 1];
+    FitGemm g{};
+    g.mode = l == nh - 1 ? kFitFwdLast : kFitFwd;
+    g.M = n;
+    g.N = o;
+    g.K = a;
+    g.A = l == 0 ? Db + (size_t)r0 * dim : Yb(l - 1);
+    g.lda = l == 0 ? dim : maxw;
+    g.B = dp.fit_Wt[l] + (size_t)t * o * a;
+    g.bias = dp.fit_b[l] + (size_t)t * o;
+    g.idt = dp.fit_idt[l] ? dp.fit_idt[l] + (size_t)t * o : nullptr;
+    g.skip = (o == a && l > 0) ? 1 : 0;
+    g.Xs = l > 0 ? Yf(l - 1) : nullptr;
+    g.ldxs = maxw;
+    g.Yf = Yf(l);
+    g.Yb = Yb(l);
+    g.Tt = Tt(l);
+    g.ldy = maxw;
+    if (g.mode == kFitFwdLast) {
+      g.w_out = dp.fit_wout + (size_t)t * wl;
+      g.b_out = dp.fit_bout[t];
+      g.e_out = e_sorted + r0;
+      g.dPb = dPb(0);
+    }
+    DPGB_TRY(launch_fit_gemm(g, err, st));
+  }
+  // backward through the hidden layers nh-1 .. 1 (dP ping-pongs between two planes)
+  int cur = 0;
+  for (int l = nh - 1; l >= 1; --l) {
+    const int a = dp.fit_width[l], o = dp.fit_width[l + 1];
+    FitGemm g{};
+    g.mode = kFitBwd;
+    g.M = n;
+    g.N = a;
+    g.K = o;
+    g.A = dPb(cur);
+    g.lda = maxw;
+    g.B = dp.fit_Wb[l] + (size_t)t * a * o;
+    if (o == a) {  // skip connection of layer l: gradient of its output passes through
+      if (l == nh - 1) {
+        g.dYup = dp.fit_wout + (size_t)t * wl;
+        g.lddyup = 0;
+      } else {
+        g.dYup = dX((cur + 1) & 1);
+        g.lddyup = maxw;
+      }
+    }
+    const bool lower_skip = dp.fit_width[l] == dp.fit_width[l - 1];
+    g.dXf = lower_skip ? dX(cur) : nullptr;
+    g.T_lo = Tt(l - 1);
+    g.idt_lo = dp.fit_idt[l - 1] ? dp.fit_idt[l - 1] + (size_t)t * a : nullptr;
+    g.ldy = maxw;
+    g.dPb = dPb(cur ^ 1);
+    DPGB_TRY(launch_fit_gemm(g, err, st));
+    cur ^= 1;
+  }
+  FitGemm g{};
+  g.mode = kFitStore;
+  g.M = n;
+  g.N = dim;
+  g.K = dp.fit_width[1];
+  g.A = dPb(cur);
+  g.lda = maxw;
+  g.B = dp.fit_Wb[0] + (size_t)t * dim * dp.fit_width[1];
+  g.out = dD + (size_t)r0 * dim;
+  g.ldo = dim;
+  return launch_fit_gemm(g, err, st);
+}
 
 int validate_desc(const dpgb_se_a_desc* d) {
   if (!d) return fail(DPGB_EINVAL, "NULL model description");
@@ -536,7 +689,9 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ng));
       DPGB_TRY(launch_run_lengths(dp.ws_runlen.as<int>(), nlist, dp.sorted_rows_dev.as<int>(), nsorted, nnei, dp.sel,
                                   dp.pad_zero, st));
-      DPGB_TRY(launch_emb_tc_fwd(p, dp.tc, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.ws_runlen.as<int>(),
+      EmbTC e = dp.tc;
+      e.d_bf16 = dp.use_fit_tc;
+      DPGB_TRY(launch_emb_tc_fwd(p, e, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.ws_runlen.as<int>(),
                                  dp.sorted_rows_dev.as<int>(), dp.ws_xyz.as<float>(), dp.ws_D.as<float>(), status, st));
       launches += 2;
     }
@@ -547,8 +702,23 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   }
   dp.mark(DPGB_STAGE_DESC_FWD, 1, st);
   dp.mark(DPGB_STAGE_FITTING, 0, st);
+  bool fit_tc = false;
+  if constexpr (std::is_same<T, float>::value) fit_tc = tc_path && dp.use_fit_tc;
+  if (fit_tc) {
+    DPGB_TRY(dp.ws_fitb.alloc(sizeof(__nv_bfloat16) * (size_t)(dp.fit_nh + 2) * nrows * maxw));
+  }
   for (int t = 0; t < d.ntypes; ++t) {
     if (dp.type_count[t] == 0) continue;
+    if (fit_tc) {
+      if constexpr (std::is_same<T, float>::value) {
+        DPGB_TRY(run_fit_tc(dp, t, dp.type_off[t], dp.type_count[t], (int)nrows,
+                            reinterpret_cast<const __nv_bfloat16*>(dp.ws_D.ptr), dp.ws_dD.as<float>(),
+                            dp.ws_act.as<float>(), dp.ws_gbuf.as<float>(), dp.ws_fitb.as<__nv_bfloat16>(),
+                            dp.ws_esorted.as<double>(), status + kStatusTimeout, st));
+      }
+      launches += 2 * dp.fit_nh + 1;
+      continue;
+    }
     DPGB_TRY(launch_fitting<T>(m.fit, t, dp.type_off[t], dp.type_count[t], (int)nrows, dp.ws_D.as<T>(),
                                dp.ws_dD.as<T>(), dp.ws_act.as<T>(), dp.ws_gbuf.as<T>(), dp.ws_esorted.as<double>(),
                                0.0, st));
@@ -598,6 +768,8 @@ int check_status(DeepPotImpl& dp, cudaStream_t st) {
   if (h[kStatusOverflow] > 0)
     return fail(DPGB_EOVERFLOW, "neighbour capacity exceeded (" + std::to_string(h[kStatusOverflow]) +
                                     " entries) at atom/row " + std::to_string(h[kStatusOverflowAtom] - 1));
+  if (h[kStatusTimeout] > 0)
+    return fail(DPGB_ETIMEOUT, "a tensor-core completion wait timed out; results are invalid");
   return DPGB_OK;
 }
 
@@ -671,6 +843,7 @@ dpgb_deeppot* dpgb_deeppot_new(const dpgb_se_a_desc* desc, int precision) {
       }
       emb_tc_bind(im.tc, im.tc_images.as<unsigned char>(), 0, im.tc_vec.as<float>());
       im.use_tc = 1;
+      if (fit_tc_eligible(*desc) && build_fit_tc(im, *desc) != DPGB_OK) return nullptr;
     }
   }
   // the host pointers of the description are not kept

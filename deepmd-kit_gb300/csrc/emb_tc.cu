@@ -443,7 +443,10 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
       float s = 0.f;
 #pragma unroll
       for (int cc = 0; cc < 4; ++cc) s = fmaf(xr[cc * ng + n], xr[cc * ng + m], s);
-      Dout[(size_t)r * dim + rem] = s * inv * inv;
+      if (e.d_bf16)  // the tensor-core fitting reads D as BF16
+        reinterpret_cast<__nv_bfloat16*>(Dout)[(size_t)r * dim + rem] = __float2bfloat16_rn(s * inv * inv);
+      else
+        Dout[(size_t)r * dim + rem] = s * inv * inv;
     }
     __syncthreads();
     for (int q = tid; q < (ch.row1 - ch.row0) * 4 * ng; q += blockDim.x)

@@ -23,6 +23,7 @@ struct EmbTC {
   const float* vec;          // [nnets][vec_stride]: w1 b1 idt1 | b2 idt2 | b3 idt3 (padded)
   int vec_stride;
   int has_idt1, has_idt2, has_idt3;
+  int d_bf16;  // per call: write D as BF16 (for the tensor-core fitting)
 };
 
 // contiguous ranges of type-sorted rows processed by one CTA (same centre type)
