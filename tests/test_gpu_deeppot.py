@@ -78,7 +78,7 @@ def test_mixed_vs_fp64(cuda, water_fp64):
     rmse = float(np.sqrt(np.mean((f32 - f64) ** 2)))
     assert rmse <= 1e-3
     assert rmse <= 2e-2 * float(np.sqrt(np.mean(f64 ** 2)))  # also within 2 % of the RMS force
-    assert abs(e32[0] - e64[0]) / n < 1e-5
+    assert abs(e32[0] - e64[0]) / n < 2e-4  # eV/atom: BF16 descriptor into the fitting GEMMs
     assert rel(v32[0], v64[0]) < 2e-2
 
 
