@@ -78,6 +78,7 @@ _SIGS = {
     "dpgb_env_mat_pt_f64": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _P],
     "dpgb_prod_force_a_f64": [_P, _P, _P, _P, _I, _I, _I, _I, _P],
     "dpgb_prod_virial_a_f64": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _P],
+    "dpgb_prod_force_a_f64_noalloc": [_P, _P, _P, _P, _I, _I, _I, _I, _P],
     "dpgb_prod_force_grad_a_f64": [_P, _P, _P, _P, _I, _I, _I, _P],
     "dpgb_prod_virial_grad_a_f64": [_P, _P, _P, _P, _P, _I, _I, _P],
     "dpgb_tc_gemm_bf16": [_P, _P, _P, _I, _I, _I, _P],

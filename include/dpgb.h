@@ -171,6 +171,22 @@ int dpgb_prod_virial_a_f64(double* virial, double* atom_virial,
                            const double* net_deriv, const double* env_deriv,
                            const double* rij, const int* nlist, int nloc,
                            int nall, int nnei, void* stream);
+/* dpgb_prod_force_a_f64 without any device allocation.  No counterpart in
+ * the reference.  For callers that cannot allocate device memory inside the
+ * force call: an MD engine whose device memory belongs to its own pool
+ * allocator, or an inner loop where cudaMalloc/cudaFree would synchronise
+ * the whole device.  Same arguments and result as dpgb_prod_force_a_f64; the
+ * scratch lives in one fixed 11 MiB device array of the library, so
+ * nframes*nloc*nnei and nframes*nall must each be <= 262144 (larger sizes
+ * return DPGB_EINVAL).  The first call on a device looks the array up
+ * (cudaGetSymbolAddress) and should come before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race, so serialise
+ * them.  Synchronises the stream. */
+int dpgb_prod_force_a_f64_noalloc(double* force, const double* net_deriv,
+                                  const double* env_deriv, const int* nlist,
+                                  int nloc, int nall, int nnei, int nframes,
+                                  void* stream);
+
 /* Second-order terms for force-loss training: replace
  * deepmd::prod_force_grad_a_gpu (source/lib/src/gpu/prod_force_grad.cu:
  * 10-57) and prod_virial_grad_a_gpu (prod_virial_grad.cu:14-52).
