@@ -253,32 +253,40 @@ int build_fit_tc(DeepPotImpl& im, const dpgb_se_a_desc& d) {
   return DPGB_OK;
 }
 
-// forward + input-gradient backward of the fitting of one type's sorted rows
-// [r0, r0+n) on the tensor cores.  Db: BF16 descriptors; dD: FP32 output.
-int run_fit_tc(DeepPotImpl& dp, int t, int r0, int n, int nrows, const __nv_bfloat16* Db, float* dD, float* act,
-               float* gbuf, __nv_bfloat16* fitb, double* e_sorted, int* err, cudaStream_t st) {
-  const int nh = dp.fit_nh, dim = dp.fit_width[0];
+// forward + input-gradient backward of the fitting of all typed rows on the
+// tensor cores, one launch per layer (each 128-row tile uses its type's
+// weights).  Db: BF16 descriptors (sorted rows); dD: FP32 output.
+int run_fit_tc(DeepPotImpl& dp, int nrows, const __nv_bfloat16* Db, float* dD, float* act, float* gbuf,
+               __nv_bfloat16* fitb, double* e_sorted, int* err, cudaStream_t st) {
+  const int nh = dp.fit_nh, dim = dp.fit_width[0], nt = dp.desc.ntypes;
   int maxw = 0;
   for (int l = 1; l <= nh; ++l) maxw = std::max(maxw, dp.fit_width[l]);
   const size_t plane = (size_t)nrows * maxw;
-  auto Yf = [&](int l) { return act + (size_t)l * plane + (size_t)r0 * maxw; };
-  auto Tt = [&](int l) { return act + (size_t)(nh + l) * plane + (size_t)r0 * maxw; };
-  auto Yb = [&](int l) { return fitb + (size_t)l * plane + (size_t)r0 * maxw; };
-  auto dPb = [&](int k) { return fitb + (size_t)(nh + k) * plane + (size_t)r0 * maxw; };
-  auto dX = [&](int k) { return gbuf + (size_t)k * plane + (size_t)r0 * maxw; };
-  const int wl = dp.fit_width[nh];
+  auto Yf = [&](int l) { return act + (size_t)l * plane; };
+  auto Tt = [&](int l) { return act + (size_t)(nh + l) * plane; };
+  auto Yb = [&](int l) { return fitb + (size_t)l * plane; };
+  auto dPb = [&](int k) { return fitb + (size_t)(nh + k) * plane; };
+  auto dX = [&](int k) { return gbuf + (size_t)k * plane; };
+  FitGemm base{};
+  base.ntypes = nt;
+  base.tile0[0] = 0;
+  for (int t = 0; t < nt; ++t) {
+    base.row0[t] = dp.type_off[t];
+    base.tile0[t + 1] = base.tile0[t] + ceil_div(dp.type_count[t], 128);
+    base.b_out[t] = dp.fit_bout[t];
+  }
+  base.row0[nt] = dp.type_off[nt];
   for (int l = 0; l < nh; ++l) {
     const int a = dp.fit_width[l], o = dp.fit_width[l + 1];
-    FitGemm g{};
+    FitGemm g = base;
     g.mode = l == nh - 1 ? kFitFwdLast : kFitFwd;
-    g.M = n;
     g.N = o;
     g.K = a;
-    g.A = l == 0 ? Db + (size_t)r0 * dim : Yb(l - 1);
+    g.A = l == 0 ? Db : Yb(l - 1);
     g.lda = l == 0 ? dim : maxw;
-    g.B = dp.fit_Wt[l] + (size_t)t * o * a;
-    g.bias = dp.fit_b[l] + (size_t)t * o;
-    g.idt = dp.fit_idt[l] ? dp.fit_idt[l] + (size_t)t * o : nullptr;
+    g.B = dp.fit_Wt[l];
+    g.bias = dp.fit_b[l];
+    g.idt = dp.fit_idt[l];
     g.skip = (o == a && l > 0) ? 1 : 0;
     g.Xs = l > 0 ? Yf(l - 1) : nullptr;
     g.ldxs = maxw;
@@ -287,9 +295,8 @@ int run_fit_tc(DeepPotImpl& dp, int t, int r0, int n, int nrows, const __nv_bflo
     g.Tt = Tt(l);
     g.ldy = maxw;
     if (g.mode == kFitFwdLast) {
-      g.w_out = dp.fit_wout + (size_t)t * wl;
-      g.b_out = dp.fit_bout[t];
-      g.e_out = e_sorted + r0;
+      g.w_out = dp.fit_wout;
+      g.e_out = e_sorted;
       g.dPb = dPb(0);
     }
     DPGB_TRY(launch_fit_gemm(g, err, st));
@@ -298,17 +305,16 @@ int run_fit_tc(DeepPotImpl& dp, int t, int r0, int n, int nrows, const __nv_bflo
   int cur = 0;
   for (int l = nh - 1; l >= 1; --l) {
     const int a = dp.fit_width[l], o = dp.fit_width[l + 1];
-    FitGemm g{};
+    FitGemm g = base;
     g.mode = kFitBwd;
-    g.M = n;
     g.N = a;
     g.K = o;
     g.A = dPb(cur);
     g.lda = maxw;
-    g.B = dp.fit_Wb[l] + (size_t)t * a * o;
+    g.B = dp.fit_Wb[l];
     if (o == a) {  // skip connection of layer l: gradient of its output passes through
       if (l == nh - 1) {
-        g.dYup = dp.fit_wout + (size_t)t * wl;
+        g.dYup = dp.fit_wout;  // [type][wl] broadcast over rows
         g.lddyup = 0;
       } else {
         g.dYup = dX((cur + 1) & 1);
@@ -318,21 +324,20 @@ int run_fit_tc(DeepPotImpl& dp, int t, int r0, int n, int nrows, const __nv_bflo
     const bool lower_skip = dp.fit_width[l] == dp.fit_width[l - 1];
     g.dXf = lower_skip ? dX(cur) : nullptr;
     g.T_lo = Tt(l - 1);
-    g.idt_lo = dp.fit_idt[l - 1] ? dp.fit_idt[l - 1] + (size_t)t * a : nullptr;
+    g.idt_lo = dp.fit_idt[l - 1];
     g.ldy = maxw;
     g.dPb = dPb(cur ^ 1);
     DPGB_TRY(launch_fit_gemm(g, err, st));
     cur ^= 1;
   }
-  FitGemm g{};
+  FitGemm g = base;
   g.mode = kFitStore;
-  g.M = n;
   g.N = dim;
   g.K = dp.fit_width[1];
   g.A = dPb(cur);
   g.lda = maxw;
-  g.B = dp.fit_Wb[0] + (size_t)t * dim * dp.fit_width[1];
-  g.out = dD + (size_t)r0 * dim;
+  g.B = dp.fit_Wb[0];
+  g.out = dD;
   g.ldo = dim;
   return launch_fit_gemm(g, err, st);
 }
@@ -707,22 +712,21 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   if (fit_tc) {
     DPGB_TRY(dp.ws_fitb.alloc(sizeof(__nv_bfloat16) * (size_t)(dp.fit_nh + 2) * nrows * maxw));
   }
-  for (int t = 0; t < d.ntypes; ++t) {
-    if (dp.type_count[t] == 0) continue;
-    if (fit_tc) {
-      if constexpr (std::is_same<T, float>::value) {
-        DPGB_TRY(run_fit_tc(dp, t, dp.type_off[t], dp.type_count[t], (int)nrows,
-                            reinterpret_cast<const __nv_bfloat16*>(dp.ws_D.ptr), dp.ws_dD.as<float>(),
-                            dp.ws_act.as<float>(), dp.ws_gbuf.as<float>(), dp.ws_fitb.as<__nv_bfloat16>(),
-                            dp.ws_esorted.as<double>(), status + kStatusTimeout, st));
-      }
-      launches += 2 * dp.fit_nh + 1;
-      continue;
+  if (fit_tc) {
+    if constexpr (std::is_same<T, float>::value) {
+      DPGB_TRY(run_fit_tc(dp, (int)nrows, reinterpret_cast<const __nv_bfloat16*>(dp.ws_D.ptr), dp.ws_dD.as<float>(),
+                          dp.ws_act.as<float>(), dp.ws_gbuf.as<float>(), dp.ws_fitb.as<__nv_bfloat16>(),
+                          dp.ws_esorted.as<double>(), status + kStatusTimeout, st));
     }
-    DPGB_TRY(launch_fitting<T>(m.fit, t, dp.type_off[t], dp.type_count[t], (int)nrows, dp.ws_D.as<T>(),
-                               dp.ws_dD.as<T>(), dp.ws_act.as<T>(), dp.ws_gbuf.as<T>(), dp.ws_esorted.as<double>(),
-                               0.0, st));
-    launches += 2 * m.fit.n_hidden + 2;
+    launches += 2 * dp.fit_nh;
+  } else {
+    for (int t = 0; t < d.ntypes; ++t) {
+      if (dp.type_count[t] == 0) continue;
+      DPGB_TRY(launch_fitting<T>(m.fit, t, dp.type_off[t], dp.type_count[t], (int)nrows, dp.ws_D.as<T>(),
+                                 dp.ws_dD.as<T>(), dp.ws_act.as<T>(), dp.ws_gbuf.as<T>(), dp.ws_esorted.as<double>(),
+                                 0.0, st));
+      launches += 2 * m.fit.n_hidden + 2;
+    }
   }
   dp.mark(DPGB_STAGE_FITTING, 1, st);
   dp.mark(DPGB_STAGE_DESC_BWD, 0, st);

@@ -4,9 +4,11 @@
 // (deepmd/pt/model/task/fitting.py:734-899 semantics; hidden layer
 // y = tanh(x W + b) * idt (+ x when the widths match)).
 //
-// One CTA computes a 128-row x (<= 256)-column tile; K is staged in chunks of
-// 64 through two shared-memory buffers so that the loads of chunk k+1 overlap
-// the MMAs of chunk k.
+// One launch covers the rows of every atom type (each 128-row tile belongs to
+// one type and uses that type's weights).  A CTA computes a 128 x BN tile; K is
+// streamed in chunks of 64 through an S-stage cp.async ring so that loads run
+// ahead of the MMAs; each stage is released when the MMAs reading it commit.
+// The epilogue stores 16 consecutive columns per thread (64-byte segments).
 #include "fit_tc.cuh"
 #include "tc.cuh"
 
@@ -14,7 +16,6 @@ namespace dpgb {
 namespace {
 
 constexpr int kKC = 64;
-constexpr int kNT = 256;
 
 __device__ __forceinline__ float tanh_fast(float x) {
   float y;
@@ -22,73 +23,127 @@ __device__ __forceinline__ float tanh_fast(float x) {
   return y;
 }
 
-// stage rows [0, nrows) x K-chunk [k0, k0+kc) of a row-major bf16 matrix
-__device__ __forceinline__ void stage(unsigned char* dst, const __nv_bfloat16* src, int ld, int nrows, int rows_valid,
-                                      int k0, int kc) {
-  const int per = kc / 8;
-  for (int q = threadIdx.x; q < nrows * per; q += blockDim.x) {
-    const int r = q / per, c8 = q - r * per;
-    uint4 v = make_uint4(0, 0, 0, 0);
-    if (r < rows_valid) v = __ldg(reinterpret_cast<const uint4*>(src + (size_t)r * ld + k0 + c8 * 8));
-    *reinterpret_cast<uint4*>(dst + tc::cm_offset(r, c8 * 8, kc)) = v;
-  }
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+__device__ __forceinline__ void ld16f(const float* p, float* v) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float4 x = q[i];
+    v[4 * i] = x.x;
+    v[4 * i + 1] = x.y;
+    v[4 * i + 2] = x.z;
+    v[4 * i + 3] = x.w;
+  }
+}
+__device__ __forceinline__ void st16f(float* p, const float* v) {
+  float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+__device__ __forceinline__ void st16b(__nv_bfloat16* p, const float* v) {
+  __nv_bfloat162 h[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+  uint4* q = reinterpret_cast<uint4*>(p);
+  q[0] = *reinterpret_cast<uint4*>(&h[0]);
+  q[1] = *reinterpret_cast<uint4*>(&h[4]);
+}
+
+template <int BN, int S>
 __global__ void __launch_bounds__(128)
 fit_gemm_kernel(FitGemm g, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ uint64_t bar[2];
+  __shared__ uint64_t bar[S];
   __shared__ uint32_t s_tmem;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * 128;
-  const int n0 = blockIdx.y * kNT;
-  const int nt = min(kNT, g.N - n0);  // multiple of 16
-  const int rows_valid = min(128, g.M - m0);
-  unsigned char* sA[2] = {smem, smem + 128 * kKC * 2};
-  unsigned char* sB[2] = {smem + 2 * 128 * kKC * 2, smem + 2 * 128 * kKC * 2 + kNT * kKC * 2};
-  if (warp == 0) tc::tmem_alloc(&s_tmem, 256);
-  if (threadIdx.x == 0) {
-    tc::mbar_init(&bar[0], 1);
-    tc::mbar_init(&bar[1], 1);
-  }
+  constexpr int SA = 128 * kKC * 2, SB = BN * kKC * 2;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  int t = 0;
+  while (t + 1 < g.ntypes && g.tile0[t + 1] <= (int)blockIdx.x) ++t;
+  const int m0 = g.row0[t] + ((int)blockIdx.x - g.tile0[t]) * 128;
+  const int rows_valid = min(128, g.row0[t + 1] - m0);
+  const int n0 = blockIdx.y * BN;
+  const int nt = min(BN, g.N - n0);  // multiple of 16
+  if (warp == 0) tc::tmem_alloc(&s_tmem, BN < 32 ? 32 : BN);
+  if (tid == 0)
+    for (int s = 0; s < S; ++s) tc::mbar_init(&bar[s], 1);
   __syncthreads();
   tc::fence_after();
   const uint32_t tbase = s_tmem;
   const uint32_t idesc = tc::idesc_bf16_f32(128, nt);
   const __nv_bfloat16* A = g.A + (size_t)m0 * g.lda;
-  const __nv_bfloat16* B = g.B + (size_t)n0 * g.K;
-  uint32_t phase[2] = {0, 0};
-  bool ok = true;
+  const __nv_bfloat16* B = g.B + ((size_t)t * g.N + n0) * g.K;
   const int nchunk = (g.K + kKC - 1) / kKC;
-  for (int i = 0; i < nchunk; ++i) {
-    const int b = i & 1;
-    const int k0 = i * kKC, kc = min(kKC, g.K - k0);
-    if (i >= 2) {  // the MMAs of chunk i-2 read this buffer
-      ok = tc::mbar_wait(&bar[b], phase[b], err) && ok;
-      phase[b] ^= 1;
+  auto load = [&](int i) {
+    unsigned char* sa = smem + (i % S) * (SA + SB);
+    unsigned char* sb = sa + SA;
+    const int k0 = i * kKC, kc = min(kKC, g.K - k0), per = kc / 8;
+    for (int q = tid; q < 128 * per; q += 128) {
+      const int r = q / per, c8 = q - r * per;
+      const bool in = r < rows_valid;
+      cp_async16(sa + tc::cm_offset(r, c8 * 8, kc), in ? (const void*)(A + (size_t)r * g.lda + k0 + c8 * 8) : (const void*)A,
+                 in ? 16 : 0);
     }
-    stage(sA[b], A, g.lda, 128, rows_valid, k0, kc);
-    stage(sB[b], B, g.K, nt, nt, k0, kc);
+    for (int q = tid; q < nt * per; q += 128) {
+      const int r = q / per, c8 = q - r * per;
+      cp_async16(sb + tc::cm_offset(r, c8 * 8, kc), B + (size_t)r * g.K + k0 + c8 * 8, 16);
+    }
+  };
+#pragma unroll
+  for (int i = 0; i < S - 1; ++i) {
+    if (i < nchunk) load(i);
+    cp_commit();
+  }
+  bool pending[S];
+  uint32_t phase[S];
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    pending[s] = false;
+    phase[s] = 0;
+  }
+  bool ok = true;
+  for (int i = 0; i < nchunk; ++i) {
+    const int s = i % S;
+    cp_wait<S - 2>();
     tc::fence_async_smem();
     __syncthreads();
     tc::fence_after();
-    if (threadIdx.x == 0) {
-      const uint32_t a0 = tc::smem_u32(sA[b]), b0 = tc::smem_u32(sB[b]);
+    if (tid == 0) {
+      const int kc = min(kKC, g.K - i * kKC);
+      const uint32_t a0 = tc::smem_u32(smem + s * (SA + SB)), b0 = a0 + SA;
       const uint32_t sbo = (uint32_t)(kc / 8) * 128;
       for (int ks = 0; ks < kc / 16; ++ks)
         tc::mma_bf16(tbase, tc::smem_desc(a0 + ks * 256, 128, sbo), tc::smem_desc(b0 + ks * 256, 128, sbo), idesc,
                      (i > 0 || ks > 0) ? 1u : 0u);
-      tc::mma_commit(&bar[b]);
+      tc::mma_commit(&bar[s]);
     }
-  }
-  // drain: the last commit covers every MMA
-  {
-    const int last = (nchunk - 1) & 1;
-    if (nchunk >= 2) {
-      ok = tc::mbar_wait(&bar[last ^ 1], phase[last ^ 1], err) && ok;
+    pending[s] = true;
+    const int j = i + S - 1;
+    if (j < nchunk) {
+      const int sj = j % S;  // the stage chunk i-1 used
+      if (pending[sj]) {
+        ok = tc::mbar_wait(&bar[sj], phase[sj], err) && ok;
+        phase[sj] ^= 1;
+        pending[sj] = false;
+      }
+      load(j);
     }
-    ok = tc::mbar_wait(&bar[last], phase[last], err) && ok;
+    cp_commit();
   }
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+    if (pending[s]) {
+      ok = tc::mbar_wait(&bar[s], phase[s], err) && ok;
+      phase[s] ^= 1;
+    }
   tc::fence_after();
   ok = __syncthreads_and(ok) != 0;
   if (ok) {
@@ -96,51 +151,84 @@ fit_gemm_kernel(FitGemm g, int* __restrict__ err) {
     const int m = m0 + r;
     const bool valid = r < rows_valid;
     double e_acc = 0.0;
+    const float* bias = g.bias ? g.bias + (size_t)t * g.N : nullptr;
+    const float* idt = g.idt ? g.idt + (size_t)t * g.N : nullptr;
+    const float* idt_lo = g.idt_lo ? g.idt_lo + (size_t)t * g.N : nullptr;
+    const float* wo = g.w_out ? g.w_out + (size_t)t * g.N : nullptr;
     for (int c0 = 0; c0 < nt; c0 += 16) {
       float v[16];
       tc::tmem_ld16(tc::taddr(tbase, warp * 32, c0), v);
       tc::tmem_ld_wait();
       if (!valid) continue;
+      const int n = n0 + c0;
+      if (g.mode == kFitFwd || g.mode == kFitFwdLast) {
+        float bb[16], id[16], xs[16], y[16], tv[16];
+        ld16f(bias + n, bb);
+        if (idt) ld16f(idt + n, id);
+        if (g.skip) ld16f(g.Xs + (size_t)m * g.ldxs + n, xs);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int n = n0 + c0 + i;
-        const float acc = v[i];
-        if (g.mode == kFitFwd || g.mode == kFitFwdLast) {
-          const float tv = tanh_fast(acc + g.bias[n]);
-          float y = g.idt ? tv * g.idt[n] : tv;
-          if (g.skip) y += g.Xs[(size_t)m * g.ldxs + n];
-          if (g.mode == kFitFwd) {
-            g.Yf[(size_t)m * g.ldy + n] = y;
-            g.Yb[(size_t)m * g.ldy + n] = __float2bfloat16_rn(y);
-            g.Tt[(size_t)m * g.ldy + n] = tv;
-          } else {
-            e_acc += (double)y * (double)g.w_out[n];
-            const float dp = g.w_out[n] * (g.idt ? g.idt[n] : 1.f) * (1.f - tv * tv);
-            g.dPb[(size_t)m * g.ldy + n] = __float2bfloat16_rn(dp);
-          }
-        } else if (g.mode == kFitBwd) {
-          float dx = acc;
-          if (g.dYup) dx += g.dYup[(size_t)m * g.lddyup + n];
-          if (g.dXf) g.dXf[(size_t)m * g.ldy + n] = dx;
-          const float tl = g.T_lo[(size_t)m * g.ldy + n];
-          const float dp = dx * (g.idt_lo ? g.idt_lo[n] : 1.f) * (1.f - tl * tl);
-          g.dPb[(size_t)m * g.ldy + n] = __float2bfloat16_rn(dp);
-        } else {
-          g.out[(size_t)m * g.ldo + n] = acc;
+        for (int i = 0; i < 16; ++i) {
+          tv[i] = tanh_fast(v[i] + bb[i]);
+          y[i] = idt ? tv[i] * id[i] : tv[i];
+          if (g.skip) y[i] += xs[i];
         }
+        if (g.mode == kFitFwd) {
+          st16f(g.Yf + (size_t)m * g.ldy + n, y);
+          st16f(g.Tt + (size_t)m * g.ldy + n, tv);
+          st16b(g.Yb + (size_t)m * g.ldy + n, y);
+        } else {
+          float w[16], dp[16];
+          ld16f(wo + n, w);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            e_acc += (double)y[i] * (double)w[i];
+            dp[i] = w[i] * (idt ? id[i] : 1.f) * (1.f - tv[i] * tv[i]);
+          }
+          st16b(g.dPb + (size_t)m * g.ldy + n, dp);
+        }
+      } else if (g.mode == kFitBwd) {
+        float dx[16], up[16], tl[16], il[16], dp[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dx[i] = v[i];
+        if (g.dYup) {
+          ld16f(g.lddyup ? g.dYup + (size_t)m * g.lddyup + n : g.dYup + (size_t)t * g.N + n, up);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) dx[i] += up[i];
+        }
+        if (g.dXf) st16f(g.dXf + (size_t)m * g.ldy + n, dx);
+        ld16f(g.T_lo + (size_t)m * g.ldy + n, tl);
+        if (idt_lo) ld16f(idt_lo + n, il);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dp[i] = dx[i] * (idt_lo ? il[i] : 1.f) * (1.f - tl[i] * tl[i]);
+        st16b(g.dPb + (size_t)m * g.ldy + n, dp);
+      } else {
+        st16f(g.out + (size_t)m * g.ldo + n, v);
       }
     }
-    if (g.mode == kFitFwdLast && valid) g.e_out[m] = e_acc + (double)g.b_out;
+    if (g.mode == kFitFwdLast && valid) g.e_out[m] = e_acc + (double)g.b_out[t];
   }
   tc::fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, 256);
+  if (warp == 0) tc::tmem_dealloc(tbase, BN < 32 ? 32 : BN);
+}
+
+template <int BN, int S>
+int launch_t(const FitGemm& g, int* err, cudaStream_t st) {
+  const size_t smem = (size_t)S * (128 + BN) * kKC * 2;
+  static bool attr = false;
+  if (!attr) {
+    DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel<BN, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  dim3 grid(g.tile0[g.ntypes], ceil_div(g.N, BN));
+  fit_gemm_kernel<BN, S><<<grid, 128, smem, st>>>(g, err);
+  return check_launch("fit_gemm");
 }
 
 }  // namespace
 
 int fit_tc_eligible(const dpgb_se_a_desc& d) {
-  if (d.dim_descrpt % 16) return 0;
+  if (d.dim_descrpt % 16 || d.ntypes > 8) return 0;
   int nin = d.dim_descrpt;
   for (int l = 0; l < d.n_fit; ++l) {
     const int w = d.fit_neuron[l];
@@ -152,16 +240,9 @@ int fit_tc_eligible(const dpgb_se_a_desc& d) {
 }
 
 int launch_fit_gemm(const FitGemm& g, int* err, cudaStream_t st) {
-  if (g.M <= 0) return DPGB_OK;
-  const size_t smem = (size_t)2 * (128 + kNT) * kKC * 2;
-  static bool attr = false;
-  if (!attr) {
-    DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
-  dim3 grid(ceil_div(g.M, 128), ceil_div(g.N, kNT));
-  fit_gemm_kernel<<<grid, 128, smem, st>>>(g, err);
-  return check_launch("fit_gemm");
+  if (g.tile0[g.ntypes] <= 0) return DPGB_OK;
+  if (g.mode == kFitFwdLast) return launch_t<256, 3>(g, err, st);  // the output layer needs whole rows
+  return launch_t<128, 3>(g, err, st);
 }
 
 }  // namespace dpgb

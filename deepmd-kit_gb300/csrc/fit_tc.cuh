@@ -9,15 +9,22 @@ namespace dpgb {
 
 enum FitMode { kFitFwd = 0, kFitFwdLast = 1, kFitBwd = 2, kFitStore = 3 };
 
-// One GEMM  acc[M, N] = A[M, K] . B^T  (A bf16 row-major with leading
-// dimension lda, B bf16 [N, K] row-major) and its epilogue:
-//  kFitFwd:     t = tanh(acc + bias); y = t*idt (+ Xs); Yf, Yb (bf16), Tt = t
-//  kFitFwdLast: as kFitFwd, then e = y . w_out + b_out, dPb = w_out*idt*(1-t^2)
-//  kFitBwd:     dx = acc (+ dYup); dXf = dx; dPb = dx*idt_lo*(1 - T_lo^2)
+// One GEMM over the type-sorted rows of all atom types (type t owns sorted
+// rows [row0[t], row0[t+1]) and uses its own weights):
+//   acc[m, n] = A[m, :] . B_t[n, :]      (A bf16 [rows, lda], B_t bf16 [N, K])
+// and its epilogue:
+//  kFitFwd:     t = tanh(acc + bias_t); y = t*idt_t (+ Xs); Yf, Yb (bf16), Tt = t
+//  kFitFwdLast: as kFitFwd, then e = y . w_out_t + b_out[t],
+//               dPb = w_out_t * idt_t * (1 - t^2)        (needs N <= 256)
+//  kFitBwd:     dx = acc (+ dYup); dXf = dx; dPb = dx * idt_lo_t * (1 - T_lo^2)
 //  kFitStore:   out = acc
+// Per-type parameter arrays are laid out [type][N] (B: [type][N][K]).
 struct FitGemm {
   int mode;
-  int M, N, K, lda;
+  int N, K, lda;
+  int ntypes;
+  int row0[9];   // sorted-row offsets of the types
+  int tile0[9];  // prefix of 128-row tiles per type
   const __nv_bfloat16* A;
   const __nv_bfloat16* B;
   const float* bias;
@@ -28,11 +35,11 @@ struct FitGemm {
   __nv_bfloat16* Yb;
   float* Tt;
   int ldy;
-  const float* w_out;
-  float b_out;
+  const float* w_out;  // [type][N]
+  float b_out[8];
   double* e_out;
   __nv_bfloat16* dPb;
-  const float* dYup;
+  const float* dYup;   // [rows][lddyup], or w_out-like [type][N] when lddyup == 0
   int lddyup;
   float* dXf;
   const float* idt_lo;
