@@ -691,13 +691,16 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     if (tc_path) {
       const int nsorted = dp.type_off[d.ntypes];
       DPGB_TRY(dp.ws_runlen.alloc(sizeof(int) * (size_t)std::max(nsorted, 1) * d.ntypes));
-      DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ng));
+      // one buffer serves the per-section partial xyz of the forward and,
+      // after it, dE/dxyz of the backward
+      DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ng * d.ntypes));
       DPGB_TRY(launch_run_lengths(dp.ws_runlen.as<int>(), nlist, dp.sorted_rows_dev.as<int>(), nsorted, nnei, dp.sel,
                                   dp.pad_zero, st));
       EmbTC e = dp.tc;
       e.d_bf16 = dp.use_fit_tc;
       DPGB_TRY(launch_emb_tc_fwd(p, e, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.ws_runlen.as<int>(),
-                                 dp.sorted_rows_dev.as<int>(), dp.ws_xyz.as<float>(), dp.ws_D.as<float>(), status, st));
+                                 dp.sorted_rows_dev.as<int>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(),
+                                 dp.ws_D.as<float>(), status, st));
       launches += 2;
     }
   }

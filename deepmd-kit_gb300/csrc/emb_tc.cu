@@ -243,10 +243,29 @@ __device__ __forceinline__ void env_deriv(const float d[3], float rmin, float rm
 
 // ---------------------------------------------------------------------------
 // shared-memory plan (bytes), identical for forward and backward where shared
+constexpr int kFinAtoms = 4;  // atoms finalised together (xyz -> D) in the forward
+constexpr int kBwdAtoms = 8;  // atoms per tile in the backward
+
+// shared-memory plans (bytes); both fit two CTAs per SM for the 25/50/100 net
 template <int W1, int W2, int W3>
-struct Plan {
+struct PlanF {
   static constexpr int K1 = (W1 + 15) / 16 * 16, N2 = (W2 + 15) / 16 * 16, N3 = (W3 + 15) / 16 * 16;
   static constexpr int LDG = W3 + 1;  // fp32 G row stride (odd: no bank conflicts)
+  static constexpr int VEC = 3 * K1 + 2 * N2 + 2 * N3;
+  static constexpr int fw2 = 0;
+  static constexpr int fw3 = fw2 + N2 * K1 * 2;
+  static constexpr int a1 = fw3 + N3 * N2 * 2;
+  static constexpr int a2 = a1 + 128 * K1 * 2;
+  static constexpr int gbuf = a2 + 128 * N2 * 2;  // G (fp32)
+  static constexpr int rn = gbuf + 128 * LDG * 4;
+  static constexpr int vec = rn + 128 * 4 * 4;
+  static constexpr int xs = vec + VEC * 4;  // finalize staging of kFinAtoms xyz
+  static constexpr int total = xs + kFinAtoms * 4 * W3 * 4;
+  static constexpr int tmem_cols = (N2 + N3 <= 256) ? 256 : 512;
+};
+template <int W1, int W2, int W3>
+struct PlanB {
+  static constexpr int K1 = (W1 + 15) / 16 * 16, N2 = (W2 + 15) / 16 * 16, N3 = (W3 + 15) / 16 * 16;
   static constexpr int VEC = 3 * K1 + 2 * N2 + 2 * N3;
   static constexpr int fw2 = 0;
   static constexpr int fw3 = fw2 + N2 * K1 * 2;
@@ -254,23 +273,20 @@ struct Plan {
   static constexpr int bw2 = bw3 + N2 * N3 * 2;
   static constexpr int a1 = bw2 + K1 * N2 * 2;
   static constexpr int a2 = a1 + 128 * K1 * 2;
-  static constexpr int a3 = a2 + 128 * N2 * 2;           // backward dP3 operand
-  static constexpr int gbuf = a3 + 128 * N3 * 2;         // forward G (fp32) / backward dxyz of tile atoms
-  static constexpr int gbytes_f = 128 * LDG * 4;
-  static constexpr int gbytes_b = kTcMaxAtoms * 4 * W3 * 4;
-  static constexpr int rn = gbuf + (gbytes_f > gbytes_b ? gbytes_f : gbytes_b);
-  static constexpr int vec = rn + 128 * 4 * 4;
-  static constexpr int vir = vec + VEC * 4;                // backward per-pair virial (double)
-  static constexpr int total = vir + 128 * 9 * 8;
+  static constexpr int a3 = a2 + 128 * N2 * 2;  // dP3 operand
+  static constexpr int gbuf = a3 + 128 * N3 * 2;  // dxyz of the tile atoms
+  static constexpr int vec = gbuf + kBwdAtoms * 4 * W3 * 4;
+  static constexpr int vir = vec + VEC * 4;  // per-pair virial (fp32)
+  static constexpr int total = vir + 128 * 9 * 4;
   static constexpr int tmem_cols = (N2 + N3 <= 256) ? 256 : 512;
 };
 
 template <int W1, int W2, int W3>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 2)
 emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ chunks, int nchunks,
                   const int* __restrict__ run_len, const int* __restrict__ sorted_rows, float* __restrict__ xyz,
-                  float* __restrict__ Dout, int* __restrict__ status) {
-  using P = Plan<W1, W2, W3>;
+                  float* __restrict__ xyzp, float* __restrict__ Dout, int* __restrict__ status) {
+  using P = PlanF<W1, W2, W3>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
   __shared__ uint32_t s_tmem;
@@ -292,11 +308,9 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
   for (int c = blockIdx.x; c < nchunks && alive; c += gridDim.x) {
     const WorkChunk ch = chunks[c];
     const int ti = ch.ti;
-    for (int q = tid; q < (ch.row1 - ch.row0) * 4 * ng; q += blockDim.x)
-      xyz[(size_t)sorted_rows[ch.row0 + q / (4 * ng)] * 4 * ng + q % (4 * ng)] = 0.f;
-    __syncthreads();
     for (int t = 0; t < p.ntypes && alive; ++t) {
       const int net = p.type_one_side ? t : t * p.ntypes + ti;
+      float* xpart = xyzp + (size_t)t * p.nrows * 4 * ng;  // this section's partial xyz
       copy16(smem + P::fw2, e.fw2 + (size_t)net * P::N2 * P::K1 * 2, P::N2 * P::K1 * 2);
       copy16(smem + P::fw3, e.fw3 + (size_t)net * P::N3 * P::N2 * 2, P::N3 * P::N2 * 2);
       for (int q = tid; q < P::VEC; q += blockDim.x) sV[q] = e.vec[(size_t)net * P::VEC + q];
@@ -422,35 +436,48 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         tc::fence_before();
         alive = __syncthreads_and(ok) != 0;
         if (!alive) break;
-        // xyz[atom][c][n] += sum_{pairs of the atom} Rn[c] G[n]  (FP32, fixed order)
+        // partial xyz of this section: sum_{pairs of the atom} Rn[c] G[n]
+        // (FP32, fixed order; plain stores, the atom is owned by this CTA)
         for (int q = tid; q < ntile * 4 * W3; q += blockDim.x) {
           const int k = q / (4 * W3), rem = q - k * 4 * W3, cc = rem / W3, n = rem - cc * W3;
           float s = 0.f;
           for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) s = fmaf(sRn[pp * 4 + cc], sG[pp * P::LDG + n], s);
-          float* dst = xyz + (size_t)s_row[k] * 4 * ng + cc * ng + n;
-          *dst += s;
+          xpart[(size_t)s_row[k] * 4 * ng + cc * ng + n] = s;
         }
         __syncthreads();
       }
     }
-    // finalize the chunk: D = (xyz/nnei)^T (xyz/nnei)[:, :axis], then scale xyz
+    // finalize the chunk, kFinAtoms atoms at a time: xyz = sum over sections
+    // / nnei (staged in shared memory), D = xyz^T xyz[:, :axis]
     const float inv = 1.f / (float)p.nnei;
     const int dim = ng * p.axis;
-    __syncthreads();
-    for (int q = tid; q < (ch.row1 - ch.row0) * dim; q += blockDim.x) {
-      const int r = ch.row0 + q / dim, rem = q % dim, n = rem / p.axis, m = rem - n * p.axis;
-      const float* xr = xyz + (size_t)sorted_rows[r] * 4 * ng;
-      float s = 0.f;
+    float* sX = reinterpret_cast<float*>(smem + P::xs);
+    for (int r0 = ch.row0; r0 < ch.row1; r0 += kFinAtoms) {
+      const int nr = min(kFinAtoms, ch.row1 - r0);
+      __syncthreads();
+      for (int q = tid; q < nr * 4 * ng; q += blockDim.x) {
+        const int a = q / (4 * ng), qq = q - a * 4 * ng;
+        const int r = r0 + a, row = sorted_rows[r];
+        float s = 0.f;
+        for (int t = 0; t < p.ntypes; ++t)
+          if (run_len[(size_t)r * p.ntypes + t] > 0) s += xyzp[((size_t)t * p.nrows + row) * 4 * ng + qq];
+        s *= inv;
+        sX[q] = s;
+        xyz[(size_t)row * 4 * ng + qq] = s;
+      }
+      __syncthreads();
+      for (int q = tid; q < nr * dim; q += blockDim.x) {
+        const int a = q / dim, rem = q - a * dim, n = rem / p.axis, m = rem - n * p.axis;
+        const float* xr = sX + a * 4 * ng;
+        float s = 0.f;
 #pragma unroll
-      for (int cc = 0; cc < 4; ++cc) s = fmaf(xr[cc * ng + n], xr[cc * ng + m], s);
-      if (e.d_bf16)  // the tensor-core fitting reads D as BF16
-        reinterpret_cast<__nv_bfloat16*>(Dout)[(size_t)r * dim + rem] = __float2bfloat16_rn(s * inv * inv);
-      else
-        Dout[(size_t)r * dim + rem] = s * inv * inv;
+        for (int cc = 0; cc < 4; ++cc) s = fmaf(xr[cc * ng + n], xr[cc * ng + m], s);
+        if (e.d_bf16)  // the tensor-core fitting reads D as BF16
+          reinterpret_cast<__nv_bfloat16*>(Dout)[(size_t)(r0 + a) * dim + rem] = __float2bfloat16_rn(s);
+        else
+          Dout[(size_t)(r0 + a) * dim + rem] = s;
+      }
     }
-    __syncthreads();
-    for (int q = tid; q < (ch.row1 - ch.row0) * 4 * ng; q += blockDim.x)
-      xyz[(size_t)sorted_rows[ch.row0 + q / (4 * ng)] * 4 * ng + q % (4 * ng)] *= inv;
     __syncthreads();
   }
   tc::fence_before();
@@ -460,16 +487,16 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 
 // ---------------------------------------------------------------------------
 template <int W1, int W2, int W3>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 2)
 emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ chunks, int nchunks,
                   const int* __restrict__ run_len, const int* __restrict__ sorted_rows,
                   const float* __restrict__ dxyz, float* __restrict__ gpair, double* __restrict__ vir_row,
                   int* __restrict__ status) {
-  using P = Plan<W1, W2, W3>;
+  using P = PlanB<W1, W2, W3>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
   __shared__ uint32_t s_tmem;
-  __shared__ int s_row[kTcMaxAtoms], s_off[kTcMaxAtoms + 1], s_ntile, s_cursor;
+  __shared__ int s_row[kBwdAtoms], s_off[kBwdAtoms + 1], s_ntile, s_cursor;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int ng = p.ng;
   if (warp == 0) tc::tmem_alloc(&s_tmem, P::tmem_cols);
@@ -479,9 +506,9 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
   const uint32_t tbase = s_tmem;
   uint32_t phase = 0;
   bool alive = true;
-  float* sDX = reinterpret_cast<float*>(smem + P::gbuf);  // [kTcMaxAtoms][4][W3]
+  float* sDX = reinterpret_cast<float*>(smem + P::gbuf);  // [kBwdAtoms][4][W3]
   float* sV = reinterpret_cast<float*>(smem + P::vec);
-  double* sVir = reinterpret_cast<double*>(smem + P::vir);
+  float* sVir = reinterpret_cast<float*>(smem + P::vir);
   const uint32_t sA1 = tc::smem_u32(smem + P::a1), sA2 = tc::smem_u32(smem + P::a2), sA3 = tc::smem_u32(smem + P::a3);
   const uint32_t sW2 = tc::smem_u32(smem + P::fw2), sW3 = tc::smem_u32(smem + P::fw3);
   const uint32_t sB3 = tc::smem_u32(smem + P::bw3), sB2 = tc::smem_u32(smem + P::bw2);
@@ -511,7 +538,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
       while (alive) {
         if (tid == 0) {
           int cur = s_cursor, n = 0, pairs = 0;
-          while (cur < ch.row1 && n < kTcMaxAtoms) {
+          while (cur < ch.row1 && n < kBwdAtoms) {
             const int len = run_len[(size_t)cur * p.ntypes + t];
             if (len == 0) {
               ++cur;
@@ -721,14 +748,14 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 #pragma unroll
         for (int k = 0; k < 3; ++k)
 #pragma unroll
-          for (int l = 0; l < 3; ++l) sVir[tid * 9 + 3 * k + l] = -(double)g[k] * (double)dv[l];
+          for (int l = 0; l < 3; ++l) sVir[tid * 9 + 3 * k + l] = -g[k] * dv[l];
         tc::fence_before();
         alive = __syncthreads_and(ok) != 0;
         if (!alive) break;
         for (int q = tid; q < ntile * 9; q += blockDim.x) {
           const int k = q / 9, comp = q - 9 * k;
           double s = 0.0;
-          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) s += sVir[pp * 9 + comp];
+          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) s += (double)sVir[pp * 9 + comp];
           vir_row[(size_t)s_row[k] * 9 + comp] += s;
         }
         __syncthreads();
@@ -785,19 +812,19 @@ __global__ void dxyz_kernel(float* __restrict__ dxyz, const float* __restrict__ 
 
 template <int W1, int W2, int W3>
 int launch_fwd_t(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks, const int* run_len,
-                 const int* sorted_rows, float* xyz, float* D, int* status, cudaStream_t st, int nsm) {
-  using P = Plan<W1, W2, W3>;
+                 const int* sorted_rows, float* xyz, float* xyzp, float* D, int* status, cudaStream_t st, int nsm) {
+  using P = PlanF<W1, W2, W3>;
   auto k = emb_tc_fwd_kernel<W1, W2, W3>;
   DPGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, P::total));
   const int grid = nchunks < nsm ? nchunks : nsm;
-  k<<<grid, 128, P::total, st>>>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, D, status);
+  k<<<grid, 128, P::total, st>>>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status);
   return check_launch("emb_tc_fwd");
 }
 template <int W1, int W2, int W3>
 int launch_bwd_t(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks, const int* run_len,
                  const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, int* status, cudaStream_t st,
                  int nsm) {
-  using P = Plan<W1, W2, W3>;
+  using P = PlanB<W1, W2, W3>;
   auto k = emb_tc_bwd_kernel<W1, W2, W3>;
   DPGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, P::total));
   const int grid = nchunks < nsm ? nchunks : nsm;
@@ -827,13 +854,14 @@ int launch_run_lengths(int* run_len, const int* nlist, const int* sorted_rows, i
 }
 
 int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks,
-                      const int* run_len, const int* sorted_rows, float* xyz, float* D, int* status, cudaStream_t st) {
+                      const int* run_len, const int* sorted_rows, float* xyz, float* xyzp, float* D, int* status,
+                      cudaStream_t st) {
   if (nchunks <= 0) return DPGB_OK;
   const int nsm = 2 * sm_count();
   if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100)
-    return launch_fwd_t<25, 50, 100>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, D, status, st, nsm);
+    return launch_fwd_t<25, 50, 100>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status, st, nsm);
   if (e.w1 == 3 && e.w2 == 6 && e.w3 == 12)
-    return launch_fwd_t<3, 6, 12>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, D, status, st, nsm);
+    return launch_fwd_t<3, 6, 12>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status, st, nsm);
   return fail(DPGB_EINVAL, "embedding widths without a tensor-core kernel");
 }
 

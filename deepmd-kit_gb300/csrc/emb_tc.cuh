@@ -45,8 +45,9 @@ size_t emb_tc_image_bytes(const EmbTC& m, int kind);  // per net: 0 fw2, 1 fw3, 
 
 int launch_run_lengths(int* run_len, const int* nlist, const int* sorted_rows, int nrows, int nnei,
                        const SelInfo& sel, int pad_zero, cudaStream_t st);
+// xyzp: per-section partial xyz, [ntypes][nrows][4][ng] FP32 scratch
 int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks,
-                      const int* run_len, const int* sorted_rows, float* xyz, float* D, int* status,
+                      const int* run_len, const int* sorted_rows, float* xyz, float* xyzp, float* D, int* status,
                       cudaStream_t st);
 int launch_dxyz(const DescParams<float>& p, const float* dD, const float* xyz, float* dxyz, cudaStream_t st);
 int launch_emb_tc_bwd(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks,
