@@ -509,16 +509,44 @@ int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host
     for (int i = 0; i < natom; ++i)
       if (atype_host[i] >= 0) sorted_rows[dp.row_pos_h[(size_t)f * natom + i]] = f * natom + i;
   // work chunks of the tensor-core embedding: contiguous sorted rows of one
-  // centre type, about two chunks per SM
+  // centre type.  The embedding kernels run one CTA per chunk with two CTAs
+  // per SM, so the rows are cut into at most 2 x SMs chunks of near-equal
+  // size (a CTA that had to take a second chunk would double the launch).
   std::vector<WorkChunk> chunks;
   {
     int dev = 0, nsm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int target = std::max(1, nsorted / std::max(1, 2 * nsm));
-    for (int t = 0; t < nt; ++t)
-      for (int r = dp.type_off[t]; r < dp.type_off[t + 1]; r += target)
-        chunks.push_back(WorkChunk{r, std::min(r + target, dp.type_off[t + 1]), t, 0});
+    const int slots = std::max(1, 2 * nsm);
+    std::vector<int> per(nt, 0);
+    std::vector<double> rem(nt, 0.0);
+    int used = 0;
+    for (int t = 0; t < nt; ++t) {
+      const int n = dp.type_off[t + 1] - dp.type_off[t];
+      if (n <= 0) continue;
+      const double share = nsorted > 0 ? (double)slots * n / nsorted : 0.0;
+      per[t] = std::max(1, std::min(n, (int)share));
+      rem[t] = share - per[t];
+      used += per[t];
+    }
+    while (used < slots) {  // largest remainder first
+      int best = -1;
+      for (int t = 0; t < nt; ++t) {
+        const int n = dp.type_off[t + 1] - dp.type_off[t];
+        if (per[t] < n && (best < 0 || rem[t] > rem[best])) best = t;
+      }
+      if (best < 0) break;
+      ++per[best];
+      rem[best] -= 1.0;
+      ++used;
+    }
+    for (int t = 0; t < nt; ++t) {
+      const int r0 = dp.type_off[t], n = dp.type_off[t + 1] - r0;
+      for (int k = 0; k < per[t]; ++k) {
+        const int a = r0 + (int)((long long)k * n / per[t]), b = r0 + (int)((long long)(k + 1) * n / per[t]);
+        if (b > a) chunks.push_back(WorkChunk{a, b, t, 0});
+      }
+    }
   }
   dp.nchunks = (int)chunks.size();
   DPGB_TRY(dp.row_pos_dev.alloc(sizeof(int) * dp.row_pos_h.size()));
