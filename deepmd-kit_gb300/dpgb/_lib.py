@@ -60,6 +60,21 @@ class SeADesc(C.Structure):
     ]
 
 
+class SeABlock(C.Structure):
+    """dpgb_se_a_block of include/dpgb.h."""
+
+    _fields_ = [
+        ("ntypes", C.c_int),
+        ("sel", C.c_int * MAX_TYPES),
+        ("type_one_side", C.c_int),
+        ("n_layer", C.c_int),
+        ("neuron", C.c_int * MAX_LAYERS),
+        ("axis_neuron", C.c_int),
+        ("resnet_dt", C.c_int),
+        ("pair_keep", C.c_int * ((MAX_TYPES + 1) * (MAX_TYPES + 1))),
+    ]
+
+
 # name -> argtypes (all return int unless listed in _RESTYPE)
 _SIGS = {
     "dpgb_last_error": [],
@@ -76,6 +91,22 @@ _SIGS = {
     "dpgb_extend_coord": [_P, _P, _P, _P, _P, _I, _DP, _IP, _I, _P],
     "dpgb_prod_env_mat_a_f64": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _P, _P, _I, _I, _D, _D, _IP, _I, _P],
     "dpgb_env_mat_pt_f64": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _P],
+    "dpgb_env_mat_pt2_f64": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _D, _P],
+    "dpgb_env_mat_pt2_f32": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _D, _P],
+    "dpgb_env_mat_pt_bwd_f64": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _D, _P],
+    "dpgb_env_mat_pt_bwd_f32": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _D, _P],
+    "dpgb_env_mat_pt_bwd_bwd_f64": [_P] * 12 + [_I, _I, _I, _I, _D, _D, _D, _P],
+    "dpgb_env_mat_pt_bwd_bwd_f32": [_P] * 12 + [_I, _I, _I, _I, _D, _D, _D, _P],
+    "dpgb_se_a_table_rows": [_D, _D, _D, _D, _D],
+    "dpgb_se_a_table_build_f64": [_P, _P, _P, _I, _D, _D, _D, _D, _D, _P],
+    "dpgb_se_a_block_param_count": [_P],
+    "dpgb_se_a_block_workspace_bytes": [_P, _I, _I, _I],
+    "dpgb_se_a_block_fwd_f64": [_P, _P, _P, _P, _P, _I, _I, _I, _P, _P, _P],
+    "dpgb_se_a_block_fwd_f32": [_P, _P, _P, _P, _P, _I, _I, _I, _P, _P, _P],
+    "dpgb_se_a_block_bwd_f64": [_P, _P, _P, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, C.c_size_t, _P],
+    "dpgb_se_a_block_bwd_f32": [_P, _P, _P, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P, _P, C.c_size_t, _P],
+    "dpgb_se_a_block_bwd_bwd_f64": [_P, _P, _P, _P, _P, _I, _I, _I] + [_P] * 8 + [C.c_size_t, _P],
+    "dpgb_se_a_block_bwd_bwd_f32": [_P, _P, _P, _P, _P, _I, _I, _I] + [_P] * 8 + [C.c_size_t, _P],
     "dpgb_prod_force_a_f64": [_P, _P, _P, _P, _I, _I, _I, _I, _P],
     "dpgb_prod_virial_a_f64": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _P],
     "dpgb_prod_force_a_f64_noalloc": [_P, _P, _P, _P, _I, _I, _I, _I, _P],
@@ -99,6 +130,8 @@ _RESTYPE = {
     "dpgb_deeppot_new": _P,
     "dpgb_deeppot_delete": None,
     "dpgb_deeppot_check_ok": C.c_char_p,
+    "dpgb_se_a_block_param_count": C.c_longlong,
+    "dpgb_se_a_block_workspace_bytes": C.c_size_t,
 }
 EXPORTED = sorted(_SIGS)
 

@@ -156,6 +156,161 @@ int dpgb_env_mat_pt_f64(double* em, double* diff, double* sw,
                         int nf, int nloc, int nall, int nnei, double rcut,
                         double rcut_smth, void* stream);
 
+/* The same with the reference's `protection` (added to the distance in the
+ * 1/r and 1/r^2 factors, env_mat.py:41-43), in FP32 or FP64 (the
+ * descriptor's `precision`), and with the local types atype [nf, nloc] of
+ * the reference signature (env_mat.py:58-70) instead of atype_ext. */
+int dpgb_env_mat_pt2_f64(double* em, double* diff, double* sw,
+                         const double* coord_ext, const int* atype,
+                         const int* nlist, const double* avg, const double* std,
+                         int nf, int nloc, int nall, int nnei, double rcut,
+                         double rcut_smth, double protection, void* stream);
+int dpgb_env_mat_pt2_f32(float* em, float* diff, float* sw,
+                         const float* coord_ext, const int* atype,
+                         const int* nlist, const float* avg, const float* std,
+                         int nf, int nloc, int nall, int nnei, double rcut,
+                         double rcut_smth, double protection, void* stream);
+
+/* Backward of prod_env_mat with respect to the extended coordinates: the
+ * gradient autograd forms through env_mat.py:18-119.  g_em [nf*nloc, nnei, 4],
+ * g_diff [.., 3] and g_sw [.., 1] (either may be NULL) -> g_coord
+ * [nf, nall, 3] (overwritten).  Pair terms are gathered per atom through a
+ * sorted transpose of the list: no atomics, reproducible. */
+int dpgb_env_mat_pt_bwd_f64(double* g_coord, const double* g_em,
+                            const double* g_diff, const double* g_sw,
+                            const double* coord_ext, const int* atype,
+                            const int* nlist, const double* std, int nf,
+                            int nloc, int nall, int nnei, double rcut,
+                            double rcut_smth, double protection, void* stream);
+int dpgb_env_mat_pt_bwd_f32(float* g_coord, const float* g_em,
+                            const float* g_diff, const float* g_sw,
+                            const float* coord_ext, const int* atype,
+                            const int* nlist, const float* std, int nf,
+                            int nloc, int nall, int nnei, double rcut,
+                            double rcut_smth, double protection, void* stream);
+
+/* Second derivative: the backward of dpgb_env_mat_pt_bwd.  Given the
+ * cotangent u [nf, nall, 3] of g_coord: gg_em [nf*nloc, nnei, 4] and
+ * gg_diff / gg_sw (either may be NULL) receive the directional derivatives
+ * of em / diff / sw along u (the map is linear in g_em, g_diff, g_sw), and
+ * gg_coord [nf, nall, 3] (may be NULL) the curvature term
+ * sum g . (d2 em / dr2) u. */
+int dpgb_env_mat_pt_bwd_bwd_f64(double* gg_em, double* gg_diff, double* gg_sw,
+                                double* gg_coord, const double* u,
+                                const double* g_em, const double* g_diff,
+                                const double* g_sw, const double* coord_ext,
+                                const int* atype, const int* nlist,
+                                const double* std, int nf, int nloc, int nall,
+                                int nnei, double rcut, double rcut_smth,
+                                double protection, void* stream);
+int dpgb_env_mat_pt_bwd_bwd_f32(float* gg_em, float* gg_diff, float* gg_sw,
+                                float* gg_coord, const float* u,
+                                const float* g_em, const float* g_diff,
+                                const float* g_sw, const float* coord_ext,
+                                const int* atype, const int* nlist,
+                                const float* std, int nf, int nloc, int nall,
+                                int nnei, double rcut, double rcut_smth,
+                                double protection, void* stream);
+
+/* ------------------------------------------------------------------------
+ * se_e2_a descriptor block on an environment matrix, with first and second
+ * derivatives: the operator behind DescrptBlockSeA.forward
+ * (deepmd/pt/model/descriptor/se_a.py:742-858).  The embedding nets'
+ * parameters are one flat device vector: for each net e (e = ii for
+ * type_one_side, else e = ii * ntypes + ti, ii the neighbour type and ti the
+ * centre type, se_a.py:805-808) and each layer l: matrix [nin_l, nout_l]
+ * row-major, bias [nout_l], then idt [nout_l] when resnet_dt.
+ * pair_keep is the (ntypes+1)^2 exclusion table of PairExcludeMask
+ * (deepmd/pt/utils/exclude_mask.py:64-141; the last type is the padding),
+ * laid out with a row stride of DPGB_MAX_TYPES + 1; 1 keeps a pair. */
+typedef struct dpgb_se_a_block {
+  int ntypes;
+  int sel[DPGB_MAX_TYPES];
+  int type_one_side;
+  int n_layer;
+  int neuron[DPGB_MAX_LAYERS];
+  int axis_neuron;
+  int resnet_dt;
+  int pair_keep[(DPGB_MAX_TYPES + 1) * (DPGB_MAX_TYPES + 1)];
+} dpgb_se_a_block;
+
+/* Compression table of one embedding net, built on the device: replaces
+ * DPTabulate._build_lower / _make_data (deepmd/utils/tabulate.py:275-370,
+ * deepmd/utils/tabulate_math.py:353-470) for se_e2_a.  params is the flat
+ * parameter vector described below, `net` the net index.  table
+ * [nrows, 6 * ng] (device) with nrows = dpgb_se_a_table_rows(...), the
+ * reference's int((upper - lower)/stride0 + (extrapolate*upper - upper)/
+ * stride1).  Synchronises the stream. */
+int dpgb_se_a_table_rows(double lower, double upper, double extrapolate,
+                         double stride0, double stride1);
+struct dpgb_se_a_block;
+int dpgb_se_a_table_build_f64(double* table, const struct dpgb_se_a_block* b,
+                              const double* params, int net, double lower,
+                              double upper, double extrapolate, double stride0,
+                              double stride1, void* stream);
+
+/* Number of parameters in the flat vector (-1 for a bad description). */
+long long dpgb_se_a_block_param_count(const dpgb_se_a_block* b);
+/* Workspace the parameter gradient needs (bytes) for nf * nloc rows at
+ * precision_bytes (8 or 4) per element. */
+size_t dpgb_se_a_block_workspace_bytes(const dpgb_se_a_block* b, int nf,
+                                       int nloc, int precision_bytes);
+
+/* Forward: rr [nf*nloc, nnei, 4] (normalised env matrix), nlist
+ * [nf*nloc, nnei], atype_ext [nf, nall] -> descriptor [nf*nloc, ng*M] and
+ * xyz [nf*nloc, 4, ng] (the reference's xyz_scatter / nnei; rot_mat is
+ * xyz^T[:, 1:4]). */
+int dpgb_se_a_block_fwd_f64(const dpgb_se_a_block* b, const double* params,
+                            const double* rr, const int* nlist,
+                            const int* atype_ext, int nf, int nloc, int nall,
+                            double* descriptor, double* xyz, void* stream);
+int dpgb_se_a_block_fwd_f32(const dpgb_se_a_block* b, const float* params,
+                            const float* rr, const int* nlist,
+                            const int* atype_ext, int nf, int nloc, int nall,
+                            float* descriptor, float* xyz, void* stream);
+
+/* Backward: cotangents of descriptor and (optionally) xyz -> g_rr
+ * [nf*nloc, nnei, 4] and, when g_params is not NULL, the parameter gradient
+ * (needs the workspace).  xyz is the forward's output. */
+int dpgb_se_a_block_bwd_f64(const dpgb_se_a_block* b, const double* params,
+                            const double* rr, const int* nlist,
+                            const int* atype_ext, int nf, int nloc, int nall,
+                            const double* xyz, const double* g_descriptor,
+                            const double* g_xyz, double* g_rr,
+                            double* g_params, void* workspace,
+                            size_t workspace_bytes, void* stream);
+int dpgb_se_a_block_bwd_f32(const dpgb_se_a_block* b, const float* params,
+                            const float* rr, const int* nlist,
+                            const int* atype_ext, int nf, int nloc, int nall,
+                            const float* xyz, const float* g_descriptor,
+                            const float* g_xyz, float* g_rr, float* g_params,
+                            void* workspace, size_t workspace_bytes,
+                            void* stream);
+
+/* Double backward: the backward of the backward, for the cotangent u_rr of
+ * g_rr (training on forces).  Outputs the cotangents of g_descriptor
+ * (gg_descriptor), of g_xyz (gg_xyz, may be NULL), of rr (gg_rr) and of the
+ * parameters (gg_params, may be NULL; needs the workspace).  Activations are
+ * recomputed, never stored. */
+int dpgb_se_a_block_bwd_bwd_f64(const dpgb_se_a_block* b, const double* params,
+                                const double* rr, const int* nlist,
+                                const int* atype_ext, int nf, int nloc,
+                                int nall, const double* g_descriptor,
+                                const double* g_xyz, const double* u_rr,
+                                double* gg_descriptor, double* gg_xyz,
+                                double* gg_rr, double* gg_params,
+                                void* workspace, size_t workspace_bytes,
+                                void* stream);
+int dpgb_se_a_block_bwd_bwd_f32(const dpgb_se_a_block* b, const float* params,
+                                const float* rr, const int* nlist,
+                                const int* atype_ext, int nf, int nloc,
+                                int nall, const float* g_descriptor,
+                                const float* g_xyz, const float* u_rr,
+                                float* gg_descriptor, float* gg_xyz,
+                                float* gg_rr, float* gg_params,
+                                void* workspace, size_t workspace_bytes,
+                                void* stream);
+
 /* ------------------------------------------------------------------------
  * Force and virial from net_deriv = dE/d em.  Replace deepmd::prod_force_a_gpu
  * (source/lib/src/gpu/prod_force.cu:4-130) and prod_virial_a_gpu

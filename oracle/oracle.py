@@ -135,6 +135,70 @@ def tabulate_fusion_se_a_grad_grad(table, info, em_x, em, dz_dx, dz_dem, last_la
 
 # --------------------------------------------------------------------------
 # region / ghosts / neighbour lists
+def table_env_range(davg, dstd, min_nbor_dist, rcut_smth, rcut):
+    """Per-type tabulation range (deepmd/utils/tabulate.py:468-498
+    _get_env_mat_range, then the per-type min/max of build() 91-96)."""
+    x = float(min_nbor_dist)
+    if x < rcut_smth:
+        sw = 1.0
+    elif x < rcut:
+        uu = (x - rcut_smth) / (rcut - rcut_smth)
+        sw = uu * uu * uu * (-6 * uu * uu + 15 * uu - 10) + 1
+    else:
+        sw = 0.0
+    davg = np.asarray(davg, dtype=np.float64)
+    dstd = np.asarray(dstd, dtype=np.float64)
+    lower = np.floor(-davg[:, 0] / dstd[:, 0])
+    upper = np.ceil(((1 / x) * sw - davg[:, 0]) / dstd[:, 0])
+    if lower.ndim > 1:
+        lower = np.min(lower, axis=tuple(range(1, lower.ndim)))
+        upper = np.max(upper, axis=tuple(range(1, upper.ndim)))
+    return lower, upper
+
+
+def table_build(layers, lower, upper, extrapolate, stride0, stride1):
+    """One net's table (deepmd/utils/tabulate.py:128-148 grid, 275-370
+    _build_lower; node values/derivatives as tabulate_math.py:353-470, tanh,
+    no timestep).  layers = [(W [nin, nout], b [nout]), ...]."""
+    xx = np.arange(lower, upper, stride0, dtype=np.float64)
+    xx = np.append(xx, np.arange(upper, extrapolate * upper, stride1, dtype=np.float64))
+    xx = np.append(xx, np.array([extrapolate * upper], dtype=np.float64))
+    nspline = int((upper - lower) / stride0 + (extrapolate * upper - upper) / stride1)
+    y = xx.reshape(-1, 1)
+    d1 = np.ones_like(y)
+    d2 = np.zeros_like(y)
+    for W, b in layers:
+        z = y @ W + b
+        z1 = d1 @ W
+        z2 = d2 @ W
+        t = np.tanh(z)
+        g = 1 - t * t
+        ny, n1, n2 = t, g * z1, g * z2 - 2 * t * g * z1 * z1
+        nin, nout = W.shape
+        if nout == nin:
+            ny, n1, n2 = ny + y, n1 + d1, n2 + d2
+        elif nout == 2 * nin:
+            ny = ny + np.concatenate([y, y], 1)
+            n1 = n1 + np.concatenate([d1, d1], 1)
+            n2 = n2 + np.concatenate([d2, d2], 1)
+        y, d1, d2 = ny, n1, n2
+    ng = y.shape[1]
+    tt = np.full((nspline, ng), stride1)
+    tt[: int((upper - lower) / stride0), :] = stride0
+    v0, v1 = y[:nspline], y[1:nspline + 1]
+    a0, a1 = d1[:nspline], d1[1:nspline + 1]
+    s0, s1 = d2[:nspline], d2[1:nspline + 1]
+    hh = v1 - v0
+    out = np.zeros((nspline, 6 * ng))
+    out[:, 0::6] = v0
+    out[:, 1::6] = a0
+    out[:, 2::6] = 0.5 * s0
+    out[:, 3::6] = (1 / (2 * tt ** 3)) * (20 * hh - (8 * a1 + 12 * a0) * tt - (3 * s0 - s1) * tt * tt)
+    out[:, 4::6] = (1 / (2 * tt ** 4)) * (-30 * hh + (14 * a1 + 16 * a0) * tt + (3 * s0 - 2 * s1) * tt * tt)
+    out[:, 5::6] = (1 / (2 * tt ** 5)) * (12 * hh - 6 * (a1 + a0) * tt + (s1 - s0) * tt * tt)
+    return out
+
+
 def normalize_coord(coord: np.ndarray, box: np.ndarray) -> np.ndarray:
     """deepmd/pt/utils/region.py:86-105: wrap into the cell."""
     cell = box.reshape(3, 3)

@@ -48,3 +48,16 @@ def cuda():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     return torch.device("cuda:0")
+
+
+def assert_table_close(t, ref, lower, upper, stride0, stride1, tol=1e-12):
+    """Tables agree as polynomials: coefficient k of a row scaled by h^k.
+    The high-order coefficients are differences of node values divided by
+    h^3..h^5, so one ulp in a node value moves them by ~1e-16 / h^5; their
+    contribution on the interval, a_k h^k, is what must agree."""
+    nrow0 = int((upper - lower) / stride0)
+    h = np.where(np.arange(t.shape[0]) < nrow0, stride0, stride1)[:, None]
+    scale = np.abs(ref[:, 0::6]).max()
+    for k in range(6):
+        d = np.abs(t[:, k::6] - ref[:, k::6]) * h ** k
+        assert d.max() <= tol * scale, (k, d.max())

@@ -3,7 +3,7 @@ reference tree is present, against the reference's own compiled library."""
 import numpy as np
 import pytest
 
-from conftest import deeppot_sea_params, golden, water_params
+from conftest import assert_table_close, deeppot_sea_params, golden, water_params
 
 import oracle as O
 
@@ -134,3 +134,22 @@ def test_water192_compressed_golden():
     assert rel(r["energy"], g["energy"][0]) < 1e-12
     assert rel(r["force"], g["force"]) < 1e-10
     assert rel(r["virial"], g["virial"]) < 1e-10
+
+
+def test_table_build_matches_reference_tables():
+    """The table-build restatement against the reference's own compression
+    tables of the water model (enable_compression, strides 0.1 / 1.0)."""
+    g = golden("water192_compressed")
+    p = water_params()
+    lower, upper = O.table_env_range(p.mean, p.stddev, float(g["min_nbor_dist"]), p.config.rcut_smth,
+                                     p.config.rcut)
+    nt = len(p.config.sel)
+    for e in range(nt * nt):
+        ti = e % nt
+        layers = [(W, b) for W, b, _ in p.emb[e]]
+        t = O.table_build(layers, lower[ti], upper[ti], float(g["extrapolate"]), float(g["stride0"]),
+                          float(g["stride1"]))
+        np.testing.assert_allclose(g[f"info_{e}"][:2], [lower[ti], upper[ti]])
+        assert t.shape == g[f"table_{e}"].shape
+        assert_table_close(t, g[f"table_{e}"], lower[ti], upper[ti], float(g["stride0"]), float(g["stride1"]))
+
