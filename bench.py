@@ -208,8 +208,94 @@ def cpu_baseline_port(sample: int, steps: int = 2):
             "sample": f"{steps} x {sample} centre atoms (full neighbourhoods) of the 12,288-atom box, FP64 oracle"}
 
 
+def run_compressed(args, world, rank, local):
+    """The compressed water box: 32,768 H2O (98,304 atoms, box 99.2 A), the
+    embedding nets replaced by GPU-built tables (stride 0.01 to the upper
+    bound, 0.1 beyond, extrapolate x5, from the same seeded weights), a
+    random walk of N(0, 0.01 A) displacements applied between consecutive
+    force evaluations.  Mixed form (FP32 table evaluation fused with the
+    contraction, FP64 reductions) timed step by step; the FP64 table form on
+    the same coordinates for the speed-up and the errors."""
+    import torch
+
+    from dpgb import params as P, synth, tabulate
+    from dpgb.deeppot import DeepPot
+
+    dev = torch.device("cuda", local)
+    params = P.init_params(P.water_config(), seed=1)
+    coord, atype, box = synth.water_box(32, seed=rank)
+    nloc = coord.shape[0]
+    # nearest-neighbour distance of the generated box (the O-H bond), the
+    # input of the tabulation range
+    min_nbor = 0.9
+    cparams = tabulate.compress_params(params, min_nbor, 5, 0.01, 0.1, device=dev)
+    boxh = box.reshape(1, 9)
+    x = torch.tensor(coord.reshape(1, -1), dtype=torch.float64, device=dev)
+    gen = torch.Generator(device=dev).manual_seed(1234 + rank)
+    mixed = DeepPot(cparams, "mixed", device=local)
+    out = mixed.eval_device(x, boxh, atype)
+    for _ in range(args.warmup):
+        mixed.eval_device(x, boxh, atype, out=out)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    mixed.set_profiling(True)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    _barrier(world)
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            x.add_(torch.randn(x.shape, dtype=x.dtype, device=dev, generator=gen), alpha=0.01)  # untimed
+            starts[k].record(stream)
+            mixed.eval_device(x, boxh, atype, out=out)
+            ends[k].record(stream)
+            mixed.collect_stages()
+        torch.cuda.synchronize()
+    _barrier(world)
+    t_ms = _allreduce_max(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), world)
+    stages, ncalls = mixed.stage_times()
+    launches = mixed.last_launches()
+    value = world * nloc * args.steps / (t_ms * 1e-3)
+    fp64 = DeepPot(cparams, "fp64", device=local)
+    o64 = fp64.eval_device(x, boxh, atype)
+    torch.cuda.synchronize()
+    s64, e64 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s64.record(stream)
+    for _ in range(args.fp64_steps):
+        fp64.eval_device(x, boxh, atype, out=o64)
+    e64.record(stream)
+    torch.cuda.synchronize()
+    fp64_ms = s64.elapsed_time(e64) / args.fp64_steps
+    mixed.eval_device(x, boxh, atype, out=out)
+    torch.cuda.synchronize()
+    f_m, f_d = out["force"].double().cpu().numpy(), o64["force"].cpu().numpy()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {
+            "workload": "compressed water 32768 H2O (98,304 atoms), box 99.2 A, tables stride 0.01/0.1 x5, "
+                        "N(0, 0.01 A) random walk between evaluations; mixed form; neighbour list rebuilt "
+                        "every evaluation",
+            "natoms": nloc, "l2": "inputs larger than L2",
+            "fp64_atom_steps_per_s": nloc / (fp64_ms * 1e-3), "fp64_ms_per_step": fp64_ms,
+            "mixed_over_fp64": value / world / (nloc / (fp64_ms * 1e-3)),
+            "force_rmse_vs_fp64_eV_per_A": float(np.sqrt(np.mean((f_m - f_d) ** 2))),
+            "force_rms_fp64": float(np.sqrt(np.mean(f_d ** 2))),
+            "energy_err_per_atom_vs_fp64": float(abs(out["energy"].item() - o64["energy"].item()) / nloc),
+            "stage_ms_per_step": {k: v / max(ncalls, 1) for k, v in stages.items()},
+            "parallelism": f"replicas x{world}",
+        },
+        "gpu_launches": launches * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="water12k", choices=["water12k", "water98k-compressed"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -232,6 +318,9 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
+    if args.workload == "water98k-compressed":
+        run_compressed(args, world, rank, local)
+        return
     from dpgb import nlist as N, params as P, synth
     from dpgb.deeppot import DeepPot
 

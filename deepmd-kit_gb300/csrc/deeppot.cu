@@ -163,6 +163,7 @@ struct DeepPotImpl {
   int nchunks = 0;
   // tensor-core embedding (mixed precision)
   int use_tc = 0;
+  int use_tab = 0;  // compressed nets in the mixed form: fused FP32 table kernels
   EmbTC tc{};
   DeviceBuffer tc_images, tc_vec, ws_runlen, ws_dxyz;
   // tensor-core fitting (mixed precision)
@@ -732,14 +733,24 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       launches += 2;
     }
   }
-  if (!tc_path) {
+  bool tab_path = false;
+  if constexpr (std::is_same<T, float>::value) {
+    tab_path = !tc_path && dp.use_tab != 0;
+    if (tab_path) {
+      DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ng));
+      DPGB_TRY(launch_tab_fwd(p, m.emb, dp.sorted_rows_dev.as<int>(), dp.type_off[d.ntypes], dp.ws_xyz.as<float>(),
+                              dp.ws_D.ptr, dp.use_fit_tc, st));
+      ++launches;
+    }
+  }
+  if (!tc_path && !tab_path) {
     DPGB_TRY(launch_desc_fwd<T>(p, m.emb, dp.ws_D.as<T>(), dp.ws_xyz.as<T>(), desc_fwd_smem<T>(p, m.emb), st));
     ++launches;
   }
   dp.mark(DPGB_STAGE_DESC_FWD, 1, st);
   dp.mark(DPGB_STAGE_FITTING, 0, st);
   bool fit_tc = false;
-  if constexpr (std::is_same<T, float>::value) fit_tc = tc_path && dp.use_fit_tc;
+  if constexpr (std::is_same<T, float>::value) fit_tc = (tc_path || tab_path) && dp.use_fit_tc;
   if (fit_tc) {
     DPGB_TRY(dp.ws_fitb.alloc(sizeof(__nv_bfloat16) * (size_t)(dp.fit_nh + 2) * nrows * maxw));
   }
@@ -771,8 +782,15 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
                                  dp.ws_vir.as<double>(), status, st));
       launches += 2;
     }
+    if (tab_path) {
+      DPGB_CUDA(cudaMemsetAsync(dp.ws_vir.ptr, 0, sizeof(double) * nrows * 9, st));
+      DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
+      DPGB_TRY(launch_tab_bwd(p, m.emb, dp.sorted_rows_dev.as<int>(), dp.type_off[d.ntypes], dp.ws_dxyz.as<float>(),
+                              dp.ws_g.as<float>(), dp.ws_vir.as<double>(), st));
+      launches += 2;
+    }
   }
-  if (!tc_path) {
+  if (!tc_path && !tab_path) {
     DPGB_TRY(launch_desc_bwd<T>(p, m.emb, dp.ws_dD.as<T>(), dp.ws_xyz.as<T>(), dp.ws_g.as<T>(), dp.ws_vir.as<double>(),
                                 desc_bwd_smem<T>(p, m.emb), st));
     ++launches;
@@ -878,6 +896,10 @@ dpgb_deeppot* dpgb_deeppot_new(const dpgb_se_a_desc* desc, int precision) {
       }
       emb_tc_bind(im.tc, im.tc_images.as<unsigned char>(), 0, im.tc_vec.as<float>());
       im.use_tc = 1;
+      if (fit_tc_eligible(*desc) && build_fit_tc(im, *desc) != DPGB_OK) return nullptr;
+    } else if (desc->compressed && tab_fused_eligible(im.ng, desc->axis_neuron) && !(no_tc && no_tc[0] == '1')) {
+      // compressed nets: fused FP32 table kernels, tensor-core fitting
+      im.use_tab = 1;
       if (fit_tc_eligible(*desc) && build_fit_tc(im, *desc) != DPGB_OK) return nullptr;
     }
   }

@@ -208,34 +208,6 @@ __device__ __forceinline__ void dense_layer(int nch, int nin, int nout, const T*
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void table_poly(const T* rowc, T xx, T delta, T& val, T& grad) {
-  const T a0 = rowc[0], a1 = rowc[1], a2 = rowc[2], a3 = rowc[3], a4 = rowc[4], a5 = rowc[5];
-  grad = a1 + ((T)2 * a2 + ((T)3 * a3 + ((T)4 * a4 + (T)5 * a5 * xx) * xx) * xx) * xx;
-  val = a0 + (a1 + (a2 + (a3 + (a4 + a5 * xx) * xx) * xx) * xx) * xx + grad * delta;
-}
-
-template <typename T>
-__device__ __forceinline__ void table_locate(const TabMeta<T>& tm, T x, int& idx, T& xx, T& delta) {
-  xx = x;
-  delta = (T)0;
-  if (xx < tm.lower) {
-    idx = 0;
-    delta = xx - tm.lower;
-    xx = (T)0;
-  } else if (xx < tm.upper) {
-    idx = (int)((xx - tm.lower) / tm.s0);
-    xx -= (idx * tm.s0 + tm.lower);
-  } else if (xx < tm.mx) {
-    idx = tm.first + (int)((xx - tm.upper) / tm.s1);
-    xx -= ((idx - tm.first) * tm.s1 + tm.upper);
-  } else {
-    idx = tm.hi_idx;
-    delta = xx - tm.mx;
-    xx = tm.hi_xx;
-  }
-}
-
 // ---------------------------------------------------------------------------
 template <typename T, int CH>
 __global__ void __launch_bounds__(kThreads)

@@ -18,6 +18,37 @@ struct TabMeta {
   long long offset;  // element offset of the net's table in the table buffer
 };
 
+// Quintic of one table interval and its derivative; delta != 0 extends the
+// end intervals linearly (tabulate.cc locate_xx_se_a with extrapolation).
+template <typename T>
+__device__ __forceinline__ void table_poly(const T* rowc, T xx, T delta, T& val, T& grad) {
+  const T a0 = rowc[0], a1 = rowc[1], a2 = rowc[2], a3 = rowc[3], a4 = rowc[4], a5 = rowc[5];
+  grad = a1 + ((T)2 * a2 + ((T)3 * a3 + ((T)4 * a4 + (T)5 * a5 * xx) * xx) * xx) * xx;
+  val = a0 + (a1 + (a2 + (a3 + (a4 + a5 * xx) * xx) * xx) * xx) * xx + grad * delta;
+}
+
+// interval index and offset of x (source/lib/src/tabulate.cc locate_xx_se_a)
+template <typename T>
+__device__ __forceinline__ void table_locate(const TabMeta<T>& tm, T x, int& idx, T& xx, T& delta) {
+  xx = x;
+  delta = (T)0;
+  if (xx < tm.lower) {
+    idx = 0;
+    delta = xx - tm.lower;
+    xx = (T)0;
+  } else if (xx < tm.upper) {
+    idx = (int)((xx - tm.lower) / tm.s0);
+    xx -= (idx * tm.s0 + tm.lower);
+  } else if (xx < tm.mx) {
+    idx = tm.first + (int)((xx - tm.upper) / tm.s1);
+    xx -= ((idx - tm.first) * tm.s1 + tm.upper);
+  } else {
+    idx = tm.hi_idx;
+    delta = xx - tm.mx;
+    xx = tm.hi_xx;
+  }
+}
+
 // Embedding nets: all nets share widths; W[l] is [nnets, nin_l, nout_l],
 // b[l] / idt[l] are [nnets, nout_l] (idt NULL when the layer has none).
 template <typename T>
@@ -89,6 +120,15 @@ int launch_desc_bwd(const DescParams<T>& p, const EmbParams<T>& e, const T* dD, 
                     T* gpair, double* vir_row, size_t smem, cudaStream_t st);
 template <typename T>
 size_t desc_bwd_smem(const DescParams<T>& p, const EmbParams<T>& e);
+
+// Compressed nets in the mixed form (tab_fused.cu): the table lookup fused
+// with the env matrix and contraction (forward: xyz in row order, D at the
+// type-sorted position, BF16 when d_bf16) and the pair-gradient backward.
+int tab_fused_eligible(int ng, int axis);
+int launch_tab_fwd(const DescParams<float>& p, const EmbParams<float>& e, const int* sorted_rows, int nsorted,
+                   float* xyz, void* D, int d_bf16, cudaStream_t st);
+int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const int* sorted_rows, int nsorted,
+                   const float* dxyz, float* gpair, double* vir_row, cudaStream_t st);
 
 // fitting of the rows [row0, row0+nrow) of one type
 template <typename T>

@@ -42,6 +42,31 @@ def env_mat_range(davg, dstd, min_nbor_dist, rcut_smth, rcut):
     return lower, upper
 
 
+def compress_params(params, min_nbor_dist, extrapolate=5, stride0=0.01, stride1=0.1, device="cuda"):
+    """A copy of a SeAParams model with GPU-built tables installed (the
+    DeepPot compressed form): tables[e] / table_info[e] per embedding net."""
+    import copy
+
+    from .descriptor import DescrptSeA
+
+    c = params.config
+    d = DescrptSeA(c.rcut, c.rcut_smth, c.sel, neuron=c.neuron, axis_neuron=c.axis_neuron,
+                   type_one_side=c.type_one_side, resnet_dt=c.resnet_dt, exclude_types=c.exclude_types,
+                   device=device)
+    sd = {k[len("atomic_model.descriptor."):]: torch.as_tensor(v) for k, v in params.to_state_dict().items()
+          if k.startswith("atomic_model.descriptor.")}
+    d.load_state_dict(sd, strict=False)
+    data, lo, up = build_tables(d, min_nbor_dist, extrapolate, stride0, stride1)
+    nt = len(c.sel)
+    out = copy.copy(params)
+    out.tables, out.table_info = [], []
+    for e in range(len(params.emb)):
+        name = f"filter_-1_net_{e}" if c.type_one_side else f"filter_{e % nt}_net_{e // nt}"
+        out.tables.append(data[name].double().cpu().numpy())
+        out.table_info.append(np.array([lo[name], up[name], up[name] * extrapolate, stride0, stride1, -1.0]))
+    return out
+
+
 def build_tables(descrpt, min_nbor_dist, extrapolate=5, stride0=0.01, stride1=0.1):
     """(data {name: table [nspline, 6*ng] on the descriptor's device}, lower
     {name: int}, upper {name: int}) for a dpgb DescrptSeA / DescrptBlockSeA."""

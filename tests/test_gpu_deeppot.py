@@ -114,3 +114,21 @@ def test_device_api_matches_host_api(water_fp64):
     np.testing.assert_array_equal(out["energy"].cpu().numpy(), e)
     np.testing.assert_array_equal(out["force"].cpu().numpy(), f)
     np.testing.assert_array_equal(out["virial"].cpu().numpy(), v)
+
+
+def test_mixed_compressed_vs_fp64_compressed(cuda):
+    """The fused FP32 table kernels (mixed form of a compressed model)
+    against the FP64 table form on a 1,536-atom box."""
+    from dpgb import synth
+    from dpgb.deeppot import DeepPot
+
+    coord, atype, box = synth.water_box(8, seed=5)
+    p = water_params(compressed=True)
+    e64, f64, v64 = DeepPot(p, "fp64").eval(coord.reshape(1, -1), box, atype)
+    e32, f32, v32 = DeepPot(p, "mixed").eval(coord.reshape(1, -1), box, atype)
+    n = atype.shape[0]
+    rmse = float(np.sqrt(np.mean((f32 - f64) ** 2)))
+    assert rmse <= 1e-3
+    assert rmse <= 2e-2 * float(np.sqrt(np.mean(f64 ** 2)))
+    assert abs(e32[0] - e64[0]) / n < 2e-4
+    assert rel(v32[0], v64[0]) < 2e-2
