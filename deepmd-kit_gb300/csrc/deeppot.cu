@@ -675,7 +675,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     DPGB_TRY(launch_nlist_pt(nlist + (size_t)f * natom * nnei, cout, dp.atype_dev.as<int>(), natom, geo[f],
                              dp.ws_spos.as<int>() + spos_n * f, dp.ws_svec.as<double>() + (size_t)3 * nshift_max * f,
                              d.rcut, dp.sel, dp.ws_cell.ptr, status, st));
-    launches += 4;
+    launches += 5;  // cell count, scan, fill, staged search, per-atom search of flagged cells
   }
   dp.mark(DPGB_STAGE_NLIST, 1, st);
   // sorted transpose of the list over local rows

@@ -237,8 +237,12 @@ struct Cand {
   int type;
 };
 
+// (distance, extended index) order.  Distances are >= +0, so their IEEE bit
+// patterns order exactly like the values: the comparison runs as 64-bit
+// integer compares instead of on the (narrow) FP64 pipe.
 __device__ __forceinline__ bool cand_less(double ra, int ia, double rb, int ib) {
-  return ra < rb || (ra == rb && ia < ib);
+  const long long a = __double_as_longlong(ra), b = __double_as_longlong(rb);
+  return a < b || (a == b && ia < ib);
 }
 
 // One warp per centre atom: gather the atoms of the stencil cells within
@@ -249,13 +253,15 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
                 const int* __restrict__ atype, const int* __restrict__ cell_of,
                 const int* __restrict__ offsets, const int* __restrict__ cell_atoms,
                 const int* __restrict__ shift_pos, const double* __restrict__ svec, int nloc,
-                CellGeom g, double rcut, SelInfo sel, int* __restrict__ status) {
+                CellGeom g, double rcut, SelInfo sel, const int* __restrict__ only_cells,
+                int* __restrict__ status) {
   __shared__ double s_r[kSearchWarps][kCap];
   __shared__ int s_idx[kSearchWarps][kCap];
   __shared__ int s_type[kSearchWarps][kCap];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kSearchWarps + warp;
   if (i >= nloc) return;
+  if (only_cells && !only_cells[cell_of[i]]) return;  // handled by the staged kernel
   int* row = nlist + (size_t)i * sel.nnei;
   for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
   if (atype[i] < 0) return;
@@ -332,6 +338,165 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
     }
     // topk(sum(sel)): candidates of global rank >= nnei are dropped
     if (rank < sel.nnei && tk < sel.ntypes && trank < sel.sel[tk]) row[sel.sec[tk] + trank] = ik;
+  }
+}
+
+// Staged form of nlist_pt_kernel: one CTA per cell.  The atoms of the cell's
+// 27 stencil cells are copied once into shared memory (image-shifted
+// coordinates, extended index, type), so the cell's centre atoms (one warp
+// each) scan them without global gathers.  Same distances (the FMA norm of
+// (r_j + shift) - r_i), same ranking by (distance, extended index), same
+// per-type placement: the list is bitwise that of nlist_pt_kernel.  A cell
+// whose stencil holds more than kStageCap atoms is flagged and left to
+// nlist_pt_kernel.
+constexpr int kCellWarps = 4;
+constexpr int kStageCap = 2048;
+constexpr int kKeptCap = 512;
+
+size_t cell_stage_smem() {
+  return (size_t)kStageCap * (3 * sizeof(float) + 2 * sizeof(int)) +
+         (size_t)kCellWarps * kKeptCap * (sizeof(double) + 2 * sizeof(int));
+}
+
+__global__ void __launch_bounds__(kCellWarps * 32)
+nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, const int* __restrict__ atype,
+                  const int* __restrict__ offsets, const int* __restrict__ cell_atoms,
+                  const int* __restrict__ shift_pos, const double* __restrict__ svec, int nloc, CellGeom g,
+                  double rcut, SelInfo sel, int* __restrict__ fallback, int* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* kr = reinterpret_cast<double*>(smem);
+  float* sx = reinterpret_cast<float*>(kr + kCellWarps * kKeptCap);
+  float* sy = sx + kStageCap;
+  float* sz = sy + kStageCap;
+  int* sidx = reinterpret_cast<int*>(sz + kStageCap);
+  int* stype = sidx + kStageCap;
+  int* kidx = stype + kStageCap;
+  int* ktype = kidx + kCellWarps * kKeptCap;
+  __shared__ int s_cell[27], s_shift[27], s_off[28];
+  const int c = blockIdx.x, tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int cz = c % g.ncell[2], cy = (c / g.ncell[2]) % g.ncell[1], cx = c / (g.ncell[1] * g.ncell[2]);
+  const int sy_ = 2 * g.nbuff[1] + 1, sz_ = 2 * g.nbuff[2] + 1;
+  if (tid < 27) {
+    const int ox = tid / 9 - 1, oy = (tid / 3) % 3 - 1, oz = tid % 3 - 1;
+    int xw, tx, yw, ty, zw, tz;
+    bool ok = wrap_cell(cx + ox, g.ncell[0], g.periodic, xw, tx) && wrap_cell(cy + oy, g.ncell[1], g.periodic, yw, ty) &&
+              wrap_cell(cz + oz, g.ncell[2], g.periodic, zw, tz);
+    ok = ok && abs(tx) <= g.nbuff[0] && abs(ty) <= g.nbuff[1] && abs(tz) <= g.nbuff[2];
+    s_cell[tid] = ok ? (xw * g.ncell[1] + yw) * g.ncell[2] + zw : -1;
+    s_shift[tid] = ok ? shift_pos[((tx + g.nbuff[0]) * sy_ + (ty + g.nbuff[1])) * sz_ + (tz + g.nbuff[2])] : 0;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    s_off[0] = 0;
+    for (int k = 0; k < 27; ++k)
+      s_off[k + 1] = s_off[k] + (s_cell[k] >= 0 ? offsets[s_cell[k] + 1] - offsets[s_cell[k]] : 0);
+  }
+  __syncthreads();
+  const int total = s_off[27];
+  if (total > kStageCap) {  // left to nlist_pt_kernel
+    if (tid == 0) fallback[c] = 1;
+    return;
+  }
+  // FP32 copies relative to a point of the centre cell (its first atom):
+  // |offsets| < ~3 cell widths, so their rounding error is ~1e-6 A — only a
+  // prefilter; kept pairs get their exact FP64 distance below
+  const int a0 = offsets[c] < offsets[c + 1] ? cell_atoms[offsets[c]] : 0;
+  const double ox = coord[3 * a0], oy = coord[3 * a0 + 1], oz = coord[3 * a0 + 2];
+  for (int q = tid; q < total; q += blockDim.x) {
+    int k = 0;
+    while (s_off[k + 1] <= q) ++k;
+    const int j = cell_atoms[offsets[s_cell[k]] + (q - s_off[k])];
+    const int s = s_shift[k];
+    sx[q] = (float)((coord[3 * j] + svec[3 * s]) - ox);
+    sy[q] = (float)((coord[3 * j + 1] + svec[3 * s + 1]) - oy);
+    sz[q] = (float)((coord[3 * j + 2] + svec[3 * s + 2]) - oz);
+    sidx[q] = s * nloc + j;
+    stype[q] = atype[j];
+  }
+  __syncthreads();
+  const float rcf = (float)rcut + 1e-3f;  // prefilter radius: well above the FP32 error
+  const float rcf2 = rcf * rcf;
+  double* wr = kr + warp * kKeptCap;
+  int* wi = kidx + warp * kKeptCap;
+  int* wt = ktype + warp * kKeptCap;
+  for (int a = offsets[c] + warp; a < offsets[c + 1]; a += kCellWarps) {
+    const int i = cell_atoms[a];
+    int* row = nlist + (size_t)i * sel.nnei;
+    for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
+    if (atype[i] < 0) continue;
+    const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
+    const int self = g.zero_shift * nloc + i;
+    const float xf = (float)(xi - ox), yf = (float)(yi - oy), zf = (float)(zi - oz);
+    int n = 0;
+    bool overflow = false;
+    for (int p0 = 0; p0 < total; p0 += 32) {
+      const int p = p0 + lane;
+      bool keep = false;
+      double r = 0.0;
+      if (p < total && stype[p] >= 0 && sidx[p] != self) {
+        const float fx = sx[p] - xf, fy = sy[p] - yf, fz = sz[p] - zf;
+        if (fx * fx + fy * fy + fz * fz <= rcf2) {
+          // exact distance, the same arithmetic as nlist_pt_kernel
+          const int e = sidx[p], s = e / nloc, j = e - s * nloc;
+          const double dx = (coord[3 * j] + svec[3 * s]) - xi;
+          const double dy = (coord[3 * j + 1] + svec[3 * s + 1]) - yi;
+          const double dz = (coord[3 * j + 2] + svec[3 * s + 2]) - zi;
+          r = dist_fma(dx, dy, dz);
+          keep = r <= rcut;
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      const int pos = n + __popc(m & ((1u << lane) - 1u));
+      if (keep) {
+        if (pos < kKeptCap) {
+          wr[pos] = r;
+          wi[pos] = sidx[p];
+          wt[pos] = stype[p];
+        } else {
+          overflow = true;
+        }
+      }
+      n += __popc(m);
+    }
+    overflow = __any_sync(0xffffffffu, overflow);
+    if (overflow) {  // more than kKeptCap within rcut: the whole cell goes to the per-atom kernel
+      if (lane == 0) fallback[c] = 1;
+      __syncwarp();
+      continue;
+    }
+    __syncwarp();
+    // rank by counting: each lane holds up to 4 kept entries in registers and
+    // streams the warp's kept list once per group of 128
+    for (int k0 = 0; k0 < n; k0 += 128) {
+      long long rk[4];
+      int ik[4], tk[4], rank[4], trank[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = k0 + lane + 32 * q;
+        rk[q] = k < n ? __double_as_longlong(wr[k]) : 0x7fffffffffffffffLL;
+        ik[q] = k < n ? wi[k] : 0x7fffffff;
+        tk[q] = k < n ? wt[k] : -1;
+        rank[q] = trank[q] = 0;
+      }
+      for (int m2 = 0; m2 < n; ++m2) {
+        const long long rm = __double_as_longlong(wr[m2]);
+        const int im = wi[m2], tm = wt[m2];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const bool lt = rm < rk[q] || (rm == rk[q] && im < ik[q]);
+          rank[q] += lt;
+          trank[q] += lt && tm == tk[q];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int t = tk[q];
+        if (k0 + lane + 32 * q < n && rank[q] < sel.nnei && t < sel.ntypes && trank[q] < sel.sel[t])
+          row[sel.sec[t] + trank[q]] = ik[q];
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -506,7 +671,7 @@ int launch_extend(double* cext, int* text, int* mapping, const double* coord, co
 
 size_t nlist_pt_workspace(int nloc, const CellGeom& g) {
   const size_t ncell = (size_t)g.ncell[0] * g.ncell[1] * g.ncell[2];
-  return sizeof(int) * (2 * (size_t)nloc + 3 * (ncell + 1)) + 256 * 4;
+  return sizeof(int) * (2 * (size_t)nloc + 4 * (ncell + 1)) + 256 * 4;
 }
 
 int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc, const CellGeom& g,
@@ -519,17 +684,28 @@ int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc,
   int* counts = cell_atoms + nloc;
   int* offsets = counts + (ncell + 1);
   int* cursor = offsets + (ncell + 1);
+  int* fallback = cursor + (ncell + 1);
   DPGB_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (ncell + 1), st));
-  DPGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * (ncell + 1), st));
+  DPGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * 2 * (ncell + 1), st));  // cursor and fallback flags
   cell_count_kernel<<<ceil_div(nloc, 256), 256, 0, st>>>(cell_of, counts, coord, nloc, g);
   DPGB_TRY(check_launch("cell_count"));
   scan_kernel<<<1, 1024, 0, st>>>(offsets, counts, ncell);
   DPGB_TRY(check_launch("cell_scan"));
   cell_fill_kernel<<<ceil_div(nloc, 256), 256, 0, st>>>(cell_atoms, cursor, offsets, cell_of, nloc);
   DPGB_TRY(check_launch("cell_fill"));
+  // the staged kernel covers the 27-cell stencil; a wider stencil (a box
+  // thinner than 2 rcut across a face) goes to the per-atom kernel whole
+  const bool staged = g.reach[0] == 1 && g.reach[1] == 1 && g.reach[2] == 1;
+  if (staged) {
+    const size_t smem = cell_stage_smem();
+    DPGB_CUDA(cudaFuncSetAttribute(nlist_cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    nlist_cell_kernel<<<ncell, kCellWarps * 32, smem, st>>>(nlist, coord, atype, offsets, cell_atoms, shift_pos_dev,
+                                                            svec_dev, nloc, g, rcut, sel, fallback, status);
+    DPGB_TRY(check_launch("nlist_cell"));
+  }
   nlist_pt_kernel<<<ceil_div(nloc, kSearchWarps), kSearchWarps * 32, 0, st>>>(
       nlist, coord, atype, cell_of, offsets, cell_atoms, shift_pos_dev, svec_dev, nloc, g, rcut, sel,
-      status);
+      staged ? fallback : nullptr, status);
   return check_launch("nlist_pt");
 }
 

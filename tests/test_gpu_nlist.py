@@ -119,3 +119,23 @@ def test_overflow_is_an_error(cuda):
     atype = np.zeros(1100, np.int32)
     with pytest.raises(_lib.DpgbError, match="within rcut"):
         N.build_neighbor_list_local(_t(coord, cuda), _t(atype, cuda, torch.int32), None, 6.0, [100])
+
+
+def test_dense_cell_takes_the_per_atom_path(cuda):
+    """A box one cell wide whose 27-cell stencil holds more atoms than the
+    staged kernel keeps in shared memory: the cell is handled by the per-atom
+    search, with the same list as the oracle."""
+    import torch
+    from dpgb import nlist as N
+
+    rng = np.random.default_rng(11)
+    n = 120
+    box = np.diag([7.5, 7.5, 7.5]).reshape(-1)
+    coord = rng.uniform(size=(n, 3)) * 7.5
+    atype = rng.integers(0, 2, size=n).astype(np.int32)
+    sel = [100, 100]
+    shifts = O.ghost_shifts(box, 6.0).astype(np.int32)
+    ext, ext_t, _ = O.extend_coord_with_ghosts(coord, atype, box, 6.0, None)
+    ref = O.build_nlist_pt(ext, ext_t, n, 6.0, sel)
+    nl = N.build_neighbor_list_local(_t(coord, cuda), _t(atype, cuda, torch.int32), box, 6.0, sel, shifts)
+    np.testing.assert_array_equal(nl.cpu().numpy(), ref)
