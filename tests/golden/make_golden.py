@@ -268,6 +268,62 @@ def make_water_compressed(params, coord, atype, box):
         virial=ret["virial"].detach().numpy().reshape(-1), **tabs, **infos)
 
 
+TRAIN_FRAMES = 4       # water frames of the force-loss training case
+TRAIN_PREF = (0.02, 1000.0)  # energy and force prefactors (start == limit)
+
+
+def train_frames():
+    from dpgb import synth
+
+    frames = [synth.water_box(4, seed=100 + k) for k in range(TRAIN_FRAMES)]
+    coord = np.stack([f[0].reshape(-1) for f in frames])
+    return coord, frames[0][1], np.stack([f[2].reshape(-1) for f in frames])
+
+
+def make_train_grad():
+    """One force-loss training step of the reference (deepmd.pt EnergyModel +
+    EnergyStdLoss, FP64 autograd) on water frames labelled by a second,
+    differently seeded model: the loss, the per-tensor gradient norms and 64
+    gradient entries (tensor name, flat index, value)."""
+    import torch
+    from deepmd.pt.loss import EnergyStdLoss
+    from dpgb import params as P
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    cfg = P.water_config()
+    coord, atype, box = train_frames()
+    nf, nloc = coord.shape[0], atype.shape[0]
+    teacher = _reference_model(P.init_params(cfg, seed=2))
+    inp = {"coord": torch.as_tensor(coord), "atype": torch.as_tensor(np.tile(atype, (nf, 1)), dtype=torch.int64),
+           "box": torch.as_tensor(box)}
+    ref = teacher.forward(**inp)
+    label = {"energy": ref["energy"].detach(), "force": ref["force"].detach(), "find_energy": 1.0,
+             "find_force": 1.0}
+    student = _reference_model(P.init_params(cfg, seed=1))
+    loss_fn = EnergyStdLoss(starter_learning_rate=1.0, start_pref_e=TRAIN_PREF[0], limit_pref_e=TRAIN_PREF[0],
+                            start_pref_f=TRAIN_PREF[1], limit_pref_f=TRAIN_PREF[1])
+    _, loss, _ = loss_fn(inp, student, label, nloc, 1.0)
+    loss.backward()
+    names, norms, pick_name, pick_idx, pick_val = [], [], [], [], []
+    rng = np.random.default_rng(64)
+    grads = {k: p.grad.detach().numpy().reshape(-1) for k, p in student.named_parameters() if p.grad is not None}
+    for k in sorted(grads):
+        names.append(k)
+        norms.append(float(np.linalg.norm(grads[k])))
+    keys = sorted(grads)
+    for _ in range(64):
+        k = keys[int(rng.integers(len(keys)))]
+        i = int(rng.integers(grads[k].size))
+        pick_name.append(k)
+        pick_idx.append(i)
+        pick_val.append(grads[k][i])
+    np.savez_compressed(
+        os.path.join(HERE, "train_grad.npz"), coord=coord, atype=atype, box=box, pref=np.array(TRAIN_PREF),
+        energy_label=ref["energy"].detach().numpy().reshape(-1), force_label=ref["force"].detach().numpy(),
+        loss=float(loss.detach()), names=np.array(names), norms=np.array(norms), pick_name=np.array(pick_name),
+        pick_idx=np.array(pick_idx), pick_val=np.array(pick_val))
+
+
 if __name__ == "__main__":
     import oracle as O
 
@@ -277,6 +333,7 @@ if __name__ == "__main__":
     make_lib_tests()
     p, c, t, b = make_water()
     make_water_compressed(p, c, t, b)
+    make_train_grad()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
