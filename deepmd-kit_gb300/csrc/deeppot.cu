@@ -110,6 +110,53 @@ __global__ void force_gather_model_kernel(double* __restrict__ force, double* __
     for (int k = 0; k < 9; ++k) atom_vir[9 * (size_t)row + k] = av[k];
 }
 
+// The same with explicit extended atoms (external list, one frame): every one
+// of the nall atoms gets its force and atomic virial (the caller sums ghost
+// entries back onto their owners, as LAMMPS's reverse communication does).
+template <typename T>
+__global__ void force_gather_ext_kernel(double* __restrict__ force, double* __restrict__ atom_vir,
+                                        const T* __restrict__ g, Transpose tr, const int* __restrict__ nlist,
+                                        const double* __restrict__ coord_ext, int nloc, int nall, int nnei) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nall) return;
+  double f[3] = {0, 0, 0};
+  if (e < nloc) {
+    const T* gr = g + (size_t)e * nnei * 3;
+    const int* nr = nlist + (size_t)e * nnei;
+    for (int s = 0; s < nnei; ++s) {
+      if (nr[s] < 0) continue;
+      f[0] += (double)gr[3 * s];
+      f[1] += (double)gr[3 * s + 1];
+      f[2] += (double)gr[3 * s + 2];
+    }
+  }
+  double av[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) av[k] = 0.0;
+  for (int t = tr.offsets[e]; t < tr.offsets[e + 1]; ++t) {
+    const int p = tr.pairs[t];
+    const double gg[3] = {(double)g[3 * (size_t)p], (double)g[3 * (size_t)p + 1], (double)g[3 * (size_t)p + 2]};
+    f[0] -= gg[0];
+    f[1] -= gg[1];
+    f[2] -= gg[2];
+    if (atom_vir) {
+      const int i = p / nnei;
+      const double d[3] = {coord_ext[3 * e] - coord_ext[3 * i], coord_ext[3 * e + 1] - coord_ext[3 * i + 1],
+                           coord_ext[3 * e + 2] - coord_ext[3 * i + 2]};
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int l = 0; l < 3; ++l) av[3 * k + l] -= gg[k] * d[l];
+    }
+  }
+  force[3 * (size_t)e] = f[0];
+  force[3 * (size_t)e + 1] = f[1];
+  force[3 * (size_t)e + 2] = f[2];
+  if (atom_vir)
+#pragma unroll
+    for (int k = 0; k < 9; ++k) atom_vir[9 * (size_t)e + k] = av[k];
+}
+
 // atom energy in the original order (+ per-type bias), 0 for virtual atoms
 __global__ void atom_energy_kernel(double* __restrict__ e_row, const double* __restrict__ e_sorted,
                                    const int* __restrict__ row_pos, const int* __restrict__ atype,
@@ -180,6 +227,11 @@ struct DeepPotImpl {
   DeviceBuffer ws_nlist, ws_cell, ws_tr, ws_keys, ws_status, ws_coord, ws_svec, ws_spos;
   DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf;
   DeviceBuffer io_coord, io_force, io_av, io_e, io_v, io_ae;
+  // external neighbour list (CSR over local atoms) kept between calls for
+  // `ago` > 0, with the ghost-inclusive types
+  DeviceBuffer ext_off, ext_idx, ext_atype;
+  int ext_nloc = -1, ext_nall = -1, ext_sorted = 0;
+  std::vector<int> ext_atype_h;
   std::string err;
   int launches = 0;
   cudaStream_t stream = nullptr;
@@ -567,21 +619,35 @@ int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host
   return DPGB_OK;
 }
 
+// An external neighbour list with explicit ghost atoms (one frame): device
+// coordinates / types of all nall atoms (local first) and a CSR list over
+// the local atoms.
+struct ExtList {
+  const double* coord;
+  const int* atype;
+  int nall;
+  const int* off;
+  const int* idx;
+  int sorted;
+};
+
 template <typename T>
 int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* coord_dev, const double* box_host,
-        double* energy, double* force, double* virial, double* atom_energy, double* atom_virial, cudaStream_t st) {
+        double* energy, double* force, double* virial, double* atom_energy, double* atom_virial, cudaStream_t st,
+        const ExtList* ext = nullptr) {
   const dpgb_se_a_desc& d = dp.desc;
   const int nnei = dp.sel.nnei;
   const long long nrows = (long long)nframes * natom;
   if (nrows >= (1LL << 31) / std::max(nnei, 1)) return fail(DPGB_EINVAL, "too many atoms for 32-bit pair ids");
+  if (ext && nframes != 1) return fail(DPGB_EINVAL, "an external neighbour list covers one frame");
   int launches = 0;
   // --- geometry (host) ---
-  std::vector<CellGeom> geo(nframes);
-  std::vector<std::vector<int>> spos(nframes);
+  std::vector<CellGeom> geo(ext ? 0 : nframes);
+  std::vector<std::vector<int>> spos(ext ? 0 : nframes);
   int nshift_max = 1;
   std::vector<std::vector<double>> svecs(nframes);
   std::vector<double> host_coord;
-  for (int f = 0; f < nframes; ++f) {
+  for (int f = 0; f < (int)geo.size(); ++f) {
     if (box_host) {
       CellGeom g0;
       DPGB_TRY(box_geom(box_host + 9 * f, g0));
@@ -622,15 +688,18 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   }
   // --- device workspace ---
   size_t cell_bytes = 0;
-  for (int f = 0; f < nframes; ++f) cell_bytes = std::max(cell_bytes, nlist_pt_workspace(natom, geo[f]));
+  for (int f = 0; f < (int)geo.size(); ++f) cell_bytes = std::max(cell_bytes, nlist_pt_workspace(natom, geo[f]));
   const long long npair = nrows * nnei;
+  // transpose keys: local rows (ghost images fold onto their atom), or every
+  // explicit extended atom with an external list (forces on ghosts returned)
+  const long long nkeys = ext ? (long long)ext->nall : nrows;
   const int ng = dp.ng, dim = dp.dim;
   int maxw = 0;
   for (int l = 1; l <= m.fit.n_hidden; ++l) maxw = std::max(maxw, m.fit.width[l]);
   DPGB_TRY(dp.ws_cell.alloc(cell_bytes));
   DPGB_TRY(dp.ws_nlist.alloc(sizeof(int) * npair));
   DPGB_TRY(dp.ws_keys.alloc(sizeof(int) * npair));
-  DPGB_TRY(dp.ws_tr.alloc(transpose_workspace(npair, (int)nrows)));
+  DPGB_TRY(dp.ws_tr.alloc(transpose_workspace(npair, (int)nkeys)));
   DPGB_TRY(dp.ws_status.alloc(sizeof(int) * kStatusSlots));
   DPGB_TRY(dp.ws_coord.alloc(sizeof(double) * nrows * 3));
   DPGB_TRY(dp.ws_svec.alloc(sizeof(double) * 3 * (size_t)nshift_max * nframes));
@@ -653,7 +722,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   {
     std::vector<double> sv((size_t)3 * nshift_max * nframes, 0.0);
     std::vector<int> sp(spos_n * nframes, -1);
-    for (int f = 0; f < nframes; ++f) {
+    for (int f = 0; f < (int)spos.size(); ++f) {
       std::copy(svecs[f].begin(), svecs[f].end(), sv.begin() + (size_t)3 * nshift_max * f);
       std::copy(spos[f].begin(), spos[f].end(), sp.begin() + spos_n * f);
     }
@@ -663,7 +732,12 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   double* coord_n = dp.ws_coord.as<double>();
   int* nlist = dp.ws_nlist.as<int>();
   dp.mark(DPGB_STAGE_NLIST, 0, st);
-  for (int f = 0; f < nframes; ++f) {
+  if (ext) {
+    DPGB_TRY(launch_format_ext(nlist, ext->coord, ext->atype, ext->off, ext->idx, natom, ext->nall, d.rcut, dp.sel,
+                               ext->sorted, status, st));
+    ++launches;
+  }
+  for (int f = 0; f < (int)geo.size(); ++f) {
     const double* cin = coord_dev + (size_t)f * natom * 3;
     double* cout = coord_n + (size_t)f * natom * 3;
     if (box_host) {
@@ -682,11 +756,14 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   dp.mark(DPGB_STAGE_TRANSPOSE, 0, st);
   Transpose tr;
   if (npair > 0) {
-    model_keys_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(dp.ws_keys.as<int>(), nlist, npair, nnei, natom);
+    // image-major indices fold onto their atom; explicit extended indices
+    // are their own keys
+    model_keys_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(dp.ws_keys.as<int>(), nlist, npair, nnei,
+                                                             ext ? ext->nall : natom);
     DPGB_TRY(check_launch("model_keys"));
     ++launches;
   }
-  DPGB_TRY(launch_transpose(tr, dp.ws_keys.as<int>(), npair, (int)nrows, 0, dp.ws_tr.ptr, status, st));
+  DPGB_TRY(launch_transpose(tr, dp.ws_keys.as<int>(), npair, (int)nkeys, 0, dp.ws_tr.ptr, status, st));
   launches += 4;
   dp.mark(DPGB_STAGE_TRANSPOSE, 1, st);
   // descriptor forward
@@ -711,6 +788,11 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   p.svec = dp.ws_svec.as<double>();
   p.nshift = nshift_max;
   p.row_pos = dp.row_pos_dev.as<int>();
+  if (ext) {
+    p.coord_ext = ext->coord;
+    p.atype_ext = ext->atype;
+    p.nall = ext->nall;
+  }
   // virtual rows have no sorted position: point them at row 0 only for
   // reading (the kernels never write a virtual row)
   bool tc_path = false;
@@ -797,9 +879,14 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   }
   dp.mark(DPGB_STAGE_DESC_BWD, 1, st);
   dp.mark(DPGB_STAGE_REDUCE, 0, st);
-  force_gather_model_kernel<T><<<ceil_div(nrows, 128), 128, 0, st>>>(
-      force, atom_virial, dp.ws_g.as<T>(), tr, nlist, coord_n, dp.ws_svec.as<double>(), nshift_max, natom, nnei,
-      (int)nrows);
+  if (ext) {
+    force_gather_ext_kernel<T><<<ceil_div(nkeys, 128), 128, 0, st>>>(force, atom_virial, dp.ws_g.as<T>(), tr, nlist,
+                                                                       ext->coord, natom, ext->nall, nnei);
+  } else {
+    force_gather_model_kernel<T><<<ceil_div(nrows, 128), 128, 0, st>>>(
+        force, atom_virial, dp.ws_g.as<T>(), tr, nlist, coord_n, dp.ws_svec.as<double>(), nshift_max, natom, nnei,
+        (int)nrows);
+  }
   DPGB_TRY(check_launch("force_gather"));
   ++launches;
   double* e_row = atom_energy ? atom_energy : dp.ws_erow.as<double>();
@@ -835,6 +922,88 @@ int compute_device_impl(DeepPotImpl& dp, int nframes, int natom, const double* c
   if (dp.precision == DPGB_PREC_FP64)
     return run<double>(dp, *dp.m64, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial, st);
   return run<float>(dp, *dp.m32, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial, st);
+}
+
+// One frame with explicit ghosts and a caller's neighbour list (the
+// DeepPot::compute(..., nghost, InputNlist, ago) path of
+// source/api_cc/src/DeepPotPT.cc:170-243).  ago == 0 (or a changed atom
+// count) takes the list afresh; ago > 0 reuses the stored one with the new
+// coordinates (the list is re-filtered at rcut and re-ordered every call,
+// as forward_lower does).  All pointers are host arrays.
+int compute_nlist_impl(DeepPotImpl& dp, int nall, int nghost, const double* coord, const int* atype, int inum,
+                       const int* ilist, const int* numneigh, const int* const* firstneigh, int ago, double* energy,
+                       double* force, double* virial, double* atom_energy, double* atom_virial) {
+  const int nloc = nall - nghost;
+  if (nall <= 0 || nghost < 0 || nloc <= 0) return fail(DPGB_EINVAL, "need nall > nghost >= 0");
+  if (!coord || !atype || !energy || !force || !virial) return fail(DPGB_EINVAL, "NULL argument");
+  cudaStream_t st = dp.stream;
+  const bool fresh = ago == 0 || dp.ext_nloc != nloc || dp.ext_nall != nall;
+  if (fresh) {
+    if (inum != nloc || !ilist || !numneigh || !firstneigh)
+      return fail(DPGB_EINVAL, "a new neighbour list needs inum == nall - nghost and ilist / numneigh / firstneigh");
+    std::vector<int> off(nloc + 1, 0), cnt(nloc, -1);
+    int maxn = 0;
+    for (int ii = 0; ii < inum; ++ii) {
+      const int i = ilist[ii];
+      if (i < 0 || i >= nloc || cnt[i] >= 0) return fail(DPGB_EINVAL, "ilist must list each local atom once");
+      if (numneigh[ii] < 0) return fail(DPGB_EINVAL, "negative numneigh");
+      cnt[i] = numneigh[ii];
+      maxn = std::max(maxn, numneigh[ii]);
+    }
+    for (int i = 0; i < nloc; ++i) off[i + 1] = off[i] + cnt[i];
+    std::vector<int> idx((size_t)std::max(off[nloc], 1), -1);
+    for (int ii = 0; ii < inum; ++ii) {
+      const int i = ilist[ii];
+      for (int k = 0; k < numneigh[ii]; ++k) {
+        const int j = firstneigh[ii][k];
+        if (j < 0 || j >= nall) return fail(DPGB_EINVAL, "neighbour index outside [0, nall)");
+        idx[(size_t)off[i] + k] = j;
+      }
+    }
+    DPGB_TRY(dp.ext_off.alloc(sizeof(int) * (nloc + 1)));
+    DPGB_TRY(dp.ext_idx.alloc(sizeof(int) * idx.size()));
+    DPGB_CUDA(cudaMemcpyAsync(dp.ext_off.ptr, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, st));
+    DPGB_CUDA(cudaMemcpyAsync(dp.ext_idx.ptr, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, st));
+    // forward_lower sorts (and cuts to sum(sel)) when the rows are wider
+    // than sum(sel) or the model is compressed (make_model.py:592-658)
+    dp.ext_sorted = (maxn > dp.sel.nnei || dp.desc.compressed) ? 1 : 0;
+    dp.ext_nloc = nloc;
+    dp.ext_nall = nall;
+    DPGB_CUDA(cudaStreamSynchronize(st));  // host staging vectors go out of scope
+  }
+  if (dp.ext_atype_h.size() != (size_t)nall || !std::equal(atype, atype + nall, dp.ext_atype_h.begin())) {
+    dp.ext_atype_h.assign(atype, atype + nall);
+    DPGB_TRY(dp.ext_atype.alloc(sizeof(int) * nall));
+    DPGB_CUDA(cudaMemcpyAsync(dp.ext_atype.ptr, dp.ext_atype_h.data(), sizeof(int) * nall, cudaMemcpyHostToDevice,
+                              st));
+  }
+  DPGB_TRY(prepare_types(dp, 1, nloc, atype, st));
+  DPGB_TRY(dp.io_coord.alloc(sizeof(double) * nall * 3));
+  DPGB_TRY(dp.io_force.alloc(sizeof(double) * nall * 3));
+  DPGB_TRY(dp.io_e.alloc(sizeof(double)));
+  DPGB_TRY(dp.io_v.alloc(sizeof(double) * 9));
+  DPGB_TRY(dp.io_ae.alloc(sizeof(double) * nall));
+  if (atom_virial) DPGB_TRY(dp.io_av.alloc(sizeof(double) * nall * 9));
+  DPGB_CUDA(cudaMemcpyAsync(dp.io_coord.ptr, coord, sizeof(double) * nall * 3, cudaMemcpyHostToDevice, st));
+  DPGB_CUDA(cudaMemsetAsync(dp.io_ae.ptr, 0, sizeof(double) * nall, st));  // ghosts carry no atom energy
+  ExtList ext{dp.io_coord.as<double>(), dp.ext_atype.as<int>(), nall, dp.ext_off.as<int>(), dp.ext_idx.as<int>(),
+              dp.ext_sorted};
+  double* ae = dp.io_ae.as<double>();
+  double* av = atom_virial ? dp.io_av.as<double>() : nullptr;
+  if (dp.precision == DPGB_PREC_FP64)
+    DPGB_TRY(run<double>(dp, *dp.m64, 1, nloc, dp.io_coord.as<double>(), nullptr, dp.io_e.as<double>(),
+                         dp.io_force.as<double>(), dp.io_v.as<double>(), ae, av, st, &ext));
+  else
+    DPGB_TRY(run<float>(dp, *dp.m32, 1, nloc, dp.io_coord.as<double>(), nullptr, dp.io_e.as<double>(),
+                        dp.io_force.as<double>(), dp.io_v.as<double>(), ae, av, st, &ext));
+  DPGB_CUDA(cudaMemcpyAsync(energy, dp.io_e.ptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+  DPGB_CUDA(cudaMemcpyAsync(force, dp.io_force.ptr, sizeof(double) * nall * 3, cudaMemcpyDeviceToHost, st));
+  DPGB_CUDA(cudaMemcpyAsync(virial, dp.io_v.ptr, sizeof(double) * 9, cudaMemcpyDeviceToHost, st));
+  if (atom_energy)
+    DPGB_CUDA(cudaMemcpyAsync(atom_energy, dp.io_ae.ptr, sizeof(double) * nall, cudaMemcpyDeviceToHost, st));
+  if (atom_virial)
+    DPGB_CUDA(cudaMemcpyAsync(atom_virial, dp.io_av.ptr, sizeof(double) * nall * 9, cudaMemcpyDeviceToHost, st));
+  return check_status(dp, st);  // synchronises
 }
 
 }  // namespace
@@ -977,6 +1146,19 @@ int dpgb_deeppot_compute_device(dpgb_deeppot* dp, int nframes, int natom, const 
   if (!dp) return fail(DPGB_EINVAL, "NULL handle");
   int rc = compute_device_impl(dp->impl, nframes, natom, coord, atype_host, box_host, energy, force, virial,
                                atom_energy, atom_virial, as_stream(stream));
+  dp->impl.err = rc == DPGB_OK ? "" : dpgb_last_error();
+  return rc;
+}
+
+int dpgb_deeppot_compute_nlist(dpgb_deeppot* dp, int nall, int nghost, const double* coord, const int* atype,
+                               const double* box, int inum, const int* ilist, const int* numneigh,
+                               const int* const* firstneigh, int ago, double* energy, double* force, double* virial,
+                               double* atom_energy, double* atom_virial) {
+  clear_error();
+  if (!dp) return fail(DPGB_EINVAL, "NULL handle");
+  (void)box;  // the caller's list and ghost coordinates already encode the periodicity
+  int rc = compute_nlist_impl(dp->impl, nall, nghost, coord, atype, inum, ilist, numneigh, firstneigh, ago, energy,
+                              force, virial, atom_energy, atom_virial);
   dp->impl.err = rc == DPGB_OK ? "" : dpgb_last_error();
   return rc;
 }

@@ -175,16 +175,12 @@ __device__ __forceinline__ void pair_env(const DescParams<float>& p, int t, int 
   const float* sd = p.dstd + ((size_t)ti * p.nnei + pi.slot) * 4;
   float e4[4] = {0.f, 0.f, 0.f, 0.f};
   if (pi.nb >= 0) {
-    const double* cf = p.coord + (size_t)f * p.nloc * 3;
-    const int s = pi.nb / p.nloc, jj = pi.nb - s * p.nloc;
-    const double* sv = p.svec + ((size_t)f * p.nshift + s) * 3;
-    const double dx = (cf[3 * jj] + sv[0]) - cf[3 * i];
-    const double dy = (cf[3 * jj + 1] + sv[1]) - cf[3 * i + 1];
-    const double dz = (cf[3 * jj + 2] + sv[2]) - cf[3 * i + 2];
-    dvec[0] = (float)dx;
-    dvec[1] = (float)dy;
-    dvec[2] = (float)dz;
-    pi.keep = p.pair_mask ? p.pair_mask[ti * p.ntypes + p.atype[jj]] : 1;
+    double dd[3];
+    const int tj = pair_disp(p, f, i, pi.nb, dd);
+    dvec[0] = (float)dd[0];
+    dvec[1] = (float)dd[1];
+    dvec[2] = (float)dd[2];
+    pi.keep = p.pair_mask ? p.pair_mask[ti * p.ntypes + tj] : 1;
     if (pi.keep) {
       const float nr2 = dvec[0] * dvec[0] + dvec[1] * dvec[1] + dvec[2] * dvec[2];
       const float nr = sqrtf(nr2);

@@ -652,7 +652,87 @@ __global__ void tr_sort_kernel(int* __restrict__ pairs, const int* __restrict__ 
   }
 }
 
+// An external neighbour list with explicit ghost atoms (CSR: row i holds
+// idx[off[i] .. off[i+1]) indices into coord_ext), formatted to typed
+// sections as forward_lower does (deepmd/pt/model/model/make_model.py:
+// 592-658 + nlist_distinguish_types): entries beyond rcut dropped; when
+// `sorted`, ordered by (FP64 distance, index) and cut to the nearest sum(sel),
+// otherwise kept in the caller's order; then per type the first sel[t].
+__global__ void __launch_bounds__(kSearchWarps * 32)
+format_ext_kernel(int* __restrict__ nlist, const double* __restrict__ coord, const int* __restrict__ atype,
+                  const int* __restrict__ off, const int* __restrict__ idx, int nloc, int nall, double rcut,
+                  SelInfo sel, int sorted, int* __restrict__ status) {
+  __shared__ double s_r[kSearchWarps][kCap];
+  __shared__ int s_idx[kSearchWarps][kCap];
+  __shared__ int s_type[kSearchWarps][kCap];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kSearchWarps + warp;
+  if (i >= nloc) return;
+  int* row = nlist + (size_t)i * sel.nnei;
+  for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
+  if (atype[i] < 0) return;
+  const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
+  const int beg = off[i], end = off[i + 1];
+  int n = 0;
+  bool overflow = false;
+  for (int p0 = beg; p0 < end; p0 += 32) {
+    const int p = p0 + lane;
+    bool keep = false;
+    double r = 0.0;
+    int j = -1, tj = -1;
+    if (p < end) {
+      j = idx[p];
+      if (j >= 0 && j < nall && (tj = atype[j]) >= 0) {
+        r = dist_fma(coord[3 * j] - xi, coord[3 * j + 1] - yi, coord[3 * j + 2] - zi);
+        keep = r <= rcut;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const int pos = n + __popc(m & ((1u << lane) - 1u));
+    if (keep) {
+      if (pos < kCap) {
+        s_r[warp][pos] = r;
+        s_idx[warp][pos] = j;
+        s_type[warp][pos] = tj;
+      } else {
+        overflow = true;
+      }
+    }
+    n += __popc(m);
+  }
+  overflow = __any_sync(0xffffffffu, overflow);
+  if (overflow) {
+    if (lane == 0) {
+      atomicMax(&status[kStatusOverflow], n);
+      atomicMax(&status[kStatusOverflowAtom], i + 1);
+    }
+    return;
+  }
+  __syncwarp();
+  for (int k = lane; k < n; k += 32) {
+    const double rk = s_r[warp][k];
+    const int ik = s_idx[warp][k], tk = s_type[warp][k];
+    int rank = 0, trank = 0;
+    for (int m2 = 0; m2 < n; ++m2) {
+      // sorted: by (distance, index); caller's order: by position in the row
+      const bool lt = sorted ? cand_less(s_r[warp][m2], s_idx[warp][m2], rk, ik) : m2 < k;
+      rank += lt;
+      trank += lt && s_type[warp][m2] == tk;
+    }
+    if (rank < sel.nnei && tk < sel.ntypes && trank < sel.sel[tk]) row[sel.sec[tk] + trank] = ik;
+  }
+}
+
 }  // namespace
+
+int launch_format_ext(int* nlist, const double* coord_ext, const int* atype_ext, const int* off, const int* idx,
+                      int nloc, int nall, double rcut, const SelInfo& sel, int sorted, int* status,
+                      cudaStream_t st) {
+  if (nloc <= 0) return DPGB_OK;
+  format_ext_kernel<<<ceil_div(nloc, kSearchWarps), kSearchWarps * 32, 0, st>>>(nlist, coord_ext, atype_ext, off, idx,
+                                                                                 nloc, nall, rcut, sel, sorted, status);
+  return check_launch("format_ext");
+}
 
 int launch_normalize(double* out, const double* in, int n, const CellGeom& g, cudaStream_t st) {
   if (n <= 0) return DPGB_OK;

@@ -58,6 +58,10 @@ int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc,
 int launch_format_nlist(int* nlist, const double* coord, const int* atype, const int* rows, int nall,
                         const int* counts, int max_nbor, int nloc, double rcut, const SelInfo& sel,
                         int* status, cudaStream_t st);
+// external list with explicit ghosts (CSR over the local atoms) -> typed list
+int launch_format_ext(int* nlist, const double* coord_ext, const int* atype_ext, const int* off, const int* idx,
+                      int nloc, int nall, double rcut, const SelInfo& sel, int sorted, int* status,
+                      cudaStream_t st);
 size_t transpose_workspace(long long npair, int nkeys);
 int launch_transpose(Transpose& tr, const int* keys, long long npair, int nkeys, int mod,
                      void* workspace, int* status, cudaStream_t st);

@@ -119,9 +119,6 @@ __host__ __device__ inline SmemLayout<T> make_layout(int nnei, int ng, int n_lay
 template <typename T, bool BWD>
 __device__ void row_env(const DescParams<T>& p, int row, int f, int i, int ti, T* s_rn, int* s_act,
                         double* s_d) {
-  const double* cf = p.coord + (size_t)f * p.nloc * 3;
-  const double xi = cf[3 * i], yi = cf[3 * i + 1], zi = cf[3 * i + 2];
-  const double* sv = p.svec + (size_t)f * p.nshift * 3;
   const T rmin = (T)p.rcut_smth, rmax = (T)p.rcut;
   for (int j = threadIdx.x; j < p.nnei; j += blockDim.x) {
     const int nb = p.nlist[(size_t)row * p.nnei + j];
@@ -131,11 +128,7 @@ __device__ void row_env(const DescParams<T>& p, int row, int f, int i, int ti, T
     int act = 0;
     double d[3] = {0.0, 0.0, 0.0};
     if (nb >= 0) {
-      const int s = nb / p.nloc, jj = nb - s * p.nloc;
-      d[0] = (cf[3 * jj] + sv[3 * s]) - xi;
-      d[1] = (cf[3 * jj + 1] + sv[3 * s + 1]) - yi;
-      d[2] = (cf[3 * jj + 2] + sv[3 * s + 2]) - zi;
-      const int tj = p.atype[jj];
+      const int tj = pair_disp(p, f, i, nb, d);
       act = p.pair_mask ? p.pair_mask[ti * p.ntypes + tj] : 1;
       if (act) {
         const T dt[3] = {(T)d[0], (T)d[1], (T)d[2]};

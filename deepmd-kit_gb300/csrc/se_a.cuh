@@ -83,7 +83,34 @@ struct DescParams {
   const double* svec;       // [nframes, nshift, 3] image shift vectors
   int nshift;
   const int* row_pos;       // [nrows] sorted (by type) row of each atom
+  // explicit extended atoms (an external neighbour list with ghost atoms,
+  // as LAMMPS passes them): when coord_ext is set, nlist holds indices into
+  // coord_ext [nframes, nall, 3] / atype_ext [nframes, nall] (local atoms
+  // first) instead of image-major extended indices
+  const double* coord_ext;
+  const int* atype_ext;
+  int nall;
 };
+
+// r_nb - r_i in FP64 for neighbour nb of local atom i of frame f, and the
+// neighbour's type.  Image-major indices: r_nb = coord[nb % nloc] + shift.
+template <typename T>
+__device__ __forceinline__ int pair_disp(const DescParams<T>& p, int f, int i, int nb, double d[3]) {
+  if (p.coord_ext) {
+    const double* ce = p.coord_ext + (size_t)f * p.nall * 3;
+    d[0] = ce[3 * nb] - ce[3 * i];
+    d[1] = ce[3 * nb + 1] - ce[3 * i + 1];
+    d[2] = ce[3 * nb + 2] - ce[3 * i + 2];
+    return p.atype_ext[(size_t)f * p.nall + nb];
+  }
+  const double* cf = p.coord + (size_t)f * p.nloc * 3;
+  const int s = nb / p.nloc, jj = nb - s * p.nloc;
+  const double* sv = p.svec + ((size_t)f * p.nshift + s) * 3;
+  d[0] = (cf[3 * jj] + sv[0]) - cf[3 * i];
+  d[1] = (cf[3 * jj + 1] + sv[1]) - cf[3 * i + 1];
+  d[2] = (cf[3 * jj + 2] + sv[2]) - cf[3 * i + 2];
+  return p.atype[jj];
+}
 
 // Fitting nets of all types: W[l] [ntypes, nin_l, nout_l] ...
 template <typename T>

@@ -59,13 +59,12 @@ __device__ __forceinline__ void slot_env(const DescParams<float>& p, int row, in
   s.d[0] = s.d[1] = s.d[2] = 0.f;
   int keep = 1;
   if (s.nb >= 0) {
-    const double* cf = p.coord + (size_t)f * p.nloc * 3;
-    const int sh = s.nb / p.nloc, jj = s.nb - sh * p.nloc;
-    const double* sv = p.svec + ((size_t)f * p.nshift + sh) * 3;
-    s.d[0] = (float)((cf[3 * jj] + sv[0]) - cf[3 * i]);
-    s.d[1] = (float)((cf[3 * jj + 1] + sv[1]) - cf[3 * i + 1]);
-    s.d[2] = (float)((cf[3 * jj + 2] + sv[2]) - cf[3 * i + 2]);
-    keep = p.pair_mask ? p.pair_mask[ti * p.ntypes + p.atype[jj]] : 1;
+    double dd[3];
+    const int tj = pair_disp(p, f, i, s.nb, dd);
+    s.d[0] = (float)dd[0];
+    s.d[1] = (float)dd[1];
+    s.d[2] = (float)dd[2];
+    keep = p.pair_mask ? p.pair_mask[ti * p.ntypes + tj] : 1;
     if (keep) {
       const float nr2 = s.d[0] * s.d[0] + s.d[1] * s.d[1] + s.d[2] * s.d[2];
       const float nr = sqrtf(nr2);

@@ -118,6 +118,8 @@ _SIGS = {
     "dpgb_deeppot_check_ok": [_P],
     "dpgb_deeppot_compute": [_P, _I, _I, _DP, _IP, _DP, _DP, _DP, _DP, _DP, _DP],
     "dpgb_deeppot_compute_device": [_P, _I, _I, _P, _IP, _DP, _P, _P, _P, _P, _P, _P],
+    "dpgb_deeppot_compute_nlist": [_P, _I, _I, _DP, _IP, _DP, _I, _IP, _IP, C.POINTER(_IP), _I, _DP, _DP, _DP,
+                                   _DP, _DP],
     "dpgb_deeppot_last_launches": [_P],
     "dpgb_deeppot_set_profiling": [_P, _I],
     "dpgb_deeppot_collect_stages": [_P],

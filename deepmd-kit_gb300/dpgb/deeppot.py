@@ -147,6 +147,42 @@ class DeepPot:
             return e, f, v, ae, av
         return e, f, v
 
+    def eval_nlist(self, coord, atype, nghost, ilist, numneigh, firstneigh, ago=0, atomic=False):
+        """One frame with explicit ghosts and the caller's neighbour list
+        (DP_DeepPotComputeNList): coord [nall, 3] (local atoms first), atype
+        [nall], the InputNlist arrays (firstneigh: one integer array per
+        entry of ilist).  Returns energy, force [nall, 3] and virial (and the
+        atomic energy [nall] / virial [nall, 9]) — forces on the ghosts
+        included."""
+        atype = np.ascontiguousarray(atype, dtype=np.int32).reshape(-1)
+        nall = atype.shape[0]
+        coord = np.ascontiguousarray(coord, dtype=np.float64).reshape(nall * 3)
+        ip = C.POINTER(C.c_int)
+        rows = [np.ascontiguousarray(r, dtype=np.int32) for r in (firstneigh or [])]
+        fn = (ip * max(len(rows), 1))(*[r.ctypes.data_as(ip) for r in rows])
+        ilist_p = numneigh_p = C.cast(None, ip)
+        if ilist is not None:  # ago > 0 may pass no list
+            ilist = np.ascontiguousarray(ilist, dtype=np.int32)
+            numneigh = np.ascontiguousarray(numneigh, dtype=np.int32)
+            ilist_p, numneigh_p = ilist.ctypes.data_as(ip), numneigh.ctypes.data_as(ip)
+        e = np.zeros(1)
+        f = np.zeros((nall, 3))
+        v = np.zeros(9)
+        ae = np.zeros(nall) if atomic else None
+        av = np.zeros((nall, 9)) if atomic else None
+        dp = C.POINTER(C.c_double)
+
+        def P(a):
+            return C.cast(None, dp) if a is None else a.ctypes.data_as(dp)
+
+        rc = _lib.lib().dpgb_deeppot_compute_nlist(self._h, nall, int(nghost), P(coord), atype.ctypes.data_as(ip),
+                                                   C.cast(None, dp), len(rows), ilist_p, numneigh_p, fn, int(ago),
+                                                   P(e), P(f), P(v), P(ae), P(av))
+        _lib.check(rc)
+        if atomic:
+            return e[0], f, v, ae, av
+        return e[0], f, v
+
     def eval_device(self, coord, box, atype, atomic: bool = False, out=None):
         """Device form: ``coord`` a CUDA float64 tensor [nframes, natom*3]
         (or [natom, 3]); ``box`` host array or None; ``atype`` host array.

@@ -442,6 +442,28 @@ int dpgb_deeppot_compute_device(dpgb_deeppot* dp, int nframes, int natom,
                                 double* atom_energy, double* atom_virial,
                                 void* stream);
 
+/* One frame with explicit ghost atoms and the caller's neighbour list, HOST
+ * buffers: the DeepPot::compute(..., nghost, InputNlist, ago) path
+ * (source/api_cc/src/DeepPotPT.cc:170-243) behind DP_DeepPotComputeNList
+ * (source/api_c/include/c_api.h:310-322).  coord [nall, 3] and atype [nall]
+ * with the nloc = nall - nghost local atoms first; the list is LAMMPS's
+ * InputNlist: ilist [inum], numneigh [inum], firstneigh[inum][numneigh[ii]]
+ * (indices in [0, nall), any order, may reach beyond rcut).  ago == 0 takes
+ * the list afresh; ago > 0 reuses the stored list with the new coordinates.
+ * Each call filters the list at rcut and orders it as forward_lower does
+ * (by distance when a row is wider than sum(sel) or the model is
+ * compressed, else the caller's order; then per type the first sel[t]).
+ * Outputs: energy [1], virial [9], force [nall, 3] and atom_virial
+ * [nall, 9] including the ghosts (the caller sums ghost entries back onto
+ * their owners), atom_energy [nall] (0 on ghosts); box is not used. */
+int dpgb_deeppot_compute_nlist(dpgb_deeppot* dp, int nall, int nghost,
+                               const double* coord, const int* atype,
+                               const double* box, int inum, const int* ilist,
+                               const int* numneigh,
+                               const int* const* firstneigh, int ago,
+                               double* energy, double* force, double* virial,
+                               double* atom_energy, double* atom_virial);
+
 /* Number of kernel launches the last compute issued (for the benchmark). */
 int dpgb_deeppot_last_launches(dpgb_deeppot* dp);
 
