@@ -157,6 +157,96 @@ __global__ void force_gather_ext_kernel(double* __restrict__ force, double* __re
     for (int k = 0; k < 9; ++k) atom_vir[9 * (size_t)e + k] = av[k];
 }
 
+// batch of frames: the key of a pair is its neighbour's global atom
+__global__ void batch_keys_kernel(int* __restrict__ keys, const int* __restrict__ nlist, long long npair, int nnei,
+                                  FrameTab ft) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npair) return;
+  const int nb = nlist[p];
+  if (nb < 0) {
+    keys[p] = -1;
+    return;
+  }
+  const int row = (int)(p / nnei);
+  const int fr = frame_of(ft.atom_off, ft.nframes, row);
+  const int beg = ft.atom_off[fr], nl = ft.atom_off[fr + 1] - beg;
+  keys[p] = beg + nb % nl;
+}
+
+// force_gather_model_kernel for a batch (per-frame image shifts)
+template <typename T>
+__global__ void force_gather_batch_kernel(double* __restrict__ force, double* __restrict__ atom_vir,
+                                          const T* __restrict__ g, Transpose tr, const int* __restrict__ nlist,
+                                          const double* __restrict__ coord, const double* __restrict__ svec,
+                                          FrameTab ft, int nnei, int nrows) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= nrows) return;
+  double f[3] = {0, 0, 0};
+  const T* gr = g + (size_t)row * nnei * 3;
+  const int* nr = nlist + (size_t)row * nnei;
+  for (int s = 0; s < nnei; ++s) {
+    if (nr[s] < 0) continue;
+    f[0] += (double)gr[3 * s];
+    f[1] += (double)gr[3 * s + 1];
+    f[2] += (double)gr[3 * s + 2];
+  }
+  double av[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) av[k] = 0.0;
+  for (int t = tr.offsets[row]; t < tr.offsets[row + 1]; ++t) {
+    const int p = tr.pairs[t];
+    const double g0 = (double)g[3 * (size_t)p], g1 = (double)g[3 * (size_t)p + 1], g2 = (double)g[3 * (size_t)p + 2];
+    f[0] -= g0;
+    f[1] -= g1;
+    f[2] -= g2;
+    if (atom_vir) {
+      const int i = p / nnei;  // centre (global row)
+      const int fr = frame_of(ft.atom_off, ft.nframes, i);
+      const int beg = ft.atom_off[fr], nl = ft.atom_off[fr + 1] - beg;
+      const int nb = nlist[p];
+      const int s = nb / nl, jj = beg + (nb - s * nl);
+      const double* sv = svec + 3 * ((size_t)ft.svec_off[fr] + s);
+      const double d[3] = {(coord[3 * jj] + sv[0]) - coord[3 * i], (coord[3 * jj + 1] + sv[1]) - coord[3 * i + 1],
+                           (coord[3 * jj + 2] + sv[2]) - coord[3 * i + 2]};
+      const double gg[3] = {g0, g1, g2};
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int l = 0; l < 3; ++l) av[3 * k + l] -= gg[k] * d[l];
+    }
+  }
+  force[3 * (size_t)row] = f[0];
+  force[3 * (size_t)row + 1] = f[1];
+  force[3 * (size_t)row + 2] = f[2];
+  if (atom_vir)
+#pragma unroll
+    for (int k = 0; k < 9; ++k) atom_vir[9 * (size_t)row + k] = av[k];
+}
+
+// per-frame sums over ragged frames: blockIdx.x = frame, blockIdx.y = 0
+// energy, 1..9 virial
+__global__ void frame_sum_batch_kernel(double* __restrict__ energy, double* __restrict__ virial,
+                                       const double* __restrict__ e_row, const double* __restrict__ vir_row,
+                                       const int* __restrict__ atom_off) {
+  __shared__ double s[256];
+  const int f = blockIdx.x, q = blockIdx.y;
+  double acc = 0.0;
+  for (int r = atom_off[f] + threadIdx.x; r < atom_off[f + 1]; r += blockDim.x)
+    acc += q == 0 ? e_row[r] : vir_row[(size_t)r * 9 + (q - 1)];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (q == 0)
+      energy[f] = s[0];
+    else
+      virial[(size_t)f * 9 + q - 1] = s[0];
+  }
+}
+
 // atom energy in the original order (+ per-type bias), 0 for virtual atoms
 __global__ void atom_energy_kernel(double* __restrict__ e_row, const double* __restrict__ e_sorted,
                                    const int* __restrict__ row_pos, const int* __restrict__ atype,
@@ -206,6 +296,9 @@ struct DeepPotImpl {
   std::vector<int> atype_cache;
   std::vector<int> row_pos_h, type_count, type_off;
   int cached_nframes = -1;
+  // bumped whenever cached device state may change (types, workspace): a
+  // batch's captured CUDA graph is replayed only while this stays put
+  unsigned long long gen = 0;
   DeviceBuffer row_pos_dev, atype_dev, sorted_rows_dev, chunks_dev;
   int nchunks = 0;
   // tensor-core embedding (mixed precision)
@@ -539,6 +632,7 @@ int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host
   const bool same = dp.cached_nframes == nframes && (int)dp.atype_cache.size() == natom &&
                     std::equal(dp.atype_cache.begin(), dp.atype_cache.end(), atype_host);
   if (same) return DPGB_OK;
+  ++dp.gen;
   const int nt = dp.desc.ntypes;
   for (int i = 0; i < natom; ++i)
     if (atype_host[i] >= nt) return fail(DPGB_EINVAL, "atom type out of range");
@@ -631,19 +725,30 @@ struct ExtList {
   int sorted;
 };
 
+// A batch of periodic frames of different sizes (device tables prepared once;
+// the evaluation itself only launches kernels, so it can be captured in a
+// CUDA graph).  The frames' atoms are the rows of one "frame" of natoms.
+struct BatchIn {
+  FrameTab ft;
+  int ncells;
+  const double* svec;
+  const int* spos;
+};
+
 template <typename T>
 int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* coord_dev, const double* box_host,
         double* energy, double* force, double* virial, double* atom_energy, double* atom_virial, cudaStream_t st,
-        const ExtList* ext = nullptr) {
+        const ExtList* ext = nullptr, const BatchIn* batch = nullptr) {
   const dpgb_se_a_desc& d = dp.desc;
   const int nnei = dp.sel.nnei;
   const long long nrows = (long long)nframes * natom;
   if (nrows >= (1LL << 31) / std::max(nnei, 1)) return fail(DPGB_EINVAL, "too many atoms for 32-bit pair ids");
-  if (ext && nframes != 1) return fail(DPGB_EINVAL, "an external neighbour list covers one frame");
+  if ((ext || batch) && nframes != 1) return fail(DPGB_EINVAL, "an external list or a batch runs as one frame");
   int launches = 0;
+  const bool own_geom = !ext && !batch;
   // --- geometry (host) ---
-  std::vector<CellGeom> geo(ext ? 0 : nframes);
-  std::vector<std::vector<int>> spos(ext ? 0 : nframes);
+  std::vector<CellGeom> geo(own_geom ? nframes : 0);
+  std::vector<std::vector<int>> spos(own_geom ? nframes : 0);
   int nshift_max = 1;
   std::vector<std::vector<double>> svecs(nframes);
   std::vector<double> host_coord;
@@ -696,6 +801,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   const int ng = dp.ng, dim = dp.dim;
   int maxw = 0;
   for (int l = 1; l <= m.fit.n_hidden; ++l) maxw = std::max(maxw, m.fit.width[l]);
+  if (batch) cell_bytes = nlist_batch_workspace(natom, batch->ncells);
   DPGB_TRY(dp.ws_cell.alloc(cell_bytes));
   DPGB_TRY(dp.ws_nlist.alloc(sizeof(int) * npair));
   DPGB_TRY(dp.ws_keys.alloc(sizeof(int) * npair));
@@ -718,8 +824,9 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
 
   int* status = dp.ws_status.as<int>();
   DPGB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * kStatusSlots, st));
-  // shift tables
-  {
+  // shift tables (a batch brings its own; nothing host-side may run inside
+  // a captured batch evaluation)
+  if (own_geom) {
     std::vector<double> sv((size_t)3 * nshift_max * nframes, 0.0);
     std::vector<int> sp(spos_n * nframes, -1);
     for (int f = 0; f < (int)spos.size(); ++f) {
@@ -736,6 +843,11 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     DPGB_TRY(launch_format_ext(nlist, ext->coord, ext->atype, ext->off, ext->idx, natom, ext->nall, d.rcut, dp.sel,
                                ext->sorted, status, st));
     ++launches;
+  }
+  if (batch) {
+    DPGB_TRY(launch_nlist_batch(nlist, coord_n, coord_dev, dp.atype_dev.as<int>(), natom, batch->ncells, batch->ft,
+                                batch->svec, batch->spos, d.rcut, dp.sel, dp.ws_cell.ptr, status, st));
+    launches += 4;
   }
   for (int f = 0; f < (int)geo.size(); ++f) {
     const double* cin = coord_dev + (size_t)f * natom * 3;
@@ -758,8 +870,11 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   if (npair > 0) {
     // image-major indices fold onto their atom; explicit extended indices
     // are their own keys
-    model_keys_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(dp.ws_keys.as<int>(), nlist, npair, nnei,
-                                                             ext ? ext->nall : natom);
+    if (batch)
+      batch_keys_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(dp.ws_keys.as<int>(), nlist, npair, nnei, batch->ft);
+    else
+      model_keys_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(dp.ws_keys.as<int>(), nlist, npair, nnei,
+                                                               ext ? ext->nall : natom);
     DPGB_TRY(check_launch("model_keys"));
     ++launches;
   }
@@ -792,6 +907,12 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     p.coord_ext = ext->coord;
     p.atype_ext = ext->atype;
     p.nall = ext->nall;
+  }
+  if (batch) {
+    p.svec = batch->svec;
+    p.frame_atom_off = batch->ft.atom_off;
+    p.frame_svec_off = batch->ft.svec_off;
+    p.nframes_batch = batch->ft.nframes;
   }
   // virtual rows have no sorted position: point them at row 0 only for
   // reading (the kernels never write a virtual row)
@@ -882,6 +1003,10 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   if (ext) {
     force_gather_ext_kernel<T><<<ceil_div(nkeys, 128), 128, 0, st>>>(force, atom_virial, dp.ws_g.as<T>(), tr, nlist,
                                                                        ext->coord, natom, ext->nall, nnei);
+  } else if (batch) {
+    force_gather_batch_kernel<T><<<ceil_div(nrows, 128), 128, 0, st>>>(force, atom_virial, dp.ws_g.as<T>(), tr, nlist,
+                                                                         coord_n, batch->svec, batch->ft, nnei,
+                                                                         (int)nrows);
   } else {
     force_gather_model_kernel<T><<<ceil_div(nrows, 128), 128, 0, st>>>(
         force, atom_virial, dp.ws_g.as<T>(), tr, nlist, coord_n, dp.ws_svec.as<double>(), nshift_max, natom, nnei,
@@ -894,7 +1019,11 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
                                                            dp.atype_dev.as<int>(), dp.bias_dev.as<double>(), natom,
                                                            (int)nrows);
   DPGB_TRY(check_launch("atom_energy"));
-  frame_sum_kernel<<<dim3(nframes, 10), 256, 0, st>>>(energy, virial, e_row, dp.ws_vir.as<double>(), natom);
+  if (batch)
+    frame_sum_batch_kernel<<<dim3(batch->ft.nframes, 10), 256, 0, st>>>(energy, virial, e_row, dp.ws_vir.as<double>(),
+                                                                         batch->ft.atom_off);
+  else
+    frame_sum_kernel<<<dim3(nframes, 10), 256, 0, st>>>(energy, virial, e_row, dp.ws_vir.as<double>(), natom);
   DPGB_TRY(check_launch("frame_sum"));
   launches += 2;
   dp.mark(DPGB_STAGE_REDUCE, 1, st);
@@ -918,6 +1047,7 @@ int compute_device_impl(DeepPotImpl& dp, int nframes, int natom, const double* c
                         double* atom_virial, cudaStream_t st) {
   if (nframes <= 0 || natom <= 0) return fail(DPGB_EINVAL, "nframes and natom must be positive");
   if (!coord || !atype_host || !energy || !force || !virial) return fail(DPGB_EINVAL, "NULL argument");
+  ++dp.gen;  // workspace may grow
   DPGB_TRY(prepare_types(dp, nframes, natom, atype_host, st));
   if (dp.precision == DPGB_PREC_FP64)
     return run<double>(dp, *dp.m64, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial, st);
@@ -937,6 +1067,7 @@ int compute_nlist_impl(DeepPotImpl& dp, int nall, int nghost, const double* coor
   if (nall <= 0 || nghost < 0 || nloc <= 0) return fail(DPGB_EINVAL, "need nall > nghost >= 0");
   if (!coord || !atype || !energy || !force || !virial) return fail(DPGB_EINVAL, "NULL argument");
   cudaStream_t st = dp.stream;
+  ++dp.gen;  // workspace may grow
   const bool fresh = ago == 0 || dp.ext_nloc != nloc || dp.ext_nall != nall;
   if (fresh) {
     if (inum != nloc || !ilist || !numneigh || !firstneigh)
@@ -1004,6 +1135,145 @@ int compute_nlist_impl(DeepPotImpl& dp, int nall, int nghost, const double* coor
   if (atom_virial)
     DPGB_CUDA(cudaMemcpyAsync(atom_virial, dp.io_av.ptr, sizeof(double) * nall * 9, cudaMemcpyDeviceToHost, st));
   return check_status(dp, st);  // synchronises
+}
+
+// ---- batches of frames of different sizes ------------------------------------
+
+// cell geometry and image tables of one periodic frame, in the reference's
+// image range (nbuff = ceil(rcut / face distance))
+int frame_geometry(const double* c, double rcut, CellGeom& g, std::vector<int>& spos, std::vector<double>& svec) {
+  auto crn = [&](int p, int q) {
+    const double x = c[p * 3 + 1] * c[q * 3 + 2] - c[p * 3 + 2] * c[q * 3 + 1];
+    const double y = c[p * 3 + 2] * c[q * 3 + 0] - c[p * 3 + 0] * c[q * 3 + 2];
+    const double z = c[p * 3 + 0] * c[q * 3 + 1] - c[p * 3 + 1] * c[q * 3 + 0];
+    return std::sqrt(x * x + y * y + z * z);
+  };
+  const double vol = std::fabs(c[0] * (c[4] * c[8] - c[5] * c[7]) - c[1] * (c[3] * c[8] - c[5] * c[6]) +
+                               c[2] * (c[3] * c[7] - c[4] * c[6]));
+  if (!(vol > 0)) return fail(DPGB_EINVAL, "batch frame with a degenerate box");
+  const int nb[3] = {(int)std::ceil(rcut / (vol / crn(1, 2))), (int)std::ceil(rcut / (vol / crn(2, 0))),
+                     (int)std::ceil(rcut / (vol / crn(0, 1)))};
+  const std::vector<int> shifts = default_shifts(nb);
+  const int ns = (int)shifts.size() / 3;
+  DPGB_TRY(periodic_geom(c, rcut, ns, shifts.data(), g, spos));
+  for (int k = 0; k < 3; ++k)
+    if (g.reach[k] > 2) return fail(DPGB_EINVAL, "batch frame thinner than rcut / 2 across a face");
+  shift_vectors(g, shifts.data(), ns, svec);
+  return DPGB_OK;
+}
+
+struct BatchImpl {
+  DeepPotImpl* dp = nullptr;
+  int nframes = 0, natoms = 0, ncells = 0;
+  std::vector<int> atype, atom_off_h;
+  DeviceBuffer atom_off, cell_off, spos_off, svec_off, geom, svec, spos;
+  BatchIn in{};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const void* cap_ptr[4] = {};
+  cudaStream_t cap_stream = nullptr;
+  unsigned long long cap_gen = ~0ull;
+  ~BatchImpl() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
+int batch_setup(BatchImpl& b, DeepPotImpl& dp, int nframes, const int* natoms, const int* atype, const double* box) {
+  if (nframes < 1 || !natoms || !atype || !box) return fail(DPGB_EINVAL, "batch: bad arguments");
+  b.dp = &dp;
+  b.nframes = nframes;
+  b.atom_off_h.assign(nframes + 1, 0);
+  std::vector<int> cell_off(nframes + 1, 0), spos_off(nframes + 1, 0), svec_off(nframes + 1, 0);
+  std::vector<CellGeom> geom(nframes);
+  std::vector<int> spos_all;
+  std::vector<double> svec_all;
+  for (int f = 0; f < nframes; ++f) {
+    if (natoms[f] < 1) return fail(DPGB_EINVAL, "batch: a frame without atoms");
+    b.atom_off_h[f + 1] = b.atom_off_h[f] + natoms[f];
+    std::vector<int> sp;
+    std::vector<double> sv;
+    DPGB_TRY(frame_geometry(box + 9 * f, dp.desc.rcut, geom[f], sp, sv));
+    cell_off[f + 1] = cell_off[f] + geom[f].ncell[0] * geom[f].ncell[1] * geom[f].ncell[2];
+    spos_off[f + 1] = spos_off[f] + (int)sp.size();
+    svec_off[f + 1] = svec_off[f] + (int)sv.size() / 3;
+    spos_all.insert(spos_all.end(), sp.begin(), sp.end());
+    svec_all.insert(svec_all.end(), sv.begin(), sv.end());
+  }
+  b.natoms = b.atom_off_h[nframes];
+  b.ncells = cell_off[nframes];
+  b.atype.assign(atype, atype + b.natoms);
+  DPGB_TRY(b.atom_off.alloc(sizeof(int) * (nframes + 1)));
+  DPGB_TRY(b.cell_off.alloc(sizeof(int) * (nframes + 1)));
+  DPGB_TRY(b.spos_off.alloc(sizeof(int) * (nframes + 1)));
+  DPGB_TRY(b.svec_off.alloc(sizeof(int) * (nframes + 1)));
+  DPGB_TRY(b.geom.alloc(sizeof(CellGeom) * nframes));
+  DPGB_TRY(b.spos.alloc(sizeof(int) * spos_all.size()));
+  DPGB_TRY(b.svec.alloc(sizeof(double) * svec_all.size()));
+  DPGB_CUDA(cudaMemcpy(b.atom_off.ptr, b.atom_off_h.data(), sizeof(int) * (nframes + 1), cudaMemcpyHostToDevice));
+  DPGB_CUDA(cudaMemcpy(b.cell_off.ptr, cell_off.data(), sizeof(int) * (nframes + 1), cudaMemcpyHostToDevice));
+  DPGB_CUDA(cudaMemcpy(b.spos_off.ptr, spos_off.data(), sizeof(int) * (nframes + 1), cudaMemcpyHostToDevice));
+  DPGB_CUDA(cudaMemcpy(b.svec_off.ptr, svec_off.data(), sizeof(int) * (nframes + 1), cudaMemcpyHostToDevice));
+  DPGB_CUDA(cudaMemcpy(b.geom.ptr, geom.data(), sizeof(CellGeom) * nframes, cudaMemcpyHostToDevice));
+  DPGB_CUDA(cudaMemcpy(b.spos.ptr, spos_all.data(), sizeof(int) * spos_all.size(), cudaMemcpyHostToDevice));
+  DPGB_CUDA(cudaMemcpy(b.svec.ptr, svec_all.data(), sizeof(double) * svec_all.size(), cudaMemcpyHostToDevice));
+  b.in.ft = FrameTab{nframes, b.atom_off.as<int>(), b.cell_off.as<int>(), b.spos_off.as<int>(), b.svec_off.as<int>(),
+                     b.geom.as<CellGeom>()};
+  b.in.ncells = b.ncells;
+  b.in.svec = b.svec.as<double>();
+  b.in.spos = b.spos.as<int>();
+  return DPGB_OK;
+}
+
+int batch_run(BatchImpl& b, const double* coord, double* energy, double* force, double* virial, cudaStream_t st) {
+  DeepPotImpl& dp = *b.dp;
+  if (dp.precision == DPGB_PREC_FP64)
+    return run<double>(dp, *dp.m64, 1, b.natoms, coord, nullptr, energy, force, virial, nullptr, nullptr, st, nullptr,
+                       &b.in);
+  return run<float>(dp, *dp.m32, 1, b.natoms, coord, nullptr, energy, force, virial, nullptr, nullptr, st, nullptr,
+                    &b.in);
+}
+
+// Device coordinates in, device outputs; with use_graph the kernel sequence
+// is captured once (after one plain evaluation has sized every buffer) and
+// replayed while the handle's cached state and the buffers stay the same.
+int batch_compute(BatchImpl& b, const double* coord, double* energy, double* force, double* virial,
+                  cudaStream_t st, int use_graph) {
+  DeepPotImpl& dp = *b.dp;
+  if (!coord || !energy || !force || !virial) return fail(DPGB_EINVAL, "batch: NULL argument");
+  DPGB_TRY(prepare_types(dp, 1, b.natoms, b.atype.data(), st));
+  const void* ptrs[4] = {coord, energy, force, virial};
+  const bool same = b.exec && dp.gen == b.cap_gen && st == b.cap_stream &&
+                    std::equal(ptrs, ptrs + 4, b.cap_ptr);
+  if (use_graph && same) {
+    DPGB_CUDA(cudaGraphLaunch(b.exec, st));
+    return DPGB_OK;
+  }
+  DPGB_TRY(batch_run(b, coord, energy, force, virial, st));
+  if (!use_graph) return DPGB_OK;
+  if (b.exec) {
+    cudaGraphExecDestroy(b.exec);
+    b.exec = nullptr;
+  }
+  if (b.graph) {
+    cudaGraphDestroy(b.graph);
+    b.graph = nullptr;
+  }
+  const int prof = dp.profiling;
+  dp.profiling = 0;  // no event records inside the graph
+  DPGB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+  const int rc = batch_run(b, coord, energy, force, virial, st);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(st, &g);
+  dp.profiling = prof;
+  DPGB_TRY(rc);
+  DPGB_CUDA(ce);
+  b.graph = g;
+  DPGB_CUDA(cudaGraphInstantiate(&b.exec, b.graph, 0));
+  std::copy(ptrs, ptrs + 4, b.cap_ptr);
+  b.cap_gen = dp.gen;
+  b.cap_stream = st;
+  return DPGB_OK;
 }
 
 }  // namespace
@@ -1147,6 +1417,66 @@ int dpgb_deeppot_compute_device(dpgb_deeppot* dp, int nframes, int natom, const 
   int rc = compute_device_impl(dp->impl, nframes, natom, coord, atype_host, box_host, energy, force, virial,
                                atom_energy, atom_virial, as_stream(stream));
   dp->impl.err = rc == DPGB_OK ? "" : dpgb_last_error();
+  return rc;
+}
+
+struct dpgb_batch {
+  BatchImpl impl;
+  dpgb_deeppot* owner = nullptr;
+  DeviceBuffer io_c, io_e, io_f, io_v;
+};
+
+dpgb_batch* dpgb_batch_new(dpgb_deeppot* dp, int nframes, const int* natoms, const int* atype, const double* box) {
+  clear_error();
+  if (!dp) {
+    fail(DPGB_EINVAL, "NULL handle");
+    return nullptr;
+  }
+  std::unique_ptr<dpgb_batch> b(new dpgb_batch());
+  b->owner = dp;
+  if (batch_setup(b->impl, dp->impl, nframes, natoms, atype, box) != DPGB_OK) return nullptr;
+  return b.release();
+}
+
+void dpgb_batch_delete(dpgb_batch* b) { delete b; }
+
+int dpgb_batch_natoms(const dpgb_batch* b) { return b ? b->impl.natoms : -1; }
+
+int dpgb_batch_compute_device(dpgb_batch* b, const double* coord, double* energy, double* force, double* virial,
+                              void* stream, int use_graph) {
+  clear_error();
+  if (!b) return fail(DPGB_EINVAL, "NULL batch");
+  cudaStream_t st = as_stream(stream);
+  if (!st) st = b->owner->impl.stream;  // graphs cannot be captured on the legacy stream
+  int rc = batch_compute(b->impl, coord, energy, force, virial, st, use_graph);
+  if (rc == DPGB_OK && !stream) rc = check_cuda(cudaStreamSynchronize(st), "batch");
+  b->owner->impl.err = rc == DPGB_OK ? "" : dpgb_last_error();
+  return rc;
+}
+
+int dpgb_batch_compute(dpgb_batch* b, const double* coord, double* energy, double* force, double* virial,
+                       int use_graph) {
+  clear_error();
+  if (!b) return fail(DPGB_EINVAL, "NULL batch");
+  DeepPotImpl& im = b->owner->impl;
+  cudaStream_t st = im.stream;
+  auto body = [&]() -> int {
+    if (!coord || !energy || !force || !virial) return fail(DPGB_EINVAL, "NULL argument");
+    const size_t n = (size_t)b->impl.natoms, nf = (size_t)b->impl.nframes;
+    DPGB_TRY(b->io_c.alloc(sizeof(double) * n * 3));
+    DPGB_TRY(b->io_f.alloc(sizeof(double) * n * 3));
+    DPGB_TRY(b->io_e.alloc(sizeof(double) * nf));
+    DPGB_TRY(b->io_v.alloc(sizeof(double) * nf * 9));
+    DPGB_CUDA(cudaMemcpyAsync(b->io_c.ptr, coord, sizeof(double) * n * 3, cudaMemcpyHostToDevice, st));
+    DPGB_TRY(batch_compute(b->impl, b->io_c.as<double>(), b->io_e.as<double>(), b->io_f.as<double>(),
+                           b->io_v.as<double>(), st, use_graph));
+    DPGB_CUDA(cudaMemcpyAsync(energy, b->io_e.ptr, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
+    DPGB_CUDA(cudaMemcpyAsync(force, b->io_f.ptr, sizeof(double) * n * 3, cudaMemcpyDeviceToHost, st));
+    DPGB_CUDA(cudaMemcpyAsync(virial, b->io_v.ptr, sizeof(double) * nf * 9, cudaMemcpyDeviceToHost, st));
+    return check_status(im, st);  // synchronises
+  };
+  int rc = body();
+  im.err = rc == DPGB_OK ? "" : dpgb_last_error();
   return rc;
 }
 

@@ -723,7 +723,238 @@ format_ext_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
   }
 }
 
+// ---- many frames in one launch (FrameTab) ---------------------------------
+
+__global__ void normalize_batch_kernel(double* __restrict__ out, int* __restrict__ cell_of, int* __restrict__ counts,
+                                       const double* __restrict__ in, int natoms, FrameTab ft) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= natoms) return;
+  const int fr = frame_of(ft.atom_off, ft.nframes, a);
+  const CellGeom& g = ft.geom[fr];
+  const double x = in[3 * a], y = in[3 * a + 1], z = in[3 * a + 2];
+  double fv[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double v = fma(z, g.rec[6 + k], fma(y, g.rec[3 + k], x * g.rec[k]));
+    v = v - floor(v);
+    fv[k] = v;
+  }
+  double w[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    w[k] = fma(fv[2], g.cell[6 + k], fma(fv[1], g.cell[3 + k], fv[0] * g.cell[k]));
+    out[3 * a + k] = w[k];
+  }
+  // cell of the wrapped position (the arithmetic of cell_count_kernel)
+  int c[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double f = (w[0] * g.rec[k] + w[1] * g.rec[3 + k] + w[2] * g.rec[6 + k]) * g.ncell[k];
+    int ci = (int)floor(f);
+    ci = ci < 0 ? 0 : (ci >= g.ncell[k] ? g.ncell[k] - 1 : ci);
+    c[k] = ci;
+  }
+  const int id = ft.cell_off[fr] + (c[0] * g.ncell[1] + c[1]) * g.ncell[2] + c[2];
+  cell_of[a] = id;
+  atomicAdd(&counts[id], 1);
+}
+
+constexpr int kBatchStageCap = 4096;
+
+size_t batch_stage_smem() {
+  return (size_t)kBatchStageCap * (3 * sizeof(float) + 2 * sizeof(int)) +
+         (size_t)kCellWarps * kKeptCap * (sizeof(double) + 2 * sizeof(int));
+}
+
+// nlist_cell_kernel over the cells of all frames; a cell whose stencil holds
+// more than kBatchStageCap atoms, or an atom with more than kKeptCap
+// neighbours, is reported as an overflow
+__global__ void __launch_bounds__(kCellWarps * 32)
+nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coord, const int* __restrict__ atype,
+                        const int* __restrict__ offsets, const int* __restrict__ cell_atoms,
+                        const int* __restrict__ shift_pos_all, const double* __restrict__ svec_all, FrameTab ft,
+                        double rcut, SelInfo sel, int* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* kr = reinterpret_cast<double*>(smem);
+  float* sx = reinterpret_cast<float*>(kr + kCellWarps * kKeptCap);
+  float* sy = sx + kBatchStageCap;
+  float* sz = sy + kBatchStageCap;
+  int* sidx = reinterpret_cast<int*>(sz + kBatchStageCap);
+  int* stype = sidx + kBatchStageCap;
+  int* kidx = stype + kBatchStageCap;
+  int* ktype = kidx + kCellWarps * kKeptCap;
+  // stencil of (2 reach + 1)^3 cells, reach <= 2 per direction (a frame
+  // thinner than rcut across a face has one cell and reach 2 there)
+  __shared__ int s_cell[125], s_shift[125], s_off[126];
+  const int cg = blockIdx.x, tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int fr = frame_of(ft.cell_off, ft.nframes, cg);
+  const CellGeom& g = ft.geom[fr];
+  const int c = cg - ft.cell_off[fr];
+  const int a_beg = ft.atom_off[fr], nloc = ft.atom_off[fr + 1] - a_beg;
+  const int* shift_pos = shift_pos_all + ft.spos_off[fr];
+  const double* svec = svec_all + 3 * (size_t)ft.svec_off[fr];
+  const int cz = c % g.ncell[2], cy = (c / g.ncell[2]) % g.ncell[1], cx = c / (g.ncell[1] * g.ncell[2]);
+  const int sy_ = 2 * g.nbuff[1] + 1, sz_ = 2 * g.nbuff[2] + 1;
+  const int wx = 2 * g.reach[0] + 1, wy = 2 * g.reach[1] + 1, wz = 2 * g.reach[2] + 1;
+  const int nst = wx * wy * wz;
+  for (int t = tid; t < nst; t += blockDim.x) {
+    const int ox = t / (wy * wz) - g.reach[0], oy = (t / wz) % wy - g.reach[1], oz = t % wz - g.reach[2];
+    int xw, tx, yw, ty, zw, tz;
+    bool ok = wrap_cell(cx + ox, g.ncell[0], g.periodic, xw, tx) && wrap_cell(cy + oy, g.ncell[1], g.periodic, yw, ty) &&
+              wrap_cell(cz + oz, g.ncell[2], g.periodic, zw, tz);
+    ok = ok && abs(tx) <= g.nbuff[0] && abs(ty) <= g.nbuff[1] && abs(tz) <= g.nbuff[2];
+    s_cell[t] = ok ? ft.cell_off[fr] + (xw * g.ncell[1] + yw) * g.ncell[2] + zw : -1;
+    s_shift[t] = ok ? shift_pos[((tx + g.nbuff[0]) * sy_ + (ty + g.nbuff[1])) * sz_ + (tz + g.nbuff[2])] : 0;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    s_off[0] = 0;
+    for (int k = 0; k < nst; ++k)
+      s_off[k + 1] = s_off[k] + (s_cell[k] >= 0 ? offsets[s_cell[k] + 1] - offsets[s_cell[k]] : 0);
+  }
+  __syncthreads();
+  const int total = s_off[nst];
+  if (offsets[cg] == offsets[cg + 1]) return;  // no centre atom in this cell
+  if (total > kBatchStageCap) {
+    if (tid == 0) {
+      atomicMax(&status[kStatusOverflow], total);
+      atomicMax(&status[kStatusOverflowAtom], cell_atoms[offsets[cg]] + 1);
+    }
+    return;
+  }
+  const int a0 = cell_atoms[offsets[cg]];
+  const double ox = coord[3 * a0], oy = coord[3 * a0 + 1], oz = coord[3 * a0 + 2];
+  for (int q = tid; q < total; q += blockDim.x) {
+    int lo = 0, hi = nst;  // s_off[lo] <= q < s_off[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (s_off[mid] <= q) lo = mid; else hi = mid;
+    }
+    const int k = lo;
+    const int j = cell_atoms[offsets[s_cell[k]] + (q - s_off[k])];  // global atom
+    const int s = s_shift[k];
+    sx[q] = (float)((coord[3 * j] + svec[3 * s]) - ox);
+    sy[q] = (float)((coord[3 * j + 1] + svec[3 * s + 1]) - oy);
+    sz[q] = (float)((coord[3 * j + 2] + svec[3 * s + 2]) - oz);
+    sidx[q] = s * nloc + (j - a_beg);
+    stype[q] = atype[j];
+  }
+  __syncthreads();
+  const float rcf = (float)rcut + 1e-3f;
+  const float rcf2 = rcf * rcf;
+  double* wr = kr + warp * kKeptCap;
+  int* wi = kidx + warp * kKeptCap;
+  int* wt = ktype + warp * kKeptCap;
+  for (int a = offsets[cg] + warp; a < offsets[cg + 1]; a += kCellWarps) {
+    const int i = cell_atoms[a];  // global atom
+    int* row = nlist + (size_t)i * sel.nnei;
+    for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
+    if (atype[i] < 0) continue;
+    const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
+    const int self = g.zero_shift * nloc + (i - a_beg);
+    const float xf = (float)(xi - ox), yf = (float)(yi - oy), zf = (float)(zi - oz);
+    int n = 0;
+    bool overflow = false;
+    for (int p0 = 0; p0 < total; p0 += 32) {
+      const int p = p0 + lane;
+      bool keep = false;
+      double r = 0.0;
+      if (p < total && stype[p] >= 0 && sidx[p] != self) {
+        const float fx = sx[p] - xf, fy = sy[p] - yf, fz = sz[p] - zf;
+        if (fx * fx + fy * fy + fz * fz <= rcf2) {
+          const int e = sidx[p], s = e / nloc, j = a_beg + (e - s * nloc);
+          const double dx = (coord[3 * j] + svec[3 * s]) - xi;
+          const double dy = (coord[3 * j + 1] + svec[3 * s + 1]) - yi;
+          const double dz = (coord[3 * j + 2] + svec[3 * s + 2]) - zi;
+          r = dist_fma(dx, dy, dz);
+          keep = r <= rcut;
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      const int pos = n + __popc(m & ((1u << lane) - 1u));
+      if (keep) {
+        if (pos < kKeptCap) {
+          wr[pos] = r;
+          wi[pos] = sidx[p];
+          wt[pos] = stype[p];
+        } else {
+          overflow = true;
+        }
+      }
+      n += __popc(m);
+    }
+    overflow = __any_sync(0xffffffffu, overflow);
+    if (overflow) {
+      if (lane == 0) {
+        atomicMax(&status[kStatusOverflow], n);
+        atomicMax(&status[kStatusOverflowAtom], i + 1);
+      }
+      __syncwarp();
+      continue;
+    }
+    __syncwarp();
+    for (int k0 = 0; k0 < n; k0 += 128) {
+      long long rk[4];
+      int ik[4], tk[4], rank[4], trank[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = k0 + lane + 32 * q;
+        rk[q] = k < n ? __double_as_longlong(wr[k]) : 0x7fffffffffffffffLL;
+        ik[q] = k < n ? wi[k] : 0x7fffffff;
+        tk[q] = k < n ? wt[k] : -1;
+        rank[q] = trank[q] = 0;
+      }
+      for (int m2 = 0; m2 < n; ++m2) {
+        const long long rm = __double_as_longlong(wr[m2]);
+        const int im = wi[m2], tm = wt[m2];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const bool lt = rm < rk[q] || (rm == rk[q] && im < ik[q]);
+          rank[q] += lt;
+          trank[q] += lt && tm == tk[q];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int t = tk[q];
+        if (k0 + lane + 32 * q < n && rank[q] < sel.nnei && t < sel.ntypes && trank[q] < sel.sel[t])
+          row[sel.sec[t] + trank[q]] = ik[q];
+      }
+    }
+    __syncwarp();
+  }
+}
+
 }  // namespace
+
+size_t nlist_batch_workspace(int natoms, int ncells) {
+  return sizeof(int) * (2 * (size_t)natoms + 3 * ((size_t)ncells + 1)) + 256 * 4;
+}
+
+int launch_nlist_batch(int* nlist, double* coord_out, const double* coord_in, const int* atype, int natoms,
+                       int ncells, const FrameTab& ft, const double* svec, const int* shift_pos, double rcut,
+                       const SelInfo& sel, void* workspace, int* status, cudaStream_t st) {
+  if (natoms <= 0) return DPGB_OK;
+  int* cell_of = reinterpret_cast<int*>(workspace);
+  int* cell_atoms = cell_of + natoms;
+  int* counts = cell_atoms + natoms;
+  int* offsets = counts + (ncells + 1);
+  int* cursor = offsets + (ncells + 1);
+  DPGB_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (ncells + 1), st));
+  DPGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * (ncells + 1), st));
+  normalize_batch_kernel<<<ceil_div(natoms, 256), 256, 0, st>>>(coord_out, cell_of, counts, coord_in, natoms, ft);
+  DPGB_TRY(check_launch("normalize_batch"));
+  scan_kernel<<<1, 1024, 0, st>>>(offsets, counts, ncells);
+  DPGB_TRY(check_launch("cell_scan_batch"));
+  cell_fill_kernel<<<ceil_div(natoms, 256), 256, 0, st>>>(cell_atoms, cursor, offsets, cell_of, natoms);
+  DPGB_TRY(check_launch("cell_fill_batch"));
+  const size_t smem = batch_stage_smem();
+  DPGB_CUDA(cudaFuncSetAttribute(nlist_cell_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  nlist_cell_batch_kernel<<<ncells, kCellWarps * 32, smem, st>>>(nlist, coord_out, atype, offsets, cell_atoms,
+                                                                  shift_pos, svec, ft, rcut, sel, status);
+  return check_launch("nlist_cell_batch");
+}
 
 int launch_format_ext(int* nlist, const double* coord_ext, const int* atype_ext, const int* off, const int* idx,
                       int nloc, int nall, double rcut, const SelInfo& sel, int sorted, int* status,

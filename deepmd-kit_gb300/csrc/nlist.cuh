@@ -58,6 +58,36 @@ int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc,
 int launch_format_nlist(int* nlist, const double* coord, const int* atype, const int* rows, int nall,
                         const int* counts, int max_nbor, int nloc, double rcut, const SelInfo& sel,
                         int* status, cudaStream_t st);
+// Many periodic frames of different sizes in one set of launches: frame f
+// owns atoms [atom_off[f], atom_off[f+1]) of the concatenated arrays, cells
+// [cell_off[f], cell_off[f+1]) of one global cell list, image shifts
+// shift_pos[spos_off[f] ..] / svec[3 * svec_off[f] ..], geometry geom[f].
+// Extended indices in the lists stay per frame: s * natoms_f + j_local.
+struct FrameTab {
+  int nframes;
+  const int* atom_off;
+  const int* cell_off;
+  const int* spos_off;
+  const int* svec_off;
+  const CellGeom* geom;
+};
+
+__device__ __forceinline__ int frame_of(const int* off, int nframes, int x) {
+  int lo = 0, hi = nframes;  // off[lo] <= x < off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= x) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+size_t nlist_batch_workspace(int natoms, int ncells);
+// wrap (normalize) and build the typed lists of every frame: coord_out
+// receives the wrapped coordinates; nlist [natoms, sum(sel)]
+int launch_nlist_batch(int* nlist, double* coord_out, const double* coord_in, const int* atype, int natoms,
+                       int ncells, const FrameTab& ft, const double* svec, const int* shift_pos, double rcut,
+                       const SelInfo& sel, void* workspace, int* status, cudaStream_t st);
+
 // external list with explicit ghosts (CSR over the local atoms) -> typed list
 int launch_format_ext(int* nlist, const double* coord_ext, const int* atype_ext, const int* off, const int* idx,
                       int nloc, int nall, double rcut, const SelInfo& sel, int sorted, int* status,

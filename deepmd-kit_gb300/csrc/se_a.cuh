@@ -90,6 +90,13 @@ struct DescParams {
   const double* coord_ext;
   const int* atype_ext;
   int nall;
+  // a batch of frames of different sizes run as one "frame" of all their
+  // atoms: when frame_atom_off is set, row r belongs to the frame f with
+  // frame_atom_off[f] <= r < frame_atom_off[f+1], nlist holds that frame's
+  // image-major indices and its shifts start at svec[3 * frame_svec_off[f]]
+  const int* frame_atom_off;
+  const int* frame_svec_off;
+  int nframes_batch;
 };
 
 // r_nb - r_i in FP64 for neighbour nb of local atom i of frame f, and the
@@ -102,6 +109,16 @@ __device__ __forceinline__ int pair_disp(const DescParams<T>& p, int f, int i, i
     d[1] = ce[3 * nb + 1] - ce[3 * i + 1];
     d[2] = ce[3 * nb + 2] - ce[3 * i + 2];
     return p.atype_ext[(size_t)f * p.nall + nb];
+  }
+  if (p.frame_atom_off) {  // batch: i is the global row
+    const int fr = frame_of(p.frame_atom_off, p.nframes_batch, i);
+    const int beg = p.frame_atom_off[fr], nl = p.frame_atom_off[fr + 1] - beg;
+    const int s = nb / nl, jj = beg + (nb - s * nl);
+    const double* sv = p.svec + 3 * ((size_t)p.frame_svec_off[fr] + s);
+    d[0] = (p.coord[3 * jj] + sv[0]) - p.coord[3 * i];
+    d[1] = (p.coord[3 * jj + 1] + sv[1]) - p.coord[3 * i + 1];
+    d[2] = (p.coord[3 * jj + 2] + sv[2]) - p.coord[3 * i + 2];
+    return p.atype[jj];
   }
   const double* cf = p.coord + (size_t)f * p.nloc * 3;
   const int s = nb / p.nloc, jj = nb - s * p.nloc;

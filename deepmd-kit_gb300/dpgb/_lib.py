@@ -120,6 +120,11 @@ _SIGS = {
     "dpgb_deeppot_compute_device": [_P, _I, _I, _P, _IP, _DP, _P, _P, _P, _P, _P, _P],
     "dpgb_deeppot_compute_nlist": [_P, _I, _I, _DP, _IP, _DP, _I, _IP, _IP, C.POINTER(_IP), _I, _DP, _DP, _DP,
                                    _DP, _DP],
+    "dpgb_batch_new": [_P, _I, _IP, _IP, _DP],
+    "dpgb_batch_delete": [_P],
+    "dpgb_batch_natoms": [_P],
+    "dpgb_batch_compute_device": [_P, _P, _P, _P, _P, _P, _I],
+    "dpgb_batch_compute": [_P, _DP, _DP, _DP, _DP, _I],
     "dpgb_deeppot_last_launches": [_P],
     "dpgb_deeppot_set_profiling": [_P, _I],
     "dpgb_deeppot_collect_stages": [_P],
@@ -130,6 +135,8 @@ _RESTYPE = {
     "dpgb_last_error": C.c_char_p,
     "dpgb_version": C.c_char_p,
     "dpgb_deeppot_new": _P,
+    "dpgb_batch_new": _P,
+    "dpgb_batch_delete": None,
     "dpgb_deeppot_delete": None,
     "dpgb_deeppot_check_ok": C.c_char_p,
     "dpgb_se_a_block_param_count": C.c_longlong,

@@ -183,6 +183,11 @@ class DeepPot:
             return e[0], f, v, ae, av
         return e[0], f, v
 
+    def batch(self, frames):
+        """A :class:`DeepPotBatch` over frames = [(coord [n_f, 3], atype [n_f],
+        box [9]), ...] of different sizes."""
+        return DeepPotBatch(self, frames)
+
     def eval_device(self, coord, box, atype, atomic: bool = False, out=None):
         """Device form: ``coord`` a CUDA float64 tensor [nframes, natom*3]
         (or [natom, 3]); ``box`` host array or None; ``atype`` host array.
@@ -215,4 +220,59 @@ class DeepPot:
             vp(ae.data_ptr()) if ae is not None else None, vp(av.data_ptr()) if av is not None else None,
             vp(torch.cuda.current_stream().cuda_stream))
         _lib.check(rc)
+        return out
+
+
+class DeepPotBatch:
+    """Many periodic frames of different sizes evaluated together
+    (``dpgb_batch_*``): one set of launches for all frames, optionally
+    captured in a CUDA graph and replayed."""
+
+    def __init__(self, dp: "DeepPot", frames):
+        self.dp = dp
+        self.natoms = np.array([len(f[1]) for f in frames], dtype=np.int32)
+        self.nframes = len(frames)
+        atype = np.ascontiguousarray(np.concatenate([np.asarray(f[1]) for f in frames]), dtype=np.int32)
+        box = np.ascontiguousarray(np.stack([np.asarray(f[2], dtype=np.float64).reshape(9) for f in frames]))
+        ip = C.POINTER(C.c_int)
+        self._h = _lib.lib().dpgb_batch_new(dp._h, self.nframes, self.natoms.ctypes.data_as(ip),
+                                            atype.ctypes.data_as(ip), box.ctypes.data_as(C.POINTER(C.c_double)))
+        if not self._h:
+            raise _lib.DpgbError(-1, _lib.lib().dpgb_last_error().decode())
+        self.offsets = np.concatenate([[0], np.cumsum(self.natoms)])
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.lib().dpgb_batch_delete(self._h)
+            self._h = None
+
+    def eval(self, coords, use_graph: bool = False):
+        """Host coordinates (list of [n_f, 3] arrays or the concatenation) ->
+        (energy [nframes], list of forces [n_f, 3], virial [nframes, 9])."""
+        if isinstance(coords, (list, tuple)):
+            coords = np.concatenate([np.asarray(c, dtype=np.float64).reshape(-1, 3) for c in coords])
+        c = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1)
+        e = np.zeros(self.nframes)
+        f = np.zeros((int(self.offsets[-1]), 3))
+        v = np.zeros((self.nframes, 9))
+        dp = C.POINTER(C.c_double)
+        _lib.check(_lib.lib().dpgb_batch_compute(self._h, c.ctypes.data_as(dp), e.ctypes.data_as(dp),
+                                                 f.ctypes.data_as(dp), v.ctypes.data_as(dp), int(use_graph)))
+        return e, [f[self.offsets[k]:self.offsets[k + 1]] for k in range(self.nframes)], v
+
+    def eval_device(self, coord, out=None, use_graph: bool = False, stream=None):
+        """CUDA float64 coordinates [natoms, 3] -> dict of CUDA tensors on the
+        current torch stream; nothing is synchronised."""
+        import torch
+
+        n = int(self.offsets[-1])
+        if out is None:
+            out = {"energy": torch.empty(self.nframes, dtype=torch.float64, device=coord.device),
+                   "force": torch.empty((n, 3), dtype=torch.float64, device=coord.device),
+                   "virial": torch.empty((self.nframes, 9), dtype=torch.float64, device=coord.device)}
+        st = torch.cuda.current_stream().cuda_stream if stream is None else stream
+        _lib.check(_lib.lib().dpgb_batch_compute_device(
+            self._h, C.c_void_p(coord.data_ptr()), C.c_void_p(out["energy"].data_ptr()),
+            C.c_void_p(out["force"].data_ptr()), C.c_void_p(out["virial"].data_ptr()), C.c_void_p(st),
+            int(use_graph)))
         return out

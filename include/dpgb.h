@@ -464,6 +464,34 @@ int dpgb_deeppot_compute_nlist(dpgb_deeppot* dp, int nall, int nghost,
                                double* energy, double* force, double* virial,
                                double* atom_energy, double* atom_virial);
 
+/* Batches of independent periodic frames of different sizes (no counterpart
+ * in the reference, which evaluates frames one shape at a time,
+ * deepmd/pt/infer/deep_eval.py): all frames go through one set of launches
+ * — a cell list over the cells of every frame, the embedding over all
+ * type-sorted atoms, the fitting per type over all frames — and the
+ * evaluation can be captured in a CUDA graph and replayed.
+ *   natoms [nframes], atype: the frames' types concatenated, box
+ *   [nframes, 9] (every frame periodic; no face thinner than rcut / 2).
+ * A batch borrows the handle's workspace: computing other systems with the
+ * handle in between is allowed and makes the next batch call re-capture. */
+typedef struct dpgb_batch dpgb_batch;
+dpgb_batch* dpgb_batch_new(dpgb_deeppot* dp, int nframes, const int* natoms,
+                           const int* atype, const double* box);
+void dpgb_batch_delete(dpgb_batch* b);
+int dpgb_batch_natoms(const dpgb_batch* b);
+/* DEVICE buffers: coord [natoms, 3] (frames concatenated), energy
+ * [nframes], force [natoms, 3], virial [nframes, 9].  use_graph: capture
+ * the kernel sequence on the first call (after one plain evaluation) and
+ * replay it while the buffer pointers, the stream and the handle's cached
+ * state stay the same.  stream NULL = the handle's stream, synchronised. */
+int dpgb_batch_compute_device(dpgb_batch* b, const double* coord,
+                              double* energy, double* force, double* virial,
+                              void* stream, int use_graph);
+/* The same with HOST buffers (copies in and out, synchronises, reports
+ * neighbour overflow). */
+int dpgb_batch_compute(dpgb_batch* b, const double* coord, double* energy,
+                       double* force, double* virial, int use_graph);
+
 /* Number of kernel launches the last compute issued (for the benchmark). */
 int dpgb_deeppot_last_launches(dpgb_deeppot* dp);
 
