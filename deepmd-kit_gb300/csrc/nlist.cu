@@ -70,10 +70,18 @@ int periodic_geom(const double* box, double rcut, int nshift, const int* shift_i
   const double rc_margin = rcut * (1.0 + 1e-9) + 1e-12;
   for (int d = 0; d < 3; ++d) {
     int n = (int)std::floor(face[d] / rc_margin);
-    n = n < 1 ? 1 : (n > 64 ? 64 : n);
+    // up to 1024 cells per direction (elongated boxes keep cells near rcut)
+    n = n < 1 ? 1 : (n > 1024 ? 1024 : n);
     g.ncell[d] = n;
     g.reach[d] = (int)std::ceil(rc_margin * n / face[d]);
     g.nbuff[d] = (int)std::ceil(rcut / face[d]);
+  }
+  // the cell list is O(cells) in memory: halve the longest direction of a
+  // huge box until it holds at most 2^24 cells
+  while ((long long)g.ncell[0] * g.ncell[1] * g.ncell[2] > (1LL << 24)) {
+    const int d = g.ncell[0] >= g.ncell[1] && g.ncell[0] >= g.ncell[2] ? 0 : (g.ncell[1] >= g.ncell[2] ? 1 : 2);
+    g.ncell[d] = (g.ncell[d] + 1) / 2;
+    g.reach[d] = (int)std::ceil(rc_margin * g.ncell[d] / face[d]);
   }
   const int sx = 2 * g.nbuff[0] + 1, sy = 2 * g.nbuff[1] + 1, sz = 2 * g.nbuff[2] + 1;
   if (nshift != sx * sy * sz)

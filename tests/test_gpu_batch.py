@@ -14,9 +14,14 @@ def rel(a, b):
 
 
 def _frames(n=7, seed=3, hi=700):
+    """Random frames plus two one-cell-thick rods (a prime number of fcc
+    cells: 1 x 1 x 37 and 1 x 1 x 401 cells, so reach 2 across two faces and
+    an elongated cell grid)."""
     from dpgb import synth
 
-    return synth.fcc_alloy_batch(nframes=n, seed=seed, lo=32, hi=hi)
+    rng = np.random.default_rng(seed + 100)
+    return synth.fcc_alloy_batch(nframes=n, seed=seed, lo=32, hi=hi) + [
+        synth.fcc_alloy_frame(4 * 37, rng), synth.fcc_alloy_frame(4 * 401, rng)]
 
 
 @pytest.fixture(scope="module")
