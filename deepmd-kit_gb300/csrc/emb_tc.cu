@@ -433,12 +433,25 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         alive = __syncthreads_and(ok) != 0;
         if (!alive) break;
         // partial xyz of this section: sum_{pairs of the atom} Rn[c] G[n]
-        // (FP32, fixed order; plain stores, the atom is owned by this CTA)
-        for (int q = tid; q < ntile * 4 * W3; q += blockDim.x) {
-          const int k = q / (4 * W3), rem = q - k * 4 * W3, cc = rem / W3, n = rem - cc * W3;
-          float s = 0.f;
-          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) s = fmaf(sRn[pp * 4 + cc], sG[pp * P::LDG + n], s);
-          xpart[(size_t)s_row[k] * 4 * ng + cc * ng + n] = s;
+        // (FP32, fixed order; plain stores, the atom is owned by this CTA).
+        // One thread per (atom, neuron) does all four components: one G load
+        // and one broadcast float4 of Rn per pair and four FMAs.
+        for (int q = tid; q < ntile * W3; q += blockDim.x) {
+          const int k = q / W3, n = q - k * W3;
+          float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) {
+            const float g = sG[pp * P::LDG + n];
+            const float4 r = *reinterpret_cast<const float4*>(sRn + pp * 4);
+            s0 = fmaf(r.x, g, s0);
+            s1 = fmaf(r.y, g, s1);
+            s2 = fmaf(r.z, g, s2);
+            s3 = fmaf(r.w, g, s3);
+          }
+          float* o = xpart + (size_t)s_row[k] * 4 * ng + n;
+          o[0] = s0;
+          o[ng] = s1;
+          o[2 * ng] = s2;
+          o[3 * ng] = s3;
         }
         __syncthreads();
       }
