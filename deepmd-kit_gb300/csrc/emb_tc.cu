@@ -515,7 +515,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
   const uint32_t tbase = s_tmem;
   uint32_t phase = 0;
   bool alive = true;
-  float* sDX = reinterpret_cast<float*>(smem + P::gbuf);  // [kBwdAtoms][4][W3]
+  float* sDX = reinterpret_cast<float*>(smem + P::gbuf);  // [kBwdAtoms][W3][4]: one float4 per neuron
   float* sV = reinterpret_cast<float*>(smem + P::vec);
   float* sVir = reinterpret_cast<float*>(smem + P::vir);
   const uint32_t sA1 = tc::smem_u32(smem + P::a1), sA2 = tc::smem_u32(smem + P::a2), sA3 = tc::smem_u32(smem + P::a3);
@@ -569,7 +569,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         if (ntile == 0) break;
         for (int q = tid; q < ntile * 4 * W3; q += blockDim.x) {
           const int k = q / (4 * W3), rem = q - k * 4 * W3, cc = rem / W3, n = rem - cc * W3;
-          sDX[q] = dxyz[(size_t)s_row[k] * 4 * ng + cc * ng + n];
+          sDX[(k * W3 + n) * 4 + cc] = dxyz[(size_t)s_row[k] * 4 * ng + cc * ng + n];
         }
         PairInfo pi;
         float rn[4], dv[3];
@@ -641,7 +641,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         tc::fence_after();
         // epilogue 3 of the backward: G, dG = Rn . dxyz, dRn (direct part),
         // dP3 = dG * idt3 * (1 - t3^2) into the BF16 operand, skip folds
-        const float* dx = sDX + pi.k * 4 * W3;
+        const float4* dx = reinterpret_cast<const float4*>(sDX) + pi.k * W3;
         float drn[4] = {0.f, 0.f, 0.f, 0.f};
         float dh2[W2];
 #pragma unroll
@@ -660,7 +660,8 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
               float g = tv * i3[o];
               if (W3 == W2) g += h2[o];
               if (W3 == 2 * W2) g += h2[o < W2 ? o : o - W2];
-              const float d0 = dx[o], d1 = dx[W3 + o], d2 = dx[2 * W3 + o], d3 = dx[3 * W3 + o];
+              const float4 dq = dx[o];
+              const float d0 = dq.x, d1 = dq.y, d2 = dq.z, d3 = dq.w;
               drn[0] = fmaf(g, d0, drn[0]);
               drn[1] = fmaf(g, d1, drn[1]);
               drn[2] = fmaf(g, d2, drn[2]);

@@ -213,14 +213,13 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ 
   const int ti = p.atype[row % p.nloc];
   const int ng = p.ng;
   const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
-  float dX[4][kTabJ];
+  // the atom's dE/dxyz, one float4 (four components) per neuron, shared by
+  // the warp's lanes (each lane walks all neurons of its own pair)
+  __shared__ float4 s_dx[kTabWarps][32 * kTabJ];
+  float4* sdx = s_dx[threadIdx.x >> 5];
   const float* dr = dxyz + (size_t)row * 4 * ng;
-#pragma unroll
-  for (int j = 0; j < kTabJ; ++j) {
-    const int n = lane + 32 * j;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) dX[c][j] = n < ng ? dr[c * ng + n] : 0.f;
-  }
+  for (int n = lane; n < ng; n += 32) sdx[n] = make_float4(dr[n], dr[ng + n], dr[2 * ng + n], dr[3 * ng + n]);
+  __syncwarp();
   double vir[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) vir[k] = 0.0;
@@ -240,45 +239,25 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ 
         table_locate(tm, s.rn[0], s.idx, s.xx, s.delta);
       }
       const bool real = have && s.nb >= 0 && s.active;  // only real kept pairs carry a gradient
+      // dR~ of this lane's pair: sum over neurons of G dX (direct term) and
+      // of (R~ . dX) G' (through s = R~[0]), in neuron order
       float mine[4] = {0.f, 0.f, 0.f, 0.f};
-      unsigned m = __ballot_sync(0xffffffffu, real);
-      while (m) {
-        const int src = __ffs(m) - 1;
-        m &= m - 1;
-        float rr[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) rr[c] = __shfl_sync(0xffffffffu, s.rn[c], src);
-        const int ix = __shfl_sync(0xffffffffu, s.idx, src);
-        const float xx = __shfl_sync(0xffffffffu, s.xx, src);
-        const float dl = __shfl_sync(0xffffffffu, s.delta, src);
-        const float* rowc = tab + (size_t)ix * 6 * ng;
-        float g4[4] = {0.f, 0.f, 0.f, 0.f}, ds = 0.f;
-#pragma unroll
-        for (int j = 0; j < kTabJ; ++j) {
-          const int n = lane + 32 * j;
-          if (n < ng) {
-            float a[6], G, Gp;
-            coeffs(rowc + 6 * n, a);
-            table_poly(a, xx, dl, G, Gp);
-            float dG = 0.f;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              dG = fmaf(rr[c], dX[c][j], dG);
-              g4[c] = fmaf(G, dX[c][j], g4[c]);
-            }
-            ds = fmaf(dG, Gp, ds);
-          }
+      if (real) {
+        const float* rowc = tab + (size_t)s.idx * 6 * ng;
+        float ds = 0.f;
+        for (int n = 0; n < ng; ++n) {
+          float a[6], G, Gp;
+          coeffs(rowc + 6 * n, a);
+          table_poly(a, s.xx, s.delta, G, Gp);
+          const float4 d = sdx[n];
+          const float dG = fmaf(s.rn[3], d.w, fmaf(s.rn[2], d.z, fmaf(s.rn[1], d.y, s.rn[0] * d.x)));
+          mine[0] = fmaf(G, d.x, mine[0]);
+          mine[1] = fmaf(G, d.y, mine[1]);
+          mine[2] = fmaf(G, d.z, mine[2]);
+          mine[3] = fmaf(G, d.w, mine[3]);
+          ds = fmaf(dG, Gp, ds);
         }
-        g4[0] += ds;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) g4[c] += __shfl_xor_sync(0xffffffffu, g4[c], o);
-        }
-        if (lane == src) {
-#pragma unroll
-          for (int c = 0; c < 4; ++c) mine[c] = g4[c];
-        }
+        mine[0] += ds;
       }
       if (have) {
         float g[3] = {0.f, 0.f, 0.f};
