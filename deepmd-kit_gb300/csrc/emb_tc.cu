@@ -795,28 +795,36 @@ __global__ void run_len_kernel(int* __restrict__ run_len, const int* __restrict_
 }
 
 // dE/dxyz (before the forward's 1/nnei): dxyz[c][n] = (sum_m dD[n][m] xyz[c][m]
-// + [n < M] sum_n' dD[n'][n] xyz[c][n']) / nnei ; one CTA per row
+// + [n < M] sum_n' dD[n'][n] xyz[c][n']) / nnei.  One warp per row: the
+// row's xyz and dD are staged in shared memory with coalesced loads.
 __global__ void dxyz_kernel(float* __restrict__ dxyz, const float* __restrict__ dD, const float* __restrict__ xyz,
-                            const int* __restrict__ row_pos, const int* __restrict__ atype, int nloc, int ng, int M,
-                            int nnei) {
-  extern __shared__ float s_x[];
-  const int row = blockIdx.x;
-  const float* xr = xyz + (size_t)row * 4 * ng;
-  for (int q = threadIdx.x; q < 4 * ng; q += blockDim.x) s_x[q] = xr[q];
-  __syncthreads();
+                            const int* __restrict__ row_pos, const int* __restrict__ atype, int nloc, int nrows,
+                            int ng, int M, int nnei) {
+  extern __shared__ float s_dx[];
+  const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = blockIdx.x * wpb + warp;
+  if (row >= nrows) return;
+  float* sx = s_dx + (size_t)warp * (4 * ng + ng * M);
+  float* sd = sx + 4 * ng;
+  float* out = dxyz + (size_t)row * 4 * ng;
   if (atype[row % nloc] < 0) {
-    for (int q = threadIdx.x; q < 4 * ng; q += blockDim.x) dxyz[(size_t)row * 4 * ng + q] = 0.f;
+    for (int q = lane; q < 4 * ng; q += 32) out[q] = 0.f;
     return;
   }
+  const float* xr = xyz + (size_t)row * 4 * ng;
   const float* d = dD + (size_t)row_pos[row] * ng * M;
+  for (int q = lane; q < 4 * ng; q += 32) sx[q] = xr[q];
+  for (int q = lane; q < ng * M; q += 32) sd[q] = d[q];
+  __syncwarp();
   const float inv = 1.f / (float)nnei;
-  for (int q = threadIdx.x; q < 4 * ng; q += blockDim.x) {
+  for (int q = lane; q < 4 * ng; q += 32) {
     const int c = q / ng, n = q - c * ng;
+    const float* xc = sx + c * ng;
     float s = 0.f;
-    for (int m = 0; m < M; ++m) s = fmaf(__ldg(d + n * M + m), s_x[c * ng + m], s);
+    for (int m = 0; m < M; ++m) s = fmaf(sd[n * M + m], xc[m], s);
     if (n < M)
-      for (int n2 = 0; n2 < ng; ++n2) s = fmaf(__ldg(d + n2 * M + n), s_x[c * ng + n2], s);
-    dxyz[(size_t)row * 4 * ng + q] = s * inv;
+      for (int n2 = 0; n2 < ng; ++n2) s = fmaf(sd[n2 * M + n], xc[n2], s);
+    out[q] = s * inv;
   }
 }
 
@@ -877,8 +885,13 @@ int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChun
 
 int launch_dxyz(const DescParams<float>& p, const float* dD, const float* xyz, float* dxyz, cudaStream_t st) {
   if (p.nrows <= 0) return DPGB_OK;
-  dxyz_kernel<<<p.nrows, 128, sizeof(float) * 4 * p.ng, st>>>(dxyz, dD, xyz, p.row_pos, p.atype, p.nloc, p.ng, p.axis,
-                                                              p.nnei);
+  const size_t per_warp = sizeof(float) * ((size_t)4 * p.ng + (size_t)p.ng * p.axis);
+  int wpb = 8;
+  while (wpb > 1 && per_warp * wpb > 96 * 1024) wpb >>= 1;
+  if (per_warp * wpb > 227 * 1024) return fail(DPGB_EINVAL, "dxyz: descriptor too wide for shared memory");
+  DPGB_CUDA(cudaFuncSetAttribute(dxyz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(per_warp * wpb)));
+  dxyz_kernel<<<ceil_div(p.nrows, wpb), 32 * wpb, per_warp * wpb, st>>>(dxyz, dD, xyz, p.row_pos, p.atype, p.nloc,
+                                                                        p.nrows, p.ng, p.axis, p.nnei);
   return check_launch("dxyz");
 }
 
