@@ -223,28 +223,57 @@ __global__ void force_gather_batch_kernel(double* __restrict__ force, double* __
     for (int k = 0; k < 9; ++k) atom_vir[9 * (size_t)row + k] = av[k];
 }
 
-// per-frame sums over ragged frames: blockIdx.x = frame, blockIdx.y = 0
-// energy, 1..9 virial
-__global__ void frame_sum_batch_kernel(double* __restrict__ energy, double* __restrict__ virial,
-                                       const double* __restrict__ e_row, const double* __restrict__ vir_row,
-                                       const int* __restrict__ atom_off) {
-  __shared__ double s[256];
-  const int f = blockIdx.x, q = blockIdx.y;
-  double acc = 0.0;
-  for (int r = atom_off[f] + threadIdx.x; r < atom_off[f + 1]; r += blockDim.x)
-    acc += q == 0 ? e_row[r] : vir_row[(size_t)r * 9 + (q - 1)];
-  s[threadIdx.x] = acc;
+// Per-frame sums of the atom energies and atom virials in two passes with a
+// fixed partition, so the result does not depend on scheduling: pass 1 gives
+// every chunk of kFrameChunk rows of a frame its 10 partial sums (energy, 9
+// virial components), pass 2 adds a frame's chunk partials in chunk order.
+// Frame f covers rows [atom_off[f], atom_off[f+1]) or, without atom_off,
+// [f*nloc, (f+1)*nloc).
+constexpr int kFrameChunk = 2048;
+constexpr int kFrameSumThreads = 256;
+
+__global__ void __launch_bounds__(kFrameSumThreads) frame_part_kernel(double* __restrict__ part,
+                                                                      const double* __restrict__ e_row,
+                                                                      const double* __restrict__ vir_row,
+                                                                      const int* __restrict__ atom_off, int nloc) {
+  const int c = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
+  const int lo = atom_off ? atom_off[f] : f * nloc, hi = atom_off ? atom_off[f + 1] : (f + 1) * nloc;
+  const int r0 = lo + c * kFrameChunk, r1 = min(hi, r0 + kFrameChunk);
+  double acc[10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q) acc[q] = 0.0;
+  for (int r = r0 + t; r < r1; r += kFrameSumThreads) {
+    acc[0] += e_row[r];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q + 1] += vir_row[(size_t)r * 9 + q];
+  }
+  __shared__ double s[kFrameSumThreads / 32][10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q)
+    for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+  if ((t & 31) == 0)
+#pragma unroll
+    for (int q = 0; q < 10; ++q) s[t >> 5][q] = acc[q];
   __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
-    __syncthreads();
+  if (t < 10) {
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < kFrameSumThreads / 32; ++w) v += s[w][t];
+    part[((size_t)f * gridDim.x + c) * 10 + t] = v;
   }
-  if (threadIdx.x == 0) {
-    if (q == 0)
-      energy[f] = s[0];
-    else
-      virial[(size_t)f * 9 + q - 1] = s[0];
-  }
+}
+
+// pass 2: one warp per frame, lane q < 10 adds the chunk partials in order
+__global__ void frame_final_kernel(double* __restrict__ energy, double* __restrict__ virial,
+                                   const double* __restrict__ part, int nchunk, int nframes) {
+  const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), q = threadIdx.x & 31;
+  if (f >= nframes || q >= 10) return;
+  double v = 0.0;
+  for (int c = 0; c < nchunk; ++c) v += part[((size_t)f * nchunk + c) * 10 + q];
+  if (q == 0)
+    energy[f] = v;
+  else
+    virial[(size_t)f * 9 + q - 1] = v;
 }
 
 // atom energy in the original order (+ per-type bias), 0 for virtual atoms
@@ -255,31 +284,6 @@ __global__ void atom_energy_kernel(double* __restrict__ e_row, const double* __r
   if (row >= nrows) return;
   const int t = atype[row % nloc];
   e_row[row] = t < 0 ? 0.0 : e_sorted[row_pos[row]] + bias[t];
-}
-
-// per-frame sums: blockIdx.x = frame, blockIdx.y = 0 energy, 1..9 virial
-__global__ void frame_sum_kernel(double* __restrict__ energy, double* __restrict__ virial,
-                                 const double* __restrict__ e_row, const double* __restrict__ vir_row,
-                                 int nloc) {
-  __shared__ double s[256];
-  const int f = blockIdx.x, q = blockIdx.y;
-  double acc = 0.0;
-  for (int i = threadIdx.x; i < nloc; i += blockDim.x) {
-    const size_t row = (size_t)f * nloc + i;
-    acc += q == 0 ? e_row[row] : vir_row[row * 9 + (q - 1)];
-  }
-  s[threadIdx.x] = acc;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    if (q == 0)
-      energy[f] = s[0];
-    else
-      virial[(size_t)f * 9 + q - 1] = s[0];
-  }
 }
 
 }  // namespace
@@ -318,7 +322,7 @@ struct DeepPotImpl {
   DeviceBuffer fit_w16, fit_f32, ws_fitb;
   // workspace
   DeviceBuffer ws_nlist, ws_cell, ws_tr, ws_keys, ws_status, ws_coord, ws_svec, ws_spos;
-  DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf;
+  DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf, ws_part;
   DeviceBuffer io_coord, io_force, io_av, io_e, io_v, io_ae;
   // external neighbour list (CSR over local atoms) kept between calls for
   // `ago` > 0, with the ghost-inclusive types
@@ -733,6 +737,7 @@ struct BatchIn {
   int ncells;
   const double* svec;
   const int* spos;
+  int max_atoms;  // atoms of the largest frame
 };
 
 template <typename T>
@@ -819,6 +824,9 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   DPGB_TRY(dp.ws_vir.alloc(sizeof(double) * nrows * 9));
   DPGB_TRY(dp.ws_erow.alloc(sizeof(double) * nrows));
   DPGB_TRY(dp.ws_esorted.alloc(sizeof(double) * nrows));
+  const int sum_frames = batch ? batch->ft.nframes : nframes;
+  const int sum_chunks = ceil_div(batch ? batch->max_atoms : natom, kFrameChunk);
+  DPGB_TRY(dp.ws_part.alloc(sizeof(double) * 10 * (size_t)sum_frames * sum_chunks));
   DPGB_TRY(dp.ws_act.alloc(sizeof(T) * 2 * m.fit.n_hidden * nrows * maxw));
   DPGB_TRY(dp.ws_gbuf.alloc(sizeof(T) * 4 * nrows * maxw));
 
@@ -1019,13 +1027,13 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
                                                            dp.atype_dev.as<int>(), dp.bias_dev.as<double>(), natom,
                                                            (int)nrows);
   DPGB_TRY(check_launch("atom_energy"));
-  if (batch)
-    frame_sum_batch_kernel<<<dim3(batch->ft.nframes, 10), 256, 0, st>>>(energy, virial, e_row, dp.ws_vir.as<double>(),
-                                                                         batch->ft.atom_off);
-  else
-    frame_sum_kernel<<<dim3(nframes, 10), 256, 0, st>>>(energy, virial, e_row, dp.ws_vir.as<double>(), natom);
+  frame_part_kernel<<<dim3(sum_chunks, sum_frames), kFrameSumThreads, 0, st>>>(
+      dp.ws_part.as<double>(), e_row, dp.ws_vir.as<double>(), batch ? batch->ft.atom_off : nullptr, natom);
+  DPGB_TRY(check_launch("frame_part"));
+  frame_final_kernel<<<ceil_div(sum_frames, 8), 256, 0, st>>>(energy, virial, dp.ws_part.as<double>(), sum_chunks,
+                                                               sum_frames);
   DPGB_TRY(check_launch("frame_sum"));
-  launches += 2;
+  launches += 3;
   dp.mark(DPGB_STAGE_REDUCE, 1, st);
   dp.launches = launches;
   return DPGB_OK;
@@ -1222,6 +1230,7 @@ int batch_setup(BatchImpl& b, DeepPotImpl& dp, int nframes, const int* natoms, c
   b.in.ncells = b.ncells;
   b.in.svec = b.svec.as<double>();
   b.in.spos = b.spos.as<int>();
+  b.in.max_atoms = *std::max_element(natoms, natoms + nframes);
   return DPGB_OK;
 }
 

@@ -804,8 +804,9 @@ __global__ void dxyz_kernel(float* __restrict__ dxyz, const float* __restrict__ 
   const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int row = blockIdx.x * wpb + warp;
   if (row >= nrows) return;
-  float* sx = s_dx + (size_t)warp * (4 * ng + ng * M);
-  float* sd = sx + 4 * ng;
+  float* sx = s_dx + (size_t)warp * (4 * ng + ng * M + 4 * M);
+  float* sdT = sx + 4 * ng;  // dD transposed: [m][n], so lanes over n read consecutive words
+  float* sT = sdT + ng * M;  // T[c][m] = sum_n' dD[n'][m] xyz[c][n']
   float* out = dxyz + (size_t)row * 4 * ng;
   if (atype[row % nloc] < 0) {
     for (int q = lane; q < 4 * ng; q += 32) out[q] = 0.f;
@@ -814,16 +815,26 @@ __global__ void dxyz_kernel(float* __restrict__ dxyz, const float* __restrict__ 
   const float* xr = xyz + (size_t)row * 4 * ng;
   const float* d = dD + (size_t)row_pos[row] * ng * M;
   for (int q = lane; q < 4 * ng; q += 32) sx[q] = xr[q];
-  for (int q = lane; q < ng * M; q += 32) sd[q] = d[q];
+  for (int q = lane; q < ng * M; q += 32) {
+    const int n = q / M, m = q - n * M;
+    sdT[m * ng + n] = d[q];
+  }
+  __syncwarp();
+  for (int q = lane; q < 4 * M; q += 32) {
+    const int c = q / M, m = q - c * M;
+    const float* xc = sx + c * ng;
+    const float* dm = sdT + m * ng;
+    float s = 0.f;
+    for (int n2 = 0; n2 < ng; ++n2) s = fmaf(dm[n2], xc[n2], s);
+    sT[q] = s;
+  }
   __syncwarp();
   const float inv = 1.f / (float)nnei;
   for (int q = lane; q < 4 * ng; q += 32) {
     const int c = q / ng, n = q - c * ng;
     const float* xc = sx + c * ng;
-    float s = 0.f;
-    for (int m = 0; m < M; ++m) s = fmaf(sd[n * M + m], xc[m], s);
-    if (n < M)
-      for (int n2 = 0; n2 < ng; ++n2) s = fmaf(sd[n2 * M + n], xc[n2], s);
+    float s = n < M ? sT[c * M + n] : 0.f;
+    for (int m = 0; m < M; ++m) s = fmaf(sdT[m * ng + n], xc[m], s);
     out[q] = s * inv;
   }
 }
@@ -885,7 +896,7 @@ int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChun
 
 int launch_dxyz(const DescParams<float>& p, const float* dD, const float* xyz, float* dxyz, cudaStream_t st) {
   if (p.nrows <= 0) return DPGB_OK;
-  const size_t per_warp = sizeof(float) * ((size_t)4 * p.ng + (size_t)p.ng * p.axis);
+  const size_t per_warp = sizeof(float) * ((size_t)4 * p.ng + (size_t)p.ng * p.axis + 4 * (size_t)p.axis);
   int wpb = 8;
   while (wpb > 1 && per_warp * wpb > 96 * 1024) wpb >>= 1;
   if (per_warp * wpb > 227 * 1024) return fail(DPGB_EINVAL, "dxyz: descriptor too wide for shared memory");

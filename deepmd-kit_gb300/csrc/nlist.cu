@@ -584,28 +584,50 @@ format_nlist_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
   if (__any_sync(0xffffffffu, dropped) && lane == 0) atomicAdd(&status[kStatusDropped], 1);
 }
 
-// single-block exclusive scan of n ints (n+1 outputs)
+// exclusive scan out[0..n] of in[0..n) (out[n] = total) by one CTA of 1024
+// threads, in tiles of 4096 consecutive elements (4 per thread): coalesced
+// loads, warp-shuffle scans, a running carry between tiles
 __global__ void scan_kernel(int* __restrict__ out, const int* __restrict__ in, int n) {
-  __shared__ int s_part[1024];
-  const int t = threadIdx.x;
-  const int per = (n + blockDim.x - 1) / blockDim.x;
-  const int b = t * per, e = min(n, b + per);
-  int s = 0;
-  for (int k = b; k < e; ++k) s += in[k];
-  s_part[t] = s;
+  __shared__ int s_warp[32];
+  __shared__ int s_carry;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t == 0) s_carry = 0;
   __syncthreads();
-  for (int o = 1; o < blockDim.x; o <<= 1) {
-    int v = t >= o ? s_part[t - o] : 0;
+  for (int base = 0; base < n; base += 4 * blockDim.x) {
+    const int idx = base + 4 * t;
+    int v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = idx + k < n ? in[idx + k] : 0;
+    const int local = v[0] + v[1] + v[2] + v[3];
+    int x = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
     __syncthreads();
-    s_part[t] += v;
+    if (warp == 0) {
+      int w = s_warp[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      s_warp[lane] = w;
+    }
+    __syncthreads();
+    int run = s_carry + (x - local) + (warp > 0 ? s_warp[warp - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (idx + k < n) out[idx + k] = run;
+      run += v[k];
+    }
+    __syncthreads();
+    if (t == 0) s_carry += s_warp[(blockDim.x >> 5) - 1];
     __syncthreads();
   }
-  int run = t == 0 ? 0 : s_part[t - 1];
-  for (int k = b; k < e; ++k) {
-    out[k] = run;
-    run += in[k];
-  }
-  if (t == blockDim.x - 1) out[n] = s_part[t];
+  if (t == 0) out[n] = s_carry;
 }
 
 // transpose: count, fill, then sort every bucket by pair id
