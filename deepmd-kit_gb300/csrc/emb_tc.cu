@@ -146,6 +146,46 @@ __device__ __forceinline__ void issue_mma(uint32_t d_tmem, uint32_t a_s, uint32_
                  ks > 0 ? 1u : 0u);
 }
 
+// Pack whole runs of section t (rows s_cursor .. row1 of the type-sorted
+// order) into one tile of at most kTcRows pairs and kMaxAtoms atoms.  Warp 0
+// loads 32 run lengths (and rows) at once and every lane runs the same greedy
+// loop over them through shuffles, so one load round trip serves up to 32
+// rows instead of one dependent load per row.
+template <int kMaxAtoms>
+__device__ __forceinline__ void pack_tile(const int* __restrict__ run_len, const int* __restrict__ sorted_rows,
+                                          int ntypes, int row1, int t, int* s_row, int* s_off, int* s_ntile,
+                                          int* s_cursor, int lane) {
+  int cur = *s_cursor, n = 0, pairs = 0;
+  bool done = false;
+  while (!done && cur < row1) {
+    const int r = cur + lane;
+    const int len = r < row1 ? run_len[(size_t)r * ntypes + t] : -1;
+    const int srow = r < row1 ? sorted_rows[r] : 0;
+    int k = 0;
+    for (; k < 32; ++k) {
+      const int lk = __shfl_sync(0xffffffffu, len, k);
+      const int sk = __shfl_sync(0xffffffffu, srow, k);
+      if (lk < 0 || (lk > 0 && (n == kMaxAtoms || pairs + lk > kTcRows))) {
+        done = true;
+        break;
+      }
+      if (lk == 0) continue;
+      if (lane == 0) {
+        s_row[n] = sk;
+        s_off[n] = pairs;
+      }
+      pairs += lk;
+      ++n;
+    }
+    cur += k;
+  }
+  if (lane == 0) {
+    s_off[n] = pairs;
+    *s_ntile = n;
+    *s_cursor = cur;
+  }
+}
+
 // Environment of the tile's pair p: fills Rn (normalised), d (displacement,
 // FP32 after the FP64 subtraction), the slot index and flags.
 struct PairInfo {
@@ -321,25 +361,8 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
       const float* i3 = b3 + P::N3;
       while (alive) {
         // pack whole runs of this section into a tile
-        if (tid == 0) {
-          int cur = s_cursor, n = 0, pairs = 0;
-          while (cur < ch.row1 && n < kTcMaxAtoms) {
-            const int len = run_len[(size_t)cur * p.ntypes + t];
-            if (len == 0) {
-              ++cur;
-              continue;
-            }
-            if (pairs + len > kTcRows) break;
-            s_row[n] = sorted_rows[cur];
-            s_off[n] = pairs;
-            pairs += len;
-            ++n;
-            ++cur;
-          }
-          s_off[n] = pairs;
-          s_ntile = n;
-          s_cursor = cur;
-        }
+        if (warp == 0)
+          pack_tile<kTcMaxAtoms>(run_len, sorted_rows, p.ntypes, ch.row1, t, s_row, s_off, &s_ntile, &s_cursor, tid & 31);
         __syncthreads();
         const int ntile = s_ntile;
         if (ntile == 0) break;
@@ -545,25 +568,8 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
       const float* b3 = i2 + P::N2;
       const float* i3 = b3 + P::N3;
       while (alive) {
-        if (tid == 0) {
-          int cur = s_cursor, n = 0, pairs = 0;
-          while (cur < ch.row1 && n < kBwdAtoms) {
-            const int len = run_len[(size_t)cur * p.ntypes + t];
-            if (len == 0) {
-              ++cur;
-              continue;
-            }
-            if (pairs + len > kTcRows) break;
-            s_row[n] = sorted_rows[cur];
-            s_off[n] = pairs;
-            pairs += len;
-            ++n;
-            ++cur;
-          }
-          s_off[n] = pairs;
-          s_ntile = n;
-          s_cursor = cur;
-        }
+        if (warp == 0)
+          pack_tile<kBwdAtoms>(run_len, sorted_rows, p.ntypes, ch.row1, t, s_row, s_off, &s_ntile, &s_cursor, tid & 31);
         __syncthreads();
         const int ntile = s_ntile;
         if (ntile == 0) break;

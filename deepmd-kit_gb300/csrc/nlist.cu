@@ -366,6 +366,104 @@ size_t cell_stage_smem() {
          (size_t)kCellWarps * kKeptCap * (sizeof(double) + 2 * sizeof(int));
 }
 
+// One centre atom against the staged stencil atoms, one warp.  Pass 1: the
+// FP32 prefilter (radius rcut + 1e-3, well above its rounding error) packs
+// the staged slots of the candidates into wi.  Pass 2: the exact FP64
+// distance, the same arithmetic as nlist_pt_kernel, on full warps over the
+// packed candidates; the pairs with r <= rcut are packed again, in place, as
+// (wr, wi, wt) = (distance, extended index, type).  The FP64 pipe is narrow on
+// this part, so taking it only with all 32 lanes busy matters.  Returns the
+// number kept, or -(candidates) - 1 when more than kKeptCap candidates.
+// Staged atom p is image shift s = sidx[p] / nloc of atom a_beg + sidx[p] % nloc.
+__device__ int staged_search_atom(double* __restrict__ wr, int* __restrict__ wi, int* __restrict__ wt,
+                                  const float* __restrict__ sx, const float* __restrict__ sy,
+                                  const float* __restrict__ sz, const int* __restrict__ sidx,
+                                  const int* __restrict__ stype, int total, int self, float xf, float yf, float zf,
+                                  float rcf2, const double* __restrict__ coord, const double* __restrict__ svec,
+                                  int nloc, int a_beg, double xi, double yi, double zi, double rcut, int lane) {
+  const unsigned below = (1u << lane) - 1u;
+  int nc = 0;
+  for (int p0 = 0; p0 < total; p0 += 32) {
+    const int p = p0 + lane;
+    bool cand = false;
+    if (p < total && stype[p] >= 0 && sidx[p] != self) {
+      const float fx = sx[p] - xf, fy = sy[p] - yf, fz = sz[p] - zf;
+      cand = fx * fx + fy * fy + fz * fz <= rcf2;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, cand);
+    const int pos = nc + __popc(m & below);
+    if (cand && pos < kKeptCap) wi[pos] = p;
+    nc += __popc(m);
+  }
+  if (nc > kKeptCap) return -nc - 1;
+  __syncwarp();
+  int n = 0;
+  for (int k0 = 0; k0 < nc; k0 += 32) {
+    const int k = k0 + lane;
+    bool keep = false;
+    double r = 0.0;
+    int e = 0, t = 0;
+    if (k < nc) {
+      const int p = wi[k];
+      e = sidx[p];
+      t = stype[p];
+      const int s = e / nloc, j = a_beg + (e - s * nloc);
+      const double dx = (coord[3 * j] + svec[3 * s]) - xi;
+      const double dy = (coord[3 * j + 1] + svec[3 * s + 1]) - yi;
+      const double dz = (coord[3 * j + 2] + svec[3 * s + 2]) - zi;
+      r = dist_fma(dx, dy, dz);
+      keep = r <= rcut;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    __syncwarp();  // every lane has read its slot before any is overwritten
+    const int pos = n + __popc(m & below);  // pos <= k: never a slot still to be read
+    if (keep) {
+      wr[pos] = r;
+      wi[pos] = e;
+      wt[pos] = t;
+    }
+    n += __popc(m);
+  }
+  __syncwarp();
+  return n;
+}
+
+// Rank a warp's kept list by (distance, extended index) and place each pair
+// in its type section while its per-type rank < sel[t] and its global rank
+// < nnei (topk of sum(sel), then the per-type split).  Each lane holds up to
+// four kept entries in registers and streams the list once per 128.
+__device__ void staged_rank_place(int* __restrict__ row, const double* __restrict__ wr, const int* __restrict__ wi,
+                                  const int* __restrict__ wt, int n, const SelInfo& sel, int lane) {
+  for (int k0 = 0; k0 < n; k0 += 128) {
+    long long rk[4];
+    int ik[4], tk[4], rank[4], trank[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = k0 + lane + 32 * q;
+      rk[q] = k < n ? __double_as_longlong(wr[k]) : 0x7fffffffffffffffLL;
+      ik[q] = k < n ? wi[k] : 0x7fffffff;
+      tk[q] = k < n ? wt[k] : -1;
+      rank[q] = trank[q] = 0;
+    }
+    for (int m2 = 0; m2 < n; ++m2) {
+      const long long rm = __double_as_longlong(wr[m2]);
+      const int im = wi[m2], tm = wt[m2];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool lt = rm < rk[q] || (rm == rk[q] && im < ik[q]);
+        rank[q] += lt;
+        trank[q] += lt && tm == tk[q];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int t = tk[q];
+      if (k0 + lane + 32 * q < n && rank[q] < sel.nnei && t < sel.ntypes && trank[q] < sel.sel[t])
+        row[sel.sec[t] + trank[q]] = ik[q];
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kCellWarps * 32)
 nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, const int* __restrict__ atype,
                   const int* __restrict__ offsets, const int* __restrict__ cell_atoms,
@@ -436,74 +534,14 @@ nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
     const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
     const int self = g.zero_shift * nloc + i;
     const float xf = (float)(xi - ox), yf = (float)(yi - oy), zf = (float)(zi - oz);
-    int n = 0;
-    bool overflow = false;
-    for (int p0 = 0; p0 < total; p0 += 32) {
-      const int p = p0 + lane;
-      bool keep = false;
-      double r = 0.0;
-      if (p < total && stype[p] >= 0 && sidx[p] != self) {
-        const float fx = sx[p] - xf, fy = sy[p] - yf, fz = sz[p] - zf;
-        if (fx * fx + fy * fy + fz * fz <= rcf2) {
-          // exact distance, the same arithmetic as nlist_pt_kernel
-          const int e = sidx[p], s = e / nloc, j = e - s * nloc;
-          const double dx = (coord[3 * j] + svec[3 * s]) - xi;
-          const double dy = (coord[3 * j + 1] + svec[3 * s + 1]) - yi;
-          const double dz = (coord[3 * j + 2] + svec[3 * s + 2]) - zi;
-          r = dist_fma(dx, dy, dz);
-          keep = r <= rcut;
-        }
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      const int pos = n + __popc(m & ((1u << lane) - 1u));
-      if (keep) {
-        if (pos < kKeptCap) {
-          wr[pos] = r;
-          wi[pos] = sidx[p];
-          wt[pos] = stype[p];
-        } else {
-          overflow = true;
-        }
-      }
-      n += __popc(m);
-    }
-    overflow = __any_sync(0xffffffffu, overflow);
-    if (overflow) {  // more than kKeptCap within rcut: the whole cell goes to the per-atom kernel
+    const int n = staged_search_atom(wr, wi, wt, sx, sy, sz, sidx, stype, total, self, xf, yf, zf, rcf2, coord, svec,
+                                     nloc, 0, xi, yi, zi, rcut, lane);
+    if (n < 0) {  // more than kKeptCap candidates: the whole cell goes to the per-atom kernel
       if (lane == 0) fallback[c] = 1;
       __syncwarp();
       continue;
     }
-    __syncwarp();
-    // rank by counting: each lane holds up to 4 kept entries in registers and
-    // streams the warp's kept list once per group of 128
-    for (int k0 = 0; k0 < n; k0 += 128) {
-      long long rk[4];
-      int ik[4], tk[4], rank[4], trank[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int k = k0 + lane + 32 * q;
-        rk[q] = k < n ? __double_as_longlong(wr[k]) : 0x7fffffffffffffffLL;
-        ik[q] = k < n ? wi[k] : 0x7fffffff;
-        tk[q] = k < n ? wt[k] : -1;
-        rank[q] = trank[q] = 0;
-      }
-      for (int m2 = 0; m2 < n; ++m2) {
-        const long long rm = __double_as_longlong(wr[m2]);
-        const int im = wi[m2], tm = wt[m2];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const bool lt = rm < rk[q] || (rm == rk[q] && im < ik[q]);
-          rank[q] += lt;
-          trank[q] += lt && tm == tk[q];
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int t = tk[q];
-        if (k0 + lane + 32 * q < n && rank[q] < sel.nnei && t < sel.ntypes && trank[q] < sel.sel[t])
-          row[sel.sec[t] + trank[q]] = ik[q];
-      }
-    }
+    staged_rank_place(row, wr, wi, wt, n, sel, lane);
     __syncwarp();
   }
 }
@@ -884,74 +922,17 @@ nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coor
     const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
     const int self = g.zero_shift * nloc + (i - a_beg);
     const float xf = (float)(xi - ox), yf = (float)(yi - oy), zf = (float)(zi - oz);
-    int n = 0;
-    bool overflow = false;
-    for (int p0 = 0; p0 < total; p0 += 32) {
-      const int p = p0 + lane;
-      bool keep = false;
-      double r = 0.0;
-      if (p < total && stype[p] >= 0 && sidx[p] != self) {
-        const float fx = sx[p] - xf, fy = sy[p] - yf, fz = sz[p] - zf;
-        if (fx * fx + fy * fy + fz * fz <= rcf2) {
-          const int e = sidx[p], s = e / nloc, j = a_beg + (e - s * nloc);
-          const double dx = (coord[3 * j] + svec[3 * s]) - xi;
-          const double dy = (coord[3 * j + 1] + svec[3 * s + 1]) - yi;
-          const double dz = (coord[3 * j + 2] + svec[3 * s + 2]) - zi;
-          r = dist_fma(dx, dy, dz);
-          keep = r <= rcut;
-        }
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      const int pos = n + __popc(m & ((1u << lane) - 1u));
-      if (keep) {
-        if (pos < kKeptCap) {
-          wr[pos] = r;
-          wi[pos] = sidx[p];
-          wt[pos] = stype[p];
-        } else {
-          overflow = true;
-        }
-      }
-      n += __popc(m);
-    }
-    overflow = __any_sync(0xffffffffu, overflow);
-    if (overflow) {
+    const int n = staged_search_atom(wr, wi, wt, sx, sy, sz, sidx, stype, total, self, xf, yf, zf, rcf2, coord, svec,
+                                     nloc, a_beg, xi, yi, zi, rcut, lane);
+    if (n < 0) {
       if (lane == 0) {
-        atomicMax(&status[kStatusOverflow], n);
+        atomicMax(&status[kStatusOverflow], -n - 1);
         atomicMax(&status[kStatusOverflowAtom], i + 1);
       }
       __syncwarp();
       continue;
     }
-    __syncwarp();
-    for (int k0 = 0; k0 < n; k0 += 128) {
-      long long rk[4];
-      int ik[4], tk[4], rank[4], trank[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int k = k0 + lane + 32 * q;
-        rk[q] = k < n ? __double_as_longlong(wr[k]) : 0x7fffffffffffffffLL;
-        ik[q] = k < n ? wi[k] : 0x7fffffff;
-        tk[q] = k < n ? wt[k] : -1;
-        rank[q] = trank[q] = 0;
-      }
-      for (int m2 = 0; m2 < n; ++m2) {
-        const long long rm = __double_as_longlong(wr[m2]);
-        const int im = wi[m2], tm = wt[m2];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const bool lt = rm < rk[q] || (rm == rk[q] && im < ik[q]);
-          rank[q] += lt;
-          trank[q] += lt && tm == tk[q];
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int t = tk[q];
-        if (k0 + lane + 32 * q < n && rank[q] < sel.nnei && t < sel.ntypes && trank[q] < sel.sel[t])
-          row[sel.sec[t] + trank[q]] = ik[q];
-      }
-    }
+    staged_rank_place(row, wr, wi, wt, n, sel, lane);
     __syncwarp();
   }
 }
