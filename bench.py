@@ -233,6 +233,8 @@ def run_compressed(args, world, rank, local):
     x = torch.tensor(coord.reshape(1, -1), dtype=torch.float64, device=dev)
     gen = torch.Generator(device=dev).manual_seed(1234 + rank)
     mixed = DeepPot(cparams, "mixed", device=local)
+    skin = 2.0 if args.skin is None else args.skin
+    mixed.set_skin(skin, args.rebuild_every)
     out = mixed.eval_device(x, boxh, atype)
     for _ in range(args.warmup):
         mixed.eval_device(x, boxh, atype, out=out)
@@ -251,11 +253,13 @@ def run_compressed(args, world, rank, local):
             mixed.collect_stages()
         torch.cuda.synchronize()
     _barrier(world)
+    mixed.check_status()  # no neighbour overflow or candidate truncation in the timed steps
     t_ms = _allreduce_max(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), world)
     stages, ncalls = mixed.stage_times()
     launches = mixed.last_launches()
     value = world * nloc * args.steps / (t_ms * 1e-3)
     fp64 = DeepPot(cparams, "fp64", device=local)
+    fp64.set_skin(skin, args.rebuild_every)
     o64 = fp64.eval_device(x, boxh, atype)
     torch.cuda.synchronize()
     s64, e64 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -276,8 +280,11 @@ def run_compressed(args, world, rank, local):
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {
             "workload": "compressed water 32768 H2O (98,304 atoms), box 99.2 A, tables stride 0.01/0.1 x5, "
-                        "N(0, 0.01 A) random walk between evaluations; mixed form; neighbour list rebuilt "
-                        "every evaluation",
+                        "N(0, 0.01 A) random walk between evaluations; mixed form; "
+                        + (f"candidates within rc + {skin:g} A rebuilt every {args.rebuild_every} evaluations "
+                           "(or on a skin/2 move), the list at rc selected every evaluation" if skin > 0 else
+                           "neighbour list rebuilt every evaluation"),
+            "skin_A": skin, "rebuild_every": args.rebuild_every,
             "natoms": nloc, "l2": "inputs larger than L2",
             "fp64_atom_steps_per_s": nloc / (fp64_ms * 1e-3), "fp64_ms_per_step": fp64_ms,
             "mixed_over_fp64": value / world / (nloc / (fp64_ms * 1e-3)),
@@ -385,6 +392,9 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--ref-sample", type=int, default=768)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skin", type=float, default=None,
+                    help="neighbour-list skin in A for water98k-compressed (default 2; 0 = rebuild every step)")
+    ap.add_argument("--rebuild-every", type=int, default=10)
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.warmup < 3:

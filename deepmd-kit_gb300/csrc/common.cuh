@@ -47,7 +47,7 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 // Device-side status word layout (one int per code, atomicMax'ed).
-enum StatusSlot { kStatusOverflow = 0, kStatusOverflowAtom = 1, kStatusTimeout = 2, kStatusSlots = 4 };
+enum StatusSlot { kStatusOverflow = 0, kStatusOverflowAtom = 1, kStatusTimeout = 2, kStatusSlots = 6 };
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

@@ -329,6 +329,20 @@ struct DeepPotImpl {
   DeviceBuffer ext_off, ext_idx, ext_atype;
   int ext_nloc = -1, ext_nall = -1, ext_sorted = 0;
   std::vector<int> ext_atype_h;
+  // skin lists (periodic frames; skin 0 = a fresh list every call): the
+  // candidates within rcut + skin are rebuilt every `skin_every` calls or when
+  // an atom moved more than skin / 2; skin_sel describes the flat candidate
+  // rows (width: skin_factor x the count a uniform density gives)
+  double skin = 0.0;
+  int skin_every = 1;
+  int skin_grow = 0;  // > 0: a candidate row needed this many slots: widen, rebuild
+  double skin_factor = 1.25;
+  SelInfo skin_sel{};
+  std::vector<double> skin_box;
+  std::vector<int> skin_atype;
+  int skin_nframes = -1;
+  const void* skin_cand_ptr = nullptr;
+  DeviceBuffer ws_gate, ws_cand, ws_skin_off, ws_skin_ref, ws_coordf, ws_svecf;
   std::string err;
   int launches = 0;
   cudaStream_t stream = nullptr;
@@ -751,6 +765,8 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   if ((ext || batch) && nframes != 1) return fail(DPGB_EINVAL, "an external list or a batch runs as one frame");
   int launches = 0;
   const bool own_geom = !ext && !batch;
+  const bool skin_on = own_geom && box_host && dp.skin > 0.0;
+  const double rc_geo = skin_on ? d.rcut + dp.skin : d.rcut;  // list radius of the cell search
   // --- geometry (host) ---
   std::vector<CellGeom> geo(own_geom ? nframes : 0);
   std::vector<std::vector<int>> spos(own_geom ? nframes : 0);
@@ -764,7 +780,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       // reference image range from the face distances
       CellGeom tmp;
       std::vector<int> dummy;
-      double face_rc = d.rcut;
+      double face_rc = rc_geo;
       // nbuff = ceil(rcut / face distance)
       const double* c = box_host + 9 * f;
       auto crn = [&](int p, int q) {
@@ -779,7 +795,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
                          (int)std::ceil(face_rc / (vol / crn(0, 1)))};
       const std::vector<int> shifts = default_shifts(nb);
       const int ns = (int)shifts.size() / 3;
-      DPGB_TRY(periodic_geom(box_host + 9 * f, d.rcut, ns, shifts.data(), geo[f], spos[f]));
+      DPGB_TRY(periodic_geom(box_host + 9 * f, rc_geo, ns, shifts.data(), geo[f], spos[f]));
       shift_vectors(geo[f], shifts.data(), ns, svecs[f]);
       nshift_max = std::max(nshift_max, ns);
       (void)tmp;
@@ -829,6 +845,56 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   DPGB_TRY(dp.ws_part.alloc(sizeof(double) * 10 * (size_t)sum_frames * sum_chunks));
   DPGB_TRY(dp.ws_act.alloc(sizeof(T) * 2 * m.fit.n_hidden * nrows * maxw));
   DPGB_TRY(dp.ws_gbuf.alloc(sizeof(T) * 4 * nrows * maxw));
+  // skin-list state: candidate capacities, buffers, and whether the stored
+  // candidates still belong to this system (else the next evaluation builds)
+  int ncand = 0;
+  double skin_margin = 0.0;
+  if (skin_on) {
+    if (dp.skin_grow > 0) {  // a row needed skin_grow slots: widen past that
+      dp.skin_factor *= std::max(1.5, 1.1 * dp.skin_grow / std::max(dp.skin_sel.nnei, 1));
+      dp.skin_grow = 0;
+      dp.skin_nframes = -1;
+    }
+    // flat candidate rows: sum(sel) scaled by the volume ratio of the two
+    // spheres and skin_factor
+    const double growth = std::pow(rc_geo / d.rcut, 3) * dp.skin_factor;
+    SelInfo cs = dp.sel;
+    cs.nnei = (int)std::ceil(dp.sel.nnei * growth / 8.0) * 8;
+    cs.strict = 1;
+    cs.flat = 1;
+    ncand = cs.nnei;
+    if (nrows >= (1LL << 31) / std::max(ncand, 1)) return fail(DPGB_EINVAL, "too many atoms for 32-bit candidate ids");
+    DPGB_TRY(dp.ws_gate.alloc(sizeof(int) * 2));
+    DPGB_TRY(dp.ws_cand.alloc(sizeof(int) * nrows * ncand));
+    DPGB_TRY(dp.ws_skin_off.alloc(sizeof(double) * nrows * 3));
+    DPGB_TRY(dp.ws_skin_ref.alloc(sizeof(double) * nrows * 3));
+    DPGB_TRY(dp.ws_coordf.alloc(sizeof(float4) * nrows));
+    DPGB_TRY(dp.ws_svecf.alloc(sizeof(float4) * (size_t)nshift_max * nframes));
+    const std::vector<double> box_now(box_host, box_host + 9 * (size_t)nframes);
+    const void* ptrs = dp.ws_cand.ptr;
+    const bool same = dp.skin_nframes == nframes && dp.skin_box == box_now && dp.skin_atype == dp.atype_cache &&
+                      dp.skin_cand_ptr == ptrs && dp.skin_sel.nnei == cs.nnei;
+    if (!same) {
+      const int init[2] = {0, -1};  // no rebuild flagged yet, no list
+      DPGB_CUDA(cudaMemcpyAsync(dp.ws_gate.ptr, init, sizeof(init), cudaMemcpyHostToDevice, st));
+      dp.skin_nframes = nframes;
+      dp.skin_box = box_now;
+      dp.skin_atype = dp.atype_cache;
+      dp.skin_cand_ptr = ptrs;
+      dp.skin_sel = cs;
+    }
+    // FP32 prefilter margin above rcut: the FP32 rounding of coordinates and
+    // shift vectors of magnitude <= cmax stays below 4e-7 cmax in a distance
+    double cmax = 0.0;
+    for (int f = 0; f < nframes; ++f) {
+      const double* c = box_host + 9 * f;
+      double len = 0.0;
+      for (int k = 0; k < 3; ++k) len += std::sqrt(c[3 * k] * c[3 * k] + c[3 * k + 1] * c[3 * k + 1] + c[3 * k + 2] * c[3 * k + 2]);
+      const int nbm = std::max(geo[f].nbuff[0], std::max(geo[f].nbuff[1], geo[f].nbuff[2]));
+      cmax = std::max(cmax, len * (nbm + 2) + dp.skin);
+    }
+    skin_margin = 1e-3 + 1e-6 * cmax;
+  }
 
   int* status = dp.ws_status.as<int>();
   DPGB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * kStatusSlots, st));
@@ -843,6 +909,12 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     }
     DPGB_CUDA(cudaMemcpyAsync(dp.ws_svec.ptr, sv.data(), sizeof(double) * sv.size(), cudaMemcpyHostToDevice, st));
     DPGB_CUDA(cudaMemcpyAsync(dp.ws_spos.ptr, sp.data(), sizeof(int) * sp.size(), cudaMemcpyHostToDevice, st));
+    if (skin_on) {
+      std::vector<float4> svf((size_t)nshift_max * nframes);
+      for (size_t q = 0; q < svf.size(); ++q)
+        svf[q] = make_float4((float)sv[3 * q], (float)sv[3 * q + 1], (float)sv[3 * q + 2], 0.f);
+      DPGB_CUDA(cudaMemcpyAsync(dp.ws_svecf.ptr, svf.data(), sizeof(float4) * svf.size(), cudaMemcpyHostToDevice, st));
+    }
   }
   double* coord_n = dp.ws_coord.as<double>();
   int* nlist = dp.ws_nlist.as<int>();
@@ -857,9 +929,30 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
                                 batch->svec, batch->spos, d.rcut, dp.sel, dp.ws_cell.ptr, status, st));
     launches += 4;
   }
+  int* gate = dp.ws_gate.as<int>();
+  if (skin_on) {
+    DPGB_TRY(launch_skin_check(gate, coord_dev, dp.ws_skin_ref.as<double>(), (int)nrows, dp.skin, dp.skin_every, st));
+    ++launches;
+  }
   for (int f = 0; f < (int)geo.size(); ++f) {
     const double* cin = coord_dev + (size_t)f * natom * 3;
     double* cout = coord_n + (size_t)f * natom * 3;
+    if (skin_on) {
+      // build (when gate[0]): wrap, candidates within rcut + skin; always:
+      // select the list at rcut from the candidates
+      const size_t a0 = (size_t)f * natom;
+      const double* svf = dp.ws_svec.as<double>() + (size_t)3 * nshift_max * f;
+      int* cand = dp.ws_cand.as<int>() + a0 * ncand;
+      DPGB_TRY(launch_skin_coords(cout, dp.ws_coordf.as<float4>() + a0, dp.ws_skin_off.as<double>() + 3 * a0,
+                                  dp.ws_skin_ref.as<double>() + 3 * a0, cin, natom, geo[f], gate, st));
+      DPGB_TRY(launch_nlist_pt(cand, cout, dp.atype_dev.as<int>(), natom, geo[f], dp.ws_spos.as<int>() + spos_n * f,
+                               svf, rc_geo, dp.skin_sel, dp.ws_cell.ptr, status, st, gate));
+      DPGB_TRY(launch_skin_select(nlist + a0 * nnei, cand, ncand, cout, dp.ws_coordf.as<float4>() + a0,
+                                  dp.atype_dev.as<int>(), svf, dp.ws_svecf.as<float4>() + (size_t)nshift_max * f,
+                                  natom, d.rcut, skin_margin, dp.sel, status, st));
+      launches += 7;
+      continue;
+    }
     if (box_host) {
       DPGB_TRY(launch_normalize(cout, cin, natom, geo[f], st));
     } else {
@@ -870,6 +963,10 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
                              dp.ws_spos.as<int>() + spos_n * f, dp.ws_svec.as<double>() + (size_t)3 * nshift_max * f,
                              d.rcut, dp.sel, dp.ws_cell.ptr, status, st));
     launches += 5;  // cell count, scan, fill, staged search, per-atom search of flagged cells
+  }
+  if (skin_on) {
+    DPGB_TRY(launch_skin_advance(gate, st));
+    ++launches;
   }
   dp.mark(DPGB_STAGE_NLIST, 1, st);
   // sorted transpose of the list over local rows
@@ -1047,6 +1144,11 @@ int check_status(DeepPotImpl& dp, cudaStream_t st) {
                                     " entries) at atom/row " + std::to_string(h[kStatusOverflowAtom] - 1));
   if (h[kStatusTimeout] > 0)
     return fail(DPGB_ETIMEOUT, "a tensor-core completion wait timed out; results are invalid");
+  if (h[kStatusTruncated] > 0) {
+    dp.skin_grow = h[kStatusTruncated];  // the next call widens the candidate rows and rebuilds
+    return fail(DPGB_EOVERFLOW, "skin candidate rows too narrow (a row needs " + std::to_string(h[kStatusTruncated]) +
+                                    " slots within rcut + skin); results are invalid");
+  }
   return DPGB_OK;
 }
 
@@ -1534,6 +1636,30 @@ int dpgb_deeppot_compute(dpgb_deeppot* dp, int nframes, int natom, const double*
     return check_status(im, st);  // synchronises
   };
   int rc = body();
+  if (rc == DPGB_EOVERFLOW && im.skin_grow > 0) rc = body();  // widened skin candidates, rebuilt
+  im.err = rc == DPGB_OK ? "" : dpgb_last_error();
+  return rc;
+}
+
+int dpgb_deeppot_set_skin(dpgb_deeppot* dp, double skin, int every) {
+  clear_error();
+  if (!dp) return fail(DPGB_EINVAL, "NULL handle");
+  if (!(skin >= 0.0) || every < 1) return fail(DPGB_EINVAL, "skin must be >= 0 and every >= 1");
+  DeepPotImpl& im = dp->impl;
+  im.skin = skin;
+  im.skin_every = every;
+  im.skin_nframes = -1;  // the next call builds
+  return DPGB_OK;
+}
+
+int dpgb_deeppot_check_status(dpgb_deeppot* dp, void* stream) {
+  clear_error();
+  if (!dp) return fail(DPGB_EINVAL, "NULL handle");
+  DeepPotImpl& im = dp->impl;
+  if (!im.ws_status.ptr) return DPGB_OK;
+  cudaStream_t st = as_stream(stream);
+  if (!st) st = im.stream;
+  const int rc = check_status(im, st);
   im.err = rc == DPGB_OK ? "" : dpgb_last_error();
   return rc;
 }

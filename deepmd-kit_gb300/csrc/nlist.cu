@@ -152,6 +152,8 @@ int sel_from_host(const int* sel_host, int ntypes, SelInfo& s) {
     s.sec[t + 1] = s.sec[t] + sel_host[t];
   }
   s.nnei = s.sec[ntypes];
+  s.strict = 0;
+  s.flat = 0;
   return DPGB_OK;
 }
 
@@ -163,11 +165,10 @@ __device__ __forceinline__ double dist_fma(double dx, double dy, double dz) {
   return sqrt(fma(dz, dz, fma(dy, dy, dx * dx)));
 }
 
-__global__ void normalize_kernel(double* __restrict__ out, const double* __restrict__ in, int n,
-                                 CellGeom g) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double x = in[3 * i], y = in[3 * i + 1], z = in[3 * i + 2];
+// wrap a point into the periodic cell (fractional coordinates mod 1), the
+// arithmetic of deepmd/pt/utils/region.py:86-105
+__device__ __forceinline__ void wrap_point(const double* in, const CellGeom& g, double* out) {
+  const double x = in[0], y = in[1], z = in[2];
   double f[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -176,8 +177,14 @@ __global__ void normalize_kernel(double* __restrict__ out, const double* __restr
     f[k] = v;
   }
 #pragma unroll
-  for (int k = 0; k < 3; ++k)
-    out[3 * i + k] = fma(f[2], g.cell[6 + k], fma(f[1], g.cell[3 + k], f[0] * g.cell[k]));
+  for (int k = 0; k < 3; ++k) out[k] = fma(f[2], g.cell[6 + k], fma(f[1], g.cell[3 + k], f[0] * g.cell[k]));
+}
+
+__global__ void normalize_kernel(double* __restrict__ out, const double* __restrict__ in, int n,
+                                 CellGeom g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  wrap_point(in + 3 * i, g, out + 3 * i);
 }
 
 __global__ void extend_kernel(double* __restrict__ cext, int* __restrict__ text,
@@ -194,9 +201,10 @@ __global__ void extend_kernel(double* __restrict__ cext, int* __restrict__ text,
 }
 
 __global__ void cell_count_kernel(int* __restrict__ cell_of, int* __restrict__ counts,
-                                  const double* __restrict__ coord, int n, CellGeom g) {
+                                  const double* __restrict__ coord, int n, CellGeom g,
+                                  const int* __restrict__ gate) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || (gate && !gate[0])) return;
   int c[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -217,9 +225,9 @@ __global__ void cell_count_kernel(int* __restrict__ cell_of, int* __restrict__ c
 
 __global__ void cell_fill_kernel(int* __restrict__ cell_atoms, int* __restrict__ cursor,
                                  const int* __restrict__ offsets, const int* __restrict__ cell_of,
-                                 int n) {
+                                 int n, const int* __restrict__ gate) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || (gate && !gate[0])) return;
   const int c = cell_of[i];
   cell_atoms[offsets[c] + atomicAdd(&cursor[c], 1)] = i;
 }
@@ -253,6 +261,23 @@ __device__ __forceinline__ bool cand_less(double ra, int ia, double rb, int ib) 
   return a < b || (a == b && ia < ib);
 }
 
+// Placement of one ranked pair: per type (the first sel[t] of its type among
+// the global top sum(sel)) or, for flat candidate rows, at its global rank.
+// A strict list records the width a missing slot would have needed.
+__device__ __forceinline__ void place_pair(int* __restrict__ row, int rank, int trank, int t, int e,
+                                           const SelInfo& sel, int* __restrict__ status) {
+  if (sel.flat) {
+    if (rank < sel.nnei)
+      row[rank] = e;
+    else if (sel.strict)
+      atomicMax(&status[kStatusTruncated], rank + 1);
+  } else if (rank < sel.nnei && t < sel.ntypes && trank < sel.sel[t]) {
+    row[sel.sec[t] + trank] = e;
+  } else if (sel.strict) {
+    atomicMax(&status[kStatusTruncated], trank + 1);
+  }
+}
+
 // One warp per centre atom: gather the atoms of the stencil cells within
 // rcut, rank them by (distance, extended index), keep the nearest nsel and
 // place each in its type section while its per-type rank < sel[t].
@@ -262,13 +287,13 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
                 const int* __restrict__ offsets, const int* __restrict__ cell_atoms,
                 const int* __restrict__ shift_pos, const double* __restrict__ svec, int nloc,
                 CellGeom g, double rcut, SelInfo sel, const int* __restrict__ only_cells,
-                int* __restrict__ status) {
+                int* __restrict__ status, const int* __restrict__ gate) {
   __shared__ double s_r[kSearchWarps][kCap];
   __shared__ int s_idx[kSearchWarps][kCap];
   __shared__ int s_type[kSearchWarps][kCap];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kSearchWarps + warp;
-  if (i >= nloc) return;
+  if (i >= nloc || (gate && !gate[0])) return;
   if (only_cells && !only_cells[cell_of[i]]) return;  // handled by the staged kernel
   int* row = nlist + (size_t)i * sel.nnei;
   for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
@@ -345,7 +370,7 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
       trank += lt && s_type[warp][m2] == tk;
     }
     // topk(sum(sel)): candidates of global rank >= nnei are dropped
-    if (rank < sel.nnei && tk < sel.ntypes && trank < sel.sel[tk]) row[sel.sec[tk] + trank] = ik;
+    place_pair(row, rank, trank, tk, ik, sel, status);
   }
 }
 
@@ -355,85 +380,28 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
 // each) scan them without global gathers.  Same distances (the FMA norm of
 // (r_j + shift) - r_i), same ranking by (distance, extended index), same
 // per-type placement: the list is bitwise that of nlist_pt_kernel.  A cell
-// whose stencil holds more than kStageCap atoms is flagged and left to
+// whose stencil holds more than stage_cap atoms is flagged and left to
 // nlist_pt_kernel.
 constexpr int kCellWarps = 4;
-constexpr int kStageCap = 2048;
-constexpr int kKeptCap = 512;
+constexpr int kKeptCap = 512;  // per-warp kept pairs of the skin selection
+// Shared memory of the staged kernels: stage_cap stencil atoms (3 floats, 2
+// ints) and, for typed lists, kept_cap pairs per warp (a double key, 2 ints).
+// 54 KB per CTA keeps four CTAs (16 warps) on an SM: typed lists stage 1536
+// atoms and keep 384 pairs per warp; flat candidate rows keep none and stage
+// 2688 (a stencil at rcut + skin).
+constexpr int kTypedStageCap = 1536, kTypedKeptCap = 384, kFlatStageCap = 2688;
 
-size_t cell_stage_smem() {
-  return (size_t)kStageCap * (3 * sizeof(float) + 2 * sizeof(int)) +
-         (size_t)kCellWarps * kKeptCap * (sizeof(double) + 2 * sizeof(int));
+size_t cell_stage_smem(int stage_cap, int kept_cap) {
+  return (size_t)stage_cap * (3 * sizeof(float) + 2 * sizeof(int)) +
+         (size_t)kCellWarps * kept_cap * (sizeof(double) + 2 * sizeof(int));
 }
 
-// One centre atom against the staged stencil atoms, one warp.  Pass 1: the
-// FP32 prefilter (radius rcut + 1e-3, well above its rounding error) packs
-// the staged slots of the candidates into wi.  Pass 2: the exact FP64
-// distance, the same arithmetic as nlist_pt_kernel, on full warps over the
-// packed candidates; the pairs with r <= rcut are packed again, in place, as
-// (wr, wi, wt) = (distance, extended index, type).  The FP64 pipe is narrow on
-// this part, so taking it only with all 32 lanes busy matters.  Returns the
-// number kept, or -(candidates) - 1 when more than kKeptCap candidates.
-// Staged atom p is image shift s = sidx[p] / nloc of atom a_beg + sidx[p] % nloc.
-__device__ int staged_search_atom(double* __restrict__ wr, int* __restrict__ wi, int* __restrict__ wt,
-                                  const float* __restrict__ sx, const float* __restrict__ sy,
-                                  const float* __restrict__ sz, const int* __restrict__ sidx,
-                                  const int* __restrict__ stype, int total, int self, float xf, float yf, float zf,
-                                  float rcf2, const double* __restrict__ coord, const double* __restrict__ svec,
-                                  int nloc, int a_beg, double xi, double yi, double zi, double rcut, int lane) {
-  const unsigned below = (1u << lane) - 1u;
-  int nc = 0;
-  for (int p0 = 0; p0 < total; p0 += 32) {
-    const int p = p0 + lane;
-    bool cand = false;
-    if (p < total && stype[p] >= 0 && sidx[p] != self) {
-      const float fx = sx[p] - xf, fy = sy[p] - yf, fz = sz[p] - zf;
-      cand = fx * fx + fy * fy + fz * fz <= rcf2;
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, cand);
-    const int pos = nc + __popc(m & below);
-    if (cand && pos < kKeptCap) wi[pos] = p;
-    nc += __popc(m);
-  }
-  if (nc > kKeptCap) return -nc - 1;
-  __syncwarp();
-  int n = 0;
-  for (int k0 = 0; k0 < nc; k0 += 32) {
-    const int k = k0 + lane;
-    bool keep = false;
-    double r = 0.0;
-    int e = 0, t = 0;
-    if (k < nc) {
-      const int p = wi[k];
-      e = sidx[p];
-      t = stype[p];
-      const int s = e / nloc, j = a_beg + (e - s * nloc);
-      const double dx = (coord[3 * j] + svec[3 * s]) - xi;
-      const double dy = (coord[3 * j + 1] + svec[3 * s + 1]) - yi;
-      const double dz = (coord[3 * j + 2] + svec[3 * s + 2]) - zi;
-      r = dist_fma(dx, dy, dz);
-      keep = r <= rcut;
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    __syncwarp();  // every lane has read its slot before any is overwritten
-    const int pos = n + __popc(m & below);  // pos <= k: never a slot still to be read
-    if (keep) {
-      wr[pos] = r;
-      wi[pos] = e;
-      wt[pos] = t;
-    }
-    n += __popc(m);
-  }
-  __syncwarp();
-  return n;
-}
-
-// Rank a warp's kept list by (distance, extended index) and place each pair
-// in its type section while its per-type rank < sel[t] and its global rank
-// < nnei (topk of sum(sel), then the per-type split).  Each lane holds up to
-// four kept entries in registers and streams the list once per 128.
+// Rank a warp's kept list by exact FP64 distance, then extended index, and
+// place it.  Each lane holds up to four kept entries in registers and
+// streams the list once per 128.
 __device__ void staged_rank_place(int* __restrict__ row, const double* __restrict__ wr, const int* __restrict__ wi,
-                                  const int* __restrict__ wt, int n, const SelInfo& sel, int lane) {
+                                  const int* __restrict__ wt, int n, const SelInfo& sel, int lane,
+                                  int* __restrict__ status) {
   for (int k0 = 0; k0 < n; k0 += 128) {
     long long rk[4];
     int ik[4], tk[4], rank[4], trank[4];
@@ -456,29 +424,313 @@ __device__ void staged_rank_place(int* __restrict__ row, const double* __restric
       }
     }
 #pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (k0 + lane + 32 * q < n) place_pair(row, rank[q], trank[q], tk[q], ik[q], sel, status);
+  }
+}
+
+// The same ranking on FP32 distances wf that lie within eps of the exact
+// FP64 ones.  Two keys closer than tie = 2 eps (or equal) may order
+// differently in FP64: then nothing of that group is placed and it returns
+// true (the caller redoes the atom in FP64 and clears the row first).
+__device__ bool rank_place_f32(int* __restrict__ row, const float* __restrict__ wf, const int* __restrict__ wi,
+                               const int* __restrict__ wt, int n, float tie, const SelInfo& sel, int lane,
+                               int* __restrict__ status) {
+  for (int k0 = 0; k0 < n; k0 += 128) {
+    float rk[4];
+    int ik[4], tk[4], rank[4], trank[4];
+    bool near = false;
+#pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const int t = tk[q];
-      if (k0 + lane + 32 * q < n && rank[q] < sel.nnei && t < sel.ntypes && trank[q] < sel.sel[t])
-        row[sel.sec[t] + trank[q]] = ik[q];
+      const int k = k0 + lane + 32 * q;
+      rk[q] = k < n ? wf[k] : __int_as_float(0x7f800000);
+      ik[q] = k < n ? wi[k] : 0x7fffffff;
+      tk[q] = k < n ? wt[k] : -1;
+      rank[q] = trank[q] = 0;
+    }
+    for (int m2 = 0; m2 < n; ++m2) {
+      const float rm = wf[m2];
+      const int im = wi[m2], tm = wt[m2];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool lt = rm < rk[q] || (rm == rk[q] && im < ik[q]);
+        rank[q] += lt;
+        trank[q] += lt && tm == tk[q];
+        near |= im != ik[q] && fabsf(rm - rk[q]) <= tie;
+      }
+    }
+    if (__any_sync(0xffffffffu, near)) return true;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (k0 + lane + 32 * q < n) place_pair(row, rank[q], trank[q], tk[q], ik[q], sel, status);
+  }
+  return false;
+}
+
+__device__ __forceinline__ bool key_less(float ka, int ea, float kb, int eb) {
+  return ka < kb || (ka == kb && ea < eb);
+}
+
+// Warp-wide bitonic sort of 128 (key, index, type) triples, element
+// 32 q + lane in register q of each lane, ascending by (key, index).
+// Partners closer than 32 are exchanged by shuffles, those 32 or 64 apart
+// sit in the same lane's registers.
+__device__ __forceinline__ void warp_sort128(float k[4], int e[4], int t[4], int lane) {
+#pragma unroll
+  for (int size = 2; size <= 128; size <<= 1) {
+#pragma unroll
+    for (int j = size >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+        const int qj = j >> 5;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int p = q ^ qj;
+          if (p > q) {
+            const bool up = ((q * 32 + lane) & size) == 0;
+            const bool sw = up ? key_less(k[p], e[p], k[q], e[q]) : key_less(k[q], e[q], k[p], e[p]);
+            if (sw) {
+              const float tk = k[q];
+              const int te = e[q], tt = t[q];
+              k[q] = k[p];
+              e[q] = e[p];
+              t[q] = t[p];
+              k[p] = tk;
+              e[p] = te;
+              t[p] = tt;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float ok = __shfl_xor_sync(0xffffffffu, k[q], j);
+          const int oe = __shfl_xor_sync(0xffffffffu, e[q], j);
+          const int ot = __shfl_xor_sync(0xffffffffu, t[q], j);
+          const int idx = q * 32 + lane;
+          const bool up = (idx & size) == 0, lower = (idx & j) == 0;
+          const bool o_less = key_less(ok, oe, k[q], e[q]);
+          if (lower == up ? o_less : !o_less) {
+            k[q] = ok;
+            e[q] = oe;
+            t[q] = ot;
+          }
+        }
+      }
     }
   }
+}
+
+// Placement of up to 128 kept pairs with FP32 keys wf (within eps of the
+// exact distances) through a warp sort: the sorted position is the global
+// rank, same-type lanes of each 32-chunk (match_any) plus the running count
+// of their type (s_base, per warp) give the rank within the type.  Two
+// neighbours in the sorted order closer than tie = 2 eps (or equal) may
+// order differently in FP64: then nothing is placed and it returns true.
+__device__ bool sort_place_f32(int* __restrict__ row, const float* __restrict__ wf, const int* __restrict__ wi,
+                               const int* __restrict__ wt, int n, float tie, const SelInfo& sel, int lane,
+                               int* __restrict__ status, int* __restrict__ s_base) {
+  float k[4];
+  int e[4], t[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int idx = q * 32 + lane;
+    k[q] = idx < n ? wf[idx] : __int_as_float(0x7f800000);
+    e[q] = idx < n ? wi[idx] : 0x7fffffff;
+    t[q] = idx < n ? wt[idx] : -1;
+  }
+  warp_sort128(k, e, t, lane);
+  bool near = false;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float next = __shfl_down_sync(0xffffffffu, k[q], 1);
+    const float first_next = __shfl_sync(0xffffffffu, k[q < 3 ? q + 1 : q], 0);
+    if (lane == 31) next = first_next;
+    const int idx = q * 32 + lane;
+    near |= idx + 1 < n && next - k[q] <= tie;
+  }
+  if (__any_sync(0xffffffffu, near)) return true;
+  if (lane < sel.ntypes) s_base[lane] = 0;
+  __syncwarp();
+  const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int tq = t[q];
+    const unsigned m = __match_any_sync(0xffffffffu, tq);
+    const int tr = (tq >= 0 ? s_base[tq] : 0) + __popc(m & below);
+    __syncwarp();
+    if (tq >= 0 && lane == __ffs(m) - 1) s_base[tq] += __popc(m);
+    __syncwarp();
+    const int idx = q * 32 + lane;
+    if (idx < n) place_pair(row, idx, tr, tq, e[q], sel, status);
+  }
+  return false;
+}
+
+// Exact FP64 distances of a warp's packed candidates (extended indices wi,
+// e = s * nloc + j, types wt; atom j is a_beg + j): those with r <= rcut are
+// packed again, in place, as (wr, wi, wt).  The FP64 pipe is narrow on this
+// part, so it runs only on full warps of packed candidates.
+__device__ int exact_keep(double* __restrict__ wr, int* __restrict__ wi, int* __restrict__ wt, int nc,
+                          const double* __restrict__ coord, const double* __restrict__ svec, int nloc, int a_beg,
+                          double xi, double yi, double zi, double rcut, int lane) {
+  const unsigned below = (1u << lane) - 1u;
+  int n = 0;
+  for (int k0 = 0; k0 < nc; k0 += 32) {
+    const int k = k0 + lane;
+    bool keep = false;
+    double r = 0.0;
+    int e = 0, t = 0;
+    if (k < nc) {
+      e = wi[k];
+      t = wt[k];
+      const int s = e / nloc, j = a_beg + (e - s * nloc);
+      const double dx = (coord[3 * j] + svec[3 * s]) - xi;
+      const double dy = (coord[3 * j + 1] + svec[3 * s + 1]) - yi;
+      const double dz = (coord[3 * j + 2] + svec[3 * s + 2]) - zi;
+      r = dist_fma(dx, dy, dz);
+      keep = r <= rcut;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    __syncwarp();  // every lane has read its slot before any is overwritten
+    const int pos = n + __popc(m & below);  // pos <= k: never a slot still to be read
+    if (keep) {
+      wr[pos] = r;
+      wi[pos] = e;
+      wt[pos] = t;
+    }
+    n += __popc(m);
+  }
+  __syncwarp();
+  return n;
+}
+
+// Error bound of the staged FP32 distances: a stencil atom lies within
+// (reach_k + 1/2) cell edges of the centre cell's centre along each cell
+// vector k, so its coordinates relative to that centre are below
+// m = sum_k (reach_k + 1/2) |a_k| / n_k; each is rounded to FP32 (<= 2^-24 m,
+// doubled for margin: u); a displacement component then errs by
+// <= 2 u + 2^-24 R and the FP32 norm adds <= 2^-22 R (R: the list radius).
+__device__ __forceinline__ float staged_eps(const CellGeom& g, double R) {
+  double m = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    const double edge = g.periodic ? sqrt(g.cell[3 * k] * g.cell[3 * k] + g.cell[3 * k + 1] * g.cell[3 * k + 1] +
+                                          g.cell[3 * k + 2] * g.cell[3 * k + 2]) / g.ncell[k]
+                                   : g.csize[k];
+    m += (g.reach[k] + 0.5) * edge;
+  }
+  const double u = m * 0x1p-23;
+  return (float)(1.7320508075688772 * (2.0 * u + R * 0x1p-24) + R * 0x1p-22 + 1e-7);
+}
+
+// centre of cell (cx, cy, cz)
+__device__ __forceinline__ void cell_centre(const CellGeom& g, int cx, int cy, int cz, double o[3]) {
+  if (g.periodic) {
+    const double f0 = (cx + 0.5) / g.ncell[0], f1 = (cy + 0.5) / g.ncell[1], f2 = (cz + 0.5) / g.ncell[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) o[k] = f0 * g.cell[k] + f1 * g.cell[3 + k] + f2 * g.cell[6 + k];
+  } else {
+    o[0] = g.origin[0] + (cx + 0.5) * g.csize[0];
+    o[1] = g.origin[1] + (cy + 0.5) * g.csize[1];
+    o[2] = g.origin[2] + (cz + 0.5) * g.csize[2];
+  }
+}
+
+// One centre atom against the staged stencil atoms (FP32 coordinates
+// relative to the cell centre), one warp, writing its row:
+// * flat candidate rows (sel.flat): every staged atom within rcut + eps, in
+//   staging order, no distances beyond FP32;
+// * typed lists: FP32 distances within eps of the exact ones decide the
+//   cutoff and the order; an atom with a distance within eps of rcut or two
+//   within 2 eps of each other is redone in exact FP64 — so the list is
+//   always that of the exact (distance, extended index) ranking.
+// Returns 0, or -(candidates) - 1 when more than kept_cap candidates (typed
+// lists; the row is then incomplete).
+__device__ int staged_list_atom(int* __restrict__ row, double* __restrict__ wr, int* __restrict__ wi,
+                                int* __restrict__ wt, const float* __restrict__ sx, const float* __restrict__ sy,
+                                const float* __restrict__ sz, const int* __restrict__ sidx,
+                                const int* __restrict__ stype, int total, int self, float xf, float yf, float zf,
+                                float eps, const double* __restrict__ coord, const double* __restrict__ svec,
+                                int nloc, int a_beg, double xi, double yi, double zi, double rcut, const SelInfo& sel,
+                                int lane, int* __restrict__ status, int* __restrict__ s_base, int kept_cap) {
+  const unsigned below = (1u << lane) - 1u;
+  const float rin = (float)rcut - eps, rout = (float)rcut + eps;
+  const float rout2 = rout * rout;
+  if (sel.flat) {
+    int nc = 0;
+    for (int p0 = 0; p0 < total; p0 += 32) {
+      const int p = p0 + lane;
+      bool cand = false;
+      if (p < total && stype[p] >= 0 && sidx[p] != self) {
+        const float fx = sx[p] - xf, fy = sy[p] - yf, fz = sz[p] - zf;
+        cand = fx * fx + fy * fy + fz * fz <= rout2;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, cand);
+      const int pos = nc + __popc(m & below);
+      if (cand && pos < sel.nnei) row[pos] = sidx[p];
+      nc += __popc(m);
+    }
+    if (nc > sel.nnei && sel.strict && lane == 0) atomicMax(&status[kStatusTruncated], nc);
+    return 0;
+  }
+  float* wf = reinterpret_cast<float*>(wr);  // FP32 keys (first half of the FP64 key buffer)
+  int nc = 0;
+  bool band = false;
+  for (int p0 = 0; p0 < total; p0 += 32) {
+    const int p = p0 + lane;
+    bool cand = false;
+    float r = 0.f;
+    if (p < total && stype[p] >= 0 && sidx[p] != self) {
+      const float fx = sx[p] - xf, fy = sy[p] - yf, fz = sz[p] - zf;
+      const float d2 = fx * fx + fy * fy + fz * fz;
+      if (d2 <= rout2) {
+        cand = true;
+        r = sqrtf(d2);
+        band |= r > rin;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, cand);
+    const int pos = nc + __popc(m & below);
+    if (cand && pos < kept_cap) {
+      wf[pos] = r;
+      wi[pos] = sidx[p];
+      wt[pos] = stype[p];
+    }
+    nc += __popc(m);
+  }
+  if (nc > kept_cap) return -nc - 1;
+  band = __any_sync(0xffffffffu, band);
+  __syncwarp();
+  if (!band && !(nc <= 128 ? sort_place_f32(row, wf, wi, wt, nc, 2.f * eps, sel, lane, status, s_base)
+                            : rank_place_f32(row, wf, wi, wt, nc, 2.f * eps, sel, lane, status)))
+    return 0;
+  // exact FP64: clear what the FP32 pass may have placed, then rank exactly
+  if (lane == 0) atomicAdd(&status[kStatusExact], 1);
+  __syncwarp();
+  for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
+  __syncwarp();
+  const int n = exact_keep(wr, wi, wt, nc, coord, svec, nloc, a_beg, xi, yi, zi, rcut, lane);
+  staged_rank_place(row, wr, wi, wt, n, sel, lane, status);
+  return 0;
 }
 
 __global__ void __launch_bounds__(kCellWarps * 32)
 nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, const int* __restrict__ atype,
                   const int* __restrict__ offsets, const int* __restrict__ cell_atoms,
                   const int* __restrict__ shift_pos, const double* __restrict__ svec, int nloc, CellGeom g,
-                  double rcut, SelInfo sel, int* __restrict__ fallback, int* __restrict__ status) {
+                  double rcut, SelInfo sel, int* __restrict__ fallback, int* __restrict__ status,
+                  const int* __restrict__ gate, int stage_cap, int kept_cap) {
+  if (gate && !gate[0]) return;
   extern __shared__ __align__(16) unsigned char smem[];
   double* kr = reinterpret_cast<double*>(smem);
-  float* sx = reinterpret_cast<float*>(kr + kCellWarps * kKeptCap);
-  float* sy = sx + kStageCap;
-  float* sz = sy + kStageCap;
-  int* sidx = reinterpret_cast<int*>(sz + kStageCap);
-  int* stype = sidx + kStageCap;
-  int* kidx = stype + kStageCap;
-  int* ktype = kidx + kCellWarps * kKeptCap;
+  float* sx = reinterpret_cast<float*>(kr + kCellWarps * kept_cap);
+  float* sy = sx + stage_cap;
+  float* sz = sy + stage_cap;
+  int* sidx = reinterpret_cast<int*>(sz + stage_cap);
+  int* stype = sidx + stage_cap;
+  int* kidx = stype + stage_cap;
+  int* ktype = kidx + kCellWarps * kept_cap;
   __shared__ int s_cell[27], s_shift[27], s_off[28];
+  __shared__ int s_tb[kCellWarps][DPGB_MAX_TYPES];  // per-type running counts of sort_place_f32
   const int c = blockIdx.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int cz = c % g.ncell[2], cy = (c / g.ncell[2]) % g.ncell[1], cx = c / (g.ncell[1] * g.ncell[2]);
@@ -500,15 +752,16 @@ nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
   }
   __syncthreads();
   const int total = s_off[27];
-  if (total > kStageCap) {  // left to nlist_pt_kernel
+  if (total > stage_cap) {  // left to nlist_pt_kernel
     if (tid == 0) fallback[c] = 1;
     return;
   }
-  // FP32 copies relative to a point of the centre cell (its first atom):
-  // |offsets| < ~3 cell widths, so their rounding error is ~1e-6 A — only a
-  // prefilter; kept pairs get their exact FP64 distance below
-  const int a0 = offsets[c] < offsets[c + 1] ? cell_atoms[offsets[c]] : 0;
-  const double ox = coord[3 * a0], oy = coord[3 * a0 + 1], oz = coord[3 * a0 + 2];
+  // FP32 copies relative to the centre cell's centre (magnitudes within 1.5
+  // cell diagonals: the rounding bound of staged_eps)
+  double oc[3];
+  cell_centre(g, cx, cy, cz, oc);
+  const double ox = oc[0], oy = oc[1], oz = oc[2];
+  const float eps = staged_eps(g, rcut);
   for (int q = tid; q < total; q += blockDim.x) {
     int k = 0;
     while (s_off[k + 1] <= q) ++k;
@@ -521,27 +774,21 @@ nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
     stype[q] = atype[j];
   }
   __syncthreads();
-  const float rcf = (float)rcut + 1e-3f;  // prefilter radius: well above the FP32 error
-  const float rcf2 = rcf * rcf;
-  double* wr = kr + warp * kKeptCap;
-  int* wi = kidx + warp * kKeptCap;
-  int* wt = ktype + warp * kKeptCap;
+  double* wr = kr + warp * kept_cap;
+  int* wi = kidx + warp * kept_cap;
+  int* wt = ktype + warp * kept_cap;
   for (int a = offsets[c] + warp; a < offsets[c + 1]; a += kCellWarps) {
     const int i = cell_atoms[a];
     int* row = nlist + (size_t)i * sel.nnei;
     for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
+    __syncwarp();
     if (atype[i] < 0) continue;
     const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
     const int self = g.zero_shift * nloc + i;
     const float xf = (float)(xi - ox), yf = (float)(yi - oy), zf = (float)(zi - oz);
-    const int n = staged_search_atom(wr, wi, wt, sx, sy, sz, sidx, stype, total, self, xf, yf, zf, rcf2, coord, svec,
-                                     nloc, 0, xi, yi, zi, rcut, lane);
-    if (n < 0) {  // more than kKeptCap candidates: the whole cell goes to the per-atom kernel
-      if (lane == 0) fallback[c] = 1;
-      __syncwarp();
-      continue;
-    }
-    staged_rank_place(row, wr, wi, wt, n, sel, lane);
+    const int r = staged_list_atom(row, wr, wi, wt, sx, sy, sz, sidx, stype, total, self, xf, yf, zf, eps, coord,
+                                   svec, nloc, 0, xi, yi, zi, rcut, sel, lane, status, s_tb[warp], kept_cap);
+    if (r < 0 && lane == 0) fallback[c] = 1;  // more than kept_cap candidates: the cell goes to the per-atom kernel
     __syncwarp();
   }
 }
@@ -625,9 +872,10 @@ format_nlist_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
 // exclusive scan out[0..n] of in[0..n) (out[n] = total) by one CTA of 1024
 // threads, in tiles of 4096 consecutive elements (4 per thread): coalesced
 // loads, warp-shuffle scans, a running carry between tiles
-__global__ void scan_kernel(int* __restrict__ out, const int* __restrict__ in, int n) {
+__global__ void scan_kernel(int* __restrict__ out, const int* __restrict__ in, int n, const int* __restrict__ gate) {
   __shared__ int s_warp[32];
   __shared__ int s_carry;
+  if (gate && !gate[0]) return;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   if (t == 0) s_carry = 0;
   __syncthreads();
@@ -829,13 +1077,15 @@ __global__ void normalize_batch_kernel(double* __restrict__ out, int* __restrict
 
 constexpr int kBatchStageCap = 4096;
 
+constexpr int kBatchKeptCap = 384;
+
 size_t batch_stage_smem() {
   return (size_t)kBatchStageCap * (3 * sizeof(float) + 2 * sizeof(int)) +
-         (size_t)kCellWarps * kKeptCap * (sizeof(double) + 2 * sizeof(int));
+         (size_t)kCellWarps * kBatchKeptCap * (sizeof(double) + 2 * sizeof(int));
 }
 
 // nlist_cell_kernel over the cells of all frames; a cell whose stencil holds
-// more than kBatchStageCap atoms, or an atom with more than kKeptCap
+// more than kBatchStageCap atoms, or an atom with more than kBatchKeptCap
 // neighbours, is reported as an overflow
 __global__ void __launch_bounds__(kCellWarps * 32)
 nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coord, const int* __restrict__ atype,
@@ -844,16 +1094,17 @@ nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coor
                         double rcut, SelInfo sel, int* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem[];
   double* kr = reinterpret_cast<double*>(smem);
-  float* sx = reinterpret_cast<float*>(kr + kCellWarps * kKeptCap);
+  float* sx = reinterpret_cast<float*>(kr + kCellWarps * kBatchKeptCap);
   float* sy = sx + kBatchStageCap;
   float* sz = sy + kBatchStageCap;
   int* sidx = reinterpret_cast<int*>(sz + kBatchStageCap);
   int* stype = sidx + kBatchStageCap;
   int* kidx = stype + kBatchStageCap;
-  int* ktype = kidx + kCellWarps * kKeptCap;
+  int* ktype = kidx + kCellWarps * kBatchKeptCap;
   // stencil of (2 reach + 1)^3 cells, reach <= 2 per direction (a frame
   // thinner than rcut across a face has one cell and reach 2 there)
   __shared__ int s_cell[125], s_shift[125], s_off[126];
+  __shared__ int s_tb[kCellWarps][DPGB_MAX_TYPES];
   const int cg = blockIdx.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int fr = frame_of(ft.cell_off, ft.nframes, cg);
@@ -891,8 +1142,10 @@ nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coor
     }
     return;
   }
-  const int a0 = cell_atoms[offsets[cg]];
-  const double ox = coord[3 * a0], oy = coord[3 * a0 + 1], oz = coord[3 * a0 + 2];
+  double oc[3];
+  cell_centre(g, cx, cy, cz, oc);
+  const double ox = oc[0], oy = oc[1], oz = oc[2];
+  const float eps = staged_eps(g, rcut);
   for (int q = tid; q < total; q += blockDim.x) {
     int lo = 0, hi = nst;  // s_off[lo] <= q < s_off[hi]
     while (hi - lo > 1) {
@@ -909,31 +1162,178 @@ nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coor
     stype[q] = atype[j];
   }
   __syncthreads();
-  const float rcf = (float)rcut + 1e-3f;
-  const float rcf2 = rcf * rcf;
-  double* wr = kr + warp * kKeptCap;
-  int* wi = kidx + warp * kKeptCap;
-  int* wt = ktype + warp * kKeptCap;
+  double* wr = kr + warp * kBatchKeptCap;
+  int* wi = kidx + warp * kBatchKeptCap;
+  int* wt = ktype + warp * kBatchKeptCap;
   for (int a = offsets[cg] + warp; a < offsets[cg + 1]; a += kCellWarps) {
     const int i = cell_atoms[a];  // global atom
     int* row = nlist + (size_t)i * sel.nnei;
     for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
+    __syncwarp();
     if (atype[i] < 0) continue;
     const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
     const int self = g.zero_shift * nloc + (i - a_beg);
     const float xf = (float)(xi - ox), yf = (float)(yi - oy), zf = (float)(zi - oz);
-    const int n = staged_search_atom(wr, wi, wt, sx, sy, sz, sidx, stype, total, self, xf, yf, zf, rcf2, coord, svec,
-                                     nloc, a_beg, xi, yi, zi, rcut, lane);
-    if (n < 0) {
-      if (lane == 0) {
-        atomicMax(&status[kStatusOverflow], -n - 1);
-        atomicMax(&status[kStatusOverflowAtom], i + 1);
-      }
-      __syncwarp();
-      continue;
+    const int r = staged_list_atom(row, wr, wi, wt, sx, sy, sz, sidx, stype, total, self, xf, yf, zf, eps, coord,
+                                   svec, nloc, a_beg, xi, yi, zi, rcut, sel, lane, status, s_tb[warp], kBatchKeptCap);
+    if (r < 0 && lane == 0) {
+      atomicMax(&status[kStatusOverflow], -r - 1);
+      atomicMax(&status[kStatusOverflowAtom], i + 1);
     }
-    staged_rank_place(row, wr, wi, wt, n, sel, lane);
     __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Skin lists: the list of an MD step reused over the next ones, as a Verlet
+// list with a skin (LAMMPS neigh_modify every / check; the `ago` argument of
+// DeepPot::compute, source/api_cc/src/DeepPotPT.cc:170-243).  Candidates of
+// everything within rcut + skin are built on wrapped coordinates; until the
+// next build the coordinates are not re-wrapped (the build's wrap offsets are
+// kept), so every candidate's image shift stays the right one, and each
+// evaluation selects its list at rcut from the candidates.
+
+// gate[0] = 1 when no list exists yet, the list is `every` evaluations old,
+// or an atom has moved more than skin / 2 since the build (beyond that a pair
+// within rcut may be missing from the candidates)
+__global__ void skin_check_kernel(int* __restrict__ gate, const double* __restrict__ coord,
+                                  const double* __restrict__ ref, int n, double half2, int every) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && (gate[1] < 0 || gate[1] >= every)) gate[0] = 1;
+  if (i >= n) return;
+  const double dx = coord[3 * i] - ref[3 * i], dy = coord[3 * i + 1] - ref[3 * i + 1],
+               dz = coord[3 * i + 2] - ref[3 * i + 2];
+  if (!(dx * dx + dy * dy + dz * dz <= half2)) gate[0] = 1;
+}
+
+// build evaluation: wrap, keep the wrap offset and the reference position;
+// reuse evaluation: the caller's coordinates plus the build's wrap offset
+__global__ void skin_coords_kernel(double* __restrict__ out, float4* __restrict__ outf, double* __restrict__ off,
+                                   double* __restrict__ ref, const double* __restrict__ in, int n, CellGeom g,
+                                   const int* __restrict__ gate) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double o[3];
+  if (gate[0]) {
+    wrap_point(in + 3 * i, g, o);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      off[3 * i + k] = o[k] - in[3 * i + k];
+      ref[3 * i + k] = in[3 * i + k];
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) o[k] = in[3 * i + k] + off[3 * i + k];
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) out[3 * i + k] = o[k];
+  outf[i] = make_float4((float)o[0], (float)o[1], (float)o[2], 0.f);
+}
+
+// One warp per centre atom: FP32 prefilter over the candidate row (absolute
+// FP32 coordinates; the margin covers their rounding), then for the packed
+// survivors the FP64 displacement (r_j + shift) - r_i rounded to FP32 and an
+// FP32 distance within eps of the exact one.  Those decide the cutoff and the
+// order unless a distance lies within eps of rcut or two within 2 eps of
+// each other: then the atom is redone with exact FP64 distances.  The list
+// is that of a fresh build on the same coordinates.
+constexpr int kSkinWarps = 4;
+
+__global__ void __launch_bounds__(kSkinWarps * 32)
+skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int ncand, const double* __restrict__ coord,
+                   const float4* __restrict__ coordf, const int* __restrict__ atype, const double* __restrict__ svec,
+                   const float4* __restrict__ svecf, int nloc, double rcut, float rcf2, float eps, SelInfo sel,
+                   int* __restrict__ status) {
+  __shared__ double s_r[kSkinWarps][kKeptCap];
+  __shared__ int s_i[kSkinWarps][kKeptCap];
+  __shared__ int s_t[kSkinWarps][kKeptCap];
+  __shared__ int s_tb[kSkinWarps][DPGB_MAX_TYPES];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kSkinWarps + warp;
+  if (i >= nloc) return;
+  int* row = nlist + (size_t)i * sel.nnei;
+  for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
+  __syncwarp();
+  if (atype[i] < 0) return;
+  const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
+  const float4 fi = coordf[i];
+  const int* c = cand + (size_t)i * ncand;
+  double* wr = s_r[warp];
+  float* wf = reinterpret_cast<float*>(wr);
+  int* wi = s_i[warp];
+  int* wt = s_t[warp];
+  const unsigned below = (1u << lane) - 1u;
+  int nc = 0;
+  for (int p0 = 0; p0 < ncand; p0 += 32) {
+    const int p = p0 + lane;
+    const int e = p < ncand ? c[p] : -1;
+    if (__all_sync(0xffffffffu, e < 0)) break;  // candidate rows are packed: padding from here on
+    bool keep = false;
+    if (e >= 0) {
+      const int s = e / nloc, j = e - s * nloc;
+      const float4 fj = coordf[j], sv = svecf[s];
+      const float fx = (fj.x + sv.x) - fi.x, fy = (fj.y + sv.y) - fi.y, fz = (fj.z + sv.z) - fi.z;
+      keep = fx * fx + fy * fy + fz * fz <= rcf2;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const int pos = nc + __popc(m & below);
+    if (keep && pos < kKeptCap) wi[pos] = e;
+    nc += __popc(m);
+  }
+  if (nc > kKeptCap) {
+    if (lane == 0) {
+      atomicMax(&status[kStatusOverflow], nc);
+      atomicMax(&status[kStatusOverflowAtom], i + 1);
+    }
+    return;
+  }
+  __syncwarp();
+  const float rin = (float)rcut - eps, rout = (float)rcut + eps;
+  int n = 0;
+  bool band = false;
+  for (int k0 = 0; k0 < nc; k0 += 32) {
+    const int k = k0 + lane;
+    bool keep = false;
+    float r = 0.f;
+    int e = 0, t = 0;
+    if (k < nc) {
+      e = wi[k];
+      const int s = e / nloc, j = e - s * nloc;
+      t = atype[j];
+      const float fx = (float)((coord[3 * j] + svec[3 * s]) - xi);
+      const float fy = (float)((coord[3 * j + 1] + svec[3 * s + 1]) - yi);
+      const float fz = (float)((coord[3 * j + 2] + svec[3 * s + 2]) - zi);
+      r = sqrtf(fx * fx + fy * fy + fz * fz);
+      keep = r <= rout;
+      band |= keep && r > rin;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    __syncwarp();  // every lane has read its slot before any is overwritten
+    const int pos = n + __popc(m & below);
+    if (keep) {
+      wf[pos] = r;
+      wi[pos] = e;
+      wt[pos] = t;
+    }
+    n += __popc(m);
+  }
+  band = __any_sync(0xffffffffu, band);
+  __syncwarp();
+  if (!band && !(n <= 128 ? sort_place_f32(row, wf, wi, wt, n, 2.f * eps, sel, lane, status, s_tb[warp])
+                           : rank_place_f32(row, wf, wi, wt, n, 2.f * eps, sel, lane, status)))
+    return;
+  if (lane == 0) atomicAdd(&status[kStatusExact], 1);
+  __syncwarp();
+  for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
+  __syncwarp();
+  const int n2 = exact_keep(wr, wi, wt, n, coord, svec, nloc, 0, xi, yi, zi, rcut, lane);
+  staged_rank_place(row, wr, wi, wt, n2, sel, lane, status);
+}
+
+__global__ void skin_advance_kernel(int* __restrict__ gate) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    gate[1] = gate[0] ? 1 : gate[1] + 1;
+    gate[0] = 0;
   }
 }
 
@@ -956,9 +1356,9 @@ int launch_nlist_batch(int* nlist, double* coord_out, const double* coord_in, co
   DPGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * (ncells + 1), st));
   normalize_batch_kernel<<<ceil_div(natoms, 256), 256, 0, st>>>(coord_out, cell_of, counts, coord_in, natoms, ft);
   DPGB_TRY(check_launch("normalize_batch"));
-  scan_kernel<<<1, 1024, 0, st>>>(offsets, counts, ncells);
+  scan_kernel<<<1, 1024, 0, st>>>(offsets, counts, ncells, nullptr);
   DPGB_TRY(check_launch("cell_scan_batch"));
-  cell_fill_kernel<<<ceil_div(natoms, 256), 256, 0, st>>>(cell_atoms, cursor, offsets, cell_of, natoms);
+  cell_fill_kernel<<<ceil_div(natoms, 256), 256, 0, st>>>(cell_atoms, cursor, offsets, cell_of, natoms, nullptr);
   DPGB_TRY(check_launch("cell_fill_batch"));
   const size_t smem = batch_stage_smem();
   DPGB_CUDA(cudaFuncSetAttribute(nlist_cell_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -982,6 +1382,37 @@ int launch_normalize(double* out, const double* in, int n, const CellGeom& g, cu
   return check_launch("normalize_coord");
 }
 
+int launch_skin_check(int* gate, const double* coord, const double* ref, int n, double skin, int every,
+                      cudaStream_t st) {
+  const double half = 0.5 * skin;
+  skin_check_kernel<<<ceil_div(std::max(n, 1), 256), 256, 0, st>>>(gate, coord, ref, n, half * half, every);
+  return check_launch("skin_check");
+}
+
+int launch_skin_coords(double* out, float4* outf, double* off, double* ref, const double* in, int n,
+                       const CellGeom& g, const int* gate, cudaStream_t st) {
+  if (n <= 0) return DPGB_OK;
+  skin_coords_kernel<<<ceil_div(n, 256), 256, 0, st>>>(out, outf, off, ref, in, n, g, gate);
+  return check_launch("skin_coords");
+}
+
+int launch_skin_select(int* nlist, const int* cand, int ncand, const double* coord, const float4* coordf,
+                       const int* atype, const double* svec, const float4* svecf, int nloc, double rcut,
+                       double margin, const SelInfo& sel, int* status, cudaStream_t st) {
+  if (nloc <= 0) return DPGB_OK;
+  const float rcf = (float)(rcut + margin);
+  // FP64 displacement rounded to FP32 (<= 2^-24 r) plus the FP32 norm (<= 2^-22 r), x1.5
+  const float eps = (float)(rcut * 1.5 * (0x1p-24 + 0x1p-22) + 1e-7);
+  skin_select_kernel<<<ceil_div(nloc, kSkinWarps), kSkinWarps * 32, 0, st>>>(
+      nlist, cand, ncand, coord, coordf, atype, svec, svecf, nloc, rcut, rcf * rcf, eps, sel, status);
+  return check_launch("skin_select");
+}
+
+int launch_skin_advance(int* gate, cudaStream_t st) {
+  skin_advance_kernel<<<1, 32, 0, st>>>(gate);
+  return check_launch("skin_advance");
+}
+
 int launch_extend(double* cext, int* text, int* mapping, const double* coord, const int* atype,
                   int nloc, int nshift, const double* svec_dev, cudaStream_t st) {
   const long long tot = (long long)nloc * nshift;
@@ -998,7 +1429,7 @@ size_t nlist_pt_workspace(int nloc, const CellGeom& g) {
 
 int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc, const CellGeom& g,
                     const int* shift_pos_dev, const double* svec_dev, double rcut,
-                    const SelInfo& sel, void* workspace, int* status, cudaStream_t st) {
+                    const SelInfo& sel, void* workspace, int* status, cudaStream_t st, const int* gate) {
   if (nloc <= 0) return DPGB_OK;
   const int ncell = g.ncell[0] * g.ncell[1] * g.ncell[2];
   int* cell_of = reinterpret_cast<int*>(workspace);
@@ -1009,25 +1440,27 @@ int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc,
   int* fallback = cursor + (ncell + 1);
   DPGB_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (ncell + 1), st));
   DPGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * 2 * (ncell + 1), st));  // cursor and fallback flags
-  cell_count_kernel<<<ceil_div(nloc, 256), 256, 0, st>>>(cell_of, counts, coord, nloc, g);
+  cell_count_kernel<<<ceil_div(nloc, 256), 256, 0, st>>>(cell_of, counts, coord, nloc, g, gate);
   DPGB_TRY(check_launch("cell_count"));
-  scan_kernel<<<1, 1024, 0, st>>>(offsets, counts, ncell);
+  scan_kernel<<<1, 1024, 0, st>>>(offsets, counts, ncell, gate);
   DPGB_TRY(check_launch("cell_scan"));
-  cell_fill_kernel<<<ceil_div(nloc, 256), 256, 0, st>>>(cell_atoms, cursor, offsets, cell_of, nloc);
+  cell_fill_kernel<<<ceil_div(nloc, 256), 256, 0, st>>>(cell_atoms, cursor, offsets, cell_of, nloc, gate);
   DPGB_TRY(check_launch("cell_fill"));
   // the staged kernel covers the 27-cell stencil; a wider stencil (a box
   // thinner than 2 rcut across a face) goes to the per-atom kernel whole
   const bool staged = g.reach[0] == 1 && g.reach[1] == 1 && g.reach[2] == 1;
   if (staged) {
-    const size_t smem = cell_stage_smem();
+    const int stage_cap = sel.flat ? kFlatStageCap : kTypedStageCap, kept_cap = sel.flat ? 0 : kTypedKeptCap;
+    const size_t smem = cell_stage_smem(stage_cap, kept_cap);
     DPGB_CUDA(cudaFuncSetAttribute(nlist_cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     nlist_cell_kernel<<<ncell, kCellWarps * 32, smem, st>>>(nlist, coord, atype, offsets, cell_atoms, shift_pos_dev,
-                                                            svec_dev, nloc, g, rcut, sel, fallback, status);
+                                                            svec_dev, nloc, g, rcut, sel, fallback, status, gate,
+                                                            stage_cap, kept_cap);
     DPGB_TRY(check_launch("nlist_cell"));
   }
   nlist_pt_kernel<<<ceil_div(nloc, kSearchWarps), kSearchWarps * 32, 0, st>>>(
       nlist, coord, atype, cell_of, offsets, cell_atoms, shift_pos_dev, svec_dev, nloc, g, rcut, sel,
-      staged ? fallback : nullptr, status);
+      staged ? fallback : nullptr, status, gate);
   return check_launch("nlist_pt");
 }
 
@@ -1059,7 +1492,7 @@ int launch_transpose(Transpose& tr, const int* keys, long long npair, int nkeys,
     tr_count_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(counts, keys, npair, nkeys);
     DPGB_TRY(check_launch("transpose_count"));
   }
-  scan_kernel<<<1, 1024, 0, st>>>(tr.offsets, counts, nkeys);
+  scan_kernel<<<1, 1024, 0, st>>>(tr.offsets, counts, nkeys, nullptr);
   DPGB_TRY(check_launch("transpose_scan"));
   if (npair > 0) {
     tr_fill_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(tr.pairs, cursor, tr.offsets, keys, npair,

@@ -8,7 +8,9 @@
 
 namespace dpgb {
 
-enum StatusExtra { kStatusDropped = 3 };
+// kStatusTruncated: widest type section a strict list (SelInfo::strict) lacked
+// kStatusExact: atoms whose list needed exact FP64 distances (FP32 ambiguous)
+enum StatusExtra { kStatusDropped = 3, kStatusTruncated = 4, kStatusExact = 5 };
 
 // Cell-list geometry of one frame (host-computed, passed by value).
 struct CellGeom {
@@ -29,6 +31,14 @@ struct SelInfo {
   int nnei;
   int sel[DPGB_MAX_TYPES];
   int sec[DPGB_MAX_TYPES + 1];
+  // 1: a pair within the cutoff that finds no slot (beyond sum(sel) or its
+  // type's sel) raises kStatusTruncated to its rank within its type + 1 (the
+  // width its type would need) — for candidate lists, which must hold every
+  // pair
+  int strict;
+  // 1: rows are flat candidate lists (every pair within the cutoff, at its
+  // rank over all types or in search order; no per-type sections)
+  int flat;
 };
 
 // Sorted transpose of a list: for key k, pairs[offsets[k] .. offsets[k+1])
@@ -54,7 +64,8 @@ int launch_extend(double* cext, int* text, int* mapping, const double* coord, co
 size_t nlist_pt_workspace(int nloc, const CellGeom& g);
 int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc, const CellGeom& g,
                     const int* shift_pos_dev, const double* svec_dev, double rcut,
-                    const SelInfo& sel, void* workspace, int* status, cudaStream_t st);
+                    const SelInfo& sel, void* workspace, int* status, cudaStream_t st,
+                    const int* gate = nullptr);
 int launch_format_nlist(int* nlist, const double* coord, const int* atype, const int* rows, int nall,
                         const int* counts, int max_nbor, int nloc, double rcut, const SelInfo& sel,
                         int* status, cudaStream_t st);
@@ -96,6 +107,29 @@ size_t transpose_workspace(long long npair, int nkeys);
 int launch_transpose(Transpose& tr, const int* keys, long long npair, int nkeys, int mod,
                      void* workspace, int* status, cudaStream_t st);
 int read_status(int* status_dev, cudaStream_t st, int out[kStatusSlots]);
+
+// Skin lists: a candidate list of every pair within rcut + skin, built on
+// wrapped coordinates, is reused over later evaluations; each evaluation
+// selects the list at rcut from it.  gate[0] = rebuild in this evaluation,
+// gate[1] = evaluations since the last build (-1: none).  The building
+// kernels (cell list, candidate search) skip their work when gate[0] == 0.
+// check: gate[0] = 1 when gate[1] is -1 or >= every, or an atom moved more
+// than skin / 2 from its position at the build (ref)
+int launch_skin_check(int* gate, const double* coord, const double* ref, int n, double skin, int every,
+                      cudaStream_t st);
+// build: out = wrapped coordinates, off = out - in, ref = in; reuse: out =
+// in + off; outf = FP32 copy of out (prefilter of the selection)
+int launch_skin_coords(double* out, float4* outf, double* off, double* ref, const double* in, int n,
+                       const CellGeom& g, const int* gate, cudaStream_t st);
+// the list at rcut from the candidate rows [nloc, ncand] (extended indices
+// s * nloc + j, -1 padding): the same ranking and per-type placement as a
+// fresh build on the same coordinates.  margin: FP32 prefilter radius above
+// rcut (covers the FP32 rounding of coordinates and shifts)
+int launch_skin_select(int* nlist, const int* cand, int ncand, const double* coord, const float4* coordf,
+                       const int* atype, const double* svec, const float4* svecf, int nloc, double rcut,
+                       double margin, const SelInfo& sel, int* status, cudaStream_t st);
+// gate[1] = gate[0] ? 1 : gate[1] + 1; gate[0] = 0
+int launch_skin_advance(int* gate, cudaStream_t st);
 int sel_from_host(const int* sel_host, int ntypes, SelInfo& s);
 
 }  // namespace dpgb

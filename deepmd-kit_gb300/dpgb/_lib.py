@@ -126,6 +126,8 @@ _SIGS = {
     "dpgb_batch_compute_device": [_P, _P, _P, _P, _P, _P, _I],
     "dpgb_batch_compute": [_P, _DP, _DP, _DP, _DP, _I],
     "dpgb_deeppot_last_launches": [_P],
+    "dpgb_deeppot_set_skin": [_P, _D, _I],
+    "dpgb_deeppot_check_status": [_P, _P],
     "dpgb_deeppot_set_profiling": [_P, _I],
     "dpgb_deeppot_collect_stages": [_P],
     "dpgb_deeppot_stage_times": [_P, _DP, _IP],

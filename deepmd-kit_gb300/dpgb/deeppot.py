@@ -110,6 +110,17 @@ class DeepPot:
     def last_launches(self) -> int:
         return int(_lib.lib().dpgb_deeppot_last_launches(self._h))
 
+    def set_skin(self, skin: float, every: int = 1) -> None:
+        """Reuse neighbour lists over calls on periodic frames: candidates
+        within rcut + skin, rebuilt every ``every`` calls or when an atom has
+        moved more than skin / 2 (``skin=0``: a fresh list each call)."""
+        _lib.check(_lib.lib().dpgb_deeppot_set_skin(self._h, float(skin), int(every)))
+
+    def check_status(self, stream=None) -> None:
+        """Synchronise and raise the device-side errors of the last
+        evaluation (the device form does not synchronise)."""
+        _lib.check(_lib.lib().dpgb_deeppot_check_status(self._h, None if stream is None else C.c_void_p(stream)))
+
     def set_profiling(self, on: bool) -> None:
         _lib.check(_lib.lib().dpgb_deeppot_set_profiling(self._h, int(on)))
 

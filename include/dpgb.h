@@ -442,6 +442,30 @@ int dpgb_deeppot_compute_device(dpgb_deeppot* dp, int nframes, int natom,
                                 double* atom_energy, double* atom_virial,
                                 void* stream);
 
+/* Neighbour-list reuse with a skin for periodic frames (both compute
+ * forms above), the device-side counterpart of an MD code's Verlet list
+ * (LAMMPS neigh_modify every/check yes) feeding DeepPot::compute's `ago`
+ * (source/api_cc/src/DeepPotPT.cc:170-243; c_api.h:310-322).  skin > 0:
+ * the candidates within rcut + skin are built on wrapped coordinates, and
+ * rebuilt when `every` calls have passed since the last build or an atom
+ * has moved more than skin / 2 since then (decided on the device; a new
+ * box, atom count or type vector also rebuilds).  Between builds the
+ * coordinates keep the build's wrap offsets and each call selects its list
+ * at rcut from the candidates, in the order and with the truncation of a
+ * fresh list.  skin = 0 (the default): a fresh list every call.  A
+ * candidate row too narrow for the pairs within rcut + skin is an error of
+ * that call (dpgb_deeppot_compute then widens the rows and repeats it
+ * once; after dpgb_deeppot_compute_device, dpgb_deeppot_check_status
+ * reports it and the next call widens and rebuilds). */
+int dpgb_deeppot_set_skin(dpgb_deeppot* dp, double skin, int every);
+
+/* Waits for `stream` (NULL: the handle's stream) and reports the
+ * device-side errors of the last evaluation: neighbour overflow, skin
+ * candidate truncation, a timed-out tensor-core wait.  The device form
+ * (dpgb_deeppot_compute_device) does not synchronise, so its caller reads
+ * these here. */
+int dpgb_deeppot_check_status(dpgb_deeppot* dp, void* stream);
+
 /* One frame with explicit ghost atoms and the caller's neighbour list, HOST
  * buffers: the DeepPot::compute(..., nghost, InputNlist, ago) path
  * (source/api_cc/src/DeepPotPT.cc:170-243) behind DP_DeepPotComputeNList

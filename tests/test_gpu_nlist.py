@@ -139,3 +139,26 @@ def test_dense_cell_takes_the_per_atom_path(cuda):
     ref = O.build_nlist_pt(ext, ext_t, n, 6.0, sel)
     nl = N.build_neighbor_list_local(_t(coord, cuda), _t(atype, cuda, torch.int32), box, 6.0, sel, shifts)
     np.testing.assert_array_equal(nl.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("spacing", [2.0, 1.5])
+def test_perfect_lattice_ties_and_cutoff(cuda, spacing):
+    """A simple cubic lattice: whole shells of exactly equal distances (ties
+    broken by extended index) and a shell exactly at rcut (6 = 3 x 2.0 = 4 x
+    1.5).  The FP32 distances cannot order such atoms, so their lists come
+    from the exact FP64 ranking: bitwise the oracle's."""
+    import torch
+    from dpgb import nlist as N
+
+    n = int(round(21.0 / spacing))
+    L = n * spacing
+    g = np.arange(n, dtype=np.float64) * spacing
+    coord = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    atype = (np.arange(coord.shape[0]) % 3 == 0).astype(np.int32)
+    box = np.diag([L, L, L]).reshape(-1)
+    sel = [140, 280]
+    shifts = O.ghost_shifts(box, 6.0).astype(np.int32)
+    ext, ext_t, _ = O.extend_coord_with_ghosts(coord, atype, box, 6.0, None)
+    ref = O.build_nlist_pt(ext, ext_t, coord.shape[0], 6.0, sel)
+    nl = N.build_neighbor_list_local(_t(coord, cuda), _t(atype, cuda, torch.int32), box, 6.0, sel, shifts)
+    np.testing.assert_array_equal(nl.cpu().numpy(), ref)
