@@ -674,15 +674,16 @@ int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host
     for (int i = 0; i < natom; ++i)
       if (atype_host[i] >= 0) sorted_rows[dp.row_pos_h[(size_t)f * natom + i]] = f * natom + i;
   // work chunks of the tensor-core embedding: contiguous sorted rows of one
-  // centre type.  The embedding kernels run one CTA per chunk with two CTAs
-  // per SM, so the rows are cut into at most 2 x SMs chunks of near-equal
-  // size (a CTA that had to take a second chunk would double the launch).
+  // centre type.  The embedding kernels run one CTA per chunk with three
+  // CTAs per SM, so the rows are cut into at most 3 x SMs chunks of
+  // near-equal size (a CTA that had to take a second chunk would double the
+  // launch).
   std::vector<WorkChunk> chunks;
   {
     int dev = 0, nsm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int slots = std::max(1, 2 * nsm);
+    const int slots = std::max(1, 3 * nsm);
     std::vector<int> per(nt, 0);
     std::vector<double> rem(nt, 0.0);
     int used = 0;

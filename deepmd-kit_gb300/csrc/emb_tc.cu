@@ -71,15 +71,18 @@ int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, Em
     if (!W1 || !W2 || !W3 || !d.emb_b[e][0] || !d.emb_b[e][1] || !d.emb_b[e][2]) return fail(DPGB_EINVAL, "missing embedding weights");
     const size_t b0 = per[0] * e, b1 = per[0] * nnets + per[1] * e, b2 = (per[0] + per[1]) * nnets + per[2] * e,
                  b3 = (per[0] + per[1] + per[2]) * nnets + per[3] * e;
+    // layer-2 outputs o sit at column c2 = neuron_col(o), layer-3 outputs at c3
     for (int o = 0; o < m.w2; ++o)
       for (int k = 0; k < m.w1; ++k) {
-        put_bf16(images, b0, o, k, m.k1, (float)W2[(size_t)k * m.w2 + o]);  // W2^T [n2 x k1]
-        put_bf16(images, b3, k, o, m.n2, (float)W2[(size_t)k * m.w2 + o]);  // W2 [k1 x n2]
+        const int c2 = neuron_col(o, m.w2, m.w1);
+        put_bf16(images, b0, c2, k, m.k1, (float)W2[(size_t)k * m.w2 + o]);  // W2^T [n2 x k1]
+        put_bf16(images, b3, k, c2, m.n2, (float)W2[(size_t)k * m.w2 + o]);  // W2 [k1 x n2]
       }
     for (int o = 0; o < m.w3; ++o)
       for (int k = 0; k < m.w2; ++k) {
-        put_bf16(images, b1, o, k, m.n2, (float)W3[(size_t)k * m.w3 + o]);  // W3^T [n3 x n2]
-        put_bf16(images, b2, k, o, m.n3, (float)W3[(size_t)k * m.w3 + o]);  // W3 [n2 x n3]
+        const int c3 = neuron_col(o, m.w3, m.w2), c2 = neuron_col(k, m.w2, m.w1);
+        put_bf16(images, b1, c3, c2, m.n2, (float)W3[(size_t)k * m.w3 + o]);  // W3^T [n3 x n2]
+        put_bf16(images, b2, c2, c3, m.n3, (float)W3[(size_t)k * m.w3 + o]);  // W3 [n2 x n3]
       }
     float* v = vec.data() + (size_t)m.vec_stride * e;
     for (int k = 0; k < m.w1; ++k) {
@@ -89,13 +92,15 @@ int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, Em
     }
     float* v2 = v + 3 * m.k1;
     for (int o = 0; o < m.w2; ++o) {
-      v2[o] = (float)d.emb_b[e][1][o];
-      v2[m.n2 + o] = d.emb_idt[e][1] ? (float)d.emb_idt[e][1][o] : 1.f;
+      const int c2 = neuron_col(o, m.w2, m.w1);
+      v2[c2] = (float)d.emb_b[e][1][o];
+      v2[m.n2 + c2] = d.emb_idt[e][1] ? (float)d.emb_idt[e][1][o] : 1.f;
     }
     float* v3 = v2 + 2 * m.n2;
     for (int o = 0; o < m.w3; ++o) {
-      v3[o] = (float)d.emb_b[e][2][o];
-      v3[m.n3 + o] = d.emb_idt[e][2] ? (float)d.emb_idt[e][2][o] : 1.f;
+      const int c3 = neuron_col(o, m.w3, m.w2);
+      v3[c3] = (float)d.emb_b[e][2][o];
+      v3[m.n3 + c3] = d.emb_idt[e][2] ? (float)d.emb_idt[e][2][o] : 1.f;
     }
     m.has_idt1 |= d.emb_idt[e][0] != nullptr;
     m.has_idt2 |= d.emb_idt[e][1] != nullptr;
@@ -137,13 +142,15 @@ __device__ __forceinline__ void store8(unsigned char* base, int r, int k0, int K
   *reinterpret_cast<uint4*>(base + tc::cm_offset(r, k0, K)) = *reinterpret_cast<uint4*>(h);
 }
 
+// D (+)= A B over kdim; acc0: add onto what D holds already (a preloaded
+// residual term) instead of overwriting it in the first step
 template <int K1, int N>
-__device__ __forceinline__ void issue_mma(uint32_t d_tmem, uint32_t a_s, uint32_t b_s, int kdim) {
+__device__ __forceinline__ void issue_mma(uint32_t d_tmem, uint32_t a_s, uint32_t b_s, int kdim, bool acc0 = false) {
   const uint32_t idesc = tc::idesc_bf16_f32(128, N);
   const uint32_t sbo = (uint32_t)(kdim / 8) * 128;
   for (int ks = 0; ks < kdim / 16; ++ks)
     tc::mma_bf16(d_tmem, tc::smem_desc(a_s + ks * 256, 128, sbo), tc::smem_desc(b_s + ks * 256, 128, sbo), idesc,
-                 ks > 0 ? 1u : 0u);
+                 (ks > 0 || acc0) ? 1u : 0u);
 }
 
 // Pack whole runs of section t (rows s_cursor .. row1 of the type-sorted
@@ -280,25 +287,34 @@ __device__ __forceinline__ void env_deriv(const float d[3], float rmin, float rm
 // ---------------------------------------------------------------------------
 // shared-memory plan (bytes), identical for forward and backward where shared
 constexpr int kFinAtoms = 4;  // atoms finalised together (xyz -> D) in the forward
-constexpr int kBwdAtoms = 8;  // atoms per tile in the backward
 
-// shared-memory plans (bytes); both fit two CTAs per SM for the 25/50/100 net
+// shared-memory plans (bytes).  Operands that are never live at the same
+// time share one region: in the forward A1 (read by the layer-2 MMA, done
+// before A2 is written), A2 (read by the layer-3 MMA, done before G is
+// written), G and the finalize staging.  Together with 128 TMEM columns (the
+// layer-3 accumulator reuses the layer-2 columns once they are read) three
+// CTAs fit on an SM for the 25/50/100 net.
 template <int W1, int W2, int W3>
 struct PlanF {
   static constexpr int K1 = (W1 + 15) / 16 * 16, N2 = (W2 + 15) / 16 * 16, N3 = (W3 + 15) / 16 * 16;
-  static constexpr int LDG = W3 + 1;  // fp32 G row stride (odd: no bank conflicts)
+  static constexpr int LDG = (W3 + 3) / 4 * 4;  // fp32 G row stride: float4 rows
   static constexpr int VEC = 3 * K1 + 2 * N2 + 2 * N3;
   static constexpr int fw2 = 0;
   static constexpr int fw3 = fw2 + N2 * K1 * 2;
-  static constexpr int a1 = fw3 + N3 * N2 * 2;
-  static constexpr int a2 = a1 + 128 * K1 * 2;
-  static constexpr int gbuf = a2 + 128 * N2 * 2;  // G (fp32)
-  static constexpr int rn = gbuf + 128 * LDG * 4;
-  static constexpr int vec = rn + 128 * 4 * 4;
-  static constexpr int xs = vec + VEC * 4;  // finalize staging of kFinAtoms xyz
-  static constexpr int total = xs + kFinAtoms * 4 * W3 * 4;
-  static constexpr int tmem_cols = (N2 + N3 <= 256) ? 256 : 512;
+  static constexpr int vec = fw3 + N3 * N2 * 2;
+  static constexpr int rn = (vec + VEC * 4 + 15) / 16 * 16;
+  static constexpr int reg = (rn + 128 * 4 * 4 + 127) / 128 * 128;
+  static constexpr int a1 = reg, a2 = reg, gbuf = reg, xs = reg;
+  static constexpr int cmax(int a, int b) { return a > b ? a : b; }
+  static constexpr int reg_bytes = cmax(cmax(128 * K1 * 2, 128 * N2 * 2), cmax(128 * LDG * 4, kFinAtoms * 4 * W3 * 4));
+  static constexpr int total = reg + reg_bytes;
+  static constexpr int tmem_cols = cmax(N2, N3) <= 128 ? 128 : 256;
 };
+// Backward: A1, A2, dP3, dP2 and the per-pair virial take turns in one region
+// (each is written after the MMA that read its predecessor completed); the
+// atoms' dE/dxyz are read through L1.  TMEM (128 columns): the layer-2 and
+// layer-3 accumulators at column 0 (in turn), dH2 at 0 and dH1 at n2, both
+// preloaded with their residual terms so that their MMAs add onto them.
 template <int W1, int W2, int W3>
 struct PlanB {
   static constexpr int K1 = (W1 + 15) / 16 * 16, N2 = (W2 + 15) / 16 * 16, N3 = (W3 + 15) / 16 * 16;
@@ -307,18 +323,17 @@ struct PlanB {
   static constexpr int fw3 = fw2 + N2 * K1 * 2;
   static constexpr int bw3 = fw3 + N3 * N2 * 2;
   static constexpr int bw2 = bw3 + N2 * N3 * 2;
-  static constexpr int a1 = bw2 + K1 * N2 * 2;
-  static constexpr int a2 = a1 + 128 * K1 * 2;
-  static constexpr int a3 = a2 + 128 * N2 * 2;  // dP3 operand
-  static constexpr int gbuf = a3 + 128 * N3 * 2;  // dxyz of the tile atoms
-  static constexpr int vec = gbuf + kBwdAtoms * 4 * W3 * 4;
-  static constexpr int vir = vec + VEC * 4;  // per-pair virial (fp32)
-  static constexpr int total = vir + 128 * 9 * 4;
-  static constexpr int tmem_cols = (N2 + N3 <= 256) ? 256 : 512;
+  static constexpr int vec = bw2 + K1 * N2 * 2;
+  static constexpr int reg = (vec + VEC * 4 + 127) / 128 * 128;
+  static constexpr int a1 = reg, a2 = reg, a3 = reg, vir = reg;
+  static constexpr int cmax(int a, int b) { return a > b ? a : b; }
+  static constexpr int reg_bytes = cmax(cmax(128 * K1 * 2, 128 * N2 * 2), cmax(128 * N3 * 2, 128 * 9 * 4));
+  static constexpr int total = reg + reg_bytes;
+  static constexpr int tmem_cols = cmax(N3, N2 + K1) <= 128 ? 128 : 256;
 };
 
 template <int W1, int W2, int W3>
-__global__ void __launch_bounds__(128, 2)
+__global__ void __launch_bounds__(128, 3)
 emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ chunks, int nchunks,
                   const int* __restrict__ run_len, const int* __restrict__ sorted_rows, float* __restrict__ xyz,
                   float* __restrict__ xyzp, float* __restrict__ Dout, int* __restrict__ status) {
@@ -408,9 +423,9 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
           tc::tmem_ld_wait();
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
-            const int o = c0 + i;
-            if (o < W2) {
-              float h = tanh_fast(v[i] + b2[o]) * i2[o];
+            const int c = c0 + i, o = col_neuron(c, W2, W1);
+            if (o >= 0) {
+              float h = tanh_fast(v[i] + b2[c]) * i2[c];
               if (W2 == W1) h += h1[o];
               if (W2 == 2 * W1) h += h1[o < W1 ? o : o - W1];
               h2[o] = pi.valid ? h : 0.f;
@@ -421,7 +436,10 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         for (int k0 = 0; k0 < P::N2; k0 += 8) {
           float v[8];
 #pragma unroll
-          for (int i = 0; i < 8; ++i) v[i] = (k0 + i < W2) ? h2[k0 + i] : 0.f;
+          for (int i = 0; i < 8; ++i) {
+            const int o = col_neuron(k0 + i, W2, W1);
+            v[i] = o >= 0 ? h2[o] : 0.f;
+          }
           store8(smem + P::a2, tid, k0, P::N2, v);
         }
         tc::fence_before();
@@ -429,26 +447,42 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         __syncthreads();
         tc::fence_after();
         if (tid == 0) {
-          issue_mma<P::N2, P::N3>(tbase + P::N2, sA2, sW3, P::N2);
+          issue_mma<P::N2, P::N3>(tbase, sA2, sW3, P::N2);  // over the consumed layer-2 columns
           tc::mma_commit(&bar);
         }
         ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;
         phase ^= 1;
         tc::fence_after();
-        // epilogue 3: G = tanh(acc + b3) * idt3 + skip(H2), kept in FP32
+        // epilogue 3: G = tanh(acc + b3) * idt3 + skip(H2), kept in FP32,
+        // stored as float4 rows
 #pragma unroll
         for (int c0 = 0; c0 < P::N3; c0 += 16) {
           float v[16];
-          tc::tmem_ld16(tc::taddr(tbase, warp * 32, P::N2 + c0), v);
+          tc::tmem_ld16(tc::taddr(tbase, warp * 32, c0), v);
           tc::tmem_ld_wait();
+          float g[16];
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
-            const int o = c0 + i;
-            if (o < W3) {
-              float g = tanh_fast(v[i] + b3[o]) * i3[o];
-              if (W3 == W2) g += h2[o];
-              if (W3 == 2 * W2) g += h2[o < W2 ? o : o - W2];
-              sG[tid * P::LDG + o] = pi.valid ? g : 0.f;
+            const int c = c0 + i, o = col_neuron(c, W3, W2);
+            g[i] = 0.f;
+            if (o >= 0) {
+              float x3 = tanh_fast(v[i] + b3[c]) * i3[c];
+              if (W3 == W2) x3 += h2[o];
+              if (W3 == 2 * W2) x3 += h2[o < W2 ? o : o - W2];
+              g[i] = pi.valid ? x3 : 0.f;
+            }
+          }
+          // G in neuron order; column pairs that hold two consecutive
+          // neurons (from an even one) go out as one float2
+          float* grow = sG + tid * P::LDG;
+#pragma unroll
+          for (int i = 0; i < 16; i += 2) {
+            const int o0 = col_neuron(c0 + i, W3, W2), o1 = col_neuron(c0 + i + 1, W3, W2);
+            if (o0 >= 0 && o1 == o0 + 1 && (o0 & 1) == 0) {
+              *reinterpret_cast<float2*>(grow + o0) = make_float2(g[i], g[i + 1]);
+            } else {
+              if (o0 >= 0) grow[o0] = g[i];
+              if (o1 >= 0) grow[o1] = g[i + 1];
             }
           }
         }
@@ -457,24 +491,36 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         if (!alive) break;
         // partial xyz of this section: sum_{pairs of the atom} Rn[c] G[n]
         // (FP32, fixed order; plain stores, the atom is owned by this CTA).
-        // One thread per (atom, neuron) does all four components: one G load
-        // and one broadcast float4 of Rn per pair and four FMAs.
-        for (int q = tid; q < ntile * W3; q += blockDim.x) {
-          const int k = q / W3, n = q - k * W3;
-          float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+        // One thread per (atom, 4 neurons): per pair one float4 of G and one
+        // of Rn feed 16 FMAs.
+        constexpr int NQ = P::LDG / 4;
+        for (int q = tid; q < ntile * NQ; q += blockDim.x) {
+          const int k = q / NQ, n0 = 4 * (q - k * NQ);
+          float4 a[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) a[c] = make_float4(0.f, 0.f, 0.f, 0.f);
           for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) {
-            const float g = sG[pp * P::LDG + n];
+            const float4 g = *reinterpret_cast<const float4*>(sG + pp * P::LDG + n0);
             const float4 r = *reinterpret_cast<const float4*>(sRn + pp * 4);
-            s0 = fmaf(r.x, g, s0);
-            s1 = fmaf(r.y, g, s1);
-            s2 = fmaf(r.z, g, s2);
-            s3 = fmaf(r.w, g, s3);
+            const float rc[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              a[c].x = fmaf(rc[c], g.x, a[c].x);
+              a[c].y = fmaf(rc[c], g.y, a[c].y);
+              a[c].z = fmaf(rc[c], g.z, a[c].z);
+              a[c].w = fmaf(rc[c], g.w, a[c].w);
+            }
           }
-          float* o = xpart + (size_t)s_row[k] * 4 * ng + n;
-          o[0] = s0;
-          o[ng] = s1;
-          o[2 * ng] = s2;
-          o[3 * ng] = s3;
+          float* o = xpart + (size_t)s_row[k] * 4 * ng + n0;
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            if (n0 + 3 < W3 && (ng & 3) == 0) {
+              *reinterpret_cast<float4*>(o + c * ng) = a[c];
+            } else {
+              const float av[4] = {a[c].x, a[c].y, a[c].z, a[c].w};
+              for (int u = 0; u < 4 && n0 + u < W3; ++u) o[c * ng + u] = av[u];
+            }
+          }
         }
         __syncthreads();
       }
@@ -518,17 +564,24 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 }
 
 // ---------------------------------------------------------------------------
+// Backward of the embedding per tile: forward recompute (t1, t2 kept in
+// registers; h1, h2 recomputed from them), then per pair dG = R~ . dxyz,
+// dR~ = sum_n G_n dxyz_n, and the chain dP3 -> dH2 -> dP2 -> dH1 -> dR~[0]
+// through the two transposed-weight MMAs.  The residual terms of dH2 and dH1
+// are folded group by group (col_neuron order) and stored into their
+// accumulators before the MMA adds the weight term.
 template <int W1, int W2, int W3>
-__global__ void __launch_bounds__(128, 2)
+__global__ void __launch_bounds__(128, 3)
 emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ chunks, int nchunks,
                   const int* __restrict__ run_len, const int* __restrict__ sorted_rows,
                   const float* __restrict__ dxyz, float* __restrict__ gpair, double* __restrict__ vir_row,
                   int* __restrict__ status) {
   using P = PlanB<W1, W2, W3>;
+  static_assert(W2 == 2 * W1 && W3 == 2 * W2, "the backward folds doubling residuals (w2 = 2 w1, w3 = 2 w2)");
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
   __shared__ uint32_t s_tmem;
-  __shared__ int s_row[kBwdAtoms], s_off[kBwdAtoms + 1], s_ntile, s_cursor;
+  __shared__ int s_row[kTcMaxAtoms], s_off[kTcMaxAtoms + 1], s_ntile, s_cursor;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int ng = p.ng;
   if (warp == 0) tc::tmem_alloc(&s_tmem, P::tmem_cols);
@@ -536,12 +589,12 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
   __syncthreads();
   tc::fence_after();
   const uint32_t tbase = s_tmem;
+  const uint32_t tlane = tc::taddr(tbase, warp * 32, 0);
   uint32_t phase = 0;
   bool alive = true;
-  float* sDX = reinterpret_cast<float*>(smem + P::gbuf);  // [kBwdAtoms][W3][4]: one float4 per neuron
   float* sV = reinterpret_cast<float*>(smem + P::vec);
   float* sVir = reinterpret_cast<float*>(smem + P::vir);
-  const uint32_t sA1 = tc::smem_u32(smem + P::a1), sA2 = tc::smem_u32(smem + P::a2), sA3 = tc::smem_u32(smem + P::a3);
+  const uint32_t sA = tc::smem_u32(smem + P::reg);  // A1, A2, dP3, dP2 in turn
   const uint32_t sW2 = tc::smem_u32(smem + P::fw2), sW3 = tc::smem_u32(smem + P::fw3);
   const uint32_t sB3 = tc::smem_u32(smem + P::bw3), sB2 = tc::smem_u32(smem + P::bw2);
   const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
@@ -563,75 +616,76 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
       const float* w1 = sV;
       const float* b1 = sV + P::K1;
       const float* i1 = sV + 2 * P::K1;
-      const float* b2 = sV + 3 * P::K1;
+      const float* b2 = sV + 3 * P::K1;  // layers 2 and 3: by column (col_neuron order)
       const float* i2 = b2 + P::N2;
       const float* b3 = i2 + P::N2;
       const float* i3 = b3 + P::N3;
       while (alive) {
         if (warp == 0)
-          pack_tile<kBwdAtoms>(run_len, sorted_rows, p.ntypes, ch.row1, t, s_row, s_off, &s_ntile, &s_cursor, tid & 31);
+          pack_tile<kTcMaxAtoms>(run_len, sorted_rows, p.ntypes, ch.row1, t, s_row, s_off, &s_ntile, &s_cursor,
+                                 tid & 31);
         __syncthreads();
         const int ntile = s_ntile;
         if (ntile == 0) break;
-        for (int q = tid; q < ntile * 4 * W3; q += blockDim.x) {
-          const int k = q / (4 * W3), rem = q - k * 4 * W3, cc = rem / W3, n = rem - cc * W3;
-          sDX[(k * W3 + n) * 4 + cc] = dxyz[(size_t)s_row[k] * 4 * ng + cc * ng + n];
-        }
         PairInfo pi;
         float rn[4], dv[3];
         pair_env(p, t, ti, s_row, s_off, ntile, tid, pi, rn, dv);
         const float x = rn[0];
-        float t1[W1], h1[W1];
+        const float vmask = pi.valid ? 1.f : 0.f;
+        float t1[W1];
 #pragma unroll
-        for (int k = 0; k < W1; ++k) {
-          const float tv = tanh_fast(fmaf(x, w1[k], b1[k]));
-          t1[k] = tv;
-          float h = tv * i1[k];
-          if (W1 == 1) h += x;
-          if (W1 == 2) h += x;
-          h1[k] = pi.valid ? h : 0.f;
-        }
+        for (int k = 0; k < W1; ++k) t1[k] = tanh_fast(fmaf(x, w1[k], b1[k]));
+        // h1 = t1 idt1 (+ x when the residual concatenates x), 0 off the tile
+        auto h1 = [&](int k) {
+          float h = t1[k] * i1[k];
+          if (W1 == 1 || W1 == 2) h += x;
+          return h * vmask;
+        };
 #pragma unroll
         for (int k0 = 0; k0 < P::K1; k0 += 8) {
           float v[8];
 #pragma unroll
-          for (int i = 0; i < 8; ++i) v[i] = (k0 + i < W1) ? h1[k0 + i] : 0.f;
+          for (int i = 0; i < 8; ++i) v[i] = (k0 + i < W1) ? h1(k0 + i) : 0.f;
           store8(smem + P::a1, tid, k0, P::K1, v);
         }
         tc::fence_async_smem();
         __syncthreads();
         tc::fence_after();
         if (tid == 0) {
-          issue_mma<P::K1, P::N2>(tbase, sA1, sW2, P::K1);
+          issue_mma<P::K1, P::N2>(tbase, sA, sW2, P::K1);
           tc::mma_commit(&bar);
         }
         bool ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout);
         phase ^= 1;
         tc::fence_after();
-        float t2[W2], h2[W2];
+        // epilogue 2: t2 (neuron order); A2 = h2 by column
+        float t2[W2];
 #pragma unroll
         for (int c0 = 0; c0 < P::N2; c0 += 16) {
           float v[16];
-          tc::tmem_ld16(tc::taddr(tbase, warp * 32, c0), v);
+          tc::tmem_ld16(tlane + c0, v);
           tc::tmem_ld_wait();
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
-            const int o = c0 + i;
-            if (o < W2) {
-              const float tv = tanh_fast(v[i] + b2[o]);
-              t2[o] = tv;
-              float h = tv * i2[o];
-              if (W2 == W1) h += h1[o];
-              if (W2 == 2 * W1) h += h1[o < W1 ? o : o - W1];
-              h2[o] = pi.valid ? h : 0.f;
-            }
+            const int cc = c0 + i, o = col_neuron(cc, W2, W1);
+            if (o >= 0) t2[o] = tanh_fast(v[i] + b2[cc]);
           }
         }
+        // h2 of neuron o (column cc): t2 idt2 + residual of h1
+        auto h2 = [&](int o, int cc) {
+          float h = t2[o] * i2[cc];
+          if (W2 == W1) h += h1(o);
+          if (W2 == 2 * W1) h += h1(o < W1 ? o : o - W1);
+          return h * vmask;
+        };
 #pragma unroll
         for (int k0 = 0; k0 < P::N2; k0 += 8) {
           float v[8];
 #pragma unroll
-          for (int i = 0; i < 8; ++i) v[i] = (k0 + i < W2) ? h2[k0 + i] : 0.f;
+          for (int i = 0; i < 8; ++i) {
+            const int o = col_neuron(k0 + i, W2, W1);
+            v[i] = o >= 0 ? h2(o, k0 + i) : 0.f;
+          }
           store8(smem + P::a2, tid, k0, P::N2, v);
         }
         tc::fence_before();
@@ -639,87 +693,93 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         __syncthreads();
         tc::fence_after();
         if (tid == 0) {
-          issue_mma<P::N2, P::N3>(tbase + P::N2, sA2, sW3, P::N2);
+          issue_mma<P::N2, P::N3>(tbase, sA, sW3, P::N2);  // over the consumed layer-2 columns
           tc::mma_commit(&bar);
         }
         ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;
         phase ^= 1;
         tc::fence_after();
-        // epilogue 3 of the backward: G, dG = Rn . dxyz, dRn (direct part),
-        // dP3 = dG * idt3 * (1 - t3^2) into the BF16 operand, skip folds
-        const float4* dx = reinterpret_cast<const float4*>(sDX) + pi.k * W3;
+        // epilogue 3: G, dG = R~ . dxyz, dR~ (direct part), dP3 = dG idt3
+        // (1 - t3^2) into the BF16 operand; the residual part of dH2 (dG of
+        // both halves folded onto their layer-2 neuron) completes group by
+        // group and goes to the dH2 accumulator columns (already read here)
+        const float4* dx = reinterpret_cast<const float4*>(dxyz + (size_t)pi.row * 4 * ng);
         float drn[4] = {0.f, 0.f, 0.f, 0.f};
-        float dh2[W2];
-#pragma unroll
-        for (int o = 0; o < W2; ++o) dh2[o] = 0.f;
 #pragma unroll
         for (int c0 = 0; c0 < P::N3; c0 += 16) {
           float v[16], dp[16];
-          tc::tmem_ld16(tc::taddr(tbase, warp * 32, P::N2 + c0), v);
+          tc::tmem_ld16(tlane + c0, v);
           tc::tmem_ld_wait();
+          // columns i and i + 8: layer-3 neurons o and w2 + o (both feed the
+          // residual of layer-2 neuron o, whose dH2 column lies in this group
+          // or an earlier one, already read by this lane)
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int o = c0 + i;
-            dp[i] = 0.f;
-            if (o < W3) {
-              const float tv = tanh_fast(v[i] + b3[o]);
-              float g = tv * i3[o];
-              if (W3 == W2) g += h2[o];
-              if (W3 == 2 * W2) g += h2[o < W2 ? o : o - W2];
-              const float4 dq = dx[o];
-              const float d0 = dq.x, d1 = dq.y, d2 = dq.z, d3 = dq.w;
-              drn[0] = fmaf(g, d0, drn[0]);
-              drn[1] = fmaf(g, d1, drn[1]);
-              drn[2] = fmaf(g, d2, drn[2]);
-              drn[3] = fmaf(g, d3, drn[3]);
-              const float dg = rn[0] * d0 + rn[1] * d1 + rn[2] * d2 + rn[3] * d3;
-              dp[i] = pi.valid ? dg * i3[o] * (1.f - tv * tv) : 0.f;
-              if (W3 == W2) dh2[o] += dg;
-              if (W3 == 2 * W2) dh2[o < W2 ? o : o - W2] += dg;
+          for (int i = 0; i < 8; ++i) {
+            float res = 0.f;
+#pragma unroll
+            for (int h = 0; h < 16; h += 8) {
+              const int cc = c0 + i + h, o = col_neuron(cc, W3, W2);
+              dp[i + h] = 0.f;
+              if (o >= 0) {
+                const float tv = tanh_fast(v[i + h] + b3[cc]);
+                const int m = o < W2 ? o : o - W2;
+                const float g = tv * i3[cc] + h2(m, neuron_col(m, W2, W1));
+                const float4 dq = pi.valid ? dx[o] : make_float4(0.f, 0.f, 0.f, 0.f);
+                drn[0] = fmaf(g, dq.x, drn[0]);
+                drn[1] = fmaf(g, dq.y, drn[1]);
+                drn[2] = fmaf(g, dq.z, drn[2]);
+                drn[3] = fmaf(g, dq.w, drn[3]);
+                const float dg = rn[0] * dq.x + rn[1] * dq.y + rn[2] * dq.z + rn[3] * dq.w;
+                res += dg;
+                dp[i + h] = dg * i3[cc] * (1.f - tv * tv) * vmask;
+              }
             }
+            const int o = col_neuron(c0 + i, W3, W2);
+            if (o >= 0) tc::tmem_st1(tlane + neuron_col(o, W2, W1), res);
           }
           store8(smem + P::a3, tid, c0, P::N3, dp);
           store8(smem + P::a3, tid, c0 + 8, P::N3, dp + 8);
         }
+        tc::tmem_st_wait();
         tc::fence_before();
         tc::fence_async_smem();
         __syncthreads();
         tc::fence_after();
         if (tid == 0) {
-          issue_mma<P::N3, P::N2>(tbase, sA3, sB3, P::N3);  // dH2 = dP3 . W3^T
+          issue_mma<P::N3, P::N2>(tbase, sA, sB3, P::N3, true);  // dH2 += dP3 . W3^T
           tc::mma_commit(&bar);
         }
         ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;
         phase ^= 1;
         tc::fence_after();
-        float dh1[W1];
-#pragma unroll
-        for (int k = 0; k < W1; ++k) dh1[k] = 0.f;
+        // epilogue 4: dP2 = dH2 idt2 (1 - t2^2) into the operand; the
+        // residual of dH1 folds group by group into its accumulator
 #pragma unroll
         for (int c0 = 0; c0 < P::N2; c0 += 16) {
           float v[16], dp[16];
-          tc::tmem_ld16(tc::taddr(tbase, warp * 32, c0), v);
+          tc::tmem_ld16(tlane + c0, v);
           tc::tmem_ld_wait();
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
-            const int o = c0 + i;
-            dp[i] = 0.f;
-            if (o < W2) {
-              const float dh = v[i] + dh2[o];
-              dp[i] = pi.valid ? dh * i2[o] * (1.f - t2[o] * t2[o]) : 0.f;
-              if (W2 == W1) dh1[o] += dh;
-              if (W2 == 2 * W1) dh1[o < W1 ? o : o - W1] += dh;
-            }
+            const int cc = c0 + i, o = col_neuron(cc, W2, W1);
+            dp[i] = o >= 0 ? v[i] * i2[cc] * (1.f - t2[o] * t2[o]) * vmask : 0.f;
           }
           store8(smem + P::a2, tid, c0, P::N2, dp);
           store8(smem + P::a2, tid, c0 + 8, P::N2, dp + 8);
+          // residual of dH1: layer-1 neurons 8 (c0 / 16) .. + 7, both halves
+          // in this group, to their dH1 columns n2 + c0 / 2 ..
+          float r[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) r[i] = col_neuron(c0 + i, W2, W1) >= 0 ? v[i] + v[i + 8] : 0.f;
+          tc::tmem_st8(tlane + P::N2 + c0 / 2, r);
         }
+        tc::tmem_st_wait();
         tc::fence_before();
         tc::fence_async_smem();
         __syncthreads();
         tc::fence_after();
         if (tid == 0) {
-          issue_mma<P::N2, P::K1>(tbase + P::N2, sA2, sB2, P::N2);  // dH1 = dP2 . W2^T
+          issue_mma<P::N2, P::K1>(tbase + P::N2, sA, sB2, P::N2, true);  // dH1 += dP2 . W2^T
           tc::mma_commit(&bar);
         }
         ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;
@@ -729,13 +789,13 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 #pragma unroll
         for (int c0 = 0; c0 < P::K1; c0 += 16) {
           float v[16];
-          tc::tmem_ld16(tc::taddr(tbase, warp * 32, P::N2 + c0), v);
+          tc::tmem_ld16(tlane + P::N2 + c0, v);
           tc::tmem_ld_wait();
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int k = c0 + i;
             if (k < W1) {
-              const float dh = v[i] + dh1[k];
+              const float dh = v[i];
               dss = fmaf(dh * i1[k] * (1.f - t1[k] * t1[k]), w1[k], dss);
               if (W1 == 1 || W1 == 2) dss += dh;
             }
@@ -761,6 +821,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
           gp[1] = g[1];
           gp[2] = g[2];
         }
+        // the operand region is free (the last MMA completed): pair virials
 #pragma unroll
         for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -800,9 +861,10 @@ __global__ void run_len_kernel(int* __restrict__ run_len, const int* __restrict_
   run_len[q] = n;
 }
 
-// dE/dxyz (before the forward's 1/nnei): dxyz[c][n] = (sum_m dD[n][m] xyz[c][m]
-// + [n < M] sum_n' dD[n'][n] xyz[c][n']) / nnei.  One warp per row: the
-// row's xyz and dD are staged in shared memory with coalesced loads.
+// dE/dxyz (before the forward's 1/nnei): dxyz[n][c] = (sum_m dD[n][m] xyz[c][m]
+// + [n < M] sum_n' dD[n'][n] xyz[c][n']) / nnei, stored [row][ng][4] (one
+// float4 per neuron for the backward kernels).  One warp per row: the row's
+// xyz and dD are staged in shared memory with coalesced loads.
 __global__ void dxyz_kernel(float* __restrict__ dxyz, const float* __restrict__ dD, const float* __restrict__ xyz,
                             const int* __restrict__ row_pos, const int* __restrict__ atype, int nloc, int nrows,
                             int ng, int M, int nnei) {
@@ -836,8 +898,8 @@ __global__ void dxyz_kernel(float* __restrict__ dxyz, const float* __restrict__ 
   }
   __syncwarp();
   const float inv = 1.f / (float)nnei;
-  for (int q = lane; q < 4 * ng; q += 32) {
-    const int c = q / ng, n = q - c * ng;
+  for (int q = lane; q < 4 * ng; q += 32) {  // out [n][c]: one float4 per neuron
+    const int n = q >> 2, c = q & 3;
     const float* xc = sx + c * ng;
     float s = n < M ? sT[c * M + n] : 0.f;
     for (int m = 0; m < M; ++m) s = fmaf(sdT[m * ng + n], xc[m], s);
@@ -892,7 +954,7 @@ int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChun
                       const int* run_len, const int* sorted_rows, float* xyz, float* xyzp, float* D, int* status,
                       cudaStream_t st) {
   if (nchunks <= 0) return DPGB_OK;
-  const int nsm = 2 * sm_count();
+  const int nsm = 3 * sm_count();  // three CTAs per SM
   if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100)
     return launch_fwd_t<25, 50, 100>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status, st, nsm);
   if (e.w1 == 3 && e.w2 == 6 && e.w3 == 12)
@@ -916,7 +978,7 @@ int launch_emb_tc_bwd(const DescParams<float>& p, const EmbTC& e, const WorkChun
                       const int* run_len, const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row,
                       int* status, cudaStream_t st) {
   if (nchunks <= 0) return DPGB_OK;
-  const int nsm = 2 * sm_count();
+  const int nsm = 3 * sm_count();  // three CTAs per SM
   if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100)
     return launch_bwd_t<25, 50, 100>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status, st,
                                      nsm);

@@ -9,8 +9,29 @@ namespace dpgb {
 constexpr int kTcRows = 128;     // MMA M: pairs per tile
 constexpr int kTcMaxAtoms = 16;  // atoms per tile
 
+// Column order of a layer's outputs (its TMEM accumulator columns, and the K
+// order of the next layer's operand).  When the layer doubles its input
+// through the residual (w_out == 2 w_in: the skip adds the input to both
+// halves), each group of 16 columns holds 8 consecutive neurons m of the
+// first half and their partners w_in + m, so the two contributions to one
+// input neuron meet in one group (the backward folds them group by group).
+// Otherwise the natural order.  -1: a padding column.  The padded width
+// 16 * ceil(w_in / 8) equals pad16(w_out).
+__host__ __device__ constexpr int col_neuron(int c, int w_out, int w_in) {
+  return w_out != 2 * w_in ? (c < w_out ? c : -1)
+                           : ((8 * (c >> 4) + (c & 7)) >= w_in ? -1
+                                                               : ((c & 15) < 8 ? 8 * (c >> 4) + (c & 7)
+                                                                               : w_in + 8 * (c >> 4) + (c & 7)));
+}
+__host__ __device__ constexpr int neuron_col(int n, int w_out, int w_in) {
+  return w_out != 2 * w_in ? n
+                           : 16 * ((n < w_in ? n : n - w_in) >> 3) + (n < w_in ? 0 : 8) + ((n < w_in ? n : n - w_in) & 7);
+}
+
 // Per-net weight images (bf16, already in the shared-memory core-matrix
 // layout) and FP32 vectors of a 3-layer embedding net 1 -> w1 -> w2 -> w3.
+// Layer-2 and layer-3 outputs are in col_neuron order (rows of fw2 / fw3,
+// K of fw3 / bw2 / bw3, the b/idt vectors of layers 2 and 3).
 struct EmbTC {
   int w1, w2, w3;        // real widths
   int k1, n2, n3;        // padded: k1 = pad16(w1), n2 = pad16(w2), n3 = pad16(w3)

@@ -218,7 +218,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ 
   __shared__ float4 s_dx[kTabWarps][32 * kTabJ];
   float4* sdx = s_dx[threadIdx.x >> 5];
   const float* dr = dxyz + (size_t)row * 4 * ng;
-  for (int n = lane; n < ng; n += 32) sdx[n] = make_float4(dr[n], dr[ng + n], dr[2 * ng + n], dr[3 * ng + n]);
+  for (int n = lane; n < ng; n += 32) sdx[n] = reinterpret_cast<const float4*>(dr)[n];  // dxyz is [row][ng][4]
   __syncwarp();
   double vir[9];
 #pragma unroll
