@@ -6,9 +6,16 @@
 //
 // One launch covers the rows of every atom type (each 128-row tile belongs to
 // one type and uses that type's weights).  A CTA computes a 128 x BN tile; K is
-// streamed in chunks of 64 through an S-stage cp.async ring so that loads run
-// ahead of the MMAs; each stage is released when the MMAs reading it commit.
-// The epilogue stores 16 consecutive columns per thread (64-byte segments).
+// streamed in chunks of 64 through an S-stage ring filled by TMA (one 2D
+// tensor copy per operand and stage, 128-byte swizzled rows, completion
+// counted in bytes on the stage's "full" barrier) by one producer thread,
+// while one MMA thread consumes the stages and releases each through its
+// "empty" barrier when the MMAs reading it commit.  Rows past the operand's
+// end and K past its width arrive as zeros.  The epilogue stores 16
+// consecutive columns per thread (64-byte segments).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "fit_tc.cuh"
 #include "tc.cuh"
 
@@ -23,15 +30,6 @@ __device__ __forceinline__ float tanh_fast(float x) {
   return y;
 }
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
 
 __device__ __forceinline__ void ld16f(const float* p, float* v) {
   const float4* q = reinterpret_cast<const float4*>(p);
@@ -60,9 +58,12 @@ __device__ __forceinline__ void st16b(__nv_bfloat16* p, const float* v) {
 
 template <int BN, int S>
 __global__ void __launch_bounds__(128)
-fit_gemm_kernel(FitGemm g, int* __restrict__ err) {
-  extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ uint64_t bar[S];
+fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b, FitGemm g,
+                int* __restrict__ err) {
+  extern __shared__ unsigned char smem_raw[];
+  // swizzled TMA tiles want 1024-byte aligned stages
+  unsigned char* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
+  __shared__ uint64_t full[S], empty[S], done;
   __shared__ uint32_t s_tmem;
   constexpr int SA = 128 * kKC * 2, SB = BN * kKC * 2;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -73,77 +74,49 @@ fit_gemm_kernel(FitGemm g, int* __restrict__ err) {
   const int n0 = blockIdx.y * BN;
   const int nt = min(BN, g.N - n0);  // multiple of 16
   if (warp == 0) tc::tmem_alloc(&s_tmem, BN < 32 ? 32 : BN);
-  if (tid == 0)
-    for (int s = 0; s < S; ++s) tc::mbar_init(&bar[s], 1);
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(&done, 1);
+    tc::fence_mbar_init();
+  }
   __syncthreads();
   tc::fence_after();
   const uint32_t tbase = s_tmem;
-  const uint32_t idesc = tc::idesc_bf16_f32(128, nt);
-  const __nv_bfloat16* A = g.A + (size_t)m0 * g.lda;
-  const __nv_bfloat16* B = g.B + ((size_t)t * g.N + n0) * g.K;
   const int nchunk = (g.K + kKC - 1) / kKC;
-  auto load = [&](int i) {
-    unsigned char* sa = smem + (i % S) * (SA + SB);
-    unsigned char* sb = sa + SA;
-    const int k0 = i * kKC, kc = min(kKC, g.K - k0), per = kc / 8;
-    for (int q = tid; q < 128 * per; q += 128) {
-      const int r = q / per, c8 = q - r * per;
-      const bool in = r < rows_valid;
-      cp_async16(sa + tc::cm_offset(r, c8 * 8, kc), in ? (const void*)(A + (size_t)r * g.lda + k0 + c8 * 8) : (const void*)A,
-                 in ? 16 : 0);
-    }
-    for (int q = tid; q < nt * per; q += 128) {
-      const int r = q / per, c8 = q - r * per;
-      cp_async16(sb + tc::cm_offset(r, c8 * 8, kc), B + (size_t)r * g.K + k0 + c8 * 8, 16);
-    }
-  };
-#pragma unroll
-  for (int i = 0; i < S - 1; ++i) {
-    if (i < nchunk) load(i);
-    cp_commit();
-  }
-  bool pending[S];
-  uint32_t phase[S];
-#pragma unroll
-  for (int s = 0; s < S; ++s) {
-    pending[s] = false;
-    phase[s] = 0;
-  }
   bool ok = true;
-  for (int i = 0; i < nchunk; ++i) {
-    const int s = i % S;
-    cp_wait<S - 2>();
-    tc::fence_async_smem();
-    __syncthreads();
-    tc::fence_after();
-    if (tid == 0) {
-      const int kc = min(kKC, g.K - i * kKC);
+  if (warp == 1 && lane == 0) {
+    // producer: chunk i into stage i % S once the MMAs of chunk i - S released it
+    for (int i = 0; i < nchunk && ok; ++i) {
+      const int s = i % S;
+      if (i >= S) ok = tc::mbar_wait(&empty[s], ((i / S) - 1) & 1, err);
+      if (!ok) break;
+      const uint32_t a0 = tc::smem_u32(smem + s * (SA + SB));
+      tc::mbar_expect_tx(&full[s], SA + SB);
+      tc::tma_load_2d(a0, &tma_a, i * kKC, m0, &full[s]);
+      tc::tma_load_2d(a0 + SA, &tma_b, i * kKC, t * g.N + n0, &full[s]);
+    }
+  } else if (warp == 0 && lane == 0) {
+    // MMA issuer: 4 steps of K = 16 per chunk (zeros past K add nothing)
+    const uint32_t idesc = tc::idesc_bf16_f32(128, nt);
+    for (int i = 0; i < nchunk && ok; ++i) {
+      const int s = i % S;
+      ok = tc::mbar_wait(&full[s], (i / S) & 1, err);
+      if (!ok) break;
+      tc::fence_after();
       const uint32_t a0 = tc::smem_u32(smem + s * (SA + SB)), b0 = a0 + SA;
-      const uint32_t sbo = (uint32_t)(kc / 8) * 128;
-      for (int ks = 0; ks < kc / 16; ++ks)
-        tc::mma_bf16(tbase, tc::smem_desc(a0 + ks * 256, 128, sbo), tc::smem_desc(b0 + ks * 256, 128, sbo), idesc,
-                     (i > 0 || ks > 0) ? 1u : 0u);
-      tc::mma_commit(&bar[s]);
-    }
-    pending[s] = true;
-    const int j = i + S - 1;
-    if (j < nchunk) {
-      const int sj = j % S;  // the stage chunk i-1 used
-      if (pending[sj]) {
-        ok = tc::mbar_wait(&bar[sj], phase[sj], err) && ok;
-        phase[sj] ^= 1;
-        pending[sj] = false;
-      }
-      load(j);
-    }
-    cp_commit();
-  }
 #pragma unroll
-  for (int s = 0; s < S; ++s)
-    if (pending[s]) {
-      ok = tc::mbar_wait(&bar[s], phase[s], err) && ok;
-      phase[s] ^= 1;
+      for (int ks = 0; ks < kKC / 16; ++ks)
+        tc::mma_bf16(tbase, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc,
+                     (i > 0 || ks > 0) ? 1u : 0u);
+      tc::mma_commit(&empty[s]);
     }
+    tc::mma_commit(&done);
+  }
+  __syncwarp();
+  ok = tc::mbar_wait(&done, 0, err) && ok;
   tc::fence_after();
   ok = __syncthreads_and(ok) != 0;
   if (ok) {
@@ -212,16 +185,50 @@ fit_gemm_kernel(FitGemm g, int* __restrict__ err) {
   if (warp == 0) tc::tmem_dealloc(tbase, BN < 32 ? 32 : BN);
 }
 
+// cuTensorMapEncodeTiled, taken from the driver through the runtime
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// bf16 matrix [rows, cols] with a row stride of ld elements, read in boxes of
+// box_rows x 64 with 128-byte swizzling (out-of-range rows / columns read 0)
+int encode_bf16_2d(CUtensorMap* m, const __nv_bfloat16* base, int rows, int cols, int ld, int box_rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return fail(DPGB_ECUDA, "cuTensorMapEncodeTiled is not available");
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || ((size_t)ld * 2) % 16)
+    return fail(DPGB_EINVAL, "fitting GEMM operand not 16-byte aligned");
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)kKC, (cuuint32_t)box_rows};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(base), dims, strides, box,
+                         es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(DPGB_ECUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return DPGB_OK;
+}
+
 template <int BN, int S>
 int launch_t(const FitGemm& g, int* err, cudaStream_t st) {
-  const size_t smem = (size_t)S * (128 + BN) * kKC * 2;
+  const size_t smem = (size_t)S * (128 + BN) * kKC * 2 + 1024;  // + alignment slack
   static bool attr = false;
   if (!attr) {
     DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel<BN, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
+  CUtensorMap ta, tb;
+  DPGB_TRY(encode_bf16_2d(&ta, g.A, g.row0[g.ntypes], g.K, g.lda, 128));
+  DPGB_TRY(encode_bf16_2d(&tb, g.B, g.ntypes * g.N, g.K, g.K, BN));
   dim3 grid(g.tile0[g.ntypes], ceil_div(g.N, BN));
-  fit_gemm_kernel<BN, S><<<grid, 128, smem, st>>>(g, err);
+  fit_gemm_kernel<BN, S><<<grid, 128, smem, st>>>(ta, tb, g, err);
   return check_launch("fit_gemm");
 }
 

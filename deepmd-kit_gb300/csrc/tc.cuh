@@ -39,6 +39,39 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
+// Descriptor of a K-major operand written by TMA with 128-byte swizzling:
+// rows of 64 bf16 (128 bytes) whose 16-byte chunks are XOR-permuted by the
+// row index mod 8, 8-row groups 1024 bytes apart (the stride byte offset;
+// the leading offset is unused for swizzled K-major operands), swizzle mode
+// 2 at [61,64).  The tile base must be 1024-byte aligned; the K = 16 steps
+// inside a 64-wide row advance the start address by 32 bytes.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// --- TMA ----------------------------------------------------------------------
+// 2D tiled load of the box at (x, y) (x: innermost, in elements; x * element
+// size a multiple of 16 bytes) into shared memory; completion counted on bar
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void* tmap, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+// arrive on bar and add `bytes` to the transaction count its phase waits for
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// mbarrier initialisation visible to the async proxy (TMA, tensor core)
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
 // instruction descriptor of kind::f16: D f32, A and B bf16, both K-major,
 // N>>3 at [17,23), M>>4 at [24,29)
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
