@@ -60,101 +60,171 @@ __global__ void model_keys_kernel(int* __restrict__ keys, const int* __restrict_
 }
 
 // F[row] = sum_slots g[row] - sum_{pairs -> row} g;  optional atomic virial on
-// the neighbour: -sum_{pairs -> row} g (x) d
+// the neighbour: -sum_{pairs -> row} g (x) d.  One warp per atom: lanes take
+// the atom's slots and its transposed pairs in a fixed interleave (partial
+// sums in GatherAcc), then a fixed xor-shuffle tree (identical in every
+// lane), so the result is the same on every run.
+constexpr int kGatherWarps = 4;
+
+// Force accumulators of the gathers.  FP64 gradients add in FP64.  FP32
+// gradients add in FP32 as an unevaluated sum hi + lo kept exact by the
+// two-sum transformation (Knuth), which is as accurate as FP64 accumulation
+// of FP32 terms here and stays off the (narrow) FP64 pipe.
 template <typename T>
-__global__ void force_gather_model_kernel(double* __restrict__ force, double* __restrict__ atom_vir,
-                                          const T* __restrict__ g, Transpose tr, const int* __restrict__ nlist,
-                                          const double* __restrict__ coord, const double* __restrict__ svec,
-                                          int nshift, int nloc, int nnei, int nrows) {
-  const int row = blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= nrows) return;
-  double f[3] = {0, 0, 0};
-  const T* gr = g + (size_t)row * nnei * 3;
-  const int* nr = nlist + (size_t)row * nnei;
-  for (int s = 0; s < nnei; ++s) {
-    if (nr[s] < 0) continue;  // padding slots carry no force (and may be unwritten)
-    f[0] += (double)gr[3 * s];
-    f[1] += (double)gr[3 * s + 1];
-    f[2] += (double)gr[3 * s + 2];
+struct GatherAcc {
+  double v[3] = {0.0, 0.0, 0.0};
+  __device__ __forceinline__ void add(int c, T x) { v[c] += (double)x; }
+  __device__ __forceinline__ void reduce() {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
   }
+  __device__ __forceinline__ double get(int c) const { return v[c]; }
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+template <>
+struct GatherAcc<float> {
+  float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
+  __device__ __forceinline__ void add(int c, float x) {
+    float e;
+    two_sum(hi[c], x, hi[c], e);
+    lo[c] += e;
+  }
+  __device__ __forceinline__ void reduce() {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, hi[c], o), ol = __shfl_xor_sync(0xffffffffu, lo[c], o);
+        float e;
+        two_sum(hi[c], oh, hi[c], e);
+        lo[c] += ol + e;
+      }
+  }
+  __device__ __forceinline__ double get(int c) const { return (double)hi[c] + (double)lo[c]; }
+};
+
+// the atom's own slots
+template <typename T>
+__device__ __forceinline__ void gather_own_slots(GatherAcc<T>& f, const T* __restrict__ gr,
+                                                 const int* __restrict__ nr, int nnei, int lane) {
+  for (int s = lane; s < nnei; s += 32) {
+    if (nr[s] < 0) continue;  // padding slots carry no force (and may be unwritten)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) f.add(c, gr[3 * s + c]);
+  }
+}
+
+// the transposed pairs of an atom (pairs whose neighbour it is), four per
+// lane at a time: the pair ids first, then their gradients, so that each
+// lane keeps several independent gathers in flight
+template <typename T, bool AV, typename Disp>
+__device__ __forceinline__ void gather_transposed(GatherAcc<T>& f, double av[9], const T* __restrict__ g,
+                                                  const Transpose& tr, int a, int lane, Disp disp) {
+  const int t1 = tr.offsets[a + 1];
+  for (int base = tr.offsets[a]; base < t1; base += 128) {
+    int pp[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int t = base + lane + 32 * k;
+      pp[k] = t < t1 ? tr.pairs[t] : -1;
+    }
+    T gv[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gv[k][c] = pp[k] >= 0 ? g[3 * (size_t)pp[k] + c] : T(0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (pp[k] < 0) continue;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f.add(c, -gv[k][c]);
+      if (AV) {
+        double d[3];
+        disp(pp[k], d);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int l = 0; l < 3; ++l) av[3 * i + l] -= (double)gv[k][i] * d[l];
+      }
+    }
+  }
+}
+
+template <typename T, bool AV>
+__device__ __forceinline__ void gather_store(double* __restrict__ force, double* __restrict__ atom_vir, size_t a,
+                                             GatherAcc<T>& f, double av[9], int lane) {
+  f.reduce();
+  if (AV)
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) av[k] += __shfl_xor_sync(0xffffffffu, av[k], o);
+  if (lane == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) force[3 * a + c] = f.get(c);
+    if (AV)
+#pragma unroll
+      for (int k = 0; k < 9; ++k) atom_vir[9 * a + k] = av[k];
+  }
+}
+
+template <typename T, bool AV>
+__global__ void __launch_bounds__(kGatherWarps * 32)
+force_gather_model_kernel(double* __restrict__ force, double* __restrict__ atom_vir, const T* __restrict__ g,
+                          Transpose tr, const int* __restrict__ nlist, const double* __restrict__ coord,
+                          const double* __restrict__ svec, int nshift, int nloc, int nnei, int nrows) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * kGatherWarps + (threadIdx.x >> 5);
+  if (row >= nrows) return;
+  GatherAcc<T> f;
+  gather_own_slots(f, g + (size_t)row * nnei * 3, nlist + (size_t)row * nnei, nnei, lane);
   double av[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) av[k] = 0.0;
-  for (int t = tr.offsets[row]; t < tr.offsets[row + 1]; ++t) {
-    const int p = tr.pairs[t];
-    const double g0 = (double)g[3 * (size_t)p], g1 = (double)g[3 * (size_t)p + 1], g2 = (double)g[3 * (size_t)p + 2];
-    f[0] -= g0;
-    f[1] -= g1;
-    f[2] -= g2;
-    if (atom_vir) {
-      const int prow = p / nnei;
-      const int fr = prow / nloc, i = prow - fr * nloc;
-      const int nb = nlist[p];
-      const int s = nb / nloc, jj = nb - s * nloc;
-      const double* cf = coord + (size_t)fr * nloc * 3;
-      const double* sv = svec + ((size_t)fr * nshift + s) * 3;
-      const double d[3] = {(cf[3 * jj] + sv[0]) - cf[3 * i], (cf[3 * jj + 1] + sv[1]) - cf[3 * i + 1],
-                           (cf[3 * jj + 2] + sv[2]) - cf[3 * i + 2]};
-      const double gg[3] = {g0, g1, g2};
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int l = 0; l < 3; ++l) av[3 * k + l] -= gg[k] * d[l];
-    }
-  }
-  force[3 * (size_t)row] = f[0];
-  force[3 * (size_t)row + 1] = f[1];
-  force[3 * (size_t)row + 2] = f[2];
-  if (atom_vir)
-#pragma unroll
-    for (int k = 0; k < 9; ++k) atom_vir[9 * (size_t)row + k] = av[k];
+  gather_transposed<T, AV>(f, av, g, tr, row, lane, [&](int p, double d[3]) {
+    const int prow = p / nnei;
+    const int fr = prow / nloc, i = prow - fr * nloc;
+    const int nb = nlist[p];
+    const int s = nb / nloc, jj = nb - s * nloc;
+    const double* cf = coord + (size_t)fr * nloc * 3;
+    const double* sv = svec + ((size_t)fr * nshift + s) * 3;
+    d[0] = (cf[3 * jj] + sv[0]) - cf[3 * i];
+    d[1] = (cf[3 * jj + 1] + sv[1]) - cf[3 * i + 1];
+    d[2] = (cf[3 * jj + 2] + sv[2]) - cf[3 * i + 2];
+  });
+  gather_store<T, AV>(force, atom_vir, (size_t)row, f, av, lane);
 }
 
 // The same with explicit extended atoms (external list, one frame): every one
 // of the nall atoms gets its force and atomic virial (the caller sums ghost
 // entries back onto their owners, as LAMMPS's reverse communication does).
-template <typename T>
-__global__ void force_gather_ext_kernel(double* __restrict__ force, double* __restrict__ atom_vir,
-                                        const T* __restrict__ g, Transpose tr, const int* __restrict__ nlist,
-                                        const double* __restrict__ coord_ext, int nloc, int nall, int nnei) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+template <typename T, bool AV>
+__global__ void __launch_bounds__(kGatherWarps * 32)
+force_gather_ext_kernel(double* __restrict__ force, double* __restrict__ atom_vir, const T* __restrict__ g,
+                        Transpose tr, const int* __restrict__ nlist, const double* __restrict__ coord_ext, int nloc,
+                        int nall, int nnei) {
+  const int lane = threadIdx.x & 31;
+  const int e = blockIdx.x * kGatherWarps + (threadIdx.x >> 5);
   if (e >= nall) return;
-  double f[3] = {0, 0, 0};
-  if (e < nloc) {
-    const T* gr = g + (size_t)e * nnei * 3;
-    const int* nr = nlist + (size_t)e * nnei;
-    for (int s = 0; s < nnei; ++s) {
-      if (nr[s] < 0) continue;
-      f[0] += (double)gr[3 * s];
-      f[1] += (double)gr[3 * s + 1];
-      f[2] += (double)gr[3 * s + 2];
-    }
-  }
+  GatherAcc<T> f;
+  if (e < nloc) gather_own_slots(f, g + (size_t)e * nnei * 3, nlist + (size_t)e * nnei, nnei, lane);
   double av[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) av[k] = 0.0;
-  for (int t = tr.offsets[e]; t < tr.offsets[e + 1]; ++t) {
-    const int p = tr.pairs[t];
-    const double gg[3] = {(double)g[3 * (size_t)p], (double)g[3 * (size_t)p + 1], (double)g[3 * (size_t)p + 2]};
-    f[0] -= gg[0];
-    f[1] -= gg[1];
-    f[2] -= gg[2];
-    if (atom_vir) {
-      const int i = p / nnei;
-      const double d[3] = {coord_ext[3 * e] - coord_ext[3 * i], coord_ext[3 * e + 1] - coord_ext[3 * i + 1],
-                           coord_ext[3 * e + 2] - coord_ext[3 * i + 2]};
+  gather_transposed<T, AV>(f, av, g, tr, e, lane, [&](int p, double d[3]) {
+    const int i = p / nnei;
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int l = 0; l < 3; ++l) av[3 * k + l] -= gg[k] * d[l];
-    }
-  }
-  force[3 * (size_t)e] = f[0];
-  force[3 * (size_t)e + 1] = f[1];
-  force[3 * (size_t)e + 2] = f[2];
-  if (atom_vir)
-#pragma unroll
-    for (int k = 0; k < 9; ++k) atom_vir[9 * (size_t)e + k] = av[k];
+    for (int l = 0; l < 3; ++l) d[l] = coord_ext[3 * e + l] - coord_ext[3 * i + l];
+  });
+  gather_store<T, AV>(force, atom_vir, (size_t)e, f, av, lane);
 }
 
 // batch of frames: the key of a pair is its neighbour's global atom
@@ -174,53 +244,30 @@ __global__ void batch_keys_kernel(int* __restrict__ keys, const int* __restrict_
 }
 
 // force_gather_model_kernel for a batch (per-frame image shifts)
-template <typename T>
-__global__ void force_gather_batch_kernel(double* __restrict__ force, double* __restrict__ atom_vir,
-                                          const T* __restrict__ g, Transpose tr, const int* __restrict__ nlist,
-                                          const double* __restrict__ coord, const double* __restrict__ svec,
-                                          FrameTab ft, int nnei, int nrows) {
-  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+template <typename T, bool AV>
+__global__ void __launch_bounds__(kGatherWarps * 32)
+force_gather_batch_kernel(double* __restrict__ force, double* __restrict__ atom_vir, const T* __restrict__ g,
+                          Transpose tr, const int* __restrict__ nlist, const double* __restrict__ coord,
+                          const double* __restrict__ svec, FrameTab ft, int nnei, int nrows) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * kGatherWarps + (threadIdx.x >> 5);
   if (row >= nrows) return;
-  double f[3] = {0, 0, 0};
-  const T* gr = g + (size_t)row * nnei * 3;
-  const int* nr = nlist + (size_t)row * nnei;
-  for (int s = 0; s < nnei; ++s) {
-    if (nr[s] < 0) continue;
-    f[0] += (double)gr[3 * s];
-    f[1] += (double)gr[3 * s + 1];
-    f[2] += (double)gr[3 * s + 2];
-  }
+  GatherAcc<T> f;
+  gather_own_slots(f, g + (size_t)row * nnei * 3, nlist + (size_t)row * nnei, nnei, lane);
   double av[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) av[k] = 0.0;
-  for (int t = tr.offsets[row]; t < tr.offsets[row + 1]; ++t) {
-    const int p = tr.pairs[t];
-    const double g0 = (double)g[3 * (size_t)p], g1 = (double)g[3 * (size_t)p + 1], g2 = (double)g[3 * (size_t)p + 2];
-    f[0] -= g0;
-    f[1] -= g1;
-    f[2] -= g2;
-    if (atom_vir) {
-      const int i = p / nnei;  // centre (global row)
-      const int fr = frame_of(ft.atom_off, ft.nframes, i);
-      const int beg = ft.atom_off[fr], nl = ft.atom_off[fr + 1] - beg;
-      const int nb = nlist[p];
-      const int s = nb / nl, jj = beg + (nb - s * nl);
-      const double* sv = svec + 3 * ((size_t)ft.svec_off[fr] + s);
-      const double d[3] = {(coord[3 * jj] + sv[0]) - coord[3 * i], (coord[3 * jj + 1] + sv[1]) - coord[3 * i + 1],
-                           (coord[3 * jj + 2] + sv[2]) - coord[3 * i + 2]};
-      const double gg[3] = {g0, g1, g2};
+  gather_transposed<T, AV>(f, av, g, tr, row, lane, [&](int p, double d[3]) {
+    const int i = p / nnei;  // centre (global row)
+    const int fr = frame_of(ft.atom_off, ft.nframes, i);
+    const int beg = ft.atom_off[fr], nl = ft.atom_off[fr + 1] - beg;
+    const int nb = nlist[p];
+    const int s = nb / nl, jj = beg + (nb - s * nl);
+    const double* sv = svec + 3 * ((size_t)ft.svec_off[fr] + s);
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int l = 0; l < 3; ++l) av[3 * k + l] -= gg[k] * d[l];
-    }
-  }
-  force[3 * (size_t)row] = f[0];
-  force[3 * (size_t)row + 1] = f[1];
-  force[3 * (size_t)row + 2] = f[2];
-  if (atom_vir)
-#pragma unroll
-    for (int k = 0; k < 9; ++k) atom_vir[9 * (size_t)row + k] = av[k];
+    for (int l = 0; l < 3; ++l) d[l] = (coord[3 * jj + l] + sv[l]) - coord[3 * i + l];
+  });
+  gather_store<T, AV>(force, atom_vir, (size_t)row, f, av, lane);
 }
 
 // Per-frame sums of the atom energies and atom virials in two passes with a
@@ -1107,16 +1154,28 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   dp.mark(DPGB_STAGE_DESC_BWD, 1, st);
   dp.mark(DPGB_STAGE_REDUCE, 0, st);
   if (ext) {
-    force_gather_ext_kernel<T><<<ceil_div(nkeys, 128), 128, 0, st>>>(force, atom_virial, dp.ws_g.as<T>(), tr, nlist,
-                                                                       ext->coord, natom, ext->nall, nnei);
+    if (atom_virial)
+      force_gather_ext_kernel<T, true><<<ceil_div(nkeys, kGatherWarps), kGatherWarps * 32, 0, st>>>(
+          force, atom_virial, dp.ws_g.as<T>(), tr, nlist, ext->coord, natom, ext->nall, nnei);
+    else
+      force_gather_ext_kernel<T, false><<<ceil_div(nkeys, kGatherWarps), kGatherWarps * 32, 0, st>>>(
+          force, nullptr, dp.ws_g.as<T>(), tr, nlist, ext->coord, natom, ext->nall, nnei);
   } else if (batch) {
-    force_gather_batch_kernel<T><<<ceil_div(nrows, 128), 128, 0, st>>>(force, atom_virial, dp.ws_g.as<T>(), tr, nlist,
-                                                                         coord_n, batch->svec, batch->ft, nnei,
-                                                                         (int)nrows);
+    if (atom_virial)
+      force_gather_batch_kernel<T, true><<<ceil_div(nrows, kGatherWarps), kGatherWarps * 32, 0, st>>>(
+          force, atom_virial, dp.ws_g.as<T>(), tr, nlist, coord_n, batch->svec, batch->ft, nnei, (int)nrows);
+    else
+      force_gather_batch_kernel<T, false><<<ceil_div(nrows, kGatherWarps), kGatherWarps * 32, 0, st>>>(
+          force, nullptr, dp.ws_g.as<T>(), tr, nlist, coord_n, batch->svec, batch->ft, nnei, (int)nrows);
   } else {
-    force_gather_model_kernel<T><<<ceil_div(nrows, 128), 128, 0, st>>>(
-        force, atom_virial, dp.ws_g.as<T>(), tr, nlist, coord_n, dp.ws_svec.as<double>(), nshift_max, natom, nnei,
-        (int)nrows);
+    if (atom_virial)
+      force_gather_model_kernel<T, true><<<ceil_div(nrows, kGatherWarps), kGatherWarps * 32, 0, st>>>(
+          force, atom_virial, dp.ws_g.as<T>(), tr, nlist, coord_n, dp.ws_svec.as<double>(), nshift_max, natom, nnei,
+          (int)nrows);
+    else
+      force_gather_model_kernel<T, false><<<ceil_div(nrows, kGatherWarps), kGatherWarps * 32, 0, st>>>(
+          force, nullptr, dp.ws_g.as<T>(), tr, nlist, coord_n, dp.ws_svec.as<double>(), nshift_max, natom, nnei,
+          (int)nrows);
   }
   DPGB_TRY(check_launch("force_gather"));
   ++launches;
