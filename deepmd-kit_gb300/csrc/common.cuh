@@ -60,6 +60,32 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// Exact sum of two floats as s + e (Knuth's two-sum; needs IEEE order of
+// operations, which holds without fast-math).  Sums of FP32 terms kept as
+// hi + lo this way are as accurate as FP64 accumulation and use the FP32
+// pipe, not the (narrow) FP64 one.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void comp_add(float& hi, float& lo, float x) {
+  float e;
+  two_sum(hi, x, hi, e);
+  lo += e;
+}
+// warp-wide compensated sum (xor tree: the same value in every lane)
+__device__ __forceinline__ double warp_comp_sum(float hi, float lo) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    float e;
+    two_sum(hi, oh, hi, e);
+    lo += ol + e;
+  }
+  return (double)hi + (double)lo;
+}
+
 // Scoped device allocation used by op-level entry points (workspace).
 struct DeviceBuffer {
   void* ptr = nullptr;

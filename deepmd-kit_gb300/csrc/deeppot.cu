@@ -83,20 +83,10 @@ struct GatherAcc {
   __device__ __forceinline__ double get(int c) const { return v[c]; }
 };
 
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
 template <>
 struct GatherAcc<float> {
   float hi[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
-  __device__ __forceinline__ void add(int c, float x) {
-    float e;
-    two_sum(hi[c], x, hi[c], e);
-    lo[c] += e;
-  }
+  __device__ __forceinline__ void add(int c, float x) { comp_add(hi[c], lo[c], x); }
   __device__ __forceinline__ void reduce() {
 #pragma unroll
     for (int c = 0; c < 3; ++c)

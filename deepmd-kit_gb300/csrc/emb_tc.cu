@@ -831,9 +831,9 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         if (!alive) break;
         for (int q = tid; q < ntile * 9; q += blockDim.x) {
           const int k = q / 9, comp = q - 9 * k;
-          double s = 0.0;
-          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) s += (double)sVir[pp * 9 + comp];
-          vir_row[(size_t)s_row[k] * 9 + comp] += s;
+          float hi = 0.f, lo = 0.f;  // compensated FP32 sum (the FP64 pipe is narrow)
+          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) comp_add(hi, lo, sVir[pp * 9 + comp]);
+          vir_row[(size_t)s_row[k] * 9 + comp] += (double)hi + (double)lo;
         }
         __syncthreads();
       }

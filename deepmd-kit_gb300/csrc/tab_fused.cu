@@ -220,9 +220,9 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ 
   const float* dr = dxyz + (size_t)row * 4 * ng;
   for (int n = lane; n < ng; n += 32) sdx[n] = reinterpret_cast<const float4*>(dr)[n];  // dxyz is [row][ng][4]
   __syncwarp();
-  double vir[9];
+  float vir_hi[9], vir_lo[9];  // compensated FP32 sums
 #pragma unroll
-  for (int k = 0; k < 9; ++k) vir[k] = 0.0;
+  for (int k = 0; k < 9; ++k) vir_hi[k] = vir_lo[k] = 0.f;
   float* gp_row = gpair + (size_t)row * p.nnei * 3;
   for (int sec = 0; sec < p.ntypes; ++sec) {
     const int net = p.type_one_side ? sec : sec * p.ntypes + ti;
@@ -274,7 +274,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ 
 #pragma unroll
           for (int k = 0; k < 3; ++k)
 #pragma unroll
-            for (int l = 0; l < 3; ++l) vir[3 * k + l] += (double)(-g[k] * s.d[l]);
+            for (int l = 0; l < 3; ++l) comp_add(vir_hi[3 * k + l], vir_lo[3 * k + l], -g[k] * s.d[l]);
         }
         gp_row[3 * slot] = g[0];
         gp_row[3 * slot + 1] = g[1];
@@ -284,9 +284,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ 
   }
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
-    double v = vir[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const double v = warp_comp_sum(vir_hi[k], vir_lo[k]);
     if (lane == 0) vir_row[(size_t)row * 9 + k] = v;
   }
 }
