@@ -313,6 +313,22 @@ __global__ void frame_final_kernel(double* __restrict__ energy, double* __restri
     virial[(size_t)f * 9 + q - 1] = v;
 }
 
+// FP32 split x = hi + lo of n points (FP64 xyz), for FP32 displacements
+__global__ void split_points_kernel(float4* __restrict__ hi, float4* __restrict__ lo, const double* __restrict__ x,
+                                   int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float h[3], l[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double v = x[3 * (size_t)i + k];
+    h[k] = (float)v;
+    l[k] = (float)(v - (double)h[k]);
+  }
+  hi[i] = make_float4(h[0], h[1], h[2], 0.f);
+  lo[i] = make_float4(l[0], l[1], l[2], 0.f);
+}
+
 // atom energy in the original order (+ per-type bias), 0 for virtual atoms
 __global__ void atom_energy_kernel(double* __restrict__ e_row, const double* __restrict__ e_sorted,
                                    const int* __restrict__ row_pos, const int* __restrict__ atype,
@@ -359,7 +375,7 @@ struct DeepPotImpl {
   DeviceBuffer fit_w16, fit_f32, ws_fitb;
   // workspace
   DeviceBuffer ws_nlist, ws_cell, ws_tr, ws_keys, ws_status, ws_coord, ws_svec, ws_spos;
-  DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf, ws_part;
+  DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf, ws_part, ws_xhi, ws_xlo, ws_shi, ws_slo;
   DeviceBuffer io_coord, io_force, io_av, io_e, io_v, io_ae;
   // external neighbour list (CSR over local atoms) kept between calls for
   // `ago` > 0, with the ghost-inclusive types
@@ -790,6 +806,7 @@ struct BatchIn {
   const double* svec;
   const int* spos;
   int max_atoms;  // atoms of the largest frame
+  int nsvec;      // shift vectors of all frames
 };
 
 template <typename T>
@@ -1056,6 +1073,32 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     p.frame_atom_off = batch->ft.atom_off;
     p.frame_svec_off = batch->ft.svec_off;
     p.nframes_batch = batch->ft.nframes;
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 splits of the coordinates and shifts: the mixed form's
+    // displacements are taken without FP64 instructions
+    const int npts = ext ? ext->nall : (int)nrows;
+    const int nsv = ext ? 0 : (batch ? batch->nsvec : nshift_max * nframes);
+    const double* pts = ext ? ext->coord : coord_n;
+    const double* svs = batch ? batch->svec : dp.ws_svec.as<double>();
+    DPGB_TRY(dp.ws_xhi.alloc(sizeof(float4) * npts));
+    DPGB_TRY(dp.ws_xlo.alloc(sizeof(float4) * npts));
+    DPGB_TRY(dp.ws_shi.alloc(sizeof(float4) * std::max(nsv, 1)));
+    DPGB_TRY(dp.ws_slo.alloc(sizeof(float4) * std::max(nsv, 1)));
+    split_points_kernel<<<ceil_div(npts, 256), 256, 0, st>>>(dp.ws_xhi.as<float4>(), dp.ws_xlo.as<float4>(), pts,
+                                                             npts);
+    DPGB_TRY(check_launch("split_points"));
+    ++launches;
+    if (nsv > 0) {
+      split_points_kernel<<<ceil_div(nsv, 256), 256, 0, st>>>(dp.ws_shi.as<float4>(), dp.ws_slo.as<float4>(), svs,
+                                                              nsv);
+      DPGB_TRY(check_launch("split_points"));
+      ++launches;
+    }
+    p.xhi = dp.ws_xhi.as<float4>();
+    p.xlo = dp.ws_xlo.as<float4>();
+    p.shi = dp.ws_shi.as<float4>();
+    p.slo = dp.ws_slo.as<float4>();
   }
   // virtual rows have no sorted position: point them at row 0 only for
   // reading (the kernels never write a virtual row)
@@ -1383,6 +1426,7 @@ int batch_setup(BatchImpl& b, DeepPotImpl& dp, int nframes, const int* natoms, c
   b.in.svec = b.svec.as<double>();
   b.in.spos = b.spos.as<int>();
   b.in.max_atoms = *std::max_element(natoms, natoms + nframes);
+  b.in.nsvec = (int)(svec_all.size() / 3);
   return DPGB_OK;
 }
 

@@ -222,11 +222,7 @@ __device__ __forceinline__ void pair_env(const DescParams<float>& p, int t, int 
   const float* sd = p.dstd + ((size_t)ti * p.nnei + pi.slot) * 4;
   float e4[4] = {0.f, 0.f, 0.f, 0.f};
   if (pi.nb >= 0) {
-    double dd[3];
-    const int tj = pair_disp(p, f, i, pi.nb, dd);
-    dvec[0] = (float)dd[0];
-    dvec[1] = (float)dd[1];
-    dvec[2] = (float)dd[2];
+    const int tj = pair_disp_f(p, f, i, pi.nb, dvec);
     pi.keep = p.pair_mask ? p.pair_mask[ti * p.ntypes + tj] : 1;
     if (pi.keep) {
       const float nr2 = dvec[0] * dvec[0] + dvec[1] * dvec[1] + dvec[2] * dvec[2];

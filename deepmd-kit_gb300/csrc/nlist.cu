@@ -61,6 +61,24 @@ static void face_distances(const CellGeom& g, double face[3]) {
   face[2] = vol / cr(0, 1);
 }
 
+// Error bound of the staged FP32 distances of a list of radius R: a stencil
+// atom lies within (reach_k + 1/2) cell edges of the centre cell's centre
+// along each cell vector k, so its coordinates relative to that centre are
+// below m = sum_k (reach_k + 1/2) |a_k| / n_k; each is rounded to FP32
+// (<= 2^-24 m, doubled for margin: u); a displacement component then errs
+// by <= 2 u + 2^-24 R and the FP32 norm adds <= 2^-22 R.
+static float staged_eps(const CellGeom& g, double R) {
+  double m = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    const double edge = g.periodic ? std::sqrt(g.cell[3 * k] * g.cell[3 * k] + g.cell[3 * k + 1] * g.cell[3 * k + 1] +
+                                               g.cell[3 * k + 2] * g.cell[3 * k + 2]) / g.ncell[k]
+                                   : g.csize[k];
+    m += (g.reach[k] + 0.5) * edge;
+  }
+  const double u = m * 0x1p-23;
+  return (float)(1.7320508075688772 * (2.0 * u + R * 0x1p-24) + R * 0x1p-22 + 1e-7);
+}
+
 int periodic_geom(const double* box, double rcut, int nshift, const int* shift_idx, CellGeom& g,
                   std::vector<int>& shift_pos) {
   DPGB_TRY(box_geom(box, g));
@@ -98,6 +116,7 @@ int periodic_geom(const double* box, double rcut, int nshift, const int* shift_i
     if (tx == 0 && ty == 0 && tz == 0) g.zero_shift = s;
   }
   g.nshift = nshift;
+  g.eps = staged_eps(g, rcut);
   return DPGB_OK;
 }
 
@@ -127,6 +146,7 @@ int open_geom(const double* coord, int n, double rcut, CellGeom& g) {
   g.nshift = 1;
   g.zero_shift = 0;
   g.periodic = 0;
+  g.eps = staged_eps(g, rcut);
   return DPGB_OK;
 }
 
@@ -604,24 +624,6 @@ __device__ int exact_keep(double* __restrict__ wr, int* __restrict__ wi, int* __
   return n;
 }
 
-// Error bound of the staged FP32 distances: a stencil atom lies within
-// (reach_k + 1/2) cell edges of the centre cell's centre along each cell
-// vector k, so its coordinates relative to that centre are below
-// m = sum_k (reach_k + 1/2) |a_k| / n_k; each is rounded to FP32 (<= 2^-24 m,
-// doubled for margin: u); a displacement component then errs by
-// <= 2 u + 2^-24 R and the FP32 norm adds <= 2^-22 R (R: the list radius).
-__device__ __forceinline__ float staged_eps(const CellGeom& g, double R) {
-  double m = 0.0;
-  for (int k = 0; k < 3; ++k) {
-    const double edge = g.periodic ? sqrt(g.cell[3 * k] * g.cell[3 * k] + g.cell[3 * k + 1] * g.cell[3 * k + 1] +
-                                          g.cell[3 * k + 2] * g.cell[3 * k + 2]) / g.ncell[k]
-                                   : g.csize[k];
-    m += (g.reach[k] + 0.5) * edge;
-  }
-  const double u = m * 0x1p-23;
-  return (float)(1.7320508075688772 * (2.0 * u + R * 0x1p-24) + R * 0x1p-22 + 1e-7);
-}
-
 // centre of cell (cx, cy, cz)
 __device__ __forceinline__ void cell_centre(const CellGeom& g, int cx, int cy, int cz, double o[3]) {
   if (g.periodic) {
@@ -731,6 +733,7 @@ nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
   int* ktype = kidx + kCellWarps * kept_cap;
   __shared__ int s_cell[27], s_shift[27], s_off[28];
   __shared__ int s_tb[kCellWarps][DPGB_MAX_TYPES];  // per-type running counts of sort_place_f32
+  __shared__ double s_oc[3];
   const int c = blockIdx.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int cz = c % g.ncell[2], cy = (c / g.ncell[2]) % g.ncell[1], cx = c / (g.ncell[1] * g.ncell[2]);
@@ -757,11 +760,11 @@ nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
     return;
   }
   // FP32 copies relative to the centre cell's centre (magnitudes within 1.5
-  // cell diagonals: the rounding bound of staged_eps)
-  double oc[3];
-  cell_centre(g, cx, cy, cz, oc);
-  const double ox = oc[0], oy = oc[1], oz = oc[2];
-  const float eps = staged_eps(g, rcut);
+  // cell diagonals: the rounding bound g.eps)
+  if (tid == 0) cell_centre(g, cx, cy, cz, s_oc);
+  __syncthreads();
+  const double ox = s_oc[0], oy = s_oc[1], oz = s_oc[2];
+  const float eps = g.eps;
   for (int q = tid; q < total; q += blockDim.x) {
     int k = 0;
     while (s_off[k + 1] <= q) ++k;
@@ -1105,6 +1108,7 @@ nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coor
   // thinner than rcut across a face has one cell and reach 2 there)
   __shared__ int s_cell[125], s_shift[125], s_off[126];
   __shared__ int s_tb[kCellWarps][DPGB_MAX_TYPES];
+  __shared__ double s_oc[3];
   const int cg = blockIdx.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int fr = frame_of(ft.cell_off, ft.nframes, cg);
@@ -1142,10 +1146,10 @@ nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coor
     }
     return;
   }
-  double oc[3];
-  cell_centre(g, cx, cy, cz, oc);
-  const double ox = oc[0], oy = oc[1], oz = oc[2];
-  const float eps = staged_eps(g, rcut);
+  if (tid == 0) cell_centre(g, cx, cy, cz, s_oc);
+  __syncthreads();
+  const double ox = s_oc[0], oy = s_oc[1], oz = s_oc[2];
+  const float eps = g.eps;
   for (int q = tid; q < total; q += blockDim.x) {
     int lo = 0, hi = nst;  // s_off[lo] <= q < s_off[hi]
     while (hi - lo > 1) {

@@ -24,6 +24,7 @@ struct CellGeom {
   int nshift;
   int zero_shift;     // position of the (0,0,0) image
   int periodic;
+  float eps;          // error bound of the staged FP32 distances (staged_eps)
 };
 
 struct SelInfo {

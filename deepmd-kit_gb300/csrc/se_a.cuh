@@ -97,7 +97,25 @@ struct DescParams {
   const int* frame_atom_off;
   const int* frame_svec_off;
   int nframes_batch;
+  // FP32 split (x = hi + lo) of the coordinates ([nrows], or [nframes, nall]
+  // with coord_ext) and of the shift vectors (as svec), for FP32
+  // displacements (pair_disp_f); NULL: displacements in FP64
+  const float4* xhi;
+  const float4* xlo;
+  const float4* shi;
+  const float4* slo;
 };
+
+// (a + s) - b in FP32 from hi + lo splits of each term: two error-free sums
+// (two_sum) carry the rounding of the high parts into the low-order part,
+// so the result is the exact value rounded once more (FP32 instructions
+// only; the FP64 pipe is narrow on this part)
+__device__ __forceinline__ float disp_split(float ah, float al, float sh, float sl, float bh, float bl) {
+  float s1, e1, s2, e2;
+  two_sum(ah, sh, s1, e1);
+  two_sum(s1, -bh, s2, e2);
+  return s2 + (((al + sl) - bl) + (e1 + e2));
+}
 
 // r_nb - r_i in FP64 for neighbour nb of local atom i of frame f, and the
 // neighbour's type.  Image-major indices: r_nb = coord[nb % nloc] + shift.
@@ -127,6 +145,50 @@ __device__ __forceinline__ int pair_disp(const DescParams<T>& p, int f, int i, i
   d[1] = (cf[3 * jj + 1] + sv[1]) - cf[3 * i + 1];
   d[2] = (cf[3 * jj + 2] + sv[2]) - cf[3 * i + 2];
   return p.atype[jj];
+}
+
+// pair_disp rounded to FP32: from the FP32 splits when the params carry
+// them, else from the FP64 displacement
+template <typename T>
+__device__ __forceinline__ int pair_disp_f(const DescParams<T>& p, int f, int i, int nb, float d[3]) {
+  if (!p.xhi) {
+    double dd[3];
+    const int t = pair_disp(p, f, i, nb, dd);
+    d[0] = (float)dd[0];
+    d[1] = (float)dd[1];
+    d[2] = (float)dd[2];
+    return t;
+  }
+  size_t aj, ai, sv = 0;
+  bool shift = true;
+  int t;
+  if (p.coord_ext) {
+    aj = (size_t)f * p.nall + nb;
+    ai = (size_t)f * p.nall + i;
+    shift = false;
+    t = p.atype_ext[aj];
+  } else if (p.frame_atom_off) {
+    const int fr = frame_of(p.frame_atom_off, p.nframes_batch, i);
+    const int beg = p.frame_atom_off[fr], nl = p.frame_atom_off[fr + 1] - beg;
+    const int s = nb / nl, jj = beg + (nb - s * nl);
+    aj = jj;
+    ai = i;
+    sv = (size_t)p.frame_svec_off[fr] + s;
+    t = p.atype[jj];
+  } else {
+    const int s = nb / p.nloc, jj = nb - s * p.nloc;
+    aj = (size_t)f * p.nloc + jj;
+    ai = (size_t)f * p.nloc + i;
+    sv = (size_t)f * p.nshift + s;
+    t = p.atype[jj];
+  }
+  const float4 jh = p.xhi[aj], jl = p.xlo[aj], ih = p.xhi[ai], il = p.xlo[ai];
+  const float4 sh = shift ? p.shi[sv] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 sl = shift ? p.slo[sv] : make_float4(0.f, 0.f, 0.f, 0.f);
+  d[0] = disp_split(jh.x, jl.x, sh.x, sl.x, ih.x, il.x);
+  d[1] = disp_split(jh.y, jl.y, sh.y, sl.y, ih.y, il.y);
+  d[2] = disp_split(jh.z, jl.z, sh.z, sl.z, ih.z, il.z);
+  return t;
 }
 
 // Fitting nets of all types: W[l] [ntypes, nin_l, nout_l] ...

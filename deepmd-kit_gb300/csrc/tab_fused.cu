@@ -59,6 +59,8 @@ __device__ __forceinline__ void slot_env(const DescParams<float>& p, int row, in
   s.d[0] = s.d[1] = s.d[2] = 0.f;
   int keep = 1;
   if (s.nb >= 0) {
+    // FP64 displacement: these kernels are bound by the table reads, which
+    // the split coordinates' extra loads would add to
     double dd[3];
     const int tj = pair_disp(p, f, i, s.nb, dd);
     s.d[0] = (float)dd[0];
