@@ -382,6 +382,13 @@ def run_batch(args, world, rank, local):
     print(json.dumps(line))
 
 
+# DRAM bytes (read + write) per launch of each stage's tensor-core kernel on
+# the 12,288-atom water step, from one ncu capture (emb_tc_fwd, emb_tc_bwd,
+# the first fitting GEMM): profiles/emb_tc_water12288.md,
+# profiles/fit_gemm_water12288.md
+DRAM_BYTES_PER_LAUNCH = {"desc_fwd": 52.6e6, "desc_bwd": 27.2e6, "fitting": 41.9e6}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="water12k", choices=["water12k", "water98k-compressed", "alloy512-batch"])
@@ -516,7 +523,9 @@ def main():
             "parallelism": f"replicas x{world}",
         },
         "roofline": {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": DRAM_BYTES_PER_LAUNCH.get(dom),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's "
+                                       "tensor-core kernel, profiles/emb_tc_water12288.md",
                      "peak_source": f"{peak_kind} bf16_tflops", "algorithmic_flops_per_launch": flops[dom]},
         "cpu_baseline": cpu,
         "e2e": e2e,
