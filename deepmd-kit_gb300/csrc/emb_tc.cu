@@ -859,9 +859,99 @@ __global__ void run_len_kernel(int* __restrict__ run_len, const int* __restrict_
 
 // dE/dxyz (before the forward's 1/nnei): dxyz[n][c] = (sum_m dD[n][m] xyz[c][m]
 // + [n < M] sum_n' dD[n'][n] xyz[c][n']) / nnei, stored [row][ng][4] (one
-// float4 per neuron for the backward kernels).  One warp per row: the row's
-// xyz and dD are staged in shared memory with coalesced loads.
-__global__ void dxyz_kernel(float* __restrict__ dxyz, const float* __restrict__ dD, const float* __restrict__ xyz,
+// float4 per neuron for the backward kernels).  One warp per row, all in
+// registers: lane l owns neurons l + 32 k and their M = 16 entries of dD;
+// xyz[:, :M] is loaded by every lane (broadcast); the second term's 4 x M
+// partial sums are combined across the warp by a reduce-scatter of
+// shuffles (five halvings leave T[2l], T[2l+1] in lane l).
+constexpr int kDxyzM = 16, kDxyzWarps = 4;
+
+__global__ void __launch_bounds__(kDxyzWarps * 32)
+dxyz_kernel(float* __restrict__ dxyz, const float* __restrict__ dD, const float* __restrict__ xyz,
+            const int* __restrict__ row_pos, const int* __restrict__ atype, int nloc, int nrows, int ng, int nnei) {
+  constexpr int M = kDxyzM;
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * kDxyzWarps + (threadIdx.x >> 5);
+  if (row >= nrows) return;
+  float4* out = reinterpret_cast<float4*>(dxyz + (size_t)row * 4 * ng);
+  if (atype[row % nloc] < 0) {
+    for (int n = lane; n < ng; n += 32) out[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const float* xr = xyz + (size_t)row * 4 * ng;  // [c][n]
+  const float* d = dD + (size_t)row_pos[row] * ng * M;  // [n][m]
+  float xm[4][M];  // xyz[c][m], m < M
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+#pragma unroll
+    for (int m4 = 0; m4 < M; m4 += 4) {
+      const float4 q = *reinterpret_cast<const float4*>(xr + c * ng + m4);
+      xm[c][m4] = q.x;
+      xm[c][m4 + 1] = q.y;
+      xm[c][m4 + 2] = q.z;
+      xm[c][m4 + 3] = q.w;
+    }
+  float T[4 * M];  // partial sum_n' dD[n'][m] xyz[c][n'] over this lane's n', index c * M + m
+#pragma unroll
+  for (int q = 0; q < 4 * M; ++q) T[q] = 0.f;
+  const float inv = 1.f / (float)nnei;
+  float4 first = make_float4(0.f, 0.f, 0.f, 0.f);  // term 1 of neuron lane (< M), completed after the reduction
+  for (int n = lane; n < ng; n += 32) {
+    float dd[M];
+    const float4* dq = reinterpret_cast<const float4*>(d + (size_t)n * M);
+#pragma unroll
+    for (int m4 = 0; m4 < M / 4; ++m4) {
+      const float4 q = dq[m4];
+      dd[4 * m4] = q.x;
+      dd[4 * m4 + 1] = q.y;
+      dd[4 * m4 + 2] = q.z;
+      dd[4 * m4 + 3] = q.w;
+    }
+    float t1[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      float s = 0.f;
+#pragma unroll
+      for (int m = 0; m < M; ++m) s = fmaf(dd[m], xm[c][m], s);
+      t1[c] = s;
+      const float xn = xr[c * ng + n];
+#pragma unroll
+      for (int m = 0; m < M; ++m) T[c * M + m] = fmaf(dd[m], xn, T[c * M + m]);
+    }
+    if (n < M)
+      first = make_float4(t1[0], t1[1], t1[2], t1[3]);
+    else
+      out[n] = make_float4(t1[0] * inv, t1[1] * inv, t1[2] * inv, t1[3] * inv);
+  }
+  // reduce-scatter of T over the warp: at each halving a lane keeps the half
+  // its lane bit selects and adds the partner's copy of it
+#pragma unroll
+  for (int h = 32, o = 16; h >= 2; h >>= 1, o >>= 1) {
+    const bool upper = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < h; ++i) {
+      const float send = upper ? T[i] : T[i + h];
+      const float keep = upper ? T[i + h] : T[i];
+      T[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+  // lane l now holds T[2l] and T[2l + 1]; neuron n < M takes T[c * M + n]
+  float tc[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int q = c * M + (lane & (M - 1));
+    const float a0 = __shfl_sync(0xffffffffu, T[0], q >> 1), a1 = __shfl_sync(0xffffffffu, T[1], q >> 1);
+    tc[c] = (q & 1) ? a1 : a0;
+  }
+  if (lane < M && lane < ng)
+    out[lane] = make_float4((first.x + tc[0]) * inv, (first.y + tc[1]) * inv, (first.z + tc[2]) * inv,
+                            (first.w + tc[3]) * inv);
+}
+
+// The same for any axis width: one warp per row with the row's xyz and dD
+// staged in shared memory (dD transposed so lanes over n read consecutive
+// words).
+__global__ void dxyz_smem_kernel(float* __restrict__ dxyz, const float* __restrict__ dD, const float* __restrict__ xyz,
                             const int* __restrict__ row_pos, const int* __restrict__ atype, int nloc, int nrows,
                             int ng, int M, int nnei) {
   extern __shared__ float s_dx[];
@@ -960,13 +1050,18 @@ int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChun
 
 int launch_dxyz(const DescParams<float>& p, const float* dD, const float* xyz, float* dxyz, cudaStream_t st) {
   if (p.nrows <= 0) return DPGB_OK;
-  const size_t per_warp = sizeof(float) * ((size_t)4 * p.ng + (size_t)p.ng * p.axis + 4 * (size_t)p.axis);
+  if (p.axis == kDxyzM && p.ng % 4 == 0) {
+    dxyz_kernel<<<ceil_div(p.nrows, kDxyzWarps), kDxyzWarps * 32, 0, st>>>(dxyz, dD, xyz, p.row_pos, p.atype,
+                                                                          p.nloc, p.nrows, p.ng, p.nnei);
+    return check_launch("dxyz");
+  }
+  const int ng = p.ng, M = p.axis;
+  const size_t per_warp = sizeof(float) * (4 * ng + ng * M + 4 * M);
   int wpb = 8;
   while (wpb > 1 && per_warp * wpb > 96 * 1024) wpb >>= 1;
-  if (per_warp * wpb > 227 * 1024) return fail(DPGB_EINVAL, "dxyz: descriptor too wide for shared memory");
-  DPGB_CUDA(cudaFuncSetAttribute(dxyz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(per_warp * wpb)));
-  dxyz_kernel<<<ceil_div(p.nrows, wpb), 32 * wpb, per_warp * wpb, st>>>(dxyz, dD, xyz, p.row_pos, p.atype, p.nloc,
-                                                                        p.nrows, p.ng, p.axis, p.nnei);
+  DPGB_CUDA(cudaFuncSetAttribute(dxyz_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(per_warp * wpb)));
+  dxyz_smem_kernel<<<ceil_div(p.nrows, wpb), 32 * wpb, per_warp * wpb, st>>>(dxyz, dD, xyz, p.row_pos, p.atype,
+                                                                             p.nloc, p.nrows, ng, M, p.nnei);
   return check_launch("dxyz");
 }
 
