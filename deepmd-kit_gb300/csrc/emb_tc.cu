@@ -623,6 +623,16 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         __syncthreads();
         const int ntile = s_ntile;
         if (ntile == 0) break;
+        // bring the tile atoms' dE/dxyz rows into L1 now; epilogue 3 reads
+        // them after the two forward MMAs
+        {
+          const int lines = (4 * ng * (int)sizeof(float) + 127) / 128;
+          for (int q = tid; q < ntile * lines; q += blockDim.x) {
+            const int k = q / lines, l = q - k * lines;
+            const char* a = reinterpret_cast<const char*>(dxyz + (size_t)s_row[k] * 4 * ng) + 128 * l;
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
+          }
+        }
         PairInfo pi;
         float rn[4], dv[3];
         pair_env(p, t, ti, s_row, s_off, ntile, tid, pi, rn, dv);
