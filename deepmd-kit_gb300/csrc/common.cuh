@@ -46,6 +46,18 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// streaming multiprocessors of the current device (looked up once)
+inline int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
 // Device-side status word layout (one int per code, atomicMax'ed).
 enum StatusSlot { kStatusOverflow = 0, kStatusOverflowAtom = 1, kStatusTimeout = 2, kStatusSlots = 6 };
 

@@ -1025,16 +1025,6 @@ int launch_bwd_t(const DescParams<float>& p, const EmbTC& e, const WorkChunk* ch
   return check_launch("emb_tc_bwd");
 }
 
-int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
 
 }  // namespace
 

@@ -312,12 +312,15 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
   __shared__ int s_idx[kSearchWarps][kCap];
   __shared__ int s_type[kSearchWarps][kCap];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * kSearchWarps + warp;
-  if (i >= nloc || (gate && !gate[0])) return;
-  if (only_cells && !only_cells[cell_of[i]]) return;  // handled by the staged kernel
+  if (gate && !gate[0]) return;
+  // atoms in a grid-stride loop: as the fallback of the staged kernel most
+  // atoms only check their cell's flag
+  for (int i = blockIdx.x * kSearchWarps + warp; i < nloc; i += gridDim.x * kSearchWarps) {
+  if (only_cells && !only_cells[cell_of[i]]) continue;  // handled by the staged kernel
+  __syncwarp();  // the previous atom's reads of s_r / s_idx / s_type are done
   int* row = nlist + (size_t)i * sel.nnei;
   for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
-  if (atype[i] < 0) return;
+  if (atype[i] < 0) continue;
   const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
   const int ci = cell_of[i];
   const int cz = ci % g.ncell[2], cy = (ci / g.ncell[2]) % g.ncell[1],
@@ -377,7 +380,7 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
       atomicMax(&status[kStatusOverflow], n);
       atomicMax(&status[kStatusOverflowAtom], i + 1);
     }
-    return;
+    continue;
   }
   __syncwarp();
   for (int k = lane; k < n; k += 32) {
@@ -391,6 +394,7 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
     }
     // topk(sum(sel)): candidates of global rank >= nnei are dropped
     place_pair(row, rank, trank, tk, ik, sel, status);
+  }
   }
 }
 
@@ -1462,9 +1466,11 @@ int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc,
                                                             stage_cap, kept_cap);
     DPGB_TRY(check_launch("nlist_cell"));
   }
-  nlist_pt_kernel<<<ceil_div(nloc, kSearchWarps), kSearchWarps * 32, 0, st>>>(
-      nlist, coord, atype, cell_of, offsets, cell_atoms, shift_pos_dev, svec_dev, nloc, g, rcut, sel,
-      staged ? fallback : nullptr, status, gate);
+  // as a fallback (staged): a bounded grid whose warps stride over the atoms
+  const int blocks = staged ? std::min(ceil_div(nloc, kSearchWarps), 16 * sm_count()) : ceil_div(nloc, kSearchWarps);
+  nlist_pt_kernel<<<blocks, kSearchWarps * 32, 0, st>>>(nlist, coord, atype, cell_of, offsets, cell_atoms,
+                                                        shift_pos_dev, svec_dev, nloc, g, rcut, sel,
+                                                        staged ? fallback : nullptr, status, gate);
   return check_launch("nlist_pt");
 }
 
