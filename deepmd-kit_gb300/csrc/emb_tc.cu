@@ -193,6 +193,15 @@ __device__ __forceinline__ void pack_tile(const int* __restrict__ run_len, const
   }
 }
 
+// TMEM columns [c0, c0 + 32) of this warp's 32 lanes (the second 16 only
+// when they exist in an NCOL-column accumulator) with one wait for both
+template <int NCOL>
+__device__ __forceinline__ void tmem_ld32(uint32_t lane_base, int c0, float (&v)[32]) {
+  tc::tmem_ld16(lane_base + c0, *reinterpret_cast<float(*)[16]>(v));
+  if (c0 + 16 < NCOL) tc::tmem_ld16(lane_base + c0 + 16, *reinterpret_cast<float(*)[16]>(v + 16));
+  tc::tmem_ld_wait();
+}
+
 // Environment of the tile's pair p: fills Rn (normalised), d (displacement,
 // FP32 after the FP64 subtraction), the slot index and flags.
 struct PairInfo {
@@ -413,13 +422,12 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         // epilogue 2: H2 = tanh(acc + b2) * idt2 + skip(H1)
         float h2[W2];
 #pragma unroll
-        for (int c0 = 0; c0 < P::N2; c0 += 16) {
-          float v[16];
-          tc::tmem_ld16(tc::taddr(tbase, warp * 32, c0), v);
-          tc::tmem_ld_wait();
+        for (int c0 = 0; c0 < P::N2; c0 += 32) {
+          float v[32];
+          tmem_ld32<P::N2>(tc::taddr(tbase, warp * 32, 0), c0, v);
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int c = c0 + i, o = col_neuron(c, W2, W1);
+          for (int i = 0; i < 32; ++i) {
+            const int c = c0 + i, o = c < P::N2 ? col_neuron(c, W2, W1) : -1;
             if (o >= 0) {
               float h = tanh_fast(v[i] + b2[c]) * i2[c];
               if (W2 == W1) h += h1[o];
@@ -452,14 +460,13 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         // epilogue 3: G = tanh(acc + b3) * idt3 + skip(H2), kept in FP32,
         // stored as float4 rows
 #pragma unroll
-        for (int c0 = 0; c0 < P::N3; c0 += 16) {
-          float v[16];
-          tc::tmem_ld16(tc::taddr(tbase, warp * 32, c0), v);
-          tc::tmem_ld_wait();
-          float g[16];
+        for (int c0 = 0; c0 < P::N3; c0 += 32) {
+          float v[32];
+          tmem_ld32<P::N3>(tc::taddr(tbase, warp * 32, 0), c0, v);
+          float g[32];
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int c = c0 + i, o = col_neuron(c, W3, W2);
+          for (int i = 0; i < 32; ++i) {
+            const int c = c0 + i, o = c < P::N3 ? col_neuron(c, W3, W2) : -1;
             g[i] = 0.f;
             if (o >= 0) {
               float x3 = tanh_fast(v[i] + b3[c]) * i3[c];
@@ -472,7 +479,8 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
           // neurons (from an even one) go out as one float2
           float* grow = sG + tid * P::LDG;
 #pragma unroll
-          for (int i = 0; i < 16; i += 2) {
+          for (int i = 0; i < 32; i += 2) {
+            if (c0 + i >= P::N3) break;
             const int o0 = col_neuron(c0 + i, W3, W2), o1 = col_neuron(c0 + i + 1, W3, W2);
             if (o0 >= 0 && o1 == o0 + 1 && (o0 & 1) == 0) {
               *reinterpret_cast<float2*>(grow + o0) = make_float2(g[i], g[i + 1]);
