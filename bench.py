@@ -236,11 +236,21 @@ def run_compressed(args, world, rank, local):
     skin = 2.0 if args.skin is None else args.skin
     mixed.set_skin(skin, args.rebuild_every)
     out = mixed.eval_device(x, boxh, atype)
+    stream = torch.cuda.current_stream()
+    # per-stage times from profiled evaluations (untimed, without the graph),
+    # over one rebuild period so that the list builds are in the average
+    mixed.set_profiling(True)
+    for _ in range(max(args.rebuild_every, 3)):
+        x.add_(torch.randn(x.shape, dtype=x.dtype, device=dev, generator=gen), alpha=0.01)
+        mixed.eval_device(x, boxh, atype, out=out)
+        mixed.collect_stages()
+    stages, ncalls = mixed.stage_times()
+    mixed.set_profiling(False)
+    if not args.no_graph:
+        mixed.set_graph(True)
     for _ in range(args.warmup):
         mixed.eval_device(x, boxh, atype, out=out)
     torch.cuda.synchronize()
-    stream = torch.cuda.current_stream()
-    mixed.set_profiling(True)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     _barrier(world)
@@ -250,12 +260,10 @@ def run_compressed(args, world, rank, local):
             starts[k].record(stream)
             mixed.eval_device(x, boxh, atype, out=out)
             ends[k].record(stream)
-            mixed.collect_stages()
         torch.cuda.synchronize()
     _barrier(world)
     mixed.check_status()  # no neighbour overflow or candidate truncation in the timed steps
     t_ms = _allreduce_max(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), world)
-    stages, ncalls = mixed.stage_times()
     launches = mixed.last_launches()
     value = world * nloc * args.steps / (t_ms * 1e-3)
     fp64 = DeepPot(cparams, "fp64", device=local)
@@ -283,7 +291,8 @@ def run_compressed(args, world, rank, local):
                         "N(0, 0.01 A) random walk between evaluations; mixed form; "
                         + (f"candidates within rc + {skin:g} A rebuilt every {args.rebuild_every} evaluations "
                            "(or on a skin/2 move), the list at rc selected every evaluation" if skin > 0 else
-                           "neighbour list rebuilt every evaluation"),
+                           "neighbour list rebuilt every evaluation")
+                        + ("" if args.no_graph else "; replayed from a CUDA graph"),
             "skin_A": skin, "rebuild_every": args.rebuild_every,
             "natoms": nloc, "l2": "inputs larger than L2",
             "fp64_atom_steps_per_s": nloc / (fp64_ms * 1e-3), "fp64_ms_per_step": fp64_ms,
@@ -402,6 +411,8 @@ def main():
     ap.add_argument("--skin", type=float, default=None,
                     help="neighbour-list skin in A for water98k-compressed (default 2; 0 = rebuild every step)")
     ap.add_argument("--rebuild-every", type=int, default=10)
+    ap.add_argument("--no-graph", action="store_true",
+                    help="time plain evaluations instead of replaying the step from a CUDA graph")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.warmup < 3:
@@ -444,10 +455,22 @@ def main():
     out = mixed.eval_device(coord_dev, boxh, atype)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
     stream = torch.cuda.current_stream()
+    # per-stage times from profiled evaluations (untimed; event marks inside
+    # the evaluation, so without the graph)
+    mixed.set_profiling(True)
+    for _ in range(max(args.warmup, 3)):
+        flush.fill_(1.0)
+        mixed.eval_device(coord_dev, boxh, atype, out=out)
+        mixed.collect_stages()
+    stages, ncalls = mixed.stage_times()
+    mixed.set_profiling(False)
+    # the timed evaluations replay the step from a CUDA graph (captured on
+    # the first call: every kernel of the step, neighbour list included)
+    if not args.no_graph:
+        mixed.set_graph(True)
     for _ in range(args.warmup):
         mixed.eval_device(coord_dev, boxh, atype, out=out)
     torch.cuda.synchronize()
-    mixed.set_profiling(True)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     _barrier(world)
@@ -458,17 +481,15 @@ def main():
             starts[k].record(stream)
             mixed.eval_device(coord_dev, boxh, atype, out=out)
             ends[k].record(stream)
-            mixed.collect_stages()
         torch.cuda.synchronize()
+    mixed.check_status()
     _barrier(world)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     t_ms = _allreduce_max(sum(step_ms), world)
     launches = mixed.last_launches()
-    stages, ncalls = mixed.stage_times()
     value = world * nloc * args.steps / (t_ms * 1e-3)
 
     # end to end through the C API with host buffers
-    mixed.set_profiling(False)
     for _ in range(2):
         mixed.eval(coord.reshape(1, -1), boxh, atype)
     _barrier(world)
@@ -513,7 +534,9 @@ def main():
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {
             "workload": "water 4096 H2O (12,288 atoms), box 49.6 A, se_e2_a rc 6 sel [46,92] emb [25,50,100] "
-                        "axis 16 fit [240,240,240]; mixed form; full step incl. neighbour list",
+                        "axis 16 fit [240,240,240]; mixed form; full step incl. neighbour list"
+                        + ("" if args.no_graph else ", replayed from a CUDA graph"),
+            "stage_times_from": "profiled evaluations without the graph",
             "natoms": nloc, "real_pairs": n_pairs, "l2": "flushed between timed steps (256 MB write, untimed)",
             "fp64_atom_steps_per_s": fp64_value, "fp64_ms_per_step": fp64_ms,
             "mixed_over_fp64": value / world / fp64_value,

@@ -396,6 +396,25 @@ struct DeepPotImpl {
   int skin_nframes = -1;
   const void* skin_cand_ptr = nullptr;
   DeviceBuffer ws_gate, ws_cand, ws_skin_off, ws_skin_ref, ws_coordf, ws_svecf;
+  // single-system CUDA graph (dpgb_deeppot_set_graph): one evaluation of a
+  // periodic system captured and replayed on the handle's stream while the
+  // key (frames, atoms, box, buffers) and the handle's state (gen) hold
+  int use_graph = 0;
+  int capturing = 0;  // inside a capture: no pageable host uploads (their data is on the device)
+  cudaGraph_t sg_graph = nullptr;
+  cudaGraphExec_t sg_exec = nullptr;
+  unsigned long long sg_gen = ~0ull;
+  int sg_nframes = -1, sg_natom = -1, sg_launches = 0;
+  std::vector<double> sg_box;
+  const void* sg_ptr[6] = {};
+  cudaEvent_t sg_ev_in = nullptr, sg_ev_out = nullptr;
+  void drop_graph() {
+    if (sg_exec) cudaGraphExecDestroy(sg_exec);
+    if (sg_graph) cudaGraphDestroy(sg_graph);
+    sg_exec = nullptr;
+    sg_graph = nullptr;
+    sg_gen = ~0ull;
+  }
   std::string err;
   int launches = 0;
   cudaStream_t stream = nullptr;
@@ -955,7 +974,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   DPGB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * kStatusSlots, st));
   // shift tables (a batch brings its own; nothing host-side may run inside
   // a captured batch evaluation)
-  if (own_geom) {
+  if (own_geom && !dp.capturing) {  // a capture replays the tables its plain run uploaded
     std::vector<double> sv((size_t)3 * nshift_max * nframes, 0.0);
     std::vector<int> sp(spos_n * nframes, -1);
     for (int f = 0; f < (int)spos.size(); ++f) {
@@ -1245,16 +1264,74 @@ int check_status(DeepPotImpl& dp, cudaStream_t st) {
   return DPGB_OK;
 }
 
+int run_any(DeepPotImpl& dp, int nframes, int natom, const double* coord, const double* box_host, double* energy,
+            double* force, double* virial, double* atom_energy, double* atom_virial, cudaStream_t st) {
+  if (dp.precision == DPGB_PREC_FP64)
+    return run<double>(dp, *dp.m64, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial, st);
+  return run<float>(dp, *dp.m32, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial, st);
+}
+
 int compute_device_impl(DeepPotImpl& dp, int nframes, int natom, const double* coord, const int* atype_host,
                         const double* box_host, double* energy, double* force, double* virial, double* atom_energy,
                         double* atom_virial, cudaStream_t st) {
   if (nframes <= 0 || natom <= 0) return fail(DPGB_EINVAL, "nframes and natom must be positive");
   if (!coord || !atype_host || !energy || !force || !virial) return fail(DPGB_EINVAL, "NULL argument");
+  const bool graph = dp.use_graph && box_host && dp.stream;
+  const void* ptrs[6] = {coord, energy, force, virial, atom_energy, atom_virial};
+  if (graph) {
+    DPGB_TRY(prepare_types(dp, nframes, natom, atype_host, st));  // a change of types bumps gen
+    const bool same = dp.sg_exec && dp.gen == dp.sg_gen && dp.sg_nframes == nframes && dp.sg_natom == natom &&
+                      std::equal(ptrs, ptrs + 6, dp.sg_ptr) &&
+                      std::equal(box_host, box_host + 9 * (size_t)nframes, dp.sg_box.begin());
+    if (same) {  // replay on the handle's stream, ordered after and before the caller's
+      cudaStream_t hs = dp.stream;
+      if (st != hs) {
+        DPGB_CUDA(cudaEventRecord(dp.sg_ev_in, st));
+        DPGB_CUDA(cudaStreamWaitEvent(hs, dp.sg_ev_in, 0));
+      }
+      DPGB_CUDA(cudaGraphLaunch(dp.sg_exec, hs));
+      if (st != hs) {
+        DPGB_CUDA(cudaEventRecord(dp.sg_ev_out, hs));
+        DPGB_CUDA(cudaStreamWaitEvent(st, dp.sg_ev_out, 0));
+      }
+      dp.launches = dp.sg_launches;
+      return DPGB_OK;
+    }
+  }
   ++dp.gen;  // workspace may grow
   DPGB_TRY(prepare_types(dp, nframes, natom, atype_host, st));
-  if (dp.precision == DPGB_PREC_FP64)
-    return run<double>(dp, *dp.m64, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial, st);
-  return run<float>(dp, *dp.m32, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial, st);
+  DPGB_TRY(run_any(dp, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial, st));
+  if (!graph) return DPGB_OK;
+  // capture the same evaluation for the next calls (this call's results come
+  // from the plain run; the capture records and does not execute)
+  dp.drop_graph();
+  if (!dp.sg_ev_in) DPGB_CUDA(cudaEventCreateWithFlags(&dp.sg_ev_in, cudaEventDisableTiming));
+  if (!dp.sg_ev_out) DPGB_CUDA(cudaEventCreateWithFlags(&dp.sg_ev_out, cudaEventDisableTiming));
+  const int launches = dp.launches, prof = dp.profiling;
+  dp.profiling = 0;  // no event records inside the graph
+  dp.capturing = 1;
+  DPGB_CUDA(cudaStreamBeginCapture(dp.stream, cudaStreamCaptureModeRelaxed));
+  const int rc = run_any(dp, nframes, natom, coord, box_host, energy, force, virial, atom_energy, atom_virial,
+                         dp.stream);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(dp.stream, &g);
+  dp.capturing = 0;
+  dp.profiling = prof;
+  dp.launches = launches;
+  if (rc != DPGB_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  DPGB_CUDA(ce);
+  dp.sg_graph = g;
+  DPGB_CUDA(cudaGraphInstantiate(&dp.sg_exec, dp.sg_graph, 0));
+  dp.sg_gen = dp.gen;
+  dp.sg_nframes = nframes;
+  dp.sg_natom = natom;
+  dp.sg_launches = launches;
+  std::copy(ptrs, ptrs + 6, dp.sg_ptr);
+  dp.sg_box.assign(box_host, box_host + 9 * (size_t)nframes);
+  return DPGB_OK;
 }
 
 // One frame with explicit ghosts and a caller's neighbour list (the
@@ -1570,6 +1647,9 @@ void dpgb_deeppot_delete(dpgb_deeppot* dp) {
   }
   for (auto& e : dp->impl.ev)
     if (e) cudaEventDestroy(e);
+  dp->impl.drop_graph();
+  if (dp->impl.sg_ev_in) cudaEventDestroy(dp->impl.sg_ev_in);
+  if (dp->impl.sg_ev_out) cudaEventDestroy(dp->impl.sg_ev_out);
   delete dp;
 }
 
@@ -1743,6 +1823,14 @@ int dpgb_deeppot_set_skin(dpgb_deeppot* dp, double skin, int every) {
   im.skin = skin;
   im.skin_every = every;
   im.skin_nframes = -1;  // the next call builds
+  return DPGB_OK;
+}
+
+int dpgb_deeppot_set_graph(dpgb_deeppot* dp, int on) {
+  clear_error();
+  if (!dp) return fail(DPGB_EINVAL, "NULL handle");
+  dp->impl.use_graph = on ? 1 : 0;
+  if (!on) dp->impl.drop_graph();
   return DPGB_OK;
 }
 

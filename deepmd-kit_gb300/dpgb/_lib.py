@@ -127,6 +127,7 @@ _SIGS = {
     "dpgb_batch_compute": [_P, _DP, _DP, _DP, _DP, _I],
     "dpgb_deeppot_last_launches": [_P],
     "dpgb_deeppot_set_skin": [_P, _D, _I],
+    "dpgb_deeppot_set_graph": [_P, _I],
     "dpgb_deeppot_check_status": [_P, _P],
     "dpgb_deeppot_set_profiling": [_P, _I],
     "dpgb_deeppot_collect_stages": [_P],

@@ -116,6 +116,11 @@ class DeepPot:
         moved more than skin / 2 (``skin=0``: a fresh list each call)."""
         _lib.check(_lib.lib().dpgb_deeppot_set_skin(self._h, float(skin), int(every)))
 
+    def set_graph(self, on: bool = True) -> None:
+        """Replay the evaluation of a periodic system from a CUDA graph while
+        its shape, box, buffers and the handle's state stay the same."""
+        _lib.check(_lib.lib().dpgb_deeppot_set_graph(self._h, int(on)))
+
     def check_status(self, stream=None) -> None:
         """Synchronise and raise the device-side errors of the last
         evaluation (the device form does not synchronise)."""

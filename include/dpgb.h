@@ -459,6 +459,16 @@ int dpgb_deeppot_compute_device(dpgb_deeppot* dp, int nframes, int natom,
  * reports it and the next call widens and rebuilds). */
 int dpgb_deeppot_set_skin(dpgb_deeppot* dp, double skin, int every);
 
+/* CUDA-graph replay of the single-system evaluation (both compute forms,
+ * periodic frames): with on = 1 the first call for a given shape, box and
+ * set of buffers runs normally and captures the evaluation into a graph;
+ * later calls with the same shape, box, buffers and handle state replay it
+ * on the handle's stream (ordered after and before the caller's stream by
+ * events) with no host-side work.  A change of any of them, or another
+ * system computed on the handle, re-captures.  on = 0 (the default)
+ * releases the graph. */
+int dpgb_deeppot_set_graph(dpgb_deeppot* dp, int on);
+
 /* Waits for `stream` (NULL: the handle's stream) and reports the
  * device-side errors of the last evaluation: neighbour overflow, skin
  * candidate truncation, a timed-out tensor-core wait.  The device form
