@@ -408,6 +408,10 @@ struct DeepPotImpl {
   std::vector<double> sg_box;
   const void* sg_ptr[6] = {};
   cudaEvent_t sg_ev_in = nullptr, sg_ev_out = nullptr;
+  // side stream of the sorted transpose (needed only by the force gather, so
+  // it runs next to the descriptor and the fitting), fork / join events
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void drop_graph() {
     if (sg_exec) cudaGraphExecDestroy(sg_exec);
     if (sg_graph) cudaGraphDestroy(sg_graph);
@@ -1044,22 +1048,30 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   }
   dp.mark(DPGB_STAGE_NLIST, 1, st);
   // sorted transpose of the list over local rows
-  dp.mark(DPGB_STAGE_TRANSPOSE, 0, st);
+  // the sorted transpose on the side stream: only the force gather needs it
+  cudaStream_t ts = st;
+  if (dp.side) {
+    DPGB_CUDA(cudaEventRecord(dp.ev_fork, st));
+    DPGB_CUDA(cudaStreamWaitEvent(dp.side, dp.ev_fork, 0));
+    ts = dp.side;
+  }
+  dp.mark(DPGB_STAGE_TRANSPOSE, 0, ts);
   Transpose tr;
   if (npair > 0) {
     // image-major indices fold onto their atom; explicit extended indices
     // are their own keys
     if (batch)
-      batch_keys_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(dp.ws_keys.as<int>(), nlist, npair, nnei, batch->ft);
+      batch_keys_kernel<<<ceil_div(npair, 256), 256, 0, ts>>>(dp.ws_keys.as<int>(), nlist, npair, nnei, batch->ft);
     else
-      model_keys_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(dp.ws_keys.as<int>(), nlist, npair, nnei,
+      model_keys_kernel<<<ceil_div(npair, 256), 256, 0, ts>>>(dp.ws_keys.as<int>(), nlist, npair, nnei,
                                                                ext ? ext->nall : natom);
     DPGB_TRY(check_launch("model_keys"));
     ++launches;
   }
-  DPGB_TRY(launch_transpose(tr, dp.ws_keys.as<int>(), npair, (int)nkeys, 0, dp.ws_tr.ptr, status, st));
+  DPGB_TRY(launch_transpose(tr, dp.ws_keys.as<int>(), npair, (int)nkeys, 0, dp.ws_tr.ptr, status, ts));
   launches += 4;
-  dp.mark(DPGB_STAGE_TRANSPOSE, 1, st);
+  dp.mark(DPGB_STAGE_TRANSPOSE, 1, ts);
+  if (dp.side) DPGB_CUDA(cudaEventRecord(dp.ev_join, dp.side));
   // descriptor forward
   DescParams<T> p{};
   p.nloc = natom;
@@ -1204,6 +1216,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     ++launches;
   }
   dp.mark(DPGB_STAGE_DESC_BWD, 1, st);
+  if (dp.side) DPGB_CUDA(cudaStreamWaitEvent(st, dp.ev_join, 0));  // the transpose is done
   dp.mark(DPGB_STAGE_REDUCE, 0, st);
   if (ext) {
     if (atom_virial)
@@ -1632,7 +1645,10 @@ dpgb_deeppot* dpgb_deeppot_new(const dpgb_se_a_desc* desc, int precision) {
   for (int t = 0; t < DPGB_MAX_TYPES; ++t)
     for (int l = 0; l <= DPGB_MAX_LAYERS; ++l) im.desc.fit_w[t][l] = im.desc.fit_b[t][l] = im.desc.fit_idt[t][l] = nullptr;
   im.desc.davg = im.desc.dstd = im.desc.atom_ener_bias = nullptr;
-  if (cudaStreamCreateWithFlags(&im.stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&im.stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&im.side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&im.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&im.ev_join, cudaEventDisableTiming) != cudaSuccess) {
     fail(DPGB_ECUDA, "stream creation failed");
     return nullptr;
   }
@@ -1648,6 +1664,12 @@ void dpgb_deeppot_delete(dpgb_deeppot* dp) {
   for (auto& e : dp->impl.ev)
     if (e) cudaEventDestroy(e);
   dp->impl.drop_graph();
+  if (dp->impl.side) {
+    cudaStreamSynchronize(dp->impl.side);
+    cudaStreamDestroy(dp->impl.side);
+  }
+  if (dp->impl.ev_fork) cudaEventDestroy(dp->impl.ev_fork);
+  if (dp->impl.ev_join) cudaEventDestroy(dp->impl.ev_join);
   if (dp->impl.sg_ev_in) cudaEventDestroy(dp->impl.sg_ev_in);
   if (dp->impl.sg_ev_out) cudaEventDestroy(dp->impl.sg_ev_out);
   delete dp;
