@@ -652,9 +652,8 @@ __device__ __forceinline__ void cell_centre(const CellGeom& g, int cx, int cy, i
 // Returns 0, or -(candidates) - 1 when more than kept_cap candidates (typed
 // lists; the row is then incomplete).
 __device__ int staged_list_atom(int* __restrict__ row, double* __restrict__ wr, int* __restrict__ wi,
-                                int* __restrict__ wt, const float* __restrict__ sx, const float* __restrict__ sy,
-                                const float* __restrict__ sz, const int* __restrict__ sidx,
-                                const int* __restrict__ stype, int total, int self, float xf, float yf, float zf,
+                                int* __restrict__ wt, const float4* __restrict__ s4, const int* __restrict__ sidx,
+                                int total, int self, float xf, float yf, float zf,
                                 float eps, const double* __restrict__ coord, const double* __restrict__ svec,
                                 int nloc, int a_beg, double xi, double yi, double zi, double rcut, const SelInfo& sel,
                                 int lane, int* __restrict__ status, int* __restrict__ s_base, int kept_cap) {
@@ -666,9 +665,12 @@ __device__ int staged_list_atom(int* __restrict__ row, double* __restrict__ wr, 
     for (int p0 = 0; p0 < total; p0 += 32) {
       const int p = p0 + lane;
       bool cand = false;
-      if (p < total && stype[p] >= 0 && sidx[p] != self) {
-        const float fx = sx[p] - xf, fy = sy[p] - yf, fz = sz[p] - zf;
-        cand = fx * fx + fy * fy + fz * fz <= rout2;
+      if (p < total) {
+        const float4 q = s4[p];  // x, y, z, type bits
+        const float fx = q.x - xf, fy = q.y - yf, fz = q.z - zf;
+        const float d2 = fx * fx + fy * fy + fz * fz;
+        // the atom itself (zero image) is the one entry at distance exactly 0
+        cand = __float_as_int(q.w) >= 0 && d2 <= rout2 && !(d2 == 0.f && sidx[p] == self);
       }
       const unsigned m = __ballot_sync(0xffffffffu, cand);
       const int pos = nc + __popc(m & below);
@@ -685,10 +687,14 @@ __device__ int staged_list_atom(int* __restrict__ row, double* __restrict__ wr, 
     const int p = p0 + lane;
     bool cand = false;
     float r = 0.f;
-    if (p < total && stype[p] >= 0 && sidx[p] != self) {
-      const float fx = sx[p] - xf, fy = sy[p] - yf, fz = sz[p] - zf;
+    int tq = -1;
+    if (p < total) {
+      const float4 q = s4[p];  // x, y, z, type bits
+      tq = __float_as_int(q.w);
+      const float fx = q.x - xf, fy = q.y - yf, fz = q.z - zf;
       const float d2 = fx * fx + fy * fy + fz * fz;
-      if (d2 <= rout2) {
+      // the atom itself (zero image) is the one entry at distance exactly 0
+      if (tq >= 0 && d2 <= rout2 && !(d2 == 0.f && sidx[p] == self)) {
         cand = true;
         r = sqrtf(d2);
         band |= r > rin;
@@ -699,7 +705,7 @@ __device__ int staged_list_atom(int* __restrict__ row, double* __restrict__ wr, 
     if (cand && pos < kept_cap) {
       wf[pos] = r;
       wi[pos] = sidx[p];
-      wt[pos] = stype[p];
+      wt[pos] = tq;
     }
     nc += __popc(m);
   }
@@ -728,12 +734,9 @@ nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
   if (gate && !gate[0]) return;
   extern __shared__ __align__(16) unsigned char smem[];
   double* kr = reinterpret_cast<double*>(smem);
-  float* sx = reinterpret_cast<float*>(kr + kCellWarps * kept_cap);
-  float* sy = sx + stage_cap;
-  float* sz = sy + stage_cap;
-  int* sidx = reinterpret_cast<int*>(sz + stage_cap);
-  int* stype = sidx + stage_cap;
-  int* kidx = stype + stage_cap;
+  float4* s4 = reinterpret_cast<float4*>(kr + kCellWarps * kept_cap);  // staged x, y, z, type bits
+  int* sidx = reinterpret_cast<int*>(s4 + stage_cap);
+  int* kidx = sidx + stage_cap;
   int* ktype = kidx + kCellWarps * kept_cap;
   __shared__ int s_cell[27], s_shift[27], s_off[28];
   __shared__ int s_tb[kCellWarps][DPGB_MAX_TYPES];  // per-type running counts of sort_place_f32
@@ -774,11 +777,9 @@ nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
     while (s_off[k + 1] <= q) ++k;
     const int j = cell_atoms[offsets[s_cell[k]] + (q - s_off[k])];
     const int s = s_shift[k];
-    sx[q] = (float)((coord[3 * j] + svec[3 * s]) - ox);
-    sy[q] = (float)((coord[3 * j + 1] + svec[3 * s + 1]) - oy);
-    sz[q] = (float)((coord[3 * j + 2] + svec[3 * s + 2]) - oz);
+    s4[q] = make_float4((float)((coord[3 * j] + svec[3 * s]) - ox), (float)((coord[3 * j + 1] + svec[3 * s + 1]) - oy),
+                        (float)((coord[3 * j + 2] + svec[3 * s + 2]) - oz), __int_as_float(atype[j]));
     sidx[q] = s * nloc + j;
-    stype[q] = atype[j];
   }
   __syncthreads();
   double* wr = kr + warp * kept_cap;
@@ -793,7 +794,7 @@ nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
     const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
     const int self = g.zero_shift * nloc + i;
     const float xf = (float)(xi - ox), yf = (float)(yi - oy), zf = (float)(zi - oz);
-    const int r = staged_list_atom(row, wr, wi, wt, sx, sy, sz, sidx, stype, total, self, xf, yf, zf, eps, coord,
+    const int r = staged_list_atom(row, wr, wi, wt, s4, sidx, total, self, xf, yf, zf, eps, coord,
                                    svec, nloc, 0, xi, yi, zi, rcut, sel, lane, status, s_tb[warp], kept_cap);
     if (r < 0 && lane == 0) fallback[c] = 1;  // more than kept_cap candidates: the cell goes to the per-atom kernel
     __syncwarp();
@@ -1101,12 +1102,9 @@ nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coor
                         double rcut, SelInfo sel, int* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem[];
   double* kr = reinterpret_cast<double*>(smem);
-  float* sx = reinterpret_cast<float*>(kr + kCellWarps * kBatchKeptCap);
-  float* sy = sx + kBatchStageCap;
-  float* sz = sy + kBatchStageCap;
-  int* sidx = reinterpret_cast<int*>(sz + kBatchStageCap);
-  int* stype = sidx + kBatchStageCap;
-  int* kidx = stype + kBatchStageCap;
+  float4* s4 = reinterpret_cast<float4*>(kr + kCellWarps * kBatchKeptCap);  // staged x, y, z, type bits
+  int* sidx = reinterpret_cast<int*>(s4 + kBatchStageCap);
+  int* kidx = sidx + kBatchStageCap;
   int* ktype = kidx + kCellWarps * kBatchKeptCap;
   // stencil of (2 reach + 1)^3 cells, reach <= 2 per direction (a frame
   // thinner than rcut across a face has one cell and reach 2 there)
@@ -1163,11 +1161,9 @@ nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coor
     const int k = lo;
     const int j = cell_atoms[offsets[s_cell[k]] + (q - s_off[k])];  // global atom
     const int s = s_shift[k];
-    sx[q] = (float)((coord[3 * j] + svec[3 * s]) - ox);
-    sy[q] = (float)((coord[3 * j + 1] + svec[3 * s + 1]) - oy);
-    sz[q] = (float)((coord[3 * j + 2] + svec[3 * s + 2]) - oz);
+    s4[q] = make_float4((float)((coord[3 * j] + svec[3 * s]) - ox), (float)((coord[3 * j + 1] + svec[3 * s + 1]) - oy),
+                        (float)((coord[3 * j + 2] + svec[3 * s + 2]) - oz), __int_as_float(atype[j]));
     sidx[q] = s * nloc + (j - a_beg);
-    stype[q] = atype[j];
   }
   __syncthreads();
   double* wr = kr + warp * kBatchKeptCap;
@@ -1182,7 +1178,7 @@ nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coor
     const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
     const int self = g.zero_shift * nloc + (i - a_beg);
     const float xf = (float)(xi - ox), yf = (float)(yi - oy), zf = (float)(zi - oz);
-    const int r = staged_list_atom(row, wr, wi, wt, sx, sy, sz, sidx, stype, total, self, xf, yf, zf, eps, coord,
+    const int r = staged_list_atom(row, wr, wi, wt, s4, sidx, total, self, xf, yf, zf, eps, coord,
                                    svec, nloc, a_beg, xi, yi, zi, rcut, sel, lane, status, s_tb[warp], kBatchKeptCap);
     if (r < 0 && lane == 0) {
       atomicMax(&status[kStatusOverflow], -r - 1);
