@@ -496,8 +496,11 @@ int build_fit_tc(DeepPotImpl& im, const dpgb_se_a_desc& d) {
 // forward + input-gradient backward of the fitting of all typed rows on the
 // tensor cores, one launch per layer (each 128-row tile uses its type's
 // weights).  Db: BF16 descriptors (sorted rows); dD: FP32 output.
+// With dxyz set (axis width 16), the last backward GEMM is folded into
+// dE/dxyz (launch_fit_dxyz) and dD is not written; *dxyz_done says so.
 int run_fit_tc(DeepPotImpl& dp, int nrows, const __nv_bfloat16* Db, float* dD, float* act, float* gbuf,
-               __nv_bfloat16* fitb, double* e_sorted, int* err, cudaStream_t st) {
+               __nv_bfloat16* fitb, double* e_sorted, int* err, cudaStream_t st, float* dxyz, const float* xyz,
+               int* dxyz_done) {
   const int nh = dp.fit_nh, dim = dp.fit_width[0], nt = dp.desc.ntypes;
   int maxw = 0;
   for (int l = 1; l <= nh; ++l) maxw = std::max(maxw, dp.fit_width[l]);
@@ -569,6 +572,27 @@ int run_fit_tc(DeepPotImpl& dp, int nrows, const __nv_bfloat16* Db, float* dD, f
     g.dPb = dPb(cur ^ 1);
     DPGB_TRY(launch_fit_gemm(g, err, st));
     cur ^= 1;
+  }
+  *dxyz_done = 0;
+  if (dxyz && dp.desc.axis_neuron == 16 && dim == 16 * dp.ng && dp.fit_width[1] <= 256) {
+    FitDxyz f{};
+    f.ntypes = base.ntypes;
+    for (int t = 0; t <= base.ntypes; ++t) {
+      f.row0[t] = base.row0[t];
+      f.tile0[t] = base.tile0[t];
+    }
+    f.K = dp.fit_width[1];
+    f.ng = dp.ng;
+    f.nnei = dp.sel.nnei;
+    f.A = dPb(cur);
+    f.lda = maxw;
+    f.B = dp.fit_Wb[0];
+    f.xyz = xyz;
+    f.sorted_rows = dp.sorted_rows_dev.as<int>();
+    f.dxyz = dxyz;
+    DPGB_TRY(launch_fit_dxyz(f, err, st));
+    *dxyz_done = 1;
+    return DPGB_OK;
   }
   FitGemm g = base;
   g.mode = kFitStore;
@@ -1174,11 +1198,15 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   if (fit_tc) {
     DPGB_TRY(dp.ws_fitb.alloc(sizeof(__nv_bfloat16) * (size_t)(dp.fit_nh + 2) * nrows * maxw));
   }
+  int dxyz_done = 0;  // dE/dxyz already formed by the fitting's last backward GEMM
   if (fit_tc) {
     if constexpr (std::is_same<T, float>::value) {
+      DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ng * std::max(d.ntypes, 1)));
       DPGB_TRY(run_fit_tc(dp, (int)nrows, reinterpret_cast<const __nv_bfloat16*>(dp.ws_D.ptr), dp.ws_dD.as<float>(),
                           dp.ws_act.as<float>(), dp.ws_gbuf.as<float>(), dp.ws_fitb.as<__nv_bfloat16>(),
-                          dp.ws_esorted.as<double>(), status + kStatusTimeout, st));
+                          dp.ws_esorted.as<double>(), status + kStatusTimeout, st,
+                          (tc_path || tab_path) ? dp.ws_dxyz.as<float>() : nullptr, dp.ws_xyz.as<float>(),
+                          &dxyz_done));
     }
     launches += 2 * dp.fit_nh;
   } else {
@@ -1196,7 +1224,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     if (tc_path) {
       // rows of virtual atoms are never visited by the tile kernels
       DPGB_CUDA(cudaMemsetAsync(dp.ws_vir.ptr, 0, sizeof(double) * nrows * 9, st));
-      DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
+      if (!dxyz_done) DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
       DPGB_TRY(launch_emb_tc_bwd(p, dp.tc, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.ws_runlen.as<int>(),
                                  dp.sorted_rows_dev.as<int>(), dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(),
                                  dp.ws_vir.as<double>(), status, st));
@@ -1204,7 +1232,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     }
     if (tab_path) {
       DPGB_CUDA(cudaMemsetAsync(dp.ws_vir.ptr, 0, sizeof(double) * nrows * 9, st));
-      DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
+      if (!dxyz_done) DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
       DPGB_TRY(launch_tab_bwd(p, m.emb, dp.sorted_rows_dev.as<int>(), dp.type_off[d.ntypes], dp.ws_dxyz.as<float>(),
                               dp.ws_g.as<float>(), dp.ws_vir.as<double>(), st));
       launches += 2;

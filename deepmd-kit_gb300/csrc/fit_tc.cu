@@ -185,6 +185,165 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   if (warp == 0) tc::tmem_dealloc(tbase, BN < 32 ? 32 : BN);
 }
 
+// dE/dD of the first layer folded into dE/dxyz (FitDxyz).  One CTA per
+// 128-row tile walks all 16 ng columns of dD in chunks of 128 (8 neurons):
+// dP1 stays in shared memory, W1 streams through an S-stage TMA ring two
+// chunks ahead, each chunk's accumulator is read by the epilogue (thread =
+// row): the first term goes out per neuron, the transposed term of the first
+// 16 neurons accumulates in registers and is added at the end.
+constexpr int kDxM = 16, kDxBN = 128, kDxStages = 8;
+
+__global__ void __launch_bounds__(256, 1)
+fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b, FitDxyz f,
+                int* __restrict__ err) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
+  constexpr int SA = 128 * kKC * 2, SB = kDxBN * kKC * 2, M = kDxM, S = kDxStages;
+  __shared__ uint64_t full[S], empty[S], a_full, acc;
+  __shared__ uint32_t s_tmem;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  int t = 0;
+  while (t + 1 < f.ntypes && f.tile0[t + 1] <= (int)blockIdx.x) ++t;
+  const int m0 = f.row0[t] + ((int)blockIdx.x - f.tile0[t]) * 128;
+  const int rows_valid = min(128, f.row0[t + 1] - m0);
+  const int ncol = f.ng * M, nk = (f.K + kKC - 1) / kKC, nchunk = (ncol + kDxBN - 1) / kDxBN;
+  const int L = nchunk * nk;  // B loads
+  unsigned char* sA = smem;              // nk stages of dP1
+  unsigned char* sB = smem + nk * SA;    // ring
+  if (warp == 0) tc::tmem_alloc(&s_tmem, kDxBN);
+  if (tid == 0) {
+    for (int q = 0; q < S; ++q) {
+      tc::mbar_init(&full[q], 1);
+      tc::mbar_init(&empty[q], 1);
+    }
+    tc::mbar_init(&a_full, 1);
+    tc::mbar_init(&acc, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tbase = s_tmem;
+  bool ok = true;
+  int next = 0;  // next B load
+  auto load_b = [&](int upto) {
+    for (; next < upto && next < L && ok; ++next) {
+      const int q = next % S;
+      if (next >= S) ok = tc::mbar_wait(&empty[q], ((next / S) - 1) & 1, err);
+      if (!ok) break;
+      const int j = next / nk, k = next - j * nk;
+      tc::mbar_expect_tx(&full[q], SB);
+      tc::tma_load_2d(tc::smem_u32(sB + q * SB), &tma_b, k * kKC, t * ncol + j * kDxBN, &full[q]);
+    }
+  };
+  if (warp == 1 && lane == 0) {
+    tc::mbar_expect_tx(&a_full, nk * SA);
+    for (int k = 0; k < nk; ++k) tc::tma_load_2d(tc::smem_u32(sA + k * SA), &tma_a, k * kKC, m0, &a_full);
+    load_b(S);
+  }
+  // the row's xyz[c][m < 16]; the transposed term of neurons m < 16.  Two
+  // warpgroups share the rows (TMEM lanes) and take alternate halves of a
+  // chunk's neurons.
+  const int r = (warp & 3) * 32 + lane, wg = warp >> 2;
+  const bool valid = r < rows_valid;
+  const int row = valid ? f.sorted_rows[m0 + r] : 0;
+  const float* xr = f.xyz + (size_t)row * 4 * f.ng;
+  float4* out = reinterpret_cast<float4*>(f.dxyz + (size_t)row * 4 * f.ng);
+  float xm[4][M], T2[4][M];
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      xm[c][m] = valid ? xr[c * f.ng + m] : 0.f;
+      T2[c][m] = 0.f;
+    }
+  const float inv = 1.f / (float)f.nnei;
+  for (int j = 0; j < nchunk && ok; ++j) {
+    const int nt = min(kDxBN, ncol - j * kDxBN);  // 128 or a multiple of 16
+    if (warp == 0 && lane == 0) {
+      if (j == 0) ok = tc::mbar_wait(&a_full, 0, err);
+      const uint32_t idesc = tc::idesc_bf16_f32(128, nt);
+      for (int k = 0; k < nk && ok; ++k) {
+        const int i = j * nk + k, q = i % S;
+        ok = tc::mbar_wait(&full[q], (i / S) & 1, err);
+        if (!ok) break;
+        tc::fence_after();
+        const uint32_t a0 = tc::smem_u32(sA + k * SA), b0 = tc::smem_u32(sB + q * SB);
+#pragma unroll
+        for (int ks = 0; ks < kKC / 16; ++ks)
+          tc::mma_bf16(tbase, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc,
+                       (k > 0 || ks > 0) ? 1u : 0u);
+        tc::mma_commit(&empty[q]);
+      }
+      tc::mma_commit(&acc);
+    }
+    __syncwarp();
+    // this warpgroup's neurons of the chunk and their xyz[c][n], loaded
+    // while the MMAs run
+    constexpr int NH = kDxBN / M / 2;
+    const int q0 = wg * NH, q1 = min(nt / M, (wg + 1) * NH);
+    float xq[NH][4];
+#pragma unroll
+    for (int h = 0; h < NH; ++h)
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        xq[h][c] = (valid && q0 + h < q1) ? xr[c * f.ng + j * (kDxBN / M) + q0 + h] : 0.f;
+    ok = tc::mbar_wait(&acc, j & 1, err) && ok;
+    tc::fence_after();
+#pragma unroll
+    for (int h = 0; h < NH; ++h) {
+      const int q = q0 + h;
+      if (q >= q1) break;
+      const int n = j * (kDxBN / M) + q;
+      float v[16];
+      tc::tmem_ld16(tc::taddr(tbase, (warp & 3) * 32, q * M), v);
+      tc::tmem_ld_wait();
+      if (!valid) continue;
+      float t1[4], xn[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        float sacc = 0.f;
+#pragma unroll
+        for (int m = 0; m < M; ++m) sacc = fmaf(v[m], xm[c][m], sacc);
+        t1[c] = sacc;
+        xn[c] = xq[h][c];
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int m = 0; m < M; ++m) T2[c][m] = fmaf(v[m], xn[c], T2[c][m]);
+      if (n < M)  // completed with the transposed term below
+        out[n] = make_float4(t1[0], t1[1], t1[2], t1[3]);
+      else
+        out[n] = make_float4(t1[0] * inv, t1[1] * inv, t1[2] * inv, t1[3] * inv);
+    }
+    tc::fence_before();
+    ok = __syncthreads_and(ok) != 0;  // the accumulator is read: the next chunk may overwrite it
+    tc::fence_after();
+    if (warp == 1 && lane == 0) load_b((j + 1) * nk + S);
+  }
+  // the second warpgroup's transposed-term partials to the first (the ring
+  // is free now), which completes neurons m < 16
+  float* s_t2 = reinterpret_cast<float*>(sB);
+  if (ok && wg == 1)
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int m = 0; m < M; ++m) s_t2[(c * M + m) * 128 + r] = T2[c][m];
+  __syncthreads();
+  if (ok && valid && wg == 0)
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      const float4 a = out[m];
+      out[m] = make_float4((a.x + (T2[0][m] + s_t2[(0 * M + m) * 128 + r])) * inv,
+                           (a.y + (T2[1][m] + s_t2[(1 * M + m) * 128 + r])) * inv,
+                           (a.z + (T2[2][m] + s_t2[(2 * M + m) * 128 + r])) * inv,
+                           (a.w + (T2[3][m] + s_t2[(3 * M + m) * 128 + r])) * inv);
+    }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tbase, kDxBN);
+}
+
 // cuTensorMapEncodeTiled, taken from the driver through the runtime
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -244,6 +403,19 @@ int fit_tc_eligible(const dpgb_se_a_desc& d) {
     nin = w;
   }
   return d.n_fit >= 1;
+}
+
+int launch_fit_dxyz(const FitDxyz& f, int* err, cudaStream_t st) {
+  if (f.tile0[f.ntypes] <= 0) return DPGB_OK;
+  const int nk = (f.K + kKC - 1) / kKC;
+  const size_t smem = (size_t)nk * 128 * kKC * 2 + (size_t)kDxStages * kDxBN * kKC * 2 + 1024;
+  if (smem > 227 * 1024) return fail(DPGB_EINVAL, "fit_dxyz: first hidden layer too wide");
+  DPGB_CUDA(cudaFuncSetAttribute(fit_dxyz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  CUtensorMap ta, tb;
+  DPGB_TRY(encode_bf16_2d(&ta, f.A, f.row0[f.ntypes], f.K, f.lda, 128));
+  DPGB_TRY(encode_bf16_2d(&tb, f.B, f.ntypes * f.ng * kDxM, f.K, f.K, kDxBN));
+  fit_dxyz_kernel<<<f.tile0[f.ntypes], 256, smem, st>>>(ta, tb, f, err);
+  return check_launch("fit_dxyz");
 }
 
 int launch_fit_gemm(const FitGemm& g, int* err, cudaStream_t st) {

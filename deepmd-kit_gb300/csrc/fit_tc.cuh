@@ -48,7 +48,25 @@ struct FitGemm {
   int ldo;
 };
 
+// dE/dD of the first fitting layer (dD = dP1 . W1 per type) folded straight
+// into dE/dxyz, dD never stored: for row r, dxyz[r][n][c] = (sum_m dD[n][m]
+// xyz[c][m] + [n < 16] sum_n' dD[n'][n] xyz[c][n']) / nnei, with dD[n][m] =
+// column 16 n + m (axis width 16).
+struct FitDxyz {
+  int ntypes;
+  int row0[9], tile0[9];   // as FitGemm
+  int K;                   // width of the first hidden layer
+  int ng, nnei;
+  const __nv_bfloat16* A;  // dP1 [rows, lda] (type-sorted rows)
+  int lda;
+  const __nv_bfloat16* B;  // W1 per type [type][16 ng][K]
+  const float* xyz;        // [rows (original order)][4][ng]
+  const int* sorted_rows;  // sorted row -> original row
+  float* dxyz;             // [rows (original order)][ng][4]
+};
+
 int fit_tc_eligible(const dpgb_se_a_desc& d);
 int launch_fit_gemm(const FitGemm& g, int* err, cudaStream_t st);
+int launch_fit_dxyz(const FitDxyz& f, int* err, cudaStream_t st);
 
 }  // namespace dpgb
