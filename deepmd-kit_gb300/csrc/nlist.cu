@@ -406,14 +406,33 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
 // per-type placement: the list is bitwise that of nlist_pt_kernel.  A cell
 // whose stencil holds more than stage_cap atoms is flagged and left to
 // nlist_pt_kernel.
-constexpr int kCellWarps = 4;
+constexpr int kCellWarps = 8;   // warps of nlist_cell_kernel (four CTAs, 32 warps per SM)
+constexpr int kBatchWarps = 4;  // warps of nlist_cell_batch_kernel
 constexpr int kKeptCap = 512;  // per-warp kept pairs of the skin selection
 // Shared memory of the staged kernels: stage_cap stencil atoms (3 floats, 2
 // ints) and, for typed lists, kept_cap pairs per warp (a double key, 2 ints).
-// 54 KB per CTA keeps four CTAs (16 warps) on an SM: typed lists stage 1536
-// atoms and keep 384 pairs per warp; flat candidate rows keep none and stage
-// 2688 (a stencil at rcut + skin).
-constexpr int kTypedStageCap = 1536, kTypedKeptCap = 384, kFlatStageCap = 2688;
+// Typed lists stage 1536 atoms and keep 192 pairs per warp (55 KB: four
+// CTAs per SM) unless the mean density asks for more (typed_kept_cap);
+// flat candidate rows keep none and stage 2688 (a stencil at rcut + skin).
+constexpr int kTypedStageCap = 1536, kTypedKeptMin = 192, kTypedKeptMax = 384, kFlatStageCap = 2688;
+
+// Kept pairs per warp for typed lists: 1.5 x the mean count within rcut
+// (the atoms' mean density) + 48, in [192, 384].  An atom with more
+// candidates sends its cell to nlist_pt_kernel.
+int typed_kept_cap(const CellGeom& g, int nloc, double rcut) {
+  double vol;
+  if (g.periodic) {
+    const double* c = g.cell;
+    vol = std::fabs(c[0] * (c[4] * c[8] - c[5] * c[7]) - c[1] * (c[3] * c[8] - c[5] * c[6]) +
+                    c[2] * (c[3] * c[7] - c[4] * c[6]));
+  } else {
+    vol = g.csize[0] * g.csize[1] * g.csize[2] * g.ncell[0] * g.ncell[1] * g.ncell[2];
+  }
+  const double mean = vol > 0 ? nloc / vol * (4.0 / 3.0) * 3.141592653589793 * rcut * rcut * rcut : 0.0;
+  const double want = 1.5 * mean + 48.0;
+  const int cap = want >= kTypedKeptMax ? kTypedKeptMax : ((int)want + 31) / 32 * 32;
+  return cap < kTypedKeptMin ? kTypedKeptMin : cap;
+}
 
 size_t cell_stage_smem(int stage_cap, int kept_cap) {
   return (size_t)stage_cap * (3 * sizeof(float) + 2 * sizeof(int)) +
@@ -544,15 +563,41 @@ __device__ __forceinline__ void warp_sort128(float k[4], int e[4], int t[4], int
   }
 }
 
-// Placement of up to 128 kept pairs with FP32 keys wf (within eps of the
-// exact distances) through a warp sort: the sorted position is the global
-// rank, same-type lanes of each 32-chunk (match_any) plus the running count
-// of their type (s_base, per warp) give the rank within the type.  Two
-// neighbours in the sorted order closer than tie = 2 eps (or equal) may
-// order differently in FP64: then nothing is placed and it returns true.
-__device__ bool sort_place_f32(int* __restrict__ row, const float* __restrict__ wf, const int* __restrict__ wi,
-                               const int* __restrict__ wt, int n, float tie, const SelInfo& sel, int lane,
-                               int* __restrict__ status, int* __restrict__ s_base) {
+// Exact FP64 distance from the centre atom (xi, yi, zi) of the atom with
+// extended index e = s * nloc + j (atom a_beg + j, shift vector s), as the
+// exact path (exact_keep) computes it.
+struct ExactDist {
+  const double* coord;
+  const double* svec;
+  int nloc, a_beg;
+  double xi, yi, zi;
+  __device__ __forceinline__ double operator()(int e) const {
+    const int s = e / nloc, j = a_beg + (e - s * nloc);
+    return dist_fma((coord[3 * j] + svec[3 * s]) - xi, (coord[3 * j + 1] + svec[3 * s + 1]) - yi,
+                    (coord[3 * j + 2] + svec[3 * s + 2]) - zi);
+  }
+};
+
+// bit p of a 128-bit mask held as four words
+__device__ __forceinline__ bool bit128(const unsigned (&w)[4], int p) {
+  const int q = p >> 5;
+  const unsigned v = q == 0 ? w[0] : (q == 1 ? w[1] : (q == 2 ? w[2] : w[3]));
+  return (v >> (p & 31)) & 1u;
+}
+
+// Placement of up to 128 kept pairs with FP32 keys (the first floats of wr,
+// within eps of the exact distances) through a warp sort: the sorted
+// position is the global rank, same-type lanes of each 32-chunk
+// (match_any) plus the running count of their type (s_base, per warp) give
+// the rank within the type.  Neighbours in the sorted order whose keys are
+// closer than tie = 2 eps (or equal) may order differently in FP64; each
+// maximal run of such positions is re-ranked by exact (distance, extended
+// index), which leaves the order that of the exact ranking: a key more than
+// 2 eps below another has the smaller exact distance.
+__device__ void sort_place_f32(int* __restrict__ row, double* __restrict__ wr, int* __restrict__ wi,
+                               int* __restrict__ wt, int n, float tie, const ExactDist& exact, const SelInfo& sel,
+                               int lane, int* __restrict__ status, int* __restrict__ s_base) {
+  const float* wf = reinterpret_cast<const float*>(wr);
   float k[4];
   int e[4], t[4];
 #pragma unroll
@@ -563,16 +608,60 @@ __device__ bool sort_place_f32(int* __restrict__ row, const float* __restrict__ 
     t[q] = idx < n ? wt[idx] : -1;
   }
   warp_sort128(k, e, t, lane);
-  bool near = false;
+  unsigned near[4];  // bit p: sorted positions p and p + 1 are within tie
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     float next = __shfl_down_sync(0xffffffffu, k[q], 1);
     const float first_next = __shfl_sync(0xffffffffu, k[q < 3 ? q + 1 : q], 0);
     if (lane == 31) next = first_next;
     const int idx = q * 32 + lane;
-    near |= idx + 1 < n && next - k[q] <= tie;
+    near[q] = __ballot_sync(0xffffffffu, idx + 1 < n && next - k[q] <= tie);
   }
-  if (__any_sync(0xffffffffu, near)) return true;
+  if (near[0] | near[1] | near[2] | near[3]) {
+    __syncwarp();  // every lane has read its FP32 key before wr is overwritten
+    bool member[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int p = q * 32 + lane;
+      member[q] = bit128(near, p) || (p > 0 && bit128(near, p - 1));
+      wi[p] = e[q];
+      wt[p] = t[q];
+      if (member[q]) wr[p] = exact(e[q]);
+    }
+    __syncwarp();
+    int np[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int p = q * 32 + lane;
+      np[q] = p;
+      if (member[q]) {
+        int lo = p, hi = p;
+        while (lo > 0 && bit128(near, lo - 1)) --lo;
+        while (bit128(near, hi)) ++hi;  // a near bit needs p + 1 < n <= 128
+        const double r = wr[p];
+        int c = 0;
+        for (int m = lo; m <= hi; ++m) {
+          const double rm = wr[m];
+          c += rm < r || (rm == r && wi[m] < e[q]);
+        }
+        np[q] = lo + c;
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (member[q]) {
+        wi[np[q]] = e[q];
+        wt[np[q]] = t[q];
+      }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int p = q * 32 + lane;
+      e[q] = wi[p];
+      t[q] = wt[p];
+    }
+  }
   if (lane < sel.ntypes) s_base[lane] = 0;
   __syncwarp();
   const unsigned below = (1u << lane) - 1u;
@@ -587,7 +676,6 @@ __device__ bool sort_place_f32(int* __restrict__ row, const float* __restrict__ 
     const int idx = q * 32 + lane;
     if (idx < n) place_pair(row, idx, tr, tq, e[q], sel, status);
   }
-  return false;
 }
 
 // Exact FP64 distances of a warp's packed candidates (extended indices wi,
@@ -712,9 +800,14 @@ __device__ int staged_list_atom(int* __restrict__ row, double* __restrict__ wr, 
   if (nc > kept_cap) return -nc - 1;
   band = __any_sync(0xffffffffu, band);
   __syncwarp();
-  if (!band && !(nc <= 128 ? sort_place_f32(row, wf, wi, wt, nc, 2.f * eps, sel, lane, status, s_base)
-                            : rank_place_f32(row, wf, wi, wt, nc, 2.f * eps, sel, lane, status)))
-    return 0;
+  if (!band) {
+    if (nc <= 128) {
+      sort_place_f32(row, wr, wi, wt, nc, 2.f * eps, ExactDist{coord, svec, nloc, a_beg, xi, yi, zi}, sel, lane,
+                     status, s_base);
+      return 0;
+    }
+    if (!rank_place_f32(row, wf, wi, wt, nc, 2.f * eps, sel, lane, status)) return 0;
+  }
   // exact FP64: clear what the FP32 pass may have placed, then rank exactly
   if (lane == 0) atomicAdd(&status[kStatusExact], 1);
   __syncwarp();
@@ -725,7 +818,7 @@ __device__ int staged_list_atom(int* __restrict__ row, double* __restrict__ wr, 
   return 0;
 }
 
-__global__ void __launch_bounds__(kCellWarps * 32)
+__global__ void __launch_bounds__(kCellWarps * 32, 4)
 nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, const int* __restrict__ atype,
                   const int* __restrict__ offsets, const int* __restrict__ cell_atoms,
                   const int* __restrict__ shift_pos, const double* __restrict__ svec, int nloc, CellGeom g,
@@ -1089,27 +1182,27 @@ constexpr int kBatchKeptCap = 384;
 
 size_t batch_stage_smem() {
   return (size_t)kBatchStageCap * (3 * sizeof(float) + 2 * sizeof(int)) +
-         (size_t)kCellWarps * kBatchKeptCap * (sizeof(double) + 2 * sizeof(int));
+         (size_t)kBatchWarps * kBatchKeptCap * (sizeof(double) + 2 * sizeof(int));
 }
 
 // nlist_cell_kernel over the cells of all frames; a cell whose stencil holds
 // more than kBatchStageCap atoms, or an atom with more than kBatchKeptCap
 // neighbours, is reported as an overflow
-__global__ void __launch_bounds__(kCellWarps * 32)
+__global__ void __launch_bounds__(kBatchWarps * 32)
 nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coord, const int* __restrict__ atype,
                         const int* __restrict__ offsets, const int* __restrict__ cell_atoms,
                         const int* __restrict__ shift_pos_all, const double* __restrict__ svec_all, FrameTab ft,
                         double rcut, SelInfo sel, int* __restrict__ status) {
   extern __shared__ __align__(16) unsigned char smem[];
   double* kr = reinterpret_cast<double*>(smem);
-  float4* s4 = reinterpret_cast<float4*>(kr + kCellWarps * kBatchKeptCap);  // staged x, y, z, type bits
+  float4* s4 = reinterpret_cast<float4*>(kr + kBatchWarps * kBatchKeptCap);  // staged x, y, z, type bits
   int* sidx = reinterpret_cast<int*>(s4 + kBatchStageCap);
   int* kidx = sidx + kBatchStageCap;
-  int* ktype = kidx + kCellWarps * kBatchKeptCap;
+  int* ktype = kidx + kBatchWarps * kBatchKeptCap;
   // stencil of (2 reach + 1)^3 cells, reach <= 2 per direction (a frame
   // thinner than rcut across a face has one cell and reach 2 there)
   __shared__ int s_cell[125], s_shift[125], s_off[126];
-  __shared__ int s_tb[kCellWarps][DPGB_MAX_TYPES];
+  __shared__ int s_tb[kBatchWarps][DPGB_MAX_TYPES];
   __shared__ double s_oc[3];
   const int cg = blockIdx.x, tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
@@ -1169,7 +1262,7 @@ nlist_cell_batch_kernel(int* __restrict__ nlist, const double* __restrict__ coor
   double* wr = kr + warp * kBatchKeptCap;
   int* wi = kidx + warp * kBatchKeptCap;
   int* wt = ktype + warp * kBatchKeptCap;
-  for (int a = offsets[cg] + warp; a < offsets[cg + 1]; a += kCellWarps) {
+  for (int a = offsets[cg] + warp; a < offsets[cg + 1]; a += kBatchWarps) {
     const int i = cell_atoms[a];  // global atom
     int* row = nlist + (size_t)i * sel.nnei;
     for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
@@ -1323,9 +1416,14 @@ skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int nc
   }
   band = __any_sync(0xffffffffu, band);
   __syncwarp();
-  if (!band && !(n <= 128 ? sort_place_f32(row, wf, wi, wt, n, 2.f * eps, sel, lane, status, s_tb[warp])
-                           : rank_place_f32(row, wf, wi, wt, n, 2.f * eps, sel, lane, status)))
-    return;
+  if (!band) {
+    if (n <= 128) {
+      sort_place_f32(row, wr, wi, wt, n, 2.f * eps, ExactDist{coord, svec, nloc, 0, xi, yi, zi}, sel, lane, status,
+                     s_tb[warp]);
+      return;
+    }
+    if (!rank_place_f32(row, wf, wi, wt, n, 2.f * eps, sel, lane, status)) return;
+  }
   if (lane == 0) atomicAdd(&status[kStatusExact], 1);
   __syncwarp();
   for (int q = lane; q < sel.nnei; q += 32) row[q] = -1;
@@ -1366,7 +1464,7 @@ int launch_nlist_batch(int* nlist, double* coord_out, const double* coord_in, co
   DPGB_TRY(check_launch("cell_fill_batch"));
   const size_t smem = batch_stage_smem();
   DPGB_CUDA(cudaFuncSetAttribute(nlist_cell_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  nlist_cell_batch_kernel<<<ncells, kCellWarps * 32, smem, st>>>(nlist, coord_out, atype, offsets, cell_atoms,
+  nlist_cell_batch_kernel<<<ncells, kBatchWarps * 32, smem, st>>>(nlist, coord_out, atype, offsets, cell_atoms,
                                                                   shift_pos, svec, ft, rcut, sel, status);
   return check_launch("nlist_cell_batch");
 }
@@ -1454,7 +1552,8 @@ int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc,
   // thinner than 2 rcut across a face) goes to the per-atom kernel whole
   const bool staged = g.reach[0] == 1 && g.reach[1] == 1 && g.reach[2] == 1;
   if (staged) {
-    const int stage_cap = sel.flat ? kFlatStageCap : kTypedStageCap, kept_cap = sel.flat ? 0 : kTypedKeptCap;
+    const int stage_cap = sel.flat ? kFlatStageCap : kTypedStageCap,
+              kept_cap = sel.flat ? 0 : typed_kept_cap(g, nloc, rcut);
     const size_t smem = cell_stage_smem(stage_cap, kept_cap);
     DPGB_CUDA(cudaFuncSetAttribute(nlist_cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     nlist_cell_kernel<<<ncell, kCellWarps * 32, smem, st>>>(nlist, coord, atype, offsets, cell_atoms, shift_pos_dev,
