@@ -11,8 +11,9 @@
 // counted in bytes on the stage's "full" barrier) by one producer thread,
 // while one MMA thread consumes the stages and releases each through its
 // "empty" barrier when the MMAs reading it commit.  Rows past the operand's
-// end and K past its width arrive as zeros.  The epilogue stores 16
-// consecutive columns per thread (64-byte segments).
+// end and K past its width arrive as zeros.  The epilogue runs one thread
+// per row in each of WG warp groups, which split the tile's columns; each
+// thread stores 16 consecutive columns at a time (64-byte segments).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -56,8 +57,8 @@ __device__ __forceinline__ void st16b(__nv_bfloat16* p, const float* v) {
   q[1] = *reinterpret_cast<uint4*>(&h[4]);
 }
 
-template <int BN, int S>
-__global__ void __launch_bounds__(128)
+template <int BN, int S, int WG>
+__global__ void __launch_bounds__(128 * WG)
 fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b, FitGemm g,
                 int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
@@ -65,7 +66,9 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   unsigned char* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
   __shared__ uint64_t full[S], empty[S], done;
   __shared__ uint32_t s_tmem;
-  constexpr int SA = 128 * kKC * 2, SB = BN * kKC * 2;
+  __shared__ float s_e[2 * (WG - 1) * 128 + 2];  // compensated partial energies of column groups 1 .. WG-1
+  constexpr int SA = 128 * kKC * 2, SB = BN * kKC * 2, CW = BN / WG;
+  static_assert(CW % 16 == 0, "column groups of whole 16-column loads");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   int t = 0;
   while (t + 1 < g.ntypes && g.tile0[t + 1] <= (int)blockIdx.x) ++t;
@@ -119,18 +122,22 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   ok = tc::mbar_wait(&done, 0, err) && ok;
   tc::fence_after();
   ok = __syncthreads_and(ok) != 0;
+  // epilogue: thread = row (warp quadrant q = TMEM lanes 32 q ..), the
+  // WG warp groups take consecutive BN / WG column ranges
+  const int q = warp & 3, h = warp >> 2;
+  const int r = q * 32 + lane;
+  const int m = m0 + r;
+  const bool valid = r < rows_valid;
+  float e_hi = 0.f, e_lo = 0.f;  // output layer: compensated sum of y w over this group's columns
   if (ok) {
-    const int r = warp * 32 + lane;
-    const int m = m0 + r;
-    const bool valid = r < rows_valid;
-    double e_acc = 0.0;
     const float* bias = g.bias ? g.bias + (size_t)t * g.N : nullptr;
     const float* idt = g.idt ? g.idt + (size_t)t * g.N : nullptr;
     const float* idt_lo = g.idt_lo ? g.idt_lo + (size_t)t * g.N : nullptr;
     const float* wo = g.w_out ? g.w_out + (size_t)t * g.N : nullptr;
-    for (int c0 = 0; c0 < nt; c0 += 16) {
+    const int cend = min(nt, (h + 1) * CW);
+    for (int c0 = h * CW; c0 < cend; c0 += 16) {
       float v[16];
-      tc::tmem_ld16(tc::taddr(tbase, warp * 32, c0), v);
+      tc::tmem_ld16(tc::taddr(tbase, q * 32, c0), v);
       tc::tmem_ld_wait();
       if (!valid) continue;
       const int n = n0 + c0;
@@ -154,7 +161,9 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
           ld16f(wo + n, w);
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
-            e_acc += (double)y[i] * (double)w[i];
+            const float pr = y[i] * w[i];
+            comp_add(e_hi, e_lo, pr);
+            e_lo += fmaf(y[i], w[i], -pr);  // the product's rounding error
             dp[i] = w[i] * (idt ? id[i] : 1.f) * (1.f - tv[i] * tv[i]);
           }
           st16b(g.dPb + (size_t)m * g.ldy + n, dp);
@@ -178,7 +187,20 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
         st16f(g.out + (size_t)m * g.ldo + n, v);
       }
     }
-    if (g.mode == kFitFwdLast && valid) g.e_out[m] = e_acc + (double)g.b_out[t];
+  }
+  if (g.mode == kFitFwdLast) {
+    if (h > 0) {
+      s_e[2 * ((h - 1) * 128 + r)] = e_hi;
+      s_e[2 * ((h - 1) * 128 + r) + 1] = e_lo;
+    }
+    __syncthreads();
+    if (ok && h == 0 && valid) {
+      for (int k = 1; k < WG; ++k) {
+        comp_add(e_hi, e_lo, s_e[2 * ((k - 1) * 128 + r)]);
+        e_lo += s_e[2 * ((k - 1) * 128 + r) + 1];
+      }
+      g.e_out[m] = ((double)e_hi + (double)e_lo) + (double)g.b_out[t];
+    }
   }
   tc::fence_before();
   __syncthreads();
@@ -375,19 +397,19 @@ int encode_bf16_2d(CUtensorMap* m, const __nv_bfloat16* base, int rows, int cols
   return DPGB_OK;
 }
 
-template <int BN, int S>
+template <int BN, int S, int WG>
 int launch_t(const FitGemm& g, int* err, cudaStream_t st) {
   const size_t smem = (size_t)S * (128 + BN) * kKC * 2 + 1024;  // + alignment slack
   static bool attr = false;
   if (!attr) {
-    DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel<BN, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel<BN, S, WG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
   CUtensorMap ta, tb;
   DPGB_TRY(encode_bf16_2d(&ta, g.A, g.row0[g.ntypes], g.K, g.lda, 128));
   DPGB_TRY(encode_bf16_2d(&tb, g.B, g.ntypes * g.N, g.K, g.K, BN));
   dim3 grid(g.tile0[g.ntypes], ceil_div(g.N, BN));
-  fit_gemm_kernel<BN, S><<<grid, 128, smem, st>>>(ta, tb, g, err);
+  fit_gemm_kernel<BN, S, WG><<<grid, 128 * WG, smem, st>>>(ta, tb, g, err);
   return check_launch("fit_gemm");
 }
 
@@ -420,8 +442,8 @@ int launch_fit_dxyz(const FitDxyz& f, int* err, cudaStream_t st) {
 
 int launch_fit_gemm(const FitGemm& g, int* err, cudaStream_t st) {
   if (g.tile0[g.ntypes] <= 0) return DPGB_OK;
-  if (g.mode == kFitFwdLast) return launch_t<256, 3>(g, err, st);  // the output layer needs whole rows
-  return launch_t<128, 3>(g, err, st);
+  if (g.mode == kFitFwdLast) return launch_t<256, 3, 2>(g, err, st);  // the output layer needs whole rows
+  return launch_t<128, 3, 2>(g, err, st);
 }
 
 }  // namespace dpgb
