@@ -67,8 +67,9 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   __shared__ uint64_t full[S], empty[S], done;
   __shared__ uint32_t s_tmem;
   __shared__ float s_e[2 * (WG - 1) * 128 + 2];  // compensated partial energies of column groups 1 .. WG-1
-  constexpr int SA = 128 * kKC * 2, SB = BN * kKC * 2, CW = BN / WG;
-  static_assert(CW % 16 == 0, "column groups of whole 16-column loads");
+  constexpr int SA = 128 * kKC * 2, SB = BN * kKC * 2;
+  constexpr uint32_t kTmemCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+  static_assert(BN % 16 == 0 && BN <= 256 && SB % 1024 == 0, "whole 16-column loads, 1024-byte aligned stages");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   int t = 0;
   while (t + 1 < g.ntypes && g.tile0[t + 1] <= (int)blockIdx.x) ++t;
@@ -76,7 +77,7 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   const int rows_valid = min(128, g.row0[t + 1] - m0);
   const int n0 = blockIdx.y * BN;
   const int nt = min(BN, g.N - n0);  // multiple of 16
-  if (warp == 0) tc::tmem_alloc(&s_tmem, BN < 32 ? 32 : BN);
+  if (warp == 0) tc::tmem_alloc(&s_tmem, kTmemCols);
   if (tid == 0) {
     for (int s = 0; s < S; ++s) {
       tc::mbar_init(&full[s], 1);
@@ -123,7 +124,7 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   tc::fence_after();
   ok = __syncthreads_and(ok) != 0;
   // epilogue: thread = row (warp quadrant q = TMEM lanes 32 q ..), the
-  // WG warp groups take consecutive BN / WG column ranges
+  // WG warp groups take the tile's 16-column groups in turn
   const int q = warp & 3, h = warp >> 2;
   const int r = q * 32 + lane;
   const int m = m0 + r;
@@ -134,8 +135,7 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
     const float* idt = g.idt ? g.idt + (size_t)t * g.N : nullptr;
     const float* idt_lo = g.idt_lo ? g.idt_lo + (size_t)t * g.N : nullptr;
     const float* wo = g.w_out ? g.w_out + (size_t)t * g.N : nullptr;
-    const int cend = min(nt, (h + 1) * CW);
-    for (int c0 = h * CW; c0 < cend; c0 += 16) {
+    for (int c0 = h * 16; c0 < nt; c0 += 16 * WG) {
       float v[16];
       tc::tmem_ld16(tc::taddr(tbase, q * 32, c0), v);
       tc::tmem_ld_wait();
@@ -204,7 +204,7 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   }
   tc::fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, BN < 32 ? 32 : BN);
+  if (warp == 0) tc::tmem_dealloc(tbase, kTmemCols);
 }
 
 // dE/dD of the first layer folded into dE/dxyz (FitDxyz).  One CTA per
@@ -441,8 +441,15 @@ int launch_fit_dxyz(const FitDxyz& f, int* err, cudaStream_t st) {
 }
 
 int launch_fit_gemm(const FitGemm& g, int* err, cudaStream_t st) {
-  if (g.tile0[g.ntypes] <= 0) return DPGB_OK;
+  const int mt = g.tile0[g.ntypes];
+  if (mt <= 0) return DPGB_OK;
   if (g.mode == kFitFwdLast) return launch_t<256, 3, 2>(g, err, st);  // the output layer needs whole rows
+  // column tile: the narrower one when it spreads the tiles more evenly over
+  // the SMs (two CTAs fit on an SM either way): for 240 columns, three
+  // 80-wide tiles per row tile rather than a 128 + 112 pair
+  const int sms = sm_count();
+  auto span = [&](int bn) { return (long long)ceil_div(mt * ceil_div(g.N, bn), 2 * sms) * bn; };
+  if (g.N % 80 == 0 && span(80) < span(128)) return launch_t<80, 3, 2>(g, err, st);
   return launch_t<128, 3, 2>(g, err, st);
 }
 
