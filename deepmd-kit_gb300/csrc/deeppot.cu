@@ -262,20 +262,31 @@ force_gather_batch_kernel(double* __restrict__ force, double* __restrict__ atom_
 
 // Per-frame sums of the atom energies and atom virials in two passes with a
 // fixed partition, so the result does not depend on scheduling: pass 1 gives
-// every chunk of kFrameChunk rows of a frame its 10 partial sums (energy, 9
+// every chunk of `chunk` rows of a frame its 10 partial sums (energy, 9
 // virial components), pass 2 adds a frame's chunk partials in chunk order.
 // Frame f covers rows [atom_off[f], atom_off[f+1]) or, without atom_off,
 // [f*nloc, (f+1)*nloc).
-constexpr int kFrameChunk = 2048;
 constexpr int kFrameSumThreads = 256;
+
+// rows per partial sum: about two blocks per SM over all frames, a power of
+// two in [256, 2048]; batches of frames of different sizes keep 2048 (their
+// grid spans the largest frame)
+int frame_chunk(long long rows, bool batch) {
+  if (batch) return 2048;
+  const long long want = rows / (2LL * sm_count());
+  int c = 256;
+  while (c < 2048 && c < want) c <<= 1;
+  return c;
+}
 
 __global__ void __launch_bounds__(kFrameSumThreads) frame_part_kernel(double* __restrict__ part,
                                                                       const double* __restrict__ e_row,
                                                                       const double* __restrict__ vir_row,
-                                                                      const int* __restrict__ atom_off, int nloc) {
+                                                                      const int* __restrict__ atom_off, int nloc,
+                                                                      int chunk) {
   const int c = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
   const int lo = atom_off ? atom_off[f] : f * nloc, hi = atom_off ? atom_off[f + 1] : (f + 1) * nloc;
-  const int r0 = lo + c * kFrameChunk, r1 = min(hi, r0 + kFrameChunk);
+  const int r0 = lo + c * chunk, r1 = min(hi, r0 + chunk);
   double acc[10];
 #pragma unroll
   for (int q = 0; q < 10; ++q) acc[q] = 0.0;
@@ -943,7 +954,8 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   DPGB_TRY(dp.ws_erow.alloc(sizeof(double) * nrows));
   DPGB_TRY(dp.ws_esorted.alloc(sizeof(double) * nrows));
   const int sum_frames = batch ? batch->ft.nframes : nframes;
-  const int sum_chunks = ceil_div(batch ? batch->max_atoms : natom, kFrameChunk);
+  const int sum_chunk = frame_chunk((long long)sum_frames * (batch ? batch->max_atoms : natom), batch != nullptr);
+  const int sum_chunks = ceil_div(batch ? batch->max_atoms : natom, sum_chunk);
   DPGB_TRY(dp.ws_part.alloc(sizeof(double) * 10 * (size_t)sum_frames * sum_chunks));
   DPGB_TRY(dp.ws_act.alloc(sizeof(T) * 2 * m.fit.n_hidden * nrows * maxw));
   DPGB_TRY(dp.ws_gbuf.alloc(sizeof(T) * 4 * nrows * maxw));
@@ -1278,7 +1290,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
                                                            (int)nrows);
   DPGB_TRY(check_launch("atom_energy"));
   frame_part_kernel<<<dim3(sum_chunks, sum_frames), kFrameSumThreads, 0, st>>>(
-      dp.ws_part.as<double>(), e_row, dp.ws_vir.as<double>(), batch ? batch->ft.atom_off : nullptr, natom);
+      dp.ws_part.as<double>(), e_row, dp.ws_vir.as<double>(), batch ? batch->ft.atom_off : nullptr, natom, sum_chunk);
   DPGB_TRY(check_launch("frame_part"));
   frame_final_kernel<<<ceil_div(sum_frames, 8), 256, 0, st>>>(energy, virial, dp.ws_part.as<double>(), sum_chunks,
                                                                sum_frames);

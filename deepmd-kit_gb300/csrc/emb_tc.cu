@@ -30,6 +30,8 @@ int emb_tc_eligible(const dpgb_se_a_desc& d) {
   const bool shape_a = (w1 == 25 && w2 == 50 && w3 == 100);
   const bool shape_b = (w1 == 3 && w2 == 6 && w3 == 12);
   if (!shape_a && !shape_b) return 0;
+  // two spare padding columns after layers 1 and 2 carry the biases
+  if (pad16(w1) - w1 < 2 || bias_col(1, w2, w1, pad16(w2)) < 0) return 0;
   for (int t = 0; t < d.ntypes; ++t)
     if (d.sel[t] > kTcRows) return 0;
   return 1;
@@ -47,6 +49,14 @@ size_t emb_tc_image_bytes(const EmbTC& m, int kind) {
 static void put_bf16(std::vector<unsigned char>& img, size_t base, int r, int k, int K, float v) {
   const __nv_bfloat16 b = __float2bfloat16_rn(v);
   std::memcpy(img.data() + base + tc::cm_offset(r, k, K), &b, 2);
+}
+
+// bias b of output row r as BF16 hi + lo on the K columns k_hi, k_lo (the
+// operand holds 1 there)
+static void put_bias(std::vector<unsigned char>& img, size_t base, int r, int k_hi, int k_lo, int K, double b) {
+  const __nv_bfloat16 hi = __float2bfloat16_rn((float)b);
+  put_bf16(img, base, r, k_hi, K, (float)b);
+  put_bf16(img, base, r, k_lo, K, (float)(b - (double)__bfloat162float(hi)));
 }
 
 int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, EmbTC& m, std::vector<float>& vec) {
@@ -71,7 +81,14 @@ int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, Em
     if (!W1 || !W2 || !W3 || !d.emb_b[e][0] || !d.emb_b[e][1] || !d.emb_b[e][2]) return fail(DPGB_EINVAL, "missing embedding weights");
     const size_t b0 = per[0] * e, b1 = per[0] * nnets + per[1] * e, b2 = (per[0] + per[1]) * nnets + per[2] * e,
                  b3 = (per[0] + per[1] + per[2]) * nnets + per[3] * e;
-    // layer-2 outputs o sit at column c2 = neuron_col(o), layer-3 outputs at c3
+    // layer-2 outputs o sit at column c2 = neuron_col(o), layer-3 outputs at
+    // c3; the biases of layers 2 and 3 on the bias columns of their inputs
+    const int k2a = m.w1, k2b = m.w1 + 1;
+    const int k3a = bias_col(0, m.w2, m.w1, m.n2), k3b = bias_col(1, m.w2, m.w1, m.n2);
+    for (int o = 0; o < m.w2; ++o)
+      put_bias(images, b0, neuron_col(o, m.w2, m.w1), k2a, k2b, m.k1, d.emb_b[e][1][o]);
+    for (int o = 0; o < m.w3; ++o)
+      put_bias(images, b1, neuron_col(o, m.w3, m.w2), k3a, k3b, m.n2, d.emb_b[e][2][o]);
     for (int o = 0; o < m.w2; ++o)
       for (int k = 0; k < m.w1; ++k) {
         const int c2 = neuron_col(o, m.w2, m.w1);
@@ -303,6 +320,8 @@ template <int W1, int W2, int W3>
 struct PlanF {
   static constexpr int K1 = (W1 + 15) / 16 * 16, N2 = (W2 + 15) / 16 * 16, N3 = (W3 + 15) / 16 * 16;
   static constexpr int LDG = (W3 + 3) / 4 * 4;  // fp32 G row stride: float4 rows
+  // operand columns holding 1 for the biases of layers 2 (A1) and 3 (A2)
+  static constexpr int ONE2a = W1, ONE2b = W1 + 1, ONE3a = bias_col(0, W2, W1, N2), ONE3b = bias_col(1, W2, W1, N2);
   static constexpr int VEC = 3 * K1 + 2 * N2 + 2 * N3;
   static constexpr int fw2 = 0;
   static constexpr int fw3 = fw2 + N2 * K1 * 2;
@@ -324,6 +343,7 @@ template <int W1, int W2, int W3>
 struct PlanB {
   static constexpr int K1 = (W1 + 15) / 16 * 16, N2 = (W2 + 15) / 16 * 16, N3 = (W3 + 15) / 16 * 16;
   static constexpr int VEC = 3 * K1 + 2 * N2 + 2 * N3;
+  static constexpr int ONE2a = W1, ONE2b = W1 + 1, ONE3a = bias_col(0, W2, W1, N2), ONE3b = bias_col(1, W2, W1, N2);
   static constexpr int fw2 = 0;
   static constexpr int fw3 = fw2 + N2 * K1 * 2;
   static constexpr int bw3 = fw3 + N3 * N2 * 2;
@@ -337,7 +357,7 @@ struct PlanB {
   static constexpr int tmem_cols = cmax(N3, N2 + K1) <= 128 ? 128 : 256;
 };
 
-template <int W1, int W2, int W3>
+template <int W1, int W2, int W3, bool IDT>
 __global__ void __launch_bounds__(128, 3)
 emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ chunks, int nchunks,
                   const int* __restrict__ run_len, const int* __restrict__ sorted_rows, float* __restrict__ xyz,
@@ -396,17 +416,18 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         float h1[W1];
 #pragma unroll
         for (int k = 0; k < W1; ++k) {
-          const float tv = tanh_fast(fmaf(x, w1[k], b1[k]));
-          float h = tv * i1[k];
-          if (W1 == 1) h += x;
-          if (W1 == 2) h += x;
-          h1[k] = pi.valid ? h : 0.f;
+          // rows past the tile's pairs carry finite values no output reads
+          float h = tanh_fast(fmaf(x, w1[k], b1[k]));
+          if (IDT) h *= i1[k];
+          if (W1 == 1 || W1 == 2) h += x;
+          h1[k] = h;
         }
 #pragma unroll
         for (int k0 = 0; k0 < P::K1; k0 += 8) {
           float v[8];
 #pragma unroll
-          for (int i = 0; i < 8; ++i) v[i] = (k0 + i < W1) ? h1[k0 + i] : 0.f;
+          for (int i = 0; i < 8; ++i)
+            v[i] = (k0 + i < W1) ? h1[k0 + i] : (k0 + i == P::ONE2a || k0 + i == P::ONE2b ? 1.f : 0.f);
           store8(smem + P::a1, tid, k0, P::K1, v);
         }
         tc::fence_async_smem();
@@ -419,7 +440,7 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         bool ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout);
         phase ^= 1;
         tc::fence_after();
-        // epilogue 2: H2 = tanh(acc + b2) * idt2 + skip(H1)
+        // epilogue 2: H2 = tanh(acc) * idt2 + skip(H1) (acc includes b2)
         float h2[W2];
 #pragma unroll
         for (int c0 = 0; c0 < P::N2; c0 += 32) {
@@ -429,10 +450,11 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
           for (int i = 0; i < 32; ++i) {
             const int c = c0 + i, o = c < P::N2 ? col_neuron(c, W2, W1) : -1;
             if (o >= 0) {
-              float h = tanh_fast(v[i] + b2[c]) * i2[c];
+              float h = tanh_fast(v[i]);
+              if (IDT) h *= i2[c];
               if (W2 == W1) h += h1[o];
               if (W2 == 2 * W1) h += h1[o < W1 ? o : o - W1];
-              h2[o] = pi.valid ? h : 0.f;
+              h2[o] = h;
             }
           }
         }
@@ -442,7 +464,7 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             const int o = col_neuron(k0 + i, W2, W1);
-            v[i] = o >= 0 ? h2[o] : 0.f;
+            v[i] = o >= 0 ? h2[o] : (k0 + i == P::ONE3a || k0 + i == P::ONE3b ? 1.f : 0.f);
           }
           store8(smem + P::a2, tid, k0, P::N2, v);
         }
@@ -457,7 +479,7 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;
         phase ^= 1;
         tc::fence_after();
-        // epilogue 3: G = tanh(acc + b3) * idt3 + skip(H2), kept in FP32,
+        // epilogue 3: G = tanh(acc) * idt3 + skip(H2) (acc includes b3), kept in FP32,
         // stored as float4 rows
 #pragma unroll
         for (int c0 = 0; c0 < P::N3; c0 += 32) {
@@ -469,10 +491,11 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
             const int c = c0 + i, o = c < P::N3 ? col_neuron(c, W3, W2) : -1;
             g[i] = 0.f;
             if (o >= 0) {
-              float x3 = tanh_fast(v[i] + b3[c]) * i3[c];
+              float x3 = tanh_fast(v[i]);
+              if (IDT) x3 *= i3[c];
               if (W3 == W2) x3 += h2[o];
               if (W3 == 2 * W2) x3 += h2[o < W2 ? o : o - W2];
-              g[i] = pi.valid ? x3 : 0.f;
+              g[i] = x3;
             }
           }
           // G in neuron order; column pairs that hold two consecutive
@@ -574,7 +597,7 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 // through the two transposed-weight MMAs.  The residual terms of dH2 and dH1
 // are folded group by group (col_neuron order) and stored into their
 // accumulators before the MMA adds the weight term.
-template <int W1, int W2, int W3>
+template <int W1, int W2, int W3, bool IDT>
 __global__ void __launch_bounds__(128, 3)
 emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ chunks, int nchunks,
                   const int* __restrict__ run_len, const int* __restrict__ sorted_rows,
@@ -645,21 +668,22 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         float rn[4], dv[3];
         pair_env(p, t, ti, s_row, s_off, ntile, tid, pi, rn, dv);
         const float x = rn[0];
-        const float vmask = pi.valid ? 1.f : 0.f;
         float t1[W1];
 #pragma unroll
         for (int k = 0; k < W1; ++k) t1[k] = tanh_fast(fmaf(x, w1[k], b1[k]));
-        // h1 = t1 idt1 (+ x when the residual concatenates x), 0 off the tile
+        // h1 = t1 idt1 (+ x when the residual concatenates x); rows past the
+        // tile's pairs carry finite values that no output reads
         auto h1 = [&](int k) {
-          float h = t1[k] * i1[k];
+          float h = IDT ? t1[k] * i1[k] : t1[k];
           if (W1 == 1 || W1 == 2) h += x;
-          return h * vmask;
+          return h;
         };
 #pragma unroll
         for (int k0 = 0; k0 < P::K1; k0 += 8) {
           float v[8];
 #pragma unroll
-          for (int i = 0; i < 8; ++i) v[i] = (k0 + i < W1) ? h1(k0 + i) : 0.f;
+          for (int i = 0; i < 8; ++i)
+            v[i] = (k0 + i < W1) ? h1(k0 + i) : (k0 + i == P::ONE2a || k0 + i == P::ONE2b ? 1.f : 0.f);
           store8(smem + P::a1, tid, k0, P::K1, v);
         }
         tc::fence_async_smem();
@@ -672,7 +696,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         bool ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout);
         phase ^= 1;
         tc::fence_after();
-        // epilogue 2: t2 (neuron order); A2 = h2 by column
+        // epilogue 2: t2 (neuron order; the accumulator includes b2); A2 = h2 by column
         float t2[W2];
 #pragma unroll
         for (int c0 = 0; c0 < P::N2; c0 += 16) {
@@ -682,15 +706,15 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int cc = c0 + i, o = col_neuron(cc, W2, W1);
-            if (o >= 0) t2[o] = tanh_fast(v[i] + b2[cc]);
+            if (o >= 0) t2[o] = tanh_fast(v[i]);
           }
         }
         // h2 of neuron o (column cc): t2 idt2 + residual of h1
         auto h2 = [&](int o, int cc) {
-          float h = t2[o] * i2[cc];
+          float h = IDT ? t2[o] * i2[cc] : t2[o];
           if (W2 == W1) h += h1(o);
           if (W2 == 2 * W1) h += h1(o < W1 ? o : o - W1);
-          return h * vmask;
+          return h;
         };
 #pragma unroll
         for (int k0 = 0; k0 < P::N2; k0 += 8) {
@@ -698,7 +722,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             const int o = col_neuron(k0 + i, W2, W1);
-            v[i] = o >= 0 ? h2(o, k0 + i) : 0.f;
+            v[i] = o >= 0 ? h2(o, k0 + i) : (k0 + i == P::ONE3a || k0 + i == P::ONE3b ? 1.f : 0.f);
           }
           store8(smem + P::a2, tid, k0, P::N2, v);
         }
@@ -735,9 +759,9 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
               const int cc = c0 + i + h, o = col_neuron(cc, W3, W2);
               dp[i + h] = 0.f;
               if (o >= 0) {
-                const float tv = tanh_fast(v[i + h] + b3[cc]);
+                const float tv = tanh_fast(v[i + h]);  // the accumulator includes b3
                 const int m = o < W2 ? o : o - W2;
-                const float g = tv * i3[cc] + h2(m, neuron_col(m, W2, W1));
+                const float g = (IDT ? tv * i3[cc] : tv) + h2(m, neuron_col(m, W2, W1));
                 const float4 dq = pi.valid ? dx[o] : make_float4(0.f, 0.f, 0.f, 0.f);
                 drn[0] = fmaf(g, dq.x, drn[0]);
                 drn[1] = fmaf(g, dq.y, drn[1]);
@@ -745,7 +769,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
                 drn[3] = fmaf(g, dq.w, drn[3]);
                 const float dg = rn[0] * dq.x + rn[1] * dq.y + rn[2] * dq.z + rn[3] * dq.w;
                 res += dg;
-                dp[i + h] = dg * i3[cc] * (1.f - tv * tv) * vmask;
+                dp[i + h] = (IDT ? dg * i3[cc] : dg) * (1.f - tv * tv);
               }
             }
             const int o = col_neuron(c0 + i, W3, W2);
@@ -776,7 +800,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int cc = c0 + i, o = col_neuron(cc, W2, W1);
-            dp[i] = o >= 0 ? v[i] * i2[cc] * (1.f - t2[o] * t2[o]) * vmask : 0.f;
+            dp[i] = o >= 0 ? (IDT ? v[i] * i2[cc] : v[i]) * (1.f - t2[o] * t2[o]) : 0.f;
           }
           store8(smem + P::a2, tid, c0, P::N2, dp);
           store8(smem + P::a2, tid, c0 + 8, P::N2, dp + 8);
@@ -810,7 +834,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
             const int k = c0 + i;
             if (k < W1) {
               const float dh = v[i];
-              dss = fmaf(dh * i1[k] * (1.f - t1[k] * t1[k]), w1[k], dss);
+              dss = fmaf((IDT ? dh * i1[k] : dh) * (1.f - t1[k] * t1[k]), w1[k], dss);
               if (W1 == 1 || W1 == 2) dss += dh;
             }
           }
@@ -1011,22 +1035,22 @@ __global__ void dxyz_smem_kernel(float* __restrict__ dxyz, const float* __restri
   }
 }
 
-template <int W1, int W2, int W3>
+template <int W1, int W2, int W3, bool IDT>
 int launch_fwd_t(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks, const int* run_len,
                  const int* sorted_rows, float* xyz, float* xyzp, float* D, int* status, cudaStream_t st, int nsm) {
   using P = PlanF<W1, W2, W3>;
-  auto k = emb_tc_fwd_kernel<W1, W2, W3>;
+  auto k = emb_tc_fwd_kernel<W1, W2, W3, IDT>;
   DPGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, P::total));
   const int grid = nchunks < nsm ? nchunks : nsm;
   k<<<grid, 128, P::total, st>>>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status);
   return check_launch("emb_tc_fwd");
 }
-template <int W1, int W2, int W3>
+template <int W1, int W2, int W3, bool IDT>
 int launch_bwd_t(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks, const int* run_len,
                  const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, int* status, cudaStream_t st,
                  int nsm) {
   using P = PlanB<W1, W2, W3>;
-  auto k = emb_tc_bwd_kernel<W1, W2, W3>;
+  auto k = emb_tc_bwd_kernel<W1, W2, W3, IDT>;
   DPGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, P::total));
   const int grid = nchunks < nsm ? nchunks : nsm;
   k<<<grid, 128, P::total, st>>>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status);
@@ -1049,10 +1073,11 @@ int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChun
                       cudaStream_t st) {
   if (nchunks <= 0) return DPGB_OK;
   const int nsm = 3 * sm_count();  // three CTAs per SM
-  if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100)
-    return launch_fwd_t<25, 50, 100>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status, st, nsm);
-  if (e.w1 == 3 && e.w2 == 6 && e.w3 == 12)
-    return launch_fwd_t<3, 6, 12>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status, st, nsm);
+  const bool idt = e.has_idt1 || e.has_idt2 || e.has_idt3;
+#define DPGB_FWD(a, b, c, i) launch_fwd_t<a, b, c, i>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status, st, nsm)
+  if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100) return idt ? DPGB_FWD(25, 50, 100, true) : DPGB_FWD(25, 50, 100, false);
+  if (e.w1 == 3 && e.w2 == 6 && e.w3 == 12) return idt ? DPGB_FWD(3, 6, 12, true) : DPGB_FWD(3, 6, 12, false);
+#undef DPGB_FWD
   return fail(DPGB_EINVAL, "embedding widths without a tensor-core kernel");
 }
 
@@ -1078,11 +1103,12 @@ int launch_emb_tc_bwd(const DescParams<float>& p, const EmbTC& e, const WorkChun
                       int* status, cudaStream_t st) {
   if (nchunks <= 0) return DPGB_OK;
   const int nsm = 3 * sm_count();  // three CTAs per SM
-  if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100)
-    return launch_bwd_t<25, 50, 100>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status, st,
-                                     nsm);
-  if (e.w1 == 3 && e.w2 == 6 && e.w3 == 12)
-    return launch_bwd_t<3, 6, 12>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status, st, nsm);
+  const bool idt = e.has_idt1 || e.has_idt2 || e.has_idt3;
+#define DPGB_BWD(a, b, c, i) \
+  launch_bwd_t<a, b, c, i>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status, st, nsm)
+  if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100) return idt ? DPGB_BWD(25, 50, 100, true) : DPGB_BWD(25, 50, 100, false);
+  if (e.w1 == 3 && e.w2 == 6 && e.w3 == 12) return idt ? DPGB_BWD(3, 6, 12, true) : DPGB_BWD(3, 6, 12, false);
+#undef DPGB_BWD
   return fail(DPGB_EINVAL, "embedding widths without a tensor-core kernel");
 }
 

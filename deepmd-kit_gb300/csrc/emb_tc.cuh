@@ -28,6 +28,17 @@ __host__ __device__ constexpr int neuron_col(int n, int w_out, int w_in) {
                            : 16 * ((n < w_in ? n : n - w_in) >> 3) + (n < w_in ? 0 : 8) + ((n < w_in ? n : n - w_in) & 7);
 }
 
+// The k-th padding column (k = 0, 1) of a layer's n padded output columns.
+// The next layer's bias rides in the MMA on two such columns: the operand
+// holds 1 there and the weight image the bias split into BF16 hi + lo, so
+// the accumulator arrives with the bias added (to ~2^-17 of it).  The first
+// layer's outputs use their natural order: columns w1 and w1 + 1.
+__host__ __device__ constexpr int bias_col(int k, int w_out, int w_in, int n) {
+  for (int c = 0; c < n; ++c)
+    if (col_neuron(c, w_out, w_in) < 0 && k-- == 0) return c;
+  return -1;
+}
+
 // Per-net weight images (bf16, already in the shared-memory core-matrix
 // layout) and FP32 vectors of a 3-layer embedding net 1 -> w1 -> w2 -> w3.
 // Layer-2 and layer-3 outputs are in col_neuron order (rows of fw2 / fw3,
@@ -41,7 +52,8 @@ struct EmbTC {
   const unsigned char* fw3;  // forward B of layer 3: W3^T [n3 x n2]
   const unsigned char* bw3;  // backward B of layer 3: W3 [n2 x n3]
   const unsigned char* bw2;  // backward B of layer 2: W2 [k1 x n2]
-  const float* vec;          // [nnets][vec_stride]: w1 b1 idt1 | b2 idt2 | b3 idt3 (padded)
+  const float* vec;          // [nnets][vec_stride]: w1 b1 idt1 | b2 idt2 | b3 idt3 (padded; b2, b3 also ride
+                             // in fw2 / fw3 on the bias columns, which is where the kernels take them from)
   int vec_stride;
   int has_idt1, has_idt2, has_idt3;
   int d_bf16;  // per call: write D as BF16 (for the tensor-core fitting)

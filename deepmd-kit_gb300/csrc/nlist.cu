@@ -313,8 +313,11 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
   __shared__ int s_type[kSearchWarps][kCap];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (gate && !gate[0]) return;
-  // atoms in a grid-stride loop: as the fallback of the staged kernel most
-  // atoms only check their cell's flag
+  // as the fallback of the staged kernel: nothing to do unless some cell was
+  // flagged (only_cells[ncell] is set with any flag)
+  if (only_cells && !only_cells[g.ncell[0] * g.ncell[1] * g.ncell[2]]) return;
+  // atoms in a grid-stride loop: as the fallback, most atoms only check their
+  // cell's flag
   for (int i = blockIdx.x * kSearchWarps + warp; i < nloc; i += gridDim.x * kSearchWarps) {
   if (only_cells && !only_cells[cell_of[i]]) continue;  // handled by the staged kernel
   __syncwarp();  // the previous atom's reads of s_r / s_idx / s_type are done
@@ -856,7 +859,7 @@ nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
   __syncthreads();
   const int total = s_off[27];
   if (total > stage_cap) {  // left to nlist_pt_kernel
-    if (tid == 0) fallback[c] = 1;
+    if (tid == 0) fallback[c] = fallback[gridDim.x] = 1;  // [ncell]: some cell is flagged
     return;
   }
   // FP32 copies relative to the centre cell's centre (magnitudes within 1.5
@@ -889,7 +892,7 @@ nlist_cell_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
     const float xf = (float)(xi - ox), yf = (float)(yi - oy), zf = (float)(zi - oz);
     const int r = staged_list_atom(row, wr, wi, wt, s4, sidx, total, self, xf, yf, zf, eps, coord,
                                    svec, nloc, 0, xi, yi, zi, rcut, sel, lane, status, s_tb[warp], kept_cap);
-    if (r < 0 && lane == 0) fallback[c] = 1;  // more than kept_cap candidates: the cell goes to the per-atom kernel
+    if (r < 0 && lane == 0) fallback[c] = fallback[gridDim.x] = 1;  // more than kept_cap candidates: to the per-atom kernel
     __syncwarp();
   }
 }
@@ -1562,7 +1565,7 @@ int launch_nlist_pt(int* nlist, const double* coord, const int* atype, int nloc,
     DPGB_TRY(check_launch("nlist_cell"));
   }
   // as a fallback (staged): a bounded grid whose warps stride over the atoms
-  const int blocks = staged ? std::min(ceil_div(nloc, kSearchWarps), 16 * sm_count()) : ceil_div(nloc, kSearchWarps);
+  const int blocks = staged ? std::min(ceil_div(nloc, kSearchWarps), 4 * sm_count()) : ceil_div(nloc, kSearchWarps);
   nlist_pt_kernel<<<blocks, kSearchWarps * 32, 0, st>>>(nlist, coord, atype, cell_of, offsets, cell_atoms,
                                                         shift_pos_dev, svec_dev, nloc, g, rcut, sel,
                                                         staged ? fallback : nullptr, status, gate);

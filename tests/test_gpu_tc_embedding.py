@@ -68,3 +68,23 @@ def test_tc_mixed_deeppot_testcase(cuda):
         err = _errors(a, r, 6)
         print("deeppot_sea mixed", b, err)
         assert err["f_rmse"] <= 1e-3 and err["e_rel"] <= 1e-4
+
+
+def test_tc_mixed_vs_fp64_resnet_dt(cuda):
+    """Embedding layers with idt (resnet_dt): the tensor-core kernels'
+    idt form against the FP64 form."""
+    from dpgb import params as P
+    from dpgb import synth
+    from dpgb.deeppot import DeepPot
+
+    cfg = P.water_config()
+    cfg.resnet_dt = True
+    p = P.init_params(cfg, seed=3)
+    coord, atype, box = synth.water_box(6, seed=5)
+    ref = DeepPot(p, "fp64").eval(coord.reshape(1, -1), box, atype)
+    got = DeepPot(p, "mixed").eval(coord.reshape(1, -1), box, atype)
+    err = _errors(got, ref, atype.size)
+    print("tc mixed vs fp64, resnet_dt", err)
+    assert err["f_rmse"] <= 1e-3
+    assert err["f_rel"] <= 2e-2
+    assert err["e_rel"] <= 1e-4
