@@ -560,27 +560,43 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
     for (int r0 = ch.row0; r0 < ch.row1; r0 += kFinAtoms) {
       const int nr = min(kFinAtoms, ch.row1 - r0);
       __syncthreads();
-      for (int q = tid; q < nr * 4 * ng; q += blockDim.x) {
-        const int a = q / (4 * ng), qq = q - a * 4 * ng;
+      // (ng == W3: index arithmetic by compile-time divisors only)
+      for (int q = tid; q < nr * 4 * W3; q += blockDim.x) {
+        const int a = q / (4 * W3), qq = q - a * 4 * W3;
         const int r = r0 + a, row = sorted_rows[r];
         float s = 0.f;
         for (int t = 0; t < p.ntypes; ++t)
-          if (run_len[(size_t)r * p.ntypes + t] > 0) s += xyzp[((size_t)t * p.nrows + row) * 4 * ng + qq];
+          if (run_len[(size_t)r * p.ntypes + t] > 0) s += xyzp[((size_t)t * p.nrows + row) * 4 * W3 + qq];
         s *= inv;
         sX[q] = s;
-        xyz[(size_t)row * 4 * ng + qq] = s;
+        xyz[(size_t)row * 4 * W3 + qq] = s;
       }
       __syncthreads();
-      for (int q = tid; q < nr * dim; q += blockDim.x) {
-        const int a = q / dim, rem = q - a * dim, n = rem / p.axis, m = rem - n * p.axis;
-        const float* xr = sX + a * 4 * ng;
-        float s = 0.f;
+      // one thread per (atom, neuron n): D[n][m] for every m < axis
+      const int M = p.axis;
+      for (int q = tid; q < nr * W3; q += blockDim.x) {
+        const int a = q / W3, n = q - a * W3;
+        const float* xr = sX + a * 4 * W3;
+        const float xn[4] = {xr[n], xr[W3 + n], xr[2 * W3 + n], xr[3 * W3 + n]};
+        const size_t o = (size_t)(r0 + a) * dim + (size_t)n * M;
+        auto dnm = [&](int m) {
+          float s = 0.f;
 #pragma unroll
-        for (int cc = 0; cc < 4; ++cc) s = fmaf(xr[cc * ng + n], xr[cc * ng + m], s);
-        if (e.d_bf16)  // the tensor-core fitting reads D as BF16
-          reinterpret_cast<__nv_bfloat16*>(Dout)[(size_t)(r0 + a) * dim + rem] = __float2bfloat16_rn(s);
-        else
-          Dout[(size_t)(r0 + a) * dim + rem] = s;
+          for (int cc = 0; cc < 4; ++cc) s = fmaf(xn[cc], xr[cc * W3 + m], s);
+          return s;
+        };
+        if (e.d_bf16 && M == 16) {  // the tensor-core fitting reads D as BF16: two 16-byte rows
+          __nv_bfloat162 h[8];
+#pragma unroll
+          for (int m = 0; m < 16; m += 2) h[m / 2] = __floats2bfloat162_rn(dnm(m), dnm(m + 1));
+          uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(Dout) + o);
+          dst[0] = *reinterpret_cast<const uint4*>(&h[0]);
+          dst[1] = *reinterpret_cast<const uint4*>(&h[4]);
+        } else if (e.d_bf16) {
+          for (int m = 0; m < M; ++m) reinterpret_cast<__nv_bfloat16*>(Dout)[o + m] = __float2bfloat16_rn(dnm(m));
+        } else {
+          for (int m = 0; m < M; ++m) Dout[o + m] = dnm(m);
+        }
       }
     }
     __syncthreads();
