@@ -128,4 +128,35 @@ struct DeviceBuffer {
   }
 };
 
+// Page-locked host staging (copies to and from it run asynchronously and at
+// full link speed; the caller's own arrays are pageable).
+struct PinnedBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  PinnedBuffer() = default;
+  PinnedBuffer(const PinnedBuffer&) = delete;
+  PinnedBuffer& operator=(const PinnedBuffer&) = delete;
+  ~PinnedBuffer() {
+    if (ptr) cudaFreeHost(ptr);
+  }
+  int alloc(size_t n) {
+    if (n <= bytes) return DPGB_OK;
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    if (n == 0) return DPGB_OK;
+    cudaError_t e = cudaHostAlloc(&ptr, n, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      return fail(DPGB_ENOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    }
+    bytes = n;
+    return DPGB_OK;
+  }
+  template <typename T>
+  T* as() const {
+    return reinterpret_cast<T*>(ptr);
+  }
+};
+
 }  // namespace dpgb

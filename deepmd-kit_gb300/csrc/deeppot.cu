@@ -388,6 +388,8 @@ struct DeepPotImpl {
   DeviceBuffer ws_nlist, ws_cell, ws_tr, ws_keys, ws_status, ws_coord, ws_svec, ws_spos;
   DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf, ws_part, ws_xhi, ws_xlo, ws_shi, ws_slo;
   DeviceBuffer io_coord, io_force, io_av, io_e, io_v, io_ae;
+  DeviceBuffer io_out;   // host API: [energy | virial | force | atom energy | atom virial]
+  PinnedBuffer io_host;  // host API staging: [coord | the outputs | status words]
   // external neighbour list (CSR over local atoms) kept between calls for
   // `ago` > 0, with the ghost-inclusive types
   DeviceBuffer ext_off, ext_idx, ext_atype;
@@ -1301,9 +1303,8 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   return DPGB_OK;
 }
 
-int check_status(DeepPotImpl& dp, cudaStream_t st) {
-  int h[kStatusSlots];
-  DPGB_TRY(read_status(dp.ws_status.as<int>(), st, h));
+// the error (if any) that the status words h of an evaluation report
+int status_result(DeepPotImpl& dp, const int* h) {
   if (h[kStatusOverflow] > 0)
     return fail(DPGB_EOVERFLOW, "neighbour capacity exceeded (" + std::to_string(h[kStatusOverflow]) +
                                     " entries) at atom/row " + std::to_string(h[kStatusOverflowAtom] - 1));
@@ -1315,6 +1316,12 @@ int check_status(DeepPotImpl& dp, cudaStream_t st) {
                                     " slots within rcut + skin); results are invalid");
   }
   return DPGB_OK;
+}
+
+int check_status(DeepPotImpl& dp, cudaStream_t st) {
+  int h[kStatusSlots];
+  DPGB_TRY(read_status(dp.ws_status.as<int>(), st, h));
+  return status_result(dp, h);
 }
 
 int run_any(DeepPotImpl& dp, int nframes, int natom, const double* coord, const double* box_host, double* energy,
@@ -1850,26 +1857,33 @@ int dpgb_deeppot_compute(dpgb_deeppot* dp, int nframes, int natom, const double*
   auto body = [&]() -> int {
     if (nframes <= 0 || natom <= 0 || !coord || !atype || !energy || !force || !virial)
       return fail(DPGB_EINVAL, "bad arguments");
+    // the outputs are one device block and the host side goes through one
+    // pinned block: one copy in, two copies out (outputs, status words), one
+    // synchronisation
     const size_t nrow = (size_t)nframes * natom;
-    DPGB_TRY(im.io_coord.alloc(sizeof(double) * nrow * 3));
-    DPGB_TRY(im.io_force.alloc(sizeof(double) * nrow * 3));
-    DPGB_TRY(im.io_e.alloc(sizeof(double) * nframes));
-    DPGB_TRY(im.io_v.alloc(sizeof(double) * nframes * 9));
-    if (atom_energy) DPGB_TRY(im.io_ae.alloc(sizeof(double) * nrow));
-    if (atom_virial) DPGB_TRY(im.io_av.alloc(sizeof(double) * nrow * 9));
-    DPGB_CUDA(cudaMemcpyAsync(im.io_coord.ptr, coord, sizeof(double) * nrow * 3, cudaMemcpyHostToDevice, st));
-    DPGB_TRY(compute_device_impl(im, nframes, natom, im.io_coord.as<double>(), atype, box, im.io_e.as<double>(),
-                                 im.io_force.as<double>(), im.io_v.as<double>(),
-                                 atom_energy ? im.io_ae.as<double>() : nullptr,
-                                 atom_virial ? im.io_av.as<double>() : nullptr, st));
-    DPGB_CUDA(cudaMemcpyAsync(energy, im.io_e.ptr, sizeof(double) * nframes, cudaMemcpyDeviceToHost, st));
-    DPGB_CUDA(cudaMemcpyAsync(force, im.io_force.ptr, sizeof(double) * nrow * 3, cudaMemcpyDeviceToHost, st));
-    DPGB_CUDA(cudaMemcpyAsync(virial, im.io_v.ptr, sizeof(double) * nframes * 9, cudaMemcpyDeviceToHost, st));
-    if (atom_energy)
-      DPGB_CUDA(cudaMemcpyAsync(atom_energy, im.io_ae.ptr, sizeof(double) * nrow, cudaMemcpyDeviceToHost, st));
-    if (atom_virial)
-      DPGB_CUDA(cudaMemcpyAsync(atom_virial, im.io_av.ptr, sizeof(double) * nrow * 9, cudaMemcpyDeviceToHost, st));
-    return check_status(im, st);  // synchronises
+    const size_t n_e = nframes, n_v = 9 * (size_t)nframes, n_f = 3 * nrow, n_ae = atom_energy ? nrow : 0,
+                 n_av = atom_virial ? 9 * nrow : 0, n_out = n_e + n_v + n_f + n_ae + n_av;
+    DPGB_TRY(im.io_coord.alloc(sizeof(double) * 3 * nrow));
+    DPGB_TRY(im.io_out.alloc(sizeof(double) * n_out));
+    DPGB_TRY(im.io_host.alloc(sizeof(double) * (3 * nrow + n_out) + sizeof(int) * kStatusSlots));
+    double* hc = im.io_host.as<double>();
+    double* ho = hc + 3 * nrow;
+    int* hs = reinterpret_cast<int*>(ho + n_out);
+    std::memcpy(hc, coord, sizeof(double) * 3 * nrow);
+    DPGB_CUDA(cudaMemcpyAsync(im.io_coord.ptr, hc, sizeof(double) * 3 * nrow, cudaMemcpyHostToDevice, st));
+    double* d = im.io_out.as<double>();
+    DPGB_TRY(compute_device_impl(im, nframes, natom, im.io_coord.as<double>(), atype, box, d, d + n_e + n_v, d + n_e,
+                                 atom_energy ? d + n_e + n_v + n_f : nullptr,
+                                 atom_virial ? d + n_e + n_v + n_f + n_ae : nullptr, st));
+    DPGB_CUDA(cudaMemcpyAsync(ho, d, sizeof(double) * n_out, cudaMemcpyDeviceToHost, st));
+    DPGB_CUDA(cudaMemcpyAsync(hs, im.ws_status.ptr, sizeof(int) * kStatusSlots, cudaMemcpyDeviceToHost, st));
+    DPGB_CUDA(cudaStreamSynchronize(st));
+    std::memcpy(energy, ho, sizeof(double) * n_e);
+    std::memcpy(virial, ho + n_e, sizeof(double) * n_v);
+    std::memcpy(force, ho + n_e + n_v, sizeof(double) * n_f);
+    if (atom_energy) std::memcpy(atom_energy, ho + n_e + n_v + n_f, sizeof(double) * n_ae);
+    if (atom_virial) std::memcpy(atom_virial, ho + n_e + n_v + n_f + n_ae, sizeof(double) * n_av);
+    return status_result(im, hs);
   };
   int rc = body();
   if (rc == DPGB_EOVERFLOW && im.skin_grow > 0) rc = body();  // widened skin candidates, rebuilt

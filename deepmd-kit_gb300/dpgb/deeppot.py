@@ -146,11 +146,11 @@ class DeepPot:
         coord = np.ascontiguousarray(coord, dtype=np.float64).reshape(-1, natom * 3)
         nf = coord.shape[0]
         boxa = None if box is None else np.ascontiguousarray(box, dtype=np.float64).reshape(nf, 9)
-        e = np.zeros(nf)
-        f = np.zeros((nf, natom, 3))
-        v = np.zeros((nf, 9))
-        ae = np.zeros((nf, natom)) if atomic else None
-        av = np.zeros((nf, natom, 9)) if atomic else None
+        e = np.empty(nf)  # every output element is written by the call
+        f = np.empty((nf, natom, 3))
+        v = np.empty((nf, 9))
+        ae = np.empty((nf, natom)) if atomic else None
+        av = np.empty((nf, natom, 9)) if atomic else None
         dp = C.POINTER(C.c_double)
 
         def P(a):
