@@ -98,6 +98,26 @@ __device__ __forceinline__ double warp_comp_sum(float hi, float lo) {
   return (double)hi + (double)lo;
 }
 
+// Division of non-negative 31-bit integers by a divisor d >= 1 fixed for a
+// launch, by one widening multiply and a shift (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", PLDI 1994): with
+// 2^l >= d and m = ceil(2^(31+l) / d) < 2^32, floor(n m / 2^(31+l)) = n / d
+// for every 0 <= n < 2^31 (the error m d - 2^(31+l) < d adds less than 1/d).
+struct FastDiv {
+  unsigned m = 1u << 31;
+  int s = 31;
+  FastDiv() = default;
+  explicit FastDiv(int d) {
+    int l = 0;
+    while ((1LL << l) < d) ++l;
+    s = 31 + l;
+    m = (unsigned)(((1ULL << s) + (unsigned long long)d - 1) / (unsigned long long)d);
+  }
+  __host__ __device__ __forceinline__ int div(int n) const {
+    return (int)(((unsigned long long)(unsigned)n * m) >> s);
+  }
+};
+
 // Scoped device allocation used by op-level entry points (workspace).
 struct DeviceBuffer {
   void* ptr = nullptr;

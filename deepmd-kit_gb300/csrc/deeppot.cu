@@ -31,6 +31,7 @@ struct DevModel {
   FitParams<T> fit{};
   T* davg = nullptr;
   T* dstd = nullptr;
+  T* dstd_inv = nullptr;
   TabMeta<T>* meta = nullptr;
   std::vector<DeviceBuffer*> owned;
   ~DevModel() {
@@ -49,14 +50,13 @@ struct DevModel {
 };
 
 // ---- pipeline kernels --------------------------------------------------------
-__global__ void model_keys_kernel(int* __restrict__ keys, const int* __restrict__ nlist, long long npair,
-                                  int nnei, int nloc) {
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void model_keys_kernel(int* __restrict__ keys, const int* __restrict__ nlist, int npair, FastDiv by_nnei,
+                                  int nloc, FastDiv by_nloc) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npair) return;
   const int nb = nlist[p];
-  const long long row = p / nnei;
-  const int f = (int)(row / nloc);
-  keys[p] = nb < 0 ? -1 : f * nloc + nb % nloc;
+  const int f = by_nloc.div(by_nnei.div(p));
+  keys[p] = nb < 0 ? -1 : f * nloc + (nb - by_nloc.div(nb) * nloc);
 }
 
 // F[row] = sum_slots g[row] - sum_{pairs -> row} g;  optional atomic virial on
@@ -729,6 +729,9 @@ int build_dev_model(DeepPotImpl& dp, DevModel<T>& m) {
   std::vector<double> avg(d.davg, d.davg + (size_t)nt * nnei * 4), sd(d.dstd, d.dstd + (size_t)nt * nnei * 4);
   m.davg = m.upload(avg);
   m.dstd = m.upload(sd);
+  std::vector<double> isd(sd.size());
+  for (size_t k = 0; k < sd.size(); ++k) isd[k] = 1.0 / sd[k];
+  m.dstd_inv = m.upload(isd);
   return DPGB_OK;
 }
 
@@ -931,6 +934,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   size_t cell_bytes = 0;
   for (int f = 0; f < (int)geo.size(); ++f) cell_bytes = std::max(cell_bytes, nlist_pt_workspace(natom, geo[f]));
   const long long npair = nrows * nnei;
+  if (npair >= (1LL << 31)) return fail(DPGB_EINVAL, "more than 2^31 neighbour slots in one evaluation");
   // transpose keys: local rows (ghost images fold onto their atom), or every
   // explicit extended atom with an external list (forces on ghosts returned)
   const long long nkeys = ext ? (long long)ext->nall : nrows;
@@ -1101,8 +1105,8 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     if (batch)
       batch_keys_kernel<<<ceil_div(npair, 256), 256, 0, ts>>>(dp.ws_keys.as<int>(), nlist, npair, nnei, batch->ft);
     else
-      model_keys_kernel<<<ceil_div(npair, 256), 256, 0, ts>>>(dp.ws_keys.as<int>(), nlist, npair, nnei,
-                                                               ext ? ext->nall : natom);
+      model_keys_kernel<<<ceil_div(npair, 256), 256, 0, ts>>>(dp.ws_keys.as<int>(), nlist, (int)npair, FastDiv(nnei),
+                                                               ext ? ext->nall : natom, FastDiv(ext ? ext->nall : natom));
     DPGB_TRY(check_launch("model_keys"));
     ++launches;
   }
@@ -1125,6 +1129,8 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   p.rcut_smth = d.rcut_smth;
   p.davg = m.davg;
   p.dstd = m.dstd;
+  p.dstd_inv = m.dstd_inv;
+  p.nloc_div = FastDiv(natom);
   p.pair_mask = d.pair_mask ? dp.pair_mask_dev.as<int>() : nullptr;
   p.coord = coord_n;
   p.atype = dp.atype_dev.as<int>();

@@ -242,10 +242,10 @@ __device__ __forceinline__ void pair_env(const DescParams<float>& p, int t, int 
   pi.k = k;
   pi.row = s_row[k];
   pi.slot = p.sec[t] + (pp - s_off[k]);
-  const int f = pi.row / p.nloc, i = pi.row - f * p.nloc;
+  const int f = p.nloc_div.div(pi.row), i = pi.row - f * p.nloc;
   pi.nb = p.nlist[(size_t)pi.row * p.nnei + pi.slot];
   const float* av = p.davg + ((size_t)ti * p.nnei + pi.slot) * 4;
-  const float* sd = p.dstd + ((size_t)ti * p.nnei + pi.slot) * 4;
+  const float* sdi = p.dstd_inv + ((size_t)ti * p.nnei + pi.slot) * 4;
   float e4[4] = {0.f, 0.f, 0.f, 0.f};
   if (pi.nb >= 0) {
     const int tj = pair_disp_f(p, f, i, pi.nb, dvec);
@@ -272,7 +272,7 @@ __device__ __forceinline__ void pair_env(const DescParams<float>& p, int t, int 
     }
   }
 #pragma unroll
-  for (int c = 0; c < 4; ++c) rn[c] = (pi.nb >= 0 && !pi.keep) ? 0.f : (e4[c] - av[c]) / sd[c];
+  for (int c = 0; c < 4; ++c) rn[c] = (pi.nb >= 0 && !pi.keep) ? 0.f : (e4[c] - av[c]) * sdi[c];
 }
 
 // d R~ / d r_centre of a kept pair (env_mat.cc:156-216), FP32
@@ -861,10 +861,10 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         if (pi.valid && pi.nb >= 0 && pi.keep) {
           float der[12];
           env_deriv(dv, rmin, rmax, der);
-          const float* sd = p.dstd + ((size_t)ti * p.nnei + pi.slot) * 4;
+          const float* sdi = p.dstd_inv + ((size_t)ti * p.nnei + pi.slot) * 4;
 #pragma unroll
           for (int cc = 0; cc < 4; ++cc) {
-            const float w = drn[cc] / sd[cc];
+            const float w = drn[cc] * sdi[cc];
 #pragma unroll
             for (int k = 0; k < 3; ++k) g[k] -= w * der[3 * cc + k];
           }
@@ -899,20 +899,22 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 }
 
 // run lengths of active slots per (sorted row, section)
+// one warp per sorted row: the row's slots are read once, coalesced, and
+// each type section's count of real neighbours is a warp sum
 __global__ void run_len_kernel(int* __restrict__ run_len, const int* __restrict__ nlist,
                                const int* __restrict__ sorted_rows, int nrows, int nnei, SelInfo sel, int pad_zero) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nrows * sel.ntypes) return;
-  const int r = q / sel.ntypes, t = q - r * sel.ntypes;
-  const int row = sorted_rows[r];
-  int n = 0;
-  if (pad_zero) {
-    const int* nl = nlist + (size_t)row * nnei + sel.sec[t];
-    for (int j = 0; j < sel.sel[t]; ++j) n += nl[j] >= 0;
-  } else {
-    n = sel.sel[t];
+  const int r = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (r >= nrows) return;  // the whole warp
+  const int* nl = nlist + (size_t)sorted_rows[r] * nnei;
+  for (int t = 0; t < sel.ntypes; ++t) {
+    int n = sel.sel[t];
+    if (pad_zero) {
+      int c = 0;
+      for (int k = sel.sec[t] + lane; k < sel.sec[t] + sel.sel[t]; k += 32) c += nl[k] >= 0;
+      n = __reduce_add_sync(0xffffffffu, c);
+    }
+    if (lane == 0) run_len[(size_t)r * sel.ntypes + t] = n;
   }
-  run_len[q] = n;
 }
 
 // dE/dxyz (before the forward's 1/nnei): dxyz[n][c] = (sum_m dD[n][m] xyz[c][m]
@@ -1079,8 +1081,7 @@ int launch_bwd_t(const DescParams<float>& p, const EmbTC& e, const WorkChunk* ch
 int launch_run_lengths(int* run_len, const int* nlist, const int* sorted_rows, int nrows, int nnei, const SelInfo& sel,
                        int pad_zero, cudaStream_t st) {
   if (nrows <= 0) return DPGB_OK;
-  run_len_kernel<<<ceil_div((long long)nrows * sel.ntypes, 256), 256, 0, st>>>(run_len, nlist, sorted_rows, nrows,
-                                                                                nnei, sel, pad_zero);
+  run_len_kernel<<<ceil_div(nrows, 8), 256, 0, st>>>(run_len, nlist, sorted_rows, nrows, nnei, sel, pad_zero);
   return check_launch("run_len");
 }
 

@@ -76,6 +76,8 @@ struct DescParams {
   double rcut, rcut_smth;
   const T* davg;  // [ntypes, nnei, 4]
   const T* dstd;
+  const T* dstd_inv;  // 1 / dstd (the mixed-precision kernels multiply)
+  FastDiv nloc_div;   // division by nloc
   const int* pair_mask;     // [ntypes*ntypes] or NULL
   const double* coord;      // [nframes, nloc, 3] normalised
   const int* atype;         // [nloc]
@@ -176,7 +178,7 @@ __device__ __forceinline__ int pair_disp_f(const DescParams<T>& p, int f, int i,
     sv = (size_t)p.frame_svec_off[fr] + s;
     t = p.atype[jj];
   } else {
-    const int s = nb / p.nloc, jj = nb - s * p.nloc;
+    const int s = p.nloc_div.div(nb), jj = nb - s * p.nloc;
     aj = (size_t)f * p.nloc + jj;
     ai = (size_t)f * p.nloc + i;
     sv = (size_t)f * p.nshift + s;

@@ -51,10 +51,10 @@ __device__ __forceinline__ float switch_f(float nr, float rmin, float rmax, floa
 
 // environment of one slot (the same arithmetic as the tensor-core path)
 __device__ __forceinline__ void slot_env(const DescParams<float>& p, int row, int ti, int slot, SlotEnv& s) {
-  const int f = row / p.nloc, i = row - f * p.nloc;
+  const int f = p.nloc_div.div(row), i = row - f * p.nloc;
   s.nb = p.nlist[(size_t)row * p.nnei + slot];
   const float* av = p.davg + ((size_t)ti * p.nnei + slot) * 4;
-  const float* sd = p.dstd + ((size_t)ti * p.nnei + slot) * 4;
+  const float* sdi = p.dstd_inv + ((size_t)ti * p.nnei + slot) * 4;
   float e4[4] = {0.f, 0.f, 0.f, 0.f};
   s.d[0] = s.d[1] = s.d[2] = 0.f;
   int keep = 1;
@@ -81,7 +81,7 @@ __device__ __forceinline__ void slot_env(const DescParams<float>& p, int row, in
     }
   }
 #pragma unroll
-  for (int c = 0; c < 4; ++c) s.rn[c] = (s.nb >= 0 && !keep) ? 0.f : (e4[c] - av[c]) / sd[c];
+  for (int c = 0; c < 4; ++c) s.rn[c] = (s.nb >= 0 && !keep) ? 0.f : (e4[c] - av[c]) * sdi[c];
   s.active = s.nb >= 0 ? keep : !p.pad_zero;
 }
 
@@ -115,14 +115,14 @@ __device__ __forceinline__ void coeffs(const float* __restrict__ rowc, float a[6
   a[5] = x2.y;
 }
 
-__global__ void __launch_bounds__(kTabWarps * 32)
+__global__ void __launch_bounds__(kTabWarps * 32, 4)  // 4 CTAs (32 warps) per SM: the table reads want the warps
 tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ sorted_rows, int nsorted,
                float* __restrict__ xyz, void* __restrict__ Dout, int d_bf16) {
   const int lane = threadIdx.x & 31;
   const int r = blockIdx.x * kTabWarps + (threadIdx.x >> 5);
   if (r >= nsorted) return;
   const int row = sorted_rows[r];
-  const int ti = p.atype[row % p.nloc];
+  const int ti = p.atype[row - p.nloc_div.div(row) * p.nloc];
   const int ng = p.ng, M = p.axis;
   float acc[4][kTabJ];
 #pragma unroll
@@ -205,14 +205,14 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ 
   }
 }
 
-__global__ void __launch_bounds__(kTabWarps * 32)
+__global__ void __launch_bounds__(kTabWarps * 32, 3)  // 3 CTAs (24 warps) per SM
 tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ sorted_rows, int nsorted,
                const float* __restrict__ dxyz, float* __restrict__ gpair, double* __restrict__ vir_row) {
   const int lane = threadIdx.x & 31;
   const int r = blockIdx.x * kTabWarps + (threadIdx.x >> 5);
   if (r >= nsorted) return;
   const int row = sorted_rows[r];
-  const int ti = p.atype[row % p.nloc];
+  const int ti = p.atype[row - p.nloc_div.div(row) * p.nloc];
   const int ng = p.ng;
   const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
   // the atom's dE/dxyz, one float4 (four components) per neuron, shared by
@@ -266,10 +266,10 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ 
         if (real) {
           float der[12];
           slot_deriv(s.d, rmin, rmax, der);
-          const float* sd = p.dstd + ((size_t)ti * p.nnei + slot) * 4;
+          const float* sdi = p.dstd_inv + ((size_t)ti * p.nnei + slot) * 4;
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
-            const float w = mine[c] / sd[c];
+            const float w = mine[c] * sdi[c];
 #pragma unroll
             for (int k = 0; k < 3; ++k) g[k] -= w * der[3 * c + k];
           }
