@@ -45,14 +45,20 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms around and
+    during the timed region.  `busy` runs one untimed evaluation of the same
+    workload: it keeps the GPU under the timed load until the first sample
+    has arrived (before the region) and until one more arrives after it, so
+    a timed region shorter than the sampling interval is still bracketed by
+    samples taken under that load."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, busy=None):
         self.index = index
+        self.busy = busy
         self.proc = None
         self.lines = []
 
@@ -60,12 +66,24 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            self._busy_until(1, 5.0)
         except OSError:
             self.proc = None
         return self
+
+    def _busy_until(self, n, timeout):
+        import torch
+
+        t0 = time.perf_counter()
+        while len(self.lines) < n and time.perf_counter() - t0 < timeout and self.proc.poll() is None:
+            if self.busy is not None:
+                self.busy()
+                torch.cuda.synchronize()
+            else:
+                time.sleep(0.005)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -73,6 +91,7 @@ class ClockSampler:
 
     def __exit__(self, *a):
         if self.proc:
+            self._busy_until(len(self.lines) + 1, 2.0)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -254,7 +273,7 @@ def run_compressed(args, world, rank, local):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     _barrier(world)
-    with ClockSampler(local) as clk:
+    with ClockSampler(local, busy=lambda: mixed.eval_device(x, boxh, atype, out=out)) as clk:
         for k in range(args.steps):
             x.add_(torch.randn(x.shape, dtype=x.dtype, device=dev, generator=gen), alpha=0.01)  # untimed
             starts[k].record(stream)
@@ -335,7 +354,7 @@ def run_batch(args, world, rank, local):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     _barrier(world)
-    with ClockSampler(local) as clk:
+    with ClockSampler(local, busy=lambda: b.eval_device(coord, out=out, use_graph=True)) as clk:
         for k in range(args.steps):
             coord.add_(torch.randn(coord.shape, dtype=coord.dtype, device=dev, generator=gen), alpha=0.005)  # untimed
             starts[k].record(stream)
@@ -475,7 +494,7 @@ def main():
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     _barrier(world)
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    with ClockSampler(local, busy=lambda: mixed.eval_device(coord_dev, boxh, atype, out=out)) as clk:
         for k in range(args.steps):
             flush.fill_(float(k))  # evict L2 between timed steps (untimed)
             starts[k].record(stream)
