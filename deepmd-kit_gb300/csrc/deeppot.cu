@@ -311,17 +311,24 @@ __global__ void __launch_bounds__(kFrameSumThreads) frame_part_kernel(double* __
   }
 }
 
-// pass 2: one warp per frame, lane q < 10 adds the chunk partials in order
+// pass 2: one warp per frame; for each of the 10 sums, lane l adds the
+// partials of chunks l, l + 32, ... and a fixed xor-shuffle tree adds the
+// lanes (the same order on every run)
 __global__ void frame_final_kernel(double* __restrict__ energy, double* __restrict__ virial,
                                    const double* __restrict__ part, int nchunk, int nframes) {
-  const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), q = threadIdx.x & 31;
-  if (f >= nframes || q >= 10) return;
-  double v = 0.0;
-  for (int c = 0; c < nchunk; ++c) v += part[((size_t)f * nchunk + c) * 10 + q];
-  if (q == 0)
-    energy[f] = v;
-  else
-    virial[(size_t)f * 9 + q - 1] = v;
+  const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (f >= nframes) return;  // the whole warp
+  for (int q = 0; q < 10; ++q) {
+    double v = 0.0;
+    for (int c = lane; c < nchunk; c += 32) v += part[((size_t)f * nchunk + c) * 10 + q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+      if (q == 0)
+        energy[f] = v;
+      else
+        virial[(size_t)f * 9 + q - 1] = v;
+    }
+  }
 }
 
 // FP32 split x = hi + lo of n points (FP64 xyz), for FP32 displacements
