@@ -588,6 +588,165 @@ __device__ __forceinline__ bool bit128(const unsigned (&w)[4], int p) {
   return (v >> (p & 31)) & 1u;
 }
 
+// Warp-wide bitonic sort of 32 R (key, index) pairs, element 32 q + lane in
+// register q of each lane, ascending by (key, index).
+template <int R>
+__device__ __forceinline__ void warp_sort_kv(float (&k)[R], int (&e)[R], int lane) {
+#pragma unroll
+  for (int size = 2; size <= 32 * R; size <<= 1) {
+#pragma unroll
+    for (int j = size >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          const int p = q ^ (j >> 5);
+          if (p > q) {
+            const bool up = ((q * 32 + lane) & size) == 0;
+            const bool sw = up ? key_less(k[p], e[p], k[q], e[q]) : key_less(k[q], e[q], k[p], e[p]);
+            if (sw) {
+              const float tk = k[q];
+              const int te = e[q];
+              k[q] = k[p];
+              e[q] = e[p];
+              k[p] = tk;
+              e[p] = te;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          const float ok = __shfl_xor_sync(0xffffffffu, k[q], j);
+          const int oe = __shfl_xor_sync(0xffffffffu, e[q], j);
+          const int idx = q * 32 + lane;
+          const bool up = (idx & size) == 0, lower = (idx & j) == 0;
+          const bool o_less = key_less(ok, oe, k[q], e[q]);
+          if (lower == up ? o_less : !o_less) {
+            k[q] = ok;
+            e[q] = oe;
+          }
+        }
+      }
+    }
+  }
+}
+
+// One type's kept pairs, compacted to the front of (wf, wi) (c <= 32 R of
+// them): warp sort by (FP32 key, index), runs of keys within tie re-ranked
+// by exact FP64 distance as in sort_place_f32, then placed by their rank
+// within the type.
+template <int R>
+__device__ void sort_place_type(int* __restrict__ row, double* __restrict__ wr, int* __restrict__ wi, int c, int t,
+                                float tie, const ExactDist& exact, const SelInfo& sel, int lane,
+                                int* __restrict__ status) {
+  const float* wf = reinterpret_cast<const float*>(wr);
+  float k[R];
+  int e[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int idx = q * 32 + lane;
+    k[q] = idx < c ? wf[idx] : __int_as_float(0x7f800000);
+    e[q] = idx < c ? wi[idx] : 0x7fffffff;
+  }
+  warp_sort_kv<R>(k, e, lane);
+  unsigned near[4] = {0u, 0u, 0u, 0u};  // bit p: sorted positions p and p + 1 are within tie
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    float next = __shfl_down_sync(0xffffffffu, k[q], 1);
+    const float first_next = __shfl_sync(0xffffffffu, k[q < R - 1 ? q + 1 : q], 0);
+    if (lane == 31) next = first_next;
+    const int idx = q * 32 + lane;
+    near[q] = __ballot_sync(0xffffffffu, idx + 1 < c && next - k[q] <= tie);
+  }
+  if (near[0] | near[1] | near[2] | near[3]) {
+    __syncwarp();  // every lane has read its FP32 key before wr is overwritten
+    bool member[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int p = q * 32 + lane;
+      member[q] = bit128(near, p) || (p > 0 && bit128(near, p - 1));
+      wi[p] = e[q];
+      if (member[q]) wr[p] = exact(e[q]);
+    }
+    __syncwarp();
+    int np[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int p = q * 32 + lane;
+      np[q] = p;
+      if (member[q]) {
+        int lo = p, hi = p;
+        while (lo > 0 && bit128(near, lo - 1)) --lo;
+        while (bit128(near, hi)) ++hi;  // a near bit needs p + 1 < c <= 32 R
+        const double r = wr[p];
+        int cnt = 0;
+        for (int m = lo; m <= hi; ++m) {
+          const double rm = wr[m];
+          cnt += rm < r || (rm == r && wi[m] < e[q]);
+        }
+        np[q] = lo + cnt;
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+      if (member[q]) wi[np[q]] = e[q];
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < R; ++q) e[q] = wi[q * 32 + lane];
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int idx = q * 32 + lane;
+    if (idx < c) place_pair(row, 0, idx, t, e[q], sel, status);
+  }
+}
+
+// The kept pairs (k, e, t: element 32 q + lane in register q), sorted and
+// placed one type at a time when that gives the same list as the global
+// ranking: no more pairs than sum(sel) (so the global cut keeps all) and at
+// most 64 of each type.  Sorting each type's few dozen pairs costs less than
+// one 128-wide sort.  Returns false (nothing written) otherwise.
+__device__ bool sort_place_by_type(int* __restrict__ row, double* __restrict__ wr, int* __restrict__ wi,
+                                   const float (&k)[4], const int (&e)[4], const int (&tt)[4], int n, float tie,
+                                   const ExactDist& exact, const SelInfo& sel, int lane,
+                                   int* __restrict__ status) {
+  if (n > sel.nnei) return false;
+  int total = 0;
+  bool fits = true;
+  for (int t = 0; t < sel.ntypes; ++t) {
+    int c = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) c += __popc(__ballot_sync(0xffffffffu, tt[q] == t && q * 32 + lane < n));
+    total += c;
+    fits = fits && c <= 64;
+  }
+  if (!fits || total != n) return false;
+  float* wf = reinterpret_cast<float*>(wr);
+  const unsigned below = (1u << lane) - 1u;
+  for (int t = 0; t < sel.ntypes; ++t) {
+    __syncwarp();  // the previous type's reads of (wf, wi) are done
+    int base = 0;  // ends as the type's count
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const bool mine = tt[q] == t && q * 32 + lane < n;
+      const unsigned m = __ballot_sync(0xffffffffu, mine);
+      if (mine) {
+        wf[base + __popc(m & below)] = k[q];
+        wi[base + __popc(m & below)] = e[q];
+      }
+      base += __popc(m);
+    }
+    __syncwarp();
+    if (base == 0) continue;
+    if (base <= 32)
+      sort_place_type<1>(row, wr, wi, base, t, tie, exact, sel, lane, status);
+    else
+      sort_place_type<2>(row, wr, wi, base, t, tie, exact, sel, lane, status);
+  }
+  return true;
+}
+
 // Placement of up to 128 kept pairs with FP32 keys (the first floats of wr,
 // within eps of the exact distances) through a warp sort: the sorted
 // position is the global rank, same-type lanes of each 32-chunk
@@ -610,6 +769,7 @@ __device__ void sort_place_f32(int* __restrict__ row, double* __restrict__ wr, i
     e[q] = idx < n ? wi[idx] : 0x7fffffff;
     t[q] = idx < n ? wt[idx] : -1;
   }
+  if (sort_place_by_type(row, wr, wi, k, e, t, n, tie, exact, sel, lane, status)) return;
   warp_sort128(k, e, t, lane);
   unsigned near[4];  // bit p: sorted positions p and p + 1 are within tie
 #pragma unroll
