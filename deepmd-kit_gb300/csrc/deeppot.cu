@@ -311,23 +311,28 @@ __global__ void __launch_bounds__(kFrameSumThreads) frame_part_kernel(double* __
   }
 }
 
-// pass 2: one warp per frame; for each of the 10 sums, lane l adds the
-// partials of chunks l, l + 32, ... and a fixed xor-shuffle tree adds the
+// pass 2: one warp per frame; lane l adds the partials (all 10 sums at
+// once) of chunks l, l + 32, ..., then a fixed xor-shuffle tree adds the
 // lanes (the same order on every run)
 __global__ void frame_final_kernel(double* __restrict__ energy, double* __restrict__ virial,
                                    const double* __restrict__ part, int nchunk, int nframes) {
   const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (f >= nframes) return;  // the whole warp
-  for (int q = 0; q < 10; ++q) {
-    double v = 0.0;
-    for (int c = lane; c < nchunk; c += 32) v += part[((size_t)f * nchunk + c) * 10 + q];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) {
-      if (q == 0)
-        energy[f] = v;
-      else
-        virial[(size_t)f * 9 + q - 1] = v;
-    }
+  double v[10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q) v[q] = 0.0;
+  for (int c = lane; c < nchunk; c += 32) {
+    const double* pc = part + ((size_t)f * nchunk + c) * 10;
+#pragma unroll
+    for (int q = 0; q < 10; ++q) v[q] += pc[q];
+  }
+#pragma unroll
+  for (int q = 0; q < 10; ++q)
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+  if (lane == 0) {
+    energy[f] = v[0];
+#pragma unroll
+    for (int q = 1; q < 10; ++q) virial[(size_t)f * 9 + q - 1] = v[q];
   }
 }
 
