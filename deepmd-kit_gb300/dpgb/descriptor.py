@@ -22,7 +22,6 @@ CUDA tensors only: there is no CPU path.
 from __future__ import annotations
 
 import ctypes as C
-import itertools
 
 import numpy as np
 import torch
@@ -229,7 +228,9 @@ class _BlockBwdFn(torch.autograd.Function):
 
 class MLPLayer(torch.nn.Module):
     """One embedding layer: y = tanh(x W + b) [* idt] (+ x, + [x, x]) — the
-    parameter names of deepmd/pt/model/network/mlp.py:81-219."""
+    parameter names of deepmd/pt/model/network/mlp.py:81-219.  As there, the
+    timestep idt exists only where a skip connection does (nout == nin or
+    2 nin, mlp.py:89-92): never on the first layer (1 -> neuron[0])."""
 
     def __init__(self, nin, nout, resnet_dt, dtype, device, gen):
         super().__init__()
@@ -238,7 +239,7 @@ class MLPLayer(torch.nn.Module):
             torch.tensor(gen.normal(0.0, std, size=(nin, nout)), dtype=dtype, device=device))
         self.bias = torch.nn.Parameter(torch.tensor(gen.normal(0.0, 1.0, size=(nout,)), dtype=dtype, device=device))
         self.idt = (torch.nn.Parameter(torch.tensor(gen.normal(0.1, 0.001, size=(nout,)), dtype=dtype, device=device))
-                    if resnet_dt else None)
+                    if resnet_dt and (nout == nin or nout == 2 * nin) else None)
 
 
 class EmbeddingNet(torch.nn.Module):
@@ -394,13 +395,16 @@ class DescrptBlockSeA(torch.nn.Module):
         return b
 
     def flat_params(self):
-        """All embedding parameters as one vector in the kernels' layout."""
+        """All embedding parameters as one vector in the kernels' layout
+        (with resnet_dt every layer has an idt slot; a layer without a
+        timestep gets ones there, an exact no-op)."""
         parts = []
         for net in self.filter_layers.networks:
             for layer in net.layers:
                 parts += [layer.matrix.reshape(-1), layer.bias.reshape(-1)]
                 if self.resnet_dt:
-                    parts.append(layer.idt.reshape(-1))
+                    parts.append(layer.idt.reshape(-1) if layer.idt is not None
+                                 else torch.ones_like(layer.bias).reshape(-1))
         return torch.cat(parts)
 
     def enable_compression(self, table_data, table_config, lower, upper):
@@ -582,18 +586,17 @@ class DescrptSeA(torch.nn.Module):
         nets = []
         for net in obj.filter_layers.networks:
             layers = []
-            for layer in net.layers:
-                var = {"w": layer.matrix.detach().cpu().numpy(), "b": layer.bias.detach().cpu().numpy()}
-                if obj.resnet_dt:
-                    var["idt"] = layer.idt.detach().cpu().numpy()
-                layers.append({"@class": "Layer", "@version": 1, "bias": True, "use_timestep": obj.resnet_dt,
+            for layer in net.layers:  # NativeLayer.serialize (dpmodel/utils/network.py:153-177)
+                var = {"w": layer.matrix.detach().cpu().numpy(), "b": layer.bias.detach().cpu().numpy(),
+                       "idt": None if layer.idt is None else layer.idt.detach().cpu().numpy()}
+                layers.append({"@class": "Layer", "@version": 2, "bias": True, "use_timestep": layer.idt is not None,
                                "activation_function": obj.activation_function, "resnet": True,
-                               "precision": obj.precision, "@variables": var})
-            nets.append({"@class": "EmbeddingNetwork", "@version": 2, "in_dim": 1, "neuron": obj.neuron,
+                               "precision": obj.precision, "trainable": True, "@variables": var})
+            # EmbeddingNet.serialize (network.py:782-801)
+            nets.append({"@class": "EmbeddingNetwork", "@version": 2, "in_dim": 1, "neuron": list(obj.neuron),
                          "activation_function": obj.activation_function, "resnet_dt": obj.resnet_dt,
-                         "precision": obj.precision, "bias": True, "layers": layers})
+                         "bias": True, "precision": obj.precision, "layers": layers})
         ndim = 1 if obj.type_one_side else 2
-        idx = list(itertools.product(range(obj.ntypes), repeat=ndim))
         return {
             "@class": "Descriptor", "type": "se_e2_a", "@version": 2, "rcut": obj.rcut, "rcut_smth": obj.rcut_smth,
             "sel": obj.sel, "neuron": obj.neuron, "axis_neuron": obj.axis_neuron, "resnet_dt": obj.resnet_dt,
@@ -601,7 +604,7 @@ class DescrptSeA(torch.nn.Module):
             "precision": obj.precision,
             "embeddings": {"@class": "NetworkCollection", "@version": 1, "ndim": ndim, "ntypes": obj.ntypes,
                            "network_type": "embedding_network",
-                           "networks": {str(i): n for i, n in zip(range(len(idx)), nets)}},
+                           "networks": nets},  # NetworkCollection.serialize (network.py:1247-1266)
             "env_mat": {"@class": "EnvMat", "@version": 1, "rcut": obj.rcut, "rcut_smth": obj.rcut_smth,
                         "protection": obj.env_protection},
             "exclude_types": obj.exclude_types, "env_protection": obj.env_protection,
@@ -632,6 +635,6 @@ class DescrptSeA(torch.nn.Module):
                     v = ld["@variables"]
                     layer.matrix.copy_(torch.as_tensor(np.asarray(v["w"]), dtype=sea.prec))
                     layer.bias.copy_(torch.as_tensor(np.asarray(v["b"]), dtype=sea.prec))
-                    if sea.resnet_dt and v.get("idt") is not None:
+                    if layer.idt is not None and v.get("idt") is not None:
                         layer.idt.copy_(torch.as_tensor(np.asarray(v["idt"]), dtype=sea.prec))
         return obj
