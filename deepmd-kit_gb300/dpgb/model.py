@@ -14,8 +14,9 @@ library GEMMs).  Forces are -dE/dr through autograd on the extended
 coordinates and reduced to the local atoms through the ghost mapping;
 ``create_graph=True`` keeps them differentiable for force-loss training.
 State-dict keys are the reference's (``atomic_model.descriptor.*``,
-``atomic_model.fitting_net.*``, ``atomic_model.out_bias``), so a reference
-checkpoint's state dict loads unchanged.
+``atomic_model.fitting_net.*``, ``atomic_model.out_bias``,
+``atomic_model.out_std``), so a reference checkpoint's state dict loads
+unchanged.
 """
 from __future__ import annotations
 
@@ -102,6 +103,9 @@ class _AtomicModel(torch.nn.Module):
         self.descriptor = descriptor
         self.fitting_net = fitting_net
         self.register_buffer("out_bias", torch.zeros((1, ntypes, 1), dtype=prec, device=device))
+        # kept for the state dict (base_atomic_model.py:134-145); the energy
+        # output adds out_bias only
+        self.register_buffer("out_std", torch.ones((1, ntypes, 1), dtype=prec, device=device))
 
 
 class EnergyModelSeA(torch.nn.Module):
