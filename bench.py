@@ -1,18 +1,27 @@
 """Benchmark: atom-steps/s of se_e2_a energy + force + virial on one GB300.
 
-Workload: 4096 water molecules (12,288 atoms, periodic cubic box 49.6 A),
-seeded synthetic coordinates (O lattice 3.1 A jittered U(+-0.3 A), H at
-0.9572 A / 104.52 deg, random rotations) and the seeded random-init water
-model (rcut 6, rcut_smth 0.5, sel [46, 92], embedding [25, 50, 100],
-axis 16, fitting [240, 240, 240]).  One step = one full evaluation from
-coordinates: wrap, cell-list neighbour list, descriptor, fitting, forces,
-virial.  `value` is the mixed-precision form with coordinates resident in
-HBM; `e2e` is the same step through the DP_DeepPotCompute-style C API with
-host buffers (host->device coordinates, device->host energy/forces/virial
-inside the timed region).  The plain FP64 form is measured on the same
-workload and reported in `config` together with the mixed-vs-FP64 errors.
+Default workload (water98k-compressed): 32,768 water molecules (98,304
+atoms, periodic cubic box 99.2 A), seeded synthetic coordinates (O lattice
+3.1 A jittered U(+-0.3 A), H at 0.9572 A / 104.52 deg, random rotations),
+the seeded random-init water model (rcut 6, rcut_smth 0.5, sel [46, 92],
+embedding [25, 50, 100], axis 16, fitting [240, 240, 240]) with its
+embedding nets compressed into fifth-order tables (stride 0.01 / 0.1,
+extrapolate x5) and its energy scaled so that forces are ~1 eV/A RMS, as in
+trained water models (dpgb.params.scale_energy).  A random walk of
+N(0, 0.01 A) displacements between consecutive evaluations; neighbour lists
+with a 2 A skin, candidates rebuilt every 10 evaluations.  One step = one
+full evaluation from coordinates: neighbour list (selection at rcut, and
+the candidate build when due), descriptor, fitting, forces, virial.
+
+`value` is the mixed-precision form with coordinates resident in HBM; `e2e`
+is the same step through the DP_DeepPotCompute-style C API with host
+buffers (host->device coordinates, device->host energy/forces/virial inside
+the timed region).  The plain FP64 form is measured on the same workload and
+reported in `config` together with the mixed-vs-FP64 errors.  Workload
+water12k: the uncompressed model on 4096 molecules (12,288 atoms).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl dpgb|reference]
+                    [--workload water98k-compressed|water12k|alloy512-batch]
 """
 from __future__ import annotations
 
@@ -164,90 +173,187 @@ def algorithmic_flops(n_atoms: int, n_pairs: int, cfg) -> dict:
     }
 
 
-def run_reference(args, world, rank):
-    """The reference's CPU path as restated by the oracle (the reference's own
-    compiled library is x86-only here and its Python model is not on the GPU
-    box), timed on the host cores on a bounded sample of the workload: the
-    full neighbourhoods of the first `sample` centre atoms of the 12,288-atom
-    box per step."""
-    if rank != 0:
-        return
+def table_bytes_flops(n_atoms: int, n_pairs: int, cfg) -> dict:
+    """Algorithmic DRAM bytes and CUDA-core FLOPs of the compressed
+    descriptor's fused table kernels per launch.  Bytes: what a launch must
+    move at least — forward: the list (4 B per slot) and coordinates in, xyz
+    (FP32 [4][ng]) and D (BF16 [ng][axis]) out; backward: the list and
+    dE/dxyz (FP32 [ng][4]) in, the pair gradients (3 FP32 per slot) and the
+    per-atom virial (9 FP64) out.  FLOPs per real pair and neuron: forward
+    the quintic (5 FMA) and the contraction (4 FMA); backward the quintic
+    with its derivative (9 FMA), dG = R~ . dX (4), dR~ (4), ds (1)."""
+    S, ng, M = cfg.nnei, cfg.ng, cfg.axis_neuron
+    return {
+        "desc_fwd": {"bytes": n_atoms * (4 * S + 24 + 16 * ng + 2 * ng * M), "flops": n_pairs * ng * 9 * 2},
+        "desc_bwd": {"bytes": n_atoms * (4 * S + 24 + 16 * ng + 12 * S + 72), "flops": n_pairs * ng * 18 * 2},
+    }
+
+
+# FP32 CUDA-core peak (no tensor cores): 152 SMs x 128 lanes x 2 FLOP x 2.07 GHz
+FP32_SIMT_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12
+
+# DRAM bytes (read + write) per launch of the dominant kernels, from one ncu
+# capture each (profiles/); None where not captured for the current build
+DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": None, "desc_bwd": None, "fitting": None}
+
+
+def table_roofline(per_step: dict, n_atoms: int, n_pairs: int, cfg) -> dict:
+    """Roofline of the compressed step's dominant stage: the fitting against
+    the measured BF16 tensor peak (its algorithmic FLOPs), the fused table
+    stages against the measured HBM bandwidth (their algorithmic bytes),
+    with their CUDA-core FP32 FLOPs against the nominal FP32 peak beside."""
+    peaks, kind = _peaks()
+    dom = max((k for k in ("desc_fwd", "fitting", "desc_bwd") if k in per_step), key=lambda k: per_step[k])
+    sec = per_step[dom] * 1e-3
+    if dom == "fitting":
+        fl = algorithmic_flops(n_atoms, n_pairs, cfg)["fitting"]
+        ach = fl / sec / 1e12
+        peak = peaks.get("bf16_tflops", 1900.0)
+        return {"bound": "tensor", "kernel": "fitting (fit_gemm x5 + fit_dxyz)", "achieved": ach, "peak": peak,
+                "unit": "TFLOP/s", "frac": ach / peak, "traffic": DRAM_BYTES_PER_LAUNCH_98K.get(dom),
+                "peak_source": f"{kind} bf16_tflops", "algorithmic_flops_per_launch": fl}
+    w = table_bytes_flops(n_atoms, n_pairs, cfg)[dom]
+    ach = w["bytes"] / sec / 1e9
+    peak = peaks.get("hbm_gbs", 6800.0)
+    simt = w["flops"] / sec / 1e12
+    return {"bound": "hbm", "kernel": {"desc_fwd": "tab_fwd", "desc_bwd": "tab_bwd"}[dom], "achieved": ach,
+            "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": DRAM_BYTES_PER_LAUNCH_98K.get(dom),
+            "peak_source": f"{kind} hbm_gbs", "algorithmic_bytes_per_launch": w["bytes"],
+            "simt_fp32": {"achieved_tflops": simt, "peak_tflops_nominal": FP32_SIMT_TFLOPS_NOMINAL,
+                          "frac": simt / FP32_SIMT_TFLOPS_NOMINAL, "flops_per_launch": w["flops"]}}
+
+
+def water_model(compressed: bool):
+    """The benchmark's water model (SeAParams, FP64): seeded random init, the
+    energy scaled to ~1 eV/A RMS forces; with compressed=True its embedding
+    nets replaced by tables built on the CPU by the oracle's restatement of
+    DPTabulate (outside any timed region; the GPU arm builds the same tables
+    on the device)."""
+    from dpgb import params as P
+
+    p = P.scale_energy(P.init_params(P.water_config(), seed=1), P.WATER_FORCE_SCALE)
+    if not compressed:
+        return p
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import copy
+
+    import oracle as O
+
+    c = p.config
+    lower, upper = O.table_env_range(p.mean, p.stddev, MIN_NBOR, c.rcut_smth, c.rcut)
+    out = copy.copy(p)
+    out.tables, out.table_info = [], []
+    for e, layers in enumerate(p.emb):
+        ti = e % c.ntypes
+        lo, up = float(lower[ti]), float(upper[ti])
+        out.tables.append(O.table_build([(w, b) for w, b, _ in layers], lo, up, 5.0, 0.01, 0.1))
+        out.table_info.append(np.array([lo, up, up * 5.0, 0.01, 0.1, -1.0]))
+    return out
+
+
+# nearest-neighbour distance of the generated water (the O-H bond), the
+# input of the tabulation range
+MIN_NBOR = 0.9
+CPU_NMOL_SIDE = 8  # the CPU arms' box: 8^3 molecules (1,536 atoms)
+
+
+def cpu_full_steps(compressed: bool, steps: int, warmup: int):
+    """The reference's CPU path (as restated by the oracle, FP64, OpenMP over
+    the host cores) timed on complete steps of a smaller box of the same
+    water (8^3 molecules, 1,536 atoms, box 24.8 A; the per-atom work of the
+    method does not depend on the box size): per step the wrap, the ghost
+    images, the neighbour list and the energy / forces / virial, each step on
+    coordinates moved by the same N(0, 0.01 A) walk.  Returns (atom-steps/s,
+    seconds per step, cores, sample text)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
-    from dpgb import params as P, synth
+    from dpgb import synth
 
+    params = water_model(compressed)
+    c = params.config
+    coord, atype, box = synth.water_box(CPU_NMOL_SIDE, seed=0)
+    rng = np.random.default_rng(7)
+    walk = [coord]
+    for _ in range(warmup + steps):
+        walk.append(walk[-1] + rng.normal(0.0, 0.01, size=coord.shape))
+    om = O.OracleModel(params)
+
+    def step(x):
+        cn = O.normalize_coord(x, box)
+        ext, ext_t, _ = O.extend_coord_with_ghosts(cn, atype, box, c.rcut)
+        nl = O.build_nlist_pt(ext, ext_t, x.shape[0], c.rcut, c.sel)
+        return om.energy_force_ext(ext, ext_t, nl, x.shape[0])
+
+    for k in range(warmup):
+        step(walk[1 + k])
+    t0 = time.perf_counter()
+    for k in range(steps):
+        step(walk[1 + warmup + k])
+    dt = time.perf_counter() - t0
+    n = coord.shape[0]
+    form = "compressed (FP64 tables)" if compressed else "plain"
+    sample = (f"{steps} complete steps (wrap, ghosts, neighbour list, E/F/V) of the {n}-atom box of the same "
+              f"water, se_e2_a {form} FP64, oracle restatement of the reference CPU path")
+    return n * steps / dt, dt / steps, O.lib().orc_num_threads(), sample
+
+
+def run_reference(args, world, rank):
+    """The reference arm: the reference's CPU path for this workload (the
+    oracle's restatement: the reference's own compiled library is built for
+    the x86 build container and its Python model needs pip modules absent on
+    the GPU host), on every host core, rank 0 only."""
+    if rank != 0:
+        return
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    params = P.init_params(P.water_config(), seed=1)
-    coord, atype, box = synth.water_box(NMOL_SIDE, seed=0)
-    om = O.OracleModel(params)
-    cn = O.normalize_coord(coord, box)
-    ext, ext_t, _ = O.extend_coord_with_ghosts(cn, atype, box, params.config.rcut)
-    nloc = coord.shape[0]
-    nl = O.build_nlist_pt(ext, ext_t, nloc, params.config.rcut, params.config.sel)
-    sample = args.ref_sample
-    for _ in range(args.warmup):
-        om.energy_force_ext(ext, ext_t, nl[:sample], sample)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        om.energy_force_ext(ext, ext_t, nl[:sample], sample)
-    dt = time.perf_counter() - t0
-    value = sample * args.steps / dt
+    compressed = args.workload == "water98k-compressed"
+    if args.workload == "alloy512-batch":
+        print(json.dumps({"impl": "reference", "unavailable": "no CPU arm for the alloy batch workload"}))
+        return
+    value, sec, ncores, sample = cpu_full_steps(compressed, args.steps, args.warmup)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sec, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": "water 4096 H2O (12,288 atoms), se_e2_a plain FP64, CPU", "natoms": nloc,
-                   "sample_atoms_per_step": sample},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.lib().orc_num_threads(), "kind": "port",
-                         "sample": f"{sample} centre atoms (full neighbourhoods) of the 12,288-atom box per step"},
+        "config": {"workload": WORKLOAD_NAME[args.workload] + "; reference CPU path, FP64",
+                   "cpu_box_atoms": 3 * CPU_NMOL_SIDE ** 3},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
 
-def cpu_baseline_port(sample: int, steps: int = 2):
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle as O
-    from dpgb import params as P, synth
+def cpu_baseline(compressed: bool, steps: int = 3):
+    value, _, ncores, sample = cpu_full_steps(compressed, steps, 1)
+    return {"value": value, "unit": UNIT, "cores": ncores, "kind": "port", "sample": sample}
 
-    params = P.init_params(P.water_config(), seed=1)
-    coord, atype, box = synth.water_box(NMOL_SIDE, seed=0)
-    om = O.OracleModel(params)
-    cn = O.normalize_coord(coord, box)
-    ext, ext_t, _ = O.extend_coord_with_ghosts(cn, atype, box, params.config.rcut)
-    nl = O.build_nlist_pt(ext, ext_t, coord.shape[0], params.config.rcut, params.config.sel)
-    om.energy_force_ext(ext, ext_t, nl[:sample], sample)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        om.energy_force_ext(ext, ext_t, nl[:sample], sample)
-    dt = time.perf_counter() - t0
-    return {"value": sample * steps / dt, "unit": UNIT, "cores": O.lib().orc_num_threads(), "kind": "port",
-            "sample": f"{steps} x {sample} centre atoms (full neighbourhoods) of the 12,288-atom box, FP64 oracle"}
+
+WORKLOAD_NAME = {
+    "water98k-compressed": "compressed water 32768 H2O (98,304 atoms), box 99.2 A, se_e2_a rc 6 sel [46,92] "
+                           "tables stride 0.01/0.1 x5, axis 16 fit [240,240,240]",
+    "water12k": "water 4096 H2O (12,288 atoms), box 49.6 A, se_e2_a rc 6 sel [46,92] emb [25,50,100] "
+                "axis 16 fit [240,240,240]",
+    "alloy512-batch": "512 fcc alloy frames, se_e2_a rc 6 rs 2 sel [60]*4",
+}
 
 
 def run_compressed(args, world, rank, local):
-    """The compressed water box: 32,768 H2O (98,304 atoms, box 99.2 A), the
-    embedding nets replaced by GPU-built tables (stride 0.01 to the upper
-    bound, 0.1 beyond, extrapolate x5, from the same seeded weights), a
-    random walk of N(0, 0.01 A) displacements applied between consecutive
-    force evaluations.  Mixed form (FP32 table evaluation fused with the
-    contraction, FP64 reductions) timed step by step; the FP64 table form on
-    the same coordinates for the speed-up and the errors."""
+    """The compressed water box (the default workload; module docstring).
+    Mixed form (FP32 table evaluation fused with the contraction, split-BF16
+    tensor-core fitting, FP64 reductions) timed step by step with the walk
+    applied between steps (untimed); the FP64 table form on the same
+    coordinates for the speed-up and the errors."""
     import torch
 
     from dpgb import params as P, synth, tabulate
     from dpgb.deeppot import DeepPot
 
     dev = torch.device("cuda", local)
-    params = P.init_params(P.water_config(), seed=1)
+    params = P.scale_energy(P.init_params(P.water_config(), seed=1), P.WATER_FORCE_SCALE)
     coord, atype, box = synth.water_box(32, seed=rank)
     nloc = coord.shape[0]
-    # nearest-neighbour distance of the generated box (the O-H bond), the
-    # input of the tabulation range
-    min_nbor = 0.9
-    cparams = tabulate.compress_params(params, min_nbor, 5, 0.01, 0.1, device=dev)
+    cparams = tabulate.compress_params(params, MIN_NBOR, 5, 0.01, 0.1, device=dev)
     boxh = box.reshape(1, 9)
     x = torch.tensor(coord.reshape(1, -1), dtype=torch.float64, device=dev)
     gen = torch.Generator(device=dev).manual_seed(1234 + rank)
@@ -256,6 +362,9 @@ def run_compressed(args, world, rank, local):
     mixed.set_skin(skin, args.rebuild_every)
     out = mixed.eval_device(x, boxh, atype)
     stream = torch.cuda.current_stream()
+    # real pairs of the workload (outside the timed region)
+    nl0 = mixed.last_nlist()[0]
+    n_pairs = int((nl0 >= 0).sum())
     # per-stage times from profiled evaluations (untimed, without the graph),
     # over one rebuild period so that the list builds are in the average
     mixed.set_profiling(True)
@@ -285,6 +394,26 @@ def run_compressed(args, world, rank, local):
     t_ms = _allreduce_max(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), world)
     launches = mixed.last_launches()
     value = world * nloc * args.steps / (t_ms * 1e-3)
+
+    # end to end through the C API with host buffers: the walk continued on
+    # host coordinates made beforehand; per step the host->device copy of the
+    # coordinates and the device->host energy / forces / virial are timed
+    xh = x.cpu().numpy().reshape(-1, 3)
+    rng = np.random.default_rng(99 + rank)
+    walk = []
+    for _ in range(args.steps + 2):
+        xh = xh + rng.normal(0.0, 0.01, size=xh.shape)
+        walk.append(np.ascontiguousarray(xh.reshape(1, -1)))
+    for w in walk[:2]:
+        mixed.eval(w, boxh, atype)
+    _barrier(world)
+    t0 = time.perf_counter()
+    for w in walk[2:]:
+        e_h, f_h, v_h = mixed.eval(w, boxh, atype)
+    e2e_s = _allreduce_max(time.perf_counter() - t0, world)
+    e2e = {"value": world * nloc * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(walk[0].nbytes), "d2h_bytes_per_step": int(8 + f_h.nbytes + v_h.nbytes)}
+
     fp64 = DeepPot(cparams, "fp64", device=local)
     fp64.set_skin(skin, args.rebuild_every)
     o64 = fp64.eval_device(x, boxh, atype)
@@ -296,32 +425,41 @@ def run_compressed(args, world, rank, local):
     e64.record(stream)
     torch.cuda.synchronize()
     fp64_ms = s64.elapsed_time(e64) / args.fp64_steps
+    mixed.set_graph(False)
     mixed.eval_device(x, boxh, atype, out=out)
     torch.cuda.synchronize()
     f_m, f_d = out["force"].double().cpu().numpy(), o64["force"].cpu().numpy()
+    v_m, v_d = out["virial"].cpu().numpy(), o64["virial"].cpu().numpy()
     if rank != 0:
         return
+    per_step = {k: v / max(ncalls, 1) for k, v in stages.items()}
+    cpu = None if args.no_cpu_baseline else cpu_baseline(True)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {
-            "workload": "compressed water 32768 H2O (98,304 atoms), box 99.2 A, tables stride 0.01/0.1 x5, "
+            "workload": WORKLOAD_NAME["water98k-compressed"] + "; energy scaled to ~1 eV/A RMS forces; "
                         "N(0, 0.01 A) random walk between evaluations; mixed form; "
                         + (f"candidates within rc + {skin:g} A rebuilt every {args.rebuild_every} evaluations "
                            "(or on a skin/2 move), the list at rc selected every evaluation" if skin > 0 else
                            "neighbour list rebuilt every evaluation")
                         + ("" if args.no_graph else "; replayed from a CUDA graph"),
             "skin_A": skin, "rebuild_every": args.rebuild_every,
-            "natoms": nloc, "l2": "inputs larger than L2",
+            "natoms": nloc, "real_pairs": n_pairs, "l2": "inputs larger than L2 (the step streams ~1 GB)",
             "fp64_atom_steps_per_s": nloc / (fp64_ms * 1e-3), "fp64_ms_per_step": fp64_ms,
             "mixed_over_fp64": value / world / (nloc / (fp64_ms * 1e-3)),
             "force_rmse_vs_fp64_eV_per_A": float(np.sqrt(np.mean((f_m - f_d) ** 2))),
             "force_rms_fp64": float(np.sqrt(np.mean(f_d ** 2))),
             "energy_err_per_atom_vs_fp64": float(abs(out["energy"].item() - o64["energy"].item()) / nloc),
-            "stage_ms_per_step": {k: v / max(ncalls, 1) for k, v in stages.items()},
+            "virial_rel_err_vs_fp64": float(np.abs(v_m - v_d).max() / np.abs(v_d).max()),
+            "stage_ms_per_step": per_step,
+            "stage_times_from": "profiled evaluations without the graph, over one rebuild period",
             "parallelism": f"replicas x{world}",
         },
+        "roofline": table_roofline(per_step, nloc, n_pairs, params.config),
+        "cpu_baseline": cpu,
+        "e2e": e2e,
         "gpu_launches": launches * args.steps,
         "clocks": clk.summary(),
     }
@@ -419,13 +557,13 @@ DRAM_BYTES_PER_LAUNCH = {"desc_fwd": 50.0e6, "desc_bwd": 27.2e6, "fitting": 41.9
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="water12k", choices=["water12k", "water98k-compressed", "alloy512-batch"])
+    ap.add_argument("--workload", default="water98k-compressed",
+                    choices=["water98k-compressed", "water12k", "alloy512-batch"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="dpgb", choices=["dpgb", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=3)
-    ap.add_argument("--ref-sample", type=int, default=768)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skin", type=float, default=None,
                     help="neighbour-list skin in A for water98k-compressed (default 2; 0 = rebuild every step)")
@@ -456,7 +594,7 @@ def main():
     from dpgb import nlist as N, params as P, synth
     from dpgb.deeppot import DeepPot
 
-    params = P.init_params(P.water_config(), seed=1)
+    params = water_model(False)
     cfg = params.config
     coord, atype, box = synth.water_box(NMOL_SIDE, seed=rank)
     nloc = coord.shape[0]
@@ -535,7 +673,8 @@ def main():
     f_rmse = float(np.sqrt(np.mean((f_m - f_d) ** 2)))
     f_rms = float(np.sqrt(np.mean(f_d ** 2)))
     e_err = float(abs(out["energy"].item() - o64["energy"].item()) / nloc)
-    v_err = float(np.abs(out["virial"].cpu().numpy() - o64["virial"].cpu().numpy()).max())
+    v_err = float(np.abs(out["virial"].cpu().numpy() - o64["virial"].cpu().numpy()).max()
+                  / np.abs(o64["virial"].cpu().numpy()).max())
 
     if rank != 0:
         return
@@ -544,23 +683,20 @@ def main():
     dom_ms = stages[dom] / max(ncalls, 1)
     achieved = flops[dom] / (dom_ms * 1e-3) / 1e12
     peak = peaks.get("bf16_tflops", 1900.0)
-    cpu = None
-    if not args.no_cpu_baseline:
-        cpu = cpu_baseline_port(sample=args.ref_sample // 2)
+    cpu = None if args.no_cpu_baseline else cpu_baseline(False)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {
-            "workload": "water 4096 H2O (12,288 atoms), box 49.6 A, se_e2_a rc 6 sel [46,92] emb [25,50,100] "
-                        "axis 16 fit [240,240,240]; mixed form; full step incl. neighbour list"
-                        + ("" if args.no_graph else ", replayed from a CUDA graph"),
+            "workload": WORKLOAD_NAME["water12k"] + "; energy scaled to ~1 eV/A RMS forces; mixed form; full "
+                        "step incl. neighbour list" + ("" if args.no_graph else ", replayed from a CUDA graph"),
             "stage_times_from": "profiled evaluations without the graph",
             "natoms": nloc, "real_pairs": n_pairs, "l2": "flushed between timed steps (256 MB write, untimed)",
             "fp64_atom_steps_per_s": fp64_value, "fp64_ms_per_step": fp64_ms,
             "mixed_over_fp64": value / world / fp64_value,
             "force_rmse_vs_fp64_eV_per_A": f_rmse, "force_rms_fp64": f_rms,
-            "energy_err_per_atom_vs_fp64": e_err, "virial_max_abs_err_vs_fp64": v_err,
+            "energy_err_per_atom_vs_fp64": e_err, "virial_rel_err_vs_fp64": v_err,
             "stage_ms_per_step": {k: v / max(ncalls, 1) for k, v in stages.items()},
             "parallelism": f"replicas x{world}",
         },

@@ -59,7 +59,20 @@ inline int sm_count() {
 }
 
 // Device-side status word layout (one int per code, atomicMax'ed).
-enum StatusSlot { kStatusOverflow = 0, kStatusOverflowAtom = 1, kStatusTimeout = 2, kStatusSlots = 6 };
+// kStatusNonFinite: 1 + the first input atom seen with a non-finite
+// coordinate (any such atom; the others stay valid to read).
+enum StatusSlot {
+  kStatusOverflow = 0,
+  kStatusOverflowAtom = 1,
+  kStatusTimeout = 2,
+  kStatusNonFinite = 6,
+  kStatusSlots = 8
+};
+
+// a coordinate triple that is not finite (NaN or +-inf) flags the status
+__device__ __forceinline__ void flag_nonfinite(const double* x, int atom, int* status) {
+  if (status && !(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) atomicMax(status + kStatusNonFinite, atom + 1);
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

@@ -430,6 +430,10 @@ struct DeepPotImpl {
   cudaGraphExec_t sg_exec = nullptr;
   unsigned long long sg_gen = ~0ull;
   int sg_nframes = -1, sg_natom = -1, sg_launches = 0;
+  // shape of the last single-system evaluation's own neighbour list
+  // (ws_nlist, ws_coord, ws_svec), for dpgb_deeppot_last_nlist; 0 frames
+  // after an external list or a batch
+  int nl_nframes = 0, nl_natom = 0, nl_nshift = 0;
   std::vector<double> sg_box;
   const void* sg_ptr[6] = {};
   cudaEvent_t sg_ev_in = nullptr, sg_ev_out = nullptr;
@@ -462,8 +466,35 @@ struct DeepPotImpl {
 
 namespace {
 
-// BF16 weight images of the tensor-core fitting: forward B = W^T [out][in],
-// backward B = W [in][out] per type; FP32 bias / timestep / output layer.
+inline int pad64(int k) { return (k + 63) / 64 * 64; }
+
+// host inputs: every coordinate (and cell entry) must be finite
+int check_finite(const double* x, size_t n, const char* what) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(x[i]))
+      return fail(DPGB_EINVAL, std::string("non-finite ") + what + " (entry " + std::to_string(i) + ")");
+  return DPGB_OK;
+}
+
+// split-BF16 row of a weight image: the high parts of w[0 .. K) in columns
+// [0, K), their low parts (the BF16 rounding of w - hi) in [Kp, Kp + K),
+// zeros elsewhere
+template <typename F>
+void push_split_row(std::vector<__nv_bfloat16>& img, int K, int Kp, F w) {
+  const size_t b = img.size();
+  img.resize(b + 2 * (size_t)Kp, __float2bfloat16_rn(0.f));
+  for (int k = 0; k < K; ++k) {
+    const double v = w(k);
+    const __nv_bfloat16 hi = __float2bfloat16_rn((float)v);
+    img[b + k] = hi;
+    img[b + Kp + k] = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
+  }
+}
+
+// split-BF16 weight images of the tensor-core fitting: forward B = W^T
+// [out][hi | lo of in], backward B = W [in][hi | lo of out] per type (rows
+// padded to whole 64-column chunks per part); FP32 bias / timestep / output
+// layer.
 int build_fit_tc(DeepPotImpl& im, const dpgb_se_a_desc& d) {
   const int nt = d.ntypes;
   im.fit_nh = d.n_fit;
@@ -474,14 +505,17 @@ int build_fit_tc(DeepPotImpl& im, const dpgb_se_a_desc& d) {
   size_t offWt[kMaxFitLayers], offWb[kMaxFitLayers], offb[kMaxFitLayers], offi[kMaxFitLayers];
   for (int l = 0; l < d.n_fit; ++l) {
     const int a = im.fit_width[l], o = im.fit_width[l + 1];
+    const double* W = d.fit_w[0][l];
     offWt[l] = w16.size();
-    for (int t = 0; t < nt; ++t)
-      for (int n = 0; n < o; ++n)
-        for (int k = 0; k < a; ++k) w16.push_back(__float2bfloat16_rn((float)d.fit_w[t][l][(size_t)k * o + n]));
+    for (int t = 0; t < nt; ++t) {
+      W = d.fit_w[t][l];
+      for (int n = 0; n < o; ++n) push_split_row(w16, a, pad64(a), [&](int k) { return W[(size_t)k * o + n]; });
+    }
     offWb[l] = w16.size();
-    for (int t = 0; t < nt; ++t)
-      for (int k = 0; k < a; ++k)
-        for (int n = 0; n < o; ++n) w16.push_back(__float2bfloat16_rn((float)d.fit_w[t][l][(size_t)k * o + n]));
+    for (int t = 0; t < nt; ++t) {
+      W = d.fit_w[t][l];
+      for (int k = 0; k < a; ++k) push_split_row(w16, o, pad64(o), [&](int n) { return W[(size_t)k * o + n]; });
+    }
     offb[l] = f32.size();
     for (int t = 0; t < nt; ++t)
       for (int n = 0; n < o; ++n) f32.push_back((float)d.fit_b[t][l][n]);
@@ -532,8 +566,13 @@ int run_fit_tc(DeepPotImpl& dp, int nrows, const __nv_bfloat16* Db, float* dD, f
   const size_t plane = (size_t)nrows * maxw;
   auto Yf = [&](int l) { return act + (size_t)l * plane; };
   auto Tt = [&](int l) { return act + (size_t)(nh + l) * plane; };
+  // BF16 planes (fit_bf16_planes of them): the hidden outputs' high and low
+  // parts, two ping-pong gradient planes and the low part of the gradient
+  // the first layer's backward reads
   auto Yb = [&](int l) { return fitb + (size_t)l * plane; };
-  auto dPb = [&](int k) { return fitb + (size_t)(nh + k) * plane; };
+  auto Yb_lo = [&](int l) { return fitb + (size_t)(nh + l) * plane; };
+  auto dPb = [&](int k) { return fitb + (size_t)(2 * nh + k) * plane; };
+  __nv_bfloat16* dP1_lo = fitb + (size_t)(2 * nh + 2) * plane;
   auto dX = [&](int k) { return gbuf + (size_t)k * plane; };
   FitGemm base{};
   base.ntypes = nt;
@@ -550,8 +589,13 @@ int run_fit_tc(DeepPotImpl& dp, int nrows, const __nv_bfloat16* Db, float* dD, f
     g.mode = l == nh - 1 ? kFitFwdLast : kFitFwd;
     g.N = o;
     g.K = a;
+    g.Kp = pad64(a);
     g.A = l == 0 ? Db : Yb(l - 1);
     g.lda = l == 0 ? dim : maxw;
+    // D (BF16, its rounding is harmless) . (W hi + W lo); the hidden outputs
+    // in split BF16 as well
+    if (l > 0) g.A_lo = Yb_lo(l - 1);
+    if (l < nh - 1) g.Yb_lo = Yb_lo(l);
     g.B = dp.fit_Wt[l];
     g.bias = dp.fit_b[l];
     g.idt = dp.fit_idt[l];
@@ -566,6 +610,7 @@ int run_fit_tc(DeepPotImpl& dp, int nrows, const __nv_bfloat16* Db, float* dD, f
       g.w_out = dp.fit_wout;
       g.e_out = e_sorted;
       g.dPb = dPb(0);
+      if (nh == 1) g.dPb_lo = dP1_lo;  // read by the first layer's backward
     }
     DPGB_TRY(launch_fit_gemm(g, err, st));
   }
@@ -577,9 +622,12 @@ int run_fit_tc(DeepPotImpl& dp, int nrows, const __nv_bfloat16* Db, float* dD, f
     g.mode = kFitBwd;
     g.N = a;
     g.K = o;
+    g.Kp = pad64(o);
+    // dP (BF16) . (W hi + W lo)
     g.A = dPb(cur);
     g.lda = maxw;
     g.B = dp.fit_Wb[l];
+    if (l == 1) g.dPb_lo = dP1_lo;  // the gradient the first layer's backward reads
     if (o == a) {  // skip connection of layer l: gradient of its output passes through
       if (l == nh - 1) {
         g.dYup = dp.fit_wout;  // [type][wl] broadcast over rows
@@ -607,9 +655,11 @@ int run_fit_tc(DeepPotImpl& dp, int nrows, const __nv_bfloat16* Db, float* dD, f
       f.tile0[t] = base.tile0[t];
     }
     f.K = dp.fit_width[1];
+    f.Kp = pad64(f.K);
     f.ng = dp.ng;
     f.nnei = dp.sel.nnei;
     f.A = dPb(cur);
+    f.A_lo = dP1_lo;
     f.lda = maxw;
     f.B = dp.fit_Wb[0];
     f.xyz = xyz;
@@ -623,7 +673,9 @@ int run_fit_tc(DeepPotImpl& dp, int nrows, const __nv_bfloat16* Db, float* dD, f
   g.mode = kFitStore;
   g.N = dim;
   g.K = dp.fit_width[1];
+  g.Kp = pad64(g.K);
   g.A = dPb(cur);
+  g.A_lo = dP1_lo;
   g.lda = maxw;
   g.B = dp.fit_Wb[0];
   g.out = dD;
@@ -903,6 +955,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   int nshift_max = 1;
   std::vector<std::vector<double>> svecs(nframes);
   std::vector<double> host_coord;
+  if (own_geom && box_host) DPGB_TRY(check_finite(box_host, 9 * (size_t)nframes, "cell"));
   for (int f = 0; f < (int)geo.size(); ++f) {
     if (box_host) {
       CellGeom g0;
@@ -937,6 +990,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
                                   cudaMemcpyDeviceToHost, st));
         DPGB_CUDA(cudaStreamSynchronize(st));
       }
+      DPGB_TRY(check_finite(host_coord.data() + (size_t)f * natom * 3, (size_t)natom * 3, "coordinate"));
       DPGB_TRY(open_geom(host_coord.data() + (size_t)f * natom * 3, natom, d.rcut, geo[f]));
       spos[f].assign(1, 0);
       svecs[f].assign(3, 0.0);
@@ -1076,7 +1130,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       const double* svf = dp.ws_svec.as<double>() + (size_t)3 * nshift_max * f;
       int* cand = dp.ws_cand.as<int>() + a0 * ncand;
       DPGB_TRY(launch_skin_coords(cout, dp.ws_coordf.as<float4>() + a0, dp.ws_skin_off.as<double>() + 3 * a0,
-                                  dp.ws_skin_ref.as<double>() + 3 * a0, cin, natom, geo[f], gate, st));
+                                  dp.ws_skin_ref.as<double>() + 3 * a0, cin, natom, geo[f], gate, st, status));
       DPGB_TRY(launch_nlist_pt(cand, cout, dp.atype_dev.as<int>(), natom, geo[f], dp.ws_spos.as<int>() + spos_n * f,
                                svf, rc_geo, dp.skin_sel, dp.ws_cell.ptr, status, st, gate));
       DPGB_TRY(launch_skin_select(nlist + a0 * nnei, cand, ncand, cout, dp.ws_coordf.as<float4>() + a0,
@@ -1086,7 +1140,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       continue;
     }
     if (box_host) {
-      DPGB_TRY(launch_normalize(cout, cin, natom, geo[f], st));
+      DPGB_TRY(launch_normalize(cout, cin, natom, geo[f], st, status));
     } else {
       DPGB_CUDA(cudaMemcpyAsync(cout, cin, sizeof(double) * natom * 3, cudaMemcpyDeviceToDevice, st));
     }
@@ -1100,6 +1154,9 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     DPGB_TRY(launch_skin_advance(gate, st));
     ++launches;
   }
+  dp.nl_nframes = own_geom ? nframes : 0;
+  dp.nl_natom = natom;
+  dp.nl_nshift = nshift_max;
   dp.mark(DPGB_STAGE_NLIST, 1, st);
   // sorted transpose of the list over local rows
   // the sorted transpose on the side stream: only the force gather needs it
@@ -1198,7 +1255,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       DPGB_TRY(dp.ws_runlen.alloc(sizeof(int) * (size_t)std::max(nsorted, 1) * d.ntypes));
       // one buffer serves the per-section partial xyz of the forward and,
       // after it, dE/dxyz of the backward
-      DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ng * d.ntypes));
+      DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ((ng + 15) / 16 * 16) * d.ntypes));
       DPGB_TRY(launch_run_lengths(dp.ws_runlen.as<int>(), nlist, dp.sorted_rows_dev.as<int>(), nsorted, nnei, dp.sel,
                                   dp.pad_zero, st));
       EmbTC e = dp.tc;
@@ -1214,8 +1271,8 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     tab_path = !tc_path && dp.use_tab != 0;
     if (tab_path) {
       DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ng));
-      DPGB_TRY(launch_tab_fwd(p, m.emb, dp.sorted_rows_dev.as<int>(), dp.type_off[d.ntypes], dp.ws_xyz.as<float>(),
-                              dp.ws_D.ptr, dp.use_fit_tc, st));
+      DPGB_TRY(launch_tab_fwd(p, m.emb, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.sorted_rows_dev.as<int>(),
+                              dp.ws_xyz.as<float>(), dp.ws_D.ptr, dp.use_fit_tc, st));
       ++launches;
     }
   }
@@ -1228,7 +1285,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   bool fit_tc = false;
   if constexpr (std::is_same<T, float>::value) fit_tc = (tc_path || tab_path) && dp.use_fit_tc;
   if (fit_tc) {
-    DPGB_TRY(dp.ws_fitb.alloc(sizeof(__nv_bfloat16) * (size_t)(dp.fit_nh + 2) * nrows * maxw));
+    DPGB_TRY(dp.ws_fitb.alloc(sizeof(__nv_bfloat16) * (size_t)(2 * dp.fit_nh + 3) * nrows * maxw));
   }
   int dxyz_done = 0;  // dE/dxyz already formed by the fitting's last backward GEMM
   if (fit_tc) {
@@ -1265,8 +1322,8 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     if (tab_path) {
       DPGB_CUDA(cudaMemsetAsync(dp.ws_vir.ptr, 0, sizeof(double) * nrows * 9, st));
       if (!dxyz_done) DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
-      DPGB_TRY(launch_tab_bwd(p, m.emb, dp.sorted_rows_dev.as<int>(), dp.type_off[d.ntypes], dp.ws_dxyz.as<float>(),
-                              dp.ws_g.as<float>(), dp.ws_vir.as<double>(), st));
+      DPGB_TRY(launch_tab_bwd(p, m.emb, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.sorted_rows_dev.as<int>(),
+                              dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(), dp.ws_vir.as<double>(), st));
       launches += 2;
     }
   }
@@ -1326,6 +1383,9 @@ int status_result(DeepPotImpl& dp, const int* h) {
   if (h[kStatusOverflow] > 0)
     return fail(DPGB_EOVERFLOW, "neighbour capacity exceeded (" + std::to_string(h[kStatusOverflow]) +
                                     " entries) at atom/row " + std::to_string(h[kStatusOverflowAtom] - 1));
+  if (h[kStatusNonFinite] > 0)
+    return fail(DPGB_EINVAL, "non-finite input coordinate (atom " + std::to_string(h[kStatusNonFinite] - 1) +
+                                 "); results are invalid");
   if (h[kStatusTimeout] > 0)
     return fail(DPGB_ETIMEOUT, "a tensor-core completion wait timed out; results are invalid");
   if (h[kStatusTruncated] > 0) {
@@ -1744,6 +1804,31 @@ const char* dpgb_deeppot_check_ok(dpgb_deeppot* dp) { return dp ? dp->impl.err.c
 
 int dpgb_deeppot_last_launches(dpgb_deeppot* dp) { return dp ? dp->impl.launches : 0; }
 
+int dpgb_deeppot_last_nlist(dpgb_deeppot* dp, int* info, int* nlist, double* coord, double* shift) {
+  clear_error();
+  if (!dp || !info) return fail(DPGB_EINVAL, "NULL handle or info");
+  DeepPotImpl& im = dp->impl;
+  info[0] = im.nl_nframes;
+  info[1] = im.nl_natom;
+  info[2] = im.sel.nnei;
+  info[3] = im.nl_nshift;
+  if (im.nl_nframes <= 0) {
+    if (nlist || coord || shift)
+      return fail(DPGB_EINVAL, "the last evaluation built no list of its own (none yet, an external list or a batch)");
+    return DPGB_OK;
+  }
+  const size_t nrows = (size_t)im.nl_nframes * im.nl_natom;
+  cudaStream_t st = im.stream;
+  if (nlist)
+    DPGB_CUDA(cudaMemcpyAsync(nlist, im.ws_nlist.ptr, sizeof(int) * nrows * im.sel.nnei, cudaMemcpyDeviceToHost, st));
+  if (coord) DPGB_CUDA(cudaMemcpyAsync(coord, im.ws_coord.ptr, sizeof(double) * nrows * 3, cudaMemcpyDeviceToHost, st));
+  if (shift)
+    DPGB_CUDA(cudaMemcpyAsync(shift, im.ws_svec.ptr, sizeof(double) * 3 * (size_t)im.nl_nshift * im.nl_nframes,
+                              cudaMemcpyDeviceToHost, st));
+  DPGB_CUDA(cudaStreamSynchronize(st));
+  return DPGB_OK;
+}
+
 int dpgb_deeppot_set_profiling(dpgb_deeppot* dp, int on) {
   clear_error();
   if (!dp) return fail(DPGB_EINVAL, "NULL handle");
@@ -1859,7 +1944,9 @@ int dpgb_deeppot_compute_nlist(dpgb_deeppot* dp, int nall, int nghost, const dou
   clear_error();
   if (!dp) return fail(DPGB_EINVAL, "NULL handle");
   (void)box;  // the caller's list and ghost coordinates already encode the periodicity
-  int rc = compute_nlist_impl(dp->impl, nall, nghost, coord, atype, inum, ilist, numneigh, firstneigh, ago, energy,
+  int rc = coord && nall > 0 ? check_finite(coord, (size_t)nall * 3, "coordinate") : DPGB_OK;
+  if (rc == DPGB_OK)
+    rc = compute_nlist_impl(dp->impl, nall, nghost, coord, atype, inum, ilist, numneigh, firstneigh, ago, energy,
                               force, virial, atom_energy, atom_virial);
   dp->impl.err = rc == DPGB_OK ? "" : dpgb_last_error();
   return rc;

@@ -39,16 +39,23 @@ int emb_tc_eligible(const dpgb_se_a_desc& d) {
 
 size_t emb_tc_image_bytes(const EmbTC& m, int kind) {
   switch (kind) {
-    case 0: return (size_t)m.n2 * m.k1 * 2;
-    case 1: return (size_t)m.n3 * m.n2 * 2;
+    case 0: case 4: return (size_t)m.n2 * m.k1 * 2;
+    case 1: case 5: return (size_t)m.n3 * m.n2 * 2;
     case 2: return (size_t)m.n2 * m.n3 * 2;
     default: return (size_t)m.k1 * m.n2 * 2;
   }
 }
+constexpr int kEmbImageKinds = 6;
 
 static void put_bf16(std::vector<unsigned char>& img, size_t base, int r, int k, int K, float v) {
   const __nv_bfloat16 b = __float2bfloat16_rn(v);
   std::memcpy(img.data() + base + tc::cm_offset(r, k, K), &b, 2);
+}
+
+// the low BF16 part of a weight (its remainder after the BF16 rounding)
+static float bf16_lo(double w) {
+  const __nv_bfloat16 hi = __float2bfloat16_rn((float)w);
+  return (float)(w - (double)__bfloat162float(hi));
 }
 
 // bias b of output row r as BF16 hi + lo on the K columns k_hi, k_lo (the
@@ -69,9 +76,12 @@ int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, Em
   m.n3 = pad16(m.w3);
   m.nnets = nnets;
   m.vec_stride = 3 * m.k1 + 2 * m.n2 + 2 * m.n3;
-  size_t per[4];
-  for (int k = 0; k < 4; ++k) per[k] = emb_tc_image_bytes(m, k);
-  images.assign((per[0] + per[1] + per[2] + per[3]) * nnets, 0);
+  size_t per[kEmbImageKinds], kind0[kEmbImageKinds + 1] = {0};
+  for (int k = 0; k < kEmbImageKinds; ++k) {
+    per[k] = emb_tc_image_bytes(m, k);
+    kind0[k + 1] = kind0[k] + per[k] * nnets;  // images of kind k: nets in order from kind0[k]
+  }
+  images.assign(kind0[kEmbImageKinds], 0);
   vec.assign((size_t)m.vec_stride * nnets, 0.f);
   m.has_idt1 = m.has_idt2 = m.has_idt3 = 0;
   for (int e = 0; e < nnets; ++e) {
@@ -79,8 +89,8 @@ int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, Em
     const double* W2 = d.emb_w[e][1];  // [w1, w2]
     const double* W3 = d.emb_w[e][2];  // [w2, w3]
     if (!W1 || !W2 || !W3 || !d.emb_b[e][0] || !d.emb_b[e][1] || !d.emb_b[e][2]) return fail(DPGB_EINVAL, "missing embedding weights");
-    const size_t b0 = per[0] * e, b1 = per[0] * nnets + per[1] * e, b2 = (per[0] + per[1]) * nnets + per[2] * e,
-                 b3 = (per[0] + per[1] + per[2]) * nnets + per[3] * e;
+    const size_t b0 = kind0[0] + per[0] * e, b1 = kind0[1] + per[1] * e, b2 = kind0[2] + per[2] * e,
+                 b3 = kind0[3] + per[3] * e, b4 = kind0[4] + per[4] * e, b5 = kind0[5] + per[5] * e;
     // layer-2 outputs o sit at column c2 = neuron_col(o), layer-3 outputs at
     // c3; the biases of layers 2 and 3 on the bias columns of their inputs
     const int k2a = m.w1, k2b = m.w1 + 1;
@@ -93,12 +103,14 @@ int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, Em
       for (int k = 0; k < m.w1; ++k) {
         const int c2 = neuron_col(o, m.w2, m.w1);
         put_bf16(images, b0, c2, k, m.k1, (float)W2[(size_t)k * m.w2 + o]);  // W2^T [n2 x k1]
+        put_bf16(images, b4, c2, k, m.k1, bf16_lo(W2[(size_t)k * m.w2 + o]));
         put_bf16(images, b3, k, c2, m.n2, (float)W2[(size_t)k * m.w2 + o]);  // W2 [k1 x n2]
       }
     for (int o = 0; o < m.w3; ++o)
       for (int k = 0; k < m.w2; ++k) {
         const int c3 = neuron_col(o, m.w3, m.w2), c2 = neuron_col(k, m.w2, m.w1);
         put_bf16(images, b1, c3, c2, m.n2, (float)W3[(size_t)k * m.w3 + o]);  // W3^T [n3 x n2]
+        put_bf16(images, b5, c3, c2, m.n2, bf16_lo(W3[(size_t)k * m.w3 + o]));
         put_bf16(images, b2, c2, c3, m.n3, (float)W3[(size_t)k * m.w3 + o]);  // W3 [n2 x n3]
       }
     float* v = vec.data() + (size_t)m.vec_stride * e;
@@ -127,12 +139,12 @@ int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, Em
 }
 
 void emb_tc_bind(EmbTC& m, const unsigned char* dev, size_t, const float* dev_vec) {
-  const size_t p0 = emb_tc_image_bytes(m, 0) * m.nnets, p1 = emb_tc_image_bytes(m, 1) * m.nnets,
-               p2 = emb_tc_image_bytes(m, 2) * m.nnets;
-  m.fw2 = dev;
-  m.fw3 = dev + p0;
-  m.bw3 = dev + p0 + p1;
-  m.bw2 = dev + p0 + p1 + p2;
+  const unsigned char** dst[kEmbImageKinds] = {&m.fw2, &m.fw3, &m.bw3, &m.bw2, &m.fw2lo, &m.fw3lo};
+  size_t off = 0;
+  for (int k = 0; k < kEmbImageKinds; ++k) {
+    *dst[k] = dev + off;
+    off += emb_tc_image_bytes(m, k) * m.nnets;
+  }
   m.vec = dev_vec;
 }
 
@@ -157,6 +169,22 @@ __device__ __forceinline__ void store8(unsigned char* base, int r, int k0, int K
 #pragma unroll
   for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
   *reinterpret_cast<uint4*>(base + tc::cm_offset(r, k0, K)) = *reinterpret_cast<uint4*>(h);
+}
+
+// the same as split-BF16 parts: the high parts (BF16 of v) at base, the low
+// parts (BF16 of v - hi) at base_lo; an MMA over each then carries the
+// operand to ~16 significant bits (1 and 0 have no low part)
+__device__ __forceinline__ void store8_split(unsigned char* base, unsigned char* base_lo, int r, int k0, int K,
+                                             const float* v) {
+  __nv_bfloat162 h[4], l[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+    l[i] = __floats2bfloat162_rn(v[2 * i] - __low2float(h[i]), v[2 * i + 1] - __high2float(h[i]));
+  }
+  const int off = tc::cm_offset(r, k0, K);
+  *reinterpret_cast<uint4*>(base + off) = *reinterpret_cast<uint4*>(h);
+  *reinterpret_cast<uint4*>(base_lo + off) = *reinterpret_cast<uint4*>(l);
 }
 
 // D (+)= A B over kdim; acc0: add onto what D holds already (a preloaded
@@ -319,18 +347,27 @@ constexpr int kFinAtoms = 4;  // atoms finalised together (xyz -> D) in the forw
 template <int W1, int W2, int W3>
 struct PlanF {
   static constexpr int K1 = (W1 + 15) / 16 * 16, N2 = (W2 + 15) / 16 * 16, N3 = (W3 + 15) / 16 * 16;
-  static constexpr int LDG = (W3 + 3) / 4 * 4;  // fp32 G row stride: float4 rows
+  // G is staged in FP32 by accumulator column, HC columns per pass (row
+  // stride LDG; a row's float4 quad q sits at quad q ^ (row & 7), so the
+  // eight rows of a float4 store phase hit distinct banks)
+  static constexpr int HC = 64, LDG = HC;
   // operand columns holding 1 for the biases of layers 2 (A1) and 3 (A2)
   static constexpr int ONE2a = W1, ONE2b = W1 + 1, ONE3a = bias_col(0, W2, W1, N2), ONE3b = bias_col(1, W2, W1, N2);
   static constexpr int VEC = 3 * K1 + 2 * N2 + 2 * N3;
+  // weights in split BF16: the high parts, then the low parts
   static constexpr int fw2 = 0;
   static constexpr int fw3 = fw2 + N2 * K1 * 2;
-  static constexpr int vec = fw3 + N3 * N2 * 2;
+  static constexpr int fw2lo = fw3 + N3 * N2 * 2;
+  static constexpr int fw3lo = fw2lo + N2 * K1 * 2;
+  static constexpr int vec = fw3lo + N3 * N2 * 2;
   static constexpr int rn = (vec + VEC * 4 + 15) / 16 * 16;
   static constexpr int reg = (rn + 128 * 4 * 4 + 127) / 128 * 128;
-  static constexpr int a1 = reg, a2 = reg, gbuf = reg, xs = reg;
+  // split-BF16 operands: the low parts follow the high parts
+  static constexpr int a1 = reg, a1lo = reg + 128 * K1 * 2, a2 = reg, a2lo = reg + 128 * N2 * 2;
+  static constexpr int gbuf = reg, xs = reg;
   static constexpr int cmax(int a, int b) { return a > b ? a : b; }
-  static constexpr int reg_bytes = cmax(cmax(128 * K1 * 2, 128 * N2 * 2), cmax(128 * LDG * 4, kFinAtoms * 4 * W3 * 4));
+  static constexpr int reg_bytes =
+      cmax(cmax(2 * 128 * K1 * 2, 2 * 128 * N2 * 2), cmax(128 * LDG * 4, kFinAtoms * 4 * W3 * 4));
   static constexpr int total = reg + reg_bytes;
   static constexpr int tmem_cols = cmax(N2, N3) <= 128 ? 128 : 256;
 };
@@ -350,9 +387,11 @@ struct PlanB {
   static constexpr int bw2 = bw3 + N2 * N3 * 2;
   static constexpr int vec = bw2 + K1 * N2 * 2;
   static constexpr int reg = (vec + VEC * 4 + 127) / 128 * 128;
-  static constexpr int a1 = reg, a2 = reg, a3 = reg, vir = reg;
+  // the recomputed forward's operands are split-BF16 (low parts after the
+  // high parts), as in the forward; the gradient operands dP3, dP2 are BF16
+  static constexpr int a1 = reg, a1lo = reg + 128 * K1 * 2, a2 = reg, a2lo = reg + 128 * N2 * 2, a3 = reg, vir = reg;
   static constexpr int cmax(int a, int b) { return a > b ? a : b; }
-  static constexpr int reg_bytes = cmax(cmax(128 * K1 * 2, 128 * N2 * 2), cmax(128 * N3 * 2, 128 * 9 * 4));
+  static constexpr int reg_bytes = cmax(cmax(2 * 128 * K1 * 2, 2 * 128 * N2 * 2), cmax(128 * N3 * 2, 128 * 9 * 4));
   static constexpr int total = reg + reg_bytes;
   static constexpr int tmem_cols = cmax(N3, N2 + K1) <= 128 ? 128 : 256;
 };
@@ -380,15 +419,19 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
   float* sRn = reinterpret_cast<float*>(smem + P::rn);
   float* sV = reinterpret_cast<float*>(smem + P::vec);
   const uint32_t sA1 = tc::smem_u32(smem + P::a1), sA2 = tc::smem_u32(smem + P::a2);
+  const uint32_t sA1lo = tc::smem_u32(smem + P::a1lo), sA2lo = tc::smem_u32(smem + P::a2lo);
   const uint32_t sW2 = tc::smem_u32(smem + P::fw2), sW3 = tc::smem_u32(smem + P::fw3);
+  const uint32_t sW2lo = tc::smem_u32(smem + P::fw2lo), sW3lo = tc::smem_u32(smem + P::fw3lo);
   for (int c = blockIdx.x; c < nchunks && alive; c += gridDim.x) {
     const WorkChunk ch = chunks[c];
     const int ti = ch.ti;
     for (int t = 0; t < p.ntypes && alive; ++t) {
       const int net = p.type_one_side ? t : t * p.ntypes + ti;
-      float* xpart = xyzp + (size_t)t * p.nrows * 4 * ng;  // this section's partial xyz
+      float* xpart = xyzp + (size_t)t * p.nrows * 4 * P::N3;  // this section's partial xyz, by column
       copy16(smem + P::fw2, e.fw2 + (size_t)net * P::N2 * P::K1 * 2, P::N2 * P::K1 * 2);
       copy16(smem + P::fw3, e.fw3 + (size_t)net * P::N3 * P::N2 * 2, P::N3 * P::N2 * 2);
+      copy16(smem + P::fw2lo, e.fw2lo + (size_t)net * P::N2 * P::K1 * 2, P::N2 * P::K1 * 2);
+      copy16(smem + P::fw3lo, e.fw3lo + (size_t)net * P::N3 * P::N2 * 2, P::N3 * P::N2 * 2);
       for (int q = tid; q < P::VEC; q += blockDim.x) sV[q] = e.vec[(size_t)net * P::VEC + q];
       if (tid == 0) s_cursor = ch.row0;
       __syncthreads();
@@ -428,13 +471,15 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 #pragma unroll
           for (int i = 0; i < 8; ++i)
             v[i] = (k0 + i < W1) ? h1[k0 + i] : (k0 + i == P::ONE2a || k0 + i == P::ONE2b ? 1.f : 0.f);
-          store8(smem + P::a1, tid, k0, P::K1, v);
+          store8_split(smem + P::a1, smem + P::a1lo, tid, k0, P::K1, v);
         }
         tc::fence_async_smem();
         __syncthreads();
         tc::fence_after();
         if (tid == 0) {
-          issue_mma<P::K1, P::N2>(tbase, sA1, sW2, P::K1);
+          issue_mma<P::K1, P::N2>(tbase, sA1, sW2, P::K1);  // hi.hi + lo.hi + hi.lo
+          issue_mma<P::K1, P::N2>(tbase, sA1lo, sW2, P::K1, true);
+          issue_mma<P::K1, P::N2>(tbase, sA1, sW2lo, P::K1, true);
           tc::mma_commit(&bar);
         }
         bool ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout);
@@ -466,7 +511,7 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
             const int o = col_neuron(k0 + i, W2, W1);
             v[i] = o >= 0 ? h2[o] : (k0 + i == P::ONE3a || k0 + i == P::ONE3b ? 1.f : 0.f);
           }
-          store8(smem + P::a2, tid, k0, P::N2, v);
+          store8_split(smem + P::a2, smem + P::a2lo, tid, k0, P::N2, v);
         }
         tc::fence_before();
         tc::fence_async_smem();
@@ -474,82 +519,74 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         tc::fence_after();
         if (tid == 0) {
           issue_mma<P::N2, P::N3>(tbase, sA2, sW3, P::N2);  // over the consumed layer-2 columns
+          issue_mma<P::N2, P::N3>(tbase, sA2lo, sW3, P::N2, true);
+          issue_mma<P::N2, P::N3>(tbase, sA2, sW3lo, P::N2, true);
           tc::mma_commit(&bar);
         }
         ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;
         phase ^= 1;
         tc::fence_after();
         // epilogue 3: G = tanh(acc) * idt3 + skip(H2) (acc includes b3), kept in FP32,
-        // stored as float4 rows
+        // staged and contracted HC accumulator columns at a time
 #pragma unroll
-        for (int c0 = 0; c0 < P::N3; c0 += 32) {
-          float v[32];
-          tmem_ld32<P::N3>(tc::taddr(tbase, warp * 32, 0), c0, v);
-          float g[32];
+        for (int cb = 0; cb < P::N3; cb += P::HC) {  // unrolled: column indices stay compile-time
+          if (!alive) break;
+          // G of columns [cb, cb + HC) by column (0 on padding columns)
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            const int c = c0 + i, o = c < P::N3 ? col_neuron(c, W3, W2) : -1;
-            g[i] = 0.f;
-            if (o >= 0) {
-              float x3 = tanh_fast(v[i]);
-              if (IDT) x3 *= i3[c];
-              if (W3 == W2) x3 += h2[o];
-              if (W3 == 2 * W2) x3 += h2[o < W2 ? o : o - W2];
-              g[i] = x3;
+          for (int c0 = 0; c0 < P::HC; c0 += 16) {
+            if (cb + c0 >= P::N3) break;
+            float v[16], g[16];
+            tc::tmem_ld16(tc::taddr(tbase, warp * 32, cb + c0), v);
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              const int c = cb + c0 + i, o = col_neuron(c, W3, W2);
+              g[i] = 0.f;
+              if (o >= 0) {
+                float x3 = tanh_fast(v[i]);
+                if (IDT) x3 *= i3[c];
+                if (W3 == W2) x3 += h2[o];
+                if (W3 == 2 * W2) x3 += h2[o < W2 ? o : o - W2];
+                g[i] = x3;
+              }
             }
-          }
-          // G in neuron order; column pairs that hold two consecutive
-          // neurons (from an even one) go out as one float2
-          float* grow = sG + tid * P::LDG;
+            float4* grow = reinterpret_cast<float4*>(sG + tid * P::LDG);
 #pragma unroll
-          for (int i = 0; i < 32; i += 2) {
-            if (c0 + i >= P::N3) break;
-            const int o0 = col_neuron(c0 + i, W3, W2), o1 = col_neuron(c0 + i + 1, W3, W2);
-            if (o0 >= 0 && o1 == o0 + 1 && (o0 & 1) == 0) {
-              *reinterpret_cast<float2*>(grow + o0) = make_float2(g[i], g[i + 1]);
-            } else {
-              if (o0 >= 0) grow[o0] = g[i];
-              if (o1 >= 0) grow[o1] = g[i + 1];
-            }
+            for (int i = 0; i < 4; ++i)
+              grow[(c0 / 4 + i) ^ (tid & 7)] = make_float4(g[4 * i], g[4 * i + 1], g[4 * i + 2], g[4 * i + 3]);
           }
+          tc::fence_before();
+          alive = __syncthreads_and(ok) != 0;
+          if (!alive) break;
+          // partial xyz of this section: sum_{pairs of the atom} Rn[c] G[n]
+          // (FP32, fixed order; plain stores, the atom is owned by this CTA),
+          // by accumulator column (rows of N3 columns).  One thread per
+          // (atom, 4 columns): per pair one float4 of G and one of Rn feed 16
+          // FMAs.
+          const int nq = (P::N3 - cb < P::HC ? P::N3 - cb : P::HC) / 4;  // a constant once unrolled
+          for (int q = tid; q < ntile * nq; q += blockDim.x) {
+            const int k = q / nq, qq = q - k * nq;
+            float4 a[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) a[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) {
+              const float4 g = reinterpret_cast<const float4*>(sG + pp * P::LDG)[qq ^ (pp & 7)];
+              const float4 r = *reinterpret_cast<const float4*>(sRn + pp * 4);
+              const float rc[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+              for (int c = 0; c < 4; ++c) {
+                a[c].x = fmaf(rc[c], g.x, a[c].x);
+                a[c].y = fmaf(rc[c], g.y, a[c].y);
+                a[c].z = fmaf(rc[c], g.z, a[c].z);
+                a[c].w = fmaf(rc[c], g.w, a[c].w);
+              }
+            }
+            float4* o = reinterpret_cast<float4*>(xpart + (size_t)s_row[k] * 4 * P::N3 + cb) + qq;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) o[c * (P::N3 / 4)] = a[c];
+          }
+          __syncthreads();
         }
-        tc::fence_before();
-        alive = __syncthreads_and(ok) != 0;
-        if (!alive) break;
-        // partial xyz of this section: sum_{pairs of the atom} Rn[c] G[n]
-        // (FP32, fixed order; plain stores, the atom is owned by this CTA).
-        // One thread per (atom, 4 neurons): per pair one float4 of G and one
-        // of Rn feed 16 FMAs.
-        constexpr int NQ = P::LDG / 4;
-        for (int q = tid; q < ntile * NQ; q += blockDim.x) {
-          const int k = q / NQ, n0 = 4 * (q - k * NQ);
-          float4 a[4];
-#pragma unroll
-          for (int c = 0; c < 4; ++c) a[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) {
-            const float4 g = *reinterpret_cast<const float4*>(sG + pp * P::LDG + n0);
-            const float4 r = *reinterpret_cast<const float4*>(sRn + pp * 4);
-            const float rc[4] = {r.x, r.y, r.z, r.w};
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              a[c].x = fmaf(rc[c], g.x, a[c].x);
-              a[c].y = fmaf(rc[c], g.y, a[c].y);
-              a[c].z = fmaf(rc[c], g.z, a[c].z);
-              a[c].w = fmaf(rc[c], g.w, a[c].w);
-            }
-          }
-          float* o = xpart + (size_t)s_row[k] * 4 * ng + n0;
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            if (n0 + 3 < W3 && (ng & 3) == 0) {
-              *reinterpret_cast<float4*>(o + c * ng) = a[c];
-            } else {
-              const float av[4] = {a[c].x, a[c].y, a[c].z, a[c].w};
-              for (int u = 0; u < 4 && n0 + u < W3; ++u) o[c * ng + u] = av[u];
-            }
-          }
-        }
-        __syncthreads();
       }
     }
     // finalize the chunk, kFinAtoms atoms at a time: xyz = sum over sections
@@ -563,10 +600,12 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
       // (ng == W3: index arithmetic by compile-time divisors only)
       for (int q = tid; q < nr * 4 * W3; q += blockDim.x) {
         const int a = q / (4 * W3), qq = q - a * 4 * W3;
+        const int cc = qq / W3, n = qq - cc * W3;
+        const int col = cc * P::N3 + neuron_col(n, W3, W2);  // the partials are by accumulator column
         const int r = r0 + a, row = sorted_rows[r];
         float s = 0.f;
         for (int t = 0; t < p.ntypes; ++t)
-          if (run_len[(size_t)r * p.ntypes + t] > 0) s += xyzp[((size_t)t * p.nrows + row) * 4 * W3 + qq];
+          if (run_len[(size_t)r * p.ntypes + t] > 0) s += xyzp[((size_t)t * p.nrows + row) * 4 * P::N3 + col];
         s *= inv;
         sX[q] = s;
         xyz[(size_t)row * 4 * W3 + qq] = s;
@@ -638,6 +677,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
   float* sV = reinterpret_cast<float*>(smem + P::vec);
   float* sVir = reinterpret_cast<float*>(smem + P::vir);
   const uint32_t sA = tc::smem_u32(smem + P::reg);  // A1, A2, dP3, dP2 in turn
+  const uint32_t sA1lo = tc::smem_u32(smem + P::a1lo), sA2lo = tc::smem_u32(smem + P::a2lo);
   const uint32_t sW2 = tc::smem_u32(smem + P::fw2), sW3 = tc::smem_u32(smem + P::fw3);
   const uint32_t sB3 = tc::smem_u32(smem + P::bw3), sB2 = tc::smem_u32(smem + P::bw2);
   const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
@@ -700,13 +740,14 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
 #pragma unroll
           for (int i = 0; i < 8; ++i)
             v[i] = (k0 + i < W1) ? h1(k0 + i) : (k0 + i == P::ONE2a || k0 + i == P::ONE2b ? 1.f : 0.f);
-          store8(smem + P::a1, tid, k0, P::K1, v);
+          store8_split(smem + P::a1, smem + P::a1lo, tid, k0, P::K1, v);
         }
         tc::fence_async_smem();
         __syncthreads();
         tc::fence_after();
         if (tid == 0) {
           issue_mma<P::K1, P::N2>(tbase, sA, sW2, P::K1);
+          issue_mma<P::K1, P::N2>(tbase, sA1lo, sW2, P::K1, true);
           tc::mma_commit(&bar);
         }
         bool ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout);
@@ -740,7 +781,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
             const int o = col_neuron(k0 + i, W2, W1);
             v[i] = o >= 0 ? h2(o, k0 + i) : (k0 + i == P::ONE3a || k0 + i == P::ONE3b ? 1.f : 0.f);
           }
-          store8(smem + P::a2, tid, k0, P::N2, v);
+          store8_split(smem + P::a2, smem + P::a2lo, tid, k0, P::N2, v);
         }
         tc::fence_before();
         tc::fence_async_smem();
@@ -748,6 +789,7 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
         tc::fence_after();
         if (tid == 0) {
           issue_mma<P::N2, P::N3>(tbase, sA, sW3, P::N2);  // over the consumed layer-2 columns
+          issue_mma<P::N2, P::N3>(tbase, sA2lo, sW3, P::N2, true);
           tc::mma_commit(&bar);
         }
         ok = tc::mbar_wait(&bar, phase, status + kStatusTimeout) && ok;

@@ -52,6 +52,8 @@ struct EmbTC {
   const unsigned char* fw3;  // forward B of layer 3: W3^T [n3 x n2]
   const unsigned char* bw3;  // backward B of layer 3: W3 [n2 x n3]
   const unsigned char* bw2;  // backward B of layer 2: W2 [k1 x n2]
+  const unsigned char* fw2lo;  // low BF16 parts of fw2 (the forward's weights are split BF16)
+  const unsigned char* fw3lo;  // low BF16 parts of fw3
   const float* vec;          // [nnets][vec_stride]: w1 b1 idt1 | b2 idt2 | b3 idt3 (padded; b2, b3 also ride
                              // in fw2 / fw3 on the bias columns, which is where the kernels take them from)
   int vec_stride;
@@ -74,11 +76,11 @@ int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, Em
                  std::vector<float>& vec);
 // fill device pointers of meta from one device buffer holding images then vec
 void emb_tc_bind(EmbTC& meta, const unsigned char* dev_images, size_t img_bytes_per_kind, const float* dev_vec);
-size_t emb_tc_image_bytes(const EmbTC& m, int kind);  // per net: 0 fw2, 1 fw3, 2 bw3, 3 bw2
+size_t emb_tc_image_bytes(const EmbTC& m, int kind);  // per net: 0 fw2, 1 fw3, 2 bw3, 3 bw2, 4 fw2lo, 5 fw3lo
 
 int launch_run_lengths(int* run_len, const int* nlist, const int* sorted_rows, int nrows, int nnei,
                        const SelInfo& sel, int pad_zero, cudaStream_t st);
-// xyzp: per-section partial xyz, [ntypes][nrows][4][ng] FP32 scratch
+// xyzp: per-section partial xyz by accumulator column, [ntypes][nrows][4][pad16(ng)] FP32 scratch
 int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks,
                       const int* run_len, const int* sorted_rows, float* xyz, float* xyzp, float* D, int* status,
                       cudaStream_t st);

@@ -25,10 +25,26 @@ namespace {
 
 constexpr int kKC = 64;
 
-__device__ __forceinline__ float tanh_fast(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
+// tanh to a few units in the last place (the hardware tanh.approx.f32 is
+// good to about 2^-11 relative, which alone moved forces by ~4e-4 of their
+// RMS): below 1/16 the odd series x - x^3/3 + 2x^5/15 - 17x^7/315 (next
+// term 62/2835 x^9 < 4e-13 there); above, 1 - 2 / (e^{2|x|} + 1) with the
+// exponential and the division of CUDA's fast intrinsics (relative error of
+// a few 1e-7 before the subtraction, which only shrinks it).
+__device__ __forceinline__ float tanh_acc(float x) {
+  const float a = fabsf(x);
+  if (a < 0.0625f) {
+    const float x2 = x * x;
+    return x * fmaf(x2, fmaf(x2, fmaf(x2, -17.f / 315.f, 2.f / 15.f), -1.f / 3.f), 1.f);
+  }
+  const float e = __expf(2.f * fminf(a, 12.f));
+  return copysignf(1.f - __fdividef(2.f, e + 1.f), x);
+}
+
+// high and low BF16 parts of an FP32 value (hi + lo carries ~16 bits)
+__device__ __forceinline__ void split_bf16(float v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(v);
+  lo = __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
 
@@ -56,26 +72,44 @@ __device__ __forceinline__ void st16b(__nv_bfloat16* p, const float* v) {
   q[0] = *reinterpret_cast<uint4*>(&h[0]);
   q[1] = *reinterpret_cast<uint4*>(&h[4]);
 }
+// 16 values as BF16 high parts at p and, when lo is set, low parts at lo
+__device__ __forceinline__ void st16b_split(__nv_bfloat16* p, __nv_bfloat16* lo, const float* v) {
+  if (!lo) {
+    st16b(p, v);
+    return;
+  }
+  __nv_bfloat16 h[16], l[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) split_bf16(v[i], h[i], l[i]);
+  uint4* q = reinterpret_cast<uint4*>(p);
+  q[0] = *reinterpret_cast<uint4*>(&h[0]);
+  q[1] = *reinterpret_cast<uint4*>(&h[8]);
+  uint4* ql = reinterpret_cast<uint4*>(lo);
+  ql[0] = *reinterpret_cast<uint4*>(&l[0]);
+  ql[1] = *reinterpret_cast<uint4*>(&l[8]);
+}
 
-template <int BN, int S, int WG>
+// NA: parts of A (1: hi, 2: hi and lo); the weight always comes as hi and
+// lo.  A stage holds one K chunk of every part, so each part is read once.
+template <int BN, int S, int WG, int NA>
 __global__ void __launch_bounds__(128 * WG)
-fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b, FitGemm g,
-                int* __restrict__ err) {
+fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_alo,
+                const __grid_constant__ CUtensorMap tma_b, FitGemm g, int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   // swizzled TMA tiles want 1024-byte aligned stages
   unsigned char* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
   __shared__ uint64_t full[S], empty[S], done;
   __shared__ uint32_t s_tmem;
   __shared__ float s_e[2 * (WG - 1) * 128 + 2];  // compensated partial energies of column groups 1 .. WG-1
-  constexpr int SA = 128 * kKC * 2, SB = BN * kKC * 2;
+  constexpr int SA = 128 * kKC * 2, SB = BN * kKC * 2, STAGE = NA * SA + 2 * SB;
   constexpr uint32_t kTmemCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
   static_assert(BN % 16 == 0 && BN <= 256 && SB % 1024 == 0, "whole 16-column loads, 1024-byte aligned stages");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   int t = 0;
-  while (t + 1 < g.ntypes && g.tile0[t + 1] <= (int)blockIdx.x) ++t;
-  const int m0 = g.row0[t] + ((int)blockIdx.x - g.tile0[t]) * 128;
+  while (t + 1 < g.ntypes && g.tile0[t + 1] <= (int)blockIdx.y) ++t;
+  const int m0 = g.row0[t] + ((int)blockIdx.y - g.tile0[t]) * 128;
   const int rows_valid = min(128, g.row0[t + 1] - m0);
-  const int n0 = blockIdx.y * BN;
+  const int n0 = blockIdx.x * BN;
   const int nt = min(BN, g.N - n0);  // multiple of 16
   if (warp == 0) tc::tmem_alloc(&s_tmem, kTmemCols);
   if (tid == 0) {
@@ -89,6 +123,7 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   __syncthreads();
   tc::fence_after();
   const uint32_t tbase = s_tmem;
+  // stage layout: A hi [, A lo], B hi, B lo
   const int nchunk = (g.K + kKC - 1) / kKC;
   bool ok = true;
   if (warp == 1 && lane == 0) {
@@ -97,24 +132,31 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
       const int s = i % S;
       if (i >= S) ok = tc::mbar_wait(&empty[s], ((i / S) - 1) & 1, err);
       if (!ok) break;
-      const uint32_t a0 = tc::smem_u32(smem + s * (SA + SB));
-      tc::mbar_expect_tx(&full[s], SA + SB);
+      const uint32_t a0 = tc::smem_u32(smem + s * STAGE), b0 = a0 + NA * SA;
+      tc::mbar_expect_tx(&full[s], STAGE);
       tc::tma_load_2d(a0, &tma_a, i * kKC, m0, &full[s]);
-      tc::tma_load_2d(a0 + SA, &tma_b, i * kKC, t * g.N + n0, &full[s]);
+      if (NA == 2) tc::tma_load_2d(a0 + SA, &tma_alo, i * kKC, m0, &full[s]);
+      tc::tma_load_2d(b0, &tma_b, i * kKC, t * g.N + n0, &full[s]);
+      tc::tma_load_2d(b0 + SB, &tma_b, g.Kp + i * kKC, t * g.N + n0, &full[s]);
     }
   } else if (warp == 0 && lane == 0) {
-    // MMA issuer: 4 steps of K = 16 per chunk (zeros past K add nothing)
+    // MMA issuer: 4 steps of K = 16 per chunk (zeros past K add nothing),
+    // each hi.hi (+ lo.hi) + hi.lo
     const uint32_t idesc = tc::idesc_bf16_f32(128, nt);
     for (int i = 0; i < nchunk && ok; ++i) {
       const int s = i % S;
       ok = tc::mbar_wait(&full[s], (i / S) & 1, err);
       if (!ok) break;
       tc::fence_after();
-      const uint32_t a0 = tc::smem_u32(smem + s * (SA + SB)), b0 = a0 + SA;
+      const uint32_t a0 = tc::smem_u32(smem + s * STAGE), b0 = a0 + NA * SA;
 #pragma unroll
-      for (int ks = 0; ks < kKC / 16; ++ks)
+      for (int ks = 0; ks < kKC / 16; ++ks) {
         tc::mma_bf16(tbase, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc,
                      (i > 0 || ks > 0) ? 1u : 0u);
+        if (NA == 2)
+          tc::mma_bf16(tbase, tc::smem_desc_sw128(a0 + SA + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc, 1u);
+        tc::mma_bf16(tbase, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + SB + ks * 32), idesc, 1u);
+      }
       tc::mma_commit(&empty[s]);
     }
     tc::mma_commit(&done);
@@ -148,14 +190,14 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
         if (g.skip) ld16f(g.Xs + (size_t)m * g.ldxs + n, xs);
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-          tv[i] = tanh_fast(v[i] + bb[i]);
+          tv[i] = tanh_acc(v[i] + bb[i]);
           y[i] = idt ? tv[i] * id[i] : tv[i];
           if (g.skip) y[i] += xs[i];
         }
         if (g.mode == kFitFwd) {
           st16f(g.Yf + (size_t)m * g.ldy + n, y);
           st16f(g.Tt + (size_t)m * g.ldy + n, tv);
-          st16b(g.Yb + (size_t)m * g.ldy + n, y);
+          st16b_split(g.Yb + (size_t)m * g.ldy + n, g.Yb_lo ? g.Yb_lo + (size_t)m * g.ldy + n : nullptr, y);
         } else {
           float w[16], dp[16];
           ld16f(wo + n, w);
@@ -166,7 +208,7 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
             e_lo += fmaf(y[i], w[i], -pr);  // the product's rounding error
             dp[i] = w[i] * (idt ? id[i] : 1.f) * (1.f - tv[i] * tv[i]);
           }
-          st16b(g.dPb + (size_t)m * g.ldy + n, dp);
+          st16b_split(g.dPb + (size_t)m * g.ldy + n, g.dPb_lo ? g.dPb_lo + (size_t)m * g.ldy + n : nullptr, dp);
         }
       } else if (g.mode == kFitBwd) {
         float dx[16], up[16], tl[16], il[16], dp[16];
@@ -182,7 +224,7 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
         if (idt_lo) ld16f(idt_lo + n, il);
 #pragma unroll
         for (int i = 0; i < 16; ++i) dp[i] = dx[i] * (idt_lo ? il[i] : 1.f) * (1.f - tl[i] * tl[i]);
-        st16b(g.dPb + (size_t)m * g.ldy + n, dp);
+        st16b_split(g.dPb + (size_t)m * g.ldy + n, g.dPb_lo ? g.dPb_lo + (size_t)m * g.ldy + n : nullptr, dp);
       } else {
         st16f(g.out + (size_t)m * g.ldo + n, v);
       }
@@ -209,15 +251,16 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
 
 // dE/dD of the first layer folded into dE/dxyz (FitDxyz).  One CTA per
 // 128-row tile walks all 16 ng columns of dD in chunks of 128 (8 neurons):
-// dP1 stays in shared memory, W1 streams through an S-stage TMA ring two
-// chunks ahead, each chunk's accumulator is read by the epilogue (thread =
-// row): the first term goes out per neuron, the transposed term of the first
-// 16 neurons accumulates in registers and is added at the end.
-constexpr int kDxM = 16, kDxBN = 128, kDxStages = 8;
+// dP1 (high and low BF16 parts) stays in shared memory, W1 (high, then low
+// part) streams through an S-stage TMA ring, each chunk's accumulator sums
+// the three split segments and is read by the epilogue (thread = row): the
+// first term goes out per neuron, the transposed term of the first 16
+// neurons accumulates in registers and is added at the end.
+constexpr int kDxM = 16, kDxBN = 128, kDxStages = 5, kDxSeg = 3;
 
 __global__ void __launch_bounds__(256, 1)
-fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_b, FitDxyz f,
-                int* __restrict__ err) {
+fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_alo,
+                const __grid_constant__ CUtensorMap tma_b, FitDxyz f, int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
   constexpr int SA = 128 * kKC * 2, SB = kDxBN * kKC * 2, M = kDxM, S = kDxStages;
@@ -229,9 +272,11 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   const int m0 = f.row0[t] + ((int)blockIdx.x - f.tile0[t]) * 128;
   const int rows_valid = min(128, f.row0[t + 1] - m0);
   const int ncol = f.ng * M, nk = (f.K + kKC - 1) / kKC, nchunk = (ncol + kDxBN - 1) / kDxBN;
-  const int L = nchunk * nk;  // B loads
-  unsigned char* sA = smem;              // nk stages of dP1
-  unsigned char* sB = smem + nk * SA;    // ring
+  const int per = kDxSeg * nk;  // B loads of one column chunk: segment-major, K chunks inside
+  const int L = nchunk * per;   // B loads
+  unsigned char* sA = smem;              // nk stages of dP1 (high part)
+  unsigned char* sAlo = smem + nk * SA;  // nk stages of dP1 (low part)
+  unsigned char* sB = smem + 2 * nk * SA;  // ring
   if (warp == 0) tc::tmem_alloc(&s_tmem, kDxBN);
   if (tid == 0) {
     for (int q = 0; q < S; ++q) {
@@ -252,14 +297,19 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
       const int q = next % S;
       if (next >= S) ok = tc::mbar_wait(&empty[q], ((next / S) - 1) & 1, err);
       if (!ok) break;
-      const int j = next / nk, k = next - j * nk;
+      const int j = next / per, rem = next - j * per, sg = rem / nk, k = rem - sg * nk;
       tc::mbar_expect_tx(&full[q], SB);
-      tc::tma_load_2d(tc::smem_u32(sB + q * SB), &tma_b, k * kKC, t * ncol + j * kDxBN, &full[q]);
+      // segments: dP hi . W hi, dP lo . W hi, dP hi . W lo
+      tc::tma_load_2d(tc::smem_u32(sB + q * SB), &tma_b, (sg == 2 ? f.Kp : 0) + k * kKC, t * ncol + j * kDxBN,
+                      &full[q]);
     }
   };
   if (warp == 1 && lane == 0) {
-    tc::mbar_expect_tx(&a_full, nk * SA);
-    for (int k = 0; k < nk; ++k) tc::tma_load_2d(tc::smem_u32(sA + k * SA), &tma_a, k * kKC, m0, &a_full);
+    tc::mbar_expect_tx(&a_full, 2 * nk * SA);
+    for (int k = 0; k < nk; ++k) {
+      tc::tma_load_2d(tc::smem_u32(sA + k * SA), &tma_a, k * kKC, m0, &a_full);
+      tc::tma_load_2d(tc::smem_u32(sAlo + k * SA), &tma_alo, k * kKC, m0, &a_full);
+    }
     load_b(S);
   }
   // the row's xyz[c][m < 16]; the transposed term of neurons m < 16.  Two
@@ -284,19 +334,23 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
     if (warp == 0 && lane == 0) {
       if (j == 0) ok = tc::mbar_wait(&a_full, 0, err);
       const uint32_t idesc = tc::idesc_bf16_f32(128, nt);
-      for (int k = 0; k < nk && ok; ++k) {
-        const int i = j * nk + k, q = i % S;
+      for (int u = 0; u < per && ok; ++u) {
+        const int i = j * per + u, q = i % S, sg = u / nk, k = u - sg * nk;
         ok = tc::mbar_wait(&full[q], (i / S) & 1, err);
         if (!ok) break;
         tc::fence_after();
-        const uint32_t a0 = tc::smem_u32(sA + k * SA), b0 = tc::smem_u32(sB + q * SB);
+        const uint32_t a0 = tc::smem_u32((sg == 1 ? sAlo : sA) + k * SA), b0 = tc::smem_u32(sB + q * SB);
 #pragma unroll
         for (int ks = 0; ks < kKC / 16; ++ks)
           tc::mma_bf16(tbase, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc,
-                       (k > 0 || ks > 0) ? 1u : 0u);
+                       (u > 0 || ks > 0) ? 1u : 0u);
         tc::mma_commit(&empty[q]);
       }
       tc::mma_commit(&acc);
+    } else if (warp == 1 && lane == 0) {
+      // the rest of this chunk's B loads, each as soon as the MMA that read
+      // its stage last has completed (a chunk needs more loads than stages)
+      load_b((j + 1) * per);
     }
     __syncwarp();
     // this warpgroup's neurons of the chunk and their xyz[c][n], loaded
@@ -341,7 +395,7 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
     tc::fence_before();
     ok = __syncthreads_and(ok) != 0;  // the accumulator is read: the next chunk may overwrite it
     tc::fence_after();
-    if (warp == 1 && lane == 0) load_b((j + 1) * nk + S);
+    if (warp == 1 && lane == 0) load_b((j + 1) * per + S);
   }
   // the second warpgroup's transposed-term partials to the first (the ring
   // is free now), which completes neurons m < 16
@@ -397,19 +451,25 @@ int encode_bf16_2d(CUtensorMap* m, const __nv_bfloat16* base, int rows, int cols
   return DPGB_OK;
 }
 
-template <int BN, int S, int WG>
+template <int BN, int S, int WG, int NA>
 int launch_t(const FitGemm& g, int* err, cudaStream_t st) {
-  const size_t smem = (size_t)S * (128 + BN) * kKC * 2 + 1024;  // + alignment slack
+  const size_t smem = (size_t)S * (NA * 128 + 2 * BN) * kKC * 2 + 1024;  // + alignment slack
   static bool attr = false;
   if (!attr) {
-    DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel<BN, S, WG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel<BN, S, WG, NA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
     attr = true;
   }
-  CUtensorMap ta, tb;
+  if (g.Kp < g.K || g.Kp % kKC || (NA == 2) != (g.A_lo != nullptr))
+    return fail(DPGB_EINVAL, "fit_gemm: bad split-BF16 operands");
+  CUtensorMap ta, talo, tb;
   DPGB_TRY(encode_bf16_2d(&ta, g.A, g.row0[g.ntypes], g.K, g.lda, 128));
-  DPGB_TRY(encode_bf16_2d(&tb, g.B, g.ntypes * g.N, g.K, g.K, BN));
-  dim3 grid(g.tile0[g.ntypes], ceil_div(g.N, BN));
-  fit_gemm_kernel<BN, S, WG><<<grid, 128 * WG, smem, st>>>(ta, tb, g, err);
+  DPGB_TRY(encode_bf16_2d(&talo, g.A_lo ? g.A_lo : g.A, g.row0[g.ntypes], g.K, g.lda, 128));
+  DPGB_TRY(encode_bf16_2d(&tb, g.B, g.ntypes * g.N, 2 * g.Kp, 2 * g.Kp, BN));
+  // the column tiles of one row tile run next to each other (they read the
+  // same A rows: L2 serves the repeats)
+  dim3 grid(ceil_div(g.N, BN), g.tile0[g.ntypes]);
+  fit_gemm_kernel<BN, S, WG, NA><<<grid, 128 * WG, smem, st>>>(ta, talo, tb, g, err);
   return check_launch("fit_gemm");
 }
 
@@ -430,27 +490,33 @@ int fit_tc_eligible(const dpgb_se_a_desc& d) {
 int launch_fit_dxyz(const FitDxyz& f, int* err, cudaStream_t st) {
   if (f.tile0[f.ntypes] <= 0) return DPGB_OK;
   const int nk = (f.K + kKC - 1) / kKC;
-  const size_t smem = (size_t)nk * 128 * kKC * 2 + (size_t)kDxStages * kDxBN * kKC * 2 + 1024;
+  const size_t smem = (size_t)2 * nk * 128 * kKC * 2 + (size_t)kDxStages * kDxBN * kKC * 2 + 1024;
   if (smem > 227 * 1024) return fail(DPGB_EINVAL, "fit_dxyz: first hidden layer too wide");
+  if (f.Kp != nk * kKC || !f.A_lo) return fail(DPGB_EINVAL, "fit_dxyz: bad split-BF16 operands");
   DPGB_CUDA(cudaFuncSetAttribute(fit_dxyz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  CUtensorMap ta, tb;
+  CUtensorMap ta, talo, tb;
   DPGB_TRY(encode_bf16_2d(&ta, f.A, f.row0[f.ntypes], f.K, f.lda, 128));
-  DPGB_TRY(encode_bf16_2d(&tb, f.B, f.ntypes * f.ng * kDxM, f.K, f.K, kDxBN));
-  fit_dxyz_kernel<<<f.tile0[f.ntypes], 256, smem, st>>>(ta, tb, f, err);
+  DPGB_TRY(encode_bf16_2d(&talo, f.A_lo, f.row0[f.ntypes], f.K, f.lda, 128));
+  DPGB_TRY(encode_bf16_2d(&tb, f.B, f.ntypes * f.ng * kDxM, 2 * f.Kp, 2 * f.Kp, kDxBN));
+  fit_dxyz_kernel<<<f.tile0[f.ntypes], 256, smem, st>>>(ta, talo, tb, f, err);
   return check_launch("fit_dxyz");
 }
 
 int launch_fit_gemm(const FitGemm& g, int* err, cudaStream_t st) {
   const int mt = g.tile0[g.ntypes];
   if (mt <= 0) return DPGB_OK;
-  if (g.mode == kFitFwdLast) return launch_t<256, 3, 2>(g, err, st);  // the output layer needs whole rows
+  // stages: three when two CTAs still fit on an SM, else two
+  const bool split_a = g.A_lo != nullptr;
+  if (g.mode == kFitFwdLast)  // the output layer needs whole rows (one CTA per SM)
+    return split_a ? launch_t<256, 2, 2, 2>(g, err, st) : launch_t<256, 2, 2, 1>(g, err, st);
   // column tile: the narrower one when it spreads the tiles more evenly over
   // the SMs (two CTAs fit on an SM either way): for 240 columns, three
   // 80-wide tiles per row tile rather than a 128 + 112 pair
   const int sms = sm_count();
   auto span = [&](int bn) { return (long long)ceil_div(mt * ceil_div(g.N, bn), 2 * sms) * bn; };
-  if (g.N % 80 == 0 && span(80) < span(128)) return launch_t<80, 3, 2>(g, err, st);
-  return launch_t<128, 3, 2>(g, err, st);
+  if (g.N % 80 == 0 && span(80) < span(128))
+    return split_a ? launch_t<80, 2, 2, 2>(g, err, st) : launch_t<80, 3, 2, 1>(g, err, st);
+  return split_a ? launch_t<128, 2, 2, 2>(g, err, st) : launch_t<128, 2, 2, 1>(g, err, st);
 }
 
 }  // namespace dpgb

@@ -201,9 +201,10 @@ __device__ __forceinline__ void wrap_point(const double* in, const CellGeom& g, 
 }
 
 __global__ void normalize_kernel(double* __restrict__ out, const double* __restrict__ in, int n,
-                                 CellGeom g) {
+                                 CellGeom g, int* __restrict__ status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  flag_nonfinite(in + 3 * i, i, status);
   wrap_point(in + 3 * i, g, out + 3 * i);
 }
 
@@ -1306,9 +1307,11 @@ format_ext_kernel(int* __restrict__ nlist, const double* __restrict__ coord, con
 // ---- many frames in one launch (FrameTab) ---------------------------------
 
 __global__ void normalize_batch_kernel(double* __restrict__ out, int* __restrict__ cell_of, int* __restrict__ counts,
-                                       const double* __restrict__ in, int natoms, FrameTab ft) {
+                                       const double* __restrict__ in, int natoms, FrameTab ft,
+                                       int* __restrict__ status) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= natoms) return;
+  flag_nonfinite(in + 3 * a, a, status);
   const int fr = frame_of(ft.atom_off, ft.nframes, a);
   const CellGeom& g = ft.geom[fr];
   const double x = in[3 * a], y = in[3 * a + 1], z = in[3 * a + 2];
@@ -1470,9 +1473,10 @@ __global__ void skin_check_kernel(int* __restrict__ gate, const double* __restri
 // reuse evaluation: the caller's coordinates plus the build's wrap offset
 __global__ void skin_coords_kernel(double* __restrict__ out, float4* __restrict__ outf, double* __restrict__ off,
                                    double* __restrict__ ref, const double* __restrict__ in, int n, CellGeom g,
-                                   const int* __restrict__ gate) {
+                                   const int* __restrict__ gate, int* __restrict__ status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  flag_nonfinite(in + 3 * i, i, status);
   double o[3];
   if (gate[0]) {
     wrap_point(in + 3 * i, g, o);
@@ -1619,7 +1623,8 @@ int launch_nlist_batch(int* nlist, double* coord_out, const double* coord_in, co
   int* cursor = offsets + (ncells + 1);
   DPGB_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (ncells + 1), st));
   DPGB_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * (ncells + 1), st));
-  normalize_batch_kernel<<<ceil_div(natoms, 256), 256, 0, st>>>(coord_out, cell_of, counts, coord_in, natoms, ft);
+  normalize_batch_kernel<<<ceil_div(natoms, 256), 256, 0, st>>>(coord_out, cell_of, counts, coord_in, natoms, ft,
+                                                                 status);
   DPGB_TRY(check_launch("normalize_batch"));
   scan_kernel<<<1, 1024, 0, st>>>(offsets, counts, ncells, nullptr);
   DPGB_TRY(check_launch("cell_scan_batch"));
@@ -1641,9 +1646,9 @@ int launch_format_ext(int* nlist, const double* coord_ext, const int* atype_ext,
   return check_launch("format_ext");
 }
 
-int launch_normalize(double* out, const double* in, int n, const CellGeom& g, cudaStream_t st) {
+int launch_normalize(double* out, const double* in, int n, const CellGeom& g, cudaStream_t st, int* status) {
   if (n <= 0) return DPGB_OK;
-  normalize_kernel<<<ceil_div(n, 256), 256, 0, st>>>(out, in, n, g);
+  normalize_kernel<<<ceil_div(n, 256), 256, 0, st>>>(out, in, n, g, status);
   return check_launch("normalize_coord");
 }
 
@@ -1655,9 +1660,9 @@ int launch_skin_check(int* gate, const double* coord, const double* ref, int n, 
 }
 
 int launch_skin_coords(double* out, float4* outf, double* off, double* ref, const double* in, int n,
-                       const CellGeom& g, const int* gate, cudaStream_t st) {
+                       const CellGeom& g, const int* gate, cudaStream_t st, int* status) {
   if (n <= 0) return DPGB_OK;
-  skin_coords_kernel<<<ceil_div(n, 256), 256, 0, st>>>(out, outf, off, ref, in, n, g, gate);
+  skin_coords_kernel<<<ceil_div(n, 256), 256, 0, st>>>(out, outf, off, ref, in, n, g, gate, status);
   return check_launch("skin_coords");
 }
 

@@ -59,7 +59,9 @@ int periodic_geom(const double* box, double rcut, int nshift, const int* shift_i
 int open_geom(const double* coord_host, int n, double rcut, CellGeom& g);
 void shift_vectors(const CellGeom& g, const int* shift_idx, int nshift, std::vector<double>& out);
 
-int launch_normalize(double* out, const double* in, int n, const CellGeom& g, cudaStream_t st);
+// status (may be NULL): flags non-finite input coordinates (kStatusNonFinite)
+int launch_normalize(double* out, const double* in, int n, const CellGeom& g, cudaStream_t st,
+                     int* status = nullptr);
 int launch_extend(double* cext, int* text, int* mapping, const double* coord, const int* atype,
                   int nloc, int nshift, const double* svec_dev, cudaStream_t st);
 size_t nlist_pt_workspace(int nloc, const CellGeom& g);
@@ -121,7 +123,7 @@ int launch_skin_check(int* gate, const double* coord, const double* ref, int n, 
 // build: out = wrapped coordinates, off = out - in, ref = in; reuse: out =
 // in + off; outf = FP32 copy of out (prefilter of the selection)
 int launch_skin_coords(double* out, float4* outf, double* off, double* ref, const double* in, int n,
-                       const CellGeom& g, const int* gate, cudaStream_t st);
+                       const CellGeom& g, const int* gate, cudaStream_t st, int* status = nullptr);
 // the list at rcut from the candidate rows [nloc, ncand] (extended indices
 // s * nloc + j, -1 padding): the same ranking and per-type placement as a
 // fresh build on the same coordinates.  margin: FP32 prefilter radius above

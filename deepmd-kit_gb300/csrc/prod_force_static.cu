@@ -13,12 +13,18 @@
 //  * it is a file-scope __device__ array of kScratchBytes (11 MiB), present
 //    on every GPU that loads the library until the process exits;
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current) and caches it; make that
-//    first call before any stream capture;
+//    cudaGetSymbolAddress (with that device current) and caches it together
+//    with the device's current CUDA context; a call that finds another
+//    context there (the primary context was reset, or the caller made its
+//    own) looks the address up again.  Make the first call on a device, and
+//    the first after a context change, before any stream capture;
 //  * every call reuses the same array and it keeps the last call's contents;
 //    the call clears what must start at zero (counters, status) itself;
 //  * two calls whose kernels overlap on the GPU (different streams, or
 //    different host threads) race on the array: serialise them.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <mutex>
 
 #include "nlist.cuh"
@@ -41,19 +47,39 @@ static __device__ __align__(256) unsigned char g_prod_force_scratch[kScratchByte
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 unsigned char* g_scratch_ptr[kMaxDevices] = {};
+CUcontext g_scratch_ctx[kMaxDevices] = {};
 
-// device address of the scratch array on the current device (looked up once)
+// the calling thread's current CUDA context (the driver's cuCtxGetCurrent,
+// taken through the runtime); null when unavailable
+CUcontext current_context() {
+  static PFN_cuCtxGetCurrent_v4000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+  }();
+  CUcontext c = nullptr;
+  if (fn && fn(&c) != CUDA_SUCCESS) c = nullptr;
+  return c;
+}
+
+// device address of the scratch array on the current device: looked up once
+// per device and context
 int scratch_address(unsigned char** out) {
   int dev = 0;
   DPGB_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(DPGB_EINVAL, "device index beyond the supported range");
+  const CUcontext ctx = current_context();  // null before the runtime made one current
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch_ptr[dev]) {
+  if (!g_scratch_ptr[dev] || !ctx || ctx != g_scratch_ctx[dev]) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_prod_force_scratch);
     if (e != cudaSuccess)
       return fail(DPGB_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
     g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+    g_scratch_ctx[dev] = current_context();  // the lookup made the device's context current
   }
   *out = g_scratch_ptr[dev];
   return DPGB_OK;

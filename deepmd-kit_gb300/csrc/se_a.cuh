@@ -232,11 +232,14 @@ size_t desc_bwd_smem(const DescParams<T>& p, const EmbParams<T>& e);
 // Compressed nets in the mixed form (tab_fused.cu): the table lookup fused
 // with the env matrix and contraction (forward: xyz in row order, D at the
 // type-sorted position, BF16 when d_bf16) and the pair-gradient backward.
+// Work: the chunks of type-sorted rows (one centre type each); D is
+// written at the type-sorted position.
+struct WorkChunk;
 int tab_fused_eligible(int ng, int axis);
-int launch_tab_fwd(const DescParams<float>& p, const EmbParams<float>& e, const int* sorted_rows, int nsorted,
-                   float* xyz, void* D, int d_bf16, cudaStream_t st);
-int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const int* sorted_rows, int nsorted,
-                   const float* dxyz, float* gpair, double* vir_row, cudaStream_t st);
+int launch_tab_fwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
+                   const int* sorted_rows, float* xyz, void* D, int d_bf16, cudaStream_t st);
+int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
+                   const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, cudaStream_t st);
 
 // fitting of the rows [row0, row0+nrow) of one type
 template <typename T>

@@ -3,26 +3,16 @@
 // fused with the environment matrix, the G^T R~ contraction, D, and on the
 // way back the pair gradients and per-atom virial — on the CUDA cores in FP32
 // (the table is a per-interval quintic: no GEMM to give the tensor cores).
-//
-// One warp per atom (rows in type-sorted order, so the warps of a CTA share
-// nets and table rows stay in L1).  Lane l owns neurons l, l+32, l+64, l+96:
-// a pair's table row (6 coefficients per neuron) is read as three float2
-// loads per neuron, contiguous across the warp.  The warp evaluates the
-// environment of 32 slots at once (one per lane) and then walks the kept
-// slots, broadcasting each slot's R~ and table interval by shuffles.
-// Backward: per pair dG_n = R~ . dxyz[:, n], dR~ = sum_n G_n dxyz[:, n] plus
-// ds = sum_n dG_n G'_n, reduced across the warp; the slot's owner lane turns
-// dR~ into the pair gradient and the pair virial.  Sums run in a fixed order:
-// results are bitwise reproducible.
+// The work decomposition is described above the kernels.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
+#include "emb_tc.cuh"
 #include "se_a.cuh"
 
 namespace dpgb {
 namespace {
-
-constexpr int kTabWarps = 8;
-constexpr int kTabJ = 4;  // neurons per lane (ng <= 128)
 
 struct SlotEnv {
   int nb;        // extended index, -1 padding
@@ -104,190 +94,381 @@ __device__ __forceinline__ void slot_deriv(const float d[3], float rmin, float r
       der[3 + 3 * c + k] = (2.f * d[c] * d[k] * inr4 - (c == k ? inr2 : 0.f)) * sw - v[c] * dsw * d[k] * inr;
 }
 
-__device__ __forceinline__ void coeffs(const float* __restrict__ rowc, float a[6]) {
-  const float2* q = reinterpret_cast<const float2*>(rowc);
-  const float2 x0 = __ldg(q), x1 = __ldg(q + 1), x2 = __ldg(q + 2);
-  a[0] = x0.x;
-  a[1] = x0.y;
-  a[2] = x1.x;
-  a[3] = x1.y;
-  a[4] = x2.x;
-  a[5] = x2.y;
+// ---------------------------------------------------------------------------
+// Both kernels run one CTA per SM (kFwdWarps / kBwdWarps warps) over the work chunks
+// (contiguous type-sorted atoms of one centre type), section by section:
+// for a section the CTA stages rows [0, rows) of that section's table in
+// shared memory (the intervals of all but the closest neighbours; a pair
+// in a row beyond them reads the table from global memory), then each warp
+// takes one atom at a time.  Lane l owns neurons l, l + 32, l + 64, l + 96,
+// so one pair's coefficients are one contiguous run of the row; a pair in
+// the same interval as the previous one (neighbours come sorted by
+// distance) reuses the coefficients already in registers.  The lanes
+// compute the environment of 32 slots at once and park it in a per-warp
+// shared-memory slot buffer, from which every lane reads each kept pair.
+// Sections after the first add to the atom's xyz (forward) and virial
+// (backward) where the previous section left them (the same CTA, after a
+// barrier).  Sums run in a fixed order: results are bitwise reproducible.
+constexpr int kFwdWarps = 16;
+constexpr int kBwdWarps = 16;
+constexpr int kTabJ = 4;       // neurons per lane (ng <= 128)
+
+struct SlotBuf {  // one kept slot, as the lanes read it (32 bytes)
+  float4 rn;
+  float xx, delta;
+  int idx, pad;
+};
+
+// shared memory: the staged rows, then 32 slot buffers per warp
+__host__ __device__ inline size_t tab_table_bytes(int rows, int ng) {
+  return ((size_t)rows * 6 * ng * sizeof(float) + 15) / 16 * 16;
 }
 
-__global__ void __launch_bounds__(kTabWarps * 32, 4)  // 4 CTAs (32 warps) per SM: the table reads want the warps
-tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ sorted_rows, int nsorted,
-               float* __restrict__ xyz, void* __restrict__ Dout, int d_bf16) {
-  const int lane = threadIdx.x & 31;
-  const int r = blockIdx.x * kTabWarps + (threadIdx.x >> 5);
-  if (r >= nsorted) return;
-  const int row = sorted_rows[r];
-  const int ti = p.atype[row - p.nloc_div.div(row) * p.nloc];
+// stage rows [0, rows) of a net's table (6 ng floats a row; the table
+// starts 8-byte aligned)
+__device__ __forceinline__ void stage_rows(float* dst, const float* __restrict__ src, int rows, int ng) {
+  const int n2 = rows * 3 * ng;  // float2 count
+  const float2* s2 = reinterpret_cast<const float2*>(src);
+  float2* d2 = reinterpret_cast<float2*>(dst);
+  for (int q = threadIdx.x; q < n2; q += blockDim.x) d2[q] = __ldg(s2 + q);
+}
+
+// the same with a row stride of row_stride floats (even; rows of 6 ng floats)
+__device__ __forceinline__ void stage_rows_strided(float* dst, const float* __restrict__ src, int rows, int ng,
+                                                   int row_stride) {
+  const int per = 3 * ng;  // float2 per row
+  const float2* s2 = reinterpret_cast<const float2*>(src);
+  float2* d2 = reinterpret_cast<float2*>(dst);
+  const int s2stride = row_stride / 2;
+  for (int q = threadIdx.x; q < rows * per; q += blockDim.x) {
+    const int rr = q / per, k = q - rr * per;
+    d2[(size_t)rr * s2stride + k] = __ldg(s2 + q);
+  }
+}
+
+// the lane's coefficients of interval ix: staged rows from shared memory,
+// the others from global memory
+// (ix is the same in every lane: the branch does not diverge)
+__device__ __forceinline__ void load_coeffs(const float* s_tab, const float* __restrict__ tab, int rows, int ix,
+                                            int ng, int lane, float (&a)[kTabJ][6]) {
+  auto put = [&](int j, float2 x0, float2 x1, float2 x2) {
+    a[j][0] = x0.x;
+    a[j][1] = x0.y;
+    a[j][2] = x1.x;
+    a[j][3] = x1.y;
+    a[j][4] = x2.x;
+    a[j][5] = x2.y;
+  };
+  if (ix < rows) {
+    const float2* q = reinterpret_cast<const float2*>(s_tab + (size_t)ix * 6 * ng + 6 * lane);
+#pragma unroll
+    for (int j = 0; j < kTabJ; ++j)
+      if (lane + 32 * j < ng) put(j, q[96 * j], q[96 * j + 1], q[96 * j + 2]);  // 32 neurons = 96 float2
+  } else {
+    const float2* q = reinterpret_cast<const float2*>(tab + (size_t)ix * 6 * ng + 6 * lane);
+#pragma unroll
+    for (int j = 0; j < kTabJ; ++j)
+      if (lane + 32 * j < ng) put(j, __ldg(q + 96 * j), __ldg(q + 96 * j + 1), __ldg(q + 96 * j + 2));
+  }
+}
+
+__global__ void __launch_bounds__(kFwdWarps * 32, 1)
+tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restrict__ chunks, int nchunks,
+               const int* __restrict__ sorted_rows, int rows_cap, float* __restrict__ xyz, void* __restrict__ Dout,
+               int d_bf16) {
+  extern __shared__ float4 smem4[];
   const int ng = p.ng, M = p.axis;
-  float acc[4][kTabJ];
+  float* s_tab = reinterpret_cast<float*>(smem4);
+  SlotBuf* s_slot = reinterpret_cast<SlotBuf*>(reinterpret_cast<unsigned char*>(smem4) + tab_table_bytes(rows_cap, ng));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  SlotBuf* my = s_slot + warp * 32;
+  const float inv = 1.f / (float)p.nnei;
+  const int dim = ng * M;
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const WorkChunk ch = chunks[c];
+    const int ti = ch.ti;
+    for (int sec = 0; sec < p.ntypes; ++sec) {
+      const int net = p.type_one_side ? sec : sec * p.ntypes + ti;
+      const TabMeta<float> tm = e.meta[net];
+      const float* tab = e.table + tm.offset;
+      const int rows = min(rows_cap, tm.hi_idx + 1);
+      __syncthreads();  // the previous section's rows are no longer read
+      stage_rows(s_tab, tab, rows, ng);
+      __syncthreads();
+      const bool last = sec == p.ntypes - 1;
+      for (int r = ch.row0 + warp; r < ch.row1; r += kFwdWarps) {
+        const int row = sorted_rows[r];
+        float* xr = xyz + (size_t)row * 4 * ng;
+        float acc[4][kTabJ];
 #pragma unroll
-  for (int c = 0; c < 4; ++c)
+        for (int cc = 0; cc < 4; ++cc)
 #pragma unroll
-    for (int j = 0; j < kTabJ; ++j) acc[c][j] = 0.f;
-  for (int sec = 0; sec < p.ntypes; ++sec) {
-    const int net = p.type_one_side ? sec : sec * p.ntypes + ti;
-    const TabMeta<float> tm = e.meta[net];
-    const float* tab = e.table + tm.offset;
-    for (int base = p.sec[sec]; base < p.sec[sec + 1]; base += 32) {
-      const int slot = base + lane;
-      SlotEnv s;
-      s.active = 0;
-      if (slot < p.sec[sec + 1]) {
-        slot_env(p, row, ti, slot, s);
-        table_locate(tm, s.rn[0], s.idx, s.xx, s.delta);
-      }
-      unsigned m = __ballot_sync(0xffffffffu, s.active);
-      while (m) {
-        const int src = __ffs(m) - 1;
-        m &= m - 1;
-        float rr[4];
+          for (int j = 0; j < kTabJ; ++j) {
+            const int n = lane + 32 * j;
+            acc[cc][j] = (sec > 0 && n < ng) ? xr[cc * ng + n] : 0.f;
+          }
+        int cur = -1;
+        float a[kTabJ][6] = {};  // lanes past ng keep zeros (a zero G adds nothing to the sums)
+        for (int base = p.sec[sec]; base < p.sec[sec + 1]; base += 32) {
+          const int slot = base + lane;
+          SlotEnv s;
+          s.active = 0;
+          if (slot < p.sec[sec + 1]) {
+            slot_env(p, row, ti, slot, s);
+            table_locate(tm, s.rn[0], s.idx, s.xx, s.delta);
+          }
+          unsigned m = __ballot_sync(0xffffffffu, s.active);
+          if (!m) continue;
+          if (s.active) {
+            SlotBuf b;
+            b.rn = make_float4(s.rn[0], s.rn[1], s.rn[2], s.rn[3]);
+            b.xx = s.xx;
+            b.delta = s.delta;
+            b.idx = s.idx;
+            b.pad = 0;
+            my[lane] = b;
+          }
+          __syncwarp();
+          while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const SlotBuf b = my[src];
+            if (b.idx != cur) {
+              cur = b.idx;
+              load_coeffs(s_tab, tab, rows, cur, ng, lane, a);
+            }
+            float G[kTabJ];
+            if (b.delta == 0.f) {  // inside the table (the same branch in every lane)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) rr[c] = __shfl_sync(0xffffffffu, s.rn[c], src);
-        const int ix = __shfl_sync(0xffffffffu, s.idx, src);
-        const float xx = __shfl_sync(0xffffffffu, s.xx, src);
-        const float dl = __shfl_sync(0xffffffffu, s.delta, src);
-        const float* rowc = tab + (size_t)ix * 6 * ng;
+              for (int j = 0; j < kTabJ; ++j)
+                G[j] = fmaf(fmaf(fmaf(fmaf(fmaf(a[j][5], b.xx, a[j][4]), b.xx, a[j][3]), b.xx, a[j][2]), b.xx,
+                                 a[j][1]),
+                            b.xx, a[j][0]);
+            } else {  // linear extension past the ends of the table
+#pragma unroll
+              for (int j = 0; j < kTabJ; ++j) {
+                float Gp;
+                table_poly(a[j], b.xx, b.delta, G[j], Gp);
+              }
+            }
+#pragma unroll
+            for (int j = 0; j < kTabJ; ++j) {
+              acc[0][j] = fmaf(b.rn.x, G[j], acc[0][j]);
+              acc[1][j] = fmaf(b.rn.y, G[j], acc[1][j]);
+              acc[2][j] = fmaf(b.rn.z, G[j], acc[2][j]);
+              acc[3][j] = fmaf(b.rn.w, G[j], acc[3][j]);
+            }
+          }
+          __syncwarp();  // the slot buffer is refilled by the next 32 slots
+        }
+        if (!last) {
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc)
+#pragma unroll
+            for (int j = 0; j < kTabJ; ++j) {
+              const int n = lane + 32 * j;
+              if (n < ng) xr[cc * ng + n] = acc[cc][j];
+            }
+          continue;
+        }
 #pragma unroll
         for (int j = 0; j < kTabJ; ++j) {
           const int n = lane + 32 * j;
-          if (n < ng) {
-            float a[6], G, Gp;
-            coeffs(rowc + 6 * n, a);
-            table_poly(a, xx, dl, G, Gp);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) acc[c][j] = fmaf(rr[c], G, acc[c][j]);
+          for (int cc = 0; cc < 4; ++cc) {
+            acc[cc][j] *= inv;
+            if (n < ng) xr[cc * ng + n] = acc[cc][j];
           }
         }
-      }
-    }
-  }
-  const float inv = 1.f / (float)p.nnei;
-  float* xr = xyz + (size_t)row * 4 * ng;
+        // D[n][m] = sum_c X[c][n] X[c][m], m < M <= 32: X[c][m] sits in lane m
+        if (M == 16) {  // the lane's row of D (16 values) as two or four 16-byte stores
 #pragma unroll
-  for (int j = 0; j < kTabJ; ++j) {
-    const int n = lane + 32 * j;
+          for (int j = 0; j < kTabJ; ++j) {
+            const int n = lane + 32 * j;
+            float o[16];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      acc[c][j] *= inv;
-      if (n < ng) xr[c * ng + n] = acc[c][j];
-    }
-  }
-  // D[n][m] = sum_c X[c][n] X[c][m], m < M <= 32: X[c][m] sits in lane m
-  const int dim = ng * M;
+            for (int mm = 0; mm < 16; ++mm) {
+              float sacc = 0.f;
 #pragma unroll
-  for (int j = 0; j < kTabJ; ++j) {
-    const int n = lane + 32 * j;
-    for (int m0 = 0; m0 < M; m0 += 8) {
-      float o[8];
+              for (int cc = 0; cc < 4; ++cc) sacc = fmaf(acc[cc][j], __shfl_sync(0xffffffffu, acc[cc][0], mm), sacc);
+              o[mm] = sacc;
+            }
+            if (n >= ng) continue;
+            const size_t at = (size_t)r * dim + (size_t)n * 16;
+            if (d_bf16) {
+              __nv_bfloat162 h[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int m = m0 + q;
-        float s = 0.f;
+              for (int i = 0; i < 8; ++i) h[i] = __floats2bfloat162_rn(o[2 * i], o[2 * i + 1]);
+              uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(Dout) + at);
+              dst[0] = *reinterpret_cast<const uint4*>(&h[0]);
+              dst[1] = *reinterpret_cast<const uint4*>(&h[4]);
+            } else {
+              float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(Dout) + at);
 #pragma unroll
-        for (int c = 0; c < 4; ++c) s = fmaf(acc[c][j], __shfl_sync(0xffffffffu, acc[c][0], m & 31), s);
-        o[q] = s;
-      }
-      if (n < ng) {
-        for (int q = 0; q < 8 && m0 + q < M; ++q) {
-          const size_t at = (size_t)r * dim + (size_t)n * M + m0 + q;
-          if (d_bf16)
-            reinterpret_cast<__nv_bfloat16*>(Dout)[at] = __float2bfloat16_rn(o[q]);
-          else
-            reinterpret_cast<float*>(Dout)[at] = o[q];
+              for (int i = 0; i < 4; ++i) dst[i] = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
+            }
+          }
+          continue;
+        }
+#pragma unroll
+        for (int j = 0; j < kTabJ; ++j) {
+          const int n = lane + 32 * j;
+          for (int m0 = 0; m0 < M; m0 += 8) {
+            float o[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int mm = m0 + q;
+              float sacc = 0.f;
+#pragma unroll
+              for (int cc = 0; cc < 4; ++cc)
+                sacc = fmaf(acc[cc][j], __shfl_sync(0xffffffffu, acc[cc][0], mm & 31), sacc);
+              o[q] = sacc;
+            }
+            if (n < ng) {
+              for (int q = 0; q < 8 && m0 + q < M; ++q) {
+                const size_t at = (size_t)r * dim + (size_t)n * M + m0 + q;
+                if (d_bf16)
+                  reinterpret_cast<__nv_bfloat16*>(Dout)[at] = __float2bfloat16_rn(o[q]);
+                else
+                  reinterpret_cast<float*>(Dout)[at] = o[q];
+              }
+            }
+          }
         }
       }
     }
   }
 }
 
-__global__ void __launch_bounds__(kTabWarps * 32, 3)  // 3 CTAs (24 warps) per SM
-tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ sorted_rows, int nsorted,
-               const float* __restrict__ dxyz, float* __restrict__ gpair, double* __restrict__ vir_row) {
-  const int lane = threadIdx.x & 31;
-  const int r = blockIdx.x * kTabWarps + (threadIdx.x >> 5);
-  if (r >= nsorted) return;
-  const int row = sorted_rows[r];
-  const int ti = p.atype[row - p.nloc_div.div(row) * p.nloc];
+// Backward: one lane per real pair.  The warp first lists the slots of the
+// atom's section that hold a neighbour (in a per-warp shared list; padding
+// slots get a zero gradient), then takes them 32 at a time: each lane forms
+// its pair's environment and walks all neurons of its interval's row,
+// G and G' in one Horner pass, dR~[c] += G dX[c] and P[c] += G' dX[c]
+// (ds = sum_c R~[c] P[c]) with dX[n] broadcast from the warp's copy of the
+// atom's dE/dxyz.  Everything is summed in the lane: no cross-lane
+// reductions.  Rows are staged with an odd float2 stride, so 16 lanes on 16
+// different rows read 16 different bank pairs.
+__global__ void __launch_bounds__(kBwdWarps * 32, 1)
+tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restrict__ chunks, int nchunks,
+               const int* __restrict__ sorted_rows, int rows_cap, int row_stride, const float* __restrict__ dxyz,
+               float* __restrict__ gpair, double* __restrict__ vir_row) {
+  extern __shared__ float4 smem4[];
   const int ng = p.ng;
+  float* s_tab = reinterpret_cast<float*>(smem4);
+  unsigned char* tail = reinterpret_cast<unsigned char*>(smem4) + (((size_t)rows_cap * row_stride * 4 + 15) / 16 * 16);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float4* s_dx = reinterpret_cast<float4*>(tail) + (size_t)warp * ng;                    // [warp][ng]
+  int* s_list = reinterpret_cast<int*>(reinterpret_cast<float4*>(tail) + (size_t)kBwdWarps * ng) +
+                (size_t)warp * p.nnei;                                                     // [warp][nnei]
   const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
-  // the atom's dE/dxyz, one float4 (four components) per neuron, shared by
-  // the warp's lanes (each lane walks all neurons of its own pair)
-  __shared__ float4 s_dx[kTabWarps][32 * kTabJ];
-  float4* sdx = s_dx[threadIdx.x >> 5];
-  const float* dr = dxyz + (size_t)row * 4 * ng;
-  for (int n = lane; n < ng; n += 32) sdx[n] = reinterpret_cast<const float4*>(dr)[n];  // dxyz is [row][ng][4]
-  __syncwarp();
-  float vir_hi[9], vir_lo[9];  // compensated FP32 sums
-#pragma unroll
-  for (int k = 0; k < 9; ++k) vir_hi[k] = vir_lo[k] = 0.f;
-  float* gp_row = gpair + (size_t)row * p.nnei * 3;
-  for (int sec = 0; sec < p.ntypes; ++sec) {
-    const int net = p.type_one_side ? sec : sec * p.ntypes + ti;
-    const TabMeta<float> tm = e.meta[net];
-    const float* tab = e.table + tm.offset;
-    for (int base = p.sec[sec]; base < p.sec[sec + 1]; base += 32) {
-      const int slot = base + lane;
-      SlotEnv s;
-      s.active = 0;
-      s.nb = -1;
-      const bool have = slot < p.sec[sec + 1];
-      if (have) {
-        slot_env(p, row, ti, slot, s);
-        table_locate(tm, s.rn[0], s.idx, s.xx, s.delta);
-      }
-      const bool real = have && s.nb >= 0 && s.active;  // only real kept pairs carry a gradient
-      // dR~ of this lane's pair: sum over neurons of G dX (direct term) and
-      // of (R~ . dX) G' (through s = R~[0]), in neuron order
-      float mine[4] = {0.f, 0.f, 0.f, 0.f};
-      if (real) {
-        const float* rowc = tab + (size_t)s.idx * 6 * ng;
-        float ds = 0.f;
-        for (int n = 0; n < ng; ++n) {
-          float a[6], G, Gp;
-          coeffs(rowc + 6 * n, a);
-          table_poly(a, s.xx, s.delta, G, Gp);
-          const float4 d = sdx[n];
-          const float dG = fmaf(s.rn[3], d.w, fmaf(s.rn[2], d.z, fmaf(s.rn[1], d.y, s.rn[0] * d.x)));
-          mine[0] = fmaf(G, d.x, mine[0]);
-          mine[1] = fmaf(G, d.y, mine[1]);
-          mine[2] = fmaf(G, d.z, mine[2]);
-          mine[3] = fmaf(G, d.w, mine[3]);
-          ds = fmaf(dG, Gp, ds);
-        }
-        mine[0] += ds;
-      }
-      if (have) {
-        float g[3] = {0.f, 0.f, 0.f};
-        if (real) {
-          float der[12];
-          slot_deriv(s.d, rmin, rmax, der);
-          const float* sdi = p.dstd_inv + ((size_t)ti * p.nnei + slot) * 4;
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const float w = mine[c] * sdi[c];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) g[k] -= w * der[3 * c + k];
+  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const WorkChunk ch = chunks[c];
+    const int ti = ch.ti;
+    for (int sec = 0; sec < p.ntypes; ++sec) {
+      const int net = p.type_one_side ? sec : sec * p.ntypes + ti;
+      const TabMeta<float> tm = e.meta[net];
+      const float* tab = e.table + tm.offset;
+      const int rows = min(rows_cap, tm.hi_idx + 1);
+      __syncthreads();
+      stage_rows_strided(s_tab, tab, rows, ng, row_stride);
+      __syncthreads();
+      for (int r = ch.row0 + warp; r < ch.row1; r += kBwdWarps) {
+        const int row = sorted_rows[r];
+        const int* nl = p.nlist + (size_t)row * p.nnei;
+        float* gp_row = gpair + (size_t)row * p.nnei * 3;
+        // the atom's dE/dxyz (dxyz is [row][ng][4]) and the section's real slots
+        for (int n = lane; n < ng; n += 32) s_dx[n] = reinterpret_cast<const float4*>(dxyz + (size_t)row * 4 * ng)[n];
+        int nreal = 0;
+        for (int base = p.sec[sec]; base < p.sec[sec + 1]; base += 32) {
+          const int slot = base + lane;
+          const bool have = slot < p.sec[sec + 1];
+          const bool real = have && nl[slot] >= 0;
+          const unsigned m = __ballot_sync(0xffffffffu, real);
+          if (real) s_list[nreal + __popc(m & ((1u << lane) - 1u))] = slot;
+          if (have && !real) {
+            gp_row[3 * slot] = 0.f;
+            gp_row[3 * slot + 1] = 0.f;
+            gp_row[3 * slot + 2] = 0.f;
           }
-#pragma unroll
-          for (int k = 0; k < 3; ++k)
-#pragma unroll
-            for (int l = 0; l < 3; ++l) comp_add(vir_hi[3 * k + l], vir_lo[3 * k + l], -g[k] * s.d[l]);
+          nreal += __popc(m);
         }
-        gp_row[3 * slot] = g[0];
-        gp_row[3 * slot + 1] = g[1];
-        gp_row[3 * slot + 2] = g[2];
+        __syncwarp();
+        float vir_hi[9], vir_lo[9];  // compensated FP32 sums of the lane's pairs
+#pragma unroll
+        for (int k = 0; k < 9; ++k) vir_hi[k] = vir_lo[k] = 0.f;
+        for (int q0 = 0; q0 < nreal; q0 += 32) {
+          const bool mine = q0 + lane < nreal;
+          const int slot = mine ? s_list[q0 + lane] : p.sec[sec];
+          SlotEnv s;
+          s.active = 0;
+          if (mine) {
+            slot_env(p, row, ti, slot, s);
+            table_locate(tm, s.rn[0], s.idx, s.xx, s.delta);
+          }
+          const bool act = mine && s.active;  // excluded type pairs carry no gradient
+          float dR[4] = {0.f, 0.f, 0.f, 0.f}, Pc[4] = {0.f, 0.f, 0.f, 0.f};
+          if (act) {
+            const float* rowc = s.idx < rows ? s_tab + (size_t)s.idx * row_stride : tab + (size_t)s.idx * 6 * ng;
+            const float xx = s.xx, dl = s.delta;
+            for (int n = 0; n < ng; ++n) {
+              const float2* q = reinterpret_cast<const float2*>(rowc + 6 * n);
+              const float2 x0 = q[0], x1 = q[1], x2 = q[2];
+              const float4 d = s_dx[n];
+              // value and derivative of the quintic in one Horner pass
+              float G = fmaf(x2.y, xx, x2.x), Gp = x2.y;
+              Gp = fmaf(Gp, xx, G);
+              G = fmaf(G, xx, x1.y);
+              Gp = fmaf(Gp, xx, G);
+              G = fmaf(G, xx, x1.x);
+              Gp = fmaf(Gp, xx, G);
+              G = fmaf(G, xx, x0.y);
+              Gp = fmaf(Gp, xx, G);
+              G = fmaf(G, xx, x0.x);
+              G = fmaf(Gp, dl, G);  // linear extension past the table ends (dl 0 inside)
+              dR[0] = fmaf(G, d.x, dR[0]);
+              dR[1] = fmaf(G, d.y, dR[1]);
+              dR[2] = fmaf(G, d.z, dR[2]);
+              dR[3] = fmaf(G, d.w, dR[3]);
+              Pc[0] = fmaf(Gp, d.x, Pc[0]);
+              Pc[1] = fmaf(Gp, d.y, Pc[1]);
+              Pc[2] = fmaf(Gp, d.z, Pc[2]);
+              Pc[3] = fmaf(Gp, d.w, Pc[3]);
+            }
+          }
+          if (mine) {
+            float g[3] = {0.f, 0.f, 0.f};
+            if (act) {
+              // dR~ (+ ds through s = R~[0]) -> the pair gradient and virial
+              const float ds = s.rn[0] * Pc[0] + s.rn[1] * Pc[1] + s.rn[2] * Pc[2] + s.rn[3] * Pc[3];
+              dR[0] += ds;
+              float der[12];
+              slot_deriv(s.d, rmin, rmax, der);
+              const float* sdi = p.dstd_inv + ((size_t)ti * p.nnei + slot) * 4;
+#pragma unroll
+              for (int cc = 0; cc < 4; ++cc) {
+                const float w = dR[cc] * sdi[cc];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) g[k] -= w * der[3 * cc + k];
+              }
+#pragma unroll
+              for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int l = 0; l < 3; ++l) comp_add(vir_hi[3 * k + l], vir_lo[3 * k + l], -g[k] * s.d[l]);
+            }
+            gp_row[3 * slot] = g[0];
+            gp_row[3 * slot + 1] = g[1];
+            gp_row[3 * slot + 2] = g[2];
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          const double vv = warp_comp_sum(vir_hi[k], vir_lo[k]);
+          if (lane == 0) vir_row[(size_t)row * 9 + k] += vv;  // zeroed before the launch
+        }
+        __syncwarp();  // the warp's dX copy and slot list are reused by its next atom
       }
     }
-  }
-#pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    const double v = warp_comp_sum(vir_hi[k], vir_lo[k]);
-    if (lane == 0) vir_row[(size_t)row * 9 + k] = v;
   }
 }
 
@@ -295,18 +476,51 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const int* __restrict__ 
 
 int tab_fused_eligible(int ng, int axis) { return ng >= 1 && ng <= 32 * kTabJ && axis >= 1 && axis <= 32; }
 
-int launch_tab_fwd(const DescParams<float>& p, const EmbParams<float>& e, const int* sorted_rows, int nsorted,
-                   float* xyz, void* D, int d_bf16, cudaStream_t st) {
-  if (nsorted <= 0) return DPGB_OK;
-  tab_fwd_kernel<<<ceil_div(nsorted, kTabWarps), kTabWarps * 32, 0, st>>>(p, e, sorted_rows, nsorted, xyz, D, d_bf16);
+namespace {
+
+// staged rows: as many as fit next to the slot buffers in the opt-in maximum
+int tab_rows_cap(int ng, int warps, size_t* smem) {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t slot = (size_t)warps * 32 * sizeof(SlotBuf);
+  const size_t avail = (size_t)optin > slot + 1024 ? (size_t)optin - slot - 1024 : 0;
+  const int rows = (int)(avail / ((size_t)6 * ng * sizeof(float)));
+  *smem = tab_table_bytes(rows, ng) + slot;
+  return rows;
+}
+
+}  // namespace
+
+int launch_tab_fwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
+                   const int* sorted_rows, float* xyz, void* D, int d_bf16, cudaStream_t st) {
+  if (nchunks <= 0) return DPGB_OK;
+  size_t smem = 0;
+  const int rows = tab_rows_cap(p.ng, kFwdWarps, &smem);
+  DPGB_CUDA(cudaFuncSetAttribute(tab_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  tab_fwd_kernel<<<std::min(nchunks, sm_count()), kFwdWarps * 32, smem, st>>>(p, e, chunks, nchunks, sorted_rows,
+                                                                               rows, xyz, D, d_bf16);
   return check_launch("tab_fwd");
 }
 
-int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const int* sorted_rows, int nsorted,
-                   const float* dxyz, float* gpair, double* vir_row, cudaStream_t st) {
-  if (nsorted <= 0) return DPGB_OK;
-  tab_bwd_kernel<<<ceil_div(nsorted, kTabWarps), kTabWarps * 32, 0, st>>>(p, e, sorted_rows, nsorted, dxyz, gpair,
-                                                                          vir_row);
+int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
+                   const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, cudaStream_t st) {
+  if (nchunks <= 0) return DPGB_OK;
+  // rows at an odd float2 stride; per warp the atom's dE/dxyz and its slot list
+  int per2 = 3 * p.ng;
+  if (per2 % 2 == 0) ++per2;
+  const int row_stride = 2 * per2;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t per_warp = (size_t)p.ng * sizeof(float4) + (size_t)p.nnei * sizeof(int);
+  const size_t fixed = (size_t)kBwdWarps * per_warp + 16 + 1024;
+  if ((size_t)optin <= fixed) return fail(DPGB_EINVAL, "tab_bwd: the neighbour list is too wide");
+  const int rows = (int)(((size_t)optin - fixed) / ((size_t)row_stride * sizeof(float)));
+  const size_t smem = ((size_t)rows * row_stride * 4 + 15) / 16 * 16 + (size_t)kBwdWarps * per_warp;
+  DPGB_CUDA(cudaFuncSetAttribute(tab_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  tab_bwd_kernel<<<std::min(nchunks, sm_count()), kBwdWarps * 32, smem, st>>>(p, e, chunks, nchunks, sorted_rows,
+                                                                               rows, row_stride, dxyz, gpair, vir_row);
   return check_launch("tab_bwd");
 }
 

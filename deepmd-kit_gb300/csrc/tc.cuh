@@ -130,18 +130,23 @@ __device__ __forceinline__ uint64_t global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Bounded wait: gives up after ~1 s, sets *err and returns false, so that a
-// wait that can never complete ends the kernel instead of hanging the GPU.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+// Bounded wait: gives up after limit_ns, sets *err and returns false, so
+// that a wait that can never complete ends the kernel instead of hanging the
+// GPU.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, int* err, uint64_t limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (global_ns() - t0 > 1000000000ull) {
+    if (global_ns() - t0 > limit_ns) {
       if (err) atomicMax(err, 1);
       return false;
     }
   }
   return true;
+}
+// the kernels' waits: ~1 s
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+  return mbar_wait_for(bar, parity, err, 1000000000ull);
 }
 
 // --- TMEM -> registers (32 lanes x 32 bits, 16 consecutive columns) -----------

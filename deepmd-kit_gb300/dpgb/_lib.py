@@ -126,6 +126,14 @@ _SIGS = {
     "dpgb_batch_compute_device": [_P, _P, _P, _P, _P, _P, _I],
     "dpgb_batch_compute": [_P, _DP, _DP, _DP, _DP, _I],
     "dpgb_deeppot_last_launches": [_P],
+    "dpgb_deeppot_last_nlist": [_P, _IP, _IP, _DP, _DP],
+    "dpgb_selftest_wait_timeout": [_D, _P],
+    "dpgb_model_file_open": [C.c_char_p, C.c_char_p, C.c_size_t],
+    "dpgb_model_file_close": [_P],
+    "dpgb_model_file_desc": [_P],
+    "dpgb_model_file_type_map": [_P],
+    "dpgb_model_file_config": [_P],
+    "dpgb_model_file_tensor": [_P, C.c_char_p, _DP, C.c_longlong, C.POINTER(C.c_longlong), _IP],
     "dpgb_deeppot_set_skin": [_P, _D, _I],
     "dpgb_deeppot_set_graph": [_P, _I],
     "dpgb_deeppot_check_status": [_P, _P],
@@ -139,6 +147,12 @@ _RESTYPE = {
     "dpgb_version": C.c_char_p,
     "dpgb_deeppot_new": _P,
     "dpgb_batch_new": _P,
+    "dpgb_model_file_open": _P,
+    "dpgb_model_file_close": None,
+    "dpgb_model_file_desc": _P,
+    "dpgb_model_file_type_map": C.c_char_p,
+    "dpgb_model_file_config": C.c_char_p,
+    "dpgb_model_file_tensor": C.c_longlong,
     "dpgb_batch_delete": None,
     "dpgb_deeppot_delete": None,
     "dpgb_deeppot_check_ok": C.c_char_p,

@@ -31,15 +31,24 @@ def nvcc() -> str:
 
 
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    """CUDA translation units (nvcc) and host-only C++ ones (g++)."""
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cc")))
 
 
 def _deps():
-    return _sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    return (_sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+            + [os.path.join(ROOT, "plugin", "deeppot_backend.cc")])
+
+
+def cxx() -> str:
+    for cand in (os.environ.get("CXX"), shutil.which("g++"), shutil.which("c++")):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("no C++ compiler found")
 
 
 def needs_build() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(PLUGIN):
         return True
     t = os.path.getmtime(LIB)
     return any(os.path.getmtime(p) > t for p in _deps())
@@ -55,11 +64,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
         flags += ["-Xptxas", "-v"]
 
     def compile_one(src):
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        cmd = [cc] + flags + ["-c", src, "-o", obj]
+        obj = os.path.join(BUILD, os.path.basename(src).rsplit(".", 1)[0] + ".o")
+        if src.endswith(".cc"):
+            cmd = [cxx(), "-std=c++17", "-O2", "-fPIC", "-I", INCLUDE, "-I", CSRC, "-c", src, "-o", obj]
+        else:
+            cmd = [cc] + flags + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
+            raise RuntimeError(f"compilation failed on {src}:\n{r.stdout}\n{r.stderr}")
         if verbose and r.stderr:
             sys.stderr.write(r.stderr)
         return obj
@@ -72,7 +84,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_plugin(cc)
     return LIB
+
+
+PLUGIN_SRC = os.path.join(ROOT, "plugin", "deeppot_backend.cc")
+# the file name a reference host looks for when it loads the backend of .pth
+# models (lib + deepmd_backend_pt + .so, in DP_BACKEND_PLUGIN_PATH)
+PLUGIN = os.path.join(PKG, "libdeepmd_backend_pt.so")
+
+
+def build_plugin(cc: str) -> str:
+    """The DeepPot backend plugin library, linked to libdpgb.so next to it."""
+    tmp = PLUGIN + ".tmp"
+    cmd = [cc, "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-shared", "-I", INCLUDE, PLUGIN_SRC, "-o", tmp,
+           "-L", PKG, "-ldpgb", "-lcudart", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"plugin build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, PLUGIN)
+    return PLUGIN
 
 
 if __name__ == "__main__":

@@ -93,6 +93,35 @@ class DeepPot:
         if not self._h:
             raise _lib.DpgbError(-1, lib.dpgb_last_error().decode())
 
+    @classmethod
+    def from_file(cls, path: str, precision: str = "fp64", device: int = 0) -> "DeepPot":
+        """A DeepPot from a frozen DeePMD-kit PyTorch model file (.pth, the
+        file DP_NewDeepPot takes), read without libtorch
+        (dpgb_model_file_open)."""
+        import torch
+
+        if not torch.cuda.is_available():
+            raise RuntimeError("dpgb DeepPot needs a CUDA device")
+        torch.cuda.set_device(device)
+        lib = _lib.lib()
+        mf = lib.dpgb_model_file_open(str(path).encode(), None, 0)
+        if not mf:
+            raise _lib.DpgbError(-1, lib.dpgb_last_error().decode())
+        try:
+            self = cls.__new__(cls)
+            self.params = None
+            self.precision = precision
+            self.device = device
+            self.type_map = lib.dpgb_model_file_type_map(mf).decode().split()
+            desc = C.cast(lib.dpgb_model_file_desc(mf), C.POINTER(_lib.SeADesc)).contents
+            self._rcut, self._ntypes = float(desc.rcut), int(desc.ntypes)
+            self._h = lib.dpgb_deeppot_new(C.byref(desc), PRECISIONS[precision])
+        finally:
+            lib.dpgb_model_file_close(mf)
+        if not self._h:
+            raise _lib.DpgbError(-1, lib.dpgb_last_error().decode())
+        return self
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
@@ -101,14 +130,34 @@ class DeepPot:
 
     @property
     def rcut(self) -> float:
-        return self.params.config.rcut
+        return self.params.config.rcut if self.params is not None else self._rcut
 
     @property
     def ntypes(self) -> int:
-        return self.params.config.ntypes
+        return self.params.config.ntypes if self.params is not None else self._ntypes
 
     def last_launches(self) -> int:
         return int(_lib.lib().dpgb_deeppot_last_launches(self._h))
+
+    def last_nlist(self):
+        """(nlist [nframes*natom, nnei] int32, coord [nframes*natom, 3],
+        shift [nframes, nshift, 3]) of the list the last evaluation built:
+        extended index e = s*natom + j is image s of atom j at coord[j] +
+        shift[frame, s]; None when that evaluation had no list of its own."""
+        lib = _lib.lib()
+        info = np.zeros(4, dtype=np.int32)
+        ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+        _lib.check(lib.dpgb_deeppot_last_nlist(self._h, info.ctypes.data_as(ip), C.cast(None, ip),
+                                               C.cast(None, dp), C.cast(None, dp)))
+        nf, natom, nnei, nshift = (int(v) for v in info)
+        if nf <= 0:
+            return None
+        nl = np.empty((nf * natom, nnei), dtype=np.int32)
+        coord = np.empty((nf * natom, 3))
+        shift = np.empty((nf, nshift, 3))
+        _lib.check(lib.dpgb_deeppot_last_nlist(self._h, info.ctypes.data_as(ip), nl.ctypes.data_as(ip),
+                                               coord.ctypes.data_as(dp), shift.ctypes.data_as(dp)))
+        return nl, coord, shift
 
     def set_skin(self, skin: float, every: int = 1) -> None:
         """Reuse neighbour lists over calls on periodic frames: candidates

@@ -204,6 +204,27 @@ def init_params(config: SeAConfig, seed: int = 1) -> SeAParams:
     return SeAParams(c, mean, std, emb, fit, np.zeros(c.ntypes), np.zeros(c.ntypes))
 
 
+# Factor that brings the seeded random-init water model's forces on the
+# synthetic water boxes (RMS 3.8e-4 eV/A) to about 1 eV/A RMS, the magnitude
+# of forces in trained liquid-water models; see scale_energy.
+WATER_FORCE_SCALE = 2650.0
+
+
+def scale_energy(params: SeAParams, factor: float) -> SeAParams:
+    """A copy of ``params`` whose energy is ``factor`` times the original:
+    the output layer of every fitting net (matrix and bias) and the per-type
+    energy biases are scaled, so forces and virials scale by the same factor
+    while the descriptor and hidden layers are unchanged.  Used to test
+    mixed-precision errors against absolute force bounds at a realistic
+    force magnitude."""
+    fit = []
+    for layers in params.fit:
+        w, b, idt = layers[-1]
+        fit.append(list(layers[:-1]) + [(w * factor, None if b is None else b * factor, idt)])
+    return dataclasses.replace(params, fit=fit, bias_atom_e=params.bias_atom_e * factor,
+                               out_bias=params.out_bias * factor)
+
+
 def water_config() -> SeAConfig:
     """The water model: rcut 6, rcut_smth 0.5, sel [46, 92], embedding
     [25, 50, 100] tanh, type_one_side false, axis 16, fitting [240]*3."""

@@ -334,7 +334,10 @@ int dpgb_prod_virial_a_f64(double* virial, double* atom_virial,
  * scratch lives in one fixed 11 MiB device array of the library, so
  * nframes*nloc*nnei and nframes*nall must each be <= 262144 (larger sizes
  * return DPGB_EINVAL).  The first call on a device looks the array up
- * (cudaGetSymbolAddress) and should come before any stream capture.  All
+ * (cudaGetSymbolAddress) and should come before any stream capture; so
+ * should the first call after the device's CUDA context changed (a reset
+ * of the primary context, or a context of the caller's own), which looks
+ * it up again.  All
  * calls share the array: calls that overlap on the GPU race, so serialise
  * them.  Synchronises the stream. */
 int dpgb_prod_force_a_f64_noalloc(double* force, const double* net_deriv,
@@ -402,15 +405,42 @@ typedef struct dpgb_se_a_desc {
 
 /* Precision of a DeepPot evaluation. */
 #define DPGB_PREC_FP64 0  /* plain FP64 throughout (the drop-in form) */
-#define DPGB_PREC_MIXED 1 /* FP64 displacement, FP32 env matrix, BF16 tensor-core
-                             embedding (split hi+lo on G) and fitting GEMMs
-                             with FP32 accumulation, FP64 energy/virial sums */
+#define DPGB_PREC_MIXED 1 /* FP64 displacement, FP32 env matrix, tensor-core
+                             embedding and fitting GEMMs in split BF16 (hi + lo
+                             operands) with FP32 accumulation, FP64
+                             energy/virial sums */
 
 typedef struct dpgb_deeppot dpgb_deeppot;
 
 /* Creates a model on the current CUDA device.  Returns NULL on failure
  * (message in dpgb_last_error()). */
 dpgb_deeppot* dpgb_deeppot_new(const dpgb_se_a_desc* desc, int precision);
+
+/* Frozen model files: the se_e2_a energy models that DeePMD-kit's PyTorch
+ * backend freezes into a .pth TorchScript archive (`dp --pt freeze`, the
+ * file DP_NewDeepPot(const char* model) takes: source/api_c/include/
+ * c_api.h:150; DeepPotPT::init, source/api_cc/src/DeepPotPT.cc:73-152),
+ * read on the host without libtorch: the configuration from the module's
+ * model_def_script, the weights by their state-dict names, compressed
+ * tables when the model was compressed.  content/size, when size > 0, is
+ * the file's content (the reference's file_content argument) and path is
+ * then not read.  Returns NULL on failure (dpgb_last_error()). */
+typedef struct dpgb_model_file dpgb_model_file;
+dpgb_model_file* dpgb_model_file_open(const char* path, const char* content,
+                                      size_t size);
+void dpgb_model_file_close(dpgb_model_file* m);
+/* The model description (valid while m is open): pass to dpgb_deeppot_new. */
+const dpgb_se_a_desc* dpgb_model_file_desc(const dpgb_model_file* m);
+/* Space-separated element names of the types ("" when the model has none). */
+const char* dpgb_model_file_type_map(const dpgb_model_file* m);
+/* The model_def_script JSON text. */
+const char* dpgb_model_file_config(const dpgb_model_file* m);
+/* A weight by state-dict name: returns its element count (-1 if absent),
+ * copies up to cap values (FP64) into out and, when ndim is set (in: the
+ * capacity of shape, out: the rank), its shape into shape. */
+long long dpgb_model_file_tensor(const dpgb_model_file* m, const char* name,
+                                 double* out, long long cap, long long* shape,
+                                 int* ndim);
 void dpgb_deeppot_delete(dpgb_deeppot* dp);
 /* Text of the last error stored on the handle, "" when the last call
  * succeeded (c_api.cc:2730 DP_DeepPotCheckOK). */
@@ -526,8 +556,36 @@ int dpgb_batch_compute_device(dpgb_batch* b, const double* coord,
 int dpgb_batch_compute(dpgb_batch* b, const double* coord, double* energy,
                        double* force, double* virial, int use_graph);
 
+/* Self-test of the bounded device-side waits (no counterpart in the
+ * reference, which has no device-side waits of its own): one kernel waits
+ * on an mbarrier that nothing completes, with a limit of limit_ms (0 < ...
+ * <= 1000), gives up, records the timeout and ends.  Returns DPGB_ETIMEOUT
+ * — the code a timed-out tensor-core wait gives every compute call — with
+ * the CUDA context still usable; DPGB_OK would mean the wait did not run
+ * out.  stream NULL = the legacy default stream; synchronises it. */
+int dpgb_selftest_wait_timeout(double limit_ms, void* stream);
+
 /* Number of kernel launches the last compute issued (for the benchmark). */
 int dpgb_deeppot_last_launches(dpgb_deeppot* dp);
+
+/* The neighbour list the last single-system evaluation built for itself,
+ * for verification (no counterpart in the reference, where the list stays
+ * inside DeepPot::compute: source/api_cc/src/DeepPotPT.cc:170-243).  HOST
+ * buffers; waits for the handle's stream:
+ *   info [4]  <- nframes, natom, nnei (= sum(sel)), nshift (0 frames: the
+ *                last evaluation had no list of its own — none yet, an
+ *                external list or a batch; then the other pointers must be
+ *                NULL);
+ *   nlist [nframes * natom, nnei] <- extended indices e = s * natom + j
+ *                (periodic image s of atom j; -1 padding), type sections of
+ *                sel[t] in the reference order (deepmd/pt/utils/nlist.py);
+ *   coord [nframes * natom, 3] <- the coordinates the list refers to
+ *                (wrapped into the cell; with a skin, with the wrap offsets
+ *                of the last candidate build);
+ *   shift [nframes, nshift, 3] <- the Cartesian shift of each image s.
+ * Any of nlist, coord, shift may be NULL. */
+int dpgb_deeppot_last_nlist(dpgb_deeppot* dp, int* info, int* nlist,
+                            double* coord, double* shift);
 
 /* Stage timing with CUDA events on the compute stream (no counterpart in
  * the reference, whose DP_PROFILER hooks the libtorch profiler instead,

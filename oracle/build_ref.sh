@@ -5,11 +5,11 @@
 # oracle/_ref/libdeepmd_ref.so.  No reference source is copied.  Used to pin
 # the restated oracle and to generate tests/golden fixtures; never shipped.
 set -euo pipefail
-REF=${DPGB_REFERENCE:-/root/reference}
+REF=${DPGB_REFERENCE:-}
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
-if [ ! -d "$REF/source/lib/src" ]; then
-  echo "build_ref: reference sources not present at $REF; skipping" >&2
+if [ -z "$REF" ] || [ ! -d "$REF/source/lib/src" ]; then
+  echo "build_ref: DPGB_REFERENCE does not name a reference checkout; skipping" >&2
   exit 0
 fi
 mkdir -p "$OUT/obj"
@@ -37,3 +37,16 @@ if [ ! -f "$OUT/libdeepmd_op_pt.so" ] || [ "$REF/source/op/pt/tabulate_multi_dev
     -Wl,-rpath,"$TORCH_DIR/lib"
   echo "build_ref: wrote $OUT/libdeepmd_op_pt.so"
 fi
+
+# The layout of the reference's backend-plugin interface (vtable slots of
+# deepmd::DeepPotBackend, field offsets of deepmd::InputNlist), printed by
+# tests/plugin/abi_probe.cc compiled against the reference's own headers,
+# for tests/test_plugin_abi.py (the reference's common.h includes a header
+# its build generates: an empty stand-in suffices here).
+REPO_DIR="$(cd "$HERE/.." && pwd)"
+mkdir -p "$OUT/probe"
+printf '#pragma once\n' > "$OUT/probe/version.h"
+g++ -std=c++17 -DPROBE_REFERENCE -I "$OUT/probe" -I "$REF/source/api_cc/include" -I "$REF/source/lib/include" \
+  "$REPO_DIR/tests/plugin/abi_probe.cc" -o "$OUT/probe/abi_probe" && \
+  "$OUT/probe/abi_probe" > "$OUT/abi_probe_reference.txt" && \
+  echo "build_ref: wrote $OUT/abi_probe_reference.txt"

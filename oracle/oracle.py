@@ -38,12 +38,14 @@ def build(force: bool = False) -> str:
 
 
 def build_ref() -> Optional[str]:
-    """Compile the reference CPU library when the reference tree is present."""
+    """Compile the reference CPU library when DPGB_REFERENCE names a
+    reference checkout (else nothing is built and None is returned)."""
     script = os.path.join(HERE, "build_ref.sh")
-    ref = os.environ.get("DPGB_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "source", "lib", "src")):
+    ref = os.environ.get("DPGB_REFERENCE", "")
+    if not ref or not os.path.isdir(os.path.join(ref, "source", "lib", "src")):
         return None
-    if not os.path.exists(REF_PATH) or os.path.getmtime(REF_PATH) < os.path.getmtime(
+    probe = os.path.join(HERE, "_ref", "abi_probe_reference.txt")
+    if not os.path.exists(REF_PATH) or not os.path.exists(probe) or os.path.getmtime(REF_PATH) < os.path.getmtime(
             os.path.join(HERE, "ref_shim.cc")):
         subprocess.check_call(["bash", script])
     return REF_PATH

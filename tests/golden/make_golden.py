@@ -35,7 +35,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("DPGB_REFERENCE", "/root/reference")
+# the reference checkout to read (required: the fixtures come from it)
+REF = os.environ.get("DPGB_REFERENCE", "")
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 sys.path.insert(0, os.path.join(REPO, "deepmd-kit_gb300"))
 
@@ -268,7 +269,25 @@ def make_water_compressed(params, coord, atype, box):
         virial=ret["virial"].detach().numpy().reshape(-1), **tabs, **infos)
 
 
-TRAIN_FRAMES = 4       # water frames of the force-loss training case
+def make_pth():
+    """A frozen model file as the reference's `dp --pt freeze` writes it
+    (deepmd/pt/entrypoints/main.py freeze: torch.jit.script + torch.jit.save
+    of the model get_model builds, model_def_script included): the reference
+    test model deeppot_sea (weights of deeppot_sea_model.npz, type map O H),
+    for the model-file reader and the DeepPot plugin backend."""
+    import torch
+    from conftest import deeppot_sea_params
+
+    params = deeppot_sea_params()
+    model = _reference_model(params)
+    script = __import__("json").loads(model.model_def_script)
+    script["type_map"] = ["O", "H"]
+    model.model_def_script = __import__("json").dumps(script)
+    model.eval()
+    torch.jit.save(torch.jit.script(model), os.path.join(HERE, "deeppot_sea.pth"))
+
+
+TRAIN_FRAMES = 16      # water frames of the force-loss training case (a batch of 16)
 TRAIN_PREF = (0.02, 1000.0)  # energy and force prefactors (start == limit)
 
 
@@ -285,7 +304,10 @@ def make_train_grad():
     EnergyStdLoss, FP64 autograd) on water frames labelled by a second,
     differently seeded model: the loss, the per-tensor gradient norms and 64
     gradient entries (tensor name, flat index, value)."""
+    import refshim
     import torch
+
+    refshim.install()
     from deepmd.pt.loss import EnergyStdLoss
     from dpgb import params as P
 
@@ -327,6 +349,9 @@ def make_train_grad():
 if __name__ == "__main__":
     import oracle as O
 
+    if not os.path.isdir(os.path.join(REF, "source")):
+        sys.exit("make_golden: set DPGB_REFERENCE to the deepmd-kit reference checkout")
+
     O.build_ref()
     make_tabulate()
     make_deeppot_case()
@@ -334,6 +359,7 @@ if __name__ == "__main__":
     p, c, t, b = make_water()
     make_water_compressed(p, c, t, b)
     make_train_grad()
+    make_pth()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -14,7 +14,9 @@ import types
 import torch  # noqa: F401  (must come before deepmd)
 import numpy as np
 
-REF = os.environ.get("DPGB_REFERENCE", "/root/reference")
+REF = os.environ.get("DPGB_REFERENCE", "")  # the reference checkout (required)
+if not os.path.isdir(os.path.join(REF, "deepmd")):
+    raise ImportError("refshim: set DPGB_REFERENCE to the deepmd-kit reference checkout")
 
 
 class _Stub(types.ModuleType):

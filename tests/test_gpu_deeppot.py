@@ -54,6 +54,32 @@ def test_deeppot_testcase(cuda):
         np.testing.assert_allclose(e[0], c[f"b{b}_atomic_energy"].sum(), rtol=1e-12)
 
 
+def test_deeppot_testcase_from_model_file(cuda):
+    """The same golden case through a frozen .pth model file read by the
+    library (DP_NewDeepPot's input), FP64 and the mixed form."""
+    import os
+
+    from conftest import GOLDEN
+    from dpgb.deeppot import DeepPot
+
+    c = golden("deeppot_sea_case")
+    for prec, tol in (("fp64", 1e-10), ("mixed", None)):
+        dp = DeepPot.from_file(os.path.join(GOLDEN, "deeppot_sea.pth"), prec)
+        assert dp.type_map == ["O", "H"] and dp.rcut == 6.0 and dp.ntypes == 2
+        for b in range(int(c["nblock"])):
+            box = c[f"b{b}_box"]
+            e, f, v, ae, av = dp.eval(c[f"b{b}_coord"], None if box.size == 0 else box, c[f"b{b}_atype"],
+                                      atomic=True)
+            if tol:
+                np.testing.assert_allclose(ae[0], c[f"b{b}_atomic_energy"], rtol=tol, atol=tol)
+                np.testing.assert_allclose(f[0].reshape(-1), c[f"b{b}_force"], rtol=tol, atol=1e-12)
+                np.testing.assert_allclose(av[0].reshape(-1), c[f"b{b}_atomic_virial"], rtol=tol, atol=1e-12)
+            else:
+                ref = c[f"b{b}_force"]
+                rmse = float(np.sqrt(np.mean((f[0].reshape(-1) - ref) ** 2)))
+                assert rmse <= 2e-2 * float(np.sqrt(np.mean(ref ** 2)))
+
+
 def test_water192_compressed_matches_reference(cuda):
     from dpgb.deeppot import DeepPot
 

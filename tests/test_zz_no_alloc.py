@@ -4,10 +4,15 @@ device memory through its own pool, or an inner loop where cudaMalloc's
 device-wide synchronisation is not acceptable).  It keeps its scratch in one
 fixed device array of the library, so its result must equal the allocating
 dpgb_prod_force_a_f64 on every call, including back-to-back calls that reuse
-the array with different inputs.  Collected last so that a failure here
-cannot hide the other tests' results; it also runs alone in a fresh process.
+the array with different inputs, and many calls in a row must leave the
+device's free memory unchanged.  Collected last so that a failure here
+cannot hide the other tests' results; the last test runs the first one again
+alone, in a fresh process.
 """
 import ctypes
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -80,3 +85,32 @@ def test_rejects_sizes_beyond_the_fixed_scratch(cuda):
     f = torch.zeros(1, nall, 3, dtype=torch.float64, device=cuda)
     with pytest.raises(_lib.DpgbError, match="must not exceed 262144"):
         _lib.call("dpgb_prod_force_a_f64_noalloc", _vp(f), _vp(nd), _vp(ed), _vp(nl), nloc, nall, nnei, 1, _stream())
+
+
+def test_no_device_allocation_over_many_calls(cuda):
+    """After one warm-up call, back-to-back calls change neither the device's
+    free memory (cudaMemGetInfo) nor torch's reserved pool."""
+    import torch
+
+    nd, ed, nl = _random_case(cuda, 11, 200, 900, 30, 3)
+    f = torch.zeros(3, 900, 3, dtype=torch.float64, device=cuda)
+    from dpgb import _lib
+
+    args = (_vp(f), _vp(nd), _vp(ed), _vp(nl), 200, 900, 30, 3, _stream())
+    _lib.call("dpgb_prod_force_a_f64_noalloc", *args)
+    torch.cuda.synchronize()
+    free0, reserved0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_reserved()
+    for _ in range(50):
+        _lib.call("dpgb_prod_force_a_f64_noalloc", *args)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_reserved() == reserved0
+
+
+def test_runs_alone_in_a_fresh_process(cuda):
+    here = os.path.dirname(os.path.abspath(__file__))
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-m", "gpu", "-p", "no:cacheprovider",
+                        os.path.join(here, "test_zz_no_alloc.py") + "::test_matches_allocating_entry_point_on_consecutive_calls"],
+                       capture_output=True, text=True, timeout=600, cwd=os.path.dirname(here))
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert "1 passed" in r.stdout
