@@ -49,13 +49,9 @@ __device__ __forceinline__ void slot_env(const DescParams<float>& p, int row, in
   s.d[0] = s.d[1] = s.d[2] = 0.f;
   int keep = 1;
   if (s.nb >= 0) {
-    // FP64 displacement: these kernels are bound by the table reads, which
-    // the split coordinates' extra loads would add to
-    double dd[3];
-    const int tj = pair_disp(p, f, i, s.nb, dd);
-    s.d[0] = (float)dd[0];
-    s.d[1] = (float)dd[1];
-    s.d[2] = (float)dd[2];
+    // the displacement from the FP32 hi + lo splits (no FP64 instructions:
+    // GB300's FP64 pipe is narrow)
+    const int tj = pair_disp_f(p, f, i, s.nb, s.d);
     keep = p.pair_mask ? p.pair_mask[ti * p.ntypes + tj] : 1;
     if (keep) {
       const float nr2 = s.d[0] * s.d[0] + s.d[1] * s.d[1] + s.d[2] * s.d[2];
@@ -411,7 +407,10 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
           if (act) {
             const float* rowc = s.idx < rows ? s_tab + (size_t)s.idx * row_stride : tab + (size_t)s.idx * 6 * ng;
             const float xx = s.xx, dl = s.delta;
-            for (int n = 0; n < ng; ++n) {
+            // two neurons per step, each into its own partial sums (two
+            // independent chains for the scheduler), added at the end
+            float dR2[4] = {0.f, 0.f, 0.f, 0.f}, Pc2[4] = {0.f, 0.f, 0.f, 0.f};
+            auto neuron = [&](int n, float (&r)[4], float (&pc)[4]) {
               const float2* q = reinterpret_cast<const float2*>(rowc + 6 * n);
               const float2 x0 = q[0], x1 = q[1], x2 = q[2];
               const float4 d = s_dx[n];
@@ -426,14 +425,25 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
               Gp = fmaf(Gp, xx, G);
               G = fmaf(G, xx, x0.x);
               G = fmaf(Gp, dl, G);  // linear extension past the table ends (dl 0 inside)
-              dR[0] = fmaf(G, d.x, dR[0]);
-              dR[1] = fmaf(G, d.y, dR[1]);
-              dR[2] = fmaf(G, d.z, dR[2]);
-              dR[3] = fmaf(G, d.w, dR[3]);
-              Pc[0] = fmaf(Gp, d.x, Pc[0]);
-              Pc[1] = fmaf(Gp, d.y, Pc[1]);
-              Pc[2] = fmaf(Gp, d.z, Pc[2]);
-              Pc[3] = fmaf(Gp, d.w, Pc[3]);
+              r[0] = fmaf(G, d.x, r[0]);
+              r[1] = fmaf(G, d.y, r[1]);
+              r[2] = fmaf(G, d.z, r[2]);
+              r[3] = fmaf(G, d.w, r[3]);
+              pc[0] = fmaf(Gp, d.x, pc[0]);
+              pc[1] = fmaf(Gp, d.y, pc[1]);
+              pc[2] = fmaf(Gp, d.z, pc[2]);
+              pc[3] = fmaf(Gp, d.w, pc[3]);
+            };
+            int n = 0;
+            for (; n + 1 < ng; n += 2) {
+              neuron(n, dR, Pc);
+              neuron(n + 1, dR2, Pc2);
+            }
+            if (n < ng) neuron(n, dR, Pc);
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+              dR[cc] += dR2[cc];
+              Pc[cc] += Pc2[cc];
             }
           }
           if (mine) {
