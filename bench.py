@@ -21,7 +21,7 @@ reported in `config` together with the mixed-vs-FP64 errors.  Workload
 water12k: the uncompressed model on 4096 molecules (12,288 atoms).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl dpgb|reference]
-                    [--workload water98k-compressed|water12k|alloy512-batch]
+                    [--workload water98k-compressed|water12k|alloy512-batch|train16]
 """
 from __future__ import annotations
 
@@ -192,9 +192,11 @@ def table_bytes_flops(n_atoms: int, n_pairs: int, cfg) -> dict:
 # FP32 CUDA-core peak (no tensor cores): 152 SMs x 128 lanes x 2 FLOP x 2.07 GHz
 FP32_SIMT_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12
 
-# DRAM bytes (read + write) per launch of the dominant kernels, from one ncu
-# capture each (profiles/); None where not captured for the current build
-DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": None, "desc_bwd": None, "fitting": None}
+# DRAM bytes (read + write) per launch of the dominant kernels of the
+# 98,304-atom compressed step, from one ncu capture each: tab_fwd, tab_bwd
+# (profiles/tab_fused_water98304_compressed.md) and the fitting stage's six
+# launches summed (five fit_gemm + fit_dxyz, one dram-bytes pass)
+DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 727.6e6, "desc_bwd": 501.5e6, "fitting": 2103.7e6}
 
 
 def table_roofline(per_step: dict, n_atoms: int, n_pairs: int, cfg) -> dict:
@@ -307,8 +309,8 @@ def run_reference(args, world, rank):
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     compressed = args.workload == "water98k-compressed"
-    if args.workload == "alloy512-batch":
-        print(json.dumps({"impl": "reference", "unavailable": "no CPU arm for the alloy batch workload"}))
+    if args.workload in ("alloy512-batch", "train16"):
+        print(json.dumps({"impl": "reference", "unavailable": f"no CPU arm for the {args.workload} workload"}))
         return
     value, sec, ncores, sample = cpu_full_steps(compressed, args.steps, args.warmup)
     line = {
@@ -335,6 +337,8 @@ WORKLOAD_NAME = {
     "water12k": "water 4096 H2O (12,288 atoms), box 49.6 A, se_e2_a rc 6 sel [46,92] emb [25,50,100] "
                 "axis 16 fit [240,240,240]",
     "alloy512-batch": "512 fcc alloy frames, se_e2_a rc 6 rs 2 sel [60]*4",
+    "train16": "force-loss Adam step on 16 water frames of 192 atoms, se_e2_a rc 6 sel [46,92] emb [25,50,100] "
+               "axis 16 fit [240,240,240], FP64",
 }
 
 
@@ -548,6 +552,89 @@ def run_batch(args, world, rank, local):
     print(json.dumps(line))
 
 
+TRAIN_FRAMES, TRAIN_NMOL_SIDE = 16, 4  # 16 frames of 64 H2O (192 atoms)
+
+
+def run_train(args, world, rank, local):
+    """One force-loss Adam step on a batch of 16 water frames (192 atoms each,
+    the 12.4 A box of different seeds), labels from a separately seeded FP64
+    teacher of the same architecture; loss 0.02 (E - E_ref)^2 / N +
+    1000 mean |F - F_ref|^2.  The step runs the model forward, forces
+    through the hand-written double backward, the loss, the weight gradient
+    and the Adam update (dpgb.train.Trainer).  ``value``: frames resident on
+    the device; ``e2e``: frames copied from host memory each step and the
+    loss read back."""
+    import torch
+
+    from dpgb import params as P, synth
+    from dpgb.model import EnergyModelSeA
+    from dpgb.train import FrameSet, LearningRateExp, Trainer
+
+    dev = torch.device("cuda", local)
+    frames = [synth.water_box(TRAIN_NMOL_SIDE, seed=100 + 1000 * rank + k) for k in range(TRAIN_FRAMES)]
+    coord = np.stack([f[0].reshape(-1) for f in frames])
+    atype, box = frames[0][1], np.stack([f[2].reshape(-1) for f in frames])
+    nf, nloc = coord.shape[0], atype.shape[0]
+    cfg = P.water_config()
+    teacher = EnergyModelSeA.from_params(P.init_params(cfg, seed=2), device=dev)
+    lab = teacher(torch.tensor(coord, device=dev), torch.tensor(np.tile(atype, (nf, 1)), device=dev),
+                  torch.tensor(box, device=dev), create_graph=False)
+    e_lab, f_lab = lab["energy"].detach().cpu().numpy(), lab["force"].detach().cpu().numpy()
+    del teacher, lab
+    loss_params = dict(start_pref_e=0.02, limit_pref_e=0.02, start_pref_f=1000.0, limit_pref_f=1000.0)
+    n_total = args.warmup + args.steps
+
+    def trainer(device_frames):
+        m = EnergyModelSeA.from_params(P.init_params(cfg, seed=1), device=dev)
+        fs = FrameSet(coord, atype, box, energy=e_lab, force=f_lab, batch_size=nf,
+                      device=dev if device_frames else None)
+        return Trainer(m, LearningRateExp(start_lr=1e-3, stop_lr=1e-5, num_steps=2 * n_total), fs,
+                       loss_params=loss_params, disp_freq=10 ** 9, disp_file=None)
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    stream = torch.cuda.current_stream()
+
+    def timed(tr, read_loss):
+        for _ in range(args.warmup):
+            tr.step()
+        torch.cuda.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        _barrier(world)
+        for k in range(args.steps):
+            flush.fill_(float(k))  # evict L2 between timed steps (untimed)
+            starts[k].record(stream)
+            tr.step()
+            if read_loss:
+                float(tr.last_loss)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        _barrier(world)
+        return _allreduce_max(sum(a.elapsed_time(b) for a, b in zip(starts, ends)), world)
+
+    tr = trainer(True)
+    with ClockSampler(local, busy=tr.step) as clk:
+        t_ms = timed(tr, False)
+    t_e2e = timed(trainer(False), True)
+    value = world * nf * nloc * args.steps / (t_ms * 1e-3)
+    e2e = world * nf * nloc * args.steps / (t_e2e * 1e-3)
+    if rank != 0:
+        return
+    h2d = coord.nbytes + nf * nloc * 8 + box.nbytes + e_lab.nbytes + f_lab.nbytes
+    line = {
+        "metric": "atom-steps/s se_e2_a force-loss training step (Adam, FP64)", "value": value,
+        "unit": "atom-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME["train16"], "frames": nf, "atoms_per_frame": nloc,
+                   "l2": "flushed between timed steps (256 MB fill)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 8},
+        "roofline": None,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 # DRAM bytes (read + write) per launch of each stage's tensor-core kernel on
 # the 12,288-atom water step, from one ncu capture (emb_tc_fwd, emb_tc_bwd,
 # the first fitting GEMM): profiles/emb_tc_water12288.md,
@@ -558,7 +645,7 @@ DRAM_BYTES_PER_LAUNCH = {"desc_fwd": 50.0e6, "desc_bwd": 27.2e6, "fitting": 41.9
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="water98k-compressed",
-                    choices=["water98k-compressed", "water12k", "alloy512-batch"])
+                    choices=["water98k-compressed", "water12k", "alloy512-batch", "train16"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -590,6 +677,9 @@ def main():
         return
     if args.workload == "alloy512-batch":
         run_batch(args, world, rank, local)
+        return
+    if args.workload == "train16":
+        run_train(args, world, rank, local)
         return
     from dpgb import nlist as N, params as P, synth
     from dpgb.deeppot import DeepPot

@@ -190,20 +190,25 @@ class EnergyModelSeA(torch.nn.Module):
 
 class EnergyStdLoss(torch.nn.Module):
     """Energy / force / virial mean-squared loss of deepmd/pt/loss/ener.py:
-    216-330: pref = limit + (start - limit) * lr / starter_lr;
-    loss = pref_e * mean(dE^2) / natoms + pref_f * mean(dF^2)
-         + pref_v * mean(dV^2) / natoms."""
+    216-330, 636-680: pref = limit + (start - limit) * lr / starter_lr;
+    loss = pref_e * find_e * mean(dE^2) / natoms^k + pref_f * find_f * mean(dF^2)
+         + pref_v * find_v * mean(dV^2) / natoms^k, k = 2 with
+    ``intensive_ener_virial`` else 1.  A term is on when both its start and
+    limit prefactors are nonzero (ener.py:160-162); ``find_<label>`` is 0
+    unless the label dict sets it, and a figure whose label is not found
+    displays as NaN (deepmd/pt/loss/loss.py:74-84)."""
 
     def __init__(self, starter_learning_rate=1.0, start_pref_e=0.02, limit_pref_e=1.0, start_pref_f=1000.0,
-                 limit_pref_f=1.0, start_pref_v=0.0, limit_pref_v=0.0, **kwargs):
+                 limit_pref_f=1.0, start_pref_v=0.0, limit_pref_v=0.0, intensive_ener_virial=False, **kwargs):
         super().__init__()
         self.starter_learning_rate = starter_learning_rate
         self.start_pref_e, self.limit_pref_e = start_pref_e, limit_pref_e
         self.start_pref_f, self.limit_pref_f = start_pref_f, limit_pref_f
         self.start_pref_v, self.limit_pref_v = start_pref_v, limit_pref_v
-        self.has_e = start_pref_e != 0.0 or limit_pref_e != 0.0
-        self.has_f = start_pref_f != 0.0 or limit_pref_f != 0.0
-        self.has_v = start_pref_v != 0.0 or limit_pref_v != 0.0
+        self.has_e = start_pref_e != 0.0 and limit_pref_e != 0.0
+        self.has_f = start_pref_f != 0.0 and limit_pref_f != 0.0
+        self.has_v = start_pref_v != 0.0 and limit_pref_v != 0.0
+        self.norm_exp = 2 if intensive_ener_virial else 1
 
     def forward(self, input_dict, model, label, natoms, learning_rate, mae=False):
         pred = model(**input_dict)
@@ -217,17 +222,25 @@ class EnergyStdLoss(torch.nn.Module):
         atom_norm = float(np.float32(1.0) / np.float32(natoms))
         loss = torch.zeros((), dtype=torch.float64, device=pred["energy"].device)
         more = {}
+        norm = atom_norm ** self.norm_exp
+
+        def shown(v, find):
+            return v if bool(find) else torch.nan
+
         if self.has_e and "energy" in label:
+            find = float(label.get("find_energy", 0.0))
             l2 = torch.mean(torch.square(pred["energy"] - label["energy"].reshape(pred["energy"].shape)))
-            loss = loss + atom_norm * pref_e * float(label.get("find_energy", 1.0)) * l2
-            more["rmse_e"] = l2.detach().sqrt() * atom_norm
+            loss = loss + norm * (pref_e * find * l2)
+            more["rmse_e"] = shown(l2.detach().sqrt() * atom_norm, find)
         if self.has_f and "force" in label:
+            find = float(label.get("find_force", 0.0))
             l2 = torch.mean(torch.square(pred["force"] - label["force"].reshape(pred["force"].shape)))
-            loss = loss + pref_f * float(label.get("find_force", 1.0)) * l2
-            more["rmse_f"] = l2.detach().sqrt()
+            loss = loss + pref_f * find * l2
+            more["rmse_f"] = shown(l2.detach().sqrt(), find)
         if self.has_v and "virial" in label:
+            find = float(label.get("find_virial", 0.0))
             l2 = torch.mean(torch.square(pred["virial"] - label["virial"].reshape(pred["virial"].shape)))
-            loss = loss + atom_norm * pref_v * float(label.get("find_virial", 1.0)) * l2
-            more["rmse_v"] = l2.detach().sqrt() * atom_norm
+            loss = loss + norm * (pref_v * find * l2)
+            more["rmse_v"] = shown(l2.detach().sqrt() * atom_norm, find)
         more["rmse"] = loss.detach().sqrt()
         return pred, loss, more

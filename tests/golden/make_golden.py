@@ -23,6 +23,12 @@ Sources of each fixture:
 * ``water192_compressed.npz`` — the same model after the reference's
   ``enable_compression`` (coarse strides so the fixture stays small): the
   tables, table_info and the compressed energy/forces/virial.
+* ``train_grad.npz`` — one force-loss step of the reference model: the loss
+  and its parameter gradient (norms and 64 entries).
+* ``train_steps.npz`` — six Adam steps of the reference's training loop
+  (its LearningRateExp, EnergyStdLoss and torch Adam + LambdaLR): rates,
+  losses, displayed figures, final weights (norms and 64 entries) and the
+  lcurve.out text of its print_header / print_on_training.
 """
 from __future__ import annotations
 
@@ -346,6 +352,121 @@ def make_train_grad():
         pick_idx=np.array(pick_idx), pick_val=np.array(pick_val))
 
 
+TRAIN_STEPS = 6        # Adam steps of the training-loop case
+TRAIN_BATCH = 4        # frames per batch: frames 0-11 train, 12-15 validate
+TRAIN_LOOP_PREF = dict(start_pref_e=0.02, limit_pref_e=1.0, start_pref_f=1000.0, limit_pref_f=1.0)
+TRAIN_LR = dict(start_lr=1e-3, stop_lr=1e-5, num_steps=TRAIN_STEPS)
+TRAIN_DISP_FREQ = 2
+TRAIN_LR_CASES = (   # schedules whose values the fixture also records
+    dict(start_lr=1e-3, stop_lr=3.51e-8, num_steps=1000000, decay_steps=5000),
+    dict(start_lr=2e-3, stop_lr_ratio=1e-4, num_steps=200000, decay_steps=5000, warmup_steps=500,
+         warmup_start_factor=0.1),
+    dict(start_lr=1e-3, stop_lr=1e-6, num_steps=50000, decay_steps=1000, smooth=True),
+    dict(start_lr=1e-3, stop_lr=1e-5, num_steps=300000, decay_steps=2000, decay_rate=0.95),
+    dict(start_lr=1e-3, stop_lr=1e-7, num_steps=400, decay_steps=5000),
+    dict(start_lr=5e-4, stop_lr=1e-8, num_steps=20000, decay_steps=100000, warmup_ratio=0.05),
+)
+
+
+def make_train_steps():
+    """Six Adam steps of the reference's training loop, assembled from its
+    own parts as deepmd/pt/train/training.py:1074-1130, 1201-1213 and
+    1385-1427 assemble them: deepmd.pt EnergyModel + EnergyStdLoss (FP64),
+    LearningRateExp (start 1e-3, stop 1e-5 over 6 steps), torch Adam with
+    the default betas behind a LambdaLR of lr(step) / start_lr.  Frames
+    0-11 train in batches of 4 in order; frames 12-15 are one validation
+    batch.  Recorded: the rate, loss and figures of every step, the
+    parameter norms and 64 entries after the last step, and the lcurve.out
+    text written by the reference's own print_header / print_on_training
+    (display every 2 steps and at step 1, validation figures included)."""
+    import io
+
+    import refshim
+    import torch
+
+    refshim.install()
+    from deepmd.dpmodel.utils.learning_rate import LearningRateExp
+    from deepmd.pt.loss import EnergyStdLoss
+    from deepmd.pt.train.training import Trainer
+    from dpgb import params as P
+
+    torch.set_num_threads(os.cpu_count() or 1)
+    cfg = P.water_config()
+    coord, atype, box = train_frames()
+    nf, nloc = coord.shape[0], atype.shape[0]
+    teacher = _reference_model(P.init_params(cfg, seed=2))
+    at = torch.as_tensor(np.tile(atype, (nf, 1)), dtype=torch.int64)
+    ref = teacher.forward(torch.as_tensor(coord), at, torch.as_tensor(box))
+    e_lab, f_lab = ref["energy"].detach(), ref["force"].detach()
+    student = _reference_model(P.init_params(cfg, seed=1))
+    lr = LearningRateExp(**TRAIN_LR)
+    loss_fn = EnergyStdLoss(starter_learning_rate=lr.start_lr, **TRAIN_LOOP_PREF)
+    opt = torch.optim.Adam(student.parameters(), lr=lr.value(0), betas=(0.9, 0.999), weight_decay=0.0)
+    for g in opt.param_groups:
+        g["initial_lr"] = lr.start_lr
+    sched = torch.optim.lr_scheduler.LambdaLR(opt, lambda s: lr.value(s) / lr.start_lr, last_epoch=-1)
+
+    def batch(lo):
+        sl = slice(lo, lo + TRAIN_BATCH)
+        inp = {"coord": torch.as_tensor(coord[sl]), "atype": at[sl], "box": torch.as_tensor(box[sl])}
+        lab = {"energy": e_lab[sl], "force": f_lab[sl], "find_energy": 1.0, "find_force": 1.0}
+        return inp, lab
+
+    class _Fmt:
+        multi_task = False
+
+    fout = io.StringIO()
+    lrs, losses, figs = [], [], []
+    keys = None
+    ntrain = 12
+    for step in range(TRAIN_STEPS):
+        opt.zero_grad(set_to_none=True)
+        inp, lab = batch((step * TRAIN_BATCH) % ntrain)
+        cur = sched.get_last_lr()[0]
+        _, loss, more = loss_fn(inp, student, lab, nloc, cur)
+        loss.backward()
+        opt.step()
+        sched.step()
+        trn = {k: float(more[k]) for k in sorted(more) if "l2_" not in k}
+        keys = sorted(trn)
+        lrs.append(cur)
+        losses.append(float(loss.detach()))
+        figs.append([trn[k] for k in keys])
+        shown = step + 1
+        if shown % TRAIN_DISP_FREQ == 0 or shown == 1:
+            vinp, vlab = batch(ntrain)
+            _, _, vmore = loss_fn(vinp, student, vlab, nloc, cur)
+            val = {k: float(vmore[k]) for k in sorted(vmore) if "l2_" not in k}
+            if shown == 1:
+                Trainer.print_header(_Fmt(), fout, trn, val)
+            Trainer.print_on_training(_Fmt(), fout, shown, cur, trn, val)
+    params = {k: p.detach().numpy().reshape(-1) for k, p in student.named_parameters() if p.numel() > 0}
+    names = sorted(params)
+    rng = np.random.default_rng(65)
+    pick_name, pick_idx, pick_val = [], [], []
+    for _ in range(64):
+        k = names[int(rng.integers(len(names)))]
+        i = int(rng.integers(params[k].size))
+        pick_name.append(k)
+        pick_idx.append(i)
+        pick_val.append(params[k][i])
+    cases, case_steps, case_lr = [], [], []
+    for kw in TRAIN_LR_CASES:
+        sched_c = LearningRateExp(**kw)
+        cases.append(repr(sorted(kw.items())))
+        steps = [0, 1, 99, 100, 101, 4999, 5000, 5001, 123456, kw["num_steps"] - 1, kw["num_steps"],
+                 2 * kw["num_steps"]]
+        case_steps.append(steps)
+        case_lr.append([sched_c.value(t) for t in steps])
+    np.savez_compressed(
+        os.path.join(HERE, "train_steps.npz"), lr_cases=np.array(cases), lr_case_steps=np.array(case_steps),
+        lr_case_values=np.array(case_lr), energy_label=e_lab.numpy().reshape(-1), force_label=f_lab.numpy(),
+        lr=np.array(lrs), loss=np.array(losses), fig_names=np.array(keys), figs=np.array(figs),
+        names=np.array(names), norms=np.array([np.linalg.norm(params[k]) for k in names]),
+        pick_name=np.array(pick_name), pick_idx=np.array(pick_idx), pick_val=np.array(pick_val),
+        lcurve=np.array(fout.getvalue()))
+
+
 if __name__ == "__main__":
     import oracle as O
 
@@ -359,6 +480,7 @@ if __name__ == "__main__":
     p, c, t, b = make_water()
     make_water_compressed(p, c, t, b)
     make_train_grad()
+    make_train_steps()
     make_pth()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):

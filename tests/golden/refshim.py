@@ -47,6 +47,7 @@ def _array_api_compat():
     m.array_namespace = array_namespace
     m.device = lambda x: getattr(x, "device", "cpu")
     m.is_numpy_array = lambda x: isinstance(x, np.ndarray)
+    m.is_array_api_obj = lambda x: isinstance(x, (np.ndarray, np.generic, torch.Tensor))
     m.is_torch_array = lambda x: isinstance(x, torch.Tensor)
     m.is_jax_array = lambda x: False
     m.is_array_api_strict_namespace = lambda x: False
@@ -60,7 +61,7 @@ def install():
     if "deepmd" in sys.modules:
         return
     for name in ("yaml", "h5py", "lmdb", "e3nn", "e3nn.o3", "wcmatch",
-                 "wcmatch.glob", "dargs"):
+                 "wcmatch.glob", "dargs", "dargs.json_schema"):
         if name not in sys.modules:
             _stub(name)
     sys.modules["wcmatch.glob"].globfilter = lambda *a, **k: []
