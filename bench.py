@@ -488,6 +488,13 @@ def run_batch(args, world, rank, local):
     gen = torch.Generator(device=dev).manual_seed(99 + rank)
     mixed = DeepPot(params, "mixed", device=local)
     b = mixed.batch(frames)
+    tune = None
+    if not args.no_tune:
+        # per-bucket work-item sizes: swept once per GPU / model shape / bucket
+        # populations (cached), outside the timed region
+        from dpgb import autotune
+
+        tune = autotune.tune_batch(b, coord)
     out = b.eval_device(coord, use_graph=True)  # plain evaluation + capture
     for _ in range(args.warmup):
         b.eval_device(coord, out=out, use_graph=True)
@@ -545,6 +552,12 @@ def run_batch(args, world, rank, local):
             "energy_err_per_atom_vs_fp64": float(np.max(np.abs(out["energy"].cpu().numpy()
                                                                - o64["energy"].cpu().numpy()) / sizes)),
             "stage_ms_one_plain_evaluation": {k: v / max(ncalls, 1) for k, v in stages.items()},
+            "buckets": {"limits": "<=128, <=512, <=2048, >2048 atoms", "frames": b.buckets()[0],
+                        "atoms": b.buckets()[1]},
+            "tiles": {"rows_per_item": b.tiles(),
+                      "tuned": None if tune is None else {
+                          "cached": tune["cached"], "default_ms": tune["default_ms"], "tuned_ms": tune["ms"],
+                          "trials": len(tune["trials"])}},
             "parallelism": f"replicas x{world}",
         },
         "clocks": clk.summary(),
@@ -655,6 +668,8 @@ def main():
     ap.add_argument("--skin", type=float, default=None,
                     help="neighbour-list skin in A for water98k-compressed (default 2; 0 = rebuild every step)")
     ap.add_argument("--rebuild-every", type=int, default=10)
+    ap.add_argument("--no-tune", action="store_true",
+                    help="alloy512-batch: keep the default work items (no per-bucket autotuning)")
     ap.add_argument("--no-graph", action="store_true",
                     help="time plain evaluations instead of replaying the step from a CUDA graph")
     args = ap.parse_args()

@@ -74,6 +74,23 @@ __device__ __forceinline__ void flag_nonfinite(const double* x, int atom, int* s
   if (status && !(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) atomicMax(status + kStatusNonFinite, atom + 1);
 }
 
+// Work items of a persistent kernel.  With a queue (an int zeroed before the
+// launch) each CTA takes the next item index from it when it finishes one,
+// so CTAs that drew short items take more of them; without a queue the
+// items go to the CTAs in a fixed stride.  Every thread of the CTA calls
+// these (they hold barriers); the item index is uniform over the CTA.
+__device__ __forceinline__ int work_first(int* queue, int* slot) {
+  if (threadIdx.x == 0) *slot = queue ? atomicAdd(queue, 1) : (int)blockIdx.x;
+  __syncthreads();
+  return *slot;
+}
+__device__ __forceinline__ int work_next(int* queue, int item, int* slot) {
+  __syncthreads();  // every thread has read the current index
+  if (threadIdx.x == 0) *slot = queue ? atomicAdd(queue, 1) : item + (int)gridDim.x;
+  __syncthreads();
+  return *slot;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -9,6 +9,7 @@
 //   the list -> desc_fwd -> fitting fwd+bwd per type -> desc_bwd ->
 //   force / atomic-virial gather -> per-frame FP64 energy and virial sums.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -381,6 +382,13 @@ struct DeepPotImpl {
   unsigned long long gen = 0;
   DeviceBuffer row_pos_dev, atype_dev, sorted_rows_dev, chunks_dev;
   int nchunks = 0;
+  // work queue of the persistent embedding / table kernels (two counters:
+  // forward, backward), used when a batch's per-bucket tile sizes cut the
+  // work items; the plan the cached rows and items were built for
+  DeviceBuffer queue_dev;
+  int use_queue = 0;
+  const void* plan_owner = nullptr;
+  unsigned long long plan_version = 0;
   // tensor-core embedding (mixed precision)
   int use_tc = 0;
   int use_tab = 0;  // compressed nets in the mixed form: fused FP32 table kernels
@@ -826,11 +834,43 @@ std::vector<int> default_shifts(const int nbuff[3]) {
   return out;
 }
 
-int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host, cudaStream_t st) {
+// Size buckets of a batch's frames (atoms <= 128, <= 512, <= 2048, more)
+// and the work-item size chosen for each: a bucket's rows (of each centre
+// type) are cut into items of at most tile_rows rows; 0 leaves them to the
+// default split (about 3 x SMs near-equal items over all rows)
+struct BatchPlan {
+  std::vector<int> row_bucket;  // bucket of every batch row
+  int tile_rows[DPGB_BATCH_BUCKETS] = {0, 0, 0, 0};
+  unsigned long long version = 0;  // from plan_versions: unique over the process
+  bool tiled() const {
+    for (int k = 0; k < DPGB_BATCH_BUCKETS; ++k)
+      if (tile_rows[k] > 0) return true;
+    return false;
+  }
+};
+
+std::atomic<unsigned long long> plan_versions{0};
+
+int bucket_of(int natoms) {
+  return natoms <= 128 ? 0 : natoms <= 512 ? 1 : natoms <= 2048 ? 2 : 3;
+}
+
+// plan: a batch's buckets and tiles (NULL: one system, or a batch without
+// tiles).  The rows of each type are ordered by bucket, then row, and the
+// work items of a tiled plan are taken from a queue, largest first.
+int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host, cudaStream_t st,
+                  const BatchPlan* plan = nullptr) {
+  if (plan && !plan->tiled()) plan = nullptr;
   const bool same = dp.cached_nframes == nframes && (int)dp.atype_cache.size() == natom &&
-                    std::equal(dp.atype_cache.begin(), dp.atype_cache.end(), atype_host);
+                    std::equal(dp.atype_cache.begin(), dp.atype_cache.end(), atype_host) &&
+                    dp.plan_owner == plan && (!plan || dp.plan_version == plan->version);
   if (same) return DPGB_OK;
+  if (plan && (nframes != 1 || (int)plan->row_bucket.size() != natom))
+    return fail(DPGB_EINVAL, "batch plan does not match the rows");
   ++dp.gen;
+  dp.cached_nframes = -1;  // until the preparation below completes
+  dp.plan_owner = plan;
+  dp.plan_version = plan ? plan->version : 0;
   const int nt = dp.desc.ntypes;
   for (int i = 0; i < natom; ++i)
     if (atype_host[i] >= nt) return fail(DPGB_EINVAL, "atom type out of range");
@@ -843,10 +883,17 @@ int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host
   // sorted position of every (frame, atom): by type, then frame, then atom
   dp.row_pos_h.assign((size_t)nframes * natom, 0);
   std::vector<int> cur(dp.type_off.begin(), dp.type_off.end() - 1);
-  for (int t = 0; t < nt; ++t)
-    for (int f = 0; f < nframes; ++f)
-      for (int i = 0; i < natom; ++i)
-        if (atype_host[i] == t) dp.row_pos_h[(size_t)f * natom + i] = cur[t]++;
+  if (plan) {
+    for (int t = 0; t < nt; ++t)
+      for (int k = 0; k < DPGB_BATCH_BUCKETS; ++k)
+        for (int i = 0; i < natom; ++i)
+          if (atype_host[i] == t && plan->row_bucket[i] == k) dp.row_pos_h[i] = cur[t]++;
+  } else {
+    for (int t = 0; t < nt; ++t)
+      for (int f = 0; f < nframes; ++f)
+        for (int i = 0; i < natom; ++i)
+          if (atype_host[i] == t) dp.row_pos_h[(size_t)f * natom + i] = cur[t]++;
+  }
   // inverse map (sorted position -> row) of the typed rows
   const int nsorted = dp.type_off[nt];
   std::vector<int> sorted_rows((size_t)std::max(nsorted, 1), 0);
@@ -886,15 +933,38 @@ int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host
       rem[best] -= 1.0;
       ++used;
     }
-    for (int t = 0; t < nt; ++t) {
-      const int r0 = dp.type_off[t], n = dp.type_off[t + 1] - r0;
-      for (int k = 0; k < per[t]; ++k) {
-        const int a = r0 + (int)((long long)k * n / per[t]), b = r0 + (int)((long long)(k + 1) * n / per[t]);
+    auto cut = [&](int r0, int n, int pieces, int t) {
+      for (int k = 0; k < pieces; ++k) {
+        const int a = r0 + (int)((long long)k * n / pieces), b = r0 + (int)((long long)(k + 1) * n / pieces);
         if (b > a) chunks.push_back(WorkChunk{a, b, t, 0});
       }
+    };
+    if (!plan) {
+      for (int t = 0; t < nt; ++t) cut(dp.type_off[t], dp.type_off[t + 1] - dp.type_off[t], per[t], t);
+    } else {
+      // per (type, bucket) segment of the sorted rows: items of at most the
+      // bucket's tile rows, or the type's default share of items
+      for (int t = 0; t < nt; ++t) {
+        const int r0 = dp.type_off[t], r1 = dp.type_off[t + 1];
+        for (int a = r0; a < r1;) {
+          const int k = plan->row_bucket[sorted_rows[a]];
+          int b = a;
+          while (b < r1 && plan->row_bucket[sorted_rows[b]] == k) ++b;
+          const int n = b - a, tile = plan->tile_rows[k];
+          const int pieces = tile > 0 ? (n + tile - 1) / tile
+                                      : std::max(1, (int)((long long)per[t] * n / std::max(r1 - r0, 1)));
+          cut(a, n, pieces, t);
+          a = b;
+        }
+      }
+      // largest items first: the queue hands the small ones out at the end
+      std::stable_sort(chunks.begin(), chunks.end(),
+                       [](const WorkChunk& x, const WorkChunk& y) { return x.row1 - x.row0 > y.row1 - y.row0; });
     }
   }
   dp.nchunks = (int)chunks.size();
+  dp.use_queue = plan ? 1 : 0;
+  if (dp.use_queue) DPGB_TRY(dp.queue_dev.alloc(2 * sizeof(int)));
   DPGB_TRY(dp.row_pos_dev.alloc(sizeof(int) * dp.row_pos_h.size()));
   DPGB_TRY(dp.atype_dev.alloc(sizeof(int) * natom));
   DPGB_TRY(dp.sorted_rows_dev.alloc(sizeof(int) * sorted_rows.size()));
@@ -911,6 +981,10 @@ int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host
   dp.cached_nframes = nframes;
   return DPGB_OK;
 }
+
+// the queue counters of the two persistent kernels (NULL without a queue)
+int* queue_fwd(DeepPotImpl& dp) { return dp.use_queue ? dp.queue_dev.as<int>() : nullptr; }
+int* queue_bwd(DeepPotImpl& dp) { return dp.use_queue ? dp.queue_dev.as<int>() + 1 : nullptr; }
 
 // An external neighbour list with explicit ghost atoms (one frame): device
 // coordinates / types of all nall atoms (local first) and a CSR list over
@@ -1249,6 +1323,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   bool tc_path = false;
   if constexpr (std::is_same<T, float>::value) tc_path = dp.use_tc != 0;
   dp.mark(DPGB_STAGE_DESC_FWD, 0, st);
+  if (dp.use_queue && (tc_path || dp.use_tab)) DPGB_CUDA(cudaMemsetAsync(dp.queue_dev.ptr, 0, 2 * sizeof(int), st));
   if constexpr (std::is_same<T, float>::value) {
     if (tc_path) {
       const int nsorted = dp.type_off[d.ntypes];
@@ -1262,7 +1337,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       e.d_bf16 = dp.use_fit_tc;
       DPGB_TRY(launch_emb_tc_fwd(p, e, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.ws_runlen.as<int>(),
                                  dp.sorted_rows_dev.as<int>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(),
-                                 dp.ws_D.as<float>(), status, st));
+                                 dp.ws_D.as<float>(), status, st, queue_fwd(dp)));
       launches += 2;
     }
   }
@@ -1272,7 +1347,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     if (tab_path) {
       DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ng));
       DPGB_TRY(launch_tab_fwd(p, m.emb, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.sorted_rows_dev.as<int>(),
-                              dp.ws_xyz.as<float>(), dp.ws_D.ptr, dp.use_fit_tc, st));
+                              dp.ws_xyz.as<float>(), dp.ws_D.ptr, dp.use_fit_tc, st, queue_fwd(dp)));
       ++launches;
     }
   }
@@ -1316,14 +1391,15 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       if (!dxyz_done) DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
       DPGB_TRY(launch_emb_tc_bwd(p, dp.tc, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.ws_runlen.as<int>(),
                                  dp.sorted_rows_dev.as<int>(), dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(),
-                                 dp.ws_vir.as<double>(), status, st));
+                                 dp.ws_vir.as<double>(), status, st, queue_bwd(dp)));
       launches += 2;
     }
     if (tab_path) {
       DPGB_CUDA(cudaMemsetAsync(dp.ws_vir.ptr, 0, sizeof(double) * nrows * 9, st));
       if (!dxyz_done) DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
       DPGB_TRY(launch_tab_bwd(p, m.emb, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.sorted_rows_dev.as<int>(),
-                              dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(), dp.ws_vir.as<double>(), st));
+                              dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(), dp.ws_vir.as<double>(), st,
+                              queue_bwd(dp)));
       launches += 2;
     }
   }
@@ -1584,6 +1660,8 @@ struct BatchImpl {
   DeepPotImpl* dp = nullptr;
   int nframes = 0, natoms = 0, ncells = 0;
   std::vector<int> atype, atom_off_h;
+  BatchPlan plan;
+  int bucket_frames[DPGB_BATCH_BUCKETS] = {}, bucket_atoms[DPGB_BATCH_BUCKETS] = {};
   DeviceBuffer atom_off, cell_off, spos_off, svec_off, geom, svec, spos;
   BatchIn in{};
   cudaGraph_t graph = nullptr;
@@ -1621,6 +1699,14 @@ int batch_setup(BatchImpl& b, DeepPotImpl& dp, int nframes, const int* natoms, c
   b.natoms = b.atom_off_h[nframes];
   b.ncells = cell_off[nframes];
   b.atype.assign(atype, atype + b.natoms);
+  b.plan.row_bucket.assign(b.natoms, 0);
+  b.plan.version = ++plan_versions;
+  for (int f = 0; f < nframes; ++f) {
+    const int k = bucket_of(natoms[f]);
+    ++b.bucket_frames[k];
+    b.bucket_atoms[k] += natoms[f];
+    std::fill(b.plan.row_bucket.begin() + b.atom_off_h[f], b.plan.row_bucket.begin() + b.atom_off_h[f + 1], k);
+  }
   DPGB_TRY(b.atom_off.alloc(sizeof(int) * (nframes + 1)));
   DPGB_TRY(b.cell_off.alloc(sizeof(int) * (nframes + 1)));
   DPGB_TRY(b.spos_off.alloc(sizeof(int) * (nframes + 1)));
@@ -1661,7 +1747,7 @@ int batch_compute(BatchImpl& b, const double* coord, double* energy, double* for
                   cudaStream_t st, int use_graph) {
   DeepPotImpl& dp = *b.dp;
   if (!coord || !energy || !force || !virial) return fail(DPGB_EINVAL, "batch: NULL argument");
-  DPGB_TRY(prepare_types(dp, 1, b.natoms, b.atype.data(), st));
+  DPGB_TRY(prepare_types(dp, 1, b.natoms, b.atype.data(), st, &b.plan));
   const void* ptrs[4] = {coord, energy, force, virial};
   const bool same = b.exec && dp.gen == b.cap_gen && st == b.cap_stream &&
                     std::equal(ptrs, ptrs + 4, b.cap_ptr);
@@ -1898,6 +1984,32 @@ dpgb_batch* dpgb_batch_new(dpgb_deeppot* dp, int nframes, const int* natoms, con
 void dpgb_batch_delete(dpgb_batch* b) { delete b; }
 
 int dpgb_batch_natoms(const dpgb_batch* b) { return b ? b->impl.natoms : -1; }
+
+int dpgb_batch_buckets(const dpgb_batch* b, int* frames, int* atoms) {
+  if (!b) return fail(DPGB_EINVAL, "batch: NULL handle");
+  for (int k = 0; k < DPGB_BATCH_BUCKETS; ++k) {
+    if (frames) frames[k] = b->impl.bucket_frames[k];
+    if (atoms) atoms[k] = b->impl.bucket_atoms[k];
+  }
+  return DPGB_OK;
+}
+
+int dpgb_batch_set_tiles(dpgb_batch* b, const int* rows_per_item) {
+  if (!b || !rows_per_item) return fail(DPGB_EINVAL, "batch: NULL argument");
+  for (int k = 0; k < DPGB_BATCH_BUCKETS; ++k)
+    if (rows_per_item[k] < 0 || rows_per_item[k] > (1 << 20)) return fail(DPGB_EINVAL, "batch: tile rows out of range");
+  BatchPlan& p = b->impl.plan;
+  if (std::equal(rows_per_item, rows_per_item + DPGB_BATCH_BUCKETS, p.tile_rows)) return DPGB_OK;
+  std::copy(rows_per_item, rows_per_item + DPGB_BATCH_BUCKETS, p.tile_rows);
+  p.version = ++plan_versions;  // the next evaluation re-cuts the items (and re-captures its graph)
+  return DPGB_OK;
+}
+
+int dpgb_batch_get_tiles(const dpgb_batch* b, int* rows_per_item) {
+  if (!b || !rows_per_item) return fail(DPGB_EINVAL, "batch: NULL argument");
+  std::copy(b->impl.plan.tile_rows, b->impl.plan.tile_rows + DPGB_BATCH_BUCKETS, rows_per_item);
+  return DPGB_OK;
+}
 
 int dpgb_batch_compute_device(dpgb_batch* b, const double* coord, double* energy, double* force, double* virial,
                               void* stream, int use_graph) {

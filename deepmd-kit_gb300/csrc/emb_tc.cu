@@ -400,7 +400,8 @@ template <int W1, int W2, int W3, bool IDT>
 __global__ void __launch_bounds__(128, 3)
 emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ chunks, int nchunks,
                   const int* __restrict__ run_len, const int* __restrict__ sorted_rows, float* __restrict__ xyz,
-                  float* __restrict__ xyzp, float* __restrict__ Dout, int* __restrict__ status) {
+                  float* __restrict__ xyzp, float* __restrict__ Dout, int* __restrict__ status,
+                  int* __restrict__ queue) {
   using P = PlanF<W1, W2, W3>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
@@ -422,7 +423,8 @@ emb_tc_fwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
   const uint32_t sA1lo = tc::smem_u32(smem + P::a1lo), sA2lo = tc::smem_u32(smem + P::a2lo);
   const uint32_t sW2 = tc::smem_u32(smem + P::fw2), sW3 = tc::smem_u32(smem + P::fw3);
   const uint32_t sW2lo = tc::smem_u32(smem + P::fw2lo), sW3lo = tc::smem_u32(smem + P::fw3lo);
-  for (int c = blockIdx.x; c < nchunks && alive; c += gridDim.x) {
+  __shared__ int s_work;
+  for (int c = work_first(queue, &s_work); c < nchunks && alive; c = work_next(queue, c, &s_work)) {
     const WorkChunk ch = chunks[c];
     const int ti = ch.ti;
     for (int t = 0; t < p.ntypes && alive; ++t) {
@@ -657,7 +659,7 @@ __global__ void __launch_bounds__(128, 3)
 emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ chunks, int nchunks,
                   const int* __restrict__ run_len, const int* __restrict__ sorted_rows,
                   const float* __restrict__ dxyz, float* __restrict__ gpair, double* __restrict__ vir_row,
-                  int* __restrict__ status) {
+                  int* __restrict__ status, int* __restrict__ queue) {
   using P = PlanB<W1, W2, W3>;
   static_assert(W2 == 2 * W1 && W3 == 2 * W2, "the backward folds doubling residuals (w2 = 2 w1, w3 = 2 w2)");
   extern __shared__ __align__(128) unsigned char smem[];
@@ -681,7 +683,8 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
   const uint32_t sW2 = tc::smem_u32(smem + P::fw2), sW3 = tc::smem_u32(smem + P::fw3);
   const uint32_t sB3 = tc::smem_u32(smem + P::bw3), sB2 = tc::smem_u32(smem + P::bw2);
   const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
-  for (int c = blockIdx.x; c < nchunks && alive; c += gridDim.x) {
+  __shared__ int s_work;
+  for (int c = work_first(queue, &s_work); c < nchunks && alive; c = work_next(queue, c, &s_work)) {
     const WorkChunk ch = chunks[c];
     const int ti = ch.ti;
     for (int q = tid; q < (ch.row1 - ch.row0) * 9; q += blockDim.x)
@@ -1097,23 +1100,24 @@ __global__ void dxyz_smem_kernel(float* __restrict__ dxyz, const float* __restri
 
 template <int W1, int W2, int W3, bool IDT>
 int launch_fwd_t(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks, const int* run_len,
-                 const int* sorted_rows, float* xyz, float* xyzp, float* D, int* status, cudaStream_t st, int nsm) {
+                 const int* sorted_rows, float* xyz, float* xyzp, float* D, int* status, cudaStream_t st, int nsm,
+                 int* queue) {
   using P = PlanF<W1, W2, W3>;
   auto k = emb_tc_fwd_kernel<W1, W2, W3, IDT>;
   DPGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, P::total));
   const int grid = nchunks < nsm ? nchunks : nsm;
-  k<<<grid, 128, P::total, st>>>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status);
+  k<<<grid, 128, P::total, st>>>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status, queue);
   return check_launch("emb_tc_fwd");
 }
 template <int W1, int W2, int W3, bool IDT>
 int launch_bwd_t(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks, const int* run_len,
                  const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, int* status, cudaStream_t st,
-                 int nsm) {
+                 int nsm, int* queue) {
   using P = PlanB<W1, W2, W3>;
   auto k = emb_tc_bwd_kernel<W1, W2, W3, IDT>;
   DPGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, P::total));
   const int grid = nchunks < nsm ? nchunks : nsm;
-  k<<<grid, 128, P::total, st>>>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status);
+  k<<<grid, 128, P::total, st>>>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status, queue);
   return check_launch("emb_tc_bwd");
 }
 
@@ -1129,11 +1133,12 @@ int launch_run_lengths(int* run_len, const int* nlist, const int* sorted_rows, i
 
 int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks,
                       const int* run_len, const int* sorted_rows, float* xyz, float* xyzp, float* D, int* status,
-                      cudaStream_t st) {
+                      cudaStream_t st, int* queue) {
   if (nchunks <= 0) return DPGB_OK;
   const int nsm = 3 * sm_count();  // three CTAs per SM
   const bool idt = e.has_idt1 || e.has_idt2 || e.has_idt3;
-#define DPGB_FWD(a, b, c, i) launch_fwd_t<a, b, c, i>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status, st, nsm)
+#define DPGB_FWD(a, b, c, i) \
+  launch_fwd_t<a, b, c, i>(p, e, chunks, nchunks, run_len, sorted_rows, xyz, xyzp, D, status, st, nsm, queue)
   if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100) return idt ? DPGB_FWD(25, 50, 100, true) : DPGB_FWD(25, 50, 100, false);
   if (e.w1 == 3 && e.w2 == 6 && e.w3 == 12) return idt ? DPGB_FWD(3, 6, 12, true) : DPGB_FWD(3, 6, 12, false);
 #undef DPGB_FWD
@@ -1159,12 +1164,12 @@ int launch_dxyz(const DescParams<float>& p, const float* dD, const float* xyz, f
 
 int launch_emb_tc_bwd(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks,
                       const int* run_len, const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row,
-                      int* status, cudaStream_t st) {
+                      int* status, cudaStream_t st, int* queue) {
   if (nchunks <= 0) return DPGB_OK;
   const int nsm = 3 * sm_count();  // three CTAs per SM
   const bool idt = e.has_idt1 || e.has_idt2 || e.has_idt3;
 #define DPGB_BWD(a, b, c, i) \
-  launch_bwd_t<a, b, c, i>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status, st, nsm)
+  launch_bwd_t<a, b, c, i>(p, e, chunks, nchunks, run_len, sorted_rows, dxyz, gpair, vir_row, status, st, nsm, queue)
   if (e.w1 == 25 && e.w2 == 50 && e.w3 == 100) return idt ? DPGB_BWD(25, 50, 100, true) : DPGB_BWD(25, 50, 100, false);
   if (e.w1 == 3 && e.w2 == 6 && e.w3 == 12) return idt ? DPGB_BWD(3, 6, 12, true) : DPGB_BWD(3, 6, 12, false);
 #undef DPGB_BWD

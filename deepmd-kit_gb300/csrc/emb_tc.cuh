@@ -61,7 +61,8 @@ struct EmbTC {
   int d_bf16;  // per call: write D as BF16 (for the tensor-core fitting)
 };
 
-// contiguous ranges of type-sorted rows processed by one CTA (same centre type)
+// contiguous ranges of type-sorted rows processed by one CTA (same centre
+// type): the work items of the persistent embedding and table kernels
 struct WorkChunk {
   int row0, row1;  // sorted-row range [row0, row1)
   int ti;          // centre type
@@ -78,15 +79,17 @@ int build_emb_tc(const dpgb_se_a_desc& d, std::vector<unsigned char>& images, Em
 void emb_tc_bind(EmbTC& meta, const unsigned char* dev_images, size_t img_bytes_per_kind, const float* dev_vec);
 size_t emb_tc_image_bytes(const EmbTC& m, int kind);  // per net: 0 fw2, 1 fw3, 2 bw3, 3 bw2, 4 fw2lo, 5 fw3lo
 
+// queue: NULL = the work items go to the CTAs in a fixed stride; else an
+// int the caller zeroed on the stream, from which the CTAs draw the items
 int launch_run_lengths(int* run_len, const int* nlist, const int* sorted_rows, int nrows, int nnei,
                        const SelInfo& sel, int pad_zero, cudaStream_t st);
 // xyzp: per-section partial xyz by accumulator column, [ntypes][nrows][4][pad16(ng)] FP32 scratch
 int launch_emb_tc_fwd(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks,
                       const int* run_len, const int* sorted_rows, float* xyz, float* xyzp, float* D, int* status,
-                      cudaStream_t st);
+                      cudaStream_t st, int* queue = nullptr);
 int launch_dxyz(const DescParams<float>& p, const float* dD, const float* xyz, float* dxyz, cudaStream_t st);
 int launch_emb_tc_bwd(const DescParams<float>& p, const EmbTC& e, const WorkChunk* chunks, int nchunks,
                       const int* run_len, const int* sorted_rows, const float* dxyz, float* gpair,
-                      double* vir_row, int* status, cudaStream_t st);
+                      double* vir_row, int* status, cudaStream_t st, int* queue = nullptr);
 
 }  // namespace dpgb

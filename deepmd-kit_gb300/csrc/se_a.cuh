@@ -237,9 +237,10 @@ size_t desc_bwd_smem(const DescParams<T>& p, const EmbParams<T>& e);
 struct WorkChunk;
 int tab_fused_eligible(int ng, int axis);
 int launch_tab_fwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
-                   const int* sorted_rows, float* xyz, void* D, int d_bf16, cudaStream_t st);
+                   const int* sorted_rows, float* xyz, void* D, int d_bf16, cudaStream_t st, int* queue = nullptr);
 int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
-                   const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, cudaStream_t st);
+                   const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, cudaStream_t st,
+                   int* queue = nullptr);
 
 // fitting of the rows [row0, row0+nrow) of one type
 template <typename T>

@@ -171,7 +171,7 @@ __device__ __forceinline__ void load_coeffs(const float* s_tab, const float* __r
 __global__ void __launch_bounds__(kFwdWarps * 32, 1)
 tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restrict__ chunks, int nchunks,
                const int* __restrict__ sorted_rows, int rows_cap, float* __restrict__ xyz, void* __restrict__ Dout,
-               int d_bf16) {
+               int d_bf16, int* __restrict__ queue) {
   extern __shared__ float4 smem4[];
   const int ng = p.ng, M = p.axis;
   float* s_tab = reinterpret_cast<float*>(smem4);
@@ -180,7 +180,8 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
   SlotBuf* my = s_slot + warp * 32;
   const float inv = 1.f / (float)p.nnei;
   const int dim = ng * M;
-  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+  __shared__ int s_work;
+  for (int c = work_first(queue, &s_work); c < nchunks; c = work_next(queue, c, &s_work)) {
     const WorkChunk ch = chunks[c];
     const int ti = ch.ti;
     for (int sec = 0; sec < p.ntypes; ++sec) {
@@ -348,7 +349,7 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
 __global__ void __launch_bounds__(kBwdWarps * 32, 1)
 tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restrict__ chunks, int nchunks,
                const int* __restrict__ sorted_rows, int rows_cap, int row_stride, const float* __restrict__ dxyz,
-               float* __restrict__ gpair, double* __restrict__ vir_row) {
+               float* __restrict__ gpair, double* __restrict__ vir_row, int* __restrict__ queue) {
   extern __shared__ float4 smem4[];
   const int ng = p.ng;
   float* s_tab = reinterpret_cast<float*>(smem4);
@@ -358,7 +359,8 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
   int* s_list = reinterpret_cast<int*>(reinterpret_cast<float4*>(tail) + (size_t)kBwdWarps * ng) +
                 (size_t)warp * p.nnei;                                                     // [warp][nnei]
   const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
-  for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+  __shared__ int s_work;
+  for (int c = work_first(queue, &s_work); c < nchunks; c = work_next(queue, c, &s_work)) {
     const WorkChunk ch = chunks[c];
     const int ti = ch.ti;
     for (int sec = 0; sec < p.ntypes; ++sec) {
@@ -503,18 +505,19 @@ int tab_rows_cap(int ng, int warps, size_t* smem) {
 }  // namespace
 
 int launch_tab_fwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
-                   const int* sorted_rows, float* xyz, void* D, int d_bf16, cudaStream_t st) {
+                   const int* sorted_rows, float* xyz, void* D, int d_bf16, cudaStream_t st, int* queue) {
   if (nchunks <= 0) return DPGB_OK;
   size_t smem = 0;
   const int rows = tab_rows_cap(p.ng, kFwdWarps, &smem);
   DPGB_CUDA(cudaFuncSetAttribute(tab_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   tab_fwd_kernel<<<std::min(nchunks, sm_count()), kFwdWarps * 32, smem, st>>>(p, e, chunks, nchunks, sorted_rows,
-                                                                               rows, xyz, D, d_bf16);
+                                                                               rows, xyz, D, d_bf16, queue);
   return check_launch("tab_fwd");
 }
 
 int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
-                   const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, cudaStream_t st) {
+                   const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, cudaStream_t st,
+                   int* queue) {
   if (nchunks <= 0) return DPGB_OK;
   // rows at an odd float2 stride; per warp the atom's dE/dxyz and its slot list
   int per2 = 3 * p.ng;
@@ -530,7 +533,8 @@ int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const 
   const size_t smem = ((size_t)rows * row_stride * 4 + 15) / 16 * 16 + (size_t)kBwdWarps * per_warp;
   DPGB_CUDA(cudaFuncSetAttribute(tab_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   tab_bwd_kernel<<<std::min(nchunks, sm_count()), kBwdWarps * 32, smem, st>>>(p, e, chunks, nchunks, sorted_rows,
-                                                                               rows, row_stride, dxyz, gpair, vir_row);
+                                                                               rows, row_stride, dxyz, gpair, vir_row,
+                                                                               queue);
   return check_launch("tab_bwd");
 }
 

@@ -125,6 +125,9 @@ _SIGS = {
     "dpgb_batch_natoms": [_P],
     "dpgb_batch_compute_device": [_P, _P, _P, _P, _P, _P, _I],
     "dpgb_batch_compute": [_P, _DP, _DP, _DP, _DP, _I],
+    "dpgb_batch_buckets": [_P, _IP, _IP],
+    "dpgb_batch_set_tiles": [_P, _IP],
+    "dpgb_batch_get_tiles": [_P, _IP],
     "dpgb_deeppot_last_launches": [_P],
     "dpgb_deeppot_last_nlist": [_P, _IP, _IP, _DP, _DP],
     "dpgb_selftest_wait_timeout": [_D, _P],

@@ -76,6 +76,16 @@ def pack_desc(params: SeAParams):
     return d, keep
 
 
+def _shape_key(d, precision: str) -> str:
+    """What a launch configuration depends on: the model's sizes (not its
+    weights) and the precision."""
+    nt = int(d.ntypes)
+    return (f"se_e2_a nt{nt} sel{[int(d.sel[i]) for i in range(nt)]} rc{float(d.rcut):g} "
+            f"emb{[int(d.emb_neuron[i]) for i in range(int(d.n_emb))]} ax{int(d.axis_neuron)} "
+            f"fit{[int(d.fit_neuron[i]) for i in range(int(d.n_fit))]} compressed{int(d.compressed)} "
+            f"one_side{int(d.type_one_side)} {precision}")
+
+
 class DeepPot:
     def __init__(self, params: SeAParams, precision: str = "fp64", device: int = 0):
         import torch
@@ -88,6 +98,7 @@ class DeepPot:
         self.device = device
         lib = _lib.lib()
         desc, keep = pack_desc(params)
+        self.shape_key = _shape_key(desc, precision)
         self._h = lib.dpgb_deeppot_new(C.byref(desc), PRECISIONS[precision])
         del keep
         if not self._h:
@@ -115,6 +126,7 @@ class DeepPot:
             self.type_map = lib.dpgb_model_file_type_map(mf).decode().split()
             desc = C.cast(lib.dpgb_model_file_desc(mf), C.POINTER(_lib.SeADesc)).contents
             self._rcut, self._ntypes = float(desc.rcut), int(desc.ntypes)
+            self.shape_key = _shape_key(desc, precision)
             self._h = lib.dpgb_deeppot_new(C.byref(desc), PRECISIONS[precision])
         finally:
             lib.dpgb_model_file_close(mf)
@@ -324,6 +336,24 @@ class DeepPotBatch:
         _lib.check(_lib.lib().dpgb_batch_compute(self._h, c.ctypes.data_as(dp), e.ctypes.data_as(dp),
                                                  f.ctypes.data_as(dp), v.ctypes.data_as(dp), int(use_graph)))
         return e, [f[self.offsets[k]:self.offsets[k + 1]] for k in range(self.nframes)], v
+
+    def buckets(self):
+        """(frames [4], atoms [4]) of the size buckets <= 128, <= 512,
+        <= 2048 and > 2048 atoms (dpgb_batch_buckets)."""
+        fr, at = (C.c_int * 4)(), (C.c_int * 4)()
+        _lib.check(_lib.lib().dpgb_batch_buckets(self._h, fr, at))
+        return list(fr), list(at)
+
+    def set_tiles(self, rows_per_item):
+        """Rows per work item of each size bucket (0 = the default split);
+        see dpgb_batch_set_tiles."""
+        t = (C.c_int * 4)(*[int(x) for x in rows_per_item])
+        _lib.check(_lib.lib().dpgb_batch_set_tiles(self._h, t))
+
+    def tiles(self):
+        t = (C.c_int * 4)()
+        _lib.check(_lib.lib().dpgb_batch_get_tiles(self._h, t))
+        return list(t)
 
     def eval_device(self, coord, out=None, use_graph: bool = False, stream=None):
         """CUDA float64 coordinates [natoms, 3] -> dict of CUDA tensors on the

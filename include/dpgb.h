@@ -556,6 +556,25 @@ int dpgb_batch_compute_device(dpgb_batch* b, const double* coord,
 int dpgb_batch_compute(dpgb_batch* b, const double* coord, double* energy,
                        double* force, double* virial, int use_graph);
 
+/* Size buckets of a batch and the work-item ("tile") size of each (no
+ * counterpart in the reference; its launch-configuration tuner registry,
+ * deepmd/kernels/autotune.py:1-87, is the precedent).  A frame of n atoms
+ * is in bucket 0 (n <= 128), 1 (<= 512), 2 (<= 2048) or 3 (more).  The
+ * persistent embedding / table kernels process the batch's rows in work
+ * items of one centre type and one bucket; with tiles set, a bucket's rows
+ * are cut into items of at most rows_per_item[k] rows (0: the default
+ * split of about 3 x SMs items over all rows) and the CTAs draw the items,
+ * largest first, from a device queue.  All zero (the default) = the
+ * default split in a fixed stride.  Results do not depend on the tiles.
+ * Setting different tiles makes the next evaluation re-cut the items and
+ * re-capture its graph. */
+#define DPGB_BATCH_BUCKETS 4
+/* frames [4], atoms [4] (either may be NULL) */
+int dpgb_batch_buckets(const dpgb_batch* b, int* frames, int* atoms);
+/* rows_per_item [4], each 0 ... 2^20 */
+int dpgb_batch_set_tiles(dpgb_batch* b, const int* rows_per_item);
+int dpgb_batch_get_tiles(const dpgb_batch* b, int* rows_per_item);
+
 /* Self-test of the bounded device-side waits (no counterpart in the
  * reference, which has no device-side waits of its own): one kernel waits
  * on an mbarrier that nothing completes, with a limit of limit_ms (0 < ...
