@@ -250,21 +250,27 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
 }
 
 // dE/dD of the first layer folded into dE/dxyz (FitDxyz).  One CTA per
-// 128-row tile walks all 16 ng columns of dD in chunks of 128 (8 neurons):
-// dP1 (high and low BF16 parts) stays in shared memory, W1 (high, then low
-// part) streams through an S-stage TMA ring, each chunk's accumulator sums
-// the three split segments and is read by the epilogue (thread = row): the
-// first term goes out per neuron, the transposed term of the first 16
-// neurons accumulates in registers and is added at the end.
-constexpr int kDxM = 16, kDxBN = 128, kDxStages = 5, kDxSeg = 3;
+// 128-row tile walks all 16 ng columns of dD in chunks of 128 (8 neurons),
+// with its warps specialised: warp 4 loads (dP1 high and low BF16 parts once
+// into shared memory, then W1 — per K chunk the high part, then the low
+// part — through an S-stage TMA ring), warp 5 issues the MMAs of a chunk
+// (the three split products dP hi . W hi, dP lo . W hi and dP hi . W lo
+// summed in one accumulator; a W hi stage serves the first two) into one of
+// two TMEM buffers, and
+// warps 0-3 (thread = row) read the other buffer: the first term goes out
+// per neuron, the transposed term of the first 16 neurons accumulates in
+// registers and is added at the end.  The MMAs of chunk j + 1 run while the
+// epilogue reads chunk j.
+constexpr int kDxM = 16, kDxBN = 128, kDxStages = 5, kDxSeg = 2;
+constexpr int kDxThreads = 192;  // 4 epilogue warps, the load warp, the MMA warp
 
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(kDxThreads, 1)
 fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_alo,
                 const __grid_constant__ CUtensorMap tma_b, FitDxyz f, int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
   constexpr int SA = 128 * kKC * 2, SB = kDxBN * kKC * 2, M = kDxM, S = kDxStages;
-  __shared__ uint64_t full[S], empty[S], a_full, acc;
+  __shared__ uint64_t full[S], empty[S], a_full, acc_full[2], acc_free[2], mma_done;
   __shared__ uint32_t s_tmem;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   int t = 0;
@@ -272,51 +278,96 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   const int m0 = f.row0[t] + ((int)blockIdx.x - f.tile0[t]) * 128;
   const int rows_valid = min(128, f.row0[t + 1] - m0);
   const int ncol = f.ng * M, nk = (f.K + kKC - 1) / kKC, nchunk = (ncol + kDxBN - 1) / kDxBN;
-  const int per = kDxSeg * nk;  // B loads of one column chunk: segment-major, K chunks inside
+  const int per = kDxSeg * nk;  // B loads of one column chunk: W hi over K, then W lo over K
   const int L = nchunk * per;   // B loads
-  unsigned char* sA = smem;              // nk stages of dP1 (high part)
-  unsigned char* sAlo = smem + nk * SA;  // nk stages of dP1 (low part)
+  unsigned char* sA = smem;                // nk stages of dP1 (high part)
+  unsigned char* sAlo = smem + nk * SA;    // nk stages of dP1 (low part)
   unsigned char* sB = smem + 2 * nk * SA;  // ring
-  if (warp == 0) tc::tmem_alloc(&s_tmem, kDxBN);
+  if (warp == 0) tc::tmem_alloc(&s_tmem, 2 * kDxBN);
   if (tid == 0) {
     for (int q = 0; q < S; ++q) {
       tc::mbar_init(&full[q], 1);
       tc::mbar_init(&empty[q], 1);
     }
     tc::mbar_init(&a_full, 1);
-    tc::mbar_init(&acc, 1);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&acc_full[b], 1);
+      tc::mbar_init(&acc_free[b], 4);  // one arrival per epilogue warp
+    }
+    tc::mbar_init(&mma_done, 1);
     tc::fence_mbar_init();
   }
   __syncthreads();
   tc::fence_after();
   const uint32_t tbase = s_tmem;
   bool ok = true;
-  int next = 0;  // next B load
-  auto load_b = [&](int upto) {
-    for (; next < upto && next < L && ok; ++next) {
-      const int q = next % S;
-      if (next >= S) ok = tc::mbar_wait(&empty[q], ((next / S) - 1) & 1, err);
-      if (!ok) break;
-      const int j = next / per, rem = next - j * per, sg = rem / nk, k = rem - sg * nk;
-      tc::mbar_expect_tx(&full[q], SB);
-      // segments: dP hi . W hi, dP lo . W hi, dP hi . W lo
-      tc::tma_load_2d(tc::smem_u32(sB + q * SB), &tma_b, (sg == 2 ? f.Kp : 0) + k * kKC, t * ncol + j * kDxBN,
-                      &full[q]);
+  if (warp == 4) {
+    if (lane == 0) {
+      tc::mbar_expect_tx(&a_full, 2 * nk * SA);
+      for (int k = 0; k < nk; ++k) {
+        tc::tma_load_2d(tc::smem_u32(sA + k * SA), &tma_a, k * kKC, m0, &a_full);
+        tc::tma_load_2d(tc::smem_u32(sAlo + k * SA), &tma_alo, k * kKC, m0, &a_full);
+      }
+      int next = 0;
+      for (; next < L && ok; ++next) {
+        const int q = next % S;
+        if (next >= S) ok = tc::mbar_wait(&empty[q], ((next / S) - 1) & 1, err);
+        if (!ok) break;
+        const int j = next / per, rem = next - j * per, sg = rem / nk, k = rem - sg * nk;
+        tc::mbar_expect_tx(&full[q], SB);
+        tc::tma_load_2d(tc::smem_u32(sB + q * SB), &tma_b, (sg == 1 ? f.Kp : 0) + k * kKC, t * ncol + j * kDxBN,
+                        &full[q]);
+      }
+      if (!ok) {
+        // a wait ran out: let the copies already issued land before the CTA
+        // ends (bounded; the most recent load of each stage)
+        tc::mbar_wait(&a_full, 0, nullptr);
+        for (int i = max(0, next - S); i < next; ++i) tc::mbar_wait(&full[i % S], (i / S) & 1, nullptr);
+      }
     }
-  };
-  if (warp == 1 && lane == 0) {
-    tc::mbar_expect_tx(&a_full, 2 * nk * SA);
-    for (int k = 0; k < nk; ++k) {
-      tc::tma_load_2d(tc::smem_u32(sA + k * SA), &tma_a, k * kKC, m0, &a_full);
-      tc::tma_load_2d(tc::smem_u32(sAlo + k * SA), &tma_alo, k * kKC, m0, &a_full);
+    __syncwarp();
+  } else if (warp == 5) {
+    if (lane == 0) {
+      ok = tc::mbar_wait(&a_full, 0, err);
+      for (int j = 0; j < nchunk && ok; ++j) {
+        const int b = j & 1;
+        // the epilogue has read chunk j - 2 out of this buffer
+        if (j >= 2) ok = tc::mbar_wait(&acc_free[b], ((j >> 1) - 1) & 1, err);
+        if (!ok) break;
+        tc::fence_after();
+        const int nt = min(kDxBN, ncol - j * kDxBN);  // 128 or a multiple of 16
+        const uint32_t idesc = tc::idesc_bf16_f32(128, nt);
+        const uint32_t dst = tbase + (uint32_t)(b * kDxBN);
+        for (int u = 0; u < per && ok; ++u) {
+          const int i = j * per + u, q = i % S, sg = u / nk, k = u - sg * nk;
+          ok = tc::mbar_wait(&full[q], (i / S) & 1, err);
+          if (!ok) break;
+          tc::fence_after();
+          const uint32_t a0 = tc::smem_u32(sA + k * SA), alo = tc::smem_u32(sAlo + k * SA);
+          const uint32_t b0 = tc::smem_u32(sB + q * SB);
+#pragma unroll
+          for (int ks = 0; ks < kKC / 16; ++ks)
+            tc::mma_bf16(dst, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc,
+                         (u > 0 || ks > 0) ? 1u : 0u);
+          if (sg == 0)  // the same W hi stage with dP lo
+#pragma unroll
+            for (int ks = 0; ks < kKC / 16; ++ks)
+              tc::mma_bf16(dst, tc::smem_desc_sw128(alo + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc, 1u);
+          tc::mma_commit(&empty[q]);
+        }
+        tc::mma_commit(&acc_full[b]);
+      }
+      // every MMA issued has completed before the accumulator is freed
+      tc::mma_commit(&mma_done);
+      tc::mbar_wait(&mma_done, 0, nullptr);
     }
-    load_b(S);
+    __syncwarp();
   }
-  // the row's xyz[c][m < 16]; the transposed term of neurons m < 16.  Two
-  // warpgroups share the rows (TMEM lanes) and take alternate halves of a
-  // chunk's neurons.
-  const int r = (warp & 3) * 32 + lane, wg = warp >> 2;
-  const bool valid = r < rows_valid;
+  // epilogue warps: the row's xyz[c][m < 16]; the transposed term of
+  // neurons m < 16
+  const int r = (warp & 3) * 32 + lane;
+  const bool epi = warp < 4;
+  const bool valid = epi && r < rows_valid;
   const int row = valid ? f.sorted_rows[m0 + r] : 0;
   const float* xr = f.xyz + (size_t)row * 4 * f.ng;
   float4* out = reinterpret_cast<float4*>(f.dxyz + (size_t)row * 4 * f.ng);
@@ -329,95 +380,76 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
       T2[c][m] = 0.f;
     }
   const float inv = 1.f / (float)f.nnei;
-  for (int j = 0; j < nchunk && ok; ++j) {
-    const int nt = min(kDxBN, ncol - j * kDxBN);  // 128 or a multiple of 16
-    if (warp == 0 && lane == 0) {
-      if (j == 0) ok = tc::mbar_wait(&a_full, 0, err);
-      const uint32_t idesc = tc::idesc_bf16_f32(128, nt);
-      for (int u = 0; u < per && ok; ++u) {
-        const int i = j * per + u, q = i % S, sg = u / nk, k = u - sg * nk;
-        ok = tc::mbar_wait(&full[q], (i / S) & 1, err);
-        if (!ok) break;
-        tc::fence_after();
-        const uint32_t a0 = tc::smem_u32((sg == 1 ? sAlo : sA) + k * SA), b0 = tc::smem_u32(sB + q * SB);
-#pragma unroll
-        for (int ks = 0; ks < kKC / 16; ++ks)
-          tc::mma_bf16(tbase, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc,
-                       (u > 0 || ks > 0) ? 1u : 0u);
-        tc::mma_commit(&empty[q]);
-      }
-      tc::mma_commit(&acc);
-    } else if (warp == 1 && lane == 0) {
-      // the rest of this chunk's B loads, each as soon as the MMA that read
-      // its stage last has completed (a chunk needs more loads than stages)
-      load_b((j + 1) * per);
-    }
-    __syncwarp();
-    // this warpgroup's neurons of the chunk and their xyz[c][n], loaded
-    // while the MMAs run
-    constexpr int NH = kDxBN / M / 2;
-    const int q0 = wg * NH, q1 = min(nt / M, (wg + 1) * NH);
-    float xq[NH][4];
+  constexpr int NH = kDxBN / M;  // neurons per chunk
+  float xqn[NH][4];                // xyz[c][n] of the next chunk's neurons, in flight
+  auto load_xq = [&](int j) {
+    const int qn = j < nchunk ? min(kDxBN, ncol - j * kDxBN) / M : 0;
 #pragma unroll
     for (int h = 0; h < NH; ++h)
 #pragma unroll
-      for (int c = 0; c < 4; ++c)
-        xq[h][c] = (valid && q0 + h < q1) ? xr[c * f.ng + j * (kDxBN / M) + q0 + h] : 0.f;
-    ok = tc::mbar_wait(&acc, j & 1, err) && ok;
-    tc::fence_after();
+      for (int c = 0; c < 4; ++c) xqn[h][c] = (valid && h < qn) ? xr[c * f.ng + j * NH + h] : 0.f;
+  };
+  if (epi) {
+    load_xq(0);
+    for (int j = 0; j < nchunk && ok; ++j) {
+      const int b = j & 1;
+      const int nt = min(kDxBN, ncol - j * kDxBN);
+      const int q1 = nt / M;
+      float xq[NH][4];
 #pragma unroll
-    for (int h = 0; h < NH; ++h) {
-      const int q = q0 + h;
-      if (q >= q1) break;
-      const int n = j * (kDxBN / M) + q;
-      float v[16];
-      tc::tmem_ld16(tc::taddr(tbase, (warp & 3) * 32, q * M), v);
-      tc::tmem_ld_wait();
-      if (!valid) continue;
-      float t1[4], xn[4];
+      for (int h = 0; h < NH; ++h)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        float sacc = 0.f;
+        for (int c = 0; c < 4; ++c) xq[h][c] = xqn[h][c];
+      load_xq(j + 1);
+      ok = tc::mbar_wait(&acc_full[b], (j >> 1) & 1, err);
+      ok = __all_sync(0xffffffffu, ok) != 0;  // the TMEM loads below are warp-wide
+      if (!ok) break;
+      tc::fence_after();
 #pragma unroll
-        for (int m = 0; m < M; ++m) sacc = fmaf(v[m], xm[c][m], sacc);
-        t1[c] = sacc;
-        xn[c] = xq[h][c];
+      for (int h = 0; h < NH; ++h) {
+        const int q = h;
+        if (q >= q1) break;
+        const int n = j * NH + q;
+        float v[16];
+        tc::tmem_ld16(tc::taddr(tbase + (uint32_t)(b * kDxBN), (warp & 3) * 32, q * M), v);
+        tc::tmem_ld_wait();
+        if (!valid) continue;
+        float t1[4], xn[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          float sacc = 0.f;
+#pragma unroll
+          for (int m = 0; m < M; ++m) sacc = fmaf(v[m], xm[c][m], sacc);
+          t1[c] = sacc;
+          xn[c] = xq[h][c];
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+          for (int m = 0; m < M; ++m) T2[c][m] = fmaf(v[m], xn[c], T2[c][m]);
+        if (n < M)  // completed with the transposed term below
+          out[n] = make_float4(t1[0], t1[1], t1[2], t1[3]);
+        else
+          out[n] = make_float4(t1[0] * inv, t1[1] * inv, t1[2] * inv, t1[3] * inv);
       }
-#pragma unroll
-      for (int c = 0; c < 4; ++c)
-#pragma unroll
-        for (int m = 0; m < M; ++m) T2[c][m] = fmaf(v[m], xn[c], T2[c][m]);
-      if (n < M)  // completed with the transposed term below
-        out[n] = make_float4(t1[0], t1[1], t1[2], t1[3]);
-      else
-        out[n] = make_float4(t1[0] * inv, t1[1] * inv, t1[2] * inv, t1[3] * inv);
+      // this warp has read buffer b: the MMAs of chunk j + 2 may overwrite it
+      tc::fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&acc_free[b]);
     }
-    tc::fence_before();
-    ok = __syncthreads_and(ok) != 0;  // the accumulator is read: the next chunk may overwrite it
-    tc::fence_after();
-    if (warp == 1 && lane == 0) load_b((j + 1) * per + S);
   }
-  // the second warpgroup's transposed-term partials to the first (the ring
-  // is free now), which completes neurons m < 16
-  float* s_t2 = reinterpret_cast<float*>(sB);
-  if (ok && wg == 1)
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-#pragma unroll
-      for (int m = 0; m < M; ++m) s_t2[(c * M + m) * 128 + r] = T2[c][m];
-  __syncthreads();
-  if (ok && valid && wg == 0)
+  // the transposed term completes neurons m < 16
+  ok = __syncthreads_and(ok) != 0;
+  if (ok && valid)
 #pragma unroll
     for (int m = 0; m < M; ++m) {
       const float4 a = out[m];
-      out[m] = make_float4((a.x + (T2[0][m] + s_t2[(0 * M + m) * 128 + r])) * inv,
-                           (a.y + (T2[1][m] + s_t2[(1 * M + m) * 128 + r])) * inv,
-                           (a.z + (T2[2][m] + s_t2[(2 * M + m) * 128 + r])) * inv,
-                           (a.w + (T2[3][m] + s_t2[(3 * M + m) * 128 + r])) * inv);
+      out[m] = make_float4((a.x + T2[0][m]) * inv, (a.y + T2[1][m]) * inv, (a.z + T2[2][m]) * inv,
+                           (a.w + T2[3][m]) * inv);
     }
   tc::fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, kDxBN);
+  if (warp == 0) tc::tmem_dealloc(tbase, 2 * kDxBN);
 }
 
 // cuTensorMapEncodeTiled, taken from the driver through the runtime
@@ -498,7 +530,7 @@ int launch_fit_dxyz(const FitDxyz& f, int* err, cudaStream_t st) {
   DPGB_TRY(encode_bf16_2d(&ta, f.A, f.row0[f.ntypes], f.K, f.lda, 128));
   DPGB_TRY(encode_bf16_2d(&talo, f.A_lo, f.row0[f.ntypes], f.K, f.lda, 128));
   DPGB_TRY(encode_bf16_2d(&tb, f.B, f.ntypes * f.ng * kDxM, 2 * f.Kp, 2 * f.Kp, kDxBN));
-  fit_dxyz_kernel<<<f.tile0[f.ntypes], 256, smem, st>>>(ta, talo, tb, f, err);
+  fit_dxyz_kernel<<<f.tile0[f.ntypes], kDxThreads, smem, st>>>(ta, talo, tb, f, err);
   return check_launch("fit_dxyz");
 }
 

@@ -340,7 +340,9 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
 // Backward: one lane per real pair.  The warp first lists the slots of the
 // atom's section that hold a neighbour (in a per-warp shared list; padding
 // slots get a zero gradient), then takes them 32 at a time: each lane forms
-// its pair's environment and walks all neurons of its interval's row,
+// its pair's environment and walks all neurons of its interval's staged row
+// (a pair whose row is not staged is walked by the whole warp, one neuron
+// per lane, after the others),
 // G and G' in one Horner pass, dR~[c] += G dX[c] and P[c] += G' dX[c]
 // (ds = sum_c R~[c] P[c]) with dX[n] broadcast from the warp's copy of the
 // atom's dE/dxyz.  Everything is summed in the lane: no cross-lane
@@ -405,9 +407,13 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             table_locate(tm, s.rn[0], s.idx, s.xx, s.delta);
           }
           const bool act = mine && s.active;  // excluded type pairs carry no gradient
+          // a pair whose interval's row is not staged (the closest
+          // neighbours) is walked by the whole warp below, so that the
+          // lane-per-pair loop reads shared memory only
+          const bool glob = act && s.idx >= rows;
           float dR[4] = {0.f, 0.f, 0.f, 0.f}, Pc[4] = {0.f, 0.f, 0.f, 0.f};
-          if (act) {
-            const float* rowc = s.idx < rows ? s_tab + (size_t)s.idx * row_stride : tab + (size_t)s.idx * 6 * ng;
+          if (act && !glob) {
+            const float* rowc = s_tab + (size_t)s.idx * row_stride;
             const float xx = s.xx, dl = s.delta;
             // two neurons per step, each into its own partial sums (two
             // independent chains for the scheduler), added at the end
@@ -437,6 +443,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
               pc[3] = fmaf(Gp, d.w, pc[3]);
             };
             int n = 0;
+#pragma unroll 2
             for (; n + 1 < ng; n += 2) {
               neuron(n, dR, Pc);
               neuron(n + 1, dR2, Pc2);
@@ -446,6 +453,55 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             for (int cc = 0; cc < 4; ++cc) {
               dR[cc] += dR2[cc];
               Pc[cc] += Pc2[cc];
+            }
+          }
+          // rows in global memory: lane l takes neurons l, l + 32, ... of
+          // the pair's row (coalesced reads), then fixed-order warp sums
+          unsigned gm = __ballot_sync(0xffffffffu, glob);
+          while (gm) {
+            const int src = __ffs(gm) - 1;
+            gm &= gm - 1;
+            const int gi = __shfl_sync(0xffffffffu, s.idx, src);
+            const float gx = __shfl_sync(0xffffffffu, s.xx, src), gd = __shfl_sync(0xffffffffu, s.delta, src);
+            const float2* grow = reinterpret_cast<const float2*>(tab + (size_t)gi * 6 * ng);
+            float r[4] = {0.f, 0.f, 0.f, 0.f}, pc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int j = 0; j < kTabJ; ++j) {
+              const int n = lane + 32 * j;
+              if (n < ng) {
+                const float2 x0 = __ldg(grow + 3 * n), x1 = __ldg(grow + 3 * n + 1), x2 = __ldg(grow + 3 * n + 2);
+                const float4 d = s_dx[n];
+                float G = fmaf(x2.y, gx, x2.x), Gp = x2.y;
+                Gp = fmaf(Gp, gx, G);
+                G = fmaf(G, gx, x1.y);
+                Gp = fmaf(Gp, gx, G);
+                G = fmaf(G, gx, x1.x);
+                Gp = fmaf(Gp, gx, G);
+                G = fmaf(G, gx, x0.y);
+                Gp = fmaf(Gp, gx, G);
+                G = fmaf(G, gx, x0.x);
+                G = fmaf(Gp, gd, G);
+                r[0] = fmaf(G, d.x, r[0]);
+                r[1] = fmaf(G, d.y, r[1]);
+                r[2] = fmaf(G, d.z, r[2]);
+                r[3] = fmaf(G, d.w, r[3]);
+                pc[0] = fmaf(Gp, d.x, pc[0]);
+                pc[1] = fmaf(Gp, d.y, pc[1]);
+                pc[2] = fmaf(Gp, d.z, pc[2]);
+                pc[3] = fmaf(Gp, d.w, pc[3]);
+              }
+            }
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+              r[cc] = warp_sum(r[cc]);
+              pc[cc] = warp_sum(pc[cc]);
+            }
+            if (lane == src) {
+#pragma unroll
+              for (int cc = 0; cc < 4; ++cc) {
+                dR[cc] = r[cc];
+                Pc[cc] = pc[cc];
+              }
             }
           }
           if (mine) {
