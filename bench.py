@@ -597,8 +597,8 @@ def run_train(args, world, rank, local):
     loss_params = dict(start_pref_e=0.02, limit_pref_e=0.02, start_pref_f=1000.0, limit_pref_f=1000.0)
     n_total = args.warmup + args.steps
 
-    def trainer(device_frames):
-        m = EnergyModelSeA.from_params(P.init_params(cfg, seed=1), device=dev)
+    def trainer(device_frames, precision="float64"):
+        m = EnergyModelSeA.from_params(P.init_params(cfg, seed=1), device=dev, precision=precision)
         fs = FrameSet(coord, atype, box, energy=e_lab, force=f_lab, batch_size=nf,
                       device=dev if device_frames else None)
         return Trainer(m, LearningRateExp(start_lr=1e-3, stop_lr=1e-5, num_steps=2 * n_total), fs,
@@ -629,6 +629,7 @@ def run_train(args, world, rank, local):
     with ClockSampler(local, busy=tr.step) as clk:
         t_ms = timed(tr, False)
     t_e2e = timed(trainer(False), True)
+    t32 = timed(trainer(True, "float32"), False)  # the reference's single-precision option
     value = world * nf * nloc * args.steps / (t_ms * 1e-3)
     e2e = world * nf * nloc * args.steps / (t_e2e * 1e-3)
     if rank != 0:
@@ -640,6 +641,8 @@ def run_train(args, world, rank, local):
         "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD_NAME["train16"], "frames": nf, "atoms_per_frame": nloc,
+                   "float32_ms_per_step": t32 / args.steps,
+                   "float32_atom_steps_per_s": world * nf * nloc * args.steps / (t32 * 1e-3),
                    "l2": "flushed between timed steps (256 MB fill)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e, "unit": "atom-steps/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 8},
         "roofline": None,

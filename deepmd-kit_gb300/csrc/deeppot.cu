@@ -445,6 +445,10 @@ struct DeepPotImpl {
   std::vector<double> sg_box;
   const void* sg_ptr[6] = {};
   cudaEvent_t sg_ev_in = nullptr, sg_ev_out = nullptr;
+  // completion of the last evaluation on the caller's stream (the device
+  // forms run there, not on `stream`): the status check and the list read
+  // without a stream of their own wait for it
+  cudaEvent_t last_done = nullptr;
   // side stream of the sorted transpose (needed only by the force gather, so
   // it runs next to the descriptor and the fitting), fork / join events
   cudaStream_t side = nullptr;
@@ -1791,6 +1795,17 @@ struct dpgb_deeppot {
   DeepPotImpl impl;
 };
 
+namespace dpgb {
+namespace {
+// record the completion of an evaluation issued on st
+int mark_done(DeepPotImpl& im, cudaStream_t st) {
+  if (!im.last_done) DPGB_CUDA(cudaEventCreateWithFlags(&im.last_done, cudaEventDisableTiming));
+  DPGB_CUDA(cudaEventRecord(im.last_done, st));
+  return DPGB_OK;
+}
+}  // namespace
+}  // namespace dpgb
+
 extern "C" {
 
 dpgb_deeppot* dpgb_deeppot_new(const dpgb_se_a_desc* desc, int precision) {
@@ -1883,6 +1898,10 @@ void dpgb_deeppot_delete(dpgb_deeppot* dp) {
   if (dp->impl.ev_join) cudaEventDestroy(dp->impl.ev_join);
   if (dp->impl.sg_ev_in) cudaEventDestroy(dp->impl.sg_ev_in);
   if (dp->impl.sg_ev_out) cudaEventDestroy(dp->impl.sg_ev_out);
+  if (dp->impl.last_done) {
+    cudaEventSynchronize(dp->impl.last_done);
+    cudaEventDestroy(dp->impl.last_done);
+  }
   delete dp;
 }
 
@@ -1905,6 +1924,7 @@ int dpgb_deeppot_last_nlist(dpgb_deeppot* dp, int* info, int* nlist, double* coo
   }
   const size_t nrows = (size_t)im.nl_nframes * im.nl_natom;
   cudaStream_t st = im.stream;
+  if (im.last_done) DPGB_CUDA(cudaStreamWaitEvent(st, im.last_done, 0));  // the list is complete
   if (nlist)
     DPGB_CUDA(cudaMemcpyAsync(nlist, im.ws_nlist.ptr, sizeof(int) * nrows * im.sel.nnei, cudaMemcpyDeviceToHost, st));
   if (coord) DPGB_CUDA(cudaMemcpyAsync(coord, im.ws_coord.ptr, sizeof(double) * nrows * 3, cudaMemcpyDeviceToHost, st));
@@ -1959,6 +1979,7 @@ int dpgb_deeppot_compute_device(dpgb_deeppot* dp, int nframes, int natom, const 
   if (!dp) return fail(DPGB_EINVAL, "NULL handle");
   int rc = compute_device_impl(dp->impl, nframes, natom, coord, atype_host, box_host, energy, force, virial,
                                atom_energy, atom_virial, as_stream(stream));
+  if (rc == DPGB_OK) rc = mark_done(dp->impl, as_stream(stream));
   dp->impl.err = rc == DPGB_OK ? "" : dpgb_last_error();
   return rc;
 }
@@ -2018,6 +2039,7 @@ int dpgb_batch_compute_device(dpgb_batch* b, const double* coord, double* energy
   cudaStream_t st = as_stream(stream);
   if (!st) st = b->owner->impl.stream;  // graphs cannot be captured on the legacy stream
   int rc = batch_compute(b->impl, coord, energy, force, virial, st, use_graph);
+  if (rc == DPGB_OK) rc = mark_done(b->owner->impl, st);
   if (rc == DPGB_OK && !stream) rc = check_cuda(cudaStreamSynchronize(st), "batch");
   b->owner->impl.err = rc == DPGB_OK ? "" : dpgb_last_error();
   return rc;
@@ -2133,7 +2155,10 @@ int dpgb_deeppot_check_status(dpgb_deeppot* dp, void* stream) {
   DeepPotImpl& im = dp->impl;
   if (!im.ws_status.ptr) return DPGB_OK;
   cudaStream_t st = as_stream(stream);
-  if (!st) st = im.stream;
+  if (!st) {  // the last evaluation's stream, through its completion event
+    st = im.stream;
+    if (im.last_done) DPGB_CUDA(cudaStreamWaitEvent(st, im.last_done, 0));
+  }
   const int rc = check_status(im, st);
   im.err = rc == DPGB_OK ? "" : dpgb_last_error();
   return rc;

@@ -499,7 +499,8 @@ int dpgb_deeppot_set_skin(dpgb_deeppot* dp, double skin, int every);
  * releases the graph. */
 int dpgb_deeppot_set_graph(dpgb_deeppot* dp, int on);
 
-/* Waits for `stream` (NULL: the handle's stream) and reports the
+/* Waits for `stream` (NULL: the stream of the last device-form evaluation,
+ * else the handle's stream) and reports the
  * device-side errors of the last evaluation: neighbour overflow, skin
  * candidate truncation, a timed-out tensor-core wait.  The device form
  * (dpgb_deeppot_compute_device) does not synchronise, so its caller reads
@@ -590,7 +591,8 @@ int dpgb_deeppot_last_launches(dpgb_deeppot* dp);
 /* The neighbour list the last single-system evaluation built for itself,
  * for verification (no counterpart in the reference, where the list stays
  * inside DeepPot::compute: source/api_cc/src/DeepPotPT.cc:170-243).  HOST
- * buffers; waits for the handle's stream:
+ * buffers; waits for that evaluation to complete (on whichever stream it
+ * ran):
  *   info [4]  <- nframes, natom, nnei (= sum(sel)), nshift (0 frames: the
  *                last evaluation had no list of its own — none yet, an
  *                external list or a batch; then the other pointers must be

@@ -225,3 +225,30 @@ def test_external_neighbour_list_reuse(cuda, water_fp64):
     fl, fml = _fold(f2, mapping, nloc), _fold(fm, mapping, nloc)
     assert float(np.sqrt(np.mean((fml - fl) ** 2))) <= 1e-3
     assert abs(em - e2) / nloc < 2e-4
+
+
+def test_list_read_waits_for_the_callers_stream(cuda):
+    """The device form runs on the caller's stream; reading the list back
+    (and the status words) afterwards waits for that evaluation even while
+    it is still queued behind other work on that stream."""
+    import torch
+
+    from dpgb import synth
+    from dpgb.deeppot import DeepPot
+
+    coord, atype, box = synth.water_box(8, seed=5)
+    dp = DeepPot(water_params(), "fp64")
+    x = torch.tensor(coord.reshape(1, -1), dtype=torch.float64, device="cuda")
+    dp.eval_device(x, box.reshape(1, 9), atype)
+    torch.cuda.synchronize()
+    first = dp.last_nlist()[0]
+    x2 = x + torch.randn(x.shape, dtype=x.dtype, device="cuda", generator=torch.Generator("cuda").manual_seed(3)) * 0.05
+    torch.cuda.synchronize()
+    torch.cuda._sleep(200_000_000)  # ~0.1 s of work queued ahead of the evaluation
+    dp.eval_device(x2, box.reshape(1, 9), atype)
+    early = dp.last_nlist()[0]
+    dp.check_status()
+    torch.cuda.synchronize()
+    late = dp.last_nlist()[0]
+    assert not np.array_equal(first, late)  # the walk changed the list
+    np.testing.assert_array_equal(early, late)

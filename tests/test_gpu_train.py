@@ -90,3 +90,42 @@ def test_training_lowers_the_loss(cuda):
     r = [h["trn"]["rmse"] for h in hist]
     assert all(b < a for a, b in zip(r, r[1:])), r
     assert abs(r[0] - 1.35) < 0.01 and r[-1] < 0.25 * r[0], r
+
+
+def test_float32_training_step_tracks_float64(cuda):
+    """The reference's single-precision option (descriptor and fitting
+    ``precision: float32``): the force-loss gradient of the FP32 model
+    against the FP64 model's on the same weights — per-tensor norms within
+    1e-3 relative, the loss within 1e-5 — and six Adam steps giving the
+    FP64 trajectory's losses within 1e-3."""
+    import torch
+
+    from dpgb import params as P
+    from dpgb.model import EnergyModelSeA
+    from dpgb.train import FrameSet, LearningRateExp, Trainer
+
+    g = golden("train_steps")
+    coord, atype, box = _frames()
+    e, f = g["energy_label"], g["force_label"]
+    out = {}
+    for prec in ("float64", "float32"):
+        m = EnergyModelSeA.from_params(P.init_params(P.water_config(), seed=1), device=cuda, precision=prec)
+        tr = Trainer(m, LearningRateExp(start_lr=1e-3, stop_lr=1e-5, num_steps=6),
+                     FrameSet(coord[:12], atype, box[:12], energy=e[:12], force=f[:12], batch_size=4),
+                     loss_params=dict(start_pref_e=0.02, limit_pref_e=1.0, start_pref_f=1000.0, limit_pref_f=1.0),
+                     disp_freq=10 ** 9, disp_file=None)
+        losses, norms = [], None
+        for k in range(6):
+            tr.step()
+            losses.append(float(tr.last_loss))
+            if k == 0:
+                norms = {n: float(p.grad.double().norm()) for n, p in m.named_parameters() if p.grad is not None}
+        out[prec] = (np.array(losses), norms)
+    l64, n64 = out["float64"]
+    l32, n32 = out["float32"]
+    assert abs(l32[0] - l64[0]) <= 1e-5 * abs(l64[0])
+    vmax = max(n64.values())
+    for name, v in n64.items():
+        assert abs(n32[name] - v) <= 1e-3 * max(v, 1e-3 * vmax), (name, n32[name], v)
+    np.testing.assert_allclose(l32, l64, rtol=1e-3)
+    np.testing.assert_allclose(l64, g["loss"], rtol=1e-9)
