@@ -449,6 +449,13 @@ struct DeepPotImpl {
   // forms run there, not on `stream`): the status check and the list read
   // without a stream of their own wait for it
   cudaEvent_t last_done = nullptr;
+  // descriptor stage on its own (dpgb_deeppot_descrpt_fwd / _bwd): the
+  // forward's parameters and extended layout, kept for its backward
+  DescParams<float> dm_p{};
+  int dm_nf = 0, dm_nloc = 0, dm_nall = 0;
+  unsigned long long evals = 0;    // evaluations and descriptor forwards issued (they share the workspace)
+  unsigned long long dm_eval = 0;  // the descriptor forward's number; 0: none
+  DeviceBuffer dm_keys, dm_tr;
   // side stream of the sorted transpose (needed only by the force gather, so
   // it runs next to the descriptor and the fitting), fork / join events
   cudaStream_t side = nullptr;
@@ -1023,6 +1030,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   const long long nrows = (long long)nframes * natom;
   if (nrows >= (1LL << 31) / std::max(nnei, 1)) return fail(DPGB_EINVAL, "too many atoms for 32-bit pair ids");
   if ((ext || batch) && nframes != 1) return fail(DPGB_EINVAL, "an external list or a batch runs as one frame");
+  ++dp.evals;
   int launches = 0;
   const bool own_geom = !ext && !batch;
   const bool skin_on = own_geom && box_host && dp.skin > 0.0;
@@ -1482,6 +1490,188 @@ int check_status(DeepPotImpl& dp, cudaStream_t st) {
   return status_result(dp, h);
 }
 
+// ---- the descriptor stage on its own (mixed form) -------------------------
+
+// out[row] = in[row_pos[row]] over dim values (typed rows; a virtual row is zero)
+__global__ void unsort_rows_kernel(float* __restrict__ out, const float* __restrict__ in, const int* __restrict__ row_pos,
+                                   const int* __restrict__ atype, int nloc, long long total, int dim) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= total) return;
+  const long long row = q / dim;
+  const int k = (int)(q - row * dim);
+  out[q] = atype[row % nloc] < 0 ? 0.f : in[(size_t)row_pos[row] * dim + k];
+}
+// out[row_pos[row]] = in[row]
+__global__ void sort_rows_kernel(float* __restrict__ out, const float* __restrict__ in, const int* __restrict__ row_pos,
+                                 const int* __restrict__ atype, int nloc, long long total, int dim) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= total) return;
+  const long long row = q / dim;
+  const int k = (int)(q - row * dim);
+  if (atype[row % nloc] >= 0) out[(size_t)row_pos[row] * dim + k] = in[q];
+}
+// transpose keys of a per-frame extended list: frame f's atom nb -> f * nall + nb
+__global__ void ext_keys_kernel(int* __restrict__ keys, const int* __restrict__ nlist, long long npair, FastDiv by_row,
+                                int nloc, int nall) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npair) return;
+  const int nb = nlist[p];
+  const int row = by_row.div((int)p), f = row / nloc;
+  keys[p] = nb < 0 ? -1 : f * nall + nb;
+}
+// dE/dr of every extended atom from the pair gradients g = dE/d(r_nb - r_i):
+// -sum over the atom's own real slots (local atoms) + sum over the pairs
+// that point at it, in FP64 in a fixed order
+__global__ void ext_pair_gather_kernel(double* __restrict__ out, const float* __restrict__ g,
+                                       const int* __restrict__ nlist, Transpose tr, int nloc, int nall, int nnei,
+                                       int nf) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (long long)nf * nall) return;
+  const int f = (int)(q / nall), j = (int)(q - (long long)f * nall);
+  double acc[3] = {0.0, 0.0, 0.0};
+  if (j < nloc) {
+    const size_t row = (size_t)f * nloc + j;
+    for (int s = 0; s < nnei; ++s)
+      if (nlist[row * nnei + s] >= 0)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) acc[k] -= (double)g[(row * nnei + s) * 3 + k];
+  }
+  for (int t = tr.offsets[q]; t < tr.offsets[q + 1]; ++t) {
+    const int p = tr.pairs[t];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc[k] += (double)g[3 * (size_t)p + k];
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) out[3 * q + k] = acc[k];
+}
+
+// The embedding stage of the mixed form behind DescrptSeA: D (FP32, rows in
+// frame-major order) and xyz = G^T R~ / nnei from per-frame extended
+// coordinates and a formatted list (typed sections, -1 padding) — the same
+// kernels as the full evaluation (tensor-core embedding, or the fused table
+// kernels of a compressed model).  The backward turns dE/dD into dE/dr of
+// every extended atom.  The forward's state stays in the handle until the
+// next forward.
+int descrpt_fwd(DeepPotImpl& dp, int nf, int nloc, int nall, const double* coord_ext, const int* atype_ext,
+                const int* atype_loc_host, const int* nlist_in, float* D_out, float* xyz_out, cudaStream_t st) {
+  if (dp.precision != DPGB_PREC_MIXED)
+    return fail(DPGB_EINVAL, "the descriptor stage on its own runs in the mixed form only");
+  if (!dp.use_tc && !dp.use_tab)
+    return fail(DPGB_EINVAL, "no tensor-core embedding for these embedding widths (and no tables)");
+  if (nf < 1 || nloc < 1 || nall < nloc || !coord_ext || !atype_ext || !atype_loc_host || !nlist_in || !D_out)
+    return fail(DPGB_EINVAL, "descrpt: bad arguments");
+  const dpgb_se_a_desc& d = dp.desc;
+  const int nnei = dp.sel.nnei, ng = dp.ng, dim = dp.dim;
+  const long long nrows = (long long)nf * nloc, npair = nrows * nnei;
+  if (npair >= (1LL << 31) || (long long)nf * nall >= (1LL << 31)) return fail(DPGB_EINVAL, "descrpt: too large");
+  dp.dm_eval = 0;
+  const unsigned long long eval_no = ++dp.evals;
+  DPGB_TRY(prepare_types(dp, nf, nloc, atype_loc_host, st));
+  DevModel<float>& m = *dp.m32;
+  DPGB_TRY(dp.ws_status.alloc(sizeof(int) * kStatusSlots));
+  DPGB_TRY(dp.ws_nlist.alloc(sizeof(int) * npair));
+  DPGB_TRY(dp.ws_xyz.alloc(sizeof(float) * nrows * 4 * ng));
+  DPGB_TRY(dp.ws_D.alloc(sizeof(float) * nrows * dim));
+  DPGB_TRY(dp.ws_dD.alloc(sizeof(float) * nrows * dim));
+  DPGB_TRY(dp.ws_g.alloc(sizeof(float) * npair * 3));
+  DPGB_TRY(dp.ws_vir.alloc(sizeof(double) * nrows * 9));
+  DPGB_TRY(dp.ws_xhi.alloc(sizeof(float4) * (size_t)nf * nall));
+  DPGB_TRY(dp.ws_xlo.alloc(sizeof(float4) * (size_t)nf * nall));
+  DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ((ng + 15) / 16 * 16) * std::max(d.ntypes, 1)));
+  int* status = dp.ws_status.as<int>();
+  DPGB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * kStatusSlots, st));
+  DPGB_CUDA(cudaMemcpyAsync(dp.ws_nlist.ptr, nlist_in, sizeof(int) * npair, cudaMemcpyDeviceToDevice, st));
+  split_points_kernel<<<ceil_div((long long)nf * nall, 256), 256, 0, st>>>(dp.ws_xhi.as<float4>(),
+                                                                          dp.ws_xlo.as<float4>(), coord_ext, nf * nall);
+  DPGB_TRY(check_launch("split_points"));
+  DescParams<float> p{};
+  p.nloc = nloc;
+  p.nrows = (int)nrows;
+  p.nnei = nnei;
+  p.ntypes = d.ntypes;
+  for (int t = 0; t <= d.ntypes; ++t) p.sec[t] = dp.sel.sec[t];
+  p.type_one_side = d.type_one_side;
+  p.ng = ng;
+  p.axis = d.axis_neuron;
+  p.pad_zero = dp.pad_zero;
+  p.rcut = d.rcut;
+  p.rcut_smth = d.rcut_smth;
+  p.davg = m.davg;
+  p.dstd = m.dstd;
+  p.dstd_inv = m.dstd_inv;
+  p.nloc_div = FastDiv(nloc);
+  p.pair_mask = d.pair_mask ? dp.pair_mask_dev.as<int>() : nullptr;
+  p.atype = dp.atype_dev.as<int>();
+  p.nlist = dp.ws_nlist.as<int>();
+  p.row_pos = dp.row_pos_dev.as<int>();
+  p.coord_ext = coord_ext;
+  p.atype_ext = atype_ext;
+  p.nall = nall;
+  p.xhi = dp.ws_xhi.as<float4>();
+  p.xlo = dp.ws_xlo.as<float4>();
+  if (dp.use_tc) {
+    const int nsorted = dp.type_off[d.ntypes];
+    DPGB_TRY(dp.ws_runlen.alloc(sizeof(int) * (size_t)std::max(nsorted, 1) * d.ntypes));
+    DPGB_TRY(launch_run_lengths(dp.ws_runlen.as<int>(), p.nlist, dp.sorted_rows_dev.as<int>(), nsorted, nnei, dp.sel,
+                                dp.pad_zero, st));
+    EmbTC e = dp.tc;
+    e.d_bf16 = 0;
+    DPGB_TRY(launch_emb_tc_fwd(p, e, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.ws_runlen.as<int>(),
+                               dp.sorted_rows_dev.as<int>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(),
+                               dp.ws_D.as<float>(), status, st));
+  } else {
+    DPGB_TRY(launch_tab_fwd(p, m.emb, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.sorted_rows_dev.as<int>(),
+                            dp.ws_xyz.as<float>(), dp.ws_D.ptr, 0, st));
+  }
+  const long long tot = nrows * dim;
+  unsort_rows_kernel<<<ceil_div(tot, 256), 256, 0, st>>>(D_out, dp.ws_D.as<float>(), p.row_pos, p.atype, nloc, tot,
+                                                         dim);
+  DPGB_TRY(check_launch("unsort_rows"));
+  if (xyz_out)
+    DPGB_CUDA(cudaMemcpyAsync(xyz_out, dp.ws_xyz.ptr, sizeof(float) * nrows * 4 * ng, cudaMemcpyDeviceToDevice, st));
+  dp.dm_p = p;
+  dp.dm_nf = nf;
+  dp.dm_nloc = nloc;
+  dp.dm_nall = nall;
+  dp.dm_eval = eval_no;
+  return DPGB_OK;
+}
+
+int descrpt_bwd(DeepPotImpl& dp, unsigned long long ticket, const float* dD_in, double* g_ext, cudaStream_t st) {
+  if (!dD_in || !g_ext) return fail(DPGB_EINVAL, "descrpt_bwd: NULL argument");
+  if (!dp.dm_eval || dp.dm_eval != dp.evals || ticket != dp.dm_eval)
+    return fail(DPGB_EINVAL, "descrpt_bwd: no descriptor forward of this handle to differentiate (another "
+                             "evaluation ran in between)");
+  const DescParams<float>& p = dp.dm_p;
+  const int nf = dp.dm_nf, nloc = dp.dm_nloc, nall = dp.dm_nall, nnei = p.nnei, dim = dp.dim;
+  const long long nrows = (long long)nf * nloc, npair = nrows * nnei, nkeys = (long long)nf * nall;
+  int* status = dp.ws_status.as<int>();
+  const long long tot = nrows * dim;
+  sort_rows_kernel<<<ceil_div(tot, 256), 256, 0, st>>>(dp.ws_dD.as<float>(), dD_in, p.row_pos, p.atype, nloc, tot, dim);
+  DPGB_TRY(check_launch("sort_rows"));
+  DPGB_CUDA(cudaMemsetAsync(dp.ws_vir.ptr, 0, sizeof(double) * nrows * 9, st));
+  DPGB_CUDA(cudaMemsetAsync(dp.ws_g.ptr, 0, sizeof(float) * npair * 3, st));  // slots no kernel visits add 0
+  DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
+  if (dp.use_tc)
+    DPGB_TRY(launch_emb_tc_bwd(p, dp.tc, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.ws_runlen.as<int>(),
+                               dp.sorted_rows_dev.as<int>(), dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(),
+                               dp.ws_vir.as<double>(), status, st));
+  else
+    DPGB_TRY(launch_tab_bwd(p, dp.m32->emb, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.sorted_rows_dev.as<int>(),
+                            dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(), dp.ws_vir.as<double>(), st));
+  DPGB_TRY(dp.dm_keys.alloc(sizeof(int) * npair));
+  DPGB_TRY(dp.dm_tr.alloc(transpose_workspace(npair, (int)nkeys)));
+  ext_keys_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(dp.dm_keys.as<int>(), p.nlist, npair, FastDiv(nnei), nloc,
+                                                        nall);
+  DPGB_TRY(check_launch("ext_keys"));
+  Transpose tr;
+  DPGB_TRY(launch_transpose(tr, dp.dm_keys.as<int>(), npair, (int)nkeys, 0, dp.dm_tr.ptr, status, st));
+  ext_pair_gather_kernel<<<ceil_div(nkeys, 256), 256, 0, st>>>(g_ext, dp.ws_g.as<float>(), p.nlist, tr, nloc, nall,
+                                                               nnei, nf);
+  DPGB_TRY(check_launch("ext_pair_gather"));
+  return DPGB_OK;
+}
+
 int run_any(DeepPotImpl& dp, int nframes, int natom, const double* coord, const double* box_host, double* energy,
             double* force, double* virial, double* atom_energy, double* atom_virial, cudaStream_t st) {
   if (dp.precision == DPGB_PREC_FP64)
@@ -1933,6 +2123,28 @@ int dpgb_deeppot_last_nlist(dpgb_deeppot* dp, int* info, int* nlist, double* coo
                               cudaMemcpyDeviceToHost, st));
   DPGB_CUDA(cudaStreamSynchronize(st));
   return DPGB_OK;
+}
+
+int dpgb_deeppot_descrpt_fwd(dpgb_deeppot* dp, int nf, int nloc, int nall, const double* coord_ext,
+                             const int* atype_ext, const int* atype_loc, const int* nlist, float* descrpt,
+                             float* xyz, unsigned long long* ticket, void* stream) {
+  clear_error();
+  if (!dp) return fail(DPGB_EINVAL, "NULL handle");
+  int rc = descrpt_fwd(dp->impl, nf, nloc, nall, coord_ext, atype_ext, atype_loc, nlist, descrpt, xyz, as_stream(stream));
+  if (rc == DPGB_OK) rc = mark_done(dp->impl, as_stream(stream));
+  if (ticket) *ticket = rc == DPGB_OK ? dp->impl.dm_eval : 0;
+  dp->impl.err = rc == DPGB_OK ? "" : dpgb_last_error();
+  return rc;
+}
+
+int dpgb_deeppot_descrpt_bwd(dpgb_deeppot* dp, unsigned long long ticket, const float* g_descrpt,
+                             double* g_coord_ext, void* stream) {
+  clear_error();
+  if (!dp) return fail(DPGB_EINVAL, "NULL handle");
+  int rc = descrpt_bwd(dp->impl, ticket, g_descrpt, g_coord_ext, as_stream(stream));
+  if (rc == DPGB_OK) rc = mark_done(dp->impl, as_stream(stream));
+  dp->impl.err = rc == DPGB_OK ? "" : dpgb_last_error();
+  return rc;
 }
 
 int dpgb_deeppot_set_profiling(dpgb_deeppot* dp, int on) {

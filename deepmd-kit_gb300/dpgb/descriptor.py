@@ -17,6 +17,14 @@ parameters, activations recomputed, ``csrc/se_a_block.cu``).  Forces through
 on these kernels.  The compressed form calls ``torch.ops.deepmd.
 tabulate_fusion_se_a`` (``dpgb.ops``), as the reference does.
 
+``precision="mixed"`` (a dpgb option beside the reference's float64 /
+float32) runs the block on the mixed form's kernels instead: the tcgen05
+embedding GEMMs (split BF16, FP32 accumulation) fused with the environment
+matrix and the contraction to D — or, compressed, the fused FP32 table
+kernels — through ``dpgb_deeppot_descrpt_fwd`` / ``_bwd``.  Its autograd
+gives dE/d coordinates (forces) but no weight gradients and no second
+derivative: an inference option (the parameters stay FP64).
+
 CUDA tensors only: there is no CPU path.
 """
 from __future__ import annotations
@@ -30,7 +38,8 @@ from torch.autograd.function import once_differentiable
 from . import _lib
 
 PRECISION = {"float64": torch.float64, "float32": torch.float32, "double": torch.float64,
-             "single": torch.float32, "default": torch.float64}
+             "single": torch.float32, "default": torch.float64,
+             "mixed": torch.float64}  # mixed: FP64 parameters, mixed-form kernels
 
 
 def _stream():
@@ -142,6 +151,35 @@ def prod_env_mat(extended_coord, nlist, atype, mean, stddev, rcut: float, rcut_s
     return _EnvMatFn.apply(coord.contiguous(), nlist.to(torch.int32).contiguous(),
                            atype.to(torch.int32).contiguous(), _c(mean, dt), _c(stddev, dt), rcut, rcut_smth,
                            protection)
+
+
+# ---------------------------------------------------------------------------
+# the block on the mixed form's kernels
+
+
+class _MixedBlockFn(torch.autograd.Function):
+    """D (and xyz) of the block from extended coordinates through a mixed
+    DeepPot handle's descriptor stage; backward: dE/dD -> dE/d coordinates."""
+
+    @staticmethod
+    def forward(ctx, coord, handle, nlist, atype_ext, atype_loc, nf, nloc, nall, ng, dim):
+        D = torch.empty((nf, nloc, dim), dtype=torch.float32, device=coord.device)
+        X = torch.empty((nf, nloc, 4, ng), dtype=torch.float32, device=coord.device)
+        ticket = C.c_ulonglong(0)
+        _lib.call("dpgb_deeppot_descrpt_fwd", handle._h, nf, nloc, nall, _p(coord), _p(atype_ext),
+                  atype_loc.ctypes.data_as(C.POINTER(C.c_int)), _p(nlist), _p(D), _p(X), C.byref(ticket), _stream())
+        ctx.handle, ctx.shape, ctx.ticket = handle, (nf, nall), ticket.value
+        ctx.mark_non_differentiable(X)
+        return D, X
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, gD, gX):
+        nf, nall = ctx.shape
+        g = torch.empty((nf, nall * 3), dtype=torch.float64, device=gD.device)
+        _lib.call("dpgb_deeppot_descrpt_bwd", ctx.handle._h, ctx.ticket, _p(gD.to(torch.float32).contiguous()), _p(g),
+                  _stream())
+        return g, None, None, None, None, None, None, None, None, None
 
 
 # ---------------------------------------------------------------------------
@@ -434,6 +472,8 @@ class DescrptBlockSeA(torch.nn.Module):
         nall = coord.shape[1] // 3
         atype = extended_atype[:, :nloc]
         nl32 = nlist.to(torch.int32).contiguous()
+        if self.precision == "mixed":
+            return self._mixed_forward(coord, nl32, extended_atype, atype, nf, nloc, nall)
         dmatrix, diff, sw = prod_env_mat(coord, nl32, atype, self.mean, self.stddev, self.rcut, self.rcut_smth,
                                          protection=self.env_protection)
         rr = dmatrix.view(nf * nloc, self.nnei, 4)
@@ -447,6 +487,56 @@ class DescrptBlockSeA(torch.nn.Module):
         rot_mat = X.permute(0, 2, 1)[:, :, 1:4]
         ng = self.filter_neuron[-1]
         return (D.view(nf, nloc, ng * self.axis_neuron), rot_mat.reshape(nf, nloc, ng, 3), None, None, sw)
+
+    def _mixed_params(self):
+        """The block as an SeAParams (with a zero 16-wide fitting the
+        descriptor stage never runs), for a mixed DeepPot handle."""
+        from .params import SeAConfig, SeAParams
+
+        cfg = SeAConfig(sel=list(self.sel), rcut=self.rcut, rcut_smth=self.rcut_smth, neuron=list(self.neuron),
+                        axis_neuron=self.axis_neuron, type_one_side=self.type_one_side, resnet_dt=self.resnet_dt,
+                        fit_neuron=[16], fit_resnet_dt=False, exclude_types=[list(t) for t in self.exclude_types])
+        npf = lambda t: t.detach().to(torch.float64).cpu().numpy()  # noqa: E731
+        emb = [[(npf(l.matrix), npf(l.bias), npf(l.idt) if l.idt is not None else None) for l in net.layers]
+               for net in self.filter_layers.networks]
+        dim = cfg.dim_descrpt
+        fit = [[(np.zeros((dim, 16)), np.zeros(16), None), (np.zeros((16, 1)), np.zeros(1), None)]
+               for _ in range(self.ntypes)]
+        tables = infos = None
+        if self.compress:
+            tables = [npf(t) for t in self.compress_data]
+            infos = [npf(t) for t in self.compress_info]
+        return SeAParams(config=cfg, mean=npf(self.mean), stddev=npf(self.stddev), emb=emb, fit=fit,
+                         bias_atom_e=np.zeros(self.ntypes), out_bias=np.zeros(self.ntypes), tables=tables,
+                         table_info=infos)
+
+    def _mixed_handle(self):
+        """A mixed DeepPot handle holding the block's current weights (rebuilt
+        when a parameter, the statistics or the tables change)."""
+        from .deeppot import DeepPot
+
+        key = (self.compress, tuple(t._version for t in self.parameters()), self.mean._version,
+               self.stddev._version, self.mean.data_ptr(), self.stddev.data_ptr())
+        cached = getattr(self, "_mixed", None)
+        if cached is None or cached[0] != key:
+            dev = self.mean.device.index if self.mean.device.index is not None else torch.cuda.current_device()
+            self._mixed = (key, DeepPot(self._mixed_params(), "mixed", device=dev))
+        return self._mixed[1]
+
+    def _mixed_forward(self, coord, nl32, extended_atype, atype, nf, nloc, nall):
+        at = atype.to(torch.int32).cpu().numpy()
+        if nf > 1 and not (at == at[:1]).all():
+            raise NotImplementedError("the mixed descriptor needs the same local atom types in every frame")
+        ng = self.filter_neuron[-1]
+        dim = ng * self.axis_neuron
+        D, X = _MixedBlockFn.apply(coord.contiguous(), self._mixed_handle(), nl32,
+                                   extended_atype.to(torch.int32).contiguous(), np.ascontiguousarray(at[0]), nf,
+                                   nloc, nall, ng, dim)
+        with torch.no_grad():  # the switch function output (not differentiated here)
+            _, _, sw = prod_env_mat(coord.detach(), nl32, atype, self.mean, self.stddev, self.rcut, self.rcut_smth,
+                                    protection=self.env_protection)
+        rot_mat = X[:, :, 1:4, :].transpose(2, 3).to(torch.float64)
+        return D.to(torch.float64), rot_mat, None, None, sw
 
     def _compressed_xyz(self, rr, nl32, extended_atype, atype, nf, nloc):
         """xyz_scatter of the compressed form: the reference's per-net loop

@@ -10,6 +10,7 @@ deepmd/pt/utils/region.py (same argument meaning and output layout).
 from __future__ import annotations
 
 import ctypes as C
+import functools
 from typing import List, Optional, Sequence
 
 import numpy as np
@@ -48,8 +49,14 @@ def to_face_distance(box: np.ndarray) -> np.ndarray:
 def image_shifts(box: np.ndarray, rcut: float) -> np.ndarray:
     """Integer image shifts [(2nbuff+1)^3, 3] in the order the reference sorts
     them (deepmd/pt/utils/nlist.py:470-498): the same ``torch.argsort`` of the
-    shift norms on the CPU, so extended indices match the reference's."""
+    shift norms on the CPU, so extended indices match the reference's.
+    Cached per buffer count (frames of one box size share it)."""
     nbuff = np.ceil(rcut / np.abs(to_face_distance(box))).astype(np.int64)
+    return _image_shifts(tuple(int(n) for n in nbuff)).copy()
+
+
+@functools.lru_cache(maxsize=64)
+def _image_shifts(nbuff) -> np.ndarray:
     xi = [torch.arange(-int(n), int(n) + 1, dtype=torch.int64) for n in nbuff]
     eye = torch.eye(3, dtype=torch.float64)
     xyz = (xi[0].view(-1, 1, 1, 1) * eye[0] + xi[1].view(1, -1, 1, 1) * eye[1]

@@ -576,6 +576,34 @@ int dpgb_batch_buckets(const dpgb_batch* b, int* frames, int* atoms);
 int dpgb_batch_set_tiles(dpgb_batch* b, const int* rows_per_item);
 int dpgb_batch_get_tiles(const dpgb_batch* b, int* rows_per_item);
 
+/* The embedding stage of the mixed form on its own, behind the Python
+ * DescrptSeA (deepmd/pt/model/descriptor/se_a.py:742-858; precision
+ * "mixed"): the handle's tensor-core embedding — or, for a compressed
+ * model, its fused FP32 table kernels — with the contraction to the
+ * descriptor D = (G^T R~)^T (G^T R~)< / nnei^2, on per-frame extended atoms
+ * and a formatted neighbour list, without the fitting.  DEVICE buffers on
+ * `stream` (NULL: the legacy stream), no synchronisation:
+ *   coord_ext [nf, nall, 3] FP64, atype_ext [nf, nall] (device), atype_loc
+ *   [nloc] HOST (the local types, the same in every frame), nlist
+ *   [nf, nloc, sum(sel)] (indices into the frame's extended atoms, type
+ *   sections in the reference order, -1 padding)
+ *   -> descrpt [nf, nloc, ng * axis] FP32, xyz [nf, nloc, 4, ng] FP32 (may
+ *   be NULL; xyz[:, :, 1:4] is the reference's rot_mat transposed).
+ * ticket (HOST, may be NULL) <- this forward's number.  The backward takes
+ * dE/d descrpt [nf, nloc, ng * axis] FP32 to dE/d coord_ext [nf, nall, 3]
+ * FP64 (every extended atom written) for the forward with that ticket, which
+ * must be the handle's latest evaluation (else DPGB_EINVAL: its state is
+ * gone).  FP64 handles return DPGB_EINVAL (their descriptor is the FP64
+ * block). */
+int dpgb_deeppot_descrpt_fwd(dpgb_deeppot* dp, int nf, int nloc, int nall,
+                             const double* coord_ext, const int* atype_ext,
+                             const int* atype_loc, const int* nlist,
+                             float* descrpt, float* xyz,
+                             unsigned long long* ticket, void* stream);
+int dpgb_deeppot_descrpt_bwd(dpgb_deeppot* dp, unsigned long long ticket,
+                             const float* g_descrpt, double* g_coord_ext,
+                             void* stream);
+
 /* Self-test of the bounded device-side waits (no counterpart in the
  * reference, which has no device-side waits of its own): one kernel waits
  * on an mbarrier that nothing completes, with a limit of limit_ms (0 < ...
