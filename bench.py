@@ -21,7 +21,7 @@ reported in `config` together with the mixed-vs-FP64 errors.  Workload
 water12k: the uncompressed model on 4096 molecules (12,288 atoms).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl dpgb|reference]
-                    [--workload water98k-compressed|water12k|alloy512-batch|train16]
+                    [--workload water98k-compressed|water12k|alloy512-batch|train16|descrpt12k]
 """
 from __future__ import annotations
 
@@ -196,7 +196,7 @@ FP32_SIMT_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12
 # 98,304-atom compressed step, from one ncu capture each: tab_fwd, tab_bwd
 # (profiles/tab_fused_water98304_compressed.md) and the fitting stage's six
 # launches summed (five fit_gemm + fit_dxyz, one dram-bytes pass)
-DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 727.6e6, "desc_bwd": 501.5e6, "fitting": 2103.7e6}
+DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 727.6e6, "desc_bwd": 489.7e6, "fitting": 2103.7e6}
 
 
 def table_roofline(per_step: dict, n_atoms: int, n_pairs: int, cfg) -> dict:
@@ -309,7 +309,7 @@ def run_reference(args, world, rank):
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     compressed = args.workload == "water98k-compressed"
-    if args.workload in ("alloy512-batch", "train16"):
+    if args.workload in ("alloy512-batch", "train16", "descrpt12k"):
         print(json.dumps({"impl": "reference", "unavailable": f"no CPU arm for the {args.workload} workload"}))
         return
     value, sec, ncores, sample = cpu_full_steps(compressed, args.steps, args.warmup)
@@ -337,6 +337,8 @@ WORKLOAD_NAME = {
     "water12k": "water 4096 H2O (12,288 atoms), box 49.6 A, se_e2_a rc 6 sel [46,92] emb [25,50,100] "
                 "axis 16 fit [240,240,240]",
     "alloy512-batch": "512 fcc alloy frames, se_e2_a rc 6 rs 2 sel [60]*4",
+    "descrpt12k": "DescrptSeA forward + coordinate backward on 4096 H2O (12,288 atoms), se_e2_a rc 6 sel [46,92] "
+                  "emb [25,50,100] axis 16, precision mixed vs float64",
     "train16": "force-loss Adam step on 16 water frames of 192 atoms, se_e2_a rc 6 sel [46,92] emb [25,50,100] "
                "axis 16 fit [240,240,240], FP64",
 }
@@ -565,6 +567,78 @@ def run_batch(args, world, rank, local):
     print(json.dumps(line))
 
 
+def run_descrpt(args, world, rank, local):
+    """The DescrptSeA drop-in on 4096 H2O (12,288 atoms): one forward and the
+    backward of a linear read-out of the descriptor to the extended
+    coordinates (autograd), precision "mixed" (tcgen05 embedding) against
+    "float64" (the FP64 block) on the same weights; the extended
+    coordinates and the list are built once, outside the timed region."""
+    import torch
+
+    from dpgb import nlist as N, synth
+    from dpgb.descriptor import DescrptSeA
+
+    dev = torch.device("cuda", local)
+    params = water_model(False)
+    c = params.config
+    coord, atype, box = synth.water_box(NMOL_SIDE, seed=rank)
+    ext, ext_t, _, nl = N.extend_input_and_build_neighbor_list(
+        torch.tensor(coord[None], dtype=torch.float64, device=dev), torch.tensor(atype[None], device=dev), c.rcut,
+        c.sel, box.reshape(1, 9))
+    ext, ext_t, nl = ext.reshape(1, -1), ext_t.long(), nl.long()
+    sd = {k[len("atomic_model.descriptor."):]: torch.as_tensor(v) for k, v in params.to_state_dict().items()
+          if k.startswith("atomic_model.descriptor.")}
+    w = torch.randn(c.dim_descrpt, dtype=torch.float64, device=dev, generator=torch.Generator(dev).manual_seed(1))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def timed(prec, steps):
+        d = DescrptSeA(rcut=c.rcut, rcut_smth=c.rcut_smth, sel=c.sel, neuron=c.neuron, axis_neuron=c.axis_neuron,
+                       type_one_side=c.type_one_side, resnet_dt=c.resnet_dt, precision=prec, device=dev)
+        d.load_state_dict(sd, strict=False)
+
+        def step():
+            x = ext.detach().requires_grad_(True)
+            D = d(x, ext_t, nl)[0]
+            (g,) = torch.autograd.grad((D * w).sum(), x)
+            return D, g
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for a, b in ev:
+            flush.fill_(1.0)
+            a.record(stream)
+            out = step()
+            b.record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev), out
+
+    _barrier(world)
+    t_mx, (Dm, gm) = timed("mixed", args.steps)
+    t_64, (D6, g6) = timed("float64", max(1, args.fp64_steps))
+    t_mx = _allreduce_max(t_mx, world)
+    nat = coord.shape[0]
+    value = world * nat * args.steps / (t_mx * 1e-3)
+    fp64_rate = nat * max(1, args.fp64_steps) / (t_64 * 1e-3)
+    if rank != 0:
+        return
+    line = {
+        "metric": "atoms/s DescrptSeA forward + backward (dE/d coordinates)", "value": value, "unit": "atoms/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mx / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16x2+f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME["descrpt12k"], "natoms": nat,
+                   "fp64_ms_per_step": t_64 / max(1, args.fp64_steps), "fp64_atoms_per_s": fp64_rate,
+                   "mixed_over_fp64": value / world / fp64_rate,
+                   "descriptor_rel_err_vs_fp64": float((Dm - D6).abs().max() / D6.abs().max()),
+                   "grad_rmse_over_rms": float((gm - g6).pow(2).mean().sqrt() / g6.pow(2).mean().sqrt()),
+                   "l2": "flushed between timed steps (256 MB fill)", "parallelism": f"replicas x{world}"},
+        "roofline": None,
+    }
+    print(json.dumps(line))
+
+
 TRAIN_FRAMES, TRAIN_NMOL_SIDE = 16, 4  # 16 frames of 64 H2O (192 atoms)
 
 
@@ -661,7 +735,7 @@ DRAM_BYTES_PER_LAUNCH = {"desc_fwd": 50.0e6, "desc_bwd": 27.2e6, "fitting": 41.9
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="water98k-compressed",
-                    choices=["water98k-compressed", "water12k", "alloy512-batch", "train16"])
+                    choices=["water98k-compressed", "water12k", "alloy512-batch", "train16", "descrpt12k"])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -698,6 +772,9 @@ def main():
         return
     if args.workload == "train16":
         run_train(args, world, rank, local)
+        return
+    if args.workload == "descrpt12k":
+        run_descrpt(args, world, rank, local)
         return
     from dpgb import nlist as N, params as P, synth
     from dpgb.deeppot import DeepPot
