@@ -407,6 +407,7 @@ struct DeepPotImpl {
   // workspace
   DeviceBuffer ws_nlist, ws_cell, ws_tr, ws_keys, ws_status, ws_coord, ws_svec, ws_spos;
   DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf, ws_part, ws_xhi, ws_xlo, ws_shi, ws_slo;
+  DeviceBuffer ws_env;  // the table path's per-pair environment, forward -> backward
   DeviceBuffer io_coord, io_force, io_av, io_e, io_v, io_ae;
   DeviceBuffer io_out;   // host API: [energy | virial | force | atom energy | atom virial]
   PinnedBuffer io_host;  // host API staging: [coord | the outputs | status words]
@@ -1358,8 +1359,10 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     tab_path = !tc_path && dp.use_tab != 0;
     if (tab_path) {
       DPGB_TRY(dp.ws_dxyz.alloc(sizeof(float) * nrows * 4 * ng));
+      DPGB_TRY(dp.ws_env.alloc(sizeof(float4) * 2 * npair));
       DPGB_TRY(launch_tab_fwd(p, m.emb, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.sorted_rows_dev.as<int>(),
-                              dp.ws_xyz.as<float>(), dp.ws_D.ptr, dp.use_fit_tc, st, queue_fwd(dp)));
+                              dp.ws_xyz.as<float>(), dp.ws_D.ptr, dp.use_fit_tc, st, queue_fwd(dp),
+                              dp.ws_env.as<float4>()));
       ++launches;
     }
   }
@@ -1411,7 +1414,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       if (!dxyz_done) DPGB_TRY(launch_dxyz(p, dp.ws_dD.as<float>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(), st));
       DPGB_TRY(launch_tab_bwd(p, m.emb, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.sorted_rows_dev.as<int>(),
                               dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(), dp.ws_vir.as<double>(), st,
-                              queue_bwd(dp)));
+                              queue_bwd(dp), dp.ws_env.as<float4>()));
       launches += 2;
     }
   }
@@ -1620,8 +1623,9 @@ int descrpt_fwd(DeepPotImpl& dp, int nf, int nloc, int nall, const double* coord
                                dp.sorted_rows_dev.as<int>(), dp.ws_xyz.as<float>(), dp.ws_dxyz.as<float>(),
                                dp.ws_D.as<float>(), status, st));
   } else {
+    DPGB_TRY(dp.ws_env.alloc(sizeof(float4) * 2 * npair));
     DPGB_TRY(launch_tab_fwd(p, m.emb, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.sorted_rows_dev.as<int>(),
-                            dp.ws_xyz.as<float>(), dp.ws_D.ptr, 0, st));
+                            dp.ws_xyz.as<float>(), dp.ws_D.ptr, 0, st, nullptr, dp.ws_env.as<float4>()));
   }
   const long long tot = nrows * dim;
   unsort_rows_kernel<<<ceil_div(tot, 256), 256, 0, st>>>(D_out, dp.ws_D.as<float>(), p.row_pos, p.atype, nloc, tot,
@@ -1658,7 +1662,8 @@ int descrpt_bwd(DeepPotImpl& dp, unsigned long long ticket, const float* dD_in, 
                                dp.ws_vir.as<double>(), status, st));
   else
     DPGB_TRY(launch_tab_bwd(p, dp.m32->emb, dp.chunks_dev.as<WorkChunk>(), dp.nchunks, dp.sorted_rows_dev.as<int>(),
-                            dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(), dp.ws_vir.as<double>(), st));
+                            dp.ws_dxyz.as<float>(), dp.ws_g.as<float>(), dp.ws_vir.as<double>(), st, nullptr,
+                            dp.ws_env.as<float4>()));
   DPGB_TRY(dp.dm_keys.alloc(sizeof(int) * npair));
   DPGB_TRY(dp.dm_tr.alloc(transpose_workspace(npair, (int)nkeys)));
   ext_keys_kernel<<<ceil_div(npair, 256), 256, 0, st>>>(dp.dm_keys.as<int>(), p.nlist, npair, FastDiv(nnei), nloc,

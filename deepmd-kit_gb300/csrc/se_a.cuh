@@ -236,11 +236,15 @@ size_t desc_bwd_smem(const DescParams<T>& p, const EmbParams<T>& e);
 // written at the type-sorted position.
 struct WorkChunk;
 int tab_fused_eligible(int ng, int axis);
+// env_out / env_in: [nrows][nnei][2] float4 (R~; displacement, kept flag)
+// of the real pairs, written by the forward and read by the backward (NULL:
+// the backward forms the environment itself)
 int launch_tab_fwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
-                   const int* sorted_rows, float* xyz, void* D, int d_bf16, cudaStream_t st, int* queue = nullptr);
+                   const int* sorted_rows, float* xyz, void* D, int d_bf16, cudaStream_t st, int* queue = nullptr,
+                   float4* env_out = nullptr);
 int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
                    const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, cudaStream_t st,
-                   int* queue = nullptr);
+                   int* queue = nullptr, const float4* env_in = nullptr);
 
 // fitting of the rows [row0, row0+nrow) of one type
 template <typename T>

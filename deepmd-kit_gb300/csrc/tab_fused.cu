@@ -14,6 +14,11 @@
 namespace dpgb {
 namespace {
 
+// a hint: move the 128-byte line holding p into L2 (global memory)
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 struct SlotEnv {
   int nb;        // extended index, -1 padding
   int active;    // contributes to xyz
@@ -105,6 +110,9 @@ __device__ __forceinline__ void slot_deriv(const float d[3], float rmin, float r
 // Sections after the first add to the atom's xyz (forward) and virial
 // (backward) where the previous section left them (the same CTA, after a
 // barrier).  Sums run in a fixed order: results are bitwise reproducible.
+// The forward can keep each real pair's environment (R~ and the
+// displacement, two float4) for the backward, which then reads it instead
+// of forming it again from the coordinates.
 constexpr int kFwdWarps = 16;
 constexpr int kBwdWarps = 16;
 constexpr int kTabJ = 4;       // neurons per lane (ng <= 128)
@@ -171,7 +179,7 @@ __device__ __forceinline__ void load_coeffs(const float* s_tab, const float* __r
 __global__ void __launch_bounds__(kFwdWarps * 32, 1)
 tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restrict__ chunks, int nchunks,
                const int* __restrict__ sorted_rows, int rows_cap, float* __restrict__ xyz, void* __restrict__ Dout,
-               int d_bf16, int* __restrict__ queue) {
+               int d_bf16, int* __restrict__ queue, float4* __restrict__ env_out) {
   extern __shared__ float4 smem4[];
   const int ng = p.ng, M = p.axis;
   float* s_tab = reinterpret_cast<float*>(smem4);
@@ -213,6 +221,11 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
           if (slot < p.sec[sec + 1]) {
             slot_env(p, row, ti, slot, s);
             table_locate(tm, s.rn[0], s.idx, s.xx, s.delta);
+            if (env_out && s.nb >= 0) {  // the pair's environment, for the backward
+              float4* eo = env_out + 2 * ((size_t)row * p.nnei + slot);
+              eo[0] = make_float4(s.rn[0], s.rn[1], s.rn[2], s.rn[3]);
+              eo[1] = make_float4(s.d[0], s.d[1], s.d[2], s.active ? 1.f : 0.f);
+            }
           }
           unsigned m = __ballot_sync(0xffffffffu, s.active);
           if (!m) continue;
@@ -351,7 +364,8 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
 __global__ void __launch_bounds__(kBwdWarps * 32, 1)
 tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restrict__ chunks, int nchunks,
                const int* __restrict__ sorted_rows, int rows_cap, int row_stride, const float* __restrict__ dxyz,
-               float* __restrict__ gpair, double* __restrict__ vir_row, int* __restrict__ queue) {
+               float* __restrict__ gpair, double* __restrict__ vir_row, int* __restrict__ queue,
+               const float4* __restrict__ env_in) {
   extern __shared__ float4 smem4[];
   const int ng = p.ng;
   float* s_tab = reinterpret_cast<float*>(smem4);
@@ -377,6 +391,16 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
         const int row = sorted_rows[r];
         const int* nl = p.nlist + (size_t)row * p.nnei;
         float* gp_row = gpair + (size_t)row * p.nnei * 3;
+        if (r + kBwdWarps < ch.row1) {
+          // the warp's next atom: its dE/dxyz, list and first pair
+          // environments move into L2 while this atom is processed
+          const int nrow = sorted_rows[r + kBwdWarps];
+          const char* nd = reinterpret_cast<const char*>(dxyz + (size_t)nrow * 4 * ng);
+          if (lane * 128 < 16 * ng) prefetch_l2(nd + lane * 128);
+          if (lane * 128 < 4 * p.nnei) prefetch_l2(reinterpret_cast<const char*>(p.nlist + (size_t)nrow * p.nnei) + lane * 128);
+          if (env_in && p.sec[sec] + lane < p.sec[sec + 1])
+            prefetch_l2(env_in + 2 * ((size_t)nrow * p.nnei + p.sec[sec] + lane));
+        }
         // the atom's dE/dxyz (dxyz is [row][ng][4]) and the section's real slots
         for (int n = lane; n < ng; n += 32) s_dx[n] = reinterpret_cast<const float4*>(dxyz + (size_t)row * 4 * ng)[n];
         int nreal = 0;
@@ -400,10 +424,26 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
         for (int q0 = 0; q0 < nreal; q0 += 32) {
           const bool mine = q0 + lane < nreal;
           const int slot = mine ? s_list[q0 + lane] : p.sec[sec];
+          if (env_in && q0 + 32 + lane < nreal)  // the next 32 pairs' environments
+            prefetch_l2(env_in + 2 * ((size_t)row * p.nnei + s_list[q0 + 32 + lane]));
           SlotEnv s;
           s.active = 0;
           if (mine) {
-            slot_env(p, row, ti, slot, s);
+            if (env_in) {  // the environment the forward formed for this pair
+              const float4* ei = env_in + 2 * ((size_t)row * p.nnei + slot);
+              const float4 a = __ldg(ei), b = __ldg(ei + 1);
+              s.nb = 0;
+              s.rn[0] = a.x;
+              s.rn[1] = a.y;
+              s.rn[2] = a.z;
+              s.rn[3] = a.w;
+              s.d[0] = b.x;
+              s.d[1] = b.y;
+              s.d[2] = b.z;
+              s.active = b.w != 0.f;
+            } else {
+              slot_env(p, row, ti, slot, s);
+            }
             table_locate(tm, s.rn[0], s.idx, s.xx, s.delta);
           }
           const bool act = mine && s.active;  // excluded type pairs carry no gradient
@@ -561,19 +601,20 @@ int tab_rows_cap(int ng, int warps, size_t* smem) {
 }  // namespace
 
 int launch_tab_fwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
-                   const int* sorted_rows, float* xyz, void* D, int d_bf16, cudaStream_t st, int* queue) {
+                   const int* sorted_rows, float* xyz, void* D, int d_bf16, cudaStream_t st, int* queue,
+                   float4* env_out) {
   if (nchunks <= 0) return DPGB_OK;
   size_t smem = 0;
   const int rows = tab_rows_cap(p.ng, kFwdWarps, &smem);
   DPGB_CUDA(cudaFuncSetAttribute(tab_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   tab_fwd_kernel<<<std::min(nchunks, sm_count()), kFwdWarps * 32, smem, st>>>(p, e, chunks, nchunks, sorted_rows,
-                                                                               rows, xyz, D, d_bf16, queue);
+                                                                               rows, xyz, D, d_bf16, queue, env_out);
   return check_launch("tab_fwd");
 }
 
 int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const WorkChunk* chunks, int nchunks,
                    const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, cudaStream_t st,
-                   int* queue) {
+                   int* queue, const float4* env_in) {
   if (nchunks <= 0) return DPGB_OK;
   // rows at an odd float2 stride; per warp the atom's dE/dxyz and its slot list
   int per2 = 3 * p.ng;
@@ -590,7 +631,7 @@ int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const 
   DPGB_CUDA(cudaFuncSetAttribute(tab_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   tab_bwd_kernel<<<std::min(nchunks, sm_count()), kBwdWarps * 32, smem, st>>>(p, e, chunks, nchunks, sorted_rows,
                                                                                rows, row_stride, dxyz, gpair, vir_row,
-                                                                               queue);
+                                                                               queue, env_in);
   return check_launch("tab_bwd");
 }
 
