@@ -488,6 +488,16 @@ namespace {
 
 inline int pad64(int k) { return (k + 63) / 64 * 64; }
 
+// host memory the CUDA driver has page-locked (cudaHostAlloc / cudaHostRegister)
+bool is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
 // host inputs: every coordinate (and cell entry) must be finite
 int check_finite(const double* x, size_t n, const char* what) {
   for (size_t i = 0; i < n; ++i)
@@ -2325,20 +2335,39 @@ int dpgb_deeppot_compute(dpgb_deeppot* dp, int nframes, int natom, const double*
     double* hc = im.io_host.as<double>();
     double* ho = hc + 3 * nrow;
     int* hs = reinterpret_cast<int*>(ho + n_out);
-    std::memcpy(hc, coord, sizeof(double) * 3 * nrow);
-    DPGB_CUDA(cudaMemcpyAsync(im.io_coord.ptr, hc, sizeof(double) * 3 * nrow, cudaMemcpyHostToDevice, st));
+    // page-locked caller buffers are copied directly; pageable ones go
+    // through the pinned staging block
+    const bool pin_in = is_pinned(coord);
+    const bool pin_out = is_pinned(energy) && is_pinned(force) && is_pinned(virial) &&
+                         (!atom_energy || is_pinned(atom_energy)) && (!atom_virial || is_pinned(atom_virial));
+    if (!pin_in) std::memcpy(hc, coord, sizeof(double) * 3 * nrow);
+    DPGB_CUDA(cudaMemcpyAsync(im.io_coord.ptr, pin_in ? coord : hc, sizeof(double) * 3 * nrow, cudaMemcpyHostToDevice,
+                              st));
     double* d = im.io_out.as<double>();
     DPGB_TRY(compute_device_impl(im, nframes, natom, im.io_coord.as<double>(), atype, box, d, d + n_e + n_v, d + n_e,
                                  atom_energy ? d + n_e + n_v + n_f : nullptr,
                                  atom_virial ? d + n_e + n_v + n_f + n_ae : nullptr, st));
-    DPGB_CUDA(cudaMemcpyAsync(ho, d, sizeof(double) * n_out, cudaMemcpyDeviceToHost, st));
+    if (pin_out) {
+      DPGB_CUDA(cudaMemcpyAsync(energy, d, sizeof(double) * n_e, cudaMemcpyDeviceToHost, st));
+      DPGB_CUDA(cudaMemcpyAsync(virial, d + n_e, sizeof(double) * n_v, cudaMemcpyDeviceToHost, st));
+      DPGB_CUDA(cudaMemcpyAsync(force, d + n_e + n_v, sizeof(double) * n_f, cudaMemcpyDeviceToHost, st));
+      if (atom_energy)
+        DPGB_CUDA(cudaMemcpyAsync(atom_energy, d + n_e + n_v + n_f, sizeof(double) * n_ae, cudaMemcpyDeviceToHost, st));
+      if (atom_virial)
+        DPGB_CUDA(cudaMemcpyAsync(atom_virial, d + n_e + n_v + n_f + n_ae, sizeof(double) * n_av,
+                                  cudaMemcpyDeviceToHost, st));
+    } else {
+      DPGB_CUDA(cudaMemcpyAsync(ho, d, sizeof(double) * n_out, cudaMemcpyDeviceToHost, st));
+    }
     DPGB_CUDA(cudaMemcpyAsync(hs, im.ws_status.ptr, sizeof(int) * kStatusSlots, cudaMemcpyDeviceToHost, st));
     DPGB_CUDA(cudaStreamSynchronize(st));
-    std::memcpy(energy, ho, sizeof(double) * n_e);
-    std::memcpy(virial, ho + n_e, sizeof(double) * n_v);
-    std::memcpy(force, ho + n_e + n_v, sizeof(double) * n_f);
-    if (atom_energy) std::memcpy(atom_energy, ho + n_e + n_v + n_f, sizeof(double) * n_ae);
-    if (atom_virial) std::memcpy(atom_virial, ho + n_e + n_v + n_f + n_ae, sizeof(double) * n_av);
+    if (!pin_out) {
+      std::memcpy(energy, ho, sizeof(double) * n_e);
+      std::memcpy(virial, ho + n_e, sizeof(double) * n_v);
+      std::memcpy(force, ho + n_e + n_v, sizeof(double) * n_f);
+      if (atom_energy) std::memcpy(atom_energy, ho + n_e + n_v + n_f, sizeof(double) * n_ae);
+      if (atom_virial) std::memcpy(atom_virial, ho + n_e + n_v + n_f + n_ae, sizeof(double) * n_av);
+    }
     return status_result(im, hs);
   };
   int rc = body();

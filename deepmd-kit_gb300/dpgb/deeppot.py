@@ -76,6 +76,15 @@ def pack_desc(params: SeAParams):
     return d, keep
 
 
+def pinned_empty(shape, dtype=np.float64) -> np.ndarray:
+    """A numpy array in page-locked host memory (kept alive by the array);
+    the host API copies such buffers without staging."""
+    import torch
+
+    t = torch.empty(int(np.prod(shape)) * np.dtype(dtype).itemsize, dtype=torch.uint8, pin_memory=True)
+    return t.numpy().view(dtype).reshape(shape)  # the array's base holds the tensor
+
+
 def _shape_key(d, precision: str) -> str:
     """What a launch configuration depends on: the model's sizes (not its
     weights) and the precision."""
@@ -200,16 +209,25 @@ class DeepPot:
         _lib.check(_lib.lib().dpgb_deeppot_stage_times(self._h, ms, C.byref(n)))
         return dict(zip(_lib.STAGES, list(ms))), int(n.value)
 
-    def eval(self, coord, box, atype, atomic: bool = False):
-        """Host arrays in and out (DP_DeepPotCompute)."""
+    def eval(self, coord, box, atype, atomic: bool = False, out=None):
+        """Host arrays in and out (DP_DeepPotCompute).  ``out``: optional
+        (energy [nf], force [nf, natom, 3], virial [nf, 9]) arrays to fill,
+        e.g. views of page-locked memory (``pinned_empty``), which the call
+        copies into directly."""
         atype = np.ascontiguousarray(atype, dtype=np.int32).reshape(-1)
         natom = atype.shape[0]
         coord = np.ascontiguousarray(coord, dtype=np.float64).reshape(-1, natom * 3)
         nf = coord.shape[0]
         boxa = None if box is None else np.ascontiguousarray(box, dtype=np.float64).reshape(nf, 9)
-        e = np.empty(nf)  # every output element is written by the call
-        f = np.empty((nf, natom, 3))
-        v = np.empty((nf, 9))
+        if out is not None:
+            e, f, v = out
+            if not (e.flags.c_contiguous and f.flags.c_contiguous and v.flags.c_contiguous) or \
+                    e.size != nf or f.size != nf * natom * 3 or v.size != nf * 9:
+                raise ValueError("out arrays must be C-contiguous float64 of the output sizes")
+        else:
+            e = np.empty(nf)  # every output element is written by the call
+            f = np.empty((nf, natom, 3))
+            v = np.empty((nf, 9))
         ae = np.empty((nf, natom)) if atomic else None
         av = np.empty((nf, natom, 9)) if atomic else None
         dp = C.POINTER(C.c_double)

@@ -452,7 +452,9 @@ const char* dpgb_deeppot_check_ok(dpgb_deeppot* dp);
  * allocated): energy [nframes], force [nframes, natom, 3], virial
  * [nframes, 9], atom_energy [nframes, natom] or NULL, atom_virial
  * [nframes, natom, 9] or NULL.  Copies in, evaluates, copies out and
- * synchronises its stream.  Neighbour lists are rebuilt every call. */
+ * synchronises its stream.  Page-locked (pinned) buffers are copied
+ * directly, pageable ones through a pinned staging block.  Neighbour lists
+ * are rebuilt every call (unless dpgb_deeppot_set_skin). */
 int dpgb_deeppot_compute(dpgb_deeppot* dp, int nframes, int natom,
                          const double* coord, const int* atype,
                          const double* box, double* energy, double* force,

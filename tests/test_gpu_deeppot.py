@@ -252,3 +252,22 @@ def test_list_read_waits_for_the_callers_stream(cuda):
     late = dp.last_nlist()[0]
     assert not np.array_equal(first, late)  # the walk changed the list
     np.testing.assert_array_equal(early, late)
+
+
+def test_host_api_with_pinned_buffers(cuda):
+    """Page-locked caller buffers (copied without staging) give the same
+    results as pageable ones."""
+    from dpgb import synth
+    from dpgb.deeppot import DeepPot, pinned_empty
+
+    coord, atype, box = synth.water_box(6, seed=9)
+    dp = DeepPot(water_params(), "mixed")
+    e0, f0, v0 = dp.eval(coord.reshape(1, -1), box.reshape(1, 9), atype)
+    cp = pinned_empty((1, coord.size))
+    cp[:] = coord.reshape(1, -1)
+    outs = (pinned_empty((1,)), pinned_empty((1, atype.size, 3)), pinned_empty((1, 9)))
+    e1, f1, v1 = dp.eval(cp, box.reshape(1, 9), atype, out=outs)
+    assert e1 is outs[0] and f1 is outs[1]
+    np.testing.assert_array_equal(e1, e0)
+    np.testing.assert_array_equal(f1, f0)
+    np.testing.assert_array_equal(v1, v0)
