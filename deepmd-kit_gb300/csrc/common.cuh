@@ -111,6 +111,17 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   const float bb = s - a;
   e = (a - (s - bb)) + (b - bb);
 }
+// (a + s) - b in FP32 from hi + lo splits of each term: two error-free sums
+// (two_sum) carry the rounding of the high parts into the low-order part,
+// so the result is the exact value rounded once more, within 2^-24 of it
+// plus a term of order 2^-48 of the operands (FP32 instructions only; the
+// FP64 pipe is narrow on this part)
+__device__ __forceinline__ float disp_split(float ah, float al, float sh, float sl, float bh, float bl) {
+  float s1, e1, s2, e2;
+  two_sum(ah, sh, s1, e1);
+  two_sum(s1, -bh, s2, e2);
+  return s2 + (((al + sl) - bl) + (e1 + e2));
+}
 __device__ __forceinline__ void comp_add(float& hi, float& lo, float x) {
   float e;
   two_sum(hi, x, hi, e);

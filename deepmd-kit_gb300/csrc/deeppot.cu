@@ -429,7 +429,7 @@ struct DeepPotImpl {
   std::vector<int> skin_atype;
   int skin_nframes = -1;
   const void* skin_cand_ptr = nullptr;
-  DeviceBuffer ws_gate, ws_cand, ws_skin_off, ws_skin_ref, ws_coordf, ws_svecf;
+  DeviceBuffer ws_gate, ws_cand, ws_skin_off, ws_skin_ref, ws_coordf, ws_svecf, ws_coordflo, ws_svecflo;
   // single-system CUDA graph (dpgb_deeppot_set_graph): one evaluation of a
   // periodic system captured and replayed on the handle's stream while the
   // key (frames, atoms, box, buffers) and the handle's state (gen) hold
@@ -1152,7 +1152,9 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     DPGB_TRY(dp.ws_skin_off.alloc(sizeof(double) * nrows * 3));
     DPGB_TRY(dp.ws_skin_ref.alloc(sizeof(double) * nrows * 3));
     DPGB_TRY(dp.ws_coordf.alloc(sizeof(float4) * nrows));
+    DPGB_TRY(dp.ws_coordflo.alloc(sizeof(float4) * nrows));
     DPGB_TRY(dp.ws_svecf.alloc(sizeof(float4) * (size_t)nshift_max * nframes));
+    DPGB_TRY(dp.ws_svecflo.alloc(sizeof(float4) * (size_t)nshift_max * nframes));
     const std::vector<double> box_now(box_host, box_host + 9 * (size_t)nframes);
     const void* ptrs = dp.ws_cand.ptr;
     const bool same = dp.skin_nframes == nframes && dp.skin_box == box_now && dp.skin_atype == dp.atype_cache &&
@@ -1192,11 +1194,18 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     }
     DPGB_CUDA(cudaMemcpyAsync(dp.ws_svec.ptr, sv.data(), sizeof(double) * sv.size(), cudaMemcpyHostToDevice, st));
     DPGB_CUDA(cudaMemcpyAsync(dp.ws_spos.ptr, sp.data(), sizeof(int) * sp.size(), cudaMemcpyHostToDevice, st));
-    if (skin_on) {
-      std::vector<float4> svf((size_t)nshift_max * nframes);
-      for (size_t q = 0; q < svf.size(); ++q)
-        svf[q] = make_float4((float)sv[3 * q], (float)sv[3 * q + 1], (float)sv[3 * q + 2], 0.f);
-      DPGB_CUDA(cudaMemcpyAsync(dp.ws_svecf.ptr, svf.data(), sizeof(float4) * svf.size(), cudaMemcpyHostToDevice, st));
+    if (skin_on) {  // the shifts' FP32 high and low parts
+      std::vector<float4> svf((size_t)2 * nshift_max * nframes);
+      const size_t nsv = (size_t)nshift_max * nframes;
+      for (size_t q = 0; q < nsv; ++q) {
+        const float h[3] = {(float)sv[3 * q], (float)sv[3 * q + 1], (float)sv[3 * q + 2]};
+        svf[q] = make_float4(h[0], h[1], h[2], 0.f);
+        svf[nsv + q] = make_float4((float)(sv[3 * q] - (double)h[0]), (float)(sv[3 * q + 1] - (double)h[1]),
+                                   (float)(sv[3 * q + 2] - (double)h[2]), 0.f);
+      }
+      DPGB_CUDA(cudaMemcpyAsync(dp.ws_svecf.ptr, svf.data(), sizeof(float4) * nsv, cudaMemcpyHostToDevice, st));
+      DPGB_CUDA(cudaMemcpyAsync(dp.ws_svecflo.ptr, svf.data() + nsv, sizeof(float4) * nsv, cudaMemcpyHostToDevice,
+                                st));
     }
   }
   double* coord_n = dp.ws_coord.as<double>();
@@ -1226,13 +1235,16 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       const size_t a0 = (size_t)f * natom;
       const double* svf = dp.ws_svec.as<double>() + (size_t)3 * nshift_max * f;
       int* cand = dp.ws_cand.as<int>() + a0 * ncand;
-      DPGB_TRY(launch_skin_coords(cout, dp.ws_coordf.as<float4>() + a0, dp.ws_skin_off.as<double>() + 3 * a0,
-                                  dp.ws_skin_ref.as<double>() + 3 * a0, cin, natom, geo[f], gate, st, status));
+      DPGB_TRY(launch_skin_coords(cout, dp.ws_coordf.as<float4>() + a0, dp.ws_coordflo.as<float4>() + a0,
+                                  dp.ws_skin_off.as<double>() + 3 * a0, dp.ws_skin_ref.as<double>() + 3 * a0, cin,
+                                  natom, geo[f], gate, st, status));
       DPGB_TRY(launch_nlist_pt(cand, cout, dp.atype_dev.as<int>(), natom, geo[f], dp.ws_spos.as<int>() + spos_n * f,
                                svf, rc_geo, dp.skin_sel, dp.ws_cell.ptr, status, st, gate));
       DPGB_TRY(launch_skin_select(nlist + a0 * nnei, cand, ncand, cout, dp.ws_coordf.as<float4>() + a0,
-                                  dp.atype_dev.as<int>(), svf, dp.ws_svecf.as<float4>() + (size_t)nshift_max * f,
-                                  natom, d.rcut, skin_margin, dp.sel, status, st));
+                                  dp.ws_coordflo.as<float4>() + a0, dp.atype_dev.as<int>(), svf,
+                                  dp.ws_svecf.as<float4>() + (size_t)nshift_max * f,
+                                  dp.ws_svecflo.as<float4>() + (size_t)nshift_max * f, natom, d.rcut, skin_margin,
+                                  dp.sel, status, st));
       launches += 7;
       continue;
     }

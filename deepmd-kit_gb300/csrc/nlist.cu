@@ -1471,9 +1471,9 @@ __global__ void skin_check_kernel(int* __restrict__ gate, const double* __restri
 
 // build evaluation: wrap, keep the wrap offset and the reference position;
 // reuse evaluation: the caller's coordinates plus the build's wrap offset
-__global__ void skin_coords_kernel(double* __restrict__ out, float4* __restrict__ outf, double* __restrict__ off,
-                                   double* __restrict__ ref, const double* __restrict__ in, int n, CellGeom g,
-                                   const int* __restrict__ gate, int* __restrict__ status) {
+__global__ void skin_coords_kernel(double* __restrict__ out, float4* __restrict__ outf, float4* __restrict__ outflo,
+                                   double* __restrict__ off, double* __restrict__ ref, const double* __restrict__ in,
+                                   int n, CellGeom g, const int* __restrict__ gate, int* __restrict__ status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   flag_nonfinite(in + 3 * i, i, status);
@@ -1491,13 +1491,18 @@ __global__ void skin_coords_kernel(double* __restrict__ out, float4* __restrict_
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) out[3 * i + k] = o[k];
-  outf[i] = make_float4((float)o[0], (float)o[1], (float)o[2], 0.f);
+  const float h[3] = {(float)o[0], (float)o[1], (float)o[2]};
+  outf[i] = make_float4(h[0], h[1], h[2], 0.f);
+  outflo[i] = make_float4((float)(o[0] - (double)h[0]), (float)(o[1] - (double)h[1]), (float)(o[2] - (double)h[2]), 0.f);
 }
 
 // One warp per centre atom: FP32 prefilter over the candidate row (absolute
 // FP32 coordinates; the margin covers their rounding), then for the packed
-// survivors the FP64 displacement (r_j + shift) - r_i rounded to FP32 and an
-// FP32 distance within eps of the exact one.  Those decide the cutoff and the
+// survivors the displacement (r_j + shift) - r_i from the hi + lo FP32
+// splits of coordinates and shifts (the exact displacement rounded once to
+// FP32, as the FP64 difference rounded to FP32 would be within its bound,
+// without the narrow FP64 pipe) and an FP32 distance within eps of the
+// exact one.  Those decide the cutoff and the
 // order unless a distance lies within eps of rcut or two within 2 eps of
 // each other: then the atom is redone with exact FP64 distances.  The list
 // is that of a fresh build on the same coordinates.
@@ -1505,8 +1510,9 @@ constexpr int kSkinWarps = 4;
 
 __global__ void __launch_bounds__(kSkinWarps * 32)
 skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int ncand, const double* __restrict__ coord,
-                   const float4* __restrict__ coordf, const int* __restrict__ atype, const double* __restrict__ svec,
-                   const float4* __restrict__ svecf, int nloc, double rcut, float rcf2, float eps, SelInfo sel,
+                   const float4* __restrict__ coordf, const float4* __restrict__ coordflo,
+                   const int* __restrict__ atype, const double* __restrict__ svec, const float4* __restrict__ svecf,
+                   const float4* __restrict__ svecflo, int nloc, double rcut, float rcf2, float eps, SelInfo sel,
                    int* __restrict__ status) {
   __shared__ double s_r[kSkinWarps][kKeptCap];
   __shared__ int s_i[kSkinWarps][kKeptCap];
@@ -1520,7 +1526,7 @@ skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int nc
   __syncwarp();
   if (atype[i] < 0) return;
   const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
-  const float4 fi = coordf[i];
+  const float4 fi = coordf[i], fil = coordflo[i];
   const int* c = cand + (size_t)i * ncand;
   double* wr = s_r[warp];
   float* wf = reinterpret_cast<float*>(wr);
@@ -1564,9 +1570,10 @@ skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int nc
       e = wi[k];
       const int s = e / nloc, j = e - s * nloc;
       t = atype[j];
-      const float fx = (float)((coord[3 * j] + svec[3 * s]) - xi);
-      const float fy = (float)((coord[3 * j + 1] + svec[3 * s + 1]) - yi);
-      const float fz = (float)((coord[3 * j + 2] + svec[3 * s + 2]) - zi);
+      const float4 jh = coordf[j], jl = coordflo[j], sh = svecf[s], sl = svecflo[s];
+      const float fx = disp_split(jh.x, jl.x, sh.x, sl.x, fi.x, fil.x);
+      const float fy = disp_split(jh.y, jl.y, sh.y, sl.y, fi.y, fil.y);
+      const float fz = disp_split(jh.z, jl.z, sh.z, sl.z, fi.z, fil.z);
       r = sqrtf(fx * fx + fy * fy + fz * fz);
       keep = r <= rout;
       band |= keep && r > rin;
@@ -1659,22 +1666,25 @@ int launch_skin_check(int* gate, const double* coord, const double* ref, int n, 
   return check_launch("skin_check");
 }
 
-int launch_skin_coords(double* out, float4* outf, double* off, double* ref, const double* in, int n,
+int launch_skin_coords(double* out, float4* outf, float4* outflo, double* off, double* ref, const double* in, int n,
                        const CellGeom& g, const int* gate, cudaStream_t st, int* status) {
   if (n <= 0) return DPGB_OK;
-  skin_coords_kernel<<<ceil_div(n, 256), 256, 0, st>>>(out, outf, off, ref, in, n, g, gate, status);
+  skin_coords_kernel<<<ceil_div(n, 256), 256, 0, st>>>(out, outf, outflo, off, ref, in, n, g, gate, status);
   return check_launch("skin_coords");
 }
 
 int launch_skin_select(int* nlist, const int* cand, int ncand, const double* coord, const float4* coordf,
-                       const int* atype, const double* svec, const float4* svecf, int nloc, double rcut,
-                       double margin, const SelInfo& sel, int* status, cudaStream_t st) {
+                       const float4* coordflo, const int* atype, const double* svec, const float4* svecf,
+                       const float4* svecflo, int nloc, double rcut, double margin, const SelInfo& sel, int* status,
+                       cudaStream_t st) {
   if (nloc <= 0) return DPGB_OK;
   const float rcf = (float)(rcut + margin);
-  // FP64 displacement rounded to FP32 (<= 2^-24 r) plus the FP32 norm (<= 2^-22 r), x1.5
+  // displacement: the exact one rounded to FP32 (<= 2^-24 r, plus ~2^-48 of
+  // the coordinates' magnitude), FP32 norm (<= 2^-22 r), x1.5
   const float eps = (float)(rcut * 1.5 * (0x1p-24 + 0x1p-22) + 1e-7);
   skin_select_kernel<<<ceil_div(nloc, kSkinWarps), kSkinWarps * 32, 0, st>>>(
-      nlist, cand, ncand, coord, coordf, atype, svec, svecf, nloc, rcut, rcf * rcf, eps, sel, status);
+      nlist, cand, ncand, coord, coordf, coordflo, atype, svec, svecf, svecflo, nloc, rcut, rcf * rcf, eps, sel,
+      status);
   return check_launch("skin_select");
 }
 

@@ -121,16 +121,18 @@ int read_status(int* status_dev, cudaStream_t st, int out[kStatusSlots]);
 int launch_skin_check(int* gate, const double* coord, const double* ref, int n, double skin, int every,
                       cudaStream_t st);
 // build: out = wrapped coordinates, off = out - in, ref = in; reuse: out =
-// in + off; outf = FP32 copy of out (prefilter of the selection)
-int launch_skin_coords(double* out, float4* outf, double* off, double* ref, const double* in, int n,
+// in + off; outf / outflo = the FP32 high and low parts of out (the
+// selection's prefilter and its split-FP32 displacements)
+int launch_skin_coords(double* out, float4* outf, float4* outflo, double* off, double* ref, const double* in, int n,
                        const CellGeom& g, const int* gate, cudaStream_t st, int* status = nullptr);
 // the list at rcut from the candidate rows [nloc, ncand] (extended indices
 // s * nloc + j, -1 padding): the same ranking and per-type placement as a
 // fresh build on the same coordinates.  margin: FP32 prefilter radius above
 // rcut (covers the FP32 rounding of coordinates and shifts)
 int launch_skin_select(int* nlist, const int* cand, int ncand, const double* coord, const float4* coordf,
-                       const int* atype, const double* svec, const float4* svecf, int nloc, double rcut,
-                       double margin, const SelInfo& sel, int* status, cudaStream_t st);
+                       const float4* coordflo, const int* atype, const double* svec, const float4* svecf,
+                       const float4* svecflo, int nloc, double rcut, double margin, const SelInfo& sel, int* status,
+                       cudaStream_t st);
 // gate[1] = gate[0] ? 1 : gate[1] + 1; gate[0] = 0
 int launch_skin_advance(int* gate, cudaStream_t st);
 int sel_from_host(const int* sel_host, int ntypes, SelInfo& s);

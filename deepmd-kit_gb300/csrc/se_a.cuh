@@ -108,17 +108,6 @@ struct DescParams {
   const float4* slo;
 };
 
-// (a + s) - b in FP32 from hi + lo splits of each term: two error-free sums
-// (two_sum) carry the rounding of the high parts into the low-order part,
-// so the result is the exact value rounded once more (FP32 instructions
-// only; the FP64 pipe is narrow on this part)
-__device__ __forceinline__ float disp_split(float ah, float al, float sh, float sl, float bh, float bl) {
-  float s1, e1, s2, e2;
-  two_sum(ah, sh, s1, e1);
-  two_sum(s1, -bh, s2, e2);
-  return s2 + (((al + sl) - bl) + (e1 + e2));
-}
-
 // r_nb - r_i in FP64 for neighbour nb of local atom i of frame f, and the
 // neighbour's type.  Image-major indices: r_nb = coord[nb % nloc] + shift.
 template <typename T>
