@@ -189,6 +189,29 @@ struct DeviceBuffer {
   }
 };
 
+// Device scratch reused across the calls of one host thread (grow-only,
+// one buffer per slot, reallocated when the thread's current device
+// changes): a call that uses it must be done with it on the device before
+// it returns (the op-level entries that use it synchronise their stream
+// before returning), so the thread's next call may overwrite it.
+inline DeviceBuffer& thread_scratch(int slot) {
+  struct Slot {
+    DeviceBuffer buf;
+    int device = -1;
+  };
+  thread_local Slot slots[4];
+  Slot& s = slots[slot & 3];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (s.device != dev) {
+    if (s.buf.ptr) cudaFree(s.buf.ptr);
+    s.buf.ptr = nullptr;
+    s.buf.bytes = 0;
+    s.device = dev;
+  }
+  return s.buf;
+}
+
 // Page-locked host staging (copies to and from it run asynchronously and at
 // full link speed; the caller's own arrays are pageable).
 struct PinnedBuffer {

@@ -263,7 +263,7 @@ int gather_pairs(T* out, const T* pg, const int* nlist, int nf, int nloc, int na
                  const char* who) {
   const long long npair = (long long)nf * nloc * nnei;
   const long long nkeys = (long long)nf * nall;
-  DeviceBuffer ws;
+  DeviceBuffer& ws = thread_scratch(0);  // done with before the status read below returns
   const size_t key_bytes = sizeof(int) * (size_t)npair;
   const size_t tr_bytes = transpose_workspace(npair, (int)nkeys);
   DPGB_TRY(ws.alloc(key_bytes + tr_bytes + sizeof(int) * kStatusSlots + 64));
@@ -307,7 +307,7 @@ int env_bwd(T* g_coord, const T* g_em, const T* g_diff, const T* g_sw, const T* 
   if (!g_coord || !coord || !atype || !nlist || !std) return fail(DPGB_EINVAL, "env_mat_pt_bwd: NULL pointer");
   cudaStream_t st = as_stream(stream);
   const long long n = (long long)nf * nloc * nnei;
-  DeviceBuffer pgb;
+  DeviceBuffer& pgb = thread_scratch(1);  // read by the gather, which synchronises
   DPGB_TRY(pgb.alloc(sizeof(T) * 3 * (size_t)std::max<long long>(n, 1)));
   if (n > 0) {
     env_bwd_pair_kernel<T><<<ceil_div(n, 256), 256, 0, st>>>(pgb.as<T>(), g_em, g_diff, g_sw, nlist, coord, atype, std,
@@ -327,7 +327,7 @@ int env_bwd_bwd(T* gg_em, T* gg_diff, T* gg_sw, T* gg_coord, const T* u, const T
   if (!gg_em || !u || !coord || !atype || !nlist || !std) return fail(DPGB_EINVAL, "env_mat_pt_bwd_bwd: NULL pointer");
   cudaStream_t st = as_stream(stream);
   const long long n = (long long)nf * nloc * nnei;
-  DeviceBuffer pgb;
+  DeviceBuffer& pgb = thread_scratch(1);  // used only with gg_coord, whose gather synchronises
   if (gg_coord) DPGB_TRY(pgb.alloc(sizeof(T) * 3 * (size_t)std::max<long long>(n, 1)));
   if (n > 0) {
     env_bwd_bwd_pair_kernel<T><<<ceil_div(n, 256), 256, 0, st>>>(gg_em, gg_diff, gg_sw, gg_coord ? pgb.as<T>() : nullptr,

@@ -2,6 +2,7 @@
 // the reference PyTorch order, and the formatting of a candidate list in the
 // reference C++ order.  Also the sorted transpose of a list used to gather
 // neighbour contributions without atomics.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -1824,6 +1825,71 @@ int dpgb_extend_coord(double* cext, int* text, int* mapping, const double* coord
   DPGB_CUDA(cudaMemcpyAsync(d.ptr, svec.data(), sizeof(double) * svec.size(), cudaMemcpyHostToDevice, st));
   DPGB_TRY(launch_extend(cext, text, mapping, coord, atype, nloc, nshift, d.as<double>(), st));
   DPGB_CUDA(cudaStreamSynchronize(st));  // before the temporary is freed
+  return DPGB_OK;
+}
+
+int dpgb_extend_input_and_build_nlist(double* coord_ext, int* atype_ext, int* mapping, int* nlist,
+                                      const double* coord, const int* atype, int nframes, int nloc,
+                                      const double* box, const int* shift_idx, int nshift, double rcut,
+                                      const int* sel_host, int ntypes, void* stream) {
+  clear_error();
+  SelInfo sel;
+  DPGB_TRY(sel_from_host(sel_host, ntypes, sel));
+  if (nframes < 1 || nloc < 1 || !coord_ext || !atype_ext || !mapping || !nlist || !coord || !atype || !box ||
+      !shift_idx || nshift < 1 || !(rcut > 0))
+    return fail(DPGB_EINVAL, "extend_input_and_build_nlist: bad args");
+  if ((long long)nframes * nloc * nshift >= (1LL << 31) || (long long)nframes * nloc * sel.nnei >= (1LL << 31))
+    return fail(DPGB_EINVAL, "extend_input_and_build_nlist: too large");
+  cudaStream_t st = as_stream(stream);
+  // host geometry of every frame, then one workspace for the largest
+  std::vector<CellGeom> geo(nframes);
+  std::vector<std::vector<int>> spos(nframes);
+  std::vector<std::vector<double>> svec(nframes);
+  size_t wbytes = 0, nspos = 1;
+  for (int f = 0; f < nframes; ++f) {
+    for (int k = 0; k < 9; ++k)
+      if (!std::isfinite(box[9 * (size_t)f + k])) return fail(DPGB_EINVAL, "extend_input_and_build_nlist: non-finite cell");
+    DPGB_TRY(periodic_geom(box + 9 * (size_t)f, rcut, nshift, shift_idx, geo[f], spos[f]));
+    shift_vectors(geo[f], shift_idx, nshift, svec[f]);
+    wbytes = std::max(wbytes, nlist_pt_workspace(nloc, geo[f]));
+    nspos = std::max(nspos, spos[f].size());
+  }
+  const size_t a16 = 16;
+  auto up = [&](size_t b) { return (b + a16 - 1) / a16 * a16; };
+  const size_t b_status = up(sizeof(int) * kStatusSlots), b_spos = up(sizeof(int) * nspos * nframes),
+               b_sv = up(sizeof(double) * 3 * (size_t)nshift * nframes), b_wrap = up(sizeof(double) * 3 * nloc);
+  DeviceBuffer& ws = thread_scratch(2);  // done with before the status read below returns
+  DPGB_TRY(ws.alloc(b_status + b_spos + b_sv + b_wrap + wbytes + 64));
+  char* base = ws.as<char>();
+  int* status = reinterpret_cast<int*>(base);
+  int* spos_d = reinterpret_cast<int*>(base + b_status);
+  double* sv_d = reinterpret_cast<double*>(base + b_status + b_spos);
+  double* wrapped = reinterpret_cast<double*>(base + b_status + b_spos + b_sv);
+  void* work = base + b_status + b_spos + b_sv + b_wrap;
+  std::vector<int> spos_all(nspos * nframes, -1);
+  std::vector<double> sv_all(3 * (size_t)nshift * nframes);
+  for (int f = 0; f < nframes; ++f) {
+    std::copy(spos[f].begin(), spos[f].end(), spos_all.begin() + nspos * f);
+    std::copy(svec[f].begin(), svec[f].end(), sv_all.begin() + 3 * (size_t)nshift * f);
+  }
+  DPGB_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * kStatusSlots, st));
+  DPGB_CUDA(cudaMemcpyAsync(spos_d, spos_all.data(), sizeof(int) * spos_all.size(), cudaMemcpyHostToDevice, st));
+  DPGB_CUDA(cudaMemcpyAsync(sv_d, sv_all.data(), sizeof(double) * sv_all.size(), cudaMemcpyHostToDevice, st));
+  const size_t nall = (size_t)nloc * nshift;
+  for (int f = 0; f < nframes; ++f) {  // frames in stream order share the wrap buffer and the workspace
+    const double* sv_f = sv_d + 3 * (size_t)nshift * f;
+    DPGB_TRY(launch_normalize(wrapped, coord + 3 * (size_t)nloc * f, nloc, geo[f], st, status));
+    DPGB_TRY(launch_extend(coord_ext + 3 * nall * f, atype_ext + nall * f, mapping + nall * f, wrapped,
+                           atype + (size_t)nloc * f, nloc, nshift, sv_f, st));
+    DPGB_TRY(launch_nlist_pt(nlist + (size_t)nloc * sel.nnei * f, wrapped, atype + (size_t)nloc * f, nloc, geo[f],
+                             spos_d + nspos * f, sv_f, rcut, sel, work, status, st));
+  }
+  int h[kStatusSlots];
+  DPGB_TRY(read_status(status, st, h));  // also keeps the workspace alive until the kernels are done
+  if (h[kStatusNonFinite] > 0) return fail(DPGB_EINVAL, "extend_input_and_build_nlist: non-finite coordinate");
+  if (h[kStatusOverflow] > 0)
+    return fail(DPGB_EOVERFLOW, "extend_input_and_build_nlist: atom " + std::to_string(h[kStatusOverflowAtom] - 1) +
+                                    " has more than 1024 atoms within rcut");
   return DPGB_OK;
 }
 

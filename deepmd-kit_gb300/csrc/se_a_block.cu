@@ -26,7 +26,7 @@
 namespace dpgb {
 namespace {
 
-constexpr int kBlockThreads = 128;
+constexpr int kBlockThreads = 256;
 constexpr int kMaxLayers = DPGB_MAX_LAYERS;
 constexpr int kMaskDim = DPGB_MAX_TYPES + 1;
 
@@ -44,6 +44,7 @@ struct BlockGeom {
   int pnet;                   // parameters per net
   int keep[kMaskDim * kMaskDim];
   int want_pgrad;
+  int stage_w;  // the current net's parameters staged in shared memory (else read from global memory)
 };
 
 template <typename T>
@@ -55,6 +56,7 @@ __device__ __forceinline__ float tanh_b<float>(float x) { return tanhf(x); }
 
 template <typename T>
 struct Smem {
+  T* w;  // the current net's parameters (staged per section)
   T *rr, *u, *X, *C, *A, *Xd;
   T *a, *ad, *t, *zd;  // [CH][sw] activations, tangents; [CH][sw] tanh, z-dot (layer l at aoff[l])
   T *bar[2], *dbar[2], *zb, *zdb;  // [CH][maxw]
@@ -69,12 +71,14 @@ __host__ __device__ inline size_t block_smem_elems(const BlockGeom& g, int ch) {
   n += 4 * (size_t)4 * g.ng;        // X, C, A, Xd
   n += 4 * (size_t)ch * g.sw;       // a, ad, t, zd
   n += 6 * (size_t)ch * g.maxw;     // bar x2, dbar x2, zb, zdb
+  if (g.stage_w) n += (size_t)g.pnet;  // w
   return n;
 }
 
 template <typename T>
 __device__ void carve(Smem<T>& s, const BlockGeom& g, int ch, unsigned char* base) {
   T* p = reinterpret_cast<T*>(base);
+  s.w = p; p += g.stage_w ? g.pnet : 0;
   s.rr = p; p += g.nnei * 4;
   s.u = p; p += g.nnei * 4;
   s.X = p; p += 4 * g.ng;
@@ -111,27 +115,52 @@ __device__ void dual_forward(const BlockGeom& g, const T* __restrict__ W, const 
     const T* b = W + g.boff[l - 1];
     const T* id = g.resnet_dt ? W + g.ioff[l - 1] : nullptr;
     const int ai = g.aoff[l - 1], ao = g.aoff[l];
-    for (int q = tid; q < np * nout; q += blockDim.x) {
-      const int p = q / nout, n = q - p * nout;
+    // one thread: four outputs n = t, t + n4, t + 2 n4, t + 3 n4 of one
+    // pair (x[k] read once for the four; consecutive threads read
+    // consecutive weights; each output's sum in the same order as one at a
+    // time)
+    const int n4 = (nout + 3) >> 2;
+    for (int q = tid; q < np * n4; q += blockDim.x) {
+      const int p = q / n4, t0 = q - p * n4;
       const T* x = s.a + p * g.sw + ai;
-      T z = b[n];
-      for (int k = 0; k < nin; ++k) z += x[k] * Wm[k * nout + n];
-      const T t = tanh_b(z);
-      T y = id ? t * id[n] : t;
-      if (nout == nin) y += x[n];
-      else if (nout == 2 * nin) y += x[n % nin];
-      s.a[p * g.sw + ao + n] = y;
-      s.t[p * g.sw + ao + n] = t;
-      if (TAN) {
-        const T* xd = s.ad + p * g.sw + ai;
-        T zd = T(0);
-        for (int k = 0; k < nin; ++k) zd += xd[k] * Wm[k * nout + n];
-        const T td = (T(1) - t * t) * zd;
-        T yd = id ? td * id[n] : td;
-        if (nout == nin) yd += xd[n];
-        else if (nout == 2 * nin) yd += xd[n % nin];
-        s.ad[p * g.sw + ao + n] = yd;
-        s.zd[p * g.sw + ao + n] = zd;
+      const T* xd = s.ad + p * g.sw + ai;
+      T z[4], zd[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        z[j] = t0 + j * n4 < nout ? b[t0 + j * n4] : T(0);
+        zd[j] = T(0);
+      }
+      for (int k = 0; k < nin; ++k) {
+        const T xk = x[k];
+        const T xdk = TAN ? xd[k] : T(0);
+        const T* wr = Wm + k * nout + t0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (t0 + j * n4 < nout) {
+            const T w = wr[j * n4];
+            z[j] += xk * w;
+            if (TAN) zd[j] += xdk * w;
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int n = t0 + j * n4;
+        if (n >= nout) break;
+        const T t = tanh_b(z[j]);
+        T y = id ? t * id[n] : t;
+        if (nout == nin) y += x[n];
+        else if (nout == 2 * nin) y += x[n % nin];
+        s.a[p * g.sw + ao + n] = y;
+        s.t[p * g.sw + ao + n] = t;
+        if (TAN) {
+          const T td = (T(1) - t * t) * zd[j];
+          T yd = id ? td * id[n] : td;
+          if (nout == nin) yd += xd[n];
+          else if (nout == 2 * nin) yd += xd[n % nin];
+          s.ad[p * g.sw + ao + n] = yd;
+          s.zd[p * g.sw + ao + n] = zd[j];
+        }
       }
     }
     __syncthreads();
@@ -143,7 +172,8 @@ __device__ void dual_forward(const BlockGeom& g, const T* __restrict__ W, const 
 // buffer index holds the cotangent of s in column 0.  Parameter gradients of
 // this chunk are added to pg (this row's slice for the net) when non-null.
 template <typename T, bool TAN>
-__device__ int dual_reverse(const BlockGeom& g, const T* __restrict__ W, const Smem<T>& s, int np, T* __restrict__ pg) {
+__device__ int dual_reverse(const BlockGeom& g, const T* __restrict__ W, const Smem<T>& s, int np,
+                            T* __restrict__ pg) {
   const int tid = threadIdx.x;
   int cur = 0;
   for (int l = g.n_layer; l >= 1; --l) {
@@ -169,14 +199,30 @@ __device__ int dual_reverse(const BlockGeom& g, const T* __restrict__ W, const S
     __syncthreads();
     if (pg) {
       T* gW = pg + g.woff[l - 1];
-      for (int q = tid; q < nin * nout; q += blockDim.x) {
-        const int k = q / nout, n = q - k * nout;
-        T acc = gW[q];
+      // one thread: n = t, t + n4, t + 2 n4, t + 3 n4 of one k (each sum
+      // in pair order; consecutive threads on consecutive n)
+      const int n4 = (nout + 3) >> 2;
+      for (int q = tid; q < nin * n4; q += blockDim.x) {
+        const int k = q / n4, t0 = q - k * n4;
+        T acc[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[j] = t0 + j * n4 < nout ? gW[k * nout + t0 + j * n4] : T(0);
         for (int p = 0; p < np; ++p) {
-          acc += s.a[p * g.sw + ai + k] * s.zb[p * g.maxw + n];
-          if (TAN) acc += s.ad[p * g.sw + ai + k] * s.zdb[p * g.maxw + n];
+          const T av = s.a[p * g.sw + ai + k];
+          const T* zr = s.zb + p * g.maxw + t0;
+          const T adv = TAN ? s.ad[p * g.sw + ai + k] : T(0);
+          const T* zdr = s.zdb + p * g.maxw + t0;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (t0 + j * n4 < nout) {
+              acc[j] += av * zr[j * n4];
+              if (TAN) acc[j] += adv * zdr[j * n4];
+            }
+          }
         }
-        gW[q] = acc;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (t0 + j * n4 < nout) gW[k * nout + t0 + j * n4] = acc[j];
       }
       T* gb = pg + g.boff[l - 1];
       T* gi = g.resnet_dt ? pg + g.ioff[l - 1] : nullptr;
@@ -197,28 +243,57 @@ __device__ int dual_reverse(const BlockGeom& g, const T* __restrict__ W, const S
     }
     T* xb = s.bar[1 - cur];
     T* xdb = s.dbar[1 - cur];
-    for (int q = tid; q < np * nin; q += blockDim.x) {
-      const int p = q / nin, k = q - p * nin;
-      T acc = T(0), accd = T(0);
+    // one thread: k = t, t + k4, t + 2 k4, t + 3 k4 of one pair (zb[n]
+    // read once for the four; each sum in n order)
+    const int k4 = (nin + 3) >> 2;
+    for (int q = tid; q < np * k4; q += blockDim.x) {
+      const int p = q / k4, t0 = q - p * k4;
+      T acc[4] = {T(0), T(0), T(0), T(0)}, accd[4] = {T(0), T(0), T(0), T(0)};
+      const T* zr = s.zb + p * g.maxw;
+      const T* zdr = s.zdb + p * g.maxw;
       for (int n = 0; n < nout; ++n) {
-        const T w = Wm[k * nout + n];
-        acc += s.zb[p * g.maxw + n] * w;
-        if (TAN) accd += s.zdb[p * g.maxw + n] * w;
+        const T zn = zr[n];
+        const T zdn = TAN ? zdr[n] : T(0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int k = t0 + j * k4;
+          if (k < nin) {
+            const T w = Wm[k * nout + n];
+            acc[j] += zn * w;
+            if (TAN) accd[j] += zdn * w;
+          }
+        }
       }
-      if (nout == nin) {
-        acc += yb[p * g.maxw + k];
-        if (TAN) accd += ydb[p * g.maxw + k];
-      } else if (nout == 2 * nin) {
-        acc += yb[p * g.maxw + k] + yb[p * g.maxw + k + nin];
-        if (TAN) accd += ydb[p * g.maxw + k] + ydb[p * g.maxw + k + nin];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int k = t0 + j * k4;
+        if (k >= nin) break;
+        T a0 = acc[j], d0 = accd[j];
+        if (nout == nin) {
+          a0 += yb[p * g.maxw + k];
+          if (TAN) d0 += ydb[p * g.maxw + k];
+        } else if (nout == 2 * nin) {
+          a0 += yb[p * g.maxw + k] + yb[p * g.maxw + k + nin];
+          if (TAN) d0 += ydb[p * g.maxw + k] + ydb[p * g.maxw + k + nin];
+        }
+        xb[p * g.maxw + k] = a0;
+        if (TAN) xdb[p * g.maxw + k] = d0;
       }
-      xb[p * g.maxw + k] = acc;
-      if (TAN) xdb[p * g.maxw + k] = accd;
     }
     __syncthreads();
     cur = 1 - cur;
   }
   return cur;
+}
+
+// the net's parameters into shared memory (section_list's barriers order
+// this against the previous section's last reads; the barrier here against
+// the next reads).  (A transposed copy for the reverse sweep measured
+// slower: the transposition costs more than the bank conflicts it saves.)
+template <typename T>
+__device__ void stage_net(const BlockGeom& g, T* __restrict__ w, const T* __restrict__ src) {
+  for (int q = threadIdx.x; q < g.pnet; q += blockDim.x) w[q] = src[q];
+  __syncthreads();
 }
 
 __device__ __forceinline__ int net_of(const BlockGeom& g, int sec, int ti) {
@@ -230,15 +305,23 @@ template <typename T>
 __device__ void section_list(const BlockGeom& g, const Smem<T>& s, const int* __restrict__ nlist_row,
                              const int* __restrict__ atype_f, int ti, int sec) {
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {  // warp 0, 32 slots at a time, in slot order
+    const int lane = threadIdx.x;
     int n = 0;
-    for (int k = g.sec[sec]; k < g.sec[sec + 1]; ++k) {
-      const int j = nlist_row[k];
-      int tj = (j >= 0 && j < g.nall) ? atype_f[j] : g.ntypes;
-      if (tj < 0 || tj > g.ntypes) tj = g.ntypes;
-      if (g.keep[ti * kMaskDim + tj]) s.list[n++] = k;
+    for (int k0 = g.sec[sec]; k0 < g.sec[sec + 1]; k0 += 32) {
+      const int k = k0 + lane;
+      bool kept = false;
+      if (k < g.sec[sec + 1]) {
+        const int j = nlist_row[k];
+        int tj = (j >= 0 && j < g.nall) ? atype_f[j] : g.ntypes;
+        if (tj < 0 || tj > g.ntypes) tj = g.ntypes;
+        kept = g.keep[ti * kMaskDim + tj] != 0;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, kept);
+      if (kept) s.list[n + __popc(m & ((1u << lane) - 1u))] = k;
+      n += __popc(m);
     }
-    *s.nact = n;
+    if (lane == 0) *s.nact = n;
   }
   __syncthreads();
 }
@@ -308,6 +391,10 @@ se_a_block_kernel(BlockGeom g, const T* __restrict__ params, const T* __restrict
       section_list(g, s, nl, atype_f, ti, sec);
       const int nact = *s.nact;
       const T* W = params + (size_t)net_of(g, sec, ti) * g.pnet;
+      if (g.stage_w) {
+        stage_net(g, s.w, W);
+        W = s.w;
+      }
       for (int c0 = 0; c0 < nact; c0 += CH) {
         const int np = min(CH, nact - c0);
         const int* lst = s.list + c0;
@@ -374,6 +461,10 @@ se_a_block_kernel(BlockGeom g, const T* __restrict__ params, const T* __restrict
     const int nact = *s.nact;
     const int e = net_of(g, sec, ti);
     const T* W = params + (size_t)e * g.pnet;
+    if (g.stage_w) {
+      stage_net(g, s.w, W);
+      W = s.w;
+    }
     T* pg = pgr ? prow + (size_t)sec * g.pnet : nullptr;
     for (int c0 = 0; c0 < nact; c0 += CH) {
       const int np = min(CH, nact - c0);
@@ -418,22 +509,37 @@ se_a_block_kernel(BlockGeom g, const T* __restrict__ params, const T* __restrict
 }
 
 // gparams[e][k] = sum over rows r (in order) and sections s with net(r, s) == e of partial[r][s][k]
+// gparams[e][k] = sum over rows r (in order) and sections s with net(r, s) == e
+// of partial[r][s][k], in two levels: sums over chunks of kReduceRows rows
+// (in row order), then the chunk sums in chunk order
+constexpr int kReduceRows = 64;
+
 template <typename T>
-__global__ void pgrad_reduce_kernel(T* __restrict__ out, const T* __restrict__ part, const int* __restrict__ atype_ext,
-                                    BlockGeom g, int nnets) {
+__global__ void pgrad_chunk_kernel(T* __restrict__ chunk_out, const T* __restrict__ part,
+                                   const int* __restrict__ atype_ext, BlockGeom g, int nnets) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= (long long)nnets * g.pnet) return;
   const int e = (int)(q / g.pnet), k = (int)(q - (long long)e * g.pnet);
   const int sec = g.type_one_side ? e : e / g.ntypes;
   const int tcen = g.type_one_side ? -1 : e % g.ntypes;
+  const int r0 = blockIdx.y * kReduceRows, r1 = min(g.nrows, r0 + kReduceRows);
   T acc = T(0);
-  for (int r = 0; r < g.nrows; ++r) {
+  for (int r = r0; r < r1; ++r) {
     const int f = r / g.nloc, i = r - f * g.nloc;
     const int ti = atype_ext[(size_t)f * g.nall + i];
     if (ti < 0 || ti >= g.ntypes) continue;
     if (tcen >= 0 && ti != tcen) continue;
     acc += part[((size_t)r * g.ntypes + sec) * g.pnet + k];
   }
+  chunk_out[(size_t)blockIdx.y * nnets * g.pnet + q] = acc;
+}
+
+template <typename T>
+__global__ void pgrad_final_kernel(T* __restrict__ out, const T* __restrict__ chunk_out, long long n, int nchunk) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  T acc = T(0);
+  for (int c = 0; c < nchunk; ++c) acc += chunk_out[(size_t)c * n + q];
   out[q] = acc;
 }
 
@@ -499,10 +605,17 @@ size_t smem_bytes(const BlockGeom& g) {
 }
 
 template <typename T, int MODE>
-int launch_block(const BlockGeom& g, const T* params, const T* rr, const int* nlist, const int* atype, const T* xyz_in,
+int launch_block(BlockGeom g, const T* params, const T* rr, const int* nlist, const int* atype, const T* xyz_in,
                  const T* gD, const T* gX, const T* u, T* oD, T* oX, T* orr, T* ogD, T* ogX, T* pg, cudaStream_t st) {
   constexpr int CH = chunk_of<T>();
-  const size_t smem = smem_bytes<T>(g);
+  // FP32: the staged weights take their reads off L1; FP64 is bound by its
+  // narrow pipe, where two CTAs per SM without them do better
+  g.stage_w = sizeof(T) == 4;
+  size_t smem = smem_bytes<T>(g);
+  if (smem > 227 * 1024) {  // no room for the weights: read them from global memory
+    g.stage_w = 0;
+    smem = smem_bytes<T>(g);
+  }
   if (smem > 227 * 1024) return fail(DPGB_EINVAL, "se_a_block: widths too large for one CTA's shared memory");
   auto k = se_a_block_kernel<T, CH, MODE>;
   DPGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -512,10 +625,14 @@ int launch_block(const BlockGeom& g, const T* params, const T* rr, const int* nl
 }
 
 template <typename T>
-int reduce_pgrad(const BlockGeom& g, T* gparams, const T* part, const int* atype, cudaStream_t st) {
+int reduce_pgrad(const BlockGeom& g, T* gparams, T* part, const int* atype, cudaStream_t st) {
   const int nnets = g.type_one_side ? g.ntypes : g.ntypes * g.ntypes;
   const long long n = (long long)nnets * g.pnet;
-  pgrad_reduce_kernel<T><<<ceil_div(n, 128), 128, 0, st>>>(gparams, part, atype, g, nnets);
+  const int nchunk = ceil_div(g.nrows, kReduceRows);
+  T* chunk_out = part + (size_t)g.nrows * g.ntypes * g.pnet;  // after the row partials in the workspace
+  pgrad_chunk_kernel<T><<<dim3(ceil_div(n, 128), nchunk), 128, 0, st>>>(chunk_out, part, atype, g, nnets);
+  DPGB_TRY(check_launch("se_a_block_pgrad_chunks"));
+  pgrad_final_kernel<T><<<ceil_div(n, 128), 128, 0, st>>>(gparams, chunk_out, n, nchunk);
   return check_launch("se_a_block_pgrad_reduce");
 }
 
@@ -532,7 +649,8 @@ int block_fwd(const dpgb_se_a_block* b, const T* params, const T* rr, const int*
 
 template <typename T>
 size_t workspace_bytes(const BlockGeom& g) {
-  return sizeof(T) * (size_t)g.nrows * g.ntypes * g.pnet;
+  const size_t nnets = g.type_one_side ? g.ntypes : (size_t)g.ntypes * g.ntypes;
+  return sizeof(T) * ((size_t)g.nrows * g.ntypes * g.pnet + (size_t)ceil_div(g.nrows, kReduceRows) * nnets * g.pnet);
 }
 
 template <typename T>
@@ -549,7 +667,7 @@ int block_bwd(const dpgb_se_a_block* b, const T* params, const T* rr, const int*
   cudaStream_t st = as_stream(stream);
   DPGB_TRY((launch_block<T, kModeBwd>(g, params, rr, nlist, atype, xyz, gD, gX, nullptr, nullptr, nullptr, grr,
                                       nullptr, nullptr, gparams ? (T*)ws : nullptr, st)));
-  if (gparams && g.nrows > 0) DPGB_TRY(reduce_pgrad<T>(g, gparams, (const T*)ws, atype, st));
+  if (gparams && g.nrows > 0) DPGB_TRY(reduce_pgrad<T>(g, gparams, (T*)ws, atype, st));
   return DPGB_OK;
 }
 
@@ -568,7 +686,7 @@ int block_bwd_bwd(const dpgb_se_a_block* b, const T* params, const T* rr, const 
   cudaStream_t st = as_stream(stream);
   DPGB_TRY((launch_block<T, kModeBwdBwd>(g, params, rr, nlist, atype, nullptr, gD, gX, u_rr, nullptr, nullptr, g_rr,
                                          g_gD, g_gX, g_params ? (T*)ws : nullptr, st)));
-  if (g_params && g.nrows > 0) DPGB_TRY(reduce_pgrad<T>(g, g_params, (const T*)ws, atype, st));
+  if (g_params && g.nrows > 0) DPGB_TRY(reduce_pgrad<T>(g, g_params, (T*)ws, atype, st));
   return DPGB_OK;
 }
 
@@ -588,7 +706,7 @@ long long dpgb_se_a_block_param_count(const dpgb_se_a_block* b) {
 size_t dpgb_se_a_block_workspace_bytes(const dpgb_se_a_block* b, int nf, int nloc, int precision_bytes) {
   BlockGeom g;
   if (make_geom(b, nf, nloc, nloc, g) != DPGB_OK) return 0;
-  return (size_t)precision_bytes * (size_t)g.nrows * g.ntypes * g.pnet;
+  return precision_bytes == 8 ? workspace_bytes<double>(g) : workspace_bytes<float>(g);
 }
 
 int dpgb_se_a_block_fwd_f64(const dpgb_se_a_block* b, const double* params, const double* rr, const int* nlist,

@@ -126,6 +126,7 @@ _SIGS = {
     "dpgb_batch_compute_device": [_P, _P, _P, _P, _P, _P, _I],
     "dpgb_batch_compute": [_P, _DP, _DP, _DP, _DP, _I],
     "dpgb_batch_buckets": [_P, _IP, _IP],
+    "dpgb_extend_input_and_build_nlist": [_P, _P, _P, _P, _P, _P, _I, _I, _DP, _IP, _I, _D, _IP, _I, _P],
     "dpgb_deeppot_descrpt_fwd": [_P, _I, _I, _I, _P, _P, _IP, _P, _P, _P, C.POINTER(C.c_ulonglong), _P],
     "dpgb_deeppot_descrpt_bwd": [_P, C.c_ulonglong, _P, _P, _P],
     "dpgb_batch_set_tiles": [_P, _IP],

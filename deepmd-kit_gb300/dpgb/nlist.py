@@ -125,6 +125,8 @@ def extend_input_and_build_neighbor_list(coord: torch.Tensor, atype: torch.Tenso
     nf = coord.shape[0] if coord.dim() == 3 or (coord.dim() == 2 and atype.dim() == 2) else 1
     coord = coord.reshape(nf, -1, 3)
     atype2 = atype.reshape(nf, -1) if atype.dim() == 2 else atype.reshape(1, -1).expand(nf, -1)
+    if box is not None and nf > 1:
+        return _extend_and_build_frames(coord, atype2, rcut, sel, np.asarray(box, np.float64).reshape(nf, 9), shifts)
     exts, ext_ts, maps, nls = [], [], [], []
     for f in range(nf):
         bf = None if box is None else np.asarray(box, np.float64).reshape(nf, 9)[f]
@@ -140,6 +142,31 @@ def extend_input_and_build_neighbor_list(coord: torch.Tensor, atype: torch.Tenso
         ext_ts.append(ext_t)
         maps.append(mp)
     return torch.stack(exts), torch.stack(ext_ts), torch.stack(maps), torch.stack(nls)
+
+
+def _extend_and_build_frames(coord: torch.Tensor, atype: torch.Tensor, rcut: float, sel: Sequence[int],
+                             box: np.ndarray, shifts: Optional[np.ndarray] = None):
+    """Periodic frames in one library call (dpgb_extend_input_and_build_nlist):
+    the image table from the largest buffer count over the frames, as the
+    reference builds one extended layout for a batch (nlist.py:470-498)."""
+    nf, nloc = coord.shape[0], coord.shape[1]
+    if shifts is None:
+        nbuff = np.max(np.stack([np.ceil(rcut / np.abs(to_face_distance(b))) for b in box]), axis=0)
+        shifts = _image_shifts(tuple(int(n) for n in nbuff)).copy()
+    shifts = np.ascontiguousarray(shifts, np.int32)
+    ns = shifts.shape[0]
+    sel_a = np.ascontiguousarray(sel, np.int32)
+    dev = coord.device
+    c = coord.to(torch.float64).contiguous()
+    at = atype.to(device=dev, dtype=torch.int32).contiguous()
+    ext = torch.empty(nf, ns * nloc, 3, dtype=torch.float64, device=dev)
+    ext_t = torch.empty(nf, ns * nloc, dtype=torch.int32, device=dev)
+    mapping = torch.empty(nf, ns * nloc, dtype=torch.int32, device=dev)
+    nl = torch.empty(nf, nloc, int(sel_a.sum()), dtype=torch.int32, device=dev)
+    b = np.ascontiguousarray(box, np.float64).reshape(nf * 9)
+    _lib.call("dpgb_extend_input_and_build_nlist", _vp(ext), _vp(ext_t), _vp(mapping), _vp(nl), _vp(c), _vp(at),
+              nf, nloc, _dp(b), _ip(shifts), ns, C.c_double(rcut), _ip(sel_a), len(sel_a), _stream())
+    return ext, ext_t, mapping, nl
 
 
 def format_nlist_a(coord_ext: torch.Tensor, atype_ext: torch.Tensor, rows: torch.Tensor, counts: torch.Tensor,

@@ -117,6 +117,25 @@ int dpgb_build_nlist_pt(int* nlist, const double* coord, const int* atype,
                         const int* shift_idx_host, int nshift, double rcut,
                         const int* sel_host, int ntypes, void* stream);
 
+/* The three steps above for nframes periodic frames at once, as
+ * extend_input_and_build_neighbor_list (deepmd/pt/utils/nlist.py:14-46)
+ * does for a batch: every frame wrapped (normalize_coord), its images in the
+ * order shift_idx gives (one table for all frames: the reference takes the
+ * largest image count over the batch) and its typed list; one workspace,
+ * one status read (synchronises the stream once).
+ *   coord [nframes, nloc, 3], atype [nframes, nloc] (device), box_host
+ *   [nframes, 9] -> coord_ext [nframes, nshift * nloc, 3], atype_ext,
+ *   mapping [nframes, nshift * nloc], nlist [nframes, nloc, sum(sel)]
+ *   (device).  Non-finite coordinates or cells return DPGB_EINVAL. */
+int dpgb_extend_input_and_build_nlist(double* coord_ext, int* atype_ext,
+                                      int* mapping, int* nlist,
+                                      const double* coord, const int* atype,
+                                      int nframes, int nloc,
+                                      const double* box_host,
+                                      const int* shift_idx_host, int nshift,
+                                      double rcut, const int* sel_host,
+                                      int ntypes, void* stream);
+
 /* Periodic wrap of coordinates into the cell: deepmd/pt/utils/region.py:86
  * normalize_coord / source/lib/src/gpu/coord.cu:45 normalize_one. */
 int dpgb_normalize_coord(double* coord_out, const double* coord, int natom,

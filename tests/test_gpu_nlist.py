@@ -162,3 +162,24 @@ def test_perfect_lattice_ties_and_cutoff(cuda, spacing):
     ref = O.build_nlist_pt(ext, ext_t, coord.shape[0], 6.0, sel)
     nl = N.build_neighbor_list_local(_t(coord, cuda), _t(atype, cuda, torch.int32), box, 6.0, sel, shifts)
     np.testing.assert_array_equal(nl.cpu().numpy(), ref)
+
+
+def test_frames_in_one_call_equal_frame_by_frame(cuda):
+    """dpgb_extend_input_and_build_nlist over several frames (one call) gives
+    each frame's wrap, images, mapping and list bit for bit as the one-frame
+    functions do."""
+    import torch
+
+    from dpgb import nlist as N, synth
+
+    frames = [synth.water_box(4, seed=60 + k) for k in range(5)]
+    coord = torch.tensor(np.stack([f[0] for f in frames]), dtype=torch.float64, device=cuda)
+    coord = coord + 7.5  # some atoms outside the cell: the wrap matters
+    atype = torch.tensor(np.stack([f[1] for f in frames]), device=cuda)
+    box = np.stack([f[2].reshape(9) for f in frames])
+    ext, ext_t, mp, nl = N.extend_input_and_build_neighbor_list(coord, atype, 6.0, [46, 92], box)
+    for f in range(len(frames)):
+        e1, t1, m1, n1 = N.extend_input_and_build_neighbor_list(coord[f:f + 1], atype[f:f + 1], 6.0, [46, 92],
+                                                                box[f:f + 1])
+        assert torch.equal(ext[f], e1[0]) and torch.equal(ext_t[f], t1[0].to(ext_t.dtype))
+        assert torch.equal(mp[f], m1[0].to(mp.dtype)) and torch.equal(nl[f], n1[0].to(nl.dtype))
