@@ -596,7 +596,7 @@ int make_geom(const dpgb_se_a_block* b, int nf, int nloc, int nall, BlockGeom& g
 
 template <typename T>
 constexpr int chunk_of() {
-  return sizeof(T) == 8 ? 8 : 16;
+  return sizeof(T) == 8 ? 8 : 32;  // pairs per chunk (shared-memory arrays of chunk x width)
 }
 
 template <typename T>

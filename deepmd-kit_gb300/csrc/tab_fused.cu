@@ -204,6 +204,14 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
       for (int r = ch.row0 + warp; r < ch.row1; r += kFwdWarps) {
         const int row = sorted_rows[r];
         float* xr = xyz + (size_t)row * 4 * ng;
+        if (r + kFwdWarps < ch.row1) {
+          // the warp's next atom: its list section (and, after the first
+          // section, its xyz so far) move into L2 while this atom is processed
+          const int nrow = sorted_rows[r + kFwdWarps];
+          const char* nlr = reinterpret_cast<const char*>(p.nlist + (size_t)nrow * p.nnei + p.sec[sec]);
+          if (lane * 128 < 4 * (p.sec[sec + 1] - p.sec[sec])) prefetch_l2(nlr + lane * 128);
+          if (sec > 0 && lane * 128 < 16 * ng) prefetch_l2(reinterpret_cast<const char*>(xyz + (size_t)nrow * 4 * ng) + lane * 128);
+        }
         float acc[4][kTabJ];
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc)
