@@ -17,6 +17,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
+
 #include "fit_tc.cuh"
 #include "tc.cuh"
 
@@ -48,205 +50,375 @@ __device__ __forceinline__ void split_bf16(float v, __nv_bfloat16& hi, __nv_bflo
 }
 
 
-__device__ __forceinline__ void ld16f(const float* p, float* v) {
-  const float4* q = reinterpret_cast<const float4*>(p);
+// --- epilogue staging -------------------------------------------------------
+// Each epilogue warp owns a 2 KB tile of shared memory through which its 32
+// rows x 16 columns pass between the thread-per-row layout of the
+// accumulator and coalesced global accesses (a warp instruction then covers
+// 8 rows x 64 bytes of FP32, or 16 rows x 32 bytes of BF16, instead of 32
+// rows x 16 bytes).  FP32 tile: row r, 16-byte chunk c at unit
+// 4 r + (c ^ ((r >> 1) & 3)); BF16 tile: unit 2 r + (c ^ ((r >> 2) & 1)).
+// Both the row-wise and the coalesced patterns are then free of bank
+// conflicts.
+constexpr int kStageFloats = 32 * 16;  // one warp's tile
+
+__device__ __forceinline__ int unit_f32(int r, int c) { return 4 * r + (c ^ ((r >> 1) & 3)); }
+__device__ __forceinline__ int unit_b16(int r, int c) { return 2 * r + (c ^ ((r >> 2) & 1)); }
+
+// this thread's row (lane) of 16 floats into / out of the tile
+__device__ __forceinline__ void put_row(float4* w, int lane, const float (&v)[16]) {
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const float4 x = q[i];
-    v[4 * i] = x.x;
-    v[4 * i + 1] = x.y;
-    v[4 * i + 2] = x.z;
-    v[4 * i + 3] = x.w;
+  for (int c = 0; c < 4; ++c) w[unit_f32(lane, c)] = make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+}
+__device__ __forceinline__ void get_row(const float4* w, int lane, float (&v)[16]) {
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float4 x = w[unit_f32(lane, c)];
+    v[4 * c] = x.x;
+    v[4 * c + 1] = x.y;
+    v[4 * c + 2] = x.z;
+    v[4 * c + 3] = x.w;
   }
 }
-__device__ __forceinline__ void st16f(float* p, const float* v) {
-  float4* q = reinterpret_cast<float4*>(p);
+// coalesced: the lane's (row (lane >> 2) + 8 k, chunk lane & 3), k = 0..3, of
+// the warp's rows starting at base (row stride ld floats); rows >= rows_ok
+// are neither read (zeros) nor written
+__device__ __forceinline__ void load_tile(float4 (&x)[4], int lane, const float* base, size_t ld, int rows_ok) {
 #pragma unroll
-  for (int i = 0; i < 4; ++i) q[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+  for (int k = 0; k < 4; ++k) {
+    const int r = (lane >> 2) + 8 * k;
+    x[k] = r < rows_ok ? *reinterpret_cast<const float4*>(base + (size_t)r * ld + 4 * (lane & 3))
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
 }
-__device__ __forceinline__ void st16b(__nv_bfloat16* p, const float* v) {
+__device__ __forceinline__ void put_tile(float4* w, int lane, const float4 (&x)[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) w[unit_f32((lane >> 2) + 8 * k, lane & 3)] = x[k];
+}
+__device__ __forceinline__ void store_tile(const float4* w, int lane, float* base, size_t ld, int rows_ok) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int r = (lane >> 2) + 8 * k;
+    if (r < rows_ok) *reinterpret_cast<float4*>(base + (size_t)r * ld + 4 * (lane & 3)) = w[unit_f32(r, lane & 3)];
+  }
+}
+// BF16: the row's 16 values rounded (lo: the rounding of the remainder when
+// hi_part is false) into the tile, then stored coalesced
+__device__ __forceinline__ void put_row_b16(float4* w, int lane, const float (&v)[16], bool hi_part) {
   __nv_bfloat162 h[8];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-  uint4* q = reinterpret_cast<uint4*>(p);
-  q[0] = *reinterpret_cast<uint4*>(&h[0]);
-  q[1] = *reinterpret_cast<uint4*>(&h[4]);
-}
-// 16 values as BF16 high parts at p and, when lo is set, low parts at lo
-__device__ __forceinline__ void st16b_split(__nv_bfloat16* p, __nv_bfloat16* lo, const float* v) {
-  if (!lo) {
-    st16b(p, v);
-    return;
+  for (int i = 0; i < 8; ++i) {
+    __nv_bfloat16 a, b, al, bl;
+    split_bf16(v[2 * i], a, al);
+    split_bf16(v[2 * i + 1], b, bl);
+    h[i] = hi_part ? __halves2bfloat162(a, b) : __halves2bfloat162(al, bl);
   }
-  __nv_bfloat16 h[16], l[16];
+  uint4* u = reinterpret_cast<uint4*>(w);
+  u[unit_b16(lane, 0)] = *reinterpret_cast<const uint4*>(&h[0]);
+  u[unit_b16(lane, 1)] = *reinterpret_cast<const uint4*>(&h[4]);
+}
+__device__ __forceinline__ void store_tile_b16(const float4* w, int lane, __nv_bfloat16* base, size_t ld,
+                                               int rows_ok) {
+  const uint4* u = reinterpret_cast<const uint4*>(w);
 #pragma unroll
-  for (int i = 0; i < 16; ++i) split_bf16(v[i], h[i], l[i]);
-  uint4* q = reinterpret_cast<uint4*>(p);
-  q[0] = *reinterpret_cast<uint4*>(&h[0]);
-  q[1] = *reinterpret_cast<uint4*>(&h[8]);
-  uint4* ql = reinterpret_cast<uint4*>(lo);
-  ql[0] = *reinterpret_cast<uint4*>(&l[0]);
-  ql[1] = *reinterpret_cast<uint4*>(&l[8]);
+  for (int k = 0; k < 2; ++k) {
+    const int r = (lane >> 1) + 16 * k;
+    if (r < rows_ok) *reinterpret_cast<uint4*>(base + (size_t)r * ld + 8 * (lane & 1)) = u[unit_b16(r, lane & 1)];
+  }
 }
 
+// FP32 values of this thread's row through the tile to global memory
+__device__ __forceinline__ void emit_f32(float4* w, int lane, const float (&v)[16], float* base, size_t ld,
+                                         int rows_ok) {
+  put_row(w, lane, v);
+  __syncwarp();
+  store_tile(w, lane, base, ld, rows_ok);
+  __syncwarp();
+}
+// split BF16 (hi at base, lo at base_lo when set)
+__device__ __forceinline__ void emit_b16(float4* w, int lane, const float (&v)[16], __nv_bfloat16* base,
+                                         __nv_bfloat16* base_lo, size_t ld, int rows_ok) {
+  put_row_b16(w, lane, v, true);
+  __syncwarp();
+  store_tile_b16(w, lane, base, ld, rows_ok);
+  __syncwarp();
+  if (base_lo) {
+    put_row_b16(w, lane, v, false);
+    __syncwarp();
+    store_tile_b16(w, lane, base_lo, ld, rows_ok);
+    __syncwarp();
+  }
+}
+
+// Per-type column vectors of the epilogue, staged in shared memory at the
+// start of the kernel: [type][3][N] floats —
+//   forward: bias, idt (1 when absent), w_out (output layer);
+//   backward: idt of the lower layer (1 when absent), the broadcast upstream
+//   gradient (dYup with lddyup == 0; 0 when absent), unused.
+__device__ __forceinline__ float fit_vec(const FitGemm& g, int t, int a, int n) {
+  const size_t o = (size_t)t * g.N + n;
+  if (g.mode == kFitBwd) {
+    if (a == 0) return g.idt_lo ? g.idt_lo[o] : 1.f;
+    if (a == 1) return (g.dYup && g.lddyup == 0) ? g.dYup[o] : 0.f;
+    return 0.f;
+  }
+  if (a == 0) return g.bias ? g.bias[o] : 0.f;
+  if (a == 1) return g.idt ? g.idt[o] : 1.f;
+  return g.w_out ? g.w_out[o] : 0.f;
+}
+// work item -> type, first row, first column (nnt column tiles per row tile)
+__device__ __forceinline__ void fit_decode(const FitGemm& g, int BN, int nnt, int it, int& t, int& m0, int& n0) {
+  const int tile = it / nnt;
+  n0 = (it - tile * nnt) * BN;
+  t = 0;
+  while (t + 1 < g.ntypes && g.tile0[t + 1] <= tile) ++t;
+  m0 = g.row0[t] + (tile - g.tile0[t]) * 128;
+}
+
+// The epilogue warps' part of fit_gemm_kernel for one mode: this warp (of
+// group h, TMEM quadrant q) walks the items j = h (mod EG) of the CTA, 16
+// accumulator columns at a time.
+template <int MODE, int BN, int EG, int NB, uint32_t kCols>
+__device__ __forceinline__ void fit_epilogue(const FitGemm& g, const float* svec, float4* wst, uint32_t tbase,
+                                             uint64_t* acc_full, uint64_t* acc_free, int* err) {
+  constexpr bool fwd = MODE == kFitFwd || MODE == kFitFwdLast, bwd = MODE == kFitBwd;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, h = warp >> 2, q = warp & 3;
+  const int nnt = (g.N + BN - 1) / BN, items = g.tile0[g.ntypes] * nnt;
+  const bool in_a = (fwd && g.skip) || (bwd && g.dYup && g.lddyup);  // row operands
+  const float* xa = fwd ? g.Xs : g.dYup;
+  const size_t lda_in = fwd ? (size_t)g.ldxs : (size_t)g.lddyup;
+  int j = h;
+  for (int it = blockIdx.x + h * gridDim.x; it < items; it += EG * gridDim.x, j += EG) {
+    const int b = j % NB;
+    int t, m0, n0;
+    fit_decode(g, BN, nnt, it, t, m0, n0);
+    const int mw = m0 + q * 32;                      // the warp's first row
+    const int rows_ok = min(32, g.row0[t + 1] - mw);  // its rows of type t
+    const int nt = min(BN, g.N - n0);
+    const float* vec = svec + (size_t)t * 3 * g.N;
+    float4 pa[4], pb[4];  // the next 16 columns' row operands (coalesced)
+    if (in_a) load_tile(pa, lane, xa + (size_t)mw * lda_in + n0, lda_in, rows_ok);
+    if (bwd) load_tile(pb, lane, g.T_lo + (size_t)mw * g.ldy + n0, g.ldy, rows_ok);
+    bool ok = tc::mbar_wait(&acc_full[b], (j / NB) & 1, err);
+    ok = __all_sync(0xffffffffu, ok) != 0;  // the TMEM loads below are warp-wide
+    if (!ok) break;
+    tc::fence_after();
+    float e_hi = 0.f, e_lo = 0.f;  // output layer: compensated sum of y w over the row
+    for (int c0 = 0; c0 < nt; c0 += 16) {
+      const int n = n0 + c0;
+      float xa_r[16], xb_r[16];
+      if (in_a) {
+        put_tile(wst, lane, pa);
+        __syncwarp();
+        get_row(wst, lane, xa_r);
+        __syncwarp();
+      }
+      if (bwd) {
+        put_tile(wst, lane, pb);
+        __syncwarp();
+        get_row(wst, lane, xb_r);
+        __syncwarp();
+      }
+      if (c0 + 16 < nt) {
+        if (in_a) load_tile(pa, lane, xa + (size_t)mw * lda_in + n + 16, lda_in, rows_ok);
+        if (bwd) load_tile(pb, lane, g.T_lo + (size_t)mw * g.ldy + n + 16, g.ldy, rows_ok);
+      }
+      float v[16];
+      tc::tmem_ld16(tc::taddr(tbase + (uint32_t)(b * kCols), q * 32, c0), v);
+      tc::tmem_ld_wait();
+      if (fwd) {
+        float tv[16];
+        const float4* bb = reinterpret_cast<const float4*>(vec + n);
+        const float4* id = reinterpret_cast<const float4*>(vec + g.N + n);
+#pragma unroll
+        for (int i4 = 0; i4 < 4; ++i4) {
+          const float4 b4 = bb[i4], d4 = id[i4];
+          const float bv[4] = {b4.x, b4.y, b4.z, b4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int i = 4 * i4 + u;
+            tv[i] = tanh_acc(v[i] + bv[u]);
+            v[i] = tv[i] * dv[u];  // y
+            if (in_a) v[i] += xa_r[i];
+          }
+        }
+        if (MODE == kFitFwd) {
+          emit_f32(wst, lane, v, g.Yf + (size_t)mw * g.ldy + n, g.ldy, rows_ok);
+          emit_f32(wst, lane, tv, g.Tt + (size_t)mw * g.ldy + n, g.ldy, rows_ok);
+          emit_b16(wst, lane, v, g.Yb + (size_t)mw * g.ldy + n, g.Yb_lo ? g.Yb_lo + (size_t)mw * g.ldy + n : nullptr,
+                   g.ldy, rows_ok);
+        } else {
+          const float4* wo = reinterpret_cast<const float4*>(vec + 2 * g.N + n);
+#pragma unroll
+          for (int i4 = 0; i4 < 4; ++i4) {
+            const float4 w4 = wo[i4], d4 = id[i4];
+            const float wv[4] = {w4.x, w4.y, w4.z, w4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int i = 4 * i4 + u;
+              const float pr = v[i] * wv[u];
+              comp_add(e_hi, e_lo, pr);
+              e_lo += fmaf(v[i], wv[u], -pr);                  // the product's rounding error
+              tv[i] = wv[u] * dv[u] * (1.f - tv[i] * tv[i]);  // dP
+            }
+          }
+          emit_b16(wst, lane, tv, g.dPb + (size_t)mw * g.ldy + n,
+                   g.dPb_lo ? g.dPb_lo + (size_t)mw * g.ldy + n : nullptr, g.ldy, rows_ok);
+        }
+      } else if (bwd) {
+        const float* il = vec + n;
+        const float* up = vec + g.N + n;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] += in_a ? xa_r[i] : up[i];  // dx (up is 0 without dYup)
+        if (g.dXf) emit_f32(wst, lane, v, g.dXf + (size_t)mw * g.ldy + n, g.ldy, rows_ok);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = v[i] * il[i] * (1.f - xb_r[i] * xb_r[i]);  // dP
+        emit_b16(wst, lane, v, g.dPb + (size_t)mw * g.ldy + n, g.dPb_lo ? g.dPb_lo + (size_t)mw * g.ldy + n : nullptr,
+                 g.ldy, rows_ok);
+      } else {
+        emit_f32(wst, lane, v, g.out + (size_t)mw * g.ldo + n, g.ldo, rows_ok);
+      }
+    }
+    // this warp has read the buffer: the MMAs of item j + NB may overwrite it
+    tc::fence_before();
+    __syncwarp();
+    if (lane == 0) tc::mbar_arrive(&acc_free[b]);
+    if (MODE == kFitFwdLast && lane < rows_ok) g.e_out[mw + lane] = ((double)e_hi + (double)e_lo) + (double)g.b_out[t];
+  }
+}
+
+// Persistent, warp-specialised GEMM: the CTA (one per SM) walks the work
+// items it, it + gridDim.x, ... (an item: one 128-row tile by one BN-column
+// tile).  Warp 4 EG streams the items' K chunks through an S-stage TMA
+// ring, warp 4 EG + 1 issues their MMAs into one of NB TMEM accumulators
+// (item j of the CTA into buffer j mod NB), and each of the EG epilogue warp
+// groups (warps 4h .. 4h + 3, thread = row) runs the epilogue of the items
+// j = h (mod EG): the MMAs of the next items overlap the epilogue of item j,
+// and the groups' epilogues overlap each other.  The epilogue reads its row
+// operands (skip input, upstream gradient, tanh values) and writes its
+// outputs through its warp's staging tile, 16 columns at a time, with the
+// next 16 columns' operands in flight.
 // NA: parts of A (1: hi, 2: hi and lo); the weight always comes as hi and
 // lo.  A stage holds one K chunk of every part, so each part is read once.
-template <int BN, int S, int WG, int NA>
-__global__ void __launch_bounds__(128 * WG)
+template <int BN, int S, int NA, int EG, int NB>
+__global__ void __launch_bounds__(128 * EG + 64, 1)
 fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_alo,
                 const __grid_constant__ CUtensorMap tma_b, FitGemm g, int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   // swizzled TMA tiles want 1024-byte aligned stages
   unsigned char* smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
-  __shared__ uint64_t full[S], empty[S], done;
+  __shared__ uint64_t full[S], empty[S], acc_full[NB], acc_free[NB], mma_done;
   __shared__ uint32_t s_tmem;
-  __shared__ float s_e[2 * (WG - 1) * 128 + 2];  // compensated partial energies of column groups 1 .. WG-1
   constexpr int SA = 128 * kKC * 2, SB = BN * kKC * 2, STAGE = NA * SA + 2 * SB;
-  constexpr uint32_t kTmemCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+  constexpr uint32_t kCols = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));  // a buffer's columns
   static_assert(BN % 16 == 0 && BN <= 256 && SB % 1024 == 0, "whole 16-column loads, 1024-byte aligned stages");
+  // the allocation: a power of two of at least NB buffers
+  constexpr uint32_t kAlloc = NB * kCols <= 128 ? 128 : (NB * kCols <= 256 ? 256 : 512);
+  static_assert(NB * kCols <= 512, "TMEM: 512 columns per SM");
+  float4* stage_tiles = reinterpret_cast<float4*>(smem + S * STAGE);
+  float* svec = reinterpret_cast<float*>(smem + S * STAGE + EG * 4 * kStageFloats * 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  int t = 0;
-  while (t + 1 < g.ntypes && g.tile0[t + 1] <= (int)blockIdx.y) ++t;
-  const int m0 = g.row0[t] + ((int)blockIdx.y - g.tile0[t]) * 128;
-  const int rows_valid = min(128, g.row0[t + 1] - m0);
-  const int n0 = blockIdx.x * BN;
-  const int nt = min(BN, g.N - n0);  // multiple of 16
-  if (warp == 0) tc::tmem_alloc(&s_tmem, kTmemCols);
+  const int nnt = (g.N + BN - 1) / BN, items = g.tile0[g.ntypes] * nnt;
+  const int nchunk = (g.K + kKC - 1) / kKC;
+  if (warp == 0) tc::tmem_alloc(&s_tmem, kAlloc);
   if (tid == 0) {
     for (int s = 0; s < S; ++s) {
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    tc::mbar_init(&done, 1);
+    for (int b = 0; b < NB; ++b) {
+      tc::mbar_init(&acc_full[b], 1);
+      tc::mbar_init(&acc_free[b], 4);  // one arrival per warp of the reading warp group
+    }
+    tc::mbar_init(&mma_done, 1);
     tc::fence_mbar_init();
+  }
+  for (int q = tid; q < g.ntypes * 3 * g.N; q += blockDim.x) {
+    const int t = q / (3 * g.N), rem = q - t * 3 * g.N, a = rem / g.N;
+    svec[q] = fit_vec(g, t, a, rem - a * g.N);
   }
   __syncthreads();
   tc::fence_after();
   const uint32_t tbase = s_tmem;
-  // stage layout: A hi [, A lo], B hi, B lo
-  const int nchunk = (g.K + kKC - 1) / kKC;
   bool ok = true;
-  if (warp == 1 && lane == 0) {
-    // producer: chunk i into stage i % S once the MMAs of chunk i - S released it
-    for (int i = 0; i < nchunk && ok; ++i) {
-      const int s = i % S;
-      if (i >= S) ok = tc::mbar_wait(&empty[s], ((i / S) - 1) & 1, err);
-      if (!ok) break;
-      const uint32_t a0 = tc::smem_u32(smem + s * STAGE), b0 = a0 + NA * SA;
-      tc::mbar_expect_tx(&full[s], STAGE);
-      tc::tma_load_2d(a0, &tma_a, i * kKC, m0, &full[s]);
-      if (NA == 2) tc::tma_load_2d(a0 + SA, &tma_alo, i * kKC, m0, &full[s]);
-      tc::tma_load_2d(b0, &tma_b, i * kKC, t * g.N + n0, &full[s]);
-      tc::tma_load_2d(b0 + SB, &tma_b, g.Kp + i * kKC, t * g.N + n0, &full[s]);
-    }
-  } else if (warp == 0 && lane == 0) {
-    // MMA issuer: 4 steps of K = 16 per chunk (zeros past K add nothing),
-    // each hi.hi (+ lo.hi) + hi.lo
-    const uint32_t idesc = tc::idesc_bf16_f32(128, nt);
-    for (int i = 0; i < nchunk && ok; ++i) {
-      const int s = i % S;
-      ok = tc::mbar_wait(&full[s], (i / S) & 1, err);
-      if (!ok) break;
-      tc::fence_after();
-      const uint32_t a0 = tc::smem_u32(smem + s * STAGE), b0 = a0 + NA * SA;
-#pragma unroll
-      for (int ks = 0; ks < kKC / 16; ++ks) {
-        tc::mma_bf16(tbase, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc,
-                     (i > 0 || ks > 0) ? 1u : 0u);
-        if (NA == 2)
-          tc::mma_bf16(tbase, tc::smem_desc_sw128(a0 + SA + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc, 1u);
-        tc::mma_bf16(tbase, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + SB + ks * 32), idesc, 1u);
-      }
-      tc::mma_commit(&empty[s]);
-    }
-    tc::mma_commit(&done);
-  }
-  __syncwarp();
-  ok = tc::mbar_wait(&done, 0, err) && ok;
-  tc::fence_after();
-  ok = __syncthreads_and(ok) != 0;
-  // epilogue: thread = row (warp quadrant q = TMEM lanes 32 q ..), the
-  // WG warp groups take the tile's 16-column groups in turn
-  const int q = warp & 3, h = warp >> 2;
-  const int r = q * 32 + lane;
-  const int m = m0 + r;
-  const bool valid = r < rows_valid;
-  float e_hi = 0.f, e_lo = 0.f;  // output layer: compensated sum of y w over this group's columns
-  if (ok) {
-    const float* bias = g.bias ? g.bias + (size_t)t * g.N : nullptr;
-    const float* idt = g.idt ? g.idt + (size_t)t * g.N : nullptr;
-    const float* idt_lo = g.idt_lo ? g.idt_lo + (size_t)t * g.N : nullptr;
-    const float* wo = g.w_out ? g.w_out + (size_t)t * g.N : nullptr;
-    for (int c0 = h * 16; c0 < nt; c0 += 16 * WG) {
-      float v[16];
-      tc::tmem_ld16(tc::taddr(tbase, q * 32, c0), v);
-      tc::tmem_ld_wait();
-      if (!valid) continue;
-      const int n = n0 + c0;
-      if (g.mode == kFitFwd || g.mode == kFitFwdLast) {
-        float bb[16], id[16], xs[16], y[16], tv[16];
-        ld16f(bias + n, bb);
-        if (idt) ld16f(idt + n, id);
-        if (g.skip) ld16f(g.Xs + (size_t)m * g.ldxs + n, xs);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          tv[i] = tanh_acc(v[i] + bb[i]);
-          y[i] = idt ? tv[i] * id[i] : tv[i];
-          if (g.skip) y[i] += xs[i];
+  if (warp == 4 * EG) {
+    if (lane == 0) {
+      // producer: the c-th chunk of the CTA into stage c % S once the MMAs
+      // of chunk c - S released it (stage layout: A hi [, A lo], B hi, B lo)
+      int c = 0;
+      for (int it = blockIdx.x; it < items && ok; it += gridDim.x) {
+        int t, m0, n0;
+        fit_decode(g, BN, nnt, it, t, m0, n0);
+        for (int i = 0; i < nchunk; ++i, ++c) {
+          const int s = c % S;
+          if (c >= S) ok = tc::mbar_wait(&empty[s], ((c / S) - 1) & 1, err);
+          if (!ok) break;
+          const uint32_t a0 = tc::smem_u32(smem + s * STAGE), b0 = a0 + NA * SA;
+          tc::mbar_expect_tx(&full[s], STAGE);
+          tc::tma_load_2d(a0, &tma_a, i * kKC, m0, &full[s]);
+          if (NA == 2) tc::tma_load_2d(a0 + SA, &tma_alo, i * kKC, m0, &full[s]);
+          tc::tma_load_2d(b0, &tma_b, i * kKC, t * g.N + n0, &full[s]);
+          tc::tma_load_2d(b0 + SB, &tma_b, g.Kp + i * kKC, t * g.N + n0, &full[s]);
         }
-        if (g.mode == kFitFwd) {
-          st16f(g.Yf + (size_t)m * g.ldy + n, y);
-          st16f(g.Tt + (size_t)m * g.ldy + n, tv);
-          st16b_split(g.Yb + (size_t)m * g.ldy + n, g.Yb_lo ? g.Yb_lo + (size_t)m * g.ldy + n : nullptr, y);
-        } else {
-          float w[16], dp[16];
-          ld16f(wo + n, w);
+      }
+      if (!ok)  // a wait ran out: the copies already issued land before the CTA ends (bounded)
+        for (int i = max(0, c - S); i < c; ++i) tc::mbar_wait(&full[i % S], (i / S) & 1, nullptr);
+    }
+    __syncwarp();
+  } else if (warp == 4 * EG + 1) {
+    if (lane == 0) {
+      // MMA issuer: 4 steps of K = 16 per chunk (zeros past K add nothing),
+      // each hi.hi (+ lo.hi) + hi.lo
+      int c = 0, j = 0;
+      for (int it = blockIdx.x; it < items && ok; it += gridDim.x, ++j) {
+        int t, m0, n0;
+        fit_decode(g, BN, nnt, it, t, m0, n0);
+        const int b = j % NB;
+        // the epilogue has read item j - NB out of this buffer
+        if (j >= NB) ok = tc::mbar_wait(&acc_free[b], ((j / NB) - 1) & 1, err);
+        if (!ok) break;
+        tc::fence_after();
+        const uint32_t idesc = tc::idesc_bf16_f32(128, min(BN, g.N - n0));
+        const uint32_t dst = tbase + (uint32_t)(b * kCols);
+        for (int i = 0; i < nchunk && ok; ++i, ++c) {
+          const int s = c % S;
+          ok = tc::mbar_wait(&full[s], (c / S) & 1, err);
+          if (!ok) break;
+          tc::fence_after();
+          const uint32_t a0 = tc::smem_u32(smem + s * STAGE), b0 = a0 + NA * SA;
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const float pr = y[i] * w[i];
-            comp_add(e_hi, e_lo, pr);
-            e_lo += fmaf(y[i], w[i], -pr);  // the product's rounding error
-            dp[i] = w[i] * (idt ? id[i] : 1.f) * (1.f - tv[i] * tv[i]);
+          for (int ks = 0; ks < kKC / 16; ++ks) {
+            tc::mma_bf16(dst, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc,
+                         (i > 0 || ks > 0) ? 1u : 0u);
+            if (NA == 2)
+              tc::mma_bf16(dst, tc::smem_desc_sw128(a0 + SA + ks * 32), tc::smem_desc_sw128(b0 + ks * 32), idesc,
+                           1u);
+            tc::mma_bf16(dst, tc::smem_desc_sw128(a0 + ks * 32), tc::smem_desc_sw128(b0 + SB + ks * 32), idesc, 1u);
           }
-          st16b_split(g.dPb + (size_t)m * g.ldy + n, g.dPb_lo ? g.dPb_lo + (size_t)m * g.ldy + n : nullptr, dp);
+          tc::mma_commit(&empty[s]);
         }
-      } else if (g.mode == kFitBwd) {
-        float dx[16], up[16], tl[16], il[16], dp[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) dx[i] = v[i];
-        if (g.dYup) {
-          ld16f(g.lddyup ? g.dYup + (size_t)m * g.lddyup + n : g.dYup + (size_t)t * g.N + n, up);
-#pragma unroll
-          for (int i = 0; i < 16; ++i) dx[i] += up[i];
-        }
-        if (g.dXf) st16f(g.dXf + (size_t)m * g.ldy + n, dx);
-        ld16f(g.T_lo + (size_t)m * g.ldy + n, tl);
-        if (idt_lo) ld16f(idt_lo + n, il);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) dp[i] = dx[i] * (idt_lo ? il[i] : 1.f) * (1.f - tl[i] * tl[i]);
-        st16b_split(g.dPb + (size_t)m * g.ldy + n, g.dPb_lo ? g.dPb_lo + (size_t)m * g.ldy + n : nullptr, dp);
-      } else {
-        st16f(g.out + (size_t)m * g.ldo + n, v);
+        if (ok) tc::mma_commit(&acc_full[b]);
       }
+      // every MMA issued has completed before the accumulators are freed
+      tc::mma_commit(&mma_done);
+      tc::mbar_wait(&mma_done, 0, nullptr);
     }
-  }
-  if (g.mode == kFitFwdLast) {
-    if (h > 0) {
-      s_e[2 * ((h - 1) * 128 + r)] = e_hi;
-      s_e[2 * ((h - 1) * 128 + r) + 1] = e_lo;
-    }
-    __syncthreads();
-    if (ok && h == 0 && valid) {
-      for (int k = 1; k < WG; ++k) {
-        comp_add(e_hi, e_lo, s_e[2 * ((k - 1) * 128 + r)]);
-        e_lo += s_e[2 * ((k - 1) * 128 + r) + 1];
-      }
-      g.e_out[m] = ((double)e_hi + (double)e_lo) + (double)g.b_out[t];
+    __syncwarp();
+  } else {
+    // epilogue: warp group h takes the CTA's items j = h, h + EG, ...
+    // (buffer j mod NB); thread = row (warp quadrant q = TMEM lanes 32 q ..)
+    float4* wst = stage_tiles + warp * (kStageFloats / 4);
+    switch (g.mode) {
+      case kFitFwd: fit_epilogue<kFitFwd, BN, EG, NB, kCols>(g, svec, wst, tbase, acc_full, acc_free, err); break;
+      case kFitFwdLast:
+        fit_epilogue<kFitFwdLast, BN, EG, NB, kCols>(g, svec, wst, tbase, acc_full, acc_free, err);
+        break;
+      case kFitBwd: fit_epilogue<kFitBwd, BN, EG, NB, kCols>(g, svec, wst, tbase, acc_full, acc_free, err); break;
+      default: fit_epilogue<kFitStore, BN, EG, NB, kCols>(g, svec, wst, tbase, acc_full, acc_free, err); break;
     }
   }
   tc::fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, kTmemCols);
+  if (warp == 0) tc::tmem_dealloc(tbase, kAlloc);
 }
 
 // dE/dD of the first layer folded into dE/dxyz (FitDxyz).  One CTA per
@@ -483,26 +655,65 @@ int encode_bf16_2d(CUtensorMap* m, const __nv_bfloat16* base, int rows, int cols
   return DPGB_OK;
 }
 
-template <int BN, int S, int WG, int NA>
+// epilogue shared memory next to the stages: the warps' staging tiles and
+// the per-type column vectors
+constexpr size_t epi_bytes(int EG, int ntypes, int N) {
+  return (size_t)EG * 4 * kStageFloats * 4 + (size_t)ntypes * 3 * N * 4;
+}
+
+// stages of a BN-column tile: as many as fit next to each other and the
+// epilogue's shared memory (for up to two types of 256 columns) in about
+// 220 KB (2 .. 6)
+template <int BN, int NA, int EG>
+constexpr int fit_stages() {
+  constexpr int stage = (NA * 128 + 2 * BN) * kKC * 2;
+  constexpr int s = (int)((220 * 1024 - epi_bytes(EG, 2, 256)) / stage);
+  return s < 2 ? 2 : (s > 6 ? 6 : s);
+}
+
+template <int BN, int NA, int EG, int NB>
 int launch_t(const FitGemm& g, int* err, cudaStream_t st) {
-  const size_t smem = (size_t)S * (NA * 128 + 2 * BN) * kKC * 2 + 1024;  // + alignment slack
-  static bool attr = false;
-  if (!attr) {
-    DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel<BN, S, WG, NA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  constexpr int S = fit_stages<BN, NA, EG>();
+  // + alignment slack; at least half of an SM's shared memory, so that one
+  // CTA (and its TMEM accumulators) sits on an SM
+  const size_t smem = std::max((size_t)S * (NA * 128 + 2 * BN) * kKC * 2 + 1024 + epi_bytes(EG, g.ntypes, g.N),
+                               (size_t)116 * 1024);
+  if (smem > 226 * 1024) return fail(DPGB_EINVAL, "fit_gemm: too many atom types for the staged epilogue");
+  static size_t attr = 0;  // the largest dynamic shared memory requested so far
+  if (attr < smem) {
+    DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel<BN, S, NA, EG, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
-    attr = true;
+    attr = smem;
   }
   if (g.Kp < g.K || g.Kp % kKC || (NA == 2) != (g.A_lo != nullptr))
     return fail(DPGB_EINVAL, "fit_gemm: bad split-BF16 operands");
+  if (g.mode == kFitFwdLast && g.N > BN) return fail(DPGB_EINVAL, "fit_gemm: the output layer needs whole rows");
   CUtensorMap ta, talo, tb;
   DPGB_TRY(encode_bf16_2d(&ta, g.A, g.row0[g.ntypes], g.K, g.lda, 128));
   DPGB_TRY(encode_bf16_2d(&talo, g.A_lo ? g.A_lo : g.A, g.row0[g.ntypes], g.K, g.lda, 128));
   DPGB_TRY(encode_bf16_2d(&tb, g.B, g.ntypes * g.N, 2 * g.Kp, 2 * g.Kp, BN));
-  // the column tiles of one row tile run next to each other (they read the
-  // same A rows: L2 serves the repeats)
-  dim3 grid(ceil_div(g.N, BN), g.tile0[g.ntypes]);
-  fit_gemm_kernel<BN, S, WG, NA><<<grid, 128 * WG, smem, st>>>(ta, talo, tb, g, err);
+  const int items = g.tile0[g.ntypes] * ceil_div(g.N, BN);
+  fit_gemm_kernel<BN, S, NA, EG, NB><<<std::min(items, sm_count()), 128 * EG + 64, smem, st>>>(ta, talo, tb, g, err);
   return check_launch("fit_gemm");
+}
+
+template <int NA>
+int launch_na(const FitGemm& g, int* err, cudaStream_t st) {
+  // Whole rows (the narrowest column tile that holds one; wider rows in
+  // tiles of 256, two accumulators) when they give every SM two items or
+  // more, so that an item's MMAs overlap another's epilogue; else narrower
+  // tiles (four accumulators) spread the rows' work over more SMs.  The
+  // output layer needs whole rows.
+  const int rows_tiles = g.tile0[g.ntypes];
+  const bool whole = g.mode == kFitFwdLast || (long long)rows_tiles * ceil_div(g.N, 256) >= 2LL * sm_count();
+  if (!whole) {
+    if (g.N % 80 == 0) return launch_t<80, NA, 2, 4>(g, err, st);
+    return launch_t<64, NA, 2, 4>(g, err, st);
+  }
+  if (g.N <= 64) return launch_t<64, NA, 2, 4>(g, err, st);
+  if (g.N <= 128) return launch_t<128, NA, 2, 4>(g, err, st);
+  if (g.N <= 240) return launch_t<240, NA, 2, 2>(g, err, st);
+  return launch_t<256, NA, 2, 2>(g, err, st);
 }
 
 }  // namespace
@@ -513,6 +724,7 @@ int fit_tc_eligible(const dpgb_se_a_desc& d) {
   for (int l = 0; l < d.n_fit; ++l) {
     const int w = d.fit_neuron[l];
     if (w % 16 || w > 256) return 0;
+    if (w > 240 && d.ntypes > 4) return 0;  // the epilogue's shared memory
     if (w == 2 * nin) return 0;  // the doubling skip is not fused here
     nin = w;
   }
@@ -535,20 +747,9 @@ int launch_fit_dxyz(const FitDxyz& f, int* err, cudaStream_t st) {
 }
 
 int launch_fit_gemm(const FitGemm& g, int* err, cudaStream_t st) {
-  const int mt = g.tile0[g.ntypes];
-  if (mt <= 0) return DPGB_OK;
-  // stages: three when two CTAs still fit on an SM, else two
-  const bool split_a = g.A_lo != nullptr;
-  if (g.mode == kFitFwdLast)  // the output layer needs whole rows (one CTA per SM)
-    return split_a ? launch_t<256, 2, 2, 2>(g, err, st) : launch_t<256, 2, 2, 1>(g, err, st);
-  // column tile: the narrower one when it spreads the tiles more evenly over
-  // the SMs (two CTAs fit on an SM either way): for 240 columns, three
-  // 80-wide tiles per row tile rather than a 128 + 112 pair
-  const int sms = sm_count();
-  auto span = [&](int bn) { return (long long)ceil_div(mt * ceil_div(g.N, bn), 2 * sms) * bn; };
-  if (g.N % 80 == 0 && span(80) < span(128))
-    return split_a ? launch_t<80, 2, 2, 2>(g, err, st) : launch_t<80, 3, 2, 1>(g, err, st);
-  return split_a ? launch_t<128, 2, 2, 2>(g, err, st) : launch_t<128, 2, 2, 1>(g, err, st);
+  if (g.tile0[g.ntypes] <= 0) return DPGB_OK;
+  if (g.N % 16) return fail(DPGB_EINVAL, "fit_gemm: width not a multiple of 16");
+  return g.A_lo ? launch_na<2>(g, err, st) : launch_na<1>(g, err, st);
 }
 
 }  // namespace dpgb
