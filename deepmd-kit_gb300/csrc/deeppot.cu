@@ -194,6 +194,49 @@ force_gather_model_kernel(double* __restrict__ force, double* __restrict__ atom_
   gather_store<T, AV>(force, atom_vir, (size_t)row, f, av, lane);
 }
 
+// Mixed form without atomic virials: the forces of a local model list with
+// no transpose.  The pair gradients g of a row add onto the row in a fixed
+// order (as in force_gather_model_kernel); each one's share on its
+// neighbour, -g, is scaled by 2^32, rounded to an integer and added with a
+// 64-bit integer atomic (red) into acc[key] — integer sums are exact, so the
+// result does not depend on the order of the adds and repeats bitwise (the
+// rounding: 2^-33 per term, far below FP32 resolution at the force scale).
+// force_fix_kernel then adds acc * 2^-32 onto the rows' own sums.
+constexpr float kFixScale = 4294967296.f;  // 2^32
+
+__global__ void __launch_bounds__(kGatherWarps * 32)
+force_scatter_model_kernel(double* __restrict__ force, unsigned long long* __restrict__ acc,
+                           const float* __restrict__ g, const int* __restrict__ nlist, int nloc, FastDiv by_nloc,
+                           int nnei, int nrows) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * kGatherWarps + (threadIdx.x >> 5);
+  if (row >= nrows) return;
+  const int fbase = by_nloc.div(row) * nloc;  // the frame's first row
+  const float* gr = g + (size_t)row * nnei * 3;
+  const int* nr = nlist + (size_t)row * nnei;
+  GatherAcc<float> f;
+  for (int s = lane; s < nnei; s += 32) {
+    const int nb = nr[s];
+    if (nb < 0) continue;  // padding slots carry no force (and may be unwritten)
+    unsigned long long* a = acc + 3 * (size_t)(fbase + nb - by_nloc.div(nb) * nloc);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float x = gr[3 * s + c];
+      f.add(c, x);
+      atomicAdd(a + c, (unsigned long long)__float2ll_rn(-x * kFixScale));
+    }
+  }
+  f.reduce();
+  if (lane == 0)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) force[3 * (size_t)row + c] = f.get(c);
+}
+
+__global__ void force_fix_kernel(double* __restrict__ force, const unsigned long long* __restrict__ acc, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) force[i] += (double)(long long)acc[i] * (1.0 / 4294967296.0);
+}
+
 // The same with explicit extended atoms (external list, one frame): every one
 // of the nall atoms gets its force and atomic virial (the caller sums ghost
 // entries back onto their owners, as LAMMPS's reverse communication does).
@@ -406,6 +449,7 @@ struct DeepPotImpl {
   DeviceBuffer fit_w16, fit_f32, ws_fitb;
   // workspace
   DeviceBuffer ws_nlist, ws_cell, ws_tr, ws_keys, ws_status, ws_coord, ws_svec, ws_spos;
+  DeviceBuffer ws_facc;  // fixed-point force sums of the scatter path
   DeviceBuffer ws_D, ws_dD, ws_xyz, ws_g, ws_vir, ws_erow, ws_esorted, ws_act, ws_gbuf, ws_part, ws_xhi, ws_xlo, ws_shi, ws_slo;
   DeviceBuffer ws_env;  // the table path's per-pair environment, forward -> backward
   DeviceBuffer io_coord, io_force, io_av, io_e, io_v, io_ae;
@@ -1107,8 +1151,15 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   if (batch) cell_bytes = nlist_batch_workspace(natom, batch->ncells);
   DPGB_TRY(dp.ws_cell.alloc(cell_bytes));
   DPGB_TRY(dp.ws_nlist.alloc(sizeof(int) * npair));
-  DPGB_TRY(dp.ws_keys.alloc(sizeof(int) * npair));
-  DPGB_TRY(dp.ws_tr.alloc(transpose_workspace(npair, (int)nkeys)));
+  // the mixed form's model-list forces without atomic virials go through
+  // the fixed-point scatter; every other gather reads the sorted transpose
+  const bool scatter = std::is_same<T, float>::value && own_geom && !atom_virial;
+  if (scatter) {
+    DPGB_TRY(dp.ws_facc.alloc(sizeof(unsigned long long) * 3 * nrows));
+  } else {
+    DPGB_TRY(dp.ws_keys.alloc(sizeof(int) * npair));
+    DPGB_TRY(dp.ws_tr.alloc(transpose_workspace(npair, (int)nkeys)));
+  }
   DPGB_TRY(dp.ws_status.alloc(sizeof(int) * kStatusSlots));
   DPGB_TRY(dp.ws_coord.alloc(sizeof(double) * nrows * 3));
   DPGB_TRY(dp.ws_svec.alloc(sizeof(double) * 3 * (size_t)nshift_max * nframes));
@@ -1270,14 +1321,17 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   // sorted transpose of the list over local rows
   // the sorted transpose on the side stream: only the force gather needs it
   cudaStream_t ts = st;
-  if (dp.side) {
+  const bool fork = dp.side && !scatter;
+  if (fork) {
     DPGB_CUDA(cudaEventRecord(dp.ev_fork, st));
     DPGB_CUDA(cudaStreamWaitEvent(dp.side, dp.ev_fork, 0));
     ts = dp.side;
   }
   dp.mark(DPGB_STAGE_TRANSPOSE, 0, ts);
-  Transpose tr;
-  if (npair > 0) {
+  Transpose tr{};
+  if (scatter) {
+    DPGB_CUDA(cudaMemsetAsync(dp.ws_facc.ptr, 0, sizeof(unsigned long long) * 3 * nrows, ts));
+  } else if (npair > 0) {
     // image-major indices fold onto their atom; explicit extended indices
     // are their own keys
     if (batch)
@@ -1288,10 +1342,12 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     DPGB_TRY(check_launch("model_keys"));
     ++launches;
   }
-  DPGB_TRY(launch_transpose(tr, dp.ws_keys.as<int>(), npair, (int)nkeys, 0, dp.ws_tr.ptr, status, ts));
-  launches += 4;
+  if (!scatter) {
+    DPGB_TRY(launch_transpose(tr, dp.ws_keys.as<int>(), npair, (int)nkeys, 0, dp.ws_tr.ptr, status, ts));
+    launches += 4;
+  }
   dp.mark(DPGB_STAGE_TRANSPOSE, 1, ts);
-  if (dp.side) DPGB_CUDA(cudaEventRecord(dp.ev_join, dp.side));
+  if (fork) DPGB_CUDA(cudaEventRecord(dp.ev_join, dp.side));
   // descriptor forward
   DescParams<T> p{};
   p.nloc = natom;
@@ -1446,9 +1502,17 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
     ++launches;
   }
   dp.mark(DPGB_STAGE_DESC_BWD, 1, st);
-  if (dp.side) DPGB_CUDA(cudaStreamWaitEvent(st, dp.ev_join, 0));  // the transpose is done
+  if (fork) DPGB_CUDA(cudaStreamWaitEvent(st, dp.ev_join, 0));  // the transpose is done
   dp.mark(DPGB_STAGE_REDUCE, 0, st);
-  if (ext) {
+  if (scatter) {
+    force_scatter_model_kernel<<<ceil_div(nrows, kGatherWarps), kGatherWarps * 32, 0, st>>>(
+        force, dp.ws_facc.as<unsigned long long>(), reinterpret_cast<const float*>(dp.ws_g.ptr), nlist, natom,
+        FastDiv(natom), nnei, (int)nrows);
+    DPGB_TRY(check_launch("force_scatter"));
+    force_fix_kernel<<<ceil_div(3 * nrows, 256), 256, 0, st>>>(force, dp.ws_facc.as<unsigned long long>(),
+                                                                (int)(3 * nrows));
+    ++launches;
+  } else if (ext) {
     if (atom_virial)
       force_gather_ext_kernel<T, true><<<ceil_div(nkeys, kGatherWarps), kGatherWarps * 32, 0, st>>>(
           force, atom_virial, dp.ws_g.as<T>(), tr, nlist, ext->coord, natom, ext->nall, nnei);
