@@ -144,6 +144,9 @@ __device__ __forceinline__ double warp_comp_sum(float hi, float lo) {
 // "Division by invariant integers using multiplication", PLDI 1994): with
 // 2^l >= d and m = ceil(2^(31+l) / d) < 2^32, floor(n m / 2^(31+l)) = n / d
 // for every 0 <= n < 2^31 (the error m d - 2^(31+l) < d adds less than 1/d).
+// scale of the 2^-32 fixed-point force sums (64-bit integers)
+constexpr float kFixScale = 4294967296.f;  // 2^32
+
 struct FastDiv {
   unsigned m = 1u << 31;
   int s = 31;

@@ -195,17 +195,17 @@ force_gather_model_kernel(double* __restrict__ force, double* __restrict__ atom_
 }
 
 // Mixed form without atomic virials: the forces of a local model list with
-// no transpose.  The pair gradients g of a row add onto the row in a fixed
-// order (as in force_gather_model_kernel); each one's share on its
-// neighbour, -g, is scaled by 2^32, rounded to an integer and added with a
-// 64-bit integer atomic (red) into acc[key] — integer sums are exact, so the
+// no transpose.  A row's pair gradients g add up in a fixed order (as in
+// force_gather_model_kernel); that sum, and each pair's share on its
+// neighbour, -g, are scaled by 2^32, rounded to integers and added with
+// 64-bit integer atomics (red) into acc — integer sums are exact, so the
 // result does not depend on the order of the adds and repeats bitwise (the
 // rounding: 2^-33 per term, far below FP32 resolution at the force scale).
-// force_fix_kernel then adds acc * 2^-32 onto the rows' own sums.
-constexpr float kFixScale = 4294967296.f;  // 2^32
+// The table backward does the same inline (DescParams::facc);
+// force_fix_kernel then converts acc to the forces.
 
 __global__ void __launch_bounds__(kGatherWarps * 32)
-force_scatter_model_kernel(double* __restrict__ force, unsigned long long* __restrict__ acc,
+force_scatter_model_kernel(unsigned long long* __restrict__ acc,
                            const float* __restrict__ g, const int* __restrict__ nlist, int nloc, FastDiv by_nloc,
                            int nnei, int nrows) {
   const int lane = threadIdx.x & 31;
@@ -229,12 +229,13 @@ force_scatter_model_kernel(double* __restrict__ force, unsigned long long* __res
   f.reduce();
   if (lane == 0)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) force[3 * (size_t)row + c] = f.get(c);
+    for (int c = 0; c < 3; ++c)
+      atomicAdd(acc + 3 * (size_t)row + c, (unsigned long long)llrint(f.get(c) * (double)kFixScale));
 }
 
 __global__ void force_fix_kernel(double* __restrict__ force, const unsigned long long* __restrict__ acc, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) force[i] += (double)(long long)acc[i] * (1.0 / 4294967296.0);
+  if (i < n) force[i] = (double)(long long)acc[i] * (1.0 / 4294967296.0);
 }
 
 // The same with explicit extended atoms (external list, one frame): every one
@@ -1365,6 +1366,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   p.dstd = m.dstd;
   p.dstd_inv = m.dstd_inv;
   p.nloc_div = FastDiv(natom);
+  p.facc = scatter ? dp.ws_facc.as<unsigned long long>() : nullptr;
   p.pair_mask = d.pair_mask ? dp.pair_mask_dev.as<int>() : nullptr;
   p.coord = coord_n;
   p.atype = dp.atype_dev.as<int>();
@@ -1505,10 +1507,13 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   if (fork) DPGB_CUDA(cudaStreamWaitEvent(st, dp.ev_join, 0));  // the transpose is done
   dp.mark(DPGB_STAGE_REDUCE, 0, st);
   if (scatter) {
-    force_scatter_model_kernel<<<ceil_div(nrows, kGatherWarps), kGatherWarps * 32, 0, st>>>(
-        force, dp.ws_facc.as<unsigned long long>(), reinterpret_cast<const float*>(dp.ws_g.ptr), nlist, natom,
-        FastDiv(natom), nnei, (int)nrows);
-    DPGB_TRY(check_launch("force_scatter"));
+    if (!tab_path) {  // the table backward added the pair gradients itself
+      force_scatter_model_kernel<<<ceil_div(nrows, kGatherWarps), kGatherWarps * 32, 0, st>>>(
+          dp.ws_facc.as<unsigned long long>(), reinterpret_cast<const float*>(dp.ws_g.ptr), nlist, natom,
+          FastDiv(natom), nnei, (int)nrows);
+      DPGB_TRY(check_launch("force_scatter"));
+      ++launches;
+    }
     force_fix_kernel<<<ceil_div(3 * nrows, 256), 256, 0, st>>>(force, dp.ws_facc.as<unsigned long long>(),
                                                                 (int)(3 * nrows));
     ++launches;

@@ -106,6 +106,10 @@ struct DescParams {
   const float4* xlo;
   const float4* shi;
   const float4* slo;
+  // forces as 2^-32 fixed-point integers [nrows][3] (model lists): when set,
+  // the table backward adds each pair's gradient onto its row and its
+  // neighbour's row with 64-bit integer atomics instead of storing it
+  unsigned long long* facc;
 };
 
 // r_nb - r_i in FP64 for neighbour nb of local atom i of frame f, and the

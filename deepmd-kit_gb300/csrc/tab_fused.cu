@@ -418,7 +418,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
           const bool real = have && nl[slot] >= 0;
           const unsigned m = __ballot_sync(0xffffffffu, real);
           if (real) s_list[nreal + __popc(m & ((1u << lane) - 1u))] = slot;
-          if (have && !real) {
+          if (have && !real && !p.facc) {
             gp_row[3 * slot] = 0.f;
             gp_row[3 * slot + 1] = 0.f;
             gp_row[3 * slot + 2] = 0.f;
@@ -429,6 +429,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
         float vir_hi[9], vir_lo[9];  // compensated FP32 sums of the lane's pairs
 #pragma unroll
         for (int k = 0; k < 9; ++k) vir_hi[k] = vir_lo[k] = 0.f;
+        float own[3] = {0.f, 0.f, 0.f};  // fixed-point forces: the row's share of the lane's pairs
         for (int q0 = 0; q0 < nreal; q0 += 32) {
           const bool mine = q0 + lane < nreal;
           const int slot = mine ? s_list[q0 + lane] : p.sec[sec];
@@ -572,10 +573,31 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
 #pragma unroll
                 for (int l = 0; l < 3; ++l) comp_add(vir_hi[3 * k + l], vir_lo[3 * k + l], -g[k] * s.d[l]);
             }
-            gp_row[3 * slot] = g[0];
-            gp_row[3 * slot + 1] = g[1];
-            gp_row[3 * slot + 2] = g[2];
+            if (p.facc) {
+              if (act) {  // -g onto the neighbour's row (image-major index: atom nb mod nloc of this frame)
+                const int nb = nl[slot];
+                const int fbase = p.nloc_div.div(row) * p.nloc;
+                unsigned long long* a = p.facc + 3 * (size_t)(fbase + nb - p.nloc_div.div(nb) * p.nloc);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                  own[k] += g[k];
+                  atomicAdd(a + k, (unsigned long long)__float2ll_rn(-g[k] * kFixScale));
+                }
+              }
+            } else {
+              gp_row[3 * slot] = g[0];
+              gp_row[3 * slot + 1] = g[1];
+              gp_row[3 * slot + 2] = g[2];
+            }
           }
+        }
+        if (p.facc) {
+#pragma unroll
+          for (int k = 0; k < 3; ++k) own[k] = warp_sum(own[k]);
+          if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+              atomicAdd(p.facc + 3 * (size_t)row + k, (unsigned long long)__float2ll_rn(own[k] * kFixScale));
         }
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
