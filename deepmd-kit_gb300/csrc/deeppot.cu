@@ -1507,7 +1507,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   if (fork) DPGB_CUDA(cudaStreamWaitEvent(st, dp.ev_join, 0));  // the transpose is done
   dp.mark(DPGB_STAGE_REDUCE, 0, st);
   if (scatter) {
-    if (!tab_path) {  // the table backward added the pair gradients itself
+    if (!tab_path && !tc_path) {  // the table and tensor-core backwards added the pair gradients themselves
       force_scatter_model_kernel<<<ceil_div(nrows, kGatherWarps), kGatherWarps * 32, 0, st>>>(
           dp.ws_facc.as<unsigned long long>(), reinterpret_cast<const float*>(dp.ws_g.ptr), nlist, natom,
           FastDiv(natom), nnei, (int)nrows);

@@ -391,7 +391,7 @@ struct PlanB {
   // high parts), as in the forward; the gradient operands dP3, dP2 are BF16
   static constexpr int a1 = reg, a1lo = reg + 128 * K1 * 2, a2 = reg, a2lo = reg + 128 * N2 * 2, a3 = reg, vir = reg;
   static constexpr int cmax(int a, int b) { return a > b ? a : b; }
-  static constexpr int reg_bytes = cmax(cmax(2 * 128 * K1 * 2, 2 * 128 * N2 * 2), cmax(128 * N3 * 2, 128 * 9 * 4));
+  static constexpr int reg_bytes = cmax(cmax(2 * 128 * K1 * 2, 2 * 128 * N2 * 2), cmax(128 * N3 * 2, 128 * 12 * 4));
   static constexpr int total = reg + reg_bytes;
   static constexpr int tmem_cols = cmax(N3, N2 + K1) <= 128 ? 128 : 256;
 };
@@ -914,25 +914,40 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
             for (int k = 0; k < 3; ++k) g[k] -= w * der[3 * cc + k];
           }
         }
-        if (pi.valid) {
+        if (p.facc) {  // -g onto the neighbour's row as 2^-32 fixed point (image-major: atom nb mod nloc)
+          if (pi.valid && pi.nb >= 0 && pi.keep) {
+            const int fbase = p.nloc_div.div(pi.row) * p.nloc;
+            unsigned long long* a = p.facc + 3 * (size_t)(fbase + pi.nb - p.nloc_div.div(pi.nb) * p.nloc);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) atomicAdd(a + k, (unsigned long long)__float2ll_rn(-g[k] * kFixScale));
+          }
+        } else if (pi.valid) {
           float* gp = gpair + ((size_t)pi.row * p.nnei + pi.slot) * 3;
           gp[0] = g[0];
           gp[1] = g[1];
           gp[2] = g[2];
         }
         // the operand region is free (the last MMA completed): pair virials
+        // and (fixed-point forces) the pair gradients, 12 per pair
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
+        for (int k = 0; k < 3; ++k) {
 #pragma unroll
-          for (int l = 0; l < 3; ++l) sVir[tid * 9 + 3 * k + l] = -g[k] * dv[l];
+          for (int l = 0; l < 3; ++l) sVir[tid * 12 + 3 * k + l] = -g[k] * dv[l];
+          sVir[tid * 12 + 9 + k] = g[k];
+        }
         tc::fence_before();
         alive = __syncthreads_and(ok) != 0;
         if (!alive) break;
-        for (int q = tid; q < ntile * 9; q += blockDim.x) {
-          const int k = q / 9, comp = q - 9 * k;
+        const int ncomp = p.facc ? 12 : 9;
+        for (int q = tid; q < ntile * ncomp; q += blockDim.x) {
+          const int k = q / ncomp, comp = q - ncomp * k;
           float hi = 0.f, lo = 0.f;  // compensated FP32 sum (the FP64 pipe is narrow)
-          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) comp_add(hi, lo, sVir[pp * 9 + comp]);
-          vir_row[(size_t)s_row[k] * 9 + comp] += (double)hi + (double)lo;
+          for (int pp = s_off[k]; pp < s_off[k + 1]; ++pp) comp_add(hi, lo, sVir[pp * 12 + comp]);
+          if (comp < 9)
+            vir_row[(size_t)s_row[k] * 9 + comp] += (double)hi + (double)lo;
+          else  // the atom's own pairs
+            atomicAdd(p.facc + 3 * (size_t)s_row[k] + comp - 9,
+                      (unsigned long long)llrint(((double)hi + (double)lo) * (double)kFixScale));
         }
         __syncthreads();
       }

@@ -1513,8 +1513,8 @@ __global__ void __launch_bounds__(kSkinWarps * 32)
 skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int ncand, const double* __restrict__ coord,
                    const float4* __restrict__ coordf, const float4* __restrict__ coordflo,
                    const int* __restrict__ atype, const double* __restrict__ svec, const float4* __restrict__ svecf,
-                   const float4* __restrict__ svecflo, int nloc, double rcut, float rcf2, float eps, SelInfo sel,
-                   int* __restrict__ status) {
+                   const float4* __restrict__ svecflo, int nloc, FastDiv by_nloc, double rcut, float rcf2, float eps,
+                   SelInfo sel, int* __restrict__ status) {
   __shared__ double s_r[kSkinWarps][kKeptCap];
   __shared__ int s_i[kSkinWarps][kKeptCap];
   __shared__ int s_t[kSkinWarps][kKeptCap];
@@ -1541,7 +1541,7 @@ skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int nc
     if (__all_sync(0xffffffffu, e < 0)) break;  // candidate rows are packed: padding from here on
     bool keep = false;
     if (e >= 0) {
-      const int s = e / nloc, j = e - s * nloc;
+      const int s = by_nloc.div(e), j = e - s * nloc;
       const float4 fj = coordf[j], sv = svecf[s];
       const float fx = (fj.x + sv.x) - fi.x, fy = (fj.y + sv.y) - fi.y, fz = (fj.z + sv.z) - fi.z;
       keep = fx * fx + fy * fy + fz * fz <= rcf2;
@@ -1569,7 +1569,7 @@ skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int nc
     int e = 0, t = 0;
     if (k < nc) {
       e = wi[k];
-      const int s = e / nloc, j = e - s * nloc;
+      const int s = by_nloc.div(e), j = e - s * nloc;
       t = atype[j];
       const float4 jh = coordf[j], jl = coordflo[j], sh = svecf[s], sl = svecflo[s];
       const float fx = disp_split(jh.x, jl.x, sh.x, sl.x, fi.x, fil.x);
@@ -1684,8 +1684,8 @@ int launch_skin_select(int* nlist, const int* cand, int ncand, const double* coo
   // the coordinates' magnitude), FP32 norm (<= 2^-22 r), x1.5
   const float eps = (float)(rcut * 1.5 * (0x1p-24 + 0x1p-22) + 1e-7);
   skin_select_kernel<<<ceil_div(nloc, kSkinWarps), kSkinWarps * 32, 0, st>>>(
-      nlist, cand, ncand, coord, coordf, coordflo, atype, svec, svecf, svecflo, nloc, rcut, rcf * rcf, eps, sel,
-      status);
+      nlist, cand, ncand, coord, coordf, coordflo, atype, svec, svecf, svecflo, nloc, FastDiv(nloc), rcut, rcf * rcf,
+      eps, sel, status);
   return check_launch("skin_select");
 }
 
