@@ -433,7 +433,7 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
 // per neuron, the transposed term of the first 16 neurons accumulates in
 // registers and is added at the end.  The MMAs of chunk j + 1 run while the
 // epilogue reads chunk j.
-constexpr int kDxM = 16, kDxBN = 128, kDxStages = 5, kDxSeg = 2;
+constexpr int kDxM = 16, kDxBN = 128, kDxStages = 4, kDxSeg = 2;
 constexpr int kDxThreads = 192;  // 4 epilogue warps, the load warp, the MMA warp
 
 __global__ void __launch_bounds__(kDxThreads, 1)
@@ -554,8 +554,23 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   const float inv = 1.f / (float)f.nnei;
   constexpr int NH = kDxBN / M;  // neurons per chunk
   float xqn[NH][4];                // xyz[c][n] of the next chunk's neurons, in flight
+  const bool vec4 = (f.ng & 3) == 0;  // the chunk's neurons of a component as 16-byte aligned float4 pairs
   auto load_xq = [&](int j) {
     const int qn = j < nchunk ? min(kDxBN, ncol - j * kDxBN) / M : 0;
+    if (vec4) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int h4 = 0; h4 < NH; h4 += 4) {
+          const float4 x = (valid && h4 < qn) ? *reinterpret_cast<const float4*>(xr + c * f.ng + j * NH + h4)
+                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+          xqn[h4][c] = x.x;
+          xqn[h4 + 1][c] = x.y;
+          xqn[h4 + 2][c] = x.z;
+          xqn[h4 + 3][c] = x.w;
+        }
+      return;
+    }
 #pragma unroll
     for (int h = 0; h < NH; ++h)
 #pragma unroll
