@@ -181,22 +181,29 @@ def table_bytes_flops(n_atoms: int, n_pairs: int, cfg) -> dict:
     dE/dxyz (FP32 [ng][4]) in, the pair gradients (3 FP32 per slot) and the
     per-atom virial (9 FP64) out.  FLOPs per real pair and neuron: forward
     the quintic (5 FMA) and the contraction (4 FMA); backward the quintic
-    with its derivative (9 FMA), dG = R~ . dX (4), dR~ (4), ds (1)."""
+    with its derivative (9 FMA), dG = R~ . dX (4), dR~ (4), ds (1).  Shared
+    memory: per real pair and neuron the interval's six FP32 coefficients
+    (24 B) in either direction, the reads that bound both kernels."""
     S, ng, M = cfg.nnei, cfg.ng, cfg.axis_neuron
+    smem = n_pairs * ng * 24
     return {
-        "desc_fwd": {"bytes": n_atoms * (4 * S + 24 + 16 * ng + 2 * ng * M), "flops": n_pairs * ng * 9 * 2},
-        "desc_bwd": {"bytes": n_atoms * (4 * S + 24 + 16 * ng + 12 * S + 72), "flops": n_pairs * ng * 18 * 2},
+        "desc_fwd": {"bytes": n_atoms * (4 * S + 24 + 16 * ng + 2 * ng * M), "flops": n_pairs * ng * 9 * 2,
+                     "smem_bytes": smem},
+        "desc_bwd": {"bytes": n_atoms * (4 * S + 24 + 16 * ng + 24 + 72), "flops": n_pairs * ng * 18 * 2,
+                     "smem_bytes": smem},
     }
 
 
 # FP32 CUDA-core peak (no tensor cores): 152 SMs x 128 lanes x 2 FLOP x 2.07 GHz
 FP32_SIMT_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12
+# shared-memory read peak: 152 SMs x 128 B per clock x 2.07 GHz
+SMEM_TBS_NOMINAL = 152 * 128 * 2.07e9 / 1e12
 
 # DRAM bytes (read + write) per launch of the dominant kernels of the
 # 98,304-atom compressed step, from one ncu capture each: tab_fwd, tab_bwd
 # (profiles/tab_fused_water98304_compressed.md) and the fitting stage's six
 # launches summed (five fit_gemm + fit_dxyz, one dram-bytes pass)
-DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 727.6e6, "desc_bwd": 489.7e6, "fitting": 2103.7e6}
+DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 1068.5e6, "desc_bwd": 765.9e6, "fitting": 2168.8e6}
 
 
 def table_roofline(per_step: dict, n_atoms: int, n_pairs: int, cfg) -> dict:
@@ -222,7 +229,10 @@ def table_roofline(per_step: dict, n_atoms: int, n_pairs: int, cfg) -> dict:
             "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": DRAM_BYTES_PER_LAUNCH_98K.get(dom),
             "peak_source": f"{kind} hbm_gbs", "algorithmic_bytes_per_launch": w["bytes"],
             "simt_fp32": {"achieved_tflops": simt, "peak_tflops_nominal": FP32_SIMT_TFLOPS_NOMINAL,
-                          "frac": simt / FP32_SIMT_TFLOPS_NOMINAL, "flops_per_launch": w["flops"]}}
+                          "frac": simt / FP32_SIMT_TFLOPS_NOMINAL, "flops_per_launch": w["flops"]},
+            "smem_table_reads": {"achieved_tbs": w["smem_bytes"] / sec / 1e12, "peak_tbs_nominal": SMEM_TBS_NOMINAL,
+                                 "frac": w["smem_bytes"] / sec / 1e12 / SMEM_TBS_NOMINAL,
+                                 "bytes_per_launch": w["smem_bytes"]}}
 
 
 def water_model(compressed: bool):
