@@ -116,6 +116,27 @@ def test_bitwise_reproducible(water_fp64):
         np.testing.assert_array_equal(x, y)
 
 
+@pytest.mark.parametrize("compressed", [False, True])
+def test_mixed_forces_bitwise_reproducible(cuda, compressed):
+    """The mixed form's forces are summed with integer atomics (2^-32 fixed
+    point): whatever order the adds land in, repeated evaluations agree
+    bitwise."""
+    from dpgb import synth
+    from dpgb.deeppot import DeepPot
+
+    coord, atype, box = synth.water_box(8, seed=11)
+    dp = DeepPot(water_params(compressed=compressed), "mixed")
+    runs = [dp.eval(coord.reshape(1, -1), box, atype) for _ in range(3)]
+    for other in runs[1:]:
+        for x, y in zip(runs[0], other):
+            np.testing.assert_array_equal(x, y)
+    # the forces sum to zero over the box (every pair adds g to one row and
+    # -g to another; what is left is the rows' own FP32 sums' rounding, far
+    # below a dropped pair's share)
+    f = runs[0][1][0]
+    assert np.abs(f.sum(axis=0)).max() < 1e-3
+
+
 def test_multi_frame_batch(water_fp64):
     from dpgb import synth
 
