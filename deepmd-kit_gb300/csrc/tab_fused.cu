@@ -382,7 +382,10 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
   float4* s_dx = reinterpret_cast<float4*>(tail) + (size_t)warp * ng;                    // [warp][ng]
   int* s_list = reinterpret_cast<int*>(reinterpret_cast<float4*>(tail) + (size_t)kBwdWarps * ng) +
                 (size_t)warp * p.nnei;                                                     // [warp][nnei]
+  int* s_perm = reinterpret_cast<int*>(reinterpret_cast<float4*>(tail) + (size_t)kBwdWarps * ng) +
+                (size_t)kBwdWarps * p.nnei + warp * 32;                                    // [warp][32]
   const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
+  const int bank_step = (row_stride / 2) & 15;  // a row's 8-byte bank pair advances by this per row
   __shared__ int s_work;
   for (int c = work_first(queue, &s_work); c < nchunks; c = work_next(queue, c, &s_work)) {
     const WorkChunk ch = chunks[c];
@@ -455,7 +458,54 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             }
             table_locate(tm, s.rn[0], s.idx, s.xx, s.delta);
           }
-          const bool act = mine && s.active;  // excluded type pairs carry no gradient
+          bool act = mine && s.active;  // excluded type pairs carry no gradient
+          int slot_p = slot;
+          bool mine_p = mine;
+          {
+            // Lanes for the pairs such that each half-warp's 8-byte
+            // coefficient loads spread over the 16 bank pairs: the distinct
+            // staged rows of one bank class (row * bank_step mod 16) go to
+            // the two halves in turn (a row's repeats stay with it, a
+            // broadcast); pairs with no staged row fill the free lanes.
+            const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
+            const bool has = act && s.idx < rows;
+            const int cls = (s.idx * bank_step) & 15;
+            const unsigned m_row = __match_any_sync(full, has ? s.idx : -1 - lane);
+            const int first = __ffs(m_row) - 1;
+            const unsigned firsts = __ballot_sync(full, has && lane == first);
+            const unsigned m_cls = __match_any_sync(full, has ? cls : -64 - lane);
+            const int half = has ? (__popc(m_cls & firsts & ((1u << first) - 1u)) & 1) : 2;
+            const unsigned A = __ballot_sync(full, half == 0), B = __ballot_sync(full, half == 1),
+                           F = __ballot_sync(full, half == 2);
+            const int nA = __popc(A), nB = __popc(B);
+            const int a_keep = min(nA, 16), b_keep = min(nB, 16);
+            const int a_occ = a_keep + max(nB - 16, 0), b_occ = b_keep + max(nA - 16, 0);
+            int pos;
+            if (half == 0) {
+              const int k = __popc(A & lt);
+              pos = k < 16 ? k : 16 + b_keep + (k - 16);
+            } else if (half == 1) {
+              const int k = __popc(B & lt);
+              pos = k < 16 ? 16 + k : a_keep + (k - 16);
+            } else {
+              const int k = __popc(F & lt);
+              pos = k < 16 - a_occ ? a_occ + k : 16 + b_occ + (k - (16 - a_occ));
+            }
+            s_perm[pos] = lane;
+            __syncwarp();
+            const int src = s_perm[lane];
+            __syncwarp();  // read before the next batch writes
+#pragma unroll
+            for (int c = 0; c < 4; ++c) s.rn[c] = __shfl_sync(full, s.rn[c], src);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) s.d[c] = __shfl_sync(full, s.d[c], src);
+            s.idx = __shfl_sync(full, s.idx, src);
+            s.xx = __shfl_sync(full, s.xx, src);
+            s.delta = __shfl_sync(full, s.delta, src);
+            slot_p = __shfl_sync(full, slot, src);
+            act = __shfl_sync(full, (int)act, src) != 0;
+            mine_p = __shfl_sync(full, (int)mine, src) != 0;
+          }
           // a pair whose interval's row is not staged (the closest
           // neighbours) is walked by the whole warp below, so that the
           // lane-per-pair loop reads shared memory only
@@ -553,7 +603,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
               }
             }
           }
-          if (mine) {
+          if (mine_p) {
             float g[3] = {0.f, 0.f, 0.f};
             if (act) {
               // dR~ (+ ds through s = R~[0]) -> the pair gradient and virial
@@ -561,7 +611,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
               dR[0] += ds;
               float der[12];
               slot_deriv(s.d, rmin, rmax, der);
-              const float* sdi = p.dstd_inv + ((size_t)ti * p.nnei + slot) * 4;
+              const float* sdi = p.dstd_inv + ((size_t)ti * p.nnei + slot_p) * 4;
 #pragma unroll
               for (int cc = 0; cc < 4; ++cc) {
                 const float w = dR[cc] * sdi[cc];
@@ -575,7 +625,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             }
             if (p.facc) {
               if (act) {  // -g onto the neighbour's row (image-major index: atom nb mod nloc of this frame)
-                const int nb = nl[slot];
+                const int nb = nl[slot_p];
                 const int fbase = p.nloc_div.div(row) * p.nloc;
                 unsigned long long* a = p.facc + 3 * (size_t)(fbase + nb - p.nloc_div.div(nb) * p.nloc);
 #pragma unroll
@@ -585,9 +635,9 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
                 }
               }
             } else {
-              gp_row[3 * slot] = g[0];
-              gp_row[3 * slot + 1] = g[1];
-              gp_row[3 * slot + 2] = g[2];
+              gp_row[3 * slot_p] = g[0];
+              gp_row[3 * slot_p + 1] = g[1];
+              gp_row[3 * slot_p + 2] = g[2];
             }
           }
         }
@@ -653,7 +703,7 @@ int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const 
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t per_warp = (size_t)p.ng * sizeof(float4) + (size_t)p.nnei * sizeof(int);
+  const size_t per_warp = (size_t)p.ng * sizeof(float4) + (size_t)p.nnei * sizeof(int) + 32 * sizeof(int);
   const size_t fixed = (size_t)kBwdWarps * per_warp + 16 + 1024;
   if ((size_t)optin <= fixed) return fail(DPGB_EINVAL, "tab_bwd: the neighbour list is too wide");
   const int rows = (int)(((size_t)optin - fixed) / ((size_t)row_stride * sizeof(float)));
