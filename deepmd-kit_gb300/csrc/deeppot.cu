@@ -1154,7 +1154,10 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   DPGB_TRY(dp.ws_nlist.alloc(sizeof(int) * npair));
   // the mixed form's model-list forces without atomic virials go through
   // the fixed-point scatter; every other gather reads the sorted transpose
-  const bool scatter = std::is_same<T, float>::value && own_geom && !atom_virial;
+  // (a batch: when the tensor-core or table backward adds the gradients
+  // itself, which finds each row's frame)
+  const bool fused_bwd = std::is_same<T, float>::value && (dp.use_tc != 0 || dp.use_tab != 0);
+  const bool scatter = std::is_same<T, float>::value && !ext && !atom_virial && (own_geom || (batch && fused_bwd));
   if (scatter) {
     DPGB_TRY(dp.ws_facc.alloc(sizeof(unsigned long long) * 3 * nrows));
   } else {

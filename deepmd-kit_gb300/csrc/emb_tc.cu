@@ -914,10 +914,9 @@ emb_tc_bwd_kernel(DescParams<float> p, EmbTC e, const WorkChunk* __restrict__ ch
             for (int k = 0; k < 3; ++k) g[k] -= w * der[3 * cc + k];
           }
         }
-        if (p.facc) {  // -g onto the neighbour's row as 2^-32 fixed point (image-major: atom nb mod nloc)
+        if (p.facc) {  // -g onto the neighbour's row as 2^-32 fixed point
           if (pi.valid && pi.nb >= 0 && pi.keep) {
-            const int fbase = p.nloc_div.div(pi.row) * p.nloc;
-            unsigned long long* a = p.facc + 3 * (size_t)(fbase + pi.nb - p.nloc_div.div(pi.nb) * p.nloc);
+            unsigned long long* a = p.facc + 3 * (size_t)neighbour_row(p, pi.row, pi.nb);
 #pragma unroll
             for (int k = 0; k < 3; ++k) atomicAdd(a + k, (unsigned long long)__float2ll_rn(-g[k] * kFixScale));
           }

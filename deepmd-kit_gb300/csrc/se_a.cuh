@@ -112,6 +112,19 @@ struct DescParams {
   unsigned long long* facc;
 };
 
+// The row whose force takes the neighbour's share of pair (row, nb): atom
+// nb mod (the frame's atom count) of the row's frame (image-major index nb;
+// a batch's frames are found from frame_atom_off).
+template <typename T>
+__device__ __forceinline__ int neighbour_row(const DescParams<T>& p, int row, int nb) {
+  if (p.frame_atom_off) {
+    const int f = frame_of(p.frame_atom_off, p.nframes_batch, row);
+    const int beg = p.frame_atom_off[f];
+    return beg + nb % (p.frame_atom_off[f + 1] - beg);
+  }
+  return p.nloc_div.div(row) * p.nloc + nb - p.nloc_div.div(nb) * p.nloc;
+}
+
 // r_nb - r_i in FP64 for neighbour nb of local atom i of frame f, and the
 // neighbour's type.  Image-major indices: r_nb = coord[nb % nloc] + shift.
 template <typename T>

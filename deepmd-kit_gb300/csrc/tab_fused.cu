@@ -624,10 +624,8 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
                 for (int l = 0; l < 3; ++l) comp_add(vir_hi[3 * k + l], vir_lo[3 * k + l], -g[k] * s.d[l]);
             }
             if (p.facc) {
-              if (act) {  // -g onto the neighbour's row (image-major index: atom nb mod nloc of this frame)
-                const int nb = nl[slot_p];
-                const int fbase = p.nloc_div.div(row) * p.nloc;
-                unsigned long long* a = p.facc + 3 * (size_t)(fbase + nb - p.nloc_div.div(nb) * p.nloc);
+              if (act) {  // -g onto the neighbour's row
+                unsigned long long* a = p.facc + 3 * (size_t)neighbour_row(p, row, nl[slot_p]);
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                   own[k] += g[k];
