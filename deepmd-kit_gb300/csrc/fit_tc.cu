@@ -34,13 +34,13 @@ constexpr int kKC = 64;
 // exponential and the division of CUDA's fast intrinsics (relative error of
 // a few 1e-7 before the subtraction, which only shrinks it).
 __device__ __forceinline__ float tanh_acc(float x) {
+  // both forms, then a select: no branch per element in the epilogues
   const float a = fabsf(x);
-  if (a < 0.0625f) {
-    const float x2 = x * x;
-    return x * fmaf(x2, fmaf(x2, fmaf(x2, -17.f / 315.f, 2.f / 15.f), -1.f / 3.f), 1.f);
-  }
+  const float x2 = x * x;
+  const float ser = x * fmaf(x2, fmaf(x2, fmaf(x2, -17.f / 315.f, 2.f / 15.f), -1.f / 3.f), 1.f);
   const float e = __expf(2.f * fminf(a, 12.f));
-  return copysignf(1.f - __fdividef(2.f, e + 1.f), x);
+  const float big = copysignf(1.f - __fdividef(2.f, e + 1.f), x);
+  return a < 0.0625f ? ser : big;
 }
 
 // high and low BF16 parts of an FP32 value (hi + lo carries ~16 bits)
@@ -101,20 +101,23 @@ __device__ __forceinline__ void store_tile(const float4* w, int lane, float* bas
     if (r < rows_ok) *reinterpret_cast<float4*>(base + (size_t)r * ld + 4 * (lane & 3)) = w[unit_f32(r, lane & 3)];
   }
 }
-// BF16: the row's 16 values rounded (lo: the rounding of the remainder when
-// hi_part is false) into the tile, then stored coalesced
-__device__ __forceinline__ void put_row_b16(float4* w, int lane, const float (&v)[16], bool hi_part) {
-  __nv_bfloat162 h[8];
+// BF16: the row's 16 values split once into high parts (units 0..63 of the
+// tile) and low parts (units 64..127), then stored coalesced
+__device__ __forceinline__ void put_row_b16(float4* w, int lane, const float (&v)[16]) {
+  __nv_bfloat162 h[8], l[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     __nv_bfloat16 a, b, al, bl;
     split_bf16(v[2 * i], a, al);
     split_bf16(v[2 * i + 1], b, bl);
-    h[i] = hi_part ? __halves2bfloat162(a, b) : __halves2bfloat162(al, bl);
+    h[i] = __halves2bfloat162(a, b);
+    l[i] = __halves2bfloat162(al, bl);
   }
   uint4* u = reinterpret_cast<uint4*>(w);
   u[unit_b16(lane, 0)] = *reinterpret_cast<const uint4*>(&h[0]);
   u[unit_b16(lane, 1)] = *reinterpret_cast<const uint4*>(&h[4]);
+  u[64 + unit_b16(lane, 0)] = *reinterpret_cast<const uint4*>(&l[0]);
+  u[64 + unit_b16(lane, 1)] = *reinterpret_cast<const uint4*>(&l[4]);
 }
 __device__ __forceinline__ void store_tile_b16(const float4* w, int lane, __nv_bfloat16* base, size_t ld,
                                                int rows_ok) {
@@ -134,19 +137,29 @@ __device__ __forceinline__ void emit_f32(float4* w, int lane, const float (&v)[1
   store_tile(w, lane, base, ld, rows_ok);
   __syncwarp();
 }
+// two FP32 rows through two tiles with one exchange (w2 == w: one after the other)
+__device__ __forceinline__ void emit2_f32(float4* w, float4* w2, int lane, const float (&a)[16], float* base_a,
+                                          const float (&b)[16], float* base_b, size_t ld, int rows_ok) {
+  if (w2 == w) {
+    emit_f32(w, lane, a, base_a, ld, rows_ok);
+    emit_f32(w, lane, b, base_b, ld, rows_ok);
+    return;
+  }
+  put_row(w, lane, a);
+  put_row(w2, lane, b);
+  __syncwarp();
+  store_tile(w, lane, base_a, ld, rows_ok);
+  store_tile(w2, lane, base_b, ld, rows_ok);
+  __syncwarp();
+}
 // split BF16 (hi at base, lo at base_lo when set)
 __device__ __forceinline__ void emit_b16(float4* w, int lane, const float (&v)[16], __nv_bfloat16* base,
                                          __nv_bfloat16* base_lo, size_t ld, int rows_ok) {
-  put_row_b16(w, lane, v, true);
+  put_row_b16(w, lane, v);
   __syncwarp();
   store_tile_b16(w, lane, base, ld, rows_ok);
+  if (base_lo) store_tile_b16(w + 64, lane, base_lo, ld, rows_ok);
   __syncwarp();
-  if (base_lo) {
-    put_row_b16(w, lane, v, false);
-    __syncwarp();
-    store_tile_b16(w, lane, base_lo, ld, rows_ok);
-    __syncwarp();
-  }
 }
 
 // Per-type column vectors of the epilogue, staged in shared memory at the
@@ -178,8 +191,8 @@ __device__ __forceinline__ void fit_decode(const FitGemm& g, int BN, int nnt, in
 // group h, TMEM quadrant q) walks the items j = h (mod EG) of the CTA, 16
 // accumulator columns at a time.
 template <int MODE, int BN, int EG, int NB, uint32_t kCols>
-__device__ __forceinline__ void fit_epilogue(const FitGemm& g, const float* svec, float4* wst, uint32_t tbase,
-                                             uint64_t* acc_full, uint64_t* acc_free, int* err) {
+__device__ __forceinline__ void fit_epilogue(const FitGemm& g, const float* svec, float4* wst, float4* wst2,
+                                             uint32_t tbase, uint64_t* acc_full, uint64_t* acc_free, int* err) {
   constexpr bool fwd = MODE == kFitFwd || MODE == kFitFwdLast, bwd = MODE == kFitBwd;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, h = warp >> 2, q = warp & 3;
   const int nnt = (g.N + BN - 1) / BN, items = g.tile0[g.ntypes] * nnt;
@@ -206,17 +219,26 @@ __device__ __forceinline__ void fit_epilogue(const FitGemm& g, const float* svec
     for (int c0 = 0; c0 < nt; c0 += 16) {
       const int n = n0 + c0;
       float xa_r[16], xb_r[16];
-      if (in_a) {
+      if (in_a && bwd && wst2 != wst) {  // both row operands through the two tiles at once
         put_tile(wst, lane, pa);
+        put_tile(wst2, lane, pb);
         __syncwarp();
         get_row(wst, lane, xa_r);
+        get_row(wst2, lane, xb_r);
         __syncwarp();
-      }
-      if (bwd) {
-        put_tile(wst, lane, pb);
-        __syncwarp();
-        get_row(wst, lane, xb_r);
-        __syncwarp();
+      } else {
+        if (in_a) {
+          put_tile(wst, lane, pa);
+          __syncwarp();
+          get_row(wst, lane, xa_r);
+          __syncwarp();
+        }
+        if (bwd) {
+          put_tile(wst, lane, pb);
+          __syncwarp();
+          get_row(wst, lane, xb_r);
+          __syncwarp();
+        }
       }
       if (c0 + 16 < nt) {
         if (in_a) load_tile(pa, lane, xa + (size_t)mw * lda_in + n + 16, lda_in, rows_ok);
@@ -242,8 +264,8 @@ __device__ __forceinline__ void fit_epilogue(const FitGemm& g, const float* svec
           }
         }
         if (MODE == kFitFwd) {
-          emit_f32(wst, lane, v, g.Yf + (size_t)mw * g.ldy + n, g.ldy, rows_ok);
-          emit_f32(wst, lane, tv, g.Tt + (size_t)mw * g.ldy + n, g.ldy, rows_ok);
+          emit2_f32(wst, wst2, lane, v, g.Yf + (size_t)mw * g.ldy + n, tv, g.Tt + (size_t)mw * g.ldy + n, g.ldy,
+                    rows_ok);
           emit_b16(wst, lane, v, g.Yb + (size_t)mw * g.ldy + n, g.Yb_lo ? g.Yb_lo + (size_t)mw * g.ldy + n : nullptr,
                    g.ldy, rows_ok);
         } else {
@@ -299,7 +321,7 @@ __device__ __forceinline__ void fit_epilogue(const FitGemm& g, const float* svec
 // next 16 columns' operands in flight.
 // NA: parts of A (1: hi, 2: hi and lo); the weight always comes as hi and
 // lo.  A stage holds one K chunk of every part, so each part is read once.
-template <int BN, int S, int NA, int EG, int NB>
+template <int BN, int S, int NA, int EG, int NB, int TILES>
 __global__ void __launch_bounds__(128 * EG + 64, 1)
 fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant__ CUtensorMap tma_alo,
                 const __grid_constant__ CUtensorMap tma_b, FitGemm g, int* __restrict__ err) {
@@ -314,8 +336,8 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   // the allocation: a power of two of at least NB buffers
   constexpr uint32_t kAlloc = NB * kCols <= 128 ? 128 : (NB * kCols <= 256 ? 256 : 512);
   static_assert(NB * kCols <= 512, "TMEM: 512 columns per SM");
-  float4* stage_tiles = reinterpret_cast<float4*>(smem + S * STAGE);
-  float* svec = reinterpret_cast<float*>(smem + S * STAGE + EG * 4 * kStageFloats * 4);
+  float4* stage_tiles = reinterpret_cast<float4*>(smem + S * STAGE);  // TILES per epilogue warp
+  float* svec = reinterpret_cast<float*>(smem + S * STAGE + TILES * EG * 4 * kStageFloats * 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nnt = (g.N + BN - 1) / BN, items = g.tile0[g.ntypes] * nnt;
   const int nchunk = (g.K + kKC - 1) / kKC;
@@ -406,14 +428,19 @@ fit_gemm_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   } else {
     // epilogue: warp group h takes the CTA's items j = h, h + EG, ...
     // (buffer j mod NB); thread = row (warp quadrant q = TMEM lanes 32 q ..)
-    float4* wst = stage_tiles + warp * (kStageFloats / 4);
+    float4* wst = stage_tiles + TILES * warp * (kStageFloats / 4);
+    float4* wst2 = TILES == 2 ? wst + kStageFloats / 4 : wst;
     switch (g.mode) {
-      case kFitFwd: fit_epilogue<kFitFwd, BN, EG, NB, kCols>(g, svec, wst, tbase, acc_full, acc_free, err); break;
-      case kFitFwdLast:
-        fit_epilogue<kFitFwdLast, BN, EG, NB, kCols>(g, svec, wst, tbase, acc_full, acc_free, err);
+      case kFitFwd:
+        fit_epilogue<kFitFwd, BN, EG, NB, kCols>(g, svec, wst, wst2, tbase, acc_full, acc_free, err);
         break;
-      case kFitBwd: fit_epilogue<kFitBwd, BN, EG, NB, kCols>(g, svec, wst, tbase, acc_full, acc_free, err); break;
-      default: fit_epilogue<kFitStore, BN, EG, NB, kCols>(g, svec, wst, tbase, acc_full, acc_free, err); break;
+      case kFitFwdLast:
+        fit_epilogue<kFitFwdLast, BN, EG, NB, kCols>(g, svec, wst, wst2, tbase, acc_full, acc_free, err);
+        break;
+      case kFitBwd:
+        fit_epilogue<kFitBwd, BN, EG, NB, kCols>(g, svec, wst, wst2, tbase, acc_full, acc_free, err);
+        break;
+      default: fit_epilogue<kFitStore, BN, EG, NB, kCols>(g, svec, wst, wst2, tbase, acc_full, acc_free, err); break;
     }
   }
   tc::fence_before();
@@ -672,61 +699,75 @@ int encode_bf16_2d(CUtensorMap* m, const __nv_bfloat16* base, int rows, int cols
 
 // epilogue shared memory next to the stages: the warps' staging tiles and
 // the per-type column vectors
-constexpr size_t epi_bytes(int EG, int ntypes, int N) {
-  return (size_t)EG * 4 * kStageFloats * 4 + (size_t)ntypes * 3 * N * 4;
+constexpr size_t epi_bytes(int EG, int tiles, int ntypes, int N) {
+  return (size_t)tiles * EG * 4 * kStageFloats * 4 + (size_t)ntypes * 3 * N * 4;
 }
 
 // stages of a BN-column tile: as many as fit next to each other and the
-// epilogue's shared memory (for up to two types of 256 columns) in about
-// 220 KB (2 .. 6)
+// epilogue's shared memory (one tile per warp, up to two types of 256
+// columns) in about 220 KB (2 .. 6)
 template <int BN, int NA, int EG>
 constexpr int fit_stages() {
   constexpr int stage = (NA * 128 + 2 * BN) * kKC * 2;
-  constexpr int s = (int)((220 * 1024 - epi_bytes(EG, 2, 256)) / stage);
+  constexpr int s = (int)((220 * 1024 - epi_bytes(EG, 1, 2, 256)) / stage);
   return s < 2 ? 2 : (s > 6 ? 6 : s);
 }
 
-template <int BN, int NA, int EG, int NB>
-int launch_t(const FitGemm& g, int* err, cudaStream_t st) {
+template <int BN, int NA, int EG, int NB, int TILES>
+int launch_tiles(const FitGemm& g, int* err, cudaStream_t st, size_t smem) {
   constexpr int S = fit_stages<BN, NA, EG>();
-  // + alignment slack; at least half of an SM's shared memory, so that one
-  // CTA (and its TMEM accumulators) sits on an SM
-  const size_t smem = std::max((size_t)S * (NA * 128 + 2 * BN) * kKC * 2 + 1024 + epi_bytes(EG, g.ntypes, g.N),
-                               (size_t)116 * 1024);
-  if (smem > 226 * 1024) return fail(DPGB_EINVAL, "fit_gemm: too many atom types for the staged epilogue");
   static size_t attr = 0;  // the largest dynamic shared memory requested so far
   if (attr < smem) {
-    DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel<BN, S, NA, EG, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
+    DPGB_CUDA(cudaFuncSetAttribute(fit_gemm_kernel<BN, S, NA, EG, NB, TILES>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = smem;
   }
-  if (g.Kp < g.K || g.Kp % kKC || (NA == 2) != (g.A_lo != nullptr))
-    return fail(DPGB_EINVAL, "fit_gemm: bad split-BF16 operands");
-  if (g.mode == kFitFwdLast && g.N > BN) return fail(DPGB_EINVAL, "fit_gemm: the output layer needs whole rows");
   CUtensorMap ta, talo, tb;
   DPGB_TRY(encode_bf16_2d(&ta, g.A, g.row0[g.ntypes], g.K, g.lda, 128));
   DPGB_TRY(encode_bf16_2d(&talo, g.A_lo ? g.A_lo : g.A, g.row0[g.ntypes], g.K, g.lda, 128));
   DPGB_TRY(encode_bf16_2d(&tb, g.B, g.ntypes * g.N, 2 * g.Kp, 2 * g.Kp, BN));
   const int items = g.tile0[g.ntypes] * ceil_div(g.N, BN);
-  fit_gemm_kernel<BN, S, NA, EG, NB><<<std::min(items, sm_count()), 128 * EG + 64, smem, st>>>(ta, talo, tb, g, err);
+  fit_gemm_kernel<BN, S, NA, EG, NB, TILES><<<std::min(items, sm_count()), 128 * EG + 64, smem, st>>>(ta, talo, tb,
+                                                                                                     g, err);
   return check_launch("fit_gemm");
+}
+
+template <int BN, int NA, int EG, int NB>
+int launch_t(const FitGemm& g, int* err, cudaStream_t st) {
+  constexpr int S = fit_stages<BN, NA, EG>();
+  if (g.Kp < g.K || g.Kp % kKC || (NA == 2) != (g.A_lo != nullptr))
+    return fail(DPGB_EINVAL, "fit_gemm: bad split-BF16 operands");
+  if (g.mode == kFitFwdLast && g.N > BN) return fail(DPGB_EINVAL, "fit_gemm: the output layer needs whole rows");
+  // + alignment slack; at least half of an SM's shared memory, so that one
+  // CTA (and its TMEM accumulators) sits on an SM.  Two staging tiles per
+  // epilogue warp where they fit (fewer exchanges per 16 columns), else one.
+  auto bytes = [&](int tiles) {
+    return std::max((size_t)S * (NA * 128 + 2 * BN) * kKC * 2 + 1024 + epi_bytes(EG, tiles, g.ntypes, g.N),
+                    (size_t)116 * 1024);
+  };
+  constexpr size_t kMax = 226 * 1024;
+  if (bytes(2) <= kMax) return launch_tiles<BN, NA, EG, NB, 2>(g, err, st, bytes(2));
+  if (bytes(1) <= kMax) return launch_tiles<BN, NA, EG, NB, 1>(g, err, st, bytes(1));
+  return fail(DPGB_EINVAL, "fit_gemm: too many atom types for the staged epilogue");
 }
 
 template <int NA>
 int launch_na(const FitGemm& g, int* err, cudaStream_t st) {
-  // Whole rows (the narrowest column tile that holds one; wider rows in
-  // tiles of 256, two accumulators) when they give every SM two items or
-  // more, so that an item's MMAs overlap another's epilogue; else narrower
-  // tiles (four accumulators) spread the rows' work over more SMs.  The
-  // output layer needs whole rows.
+  // Row tiles that give every SM two items or more: 128-column items in the
+  // forward hidden layers, whole rows (two accumulators) in the output
+  // layer and the backward; fewer: 80- (or 64-) column items spread the
+  // rows' work over more SMs.
   const int rows_tiles = g.tile0[g.ntypes];
-  const bool whole = g.mode == kFitFwdLast || (long long)rows_tiles * ceil_div(g.N, 256) >= 2LL * sm_count();
-  if (!whole) {
+  const bool enough = g.mode == kFitFwdLast || (long long)rows_tiles * ceil_div(g.N, 256) >= 2LL * sm_count();
+  if (!enough) {
     if (g.N % 80 == 0) return launch_t<80, NA, 2, 4>(g, err, st);
     return launch_t<64, NA, 2, 4>(g, err, st);
   }
   if (g.N <= 64) return launch_t<64, NA, 2, 4>(g, err, st);
-  if (g.N <= 128) return launch_t<128, NA, 2, 4>(g, err, st);
+  // the forward hidden layers: column tiles of 128 with four accumulators,
+  // so that the MMAs run ahead of both epilogue groups (measured faster
+  // there); the output layer and the backward keep whole rows
+  if (g.N <= 128 || g.mode == kFitFwd) return launch_t<128, NA, 2, 4>(g, err, st);
   if (g.N <= 240) return launch_t<240, NA, 2, 2>(g, err, st);
   return launch_t<256, NA, 2, 2>(g, err, st);
 }
