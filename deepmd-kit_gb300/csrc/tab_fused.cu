@@ -153,6 +153,7 @@ __device__ __forceinline__ void stage_rows_strided(float* dst, const float* __re
 // the lane's coefficients of interval ix: staged rows from shared memory,
 // the others from global memory
 // (ix is the same in every lane: the branch does not diverge)
+template <int J = kTabJ>
 __device__ __forceinline__ void load_coeffs(const float* s_tab, const float* __restrict__ tab, int rows, int ix,
                                             int ng, int lane, float (&a)[kTabJ][6]) {
   auto put = [&](int j, float2 x0, float2 x1, float2 x2) {
@@ -166,16 +167,22 @@ __device__ __forceinline__ void load_coeffs(const float* s_tab, const float* __r
   if (ix < rows) {
     const float2* q = reinterpret_cast<const float2*>(s_tab + (size_t)ix * 6 * ng + 6 * lane);
 #pragma unroll
-    for (int j = 0; j < kTabJ; ++j)
+    for (int j = 0; j < J; ++j)
       if (lane + 32 * j < ng) put(j, q[96 * j], q[96 * j + 1], q[96 * j + 2]);  // 32 neurons = 96 float2
   } else {
     const float2* q = reinterpret_cast<const float2*>(tab + (size_t)ix * 6 * ng + 6 * lane);
 #pragma unroll
-    for (int j = 0; j < kTabJ; ++j)
+    for (int j = 0; j < J; ++j)
       if (lane + 32 * j < ng) put(j, __ldg(q + 96 * j), __ldg(q + 96 * j + 1), __ldg(q + 96 * j + 2));
   }
 }
 
+// TG: 0, or the lane-group size (4 or 8) of the tail neurons 32 (kTabJ - 1)
+// .. ng - 1 (at most TG of them): those are not walked by the per-pair loop
+// (where all 32 lanes would step through them for the few lanes that hold
+// one) but afterwards, 32 / TG pairs at a time, TG lanes per pair, and
+// summed across the groups at the end of the atom's section.
+template <int TG>
 __global__ void __launch_bounds__(kFwdWarps * 32, 1)
 tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restrict__ chunks, int nchunks,
                const int* __restrict__ sorted_rows, int rows_cap, float* __restrict__ xyz, void* __restrict__ Dout,
@@ -220,8 +227,10 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             const int n = lane + 32 * j;
             acc[cc][j] = (sec > 0 && n < ng) ? xr[cc * ng + n] : 0.f;
           }
+        constexpr int J = TG ? kTabJ - 1 : kTabJ;  // neuron steps of the per-pair loop
         int cur = -1;
         float a[kTabJ][6] = {};  // lanes past ng keep zeros (a zero G adds nothing to the sums)
+        float tacc[4] = {0.f, 0.f, 0.f, 0.f};  // the lane's tail-neuron partial sums
         for (int base = p.sec[sec]; base < p.sec[sec + 1]; base += 32) {
           const int slot = base + lane;
           SlotEnv s;
@@ -235,49 +244,92 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
               eo[1] = make_float4(s.d[0], s.d[1], s.d[2], s.active ? 1.f : 0.f);
             }
           }
-          unsigned m = __ballot_sync(0xffffffffu, s.active);
+          const unsigned m = __ballot_sync(0xffffffffu, s.active);
           if (!m) continue;
-          if (s.active) {
+          const int cnt = __popc(m);
+          if (s.active) {  // the kept slots packed in lane order
             SlotBuf b;
             b.rn = make_float4(s.rn[0], s.rn[1], s.rn[2], s.rn[3]);
             b.xx = s.xx;
             b.delta = s.delta;
             b.idx = s.idx;
             b.pad = 0;
-            my[lane] = b;
+            my[__popc(m & ((1u << lane) - 1u))] = b;
           }
           __syncwarp();
-          while (m) {
-            const int src = __ffs(m) - 1;
-            m &= m - 1;
-            const SlotBuf b = my[src];
+          for (int k = 0; k < cnt; ++k) {
+            const SlotBuf b = my[k];
             if (b.idx != cur) {
               cur = b.idx;
-              load_coeffs(s_tab, tab, rows, cur, ng, lane, a);
+              load_coeffs<J>(s_tab, tab, rows, cur, ng, lane, a);
             }
-            float G[kTabJ];
+            float G[J];
             if (b.delta == 0.f) {  // inside the table (the same branch in every lane)
 #pragma unroll
-              for (int j = 0; j < kTabJ; ++j)
+              for (int j = 0; j < J; ++j)
                 G[j] = fmaf(fmaf(fmaf(fmaf(fmaf(a[j][5], b.xx, a[j][4]), b.xx, a[j][3]), b.xx, a[j][2]), b.xx,
                                  a[j][1]),
                             b.xx, a[j][0]);
             } else {  // linear extension past the ends of the table
 #pragma unroll
-              for (int j = 0; j < kTabJ; ++j) {
+              for (int j = 0; j < J; ++j) {
                 float Gp;
                 table_poly(a[j], b.xx, b.delta, G[j], Gp);
               }
             }
 #pragma unroll
-            for (int j = 0; j < kTabJ; ++j) {
+            for (int j = 0; j < J; ++j) {
               acc[0][j] = fmaf(b.rn.x, G[j], acc[0][j]);
               acc[1][j] = fmaf(b.rn.y, G[j], acc[1][j]);
               acc[2][j] = fmaf(b.rn.z, G[j], acc[2][j]);
               acc[3][j] = fmaf(b.rn.w, G[j], acc[3][j]);
             }
           }
+          if (TG) {  // the tail neurons: lane group k % (32 / TG) takes pair k, lane q of it neuron 32 J + q
+            const int q = lane % TG, n = 32 * J + q;
+            if (n < ng)
+              for (int k = lane / TG; k < cnt; k += 32 / (TG ? TG : 32)) {
+                const SlotBuf b = my[k];
+                const float2* c2 = reinterpret_cast<const float2*>(
+                    (b.idx < rows ? s_tab : tab) + (size_t)b.idx * 6 * ng + 6 * n);
+                float c6[6];
+                float2 x0, x1, x2;
+                if (b.idx < rows) {
+                  x0 = c2[0];
+                  x1 = c2[1];
+                  x2 = c2[2];
+                } else {
+                  x0 = __ldg(c2);
+                  x1 = __ldg(c2 + 1);
+                  x2 = __ldg(c2 + 2);
+                }
+                c6[0] = x0.x;
+                c6[1] = x0.y;
+                c6[2] = x1.x;
+                c6[3] = x1.y;
+                c6[4] = x2.x;
+                c6[5] = x2.y;
+                float G, Gp;
+                if (b.delta == 0.f)
+                  G = fmaf(fmaf(fmaf(fmaf(fmaf(c6[5], b.xx, c6[4]), b.xx, c6[3]), b.xx, c6[2]), b.xx, c6[1]), b.xx,
+                           c6[0]);
+                else
+                  table_poly(c6, b.xx, b.delta, G, Gp);
+                tacc[0] = fmaf(b.rn.x, G, tacc[0]);
+                tacc[1] = fmaf(b.rn.y, G, tacc[1]);
+                tacc[2] = fmaf(b.rn.z, G, tacc[2]);
+                tacc[3] = fmaf(b.rn.w, G, tacc[3]);
+              }
+          }
           __syncwarp();  // the slot buffer is refilled by the next 32 slots
+        }
+        if (TG) {  // sum the tail neurons' partials over the lane groups into lanes 0 .. TG - 1
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) {
+#pragma unroll
+            for (int o = TG; o < 32; o <<= 1) tacc[cc] += __shfl_xor_sync(0xffffffffu, tacc[cc], o);
+            if (lane < TG) acc[cc][kTabJ - 1] += tacc[cc];
+          }
         }
         if (!last) {
 #pragma unroll
@@ -684,9 +736,21 @@ int launch_tab_fwd(const DescParams<float>& p, const EmbParams<float>& e, const 
   if (nchunks <= 0) return DPGB_OK;
   size_t smem = 0;
   const int rows = tab_rows_cap(p.ng, kFwdWarps, &smem);
-  DPGB_CUDA(cudaFuncSetAttribute(tab_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  tab_fwd_kernel<<<std::min(nchunks, sm_count()), kFwdWarps * 32, smem, st>>>(p, e, chunks, nchunks, sorted_rows,
-                                                                               rows, xyz, D, d_bf16, queue, env_out);
+  // the neurons past the last full 32 go to the tail pass when there are at
+  // most 8 of them
+  const int tail = p.ng - 32 * (kTabJ - 1);
+  auto run = [&](auto kern) -> int {
+    DPGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<std::min(nchunks, sm_count()), kFwdWarps * 32, smem, st>>>(p, e, chunks, nchunks, sorted_rows, rows, xyz,
+                                                                        D, d_bf16, queue, env_out);
+    return DPGB_OK;
+  };
+  if (tail >= 1 && tail <= 4)
+    DPGB_TRY(run(tab_fwd_kernel<4>));
+  else if (tail >= 5 && tail <= 8)
+    DPGB_TRY(run(tab_fwd_kernel<8>));
+  else
+    DPGB_TRY(run(tab_fwd_kernel<0>));
   return check_launch("tab_fwd");
 }
 
