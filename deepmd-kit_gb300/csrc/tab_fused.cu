@@ -520,7 +520,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             // the two halves in turn (a row's repeats stay with it, a
             // broadcast); pairs with no staged row fill the free lanes.
             const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
-            const bool has = act && s.idx < rows;
+            const bool has = act && s.idx < rows && s.delta == 0.f;
             const int cls = (s.idx * bank_step) & 15;
             const unsigned m_row = __match_any_sync(full, has ? s.idx : -1 - lane);
             const int first = __ffs(m_row) - 1;
@@ -559,13 +559,15 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             mine_p = __shfl_sync(full, (int)mine, src) != 0;
           }
           // a pair whose interval's row is not staged (the closest
-          // neighbours) is walked by the whole warp below, so that the
-          // lane-per-pair loop reads shared memory only
-          const bool glob = act && s.idx >= rows;
+          // neighbours), or that lies past the ends of the table (linear
+          // extension), is walked by the whole warp below, so that the
+          // lane-per-pair loop reads shared memory only and evaluates the
+          // plain quintic
+          const bool glob = act && (s.idx >= rows || s.delta != 0.f);
           float dR[4] = {0.f, 0.f, 0.f, 0.f}, Pc[4] = {0.f, 0.f, 0.f, 0.f};
           if (act && !glob) {
             const float* rowc = s_tab + (size_t)s.idx * row_stride;
-            const float xx = s.xx, dl = s.delta;
+            const float xx = s.xx;
             // two neurons per step, each into its own partial sums (two
             // independent chains for the scheduler), added at the end
             float dR2[4] = {0.f, 0.f, 0.f, 0.f}, Pc2[4] = {0.f, 0.f, 0.f, 0.f};
@@ -583,7 +585,6 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
               G = fmaf(G, xx, x0.y);
               Gp = fmaf(Gp, xx, G);
               G = fmaf(G, xx, x0.x);
-              G = fmaf(Gp, dl, G);  // linear extension past the table ends (dl 0 inside)
               r[0] = fmaf(G, d.x, r[0]);
               r[1] = fmaf(G, d.y, r[1]);
               r[2] = fmaf(G, d.z, r[2]);
