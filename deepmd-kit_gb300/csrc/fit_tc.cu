@@ -631,10 +631,14 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
         float t1[4], xn[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          float sacc = 0.f;
+          // two interleaved chains of M / 2 (eight independent chains with c)
+          float s0 = 0.f, s1 = 0.f;
 #pragma unroll
-          for (int m = 0; m < M; ++m) sacc = fmaf(v[m], xm[c][m], sacc);
-          t1[c] = sacc;
+          for (int m = 0; m < M; m += 2) {
+            s0 = fmaf(v[m], xm[c][m], s0);
+            s1 = fmaf(v[m + 1], xm[c][m + 1], s1);
+          }
+          t1[c] = s0 + s1;
           xn[c] = xq[h][c];
         }
 #pragma unroll
