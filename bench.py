@@ -203,7 +203,7 @@ SMEM_TBS_NOMINAL = 152 * 128 * 2.07e9 / 1e12
 # 98,304-atom compressed step, from one ncu capture each: tab_fwd, tab_bwd
 # (profiles/tab_fused_water98304_compressed.md) and the fitting stage's six
 # launches summed (five fit_gemm + fit_dxyz, one dram-bytes pass)
-DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 1068.5e6, "desc_bwd": 765.9e6, "fitting": 2168.8e6}
+DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 1067.8e6, "desc_bwd": 766.6e6, "fitting": 2142.3e6}
 
 
 def table_roofline(per_step: dict, n_atoms: int, n_pairs: int, cfg) -> dict:
