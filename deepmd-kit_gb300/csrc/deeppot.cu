@@ -1157,9 +1157,12 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   // (a batch: when the tensor-core or table backward adds the gradients
   // itself, which finds each row's frame)
   const bool fused_bwd = std::is_same<T, float>::value && (dp.use_tc != 0 || dp.use_tab != 0);
-  const bool scatter = std::is_same<T, float>::value && !ext && !atom_virial && (own_geom || (batch && fused_bwd));
+  // (an external list: every explicit extended atom gets its force, as the
+  // transpose path gives it)
+  const bool scatter =
+      std::is_same<T, float>::value && !atom_virial && (own_geom || ((batch || ext) && fused_bwd));
   if (scatter) {
-    DPGB_TRY(dp.ws_facc.alloc(sizeof(unsigned long long) * 3 * nrows));
+    DPGB_TRY(dp.ws_facc.alloc(sizeof(unsigned long long) * 3 * nkeys));
   } else {
     DPGB_TRY(dp.ws_keys.alloc(sizeof(int) * npair));
     DPGB_TRY(dp.ws_tr.alloc(transpose_workspace(npair, (int)nkeys)));
@@ -1334,7 +1337,7 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
   dp.mark(DPGB_STAGE_TRANSPOSE, 0, ts);
   Transpose tr{};
   if (scatter) {
-    DPGB_CUDA(cudaMemsetAsync(dp.ws_facc.ptr, 0, sizeof(unsigned long long) * 3 * nrows, ts));
+    DPGB_CUDA(cudaMemsetAsync(dp.ws_facc.ptr, 0, sizeof(unsigned long long) * 3 * nkeys, ts));
   } else if (npair > 0) {
     // image-major indices fold onto their atom; explicit extended indices
     // are their own keys
@@ -1517,8 +1520,8 @@ int run(DeepPotImpl& dp, DevModel<T>& m, int nframes, int natom, const double* c
       DPGB_TRY(check_launch("force_scatter"));
       ++launches;
     }
-    force_fix_kernel<<<ceil_div(3 * nrows, 256), 256, 0, st>>>(force, dp.ws_facc.as<unsigned long long>(),
-                                                                (int)(3 * nrows));
+    force_fix_kernel<<<ceil_div(3 * nkeys, 256), 256, 0, st>>>(force, dp.ws_facc.as<unsigned long long>(),
+                                                                (int)(3 * nkeys));
     ++launches;
   } else if (ext) {
     if (atom_virial)

@@ -112,11 +112,13 @@ struct DescParams {
   unsigned long long* facc;
 };
 
-// The row whose force takes the neighbour's share of pair (row, nb): atom
-// nb mod (the frame's atom count) of the row's frame (image-major index nb;
-// a batch's frames are found from frame_atom_off).
+// The row whose force takes the neighbour's share of pair (row, nb): the
+// explicit extended atom nb with an external list (ghosts included), else
+// atom nb mod (the frame's atom count) of the row's frame (image-major index
+// nb; a batch's frames are found from frame_atom_off).
 template <typename T>
 __device__ __forceinline__ int neighbour_row(const DescParams<T>& p, int row, int nb) {
+  if (p.coord_ext) return nb;
   if (p.frame_atom_off) {
     const int f = frame_of(p.frame_atom_off, p.nframes_batch, row);
     const int beg = p.frame_atom_off[f];
