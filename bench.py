@@ -154,7 +154,7 @@ def _barrier(world):
 
 
 def algorithmic_flops(n_atoms: int, n_pairs: int, cfg) -> dict:
-    """FLOPs of one E+F+V step per stage (the survey's per-atom-step counts):
+    """FLOPs of one E+F+V step per stage (per pair and per atom):
     embedding 2*(25+25*50+50*100) per pair, G^T R~ 2*4*100 per pair, D
     2*100*4*16 per atom, fitting 2*(1600*240+2*240*240+240) per atom; the
     force pass repeats the input-gradient of each GEMM, the descriptor
