@@ -116,15 +116,22 @@ struct DescParams {
 // explicit extended atom nb with an external list (ghosts included), else
 // atom nb mod (the frame's atom count) of the row's frame (image-major index
 // nb; a batch's frames are found from frame_atom_off).
-template <typename T>
+// KEY: the list kind when known at compile time (kKeyModel, kKeyBatch,
+// kKeyExt), or kKeyAny to decide from p.
+enum { kKeyModel = 0, kKeyBatch = 1, kKeyExt = 2, kKeyAny = 3 };
+template <int KEY = kKeyAny, typename T>
 __device__ __forceinline__ int neighbour_row(const DescParams<T>& p, int row, int nb) {
-  if (p.coord_ext) return nb;
-  if (p.frame_atom_off) {
+  if (KEY == kKeyExt || (KEY == kKeyAny && p.coord_ext)) return nb;
+  if (KEY == kKeyBatch || (KEY == kKeyAny && p.frame_atom_off)) {
     const int f = frame_of(p.frame_atom_off, p.nframes_batch, row);
     const int beg = p.frame_atom_off[f];
     return beg + nb % (p.frame_atom_off[f + 1] - beg);
   }
   return p.nloc_div.div(row) * p.nloc + nb - p.nloc_div.div(nb) * p.nloc;
+}
+template <typename T>
+__host__ __device__ inline int list_key_kind(const DescParams<T>& p) {
+  return p.coord_ext ? kKeyExt : (p.frame_atom_off ? kKeyBatch : kKeyModel);
 }
 
 // r_nb - r_i in FP64 for neighbour nb of local atom i of frame f, and the

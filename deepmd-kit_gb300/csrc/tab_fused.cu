@@ -352,16 +352,22 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
         }
         // D[n][m] = sum_c X[c][n] X[c][m], m < M <= 32: X[c][m] sits in lane m
         if (M == 16) {  // the lane's row of D (16 values) as two or four 16-byte stores
+          // X[:][m < 16] (and the tail neurons' X) through the warp's slot
+          // buffer, read back as broadcasts
+          float4* xs = reinterpret_cast<float4*>(my);
+          __syncwarp();
+          if (lane < 16) xs[lane] = make_float4(acc[0][0], acc[1][0], acc[2][0], acc[3][0]);
+          if (TG && lane < TG)
+            xs[16 + lane] = make_float4(acc[0][kTabJ - 1], acc[1][kTabJ - 1], acc[2][kTabJ - 1], acc[3][kTabJ - 1]);
+          __syncwarp();
 #pragma unroll
-          for (int j = 0; j < kTabJ; ++j) {
+          for (int j = 0; j < J; ++j) {
             const int n = lane + 32 * j;
             float o[16];
 #pragma unroll
             for (int mm = 0; mm < 16; ++mm) {
-              float sacc = 0.f;
-#pragma unroll
-              for (int cc = 0; cc < 4; ++cc) sacc = fmaf(acc[cc][j], __shfl_sync(0xffffffffu, acc[cc][0], mm), sacc);
-              o[mm] = sacc;
+              const float4 x = xs[mm];
+              o[mm] = fmaf(acc[3][j], x.w, fmaf(acc[2][j], x.z, fmaf(acc[1][j], x.y, acc[0][j] * x.x)));
             }
             if (n >= ng) continue;
             const size_t at = (size_t)r * dim + (size_t)n * 16;
@@ -376,6 +382,20 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
               float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(Dout) + at);
 #pragma unroll
               for (int i = 0; i < 4; ++i) dst[i] = make_float4(o[4 * i], o[4 * i + 1], o[4 * i + 2], o[4 * i + 3]);
+            }
+          }
+          if (TG) {  // the tail neurons' rows of D: lane takes neuron 32 J + lane / 8, columns 2 (lane % 8), + 1
+            const int q = lane >> 3, mc = 2 * (lane & 7), n = 32 * J + q;
+            if (q < TG && n < ng) {
+              const float4 xn = xs[16 + q], a0 = xs[mc], a1 = xs[mc + 1];
+              const float o0 = fmaf(xn.w, a0.w, fmaf(xn.z, a0.z, fmaf(xn.y, a0.y, xn.x * a0.x)));
+              const float o1 = fmaf(xn.w, a1.w, fmaf(xn.z, a1.z, fmaf(xn.y, a1.y, xn.x * a1.x)));
+              const size_t at = (size_t)r * dim + (size_t)n * 16 + mc;
+              if (d_bf16)
+                *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<__nv_bfloat16*>(Dout) + at) =
+                    __floats2bfloat162_rn(o0, o1);
+              else
+                *reinterpret_cast<float2*>(reinterpret_cast<float*>(Dout) + at) = make_float2(o0, o1);
             }
           }
           continue;
@@ -421,6 +441,10 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
 // atom's dE/dxyz.  Everything is summed in the lane: no cross-lane
 // reductions.  Rows are staged with an odd float2 stride, so 16 lanes on 16
 // different rows read 16 different bank pairs.
+// KEY: the kind of list (kKeyModel, kKeyBatch, kKeyExt), fixed per
+// instantiation so that the fixed-point force atomics find the neighbour's
+// row without run-time branches
+template <int KEY>
 __global__ void __launch_bounds__(kBwdWarps * 32, 1)
 tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restrict__ chunks, int nchunks,
                const int* __restrict__ sorted_rows, int rows_cap, int row_stride, const float* __restrict__ dxyz,
@@ -678,7 +702,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             }
             if (p.facc) {
               if (act) {  // -g onto the neighbour's row
-                unsigned long long* a = p.facc + 3 * (size_t)neighbour_row(p, row, nl[slot_p]);
+                unsigned long long* a = p.facc + 3 * (size_t)neighbour_row<KEY>(p, row, nl[slot_p]);
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                   own[k] += g[k];
@@ -771,10 +795,20 @@ int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const 
   if ((size_t)optin <= fixed) return fail(DPGB_EINVAL, "tab_bwd: the neighbour list is too wide");
   const int rows = (int)(((size_t)optin - fixed) / ((size_t)row_stride * sizeof(float)));
   const size_t smem = ((size_t)rows * row_stride * 4 + 15) / 16 * 16 + (size_t)kBwdWarps * per_warp;
-  DPGB_CUDA(cudaFuncSetAttribute(tab_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  tab_bwd_kernel<<<std::min(nchunks, sm_count()), kBwdWarps * 32, smem, st>>>(p, e, chunks, nchunks, sorted_rows,
-                                                                               rows, row_stride, dxyz, gpair, vir_row,
-                                                                               queue, env_in);
+  auto run = [&](auto kern) -> int {
+    DPGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<std::min(nchunks, sm_count()), kBwdWarps * 32, smem, st>>>(p, e, chunks, nchunks, sorted_rows, rows,
+                                                                        row_stride, dxyz, gpair, vir_row, queue,
+                                                                        env_in);
+    return DPGB_OK;
+  };
+  const int kind = list_key_kind(p);
+  if (kind == kKeyExt)
+    DPGB_TRY(run(tab_bwd_kernel<kKeyExt>));
+  else if (kind == kKeyBatch)
+    DPGB_TRY(run(tab_bwd_kernel<kKeyBatch>));
+  else
+    DPGB_TRY(run(tab_bwd_kernel<kKeyModel>));
   return check_launch("tab_bwd");
 }
 
