@@ -441,9 +441,10 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
 // atom's dE/dxyz.  Everything is summed in the lane: no cross-lane
 // reductions.  Rows are staged with an odd float2 stride, so 16 lanes on 16
 // different rows read 16 different bank pairs.
-// KEY: the kind of list (kKeyModel, kKeyBatch, kKeyExt), fixed per
-// instantiation so that the fixed-point force atomics find the neighbour's
-// row without run-time branches
+// KEY: kKeyAny, or the kind of list (kKeyModel, kKeyBatch, kKeyExt) when
+// the pairs' environments come from the forward (env_in) and the forces go
+// to the fixed-point sums (p.facc): that case is compiled without the
+// other paths' branches, the neighbour's row found without run-time tests
 template <int KEY>
 __global__ void __launch_bounds__(kBwdWarps * 32, 1)
 tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restrict__ chunks, int nchunks,
@@ -497,7 +498,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
           const bool real = have && nl[slot] >= 0;
           const unsigned m = __ballot_sync(0xffffffffu, real);
           if (real) s_list[nreal + __popc(m & ((1u << lane) - 1u))] = slot;
-          if (have && !real && !p.facc) {
+          if (have && !real && !(KEY != kKeyAny || p.facc)) {
             gp_row[3 * slot] = 0.f;
             gp_row[3 * slot + 1] = 0.f;
             gp_row[3 * slot + 2] = 0.f;
@@ -517,7 +518,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
           SlotEnv s;
           s.active = 0;
           if (mine) {
-            if (env_in) {  // the environment the forward formed for this pair
+            if (KEY != kKeyAny || env_in) {  // the environment the forward formed for this pair
               const float4* ei = env_in + 2 * ((size_t)row * p.nnei + slot);
               const float4 a = __ldg(ei), b = __ldg(ei + 1);
               s.nb = 0;
@@ -700,9 +701,9 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
 #pragma unroll
                 for (int l = 0; l < 3; ++l) comp_add(vir_hi[3 * k + l], vir_lo[3 * k + l], -g[k] * s.d[l]);
             }
-            if (p.facc) {
+            if (KEY != kKeyAny || p.facc) {
               if (act) {  // -g onto the neighbour's row
-                unsigned long long* a = p.facc + 3 * (size_t)neighbour_row<KEY>(p, row, nl[slot_p]);
+                unsigned long long* a = p.facc + 3 * (size_t)neighbour_row<KEY == kKeyAny ? kKeyAny : KEY>(p, row, nl[slot_p]);
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                   own[k] += g[k];
@@ -716,7 +717,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             }
           }
         }
-        if (p.facc) {
+        if (KEY != kKeyAny || p.facc) {
 #pragma unroll
           for (int k = 0; k < 3; ++k) own[k] = warp_sum(own[k]);
           if (lane == 0)
@@ -803,7 +804,9 @@ int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const 
     return DPGB_OK;
   };
   const int kind = list_key_kind(p);
-  if (kind == kKeyExt)
+  if (!env_in || !p.facc)
+    DPGB_TRY(run(tab_bwd_kernel<kKeyAny>));
+  else if (kind == kKeyExt)
     DPGB_TRY(run(tab_bwd_kernel<kKeyExt>));
   else if (kind == kKeyBatch)
     DPGB_TRY(run(tab_bwd_kernel<kKeyBatch>));
