@@ -570,13 +570,15 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
   const int row = valid ? f.sorted_rows[m0 + r] : 0;
   const float* xr = f.xyz + (size_t)row * 4 * f.ng;
   float4* out = reinterpret_cast<float4*>(f.dxyz + (size_t)row * 4 * f.ng);
-  float xm[4][M], T2[4][M];
+  // neurons m < 16 in (even, odd) pairs, for the packed FP32 FMA (two IEEE
+  // fmaf results per instruction)
+  float2 xm[4][M / 2], T2[4][M / 2];
 #pragma unroll
   for (int c = 0; c < 4; ++c)
 #pragma unroll
-    for (int m = 0; m < M; ++m) {
-      xm[c][m] = valid ? xr[c * f.ng + m] : 0.f;
-      T2[c][m] = 0.f;
+    for (int k = 0; k < M / 2; ++k) {
+      xm[c][k] = valid ? make_float2(xr[c * f.ng + 2 * k], xr[c * f.ng + 2 * k + 1]) : make_float2(0.f, 0.f);
+      T2[c][k] = make_float2(0.f, 0.f);
     }
   const float inv = 1.f / (float)f.nnei;
   constexpr int NH = kDxBN / M;  // neurons per chunk
@@ -628,23 +630,24 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
         tc::tmem_ld16(tc::taddr(tbase + (uint32_t)(b * kDxBN), (warp & 3) * 32, q * M), v);
         tc::tmem_ld_wait();
         if (!valid) continue;
-        float t1[4], xn[4];
+        float2 v2[M / 2];
+#pragma unroll
+        for (int k = 0; k < M / 2; ++k) v2[k] = make_float2(v[2 * k], v[2 * k + 1]);
+        float t1[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          // two interleaved chains of M / 2 (eight independent chains with c)
-          float s0 = 0.f, s1 = 0.f;
+          // two interleaved chains of M / 2, even and odd m (eight independent chains with c)
+          float2 s01 = make_float2(0.f, 0.f);
 #pragma unroll
-          for (int m = 0; m < M; m += 2) {
-            s0 = fmaf(v[m], xm[c][m], s0);
-            s1 = fmaf(v[m + 1], xm[c][m + 1], s1);
-          }
-          t1[c] = s0 + s1;
-          xn[c] = xq[h][c];
+          for (int k = 0; k < M / 2; ++k) s01 = __ffma2_rn(v2[k], xm[c][k], s01);
+          t1[c] = s01.x + s01.y;
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
+        for (int c = 0; c < 4; ++c) {
+          const float2 xn = make_float2(xq[h][c], xq[h][c]);
 #pragma unroll
-          for (int m = 0; m < M; ++m) T2[c][m] = fmaf(v[m], xn[c], T2[c][m]);
+          for (int k = 0; k < M / 2; ++k) T2[c][k] = __ffma2_rn(v2[k], xn, T2[c][k]);
+        }
         if (n < M)  // completed with the transposed term below
           out[n] = make_float4(t1[0], t1[1], t1[2], t1[3]);
         else
@@ -662,8 +665,8 @@ fit_dxyz_kernel(const __grid_constant__ CUtensorMap tma_a, const __grid_constant
 #pragma unroll
     for (int m = 0; m < M; ++m) {
       const float4 a = out[m];
-      out[m] = make_float4((a.x + T2[0][m]) * inv, (a.y + T2[1][m]) * inv, (a.z + T2[2][m]) * inv,
-                           (a.w + T2[3][m]) * inv);
+      auto t2 = [&](int c) { return (m & 1) ? T2[c][m >> 1].y : T2[c][m >> 1].x; };
+      out[m] = make_float4((a.x + t2(0)) * inv, (a.y + t2(1)) * inv, (a.z + t2(2)) * inv, (a.w + t2(3)) * inv);
     }
   tc::fence_before();
   __syncthreads();

@@ -1535,6 +1535,7 @@ skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int nc
   int* wt = s_t[warp];
   const unsigned below = (1u << lane) - 1u;
   int nc = 0;
+#pragma unroll 2
   for (int p0 = 0; p0 < ncand; p0 += 32) {
     const int p = p0 + lane;
     const int e = p < ncand ? c[p] : -1;
@@ -1562,6 +1563,7 @@ skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int nc
   const float rin = (float)rcut - eps, rout = (float)rcut + eps;
   int n = 0;
   bool band = false;
+#pragma unroll 2
   for (int k0 = 0; k0 < nc; k0 += 32) {
     const int k = k0 + lane;
     bool keep = false;

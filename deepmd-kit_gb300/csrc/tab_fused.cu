@@ -45,9 +45,10 @@ __device__ __forceinline__ float switch_f(float nr, float rmin, float rmax, floa
 }
 
 // environment of one slot (the same arithmetic as the tensor-core path)
-__device__ __forceinline__ void slot_env(const DescParams<float>& p, int row, int ti, int slot, SlotEnv& s) {
+// whose list entry nb the caller has read already
+__device__ __forceinline__ void slot_env(const DescParams<float>& p, int row, int ti, int slot, int nb, SlotEnv& s) {
   const int f = p.nloc_div.div(row), i = row - f * p.nloc;
-  s.nb = p.nlist[(size_t)row * p.nnei + slot];
+  s.nb = nb;
   const float* av = p.davg + ((size_t)ti * p.nnei + slot) * 4;
   const float* sdi = p.dstd_inv + ((size_t)ti * p.nnei + slot) * 4;
   float e4[4] = {0.f, 0.f, 0.f, 0.f};
@@ -74,6 +75,9 @@ __device__ __forceinline__ void slot_env(const DescParams<float>& p, int row, in
 #pragma unroll
   for (int c = 0; c < 4; ++c) s.rn[c] = (s.nb >= 0 && !keep) ? 0.f : (e4[c] - av[c]) * sdi[c];
   s.active = s.nb >= 0 ? keep : !p.pad_zero;
+}
+__device__ __forceinline__ void slot_env(const DescParams<float>& p, int row, int ti, int slot, SlotEnv& s) {
+  slot_env(p, row, ti, slot, p.nlist[(size_t)row * p.nnei + slot], s);
 }
 
 // d e / d r_centre of a kept pair (source/lib/src/env_mat.cc:156-216), FP32
@@ -137,17 +141,28 @@ __device__ __forceinline__ void stage_rows(float* dst, const float* __restrict__
   for (int q = threadIdx.x; q < n2; q += blockDim.x) d2[q] = __ldg(s2 + q);
 }
 
-// the same with a row stride of row_stride floats (even; rows of 6 ng floats)
-__device__ __forceinline__ void stage_rows_strided(float* dst, const float* __restrict__ src, int rows, int ng,
-                                                   int row_stride) {
-  const int per = 3 * ng;  // float2 per row
-  const float2* s2 = reinterpret_cast<const float2*>(src);
+// the same with a row stride of row_stride floats (even) and the neurons
+// interleaved in pairs: float2 6 m + c of a staged row holds coefficient c
+// of neurons 2 m and 2 m + 1 (a neuron past ng reads as zeros), so that one
+// packed FMA evaluates both neurons
+__device__ __forceinline__ void stage_rows_paired(float* dst, const float* __restrict__ src, int rows, int ng,
+                                                  int row_stride) {
+  const int per = 3 * ((ng + 1) & ~1);  // float2 per staged row
   float2* d2 = reinterpret_cast<float2*>(dst);
   const int s2stride = row_stride / 2;
   for (int q = threadIdx.x; q < rows * per; q += blockDim.x) {
     const int rr = q / per, k = q - rr * per;
-    d2[(size_t)rr * s2stride + k] = __ldg(s2 + q);
+    const int m = k / 6, c = k - 6 * m, n = 2 * m;
+    const float* row = src + (size_t)rr * 6 * ng;
+    d2[(size_t)rr * s2stride + k] = make_float2(__ldg(row + 6 * n + c), n + 1 < ng ? __ldg(row + 6 * n + 6 + c) : 0.f);
   }
+}
+
+// component c of dX[n] in the paired copy of an atom's dE/dxyz: float4
+// 2 m holds (x, y) and 2 m + 1 holds (z, w) of neurons 2 m and 2 m + 1,
+// each as a (neuron 2 m, neuron 2 m + 1) pair
+__device__ __forceinline__ float paired_dx(const float4* s_dx, int n, int c) {
+  return reinterpret_cast<const float*>(s_dx)[(n >> 1) * 8 + 2 * c + (n & 1)];
 }
 
 // the lane's coefficients of interval ix: staged rows from shared memory,
@@ -231,12 +246,16 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
         int cur = -1;
         float a[kTabJ][6] = {};  // lanes past ng keep zeros (a zero G adds nothing to the sums)
         float tacc[4] = {0.f, 0.f, 0.f, 0.f};  // the lane's tail-neuron partial sums
+        const int* nlr = p.nlist + (size_t)row * p.nnei;
+        int nb_next = p.sec[sec] + lane < p.sec[sec + 1] ? nlr[p.sec[sec] + lane] : -1;
         for (int base = p.sec[sec]; base < p.sec[sec + 1]; base += 32) {
           const int slot = base + lane;
+          const int nb_cur = nb_next;
+          nb_next = slot + 32 < p.sec[sec + 1] ? nlr[slot + 32] : -1;  // the next batch's entry, loaded ahead
           SlotEnv s;
           s.active = 0;
           if (slot < p.sec[sec + 1]) {
-            slot_env(p, row, ti, slot, s);
+            slot_env(p, row, ti, slot, nb_cur, s);
             table_locate(tm, s.rn[0], s.idx, s.xx, s.delta);
             if (env_out && s.nb >= 0) {  // the pair's environment, for the backward
               float4* eo = env_out + 2 * ((size_t)row * p.nnei + slot);
@@ -257,6 +276,7 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             my[__popc(m & ((1u << lane) - 1u))] = b;
           }
           __syncwarp();
+#pragma unroll 2
           for (int k = 0; k < cnt; ++k) {
             const SlotBuf b = my[k];
             if (b.idx != cur) {
@@ -440,7 +460,10 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
 // (ds = sum_c R~[c] P[c]) with dX[n] broadcast from the warp's copy of the
 // atom's dE/dxyz.  Everything is summed in the lane: no cross-lane
 // reductions.  Rows are staged with an odd float2 stride, so 16 lanes on 16
-// different rows read 16 different bank pairs.
+// different rows read 16 different bank pairs, and with the neurons
+// interleaved in pairs (as is the copy of dE/dxyz): the two neurons of a
+// pair go through the packed FP32 FMA together (two IEEE fmaf results per
+// instruction), even neurons into one partial sum and odd ones into another.
 // KEY: kKeyAny, or the kind of list (kKeyModel, kKeyBatch, kKeyExt) when
 // the pairs' environments come from the forward (env_in) and the forces go
 // to the fixed-point sums (p.facc): that case is compiled without the
@@ -456,10 +479,11 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
   float* s_tab = reinterpret_cast<float*>(smem4);
   unsigned char* tail = reinterpret_cast<unsigned char*>(smem4) + (((size_t)rows_cap * row_stride * 4 + 15) / 16 * 16);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float4* s_dx = reinterpret_cast<float4*>(tail) + (size_t)warp * ng;                    // [warp][ng]
-  int* s_list = reinterpret_cast<int*>(reinterpret_cast<float4*>(tail) + (size_t)kBwdWarps * ng) +
+  const int ng2 = (ng + 1) & ~1;                                                          // even
+  float4* s_dx = reinterpret_cast<float4*>(tail) + (size_t)warp * ng2;                   // [warp][ng2], paired
+  int* s_list = reinterpret_cast<int*>(reinterpret_cast<float4*>(tail) + (size_t)kBwdWarps * ng2) +
                 (size_t)warp * p.nnei;                                                     // [warp][nnei]
-  int* s_perm = reinterpret_cast<int*>(reinterpret_cast<float4*>(tail) + (size_t)kBwdWarps * ng) +
+  int* s_perm = reinterpret_cast<int*>(reinterpret_cast<float4*>(tail) + (size_t)kBwdWarps * ng2) +
                 (size_t)kBwdWarps * p.nnei + warp * 32;                                    // [warp][32]
   const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
   const int bank_step = (row_stride / 2) & 15;  // a row's 8-byte bank pair advances by this per row
@@ -473,7 +497,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
       const float* tab = e.table + tm.offset;
       const int rows = min(rows_cap, tm.hi_idx + 1);
       __syncthreads();
-      stage_rows_strided(s_tab, tab, rows, ng, row_stride);
+      stage_rows_paired(s_tab, tab, rows, ng, row_stride);
       __syncthreads();
       for (int r = ch.row0 + warp; r < ch.row1; r += kBwdWarps) {
         const int row = sorted_rows[r];
@@ -489,8 +513,13 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
           if (env_in && p.sec[sec] + lane < p.sec[sec + 1])
             prefetch_l2(env_in + 2 * ((size_t)nrow * p.nnei + p.sec[sec] + lane));
         }
-        // the atom's dE/dxyz (dxyz is [row][ng][4]) and the section's real slots
-        for (int n = lane; n < ng; n += 32) s_dx[n] = reinterpret_cast<const float4*>(dxyz + (size_t)row * 4 * ng)[n];
+        // the atom's dE/dxyz (dxyz is [row][ng][4]), paired, and the section's real slots
+        for (int m = lane; 2 * m < ng; m += 32) {
+          const float4* src = reinterpret_cast<const float4*>(dxyz + (size_t)row * 4 * ng) + 2 * m;
+          const float4 a = src[0], b = 2 * m + 1 < ng ? src[1] : make_float4(0.f, 0.f, 0.f, 0.f);
+          s_dx[2 * m] = make_float4(a.x, b.x, a.y, b.y);
+          s_dx[2 * m + 1] = make_float4(a.z, b.z, a.w, b.w);
+        }
         int nreal = 0;
         for (int base = p.sec[sec]; base < p.sec[sec + 1]; base += 32) {
           const int slot = base + lane;
@@ -591,45 +620,40 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
           const bool glob = act && (s.idx >= rows || s.delta != 0.f);
           float dR[4] = {0.f, 0.f, 0.f, 0.f}, Pc[4] = {0.f, 0.f, 0.f, 0.f};
           if (act && !glob) {
-            const float* rowc = s_tab + (size_t)s.idx * row_stride;
-            const float xx = s.xx;
-            // two neurons per step, each into its own partial sums (two
-            // independent chains for the scheduler), added at the end
-            float dR2[4] = {0.f, 0.f, 0.f, 0.f}, Pc2[4] = {0.f, 0.f, 0.f, 0.f};
-            auto neuron = [&](int n, float (&r)[4], float (&pc)[4]) {
-              const float2* q = reinterpret_cast<const float2*>(rowc + 6 * n);
-              const float2 x0 = q[0], x1 = q[1], x2 = q[2];
-              const float4 d = s_dx[n];
+            const float2* rowc = reinterpret_cast<const float2*>(s_tab + (size_t)s.idx * row_stride);
+            const float2 xx = make_float2(s.xx, s.xx);
+            // neurons 2 m (.x) and 2 m + 1 (.y) per step, even and odd
+            // neurons into their own partial sums, added at the end
+            float2 r2[4], pc2[4];
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) r2[cc] = pc2[cc] = make_float2(0.f, 0.f);
+#pragma unroll 8
+            for (int m = 0; 2 * m < ng; ++m) {
+              const float2* q = rowc + 6 * m;  // coefficient c of both neurons
+              const float2 c0 = q[0], c1 = q[1], c2 = q[2], c3 = q[3], c4 = q[4], c5 = q[5];
+              const float4 dxy = s_dx[2 * m], dzw = s_dx[2 * m + 1];
               // value and derivative of the quintic in one Horner pass
-              float G = fmaf(x2.y, xx, x2.x), Gp = x2.y;
-              Gp = fmaf(Gp, xx, G);
-              G = fmaf(G, xx, x1.y);
-              Gp = fmaf(Gp, xx, G);
-              G = fmaf(G, xx, x1.x);
-              Gp = fmaf(Gp, xx, G);
-              G = fmaf(G, xx, x0.y);
-              Gp = fmaf(Gp, xx, G);
-              G = fmaf(G, xx, x0.x);
-              r[0] = fmaf(G, d.x, r[0]);
-              r[1] = fmaf(G, d.y, r[1]);
-              r[2] = fmaf(G, d.z, r[2]);
-              r[3] = fmaf(G, d.w, r[3]);
-              pc[0] = fmaf(Gp, d.x, pc[0]);
-              pc[1] = fmaf(Gp, d.y, pc[1]);
-              pc[2] = fmaf(Gp, d.z, pc[2]);
-              pc[3] = fmaf(Gp, d.w, pc[3]);
-            };
-            int n = 0;
-#pragma unroll 2
-            for (; n + 1 < ng; n += 2) {
-              neuron(n, dR, Pc);
-              neuron(n + 1, dR2, Pc2);
+              float2 G = __ffma2_rn(c5, xx, c4), Gp = c5;
+              Gp = __ffma2_rn(Gp, xx, G);
+              G = __ffma2_rn(G, xx, c3);
+              Gp = __ffma2_rn(Gp, xx, G);
+              G = __ffma2_rn(G, xx, c2);
+              Gp = __ffma2_rn(Gp, xx, G);
+              G = __ffma2_rn(G, xx, c1);
+              Gp = __ffma2_rn(Gp, xx, G);
+              G = __ffma2_rn(G, xx, c0);
+              const float2 d[4] = {make_float2(dxy.x, dxy.y), make_float2(dxy.z, dxy.w), make_float2(dzw.x, dzw.y),
+                                   make_float2(dzw.z, dzw.w)};
+#pragma unroll
+              for (int cc = 0; cc < 4; ++cc) {
+                r2[cc] = __ffma2_rn(G, d[cc], r2[cc]);
+                pc2[cc] = __ffma2_rn(Gp, d[cc], pc2[cc]);
+              }
             }
-            if (n < ng) neuron(n, dR, Pc);
 #pragma unroll
             for (int cc = 0; cc < 4; ++cc) {
-              dR[cc] += dR2[cc];
-              Pc[cc] += Pc2[cc];
+              dR[cc] = r2[cc].x + r2[cc].y;
+              Pc[cc] = pc2[cc].x + pc2[cc].y;
             }
           }
           // rows in global memory: lane l takes neurons l, l + 32, ... of
@@ -647,7 +671,8 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
               const int n = lane + 32 * j;
               if (n < ng) {
                 const float2 x0 = __ldg(grow + 3 * n), x1 = __ldg(grow + 3 * n + 1), x2 = __ldg(grow + 3 * n + 2);
-                const float4 d = s_dx[n];
+                const float4 d = make_float4(paired_dx(s_dx, n, 0), paired_dx(s_dx, n, 1), paired_dx(s_dx, n, 2),
+                                             paired_dx(s_dx, n, 3));
                 float G = fmaf(x2.y, gx, x2.x), Gp = x2.y;
                 Gp = fmaf(Gp, gx, G);
                 G = fmaf(G, gx, x1.y);
@@ -784,14 +809,16 @@ int launch_tab_bwd(const DescParams<float>& p, const EmbParams<float>& e, const 
                    const int* sorted_rows, const float* dxyz, float* gpair, double* vir_row, cudaStream_t st,
                    int* queue, const float4* env_in) {
   if (nchunks <= 0) return DPGB_OK;
-  // rows at an odd float2 stride; per warp the atom's dE/dxyz and its slot list
-  int per2 = 3 * p.ng;
+  // rows (neurons paired, ng rounded up to even) at an odd float2 stride;
+  // per warp the atom's dE/dxyz (paired) and its slot list
+  const int ng2 = (p.ng + 1) & ~1;
+  int per2 = 3 * ng2;
   if (per2 % 2 == 0) ++per2;
   const int row_stride = 2 * per2;
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t per_warp = (size_t)p.ng * sizeof(float4) + (size_t)p.nnei * sizeof(int) + 32 * sizeof(int);
+  const size_t per_warp = (size_t)ng2 * sizeof(float4) + (size_t)p.nnei * sizeof(int) + 32 * sizeof(int);
   const size_t fixed = (size_t)kBwdWarps * per_warp + 16 + 1024;
   if ((size_t)optin <= fixed) return fail(DPGB_EINVAL, "tab_bwd: the neighbour list is too wide");
   const int rows = (int)(((size_t)optin - fixed) / ((size_t)row_stride * sizeof(float)));
