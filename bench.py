@@ -200,10 +200,10 @@ FP32_SIMT_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12
 SMEM_TBS_NOMINAL = 152 * 128 * 2.07e9 / 1e12
 
 # DRAM bytes (read + write) per launch of the dominant kernels of the
-# 98,304-atom compressed step, from one ncu capture each: tab_fwd, tab_bwd
-# (profiles/tab_fused_water98304_compressed.md) and the fitting stage's six
-# launches summed (five fit_gemm + fit_dxyz, one dram-bytes pass)
-DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 1067.8e6, "desc_bwd": 766.6e6, "fitting": 2142.3e6}
+# 98,304-atom compressed step, from one ncu dram-bytes pass over one
+# evaluation: tab_fwd, tab_bwd and the fitting stage's six launches summed
+# (five fit_gemm + fit_dxyz)
+DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 1068.1e6, "desc_bwd": 765.6e6, "fitting": 2143.4e6}
 
 
 def table_roofline(per_step: dict, n_atoms: int, n_pairs: int, cfg) -> dict:
