@@ -413,7 +413,7 @@ nlist_pt_kernel(int* __restrict__ nlist, const double* __restrict__ coord,
 // nlist_pt_kernel.
 constexpr int kCellWarps = 8;   // warps of nlist_cell_kernel (four CTAs, 32 warps per SM)
 constexpr int kBatchWarps = 4;  // warps of nlist_cell_batch_kernel
-constexpr int kKeptCap = 512;  // per-warp kept pairs of the skin selection
+constexpr int kKeptCap = 512;  // per-warp kept pairs of the skin selection (at most)
 // Shared memory of the staged kernels: stage_cap stencil atoms (3 floats, 2
 // ints) and, for typed lists, kept_cap pairs per warp (a double key, 2 ints).
 // Typed lists stage 1536 atoms and keep 192 pairs per warp (55 KB: four
@@ -1509,15 +1509,18 @@ __global__ void skin_coords_kernel(double* __restrict__ out, float4* __restrict_
 // is that of a fresh build on the same coordinates.
 constexpr int kSkinWarps = 4;
 
-__global__ void __launch_bounds__(kSkinWarps * 32)
-skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int ncand, const double* __restrict__ coord,
+// kept_cap: the per-warp kept-pair capacity of the dynamic shared memory
+// (the candidate width rounded up to 32, at least 128, at most kKeptCap:
+// the kept pairs cannot outnumber the candidates), so that more warps fit
+// on an SM when the candidate rows are narrow
+__global__ void __launch_bounds__(kSkinWarps * 32, 8)
+skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int ncand, int kept_cap,
+                   const double* __restrict__ coord,
                    const float4* __restrict__ coordf, const float4* __restrict__ coordflo,
                    const int* __restrict__ atype, const double* __restrict__ svec, const float4* __restrict__ svecf,
                    const float4* __restrict__ svecflo, int nloc, FastDiv by_nloc, double rcut, float rcf2, float eps,
                    SelInfo sel, int* __restrict__ status) {
-  __shared__ double s_r[kSkinWarps][kKeptCap];
-  __shared__ int s_i[kSkinWarps][kKeptCap];
-  __shared__ int s_t[kSkinWarps][kKeptCap];
+  extern __shared__ double s_kept[];  // [warp][kept_cap] distances, then indices, then types
   __shared__ int s_tb[kSkinWarps][DPGB_MAX_TYPES];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kSkinWarps + warp;
@@ -1529,10 +1532,10 @@ skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int nc
   const double xi = coord[3 * i], yi = coord[3 * i + 1], zi = coord[3 * i + 2];
   const float4 fi = coordf[i], fil = coordflo[i];
   const int* c = cand + (size_t)i * ncand;
-  double* wr = s_r[warp];
+  double* wr = s_kept + (size_t)warp * kept_cap;
   float* wf = reinterpret_cast<float*>(wr);
-  int* wi = s_i[warp];
-  int* wt = s_t[warp];
+  int* wi = reinterpret_cast<int*>(s_kept + (size_t)kSkinWarps * kept_cap) + (size_t)warp * kept_cap;
+  int* wt = wi + (size_t)kSkinWarps * kept_cap;
   const unsigned below = (1u << lane) - 1u;
   int nc = 0;
 #pragma unroll 2
@@ -1549,10 +1552,10 @@ skin_select_kernel(int* __restrict__ nlist, const int* __restrict__ cand, int nc
     }
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     const int pos = nc + __popc(m & below);
-    if (keep && pos < kKeptCap) wi[pos] = e;
+    if (keep && pos < kept_cap) wi[pos] = e;
     nc += __popc(m);
   }
-  if (nc > kKeptCap) {
+  if (nc > kept_cap) {
     if (lane == 0) {
       atomicMax(&status[kStatusOverflow], nc);
       atomicMax(&status[kStatusOverflowAtom], i + 1);
@@ -1685,9 +1688,11 @@ int launch_skin_select(int* nlist, const int* cand, int ncand, const double* coo
   // displacement: the exact one rounded to FP32 (<= 2^-24 r, plus ~2^-48 of
   // the coordinates' magnitude), FP32 norm (<= 2^-22 r), x1.5
   const float eps = (float)(rcut * 1.5 * (0x1p-24 + 0x1p-22) + 1e-7);
-  skin_select_kernel<<<ceil_div(nloc, kSkinWarps), kSkinWarps * 32, 0, st>>>(
-      nlist, cand, ncand, coord, coordf, coordflo, atype, svec, svecf, svecflo, nloc, FastDiv(nloc), rcut, rcf * rcf,
-      eps, sel, status);
+  const int kept_cap = std::max(128, std::min(kKeptCap, (ncand + 31) / 32 * 32));
+  const size_t smem = (size_t)kSkinWarps * kept_cap * (sizeof(double) + 2 * sizeof(int));  // <= 32 KB
+  skin_select_kernel<<<ceil_div(nloc, kSkinWarps), kSkinWarps * 32, smem, st>>>(
+      nlist, cand, ncand, kept_cap, coord, coordf, coordflo, atype, svec, svecf, svecflo, nloc, FastDiv(nloc), rcut,
+      rcf * rcf, eps, sel, status);
   return check_launch("skin_select");
 }
 
