@@ -971,13 +971,17 @@ int prepare_types(DeepPotImpl& dp, int nframes, int natom, const int* atype_host
   // centre type.  The embedding kernels run one CTA per chunk with three
   // CTAs per SM, so the rows are cut into at most 3 x SMs chunks of
   // near-equal size (a CTA that had to take a second chunk would double the
-  // launch).
+  // launch).  The table kernels (compressed nets) run one persistent CTA
+  // per SM that stages each section's table rows for a chunk behind a
+  // barrier, where its warps wait for the slowest: they take SMs chunks,
+  // one per CTA (three per CTA had cost 0.2 ms of barrier waits in the
+  // 98,304-atom step).
   std::vector<WorkChunk> chunks;
   {
     int dev = 0, nsm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int slots = std::max(1, 3 * nsm);
+    const int slots = std::max(1, (dp.use_tab && !plan ? 1 : 3) * nsm);
     std::vector<int> per(nt, 0);
     std::vector<double> rem(nt, 0.0);
     int used = 0;
