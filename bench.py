@@ -203,7 +203,7 @@ SMEM_TBS_NOMINAL = 152 * 128 * 2.07e9 / 1e12
 # 98,304-atom compressed step, from one ncu dram-bytes pass over one
 # evaluation: tab_fwd, tab_bwd and the fitting stage's six launches summed
 # (five fit_gemm + fit_dxyz)
-DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 1068.1e6, "desc_bwd": 765.6e6, "fitting": 2143.4e6}
+DRAM_BYTES_PER_LAUNCH_98K = {"desc_fwd": 1089.6e6, "desc_bwd": 772.0e6, "fitting": 2143.0e6}
 
 
 def table_roofline(per_step: dict, n_atoms: int, n_pairs: int, cfg) -> dict:
