@@ -192,6 +192,22 @@ __device__ __forceinline__ void load_coeffs(const float* s_tab, const float* __r
   }
 }
 
+// The warps of a CTA take a chunk's atoms from a shared counter: warp w
+// starts with atoms row0 + w and row0 + W + w, and each atom it finishes
+// hands it the next one from the counter, so that it knows its next atom
+// one ahead (for the prefetches) and the warps reach the section's barrier
+// within about one atom of each other.  An atom's sums run in one warp in a
+// fixed order, whichever warp takes it: results do not depend on the
+// assignment.
+__device__ __forceinline__ int take_atom(int* s_next, int& r_next, int lane) {
+  int g = 0;
+  if (lane == 0) g = atomicAdd(s_next, 1);
+  g = __shfl_sync(0xffffffffu, g, 0);
+  const int r = r_next;
+  r_next = g;
+  return r;
+}
+
 // TG: 0, or the lane-group size (4 or 8) of the tail neurons 32 (kTabJ - 1)
 // .. ng - 1 (at most TG of them): those are not walked by the per-pair loop
 // (where all 32 lanes would step through them for the few lanes that hold
@@ -210,7 +226,7 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
   SlotBuf* my = s_slot + warp * 32;
   const float inv = 1.f / (float)p.nnei;
   const int dim = ng * M;
-  __shared__ int s_work;
+  __shared__ int s_work, s_next;
   for (int c = work_first(queue, &s_work); c < nchunks; c = work_next(queue, c, &s_work)) {
     const WorkChunk ch = chunks[c];
     const int ti = ch.ti;
@@ -221,15 +237,17 @@ tab_fwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
       const int rows = min(rows_cap, tm.hi_idx + 1);
       __syncthreads();  // the previous section's rows are no longer read
       stage_rows(s_tab, tab, rows, ng);
+      if (threadIdx.x == 0) s_next = ch.row0 + 2 * kFwdWarps;
       __syncthreads();
       const bool last = sec == p.ntypes - 1;
-      for (int r = ch.row0 + warp; r < ch.row1; r += kFwdWarps) {
+      int r_next = ch.row0 + kFwdWarps + warp;
+      for (int r = ch.row0 + warp; r < ch.row1; r = take_atom(&s_next, r_next, lane)) {
         const int row = sorted_rows[r];
         float* xr = xyz + (size_t)row * 4 * ng;
-        if (r + kFwdWarps < ch.row1) {
+        if (r_next < ch.row1) {
           // the warp's next atom: its list section (and, after the first
           // section, its xyz so far) move into L2 while this atom is processed
-          const int nrow = sorted_rows[r + kFwdWarps];
+          const int nrow = sorted_rows[r_next];
           const char* nlr = reinterpret_cast<const char*>(p.nlist + (size_t)nrow * p.nnei + p.sec[sec]);
           if (lane * 128 < 4 * (p.sec[sec + 1] - p.sec[sec])) prefetch_l2(nlr + lane * 128);
           if (sec > 0 && lane * 128 < 16 * ng) prefetch_l2(reinterpret_cast<const char*>(xyz + (size_t)nrow * 4 * ng) + lane * 128);
@@ -487,7 +505,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
                 (size_t)kBwdWarps * p.nnei + warp * 32;                                    // [warp][32]
   const float rmin = (float)p.rcut_smth, rmax = (float)p.rcut;
   const int bank_step = (row_stride / 2) & 15;  // a row's 8-byte bank pair advances by this per row
-  __shared__ int s_work;
+  __shared__ int s_work, s_next;
   for (int c = work_first(queue, &s_work); c < nchunks; c = work_next(queue, c, &s_work)) {
     const WorkChunk ch = chunks[c];
     const int ti = ch.ti;
@@ -498,15 +516,17 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
       const int rows = min(rows_cap, tm.hi_idx + 1);
       __syncthreads();
       stage_rows_paired(s_tab, tab, rows, ng, row_stride);
+      if (threadIdx.x == 0) s_next = ch.row0 + 2 * kBwdWarps;
       __syncthreads();
-      for (int r = ch.row0 + warp; r < ch.row1; r += kBwdWarps) {
+      int r_next = ch.row0 + kBwdWarps + warp;
+      for (int r = ch.row0 + warp; r < ch.row1; r = take_atom(&s_next, r_next, lane)) {
         const int row = sorted_rows[r];
         const int* nl = p.nlist + (size_t)row * p.nnei;
         float* gp_row = gpair + (size_t)row * p.nnei * 3;
-        if (r + kBwdWarps < ch.row1) {
+        if (r_next < ch.row1) {
           // the warp's next atom: its dE/dxyz, list and first pair
           // environments move into L2 while this atom is processed
-          const int nrow = sorted_rows[r + kBwdWarps];
+          const int nrow = sorted_rows[r_next];
           const char* nd = reinterpret_cast<const char*>(dxyz + (size_t)nrow * 4 * ng);
           if (lane * 128 < 16 * ng) prefetch_l2(nd + lane * 128);
           if (lane * 128 < 4 * p.nnei) prefetch_l2(reinterpret_cast<const char*>(p.nlist + (size_t)nrow * p.nnei) + lane * 128);
