@@ -742,8 +742,7 @@ def run_train(args, world, rank, local):
 
 # DRAM bytes (read + write) per launch of each stage's tensor-core kernel on
 # the 12,288-atom water step, from one ncu capture (emb_tc_fwd, emb_tc_bwd,
-# the first fitting GEMM): profiles/emb_tc_water12288.md,
-# profiles/fit_gemm_water12288.md
+# the first fitting GEMM)
 DRAM_BYTES_PER_LAUNCH = {"desc_fwd": 57.4e6, "desc_bwd": 27.2e6, "fitting": 41.9e6}
 
 
@@ -908,7 +907,7 @@ def main():
         "roofline": {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": DRAM_BYTES_PER_LAUNCH.get(dom),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's "
-                                       "tensor-core kernel, profiles/emb_tc_water12288.md",
+                                       "tensor-core kernel (one capture of the 12,288-atom step)",
                      "peak_source": f"{peak_kind} bf16_tflops", "algorithmic_flops_per_launch": flops[dom]},
         "cpu_baseline": cpu,
         "e2e": e2e,
