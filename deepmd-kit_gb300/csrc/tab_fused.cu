@@ -647,7 +647,7 @@ tab_bwd_kernel(DescParams<float> p, EmbParams<float> e, const WorkChunk* __restr
             float2 r2[4], pc2[4];
 #pragma unroll
             for (int cc = 0; cc < 4; ++cc) r2[cc] = pc2[cc] = make_float2(0.f, 0.f);
-#pragma unroll 8
+#pragma unroll 10
             for (int m = 0; 2 * m < ng; ++m) {
               const float2* q = rowc + 6 * m;  // coefficient c of both neurons
               const float2 c0 = q[0], c1 = q[1], c2 = q[2], c3 = q[3], c4 = q[4], c5 = q[5];
